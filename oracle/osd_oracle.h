@@ -1,0 +1,69 @@
+/*
+ * osd_oracle.h -- CPU restatement of the Osd evaluation path, used ONLY as the checker.
+ *
+ * TEST INFRASTRUCTURE.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg may load liboracle.so.  The GB300 product never calls into it.
+ *
+ * Pinning: every function here is checked against fixtures produced by the reference itself
+ * (tests/golden/make_golden.py drives oracle/_ref/libosdref.so, the reference's own Far/Osd
+ * CPU code compiled from source).  Float results are required to be bitwise identical to
+ * Osd::CpuEvaluator; integer results (PatchMap handles, PatchParam decode) identical.
+ *
+ * Conventions shared with the C-ABI in include/osd_gb300.h:
+ *   - a buffer descriptor is int[3] = {offset, length, stride} (osd/bufferDescriptor.h:61-103)
+ *     and raw pointers exclude the offset (osd/cudaEvaluator.h:147-155);
+ *   - a stencil range [start, end) writes dst element i (absolute), as the reference CUDA
+ *     kernels do (osd/cudaKernel.cu:85-98);
+ *   - a patch coord is 5 x 32-bit {arrayIndex, patchIndex, vertIndex, float s, float t}
+ *     (osd/patchBasisTypes.h:249-255), a patch array 6 ints (:272-279), a patch param
+ *     3 x 32-bit {field0, field1, float sharpness} (:301-305).
+ */
+#ifndef OSD_ORACLE_H
+#define OSD_ORACLE_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* EvalStencils: nout = 1 (P), 3 (P, du, dv) or 6 (P, du, dv, duu, duv, dvv).
+ * Sequential float accumulation in stencil order (osd/cpuKernel.cpp:71-240).
+ * Returns 1 on success, 0 when a descriptor length differs from the source length. */
+int orc_eval_stencils_f(const float *src, const int *srcDesc, int nout, float *const *dst,
+                        const int *dstDesc, const int *sizes, const int *offsets,
+                        const int *indices, const float *const *weights, int start, int end,
+                        int nthreads);
+
+/* FP64 oracle: the same float tables applied in double; dst are double buffers laid out with
+ * the same descriptors. */
+int orc_eval_stencils_d(const float *src, const int *srcDesc, int nout, double *const *dst,
+                        const int *dstDesc, const int *sizes, const int *offsets,
+                        const int *indices, const float *const *weights, int start, int end,
+                        int nthreads);
+
+/* Patch basis for one point (osd/patchBasis.h:1558-1610): w is [6][20] (P, Ds, Dt, Dss, Dst,
+ * Dtt); returns the number of control points (0 for an unknown type). */
+int orc_patch_basis_f(int patchType, int field0, int field1, float s, float t, float *w);
+int orc_patch_basis_d(int patchType, int field0, int field1, double s, double t, double *w);
+
+/* EvalPatches (osd/cpuEvaluator.cpp:157-381).  dst[k] may be NULL to skip an output. */
+int orc_eval_patches_f(const float *src, const int *srcDesc, int nout, float *const *dst,
+                       const int *dstDesc, int ncoords, const void *coords, const int *arrays,
+                       const int *patchIndices, const void *params, int nthreads);
+int orc_eval_patches_d(const float *src, const int *srcDesc, int nout, double *const *dst,
+                       const int *dstDesc, int ncoords, const void *coords, const int *arrays,
+                       const int *patchIndices, const void *params, int nthreads);
+
+/* PatchMap (far/patchMap.h, far/patchMap.cpp).  params: 3 x 32-bit per patch (only
+ * field0/field1 are read); arrays: 6 ints per patch array; triangular: 1 when the table's
+ * varying patches have 3 CVs (tri patch layout). */
+void *orc_patchmap_build(int numArrays, const int *arrays, const void *params, int triangular);
+void orc_patchmap_free(void *map);
+/* handles: 3 ints per query (arrayIndex, patchIndex, vertIndex), -1s when not found.
+ * Returns the number of queries found. */
+int orc_find_patches(const void *map, int n, const int *faces, const double *u,
+                     const double *v, int *handles);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,218 @@
+"""ctypes wrapper over oracle/_ref/libosdref.so: the reference's own Far/Osd CPU code.
+
+TEST INFRASTRUCTURE ONLY.  Available where the reference sources were present to compile
+(``make -C oracle ref``); used to generate golden fixtures and to cross-check the oracle.
+Nothing in the product imports this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libosdref.so")
+
+_lib = None
+
+
+def available() -> bool:
+    return os.path.exists(LIB_PATH)
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = C.CDLL(LIB_PATH)
+        vp = C.c_void_p
+        _lib.ref_refiner_create.restype = vp
+        _lib.ref_stencils_create.restype = vp
+        _lib.ref_limit_stencils_create.restype = vp
+        _lib.ref_patches_create.restype = vp
+        _lib.ref_stencils_nnz.restype = C.c_long
+        for name in ("ref_refiner_destroy", "ref_refine_uniform", "ref_refine_adaptive",
+                     "ref_num_vertices_total", "ref_level_num_vertices", "ref_max_level",
+                     "ref_num_ptex_faces", "ref_ptex_face_ids", "ref_stencils_num",
+                     "ref_stencils_nnz", "ref_stencils_num_control", "ref_stencils_copy",
+                     "ref_stencils_destroy", "ref_patches_destroy", "ref_patches_counts",
+                     "ref_patches_copy", "ref_patches_copy_stencils", "ref_find_patches",
+                     "ref_cpu_eval_stencils", "ref_cpu_eval_patches", "ref_eval_patches_fp64",
+                     "ref_omp_set_threads"):
+            getattr(_lib, name).argtypes = None
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+class Refiner:
+    """Far::TopologyRefiner built from a shapes.Cage (far/topologyRefinerFactory.h)."""
+
+    def __init__(self, cage, boundary: int = 1):
+        self.cage = cage
+        L = lib()
+        cv = np.ascontiguousarray(cage.crease_verts, np.int32).ravel()
+        cs = np.ascontiguousarray(cage.crease_sharpness, np.float32)
+        self._keep = (cage.verts_per_face, cage.face_verts, cv, cs)
+        self.h = L.ref_refiner_create(
+            C.c_int(cage.scheme), C.c_int(cage.num_vertices), C.c_int(cage.num_faces),
+            _p(cage.verts_per_face), _p(cage.face_verts), C.c_int(len(cs)), _p(cv), _p(cs),
+            C.c_int(0), None, None, C.c_int(boundary))
+        if not self.h:
+            raise RuntimeError("TopologyRefinerFactory::Create failed")
+        self.h = C.c_void_p(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ref_refiner_destroy(self.h)
+            self.h = None
+
+    def refine_uniform(self, level):
+        lib().ref_refine_uniform(self.h, C.c_int(level))
+        return self
+
+    def refine_adaptive(self, level, single_crease=False, inf_sharp=False):
+        lib().ref_refine_adaptive(self.h, C.c_int(level), C.c_int(int(single_crease)),
+                                  C.c_int(int(inf_sharp)))
+        return self
+
+    def num_vertices_total(self):
+        return lib().ref_num_vertices_total(self.h)
+
+    def level_num_vertices(self, level):
+        return lib().ref_level_num_vertices(self.h, C.c_int(level))
+
+    def num_ptex_faces(self):
+        return lib().ref_num_ptex_faces(self.h)
+
+    def ptex_face_ids(self):
+        out = np.zeros(self.cage.num_faces, np.int32)
+        lib().ref_ptex_face_ids(self.h, _p(out))
+        return out
+
+
+def _copy_stencils(h, limit, use_double):
+    L = lib()
+    n = L.ref_stencils_num(h)
+    nnz = L.ref_stencils_nnz(h)
+    wt = np.float64 if use_double else np.float32
+    sizes = np.zeros(n, np.int32)
+    offsets = np.zeros(n, np.int32)
+    idx = np.zeros(nnz, np.int32)
+    ws = [np.zeros(nnz, wt) for _ in range(6 if limit else 1)]
+    arr = (C.c_void_p * 6)(*([w.ctypes.data for w in ws] + [None] * (6 - len(ws))))
+    L.ref_stencils_copy(h, _p(sizes), _p(offsets), _p(idx), arr)
+    out = dict(sizes=sizes, offsets=offsets, indices=idx, weights=ws[0],
+               num_control=L.ref_stencils_num_control(h))
+    if limit:
+        for k, name in enumerate(("du", "dv", "duu", "duv", "dvv"), 1):
+            out[name + "_weights"] = ws[k]
+    L.ref_stencils_destroy(h)
+    return out
+
+
+def stencil_table(refiner, use_double=False, intermediate=True, factorize=True,
+                  control=False, max_level=10):
+    """Far::StencilTableFactoryReal<REAL>::Create (far/stencilTableFactory.cpp:78-151)."""
+    h = C.c_void_p(lib().ref_stencils_create(refiner.h, C.c_int(int(use_double)),
+                                             C.c_int(int(intermediate)), C.c_int(int(factorize)),
+                                             C.c_int(int(control)), C.c_int(max_level)))
+    return _copy_stencils(h, False, use_double)
+
+
+def limit_stencil_table(refiner, ptex, s, t, use_double=False, d1=True, d2=False):
+    """Far::LimitStencilTableFactoryReal<REAL>::Create (far/stencilTableFactory.cpp:411-662)."""
+    ptex = np.ascontiguousarray(ptex, np.int32)
+    s = np.ascontiguousarray(s, np.float64)
+    t = np.ascontiguousarray(t, np.float64)
+    h = C.c_void_p(lib().ref_limit_stencils_create(refiner.h, C.c_int(int(use_double)),
+                                                   C.c_int(len(ptex)), _p(ptex), _p(s), _p(t),
+                                                   C.c_int(int(d1)), C.c_int(int(d2))))
+    return _copy_stencils(h, True, use_double)
+
+
+class Patches:
+    """Far::PatchTable + Osd::CpuPatchTable flattening + Far::PatchMap."""
+
+    ENDCAP_BILINEAR, ENDCAP_BSPLINE, ENDCAP_GREGORY = 1, 2, 3
+
+    def __init__(self, refiner, endcap=3, max_isolation=10, single_crease=False,
+                 inf_sharp=False, share_endcap_points=True):
+        L = lib()
+        self.h = C.c_void_p(L.ref_patches_create(refiner.h, C.c_int(endcap), C.c_int(max_isolation),
+                                                 C.c_int(int(single_crease)), C.c_int(int(inf_sharp)),
+                                                 C.c_int(int(share_endcap_points))))
+        counts = np.zeros(6, np.int64)
+        L.ref_patches_counts(self.h, _p(counts))
+        na, ni, npar, nloc, nst, nnz = (int(x) for x in counts)
+        self.arrays = np.zeros((na, 6), np.int32)
+        self.indices = np.zeros(ni, np.int32)
+        self.params = np.zeros((npar, 3), np.int32)
+        L.ref_patches_copy(self.h, _p(self.arrays), _p(self.indices), _p(self.params))
+        self.num_local_points = nloc
+        self.st = dict(sizes=np.zeros(nst, np.int32), offsets=np.zeros(nst, np.int32),
+                       indices=np.zeros(nnz, np.int32), weights=np.zeros(nnz, np.float32))
+        L.ref_patches_copy_stencils(self.h, _p(self.st["sizes"]), _p(self.st["offsets"]),
+                                    _p(self.st["indices"]), _p(self.st["weights"]))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().ref_patches_destroy(self.h)
+            self.h = None
+
+    def find_patches(self, faces, u, v):
+        faces = np.ascontiguousarray(faces, np.int32)
+        u = np.ascontiguousarray(u, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        handles = np.zeros((len(faces), 3), np.int32)
+        found = np.zeros(len(faces), np.int32)
+        lib().ref_find_patches(self.h, C.c_int(len(faces)), _p(faces), _p(u), _p(v),
+                               _p(handles), _p(found))
+        return handles, found
+
+    def eval_fp64(self, src, length, stride, handles, s, t):
+        """Far::PatchTable::EvaluateBasis<double> + double accumulation; [n, 6, length]."""
+        n = len(handles)
+        out = np.zeros((n, 6, length), np.float64)
+        lib().ref_eval_patches_fp64(self.h, _p(np.ascontiguousarray(src, np.float32)),
+                                    C.c_int(length), C.c_int(stride), C.c_int(n),
+                                    _p(np.ascontiguousarray(handles, np.int32)),
+                                    _p(np.ascontiguousarray(s, np.float64)),
+                                    _p(np.ascontiguousarray(t, np.float64)), _p(out))
+        return out
+
+
+def _desc_arr(descs):
+    return np.asarray(descs, np.int32).ravel()
+
+
+def cpu_eval_stencils(src, src_desc, dsts, dst_descs, sizes, offsets, indices, weights,
+                      start, end, omp=False):
+    """Osd::CpuEvaluator / OmpEvaluator ::EvalStencils (osd/cpuEvaluator.cpp:37-125)."""
+    nout = len(dsts)
+    dp = (C.c_void_p * nout)(*[d.ctypes.data for d in dsts])
+    wp = (C.c_void_p * nout)(*[w.ctypes.data for w in weights])
+    sd = np.asarray(src_desc, np.int32)
+    dd = _desc_arr(dst_descs)
+    ok = lib().ref_cpu_eval_stencils(_p(src), _p(sd), C.c_int(nout), dp, _p(dd), _p(sizes),
+                                     _p(offsets), _p(indices), wp, C.c_int(start), C.c_int(end),
+                                     C.c_int(int(omp)))
+    return bool(ok)
+
+
+def cpu_eval_patches(src, src_desc, dsts, dst_descs, coords, arrays, indices, params):
+    """Osd::CpuEvaluator::EvalPatches (osd/cpuEvaluator.cpp:157-381)."""
+    nout = len(dsts)
+    dp = (C.c_void_p * nout)(*[d.ctypes.data for d in dsts])
+    sd = np.asarray(src_desc, np.int32)
+    dd = _desc_arr(dst_descs)
+    ok = lib().ref_cpu_eval_patches(_p(src), _p(sd), C.c_int(nout), dp, _p(dd),
+                                    C.c_int(coords.shape[0]), _p(coords), _p(arrays),
+                                    _p(indices), _p(params))
+    return bool(ok)
+
+
+def omp_set_threads(n):
+    lib().ref_omp_set_threads(C.c_int(n))

@@ -1,0 +1,439 @@
+// C entry points over the reference's own Far / Osd CPU code.
+//
+// TEST INFRASTRUCTURE ONLY.  This file is compiled together with the reference sources by
+// oracle/Makefile into oracle/_ref/libosdref.so.  It is used to (a) generate the golden
+// fixtures under tests/golden/, (b) pin the C restatement in osd_oracle.c against the
+// reference itself, and (c) time the reference CpuEvaluator / OmpEvaluator where the
+// reference is available.  Nothing in the product links or loads it.
+//
+// Every call below forwards to the public reference API named in its comment.
+
+#include <opensubdiv/far/topologyDescriptor.h>
+#include <opensubdiv/far/stencilTableFactory.h>
+#include <opensubdiv/far/patchTableFactory.h>
+#include <opensubdiv/far/patchMap.h>
+#include <opensubdiv/far/ptexIndices.h>
+#include <opensubdiv/osd/cpuEvaluator.h>
+#include <opensubdiv/osd/ompEvaluator.h>
+#include <opensubdiv/osd/cpuPatchTable.h>
+#include <opensubdiv/osd/bufferDescriptor.h>
+
+#include <cstring>
+#include <vector>
+
+using namespace OpenSubdiv;
+
+namespace {
+
+struct Refiner {
+    Far::TopologyRefiner *r = nullptr;
+};
+
+struct Stencils {
+    int useDouble = 0;
+    int limit = 0;
+    Far::StencilTableReal<float> const *f = nullptr;
+    Far::StencilTableReal<double> const *d = nullptr;
+    Far::LimitStencilTableReal<float> const *lf = nullptr;
+    Far::LimitStencilTableReal<double> const *ld = nullptr;
+};
+
+struct Patches {
+    Far::PatchTable const *pt = nullptr;
+    Osd::CpuPatchTable *cpu = nullptr;
+    Far::PatchMap *map = nullptr;
+    Far::StencilTable const *all = nullptr;   // refined + local point stencils (float)
+};
+
+template <class T>
+void copyVec(std::vector<T> const &v, T *out) {
+    if (out && !v.empty()) std::memcpy(out, v.data(), v.size() * sizeof(T));
+}
+
+// Weight vectors of a Far table may hold more entries than it has control indices; only the
+// first nnz (= number of control indices) are meaningful.
+template <class T>
+void copyN(std::vector<T> const &v, T *out, size_t n) {
+    if (out && !v.empty()) std::memcpy(out, v.data(), (v.size() < n ? v.size() : n) * sizeof(T));
+}
+
+}  // namespace
+
+extern "C" {
+
+// Far::TopologyRefinerFactory<TopologyDescriptor>::Create (far/topologyRefinerFactory.h)
+// scheme: 0 bilinear, 1 catmark, 2 loop.  boundary: Sdc::Options::VtxBoundaryInterpolation.
+void *ref_refiner_create(int scheme, int nverts, int nfaces, const int *vertsPerFace,
+                         const int *faceVerts, int ncreases, const int *creaseVerts,
+                         const float *creaseSharp, int ncorners, const int *cornerVerts,
+                         const float *cornerSharp, int boundary) {
+    Far::TopologyDescriptor desc;
+    desc.numVertices = nverts;
+    desc.numFaces = nfaces;
+    desc.numVertsPerFace = vertsPerFace;
+    desc.vertIndicesPerFace = faceVerts;
+    desc.numCreases = ncreases;
+    desc.creaseVertexIndexPairs = creaseVerts;
+    desc.creaseWeights = creaseSharp;
+    desc.numCorners = ncorners;
+    desc.cornerVertexIndices = cornerVerts;
+    desc.cornerWeights = cornerSharp;
+
+    Sdc::SchemeType type = scheme == 0 ? Sdc::SCHEME_BILINEAR
+                         : scheme == 1 ? Sdc::SCHEME_CATMARK : Sdc::SCHEME_LOOP;
+    Sdc::Options opts;
+    opts.SetVtxBoundaryInterpolation((Sdc::Options::VtxBoundaryInterpolation)boundary);
+    Far::TopologyRefinerFactory<Far::TopologyDescriptor>::Options fo(type, opts);
+    Refiner *h = new Refiner;
+    h->r = Far::TopologyRefinerFactory<Far::TopologyDescriptor>::Create(desc, fo);
+    if (!h->r) { delete h; return nullptr; }
+    return h;
+}
+
+void ref_refiner_destroy(void *p) {
+    Refiner *h = (Refiner *)p;
+    if (!h) return;
+    delete h->r;
+    delete h;
+}
+
+// Far::TopologyRefiner::RefineUniform (far/topologyRefiner.h:146)
+void ref_refine_uniform(void *p, int level) {
+    Far::TopologyRefiner::UniformOptions o(level);
+    ((Refiner *)p)->r->RefineUniform(o);
+}
+
+// Far::TopologyRefiner::RefineAdaptive (far/topologyRefiner.h:192), options chosen the way
+// PatchTableFactory::Options::GetRefineAdaptiveOptions derives them.
+void ref_refine_adaptive(void *p, int isolation, int useSingleCrease, int useInfSharp) {
+    Far::PatchTableFactory::Options po(isolation);
+    po.useSingleCreasePatch = useSingleCrease;
+    po.useInfSharpPatch = useInfSharp;
+    ((Refiner *)p)->r->RefineAdaptive(po.GetRefineAdaptiveOptions());
+}
+
+int ref_num_vertices_total(void *p) { return ((Refiner *)p)->r->GetNumVerticesTotal(); }
+int ref_level_num_vertices(void *p, int level) {
+    return ((Refiner *)p)->r->GetLevel(level).GetNumVertices();
+}
+int ref_max_level(void *p) { return ((Refiner *)p)->r->GetMaxLevel(); }
+int ref_num_ptex_faces(void *p) {
+    Far::PtexIndices pi(*((Refiner *)p)->r);
+    return pi.GetNumFaces();
+}
+// Far::PtexIndices::GetFaceId (far/ptexIndices.cpp)
+void ref_ptex_face_ids(void *p, int *out) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    Far::PtexIndices pi(*r);
+    int n = r->GetLevel(0).GetNumFaces();
+    for (int i = 0; i < n; ++i) out[i] = pi.GetFaceId(i);
+}
+
+// Far::StencilTableFactoryReal<REAL>::Create (far/stencilTableFactory.cpp:78-151)
+void *ref_stencils_create(void *p, int useDouble, int genIntermediate, int factorize,
+                          int genCtrl, int maxLevel) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    Stencils *s = new Stencils;
+    s->useDouble = useDouble;
+    if (useDouble) {
+        Far::StencilTableFactoryReal<double>::Options o;
+        o.generateIntermediateLevels = genIntermediate;
+        o.factorizeIntermediateLevels = factorize;
+        o.generateControlVerts = genCtrl;
+        o.generateOffsets = true;
+        o.maxLevel = maxLevel;
+        s->d = Far::StencilTableFactoryReal<double>::Create(*r, o);
+    } else {
+        Far::StencilTableFactoryReal<float>::Options o;
+        o.generateIntermediateLevels = genIntermediate;
+        o.factorizeIntermediateLevels = factorize;
+        o.generateControlVerts = genCtrl;
+        o.generateOffsets = true;
+        o.maxLevel = maxLevel;
+        s->f = Far::StencilTableFactoryReal<float>::Create(*r, o);
+    }
+    return s;
+}
+
+// Far::LimitStencilTableFactoryReal<REAL>::Create (far/stencilTableFactory.cpp:411-662)
+// Locations are given one per (ptex face, s, t) triple.
+void *ref_limit_stencils_create(void *p, int useDouble, int n, const int *ptex,
+                                const double *su, const double *tv, int d1, int d2) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    Stencils *s = new Stencils;
+    s->useDouble = useDouble;
+    s->limit = 1;
+    if (useDouble) {
+        typedef Far::LimitStencilTableFactoryReal<double> F;
+        F::LocationArrayVec locs(n);
+        for (int i = 0; i < n; ++i) {
+            locs[i].ptexIdx = ptex[i];
+            locs[i].numLocations = 1;
+            locs[i].s = su + i;
+            locs[i].t = tv + i;
+        }
+        F::Options o;
+        o.generate1stDerivatives = d1;
+        o.generate2ndDerivatives = d2;
+        s->ld = F::Create(*r, locs, nullptr, nullptr, o);
+    } else {
+        typedef Far::LimitStencilTableFactoryReal<float> F;
+        std::vector<float> sf(su, su + n), tf(tv, tv + n);
+        F::LocationArrayVec locs(n);
+        for (int i = 0; i < n; ++i) {
+            locs[i].ptexIdx = ptex[i];
+            locs[i].numLocations = 1;
+            locs[i].s = sf.data() + i;
+            locs[i].t = tf.data() + i;
+        }
+        F::Options o;
+        o.generate1stDerivatives = d1;
+        o.generate2ndDerivatives = d2;
+        s->lf = F::Create(*r, locs, nullptr, nullptr, o);
+    }
+    return s;
+}
+
+void ref_stencils_destroy(void *p) {
+    Stencils *s = (Stencils *)p;
+    if (!s) return;
+    delete s->f; delete s->d; delete s->lf; delete s->ld;
+    delete s;
+}
+
+static Far::StencilTableReal<float> const *asF(Stencils *s) {
+    return s->limit ? s->lf : s->f;
+}
+static Far::StencilTableReal<double> const *asD(Stencils *s) {
+    return s->limit ? s->ld : s->d;
+}
+
+int ref_stencils_num(void *p) {
+    Stencils *s = (Stencils *)p;
+    if (s->useDouble) return asD(s) ? asD(s)->GetNumStencils() : 0;
+    return asF(s) ? asF(s)->GetNumStencils() : 0;
+}
+long ref_stencils_nnz(void *p) {
+    Stencils *s = (Stencils *)p;
+    if (s->useDouble) return asD(s) ? (long)asD(s)->GetControlIndices().size() : 0;
+    return asF(s) ? (long)asF(s)->GetControlIndices().size() : 0;
+}
+int ref_stencils_num_control(void *p) {
+    Stencils *s = (Stencils *)p;
+    if (s->useDouble) return asD(s) ? asD(s)->GetNumControlVertices() : 0;
+    return asF(s) ? asF(s)->GetNumControlVertices() : 0;
+}
+
+// Copies sizes/offsets/indices and the weight arrays (float or double per the table).
+// w[0..5] = weights, du, dv, duu, duv, dvv; entries may be NULL or absent (limit only).
+void ref_stencils_copy(void *p, int *sizes, int *offsets, int *indices, void **w) {
+    Stencils *s = (Stencils *)p;
+    if (s->useDouble) {
+        auto t = asD(s);
+        size_t nnz = t->GetControlIndices().size();
+        copyVec(t->GetSizes(), sizes);
+        copyVec(t->GetOffsets(), offsets);
+        copyVec(t->GetControlIndices(), indices);
+        copyN(t->GetWeights(), (double *)w[0], nnz);
+        if (s->limit) {
+            copyN(s->ld->GetDuWeights(), (double *)w[1], nnz);
+            copyN(s->ld->GetDvWeights(), (double *)w[2], nnz);
+            copyN(s->ld->GetDuuWeights(), (double *)w[3], nnz);
+            copyN(s->ld->GetDuvWeights(), (double *)w[4], nnz);
+            copyN(s->ld->GetDvvWeights(), (double *)w[5], nnz);
+        }
+    } else {
+        auto t = asF(s);
+        size_t nnz = t->GetControlIndices().size();
+        copyVec(t->GetSizes(), sizes);
+        copyVec(t->GetOffsets(), offsets);
+        copyVec(t->GetControlIndices(), indices);
+        copyN(t->GetWeights(), (float *)w[0], nnz);
+        if (s->limit) {
+            copyN(s->lf->GetDuWeights(), (float *)w[1], nnz);
+            copyN(s->lf->GetDvWeights(), (float *)w[2], nnz);
+            copyN(s->lf->GetDuuWeights(), (float *)w[3], nnz);
+            copyN(s->lf->GetDuvWeights(), (float *)w[4], nnz);
+            copyN(s->lf->GetDvvWeights(), (float *)w[5], nnz);
+        }
+    }
+}
+
+// Osd::CpuEvaluator::EvalStencils, all three overloads (osd/cpuEvaluator.cpp:37-125).
+// dsts/dstDescs/wts hold 1, 3 or 6 outputs.  Descriptors are (offset, length, stride).
+int ref_cpu_eval_stencils(const float *src, const int *srcDesc, int nout, float **dsts,
+                          const int *dstDescs, const int *sizes, const int *offsets,
+                          const int *indices, const float **wts, int start, int end,
+                          int useOmp) {
+    Osd::BufferDescriptor sd(srcDesc[0], srcDesc[1], srcDesc[2]);
+    Osd::BufferDescriptor d[6];
+    for (int i = 0; i < nout; ++i)
+        d[i] = Osd::BufferDescriptor(dstDescs[3 * i], dstDescs[3 * i + 1], dstDescs[3 * i + 2]);
+    bool ok = false;
+    if (nout == 1) {
+        ok = useOmp ? Osd::OmpEvaluator::EvalStencils(src, sd, dsts[0], d[0], sizes, offsets,
+                                                      indices, wts[0], start, end)
+                    : Osd::CpuEvaluator::EvalStencils(src, sd, dsts[0], d[0], sizes, offsets,
+                                                      indices, wts[0], start, end);
+    } else if (nout == 3) {
+        ok = useOmp ? Osd::OmpEvaluator::EvalStencils(src, sd, dsts[0], d[0], dsts[1], d[1],
+                                                      dsts[2], d[2], sizes, offsets, indices,
+                                                      wts[0], wts[1], wts[2], start, end)
+                    : Osd::CpuEvaluator::EvalStencils(src, sd, dsts[0], d[0], dsts[1], d[1],
+                                                      dsts[2], d[2], sizes, offsets, indices,
+                                                      wts[0], wts[1], wts[2], start, end);
+    } else if (nout == 6) {
+        ok = useOmp ? Osd::OmpEvaluator::EvalStencils(
+                          src, sd, dsts[0], d[0], dsts[1], d[1], dsts[2], d[2], dsts[3], d[3],
+                          dsts[4], d[4], dsts[5], d[5], sizes, offsets, indices, wts[0], wts[1],
+                          wts[2], wts[3], wts[4], wts[5], start, end)
+                    : Osd::CpuEvaluator::EvalStencils(
+                          src, sd, dsts[0], d[0], dsts[1], d[1], dsts[2], d[2], dsts[3], d[3],
+                          dsts[4], d[4], dsts[5], d[5], sizes, offsets, indices, wts[0], wts[1],
+                          wts[2], wts[3], wts[4], wts[5], start, end);
+    }
+    return ok ? 1 : 0;
+}
+
+void ref_omp_set_threads(int n) { Osd::OmpEvaluator::SetNumThreads(n); }
+
+// Far::PatchTableFactory::Create (far/patchTableFactory.h:175) on an already refined
+// refiner, then Osd::CpuPatchTable (osd/cpuPatchTable.cpp:35-158) to flatten it and
+// Far::PatchMap (far/patchMap.cpp) for lookups.  A stencil table covering refined and
+// local points is built the way examples/glEvalLimit does (StencilTableFactory with
+// intermediate levels + AppendLocalPointStencilTable).
+void *ref_patches_create(void *p, int endcap, int maxIsolation, int useSingleCrease,
+                         int useInfSharp, int shareEndCapPoints) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    Far::PatchTableFactory::Options po(maxIsolation);
+    po.SetEndCapType((Far::PatchTableFactory::Options::EndCapType)endcap);
+    po.useSingleCreasePatch = useSingleCrease;
+    po.useInfSharpPatch = useInfSharp;
+    po.shareEndCapPatchPoints = shareEndCapPoints;
+    Patches *h = new Patches;
+    h->pt = Far::PatchTableFactory::Create(*r, po);
+    h->cpu = Osd::CpuPatchTable::Create(h->pt, nullptr);
+    h->map = new Far::PatchMap(*h->pt);
+
+    Far::StencilTableFactory::Options so;
+    so.generateOffsets = true;
+    // Patch indices count vertices of every level after the base (uniform tables offset the
+    // last level by all earlier levels, far/patchTableFactory.cpp:813-814), so the source
+    // buffer holds all levels.
+    so.generateIntermediateLevels = true;
+    Far::StencilTable const *st = Far::StencilTableFactory::Create(*r, so);
+    Far::StencilTable const *local = h->pt->GetLocalPointStencilTable();
+    if (local) {
+        Far::StencilTable const *all =
+            Far::StencilTableFactory::AppendLocalPointStencilTable(*r, st, local);
+        delete st;
+        st = all;
+    }
+    h->all = st;
+    return h;
+}
+
+void ref_patches_destroy(void *p) {
+    Patches *h = (Patches *)p;
+    if (!h) return;
+    delete h->map;
+    delete h->cpu;
+    delete h->all;
+    delete h->pt;
+    delete h;
+}
+
+// counts[0..5] = numArrays, indexSize, paramSize, numLocalPoints, stencils(all), nnz(all)
+void ref_patches_counts(void *p, long *counts) {
+    Patches *h = (Patches *)p;
+    counts[0] = h->pt->GetNumPatchArrays();
+    counts[1] = (long)h->cpu->GetPatchIndexSize();
+    counts[2] = (long)h->cpu->GetPatchParamSize();
+    counts[3] = h->pt->GetNumLocalPoints();
+    counts[4] = h->all ? h->all->GetNumStencils() : 0;
+    counts[5] = h->all ? (long)h->all->GetControlIndices().size() : 0;
+}
+
+// arrays: 6 ints per array (Osd::PatchArray, osd/types.h:66-125);
+// params: 3 x 32-bit per patch (Osd::PatchParam field0, field1, sharpness bits)
+void ref_patches_copy(void *p, int *arrays, int *indices, int *params) {
+    Patches *h = (Patches *)p;
+    int na = h->pt->GetNumPatchArrays();
+    std::memcpy(arrays, h->cpu->GetPatchArrayBuffer(), sizeof(Osd::PatchArray) * na);
+    std::memcpy(indices, h->cpu->GetPatchIndexBuffer(), sizeof(int) * h->cpu->GetPatchIndexSize());
+    std::memcpy(params, h->cpu->GetPatchParamBuffer(),
+                sizeof(Osd::PatchParam) * h->cpu->GetPatchParamSize());
+}
+
+void ref_patches_copy_stencils(void *p, int *sizes, int *offsets, int *indices, float *w) {
+    Patches *h = (Patches *)p;
+    copyVec(h->all->GetSizes(), sizes);
+    copyVec(h->all->GetOffsets(), offsets);
+    copyVec(h->all->GetControlIndices(), indices);
+    copyN(h->all->GetWeights(), w, h->all->GetControlIndices().size());
+}
+
+// Far::PatchMap::FindPatch (far/patchMap.h:192-231).  handles: 3 ints per query
+// (arrayIndex, patchIndex, vertIndex); found[i] = 0 when FindPatch returns NULL.
+void ref_find_patches(void *p, int n, const int *faces, const double *u, const double *v,
+                      int *handles, int *found) {
+    Patches *h = (Patches *)p;
+    for (int i = 0; i < n; ++i) {
+        Far::PatchMap::Handle const *hd = h->map->FindPatch(faces[i], u[i], v[i]);
+        found[i] = hd ? 1 : 0;
+        handles[3 * i + 0] = hd ? hd->arrayIndex : -1;
+        handles[3 * i + 1] = hd ? hd->patchIndex : -1;
+        handles[3 * i + 2] = hd ? hd->vertIndex : -1;
+    }
+}
+
+// Osd::CpuEvaluator::EvalPatches, all three overloads (osd/cpuEvaluator.cpp:157-381).
+// coords: 5 x 32-bit per point (Osd::PatchCoord).  nout = 1, 3 or 6.
+int ref_cpu_eval_patches(const float *src, const int *srcDesc, int nout, float **dsts,
+                         const int *dstDescs, int ncoords, const void *coords,
+                         const void *arrays, const int *indices, const void *params) {
+    Osd::BufferDescriptor sd(srcDesc[0], srcDesc[1], srcDesc[2]);
+    Osd::BufferDescriptor d[6];
+    for (int i = 0; i < nout; ++i)
+        d[i] = Osd::BufferDescriptor(dstDescs[3 * i], dstDescs[3 * i + 1], dstDescs[3 * i + 2]);
+    const Osd::PatchCoord *pc = (const Osd::PatchCoord *)coords;
+    const Osd::PatchArray *pa = (const Osd::PatchArray *)arrays;
+    const Osd::PatchParam *pp = (const Osd::PatchParam *)params;
+    bool ok = false;
+    if (nout == 1)
+        ok = Osd::CpuEvaluator::EvalPatches(src, sd, dsts[0], d[0], ncoords, pc, pa, indices, pp);
+    else if (nout == 3)
+        ok = Osd::CpuEvaluator::EvalPatches(src, sd, dsts[0], d[0], dsts[1], d[1], dsts[2], d[2],
+                                            ncoords, pc, pa, indices, pp);
+    else if (nout == 6)
+        ok = Osd::CpuEvaluator::EvalPatches(src, sd, dsts[0], d[0], dsts[1], d[1], dsts[2], d[2],
+                                            dsts[3], d[3], dsts[4], d[4], dsts[5], d[5],
+                                            ncoords, pc, pa, indices, pp);
+    return ok ? 1 : 0;
+}
+
+// Far::PatchTable::EvaluateBasis<double> (far/patchTable.cpp:579-625) and a double
+// accumulation of the same (float) source points: the FP64 oracle for EvalPatches.
+// out: 6 outputs x length doubles per point (P, du, dv, duu, duv, dvv).
+void ref_eval_patches_fp64(void *p, const float *src, int length, int srcStride, int n,
+                           const int *handles, const double *s, const double *t, double *out) {
+    Patches *h = (Patches *)p;
+    double w[6][20];
+    for (int i = 0; i < n; ++i) {
+        Far::PatchTable::PatchHandle hd;
+        hd.arrayIndex = handles[3 * i];
+        hd.patchIndex = handles[3 * i + 1];
+        hd.vertIndex = handles[3 * i + 2];
+        h->pt->EvaluateBasis<double>(hd, s[i], t[i], w[0], w[1], w[2], w[3], w[4], w[5]);
+        Far::ConstIndexArray cvs = h->pt->GetPatchVertices(hd);
+        double *o = out + (size_t)i * 6 * length;
+        for (int k = 0; k < 6 * length; ++k) o[k] = 0.0;
+        for (int j = 0; j < cvs.size(); ++j) {
+            const float *sv = src + (size_t)cvs[j] * srcStride;
+            for (int k = 0; k < 6; ++k)
+                for (int e = 0; e < length; ++e) o[k * length + e] += w[k][j] * (double)sv[e];
+        }
+    }
+}
+
+}  // extern "C"

@@ -1,0 +1,202 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Run in a container that has the reference sources (it builds oracle/_ref/libosdref.so, the
+reference's own Far + Osd CPU code compiled from source, and drives it through
+oracle/ref_shim.cpp):
+
+    make -C oracle ref && python tests/golden/make_golden.py
+
+Every array written here comes out of the reference: Far factories build the tables,
+Osd::CpuEvaluator produces the float outputs, Far::PatchMap the handles and
+Far::PatchTable::EvaluateBasis<double> the FP64 outputs.  The cages are the seeded
+synthetic shapes of opensubdiv_gb300/shapes.py at reduced sizes.
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from opensubdiv_gb300 import shapes  # noqa: E402
+import ref  # noqa: E402
+
+
+def cage_arrays(cage):
+    return dict(positions=cage.positions, verts_per_face=cage.verts_per_face,
+                face_verts=cage.face_verts, scheme=np.int32(cage.scheme),
+                crease_verts=np.asarray(cage.crease_verts, np.int32).reshape(-1, 2),
+                crease_sharpness=np.asarray(cage.crease_sharpness, np.float32))
+
+
+def eval_cpu(src, sdesc, table, nout, ddescs, n_dst, dst_len):
+    outs = [np.zeros(n_dst, np.float32) for _ in range(nout)]
+    names = ("du", "dv", "duu", "duv", "dvv")[: nout - 1]
+    ws = [table["weights"]] + [table[k + "_weights"] for k in names]
+    ok = ref.cpu_eval_stencils(src, sdesc, outs, ddescs, table["sizes"], table["offsets"],
+                               table["indices"], ws, 0, len(table["sizes"]))
+    assert ok
+    return outs
+
+
+def stencil_fixture(path, cage, level, seed, limit_level=None, nlimit=0):
+    rng = np.random.default_rng(seed)
+    out = dict(cage_arrays(cage))
+    r = ref.Refiner(cage).refine_uniform(level)
+    st = ref.stencil_table(r, intermediate=False)
+    std = ref.stencil_table(r, use_double=True, intermediate=False)
+    assert np.array_equal(st["indices"], std["indices"])
+    n = len(st["sizes"])
+    nc = cage.num_vertices
+    out.update(level=np.int32(level), sizes=st["sizes"], offsets=st["offsets"],
+               indices=st["indices"], weights=st["weights"], weights_fp64=std["weights"])
+    # xyz, stride 3
+    src3 = cage.positions.reshape(-1).copy()
+    out["out3"] = eval_cpu(src3, (0, 3, 3), st, 1, [(0, 3, 3)], n * 3, 3)[0]
+    # 8 interleaved primvars: xyz + 5 channels U[-1, 1]
+    src8 = np.concatenate([cage.positions, rng.uniform(-1, 1, (nc, 5)).astype(np.float32)], 1)
+    src8 = src8.astype(np.float32).reshape(-1)
+    out["src8"] = src8
+    out["out8"] = eval_cpu(src8, (0, 8, 8), st, 1, [(0, 8, 8)], n * 8, 8)[0]
+    # strided + offset descriptors: source stride 7 (xyz at 2), destination stride 5 (at 1)
+    src7 = rng.uniform(-1, 1, (nc, 7)).astype(np.float32)
+    src7[:, 2:5] = cage.positions
+    src7 = src7.reshape(-1)
+    out["src7"] = src7
+    out["out_strided"] = eval_cpu(src7, (2, 3, 7), st, 1, [(1, 3, 5)], n * 5 + 5, 3)[0]
+    # in place, the way Osd::Mesh::Refine calls it (osd/mesh.h:501-540)
+    buf = np.zeros((nc + n) * 3, np.float32)
+    buf[: nc * 3] = cage.positions.reshape(-1)
+    ok = ref.cpu_eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], st["sizes"],
+                               st["offsets"], st["indices"], [st["weights"]], 0, n)
+    assert ok
+    out["out_inplace"] = buf
+    if limit_level is not None and nlimit > 0:
+        ra = ref.Refiner(cage).refine_adaptive(limit_level)
+        face, u, v = shapes.uniform_locations(cage, nlimit, seed=seed + 7)
+        lt = ref.limit_stencil_table(ra, face, u, v, d1=True, d2=True)
+        ltd = ref.limit_stencil_table(ra, face, u, v, use_double=True, d1=True, d2=True)
+        assert np.array_equal(lt["indices"], ltd["indices"])
+        m = len(lt["sizes"])
+        out.update(limit_level=np.int32(limit_level), limit_face=face, limit_u=u, limit_v=v)
+        for k in ("sizes", "offsets", "indices", "weights", "du_weights", "dv_weights",
+                  "duu_weights", "duv_weights", "dvv_weights"):
+            out["limit_" + k] = lt[k]
+            if k.endswith("weights"):
+                out["limit_" + k + "_fp64"] = ltd[k]
+        o6 = eval_cpu(src3, (0, 3, 3), lt, 6, [(0, 3, 3)] * 6, m * 3, 3)
+        o3 = eval_cpu(src3, (0, 3, 3), lt, 3, [(0, 3, 3)] * 3, m * 3, 3)
+        for a, b in zip(o3, o6[:3]):
+            assert np.array_equal(a, b)
+        out["limit_out6"] = np.stack(o6)
+    np.savez_compressed(path, **out)
+    return out
+
+
+def edge_queries(nptex, rng, n):
+    """Queries on exact quadrant medians, corners and the largest float below 1."""
+    vals = np.array([0.0, 0.5, 1.0, 0.25, 0.75, 0.125, 0.375, np.nextafter(np.float32(1), 0),
+                     0.0625, 0.9375], np.float32)
+    face = rng.integers(0, nptex, n).astype(np.int32)
+    u = vals[rng.integers(0, len(vals), n)]
+    v = vals[rng.integers(0, len(vals), n)]
+    return face, u, v
+
+
+def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3):
+    rng = np.random.default_rng(seed)
+    out = dict(cage_arrays(cage))
+    r = ref.Refiner(cage)
+    if adaptive:
+        r.refine_adaptive(level)
+    else:
+        r.refine_uniform(level)
+    p = ref.Patches(r, endcap=endcap, max_isolation=level)
+    nc = cage.num_vertices
+    ns = len(p.st["sizes"])
+    buf = np.zeros((nc + ns) * 3, np.float32)
+    buf[: nc * 3] = cage.positions.reshape(-1)
+    ok = ref.cpu_eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], p.st["sizes"],
+                               p.st["offsets"], p.st["indices"], [p.st["weights"]], 0, ns)
+    assert ok
+    nptex = r.num_ptex_faces()
+    f1, u1, v1 = shapes.uniform_locations(cage, nq, seed=seed + 3)
+    f2, u2, v2 = edge_queries(nptex, rng, nq // 10)
+    # out-of-range faces: FindPatch returns NULL (far/patchMap.h:205)
+    f3 = np.array([-1, nptex, nptex + 5], np.int32)
+    u3 = np.array([0.5, 0.5, 0.1], np.float32)
+    v3 = np.array([0.5, 0.2, 0.1], np.float32)
+    faces = np.concatenate([f1, f2, f3])
+    u = np.concatenate([u1, u2, u3])
+    v = np.concatenate([v1, v2, v3])
+    if cage.scheme == shapes.LOOP:
+        fold = (u + v) > 1.0
+        u[fold] = 1.0 - u[fold]
+        v[fold] = 1.0 - v[fold]
+    handles, found = p.find_patches(faces, u.astype(np.float64), v.astype(np.float64))
+    sel = np.nonzero(found)[0]
+    coords = np.zeros((len(sel), 5), np.int32)
+    coords[:, :3] = handles[sel]
+    coords[:, 3] = u[sel].view(np.int32)
+    coords[:, 4] = v[sel].view(np.int32)
+    outs = [np.zeros(len(sel) * 3, np.float32) for _ in range(6)]
+    ok = ref.cpu_eval_patches(buf, (0, 3, 3), outs, [(0, 3, 3)] * 6, coords, p.arrays,
+                              p.indices, p.params)
+    assert ok
+    fp64 = p.eval_fp64(buf, 3, 3, handles[sel], u[sel].astype(np.float64),
+                       v[sel].astype(np.float64))
+    out.update(level=np.int32(level), adaptive=np.int32(adaptive), endcap=np.int32(endcap),
+               arrays=p.arrays, patch_indices=p.indices, params=p.params,
+               num_local_points=np.int32(p.num_local_points), src=buf,
+               num_ptex=np.int32(nptex), q_face=faces, q_u=u, q_v=v, q_handles=handles,
+               q_found=found, coords=coords, out6=np.stack(outs).reshape(6, -1, 3),
+               out6_fp64=fp64.transpose(1, 0, 2).copy(),
+               triangular=np.int32(cage.scheme == shapes.LOOP))
+    np.savez_compressed(path, **out)
+    return out
+
+
+def main():
+    if not ref.available():
+        raise SystemExit("oracle/_ref/libosdref.so missing: run `make -C oracle ref` first")
+    g = HERE
+    # Config-1 family: noisy 8x8-per-face cube, Catmull-Clark.
+    cube = shapes.cube(8, noise=0.01, seed=1)
+    stencil_fixture(os.path.join(g, "cube8_uniform_L3.npz"), cube, 3, seed=11,
+                    limit_level=3, nlimit=600)
+    # Config-2 family at reduced size: torus with triangles and semi-sharp creases.
+    tor = shapes.torus(32, 16, tri_fraction=0.05, crease_fraction=0.02, seed=2)
+    stencil_fixture(os.path.join(g, "torus32x16_uniform_L2.npz"), tor, 2, seed=12,
+                    limit_level=4, nlimit=600)
+    # Loop uniform stencils (icosphere and creased all-triangle torus).
+    ico = shapes.icosphere(2, noise=0.005, seed=3)
+    stencil_fixture(os.path.join(g, "icosphere2_uniform_L2.npz"), ico, 2, seed=13)
+    ltor = shapes.torus(12, 8, crease_fraction=0.05, seed=4, scheme=shapes.LOOP)
+    stencil_fixture(os.path.join(g, "looptorus12x8_uniform_L2.npz"), ltor, 2, seed=14)
+    # Config-3 family: adaptive patch tables with Gregory-basis end caps.
+    patch_fixture(os.path.join(g, "torus32x16_patches_L4.npz"), tor, 4, seed=21)
+    patch_fixture(os.path.join(g, "icosphere2_patches_L3.npz"), ico, 3, seed=22)
+    # Boundaries: open grids (B-spline and box-spline boundary masks).
+    patch_fixture(os.path.join(g, "grid6_patches_L3.npz"), shapes.grid(6, 6, seed=5), 3,
+                  seed=23, nq=1500)
+    patch_fixture(os.path.join(g, "trigrid6_patches_L3.npz"),
+                  shapes.grid(6, 6, seed=6, scheme=shapes.LOOP), 3, seed=24, nq=1500)
+    # B-spline end caps and uniform (linear) tables.
+    patch_fixture(os.path.join(g, "cube8_patches_bspline_L2.npz"), cube, 2, seed=25, nq=1500,
+                  endcap=2)
+    patch_fixture(os.path.join(g, "cube8_uniform_quads_L1.npz"), cube, 1, seed=26, nq=1500,
+                  adaptive=False)
+    patch_fixture(os.path.join(g, "icosphere2_uniform_tris_L1.npz"), ico, 1, seed=27,
+                  nq=1500, adaptive=False)
+    for f in sorted(os.listdir(g)):
+        if f.endswith(".npz"):
+            print(f"{f:40s} {os.path.getsize(os.path.join(g, f)) / 1024:8.1f} KiB")
+
+
+if __name__ == "__main__":
+    main()

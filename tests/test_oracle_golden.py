@@ -1,0 +1,114 @@
+"""Pin the C oracle (oracle/osd_oracle.c) to the reference's own outputs.
+
+The fixtures in tests/golden/ were produced by the reference (Far factories, Osd::CpuEvaluator,
+Far::PatchMap, Far::PatchTable::EvaluateBasis<double>) through tests/golden/make_golden.py.
+The oracle must reproduce the float results bit for bit, the PatchMap handles exactly and the
+FP64 results exactly.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+STENCIL_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz")))
+PATCH_FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*.npz"))) - set(STENCIL_FIXTURES))
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.int32)
+
+
+@pytest.mark.parametrize("path", STENCIL_FIXTURES, ids=os.path.basename)
+def test_eval_stencils_bitwise(path):
+    z = np.load(path)
+    n = len(z["sizes"])
+    tbl = (z["sizes"], z["offsets"], z["indices"])
+    o3 = np.zeros(n * 3, np.float32)
+    assert oracle.eval_stencils(z["positions"].ravel(), (0, 3, 3), [o3], [(0, 3, 3)], *tbl,
+                                [z["weights"]])
+    assert np.array_equal(bits(o3), bits(z["out3"]))
+    o8 = np.zeros(n * 8, np.float32)
+    assert oracle.eval_stencils(z["src8"], (0, 8, 8), [o8], [(0, 8, 8)], *tbl, [z["weights"]])
+    assert np.array_equal(bits(o8), bits(z["out8"]))
+    o5 = np.zeros(n * 5 + 5, np.float32)
+    assert oracle.eval_stencils(z["src7"], (2, 3, 7), [o5], [(1, 3, 5)], *tbl, [z["weights"]])
+    assert np.array_equal(bits(o5), bits(z["out_strided"]))
+    # in place: source and destination are one buffer (osd/mesh.h:501-540)
+    nc = len(z["positions"])
+    buf = np.zeros((nc + n) * 3, np.float32)
+    buf[: nc * 3] = z["positions"].ravel()
+    assert oracle.eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], *tbl, [z["weights"]])
+    assert np.array_equal(bits(buf), bits(z["out_inplace"]))
+
+
+@pytest.mark.parametrize("path", [p for p in STENCIL_FIXTURES if "limit_sizes" in np.load(p)],
+                         ids=os.path.basename)
+def test_eval_limit_stencils_with_derivatives_bitwise(path):
+    z = np.load(path)
+    m = len(z["limit_sizes"])
+    names = ("weights", "du_weights", "dv_weights", "duu_weights", "duv_weights", "dvv_weights")
+    ws = [z["limit_" + k] for k in names]
+    tbl = (z["limit_sizes"], z["limit_offsets"], z["limit_indices"])
+    for nout in (1, 3, 6):
+        outs = [np.zeros(m * 3, np.float32) for _ in range(nout)]
+        assert oracle.eval_stencils(z["positions"].ravel(), (0, 3, 3), outs, [(0, 3, 3)] * nout,
+                                    *tbl, ws[:nout])
+        for k in range(nout):
+            assert np.array_equal(bits(outs[k]), bits(z["limit_out6"][k])), names[k]
+
+
+@pytest.mark.parametrize("path", STENCIL_FIXTURES, ids=os.path.basename)
+def test_fp64_stencils_against_reference_double_tables(path):
+    """The FP64 oracle (float tables applied in double) against the reference's double
+    factory (same indices, double weights): they differ only by the float rounding of the
+    weights."""
+    z = np.load(path)
+    n = len(z["sizes"])
+    od = np.zeros(n * 3, np.float64)
+    assert oracle.eval_stencils(z["positions"].ravel(), (0, 3, 3), [od], [(0, 3, 3)], z["sizes"],
+                                z["offsets"], z["indices"], [z["weights"]], fp64=True)
+    src = z["positions"].astype(np.float64)
+    rows = np.repeat(np.arange(n), z["sizes"])
+    ref64 = np.zeros((n, 3))
+    np.add.at(ref64, rows, z["weights_fp64"][:, None] * src[z["indices"]])
+    diag = float(np.linalg.norm(src.max(0) - src.min(0)))
+    assert np.abs(od.reshape(n, 3) - ref64).max() <= 1e-6 * diag
+    # and the float result is within the accuracy bound of both
+    assert np.abs(z["out3"].reshape(n, 3) - ref64).max() <= 1e-5 * diag
+
+
+@pytest.mark.parametrize("path", PATCH_FIXTURES, ids=os.path.basename)
+def test_patchmap_handles_exact(path):
+    z = np.load(path)
+    pm = oracle.PatchMap(z["arrays"], z["params"], int(z["triangular"]))
+    h = pm.find(z["q_face"], z["q_u"].astype(np.float64), z["q_v"].astype(np.float64))
+    assert np.array_equal(h, z["q_handles"])
+    assert np.array_equal((h[:, 0] >= 0).astype(np.int32), z["q_found"])
+
+
+@pytest.mark.parametrize("path", PATCH_FIXTURES, ids=os.path.basename)
+def test_eval_patches_bitwise_and_fp64(path):
+    z = np.load(path)
+    m = z["coords"].shape[0]
+    args = (z["coords"], z["arrays"], z["patch_indices"], z["params"])
+    outs = [np.zeros(m * 3, np.float32) for _ in range(6)]
+    assert oracle.eval_patches(z["src"], (0, 3, 3), outs, [(0, 3, 3)] * 6, *args)
+    for k in range(6):
+        assert np.array_equal(bits(outs[k]), bits(z["out6"][k].ravel())), k
+    outd = [np.zeros(m * 3, np.float64) for _ in range(6)]
+    assert oracle.eval_patches(z["src"], (0, 3, 3), outd, [(0, 3, 3)] * 6, *args, fp64=True)
+    for k in range(6):
+        assert np.array_equal(outd[k], z["out6_fp64"][k].ravel()), k
+
+
+def test_descriptor_length_mismatch_is_rejected():
+    """CpuEvaluator returns false when a destination length differs from the source's
+    (osd/cpuEvaluator.cpp:46-47)."""
+    z = np.load(STENCIL_FIXTURES[0])
+    o = np.zeros(len(z["sizes"]) * 4, np.float32)
+    assert not oracle.eval_stencils(z["positions"].ravel(), (0, 3, 3), [o], [(0, 4, 4)],
+                                    z["sizes"], z["offsets"], z["indices"], [z["weights"]])
