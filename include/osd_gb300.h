@@ -1,0 +1,197 @@
+/*
+ * osd_gb300.h -- C ABI of the GB300 (sm_103a) Osd evaluator: libosd_gb300.so.
+ *
+ * This is the boundary the reference's own FFI for the evaluation path binds: the extern "C"
+ * block of opensubdiv/osd/cudaKernel.cu:349-426 (CudaEvalStencils, CudaEvalPatches,
+ * CudaEvalPatchesWithDerivatives) plus the device-table and vertex-buffer objects of
+ * osd/cudaEvaluator.h:52-92, osd/cudaPatchTable.h:51-110 and osd/cudaVertexBuffer.h:42-79.
+ * No C++ or CUDA types cross it: plain pointers, ints and an opaque stream handle
+ * (a cudaStream_t passed as void*; NULL means the legacy default stream).
+ *
+ * Pointer conventions follow the reference exactly:
+ *   - EvalStencils / EvalPatches take raw DEVICE pointers that already include the
+ *     BufferDescriptor offset (cudaEvaluator.cpp:159-162 adds srcDesc.offset before calling
+ *     CudaEvalStencils); `length` floats are read/written per element, `*Stride` floats apart;
+ *   - a stencil range [start, end) writes destination elements start..end-1 at their absolute
+ *     positions, as cudaKernel.cu:85-98 does;
+ *   - patch coords / arrays / params are the POD layouts OsdPatchCoord (5 x 32 bit),
+ *     OsdPatchArray (6 ints) and OsdPatchParam (3 x 32 bit) of osd/patchBasisTypes.h:249-313.
+ *
+ * Differences from the reference, all additive:
+ *   - every call returns a status (GB300_OK = 0) instead of void, and validates its
+ *     arguments on the host before any launch; GB300GetLastErrorString() explains a failure;
+ *   - every call takes a stream;
+ *   - derivative stencils are ONE fused launch (the reference makes 3 or 6 launches,
+ *     cudaEvaluator.cpp:171-292).
+ * Launches are asynchronous: results are ready after GB300Synchronize(stream) (the
+ * reference's CudaEvaluator::Synchronize, cudaEvaluator.cpp:377-380) or any later
+ * synchronising call on that stream.
+ */
+#ifndef OSD_GB300_H
+#define OSD_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    GB300_OK = 0,
+    GB300_ERR_INVALID_ARGUMENT = 1, /* null pointer, bad length/stride, inconsistent sizes */
+    GB300_ERR_CUDA = 2,             /* a CUDA runtime call or launch failed */
+    GB300_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed; nothing was left allocated */
+    GB300_ERR_UNSUPPORTED = 4,      /* e.g. an unknown patch type in a patch array */
+    GB300_ERR_DEVICE_TIMEOUT = 5    /* a bounded device-side wait gave up (see DESIGN) */
+};
+
+/* Patch types (Far::PatchDescriptor::Type, far/patchDescriptor.h:48-63). */
+enum {
+    GB300_PATCH_QUADS = 3,
+    GB300_PATCH_TRIANGLES = 4,
+    GB300_PATCH_LOOP = 5,
+    GB300_PATCH_REGULAR = 6,
+    GB300_PATCH_GREGORY_BASIS = 9,
+    GB300_PATCH_GREGORY_TRIANGLE = 10
+};
+
+/* ---- status ---------------------------------------------------------------------------- */
+
+/* Message for the last failing call on this thread ("" after success). */
+const char *GB300GetLastErrorString(void);
+
+/* Library version as MAJOR*10000 + MINOR*100 + PATCH. */
+int GB300GetVersion(void);
+
+/* Blocks until all work queued on `stream` has finished; replaces
+ * CudaEvaluator::Synchronize (osd/cudaEvaluator.cpp:377-380). */
+int GB300Synchronize(void *stream);
+
+/* ---- EvalStencils -------------------------------------------------------------------------- */
+
+/* dst[i] = sum_j weights[offsets[i]+j] * src[indices[offsets[i]+j]] for i in [start, end).
+ * Replaces CudaEvalStencils (osd/cudaKernel.cu:351-383).  `sizes`, `offsets`, `indices`,
+ * `weights` are device arrays of the Far::StencilTable (far/stencilTable.h:263-268).
+ * Source and destination may be the same buffer (Osd::Mesh::Refine, osd/mesh.h:501-540) as
+ * long as no destination element is also read as a source by another stencil. */
+int GB300EvalStencils(const float *src, float *dst, int length, int srcStride, int dstStride,
+                      const int *sizes, const int *offsets, const int *indices,
+                      const float *weights, int start, int end, void *stream);
+
+/* Fused value + first (+ second) derivative stencils in one pass over the table.
+ * Replaces the 3- and 6-launch paths of CudaEvaluator::EvalStencils
+ * (osd/cudaEvaluator.cpp:171-292) over a Far::LimitStencilTable (stencilTable.h:409-579).
+ * Any output pointer may be NULL to skip it (its weights are then not read); duu/duv/dvv
+ * with their weights may all be NULL for first derivatives only. */
+int GB300EvalStencilsWithDerivatives(
+    const float *src, float *dst, float *du, float *dv, float *duu, float *duv, float *dvv,
+    int length, int srcStride, int dstStride, int duStride, int dvStride, int duuStride,
+    int duvStride, int dvvStride, const int *sizes, const int *offsets, const int *indices,
+    const float *weights, const float *duWeights, const float *dvWeights,
+    const float *duuWeights, const float *duvWeights, const float *dvvWeights, int start,
+    int end, void *stream);
+
+/* ---- EvalPatches --------------------------------------------------------------------------- */
+
+/* Limit-surface positions at `numPatchCoords` patch coordinates.  Replaces CudaEvalPatches
+ * (osd/cudaKernel.cu:387-402).  Coords whose arrayIndex is negative (a PatchMap miss) produce
+ * zeros. */
+int GB300EvalPatches(const float *src, float *dst, int length, int srcStride, int dstStride,
+                     int numPatchCoords, const void *patchCoords, const void *patchArrays,
+                     const int *patchIndices, const void *patchParams, void *stream);
+
+/* Positions and derivatives; any output may be NULL.  Replaces
+ * CudaEvalPatchesWithDerivatives (osd/cudaKernel.cu:404-424). */
+int GB300EvalPatchesWithDerivatives(
+    const float *src, float *dst, float *du, float *dv, float *duu, float *duv, float *dvv,
+    int length, int srcStride, int dstStride, int duStride, int dvStride, int duuStride,
+    int duvStride, int dvvStride, int numPatchCoords, const void *patchCoords,
+    const void *patchArrays, const int *patchIndices, const void *patchParams, void *stream);
+
+/* ---- device stencil table (CudaStencilTable, osd/cudaEvaluator.h:52-92) ------------------ */
+
+typedef struct GB300StencilTable GB300StencilTable;
+
+/* Copies a stencil table from HOST arrays (Far::StencilTable::GetSizes/GetOffsets/
+ * GetControlIndices/GetWeights and, for limit tables, GetDu..DvvWeights; pass NULL for absent
+ * derivative arrays) into device memory.  nnz = number of control indices.  On failure
+ * returns NULL and frees anything partially allocated. */
+GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const int *sizes,
+                                           const int *offsets, const int *indices,
+                                           const float *weights, const float *duWeights,
+                                           const float *dvWeights, const float *duuWeights,
+                                           const float *duvWeights, const float *dvvWeights,
+                                           void *stream);
+void GB300StencilTableDestroy(GB300StencilTable *table);
+int GB300StencilTableGetNumStencils(const GB300StencilTable *table);
+int64_t GB300StencilTableGetNumIndices(const GB300StencilTable *table);
+/* which: 0 sizes, 1 offsets, 2 indices, 3 weights, 4 du, 5 dv, 6 duu, 7 duv, 8 dvv. */
+void *GB300StencilTableGetBuffer(const GB300StencilTable *table, int which);
+
+/* EvalStencils over a device table (CudaEvaluator::EvalStencils template form,
+ * osd/cudaEvaluator.h:125-142): all stencils [0, numStencils), outputs as in
+ * GB300EvalStencilsWithDerivatives (NULL outputs skipped). */
+int GB300StencilTableEval(const GB300StencilTable *table, const float *src, float *dst,
+                          float *du, float *dv, float *duu, float *duv, float *dvv, int length,
+                          int srcStride, int dstStride, int duStride, int dvStride,
+                          int duuStride, int duvStride, int dvvStride, void *stream);
+
+/* ---- device patch table (CudaPatchTable, osd/cudaPatchTable.h:51-110) -------------------- */
+
+typedef struct GB300PatchTable GB300PatchTable;
+
+/* Copies a flattened patch table (Osd::CpuPatchTable layout: PatchArray[numArrays],
+ * patch index buffer, PatchParam[numPatches]) from HOST memory into device memory, and
+ * builds the device PatchMap (far/patchMap.cpp) from the params.  `triangular` selects the
+ * triangle quadtree (Loop-scheme tables). */
+GB300PatchTable *GB300PatchTableCreate(int numArrays, const void *patchArrays,
+                                       int64_t numIndices, const int *patchIndices,
+                                       int numPatches, const void *patchParams, int triangular,
+                                       void *stream);
+void GB300PatchTableDestroy(GB300PatchTable *table);
+/* which: 0 patch arrays, 1 patch indices, 2 patch params. */
+void *GB300PatchTableGetBuffer(const GB300PatchTable *table, int which);
+int GB300PatchTableGetNumArrays(const GB300PatchTable *table);
+int GB300PatchTableGetNumPatches(const GB300PatchTable *table);
+
+/* Device Far::PatchMap::FindPatch (far/patchMap.h:192-231) for n queries (face, u, v) held in
+ * DEVICE memory; writes one OsdPatchCoord per query (s, t = u, v) to `coordsOut` (device).
+ * Misses (faces outside the table or holes) get handle {-1, -1, -1}.  Handles are bit-exact
+ * with the reference's double-precision walk for float inputs. */
+int GB300PatchTableFindPatches(const GB300PatchTable *table, int n, const int *faces,
+                               const float *u, const float *v, void *coordsOut, void *stream);
+
+/* EvalPatches against a device table (CudaEvaluator::EvalPatches template form). */
+int GB300PatchTableEval(const GB300PatchTable *table, const float *src, float *dst, float *du,
+                        float *dv, float *duu, float *duv, float *dvv, int length,
+                        int srcStride, int dstStride, int duStride, int dvStride,
+                        int duuStride, int duvStride, int dvvStride, int numPatchCoords,
+                        const void *patchCoords, void *stream);
+
+/* ---- vertex buffer (CudaVertexBuffer, osd/cudaVertexBuffer.h:42-79) ---------------------- */
+
+typedef struct GB300VertexBuffer GB300VertexBuffer;
+
+/* numElements floats per vertex; sizes are computed in 64 bits (the reference computes them
+ * in int, cudaVertexBuffer.cpp:85). */
+GB300VertexBuffer *GB300VertexBufferCreate(int numElements, int numVertices);
+void GB300VertexBufferDestroy(GB300VertexBuffer *buffer);
+/* Host -> device copy of numVertices vertices starting at startVertex
+ * (CudaVertexBuffer::UpdateData, cudaVertexBuffer.cpp:55-63).  Asynchronous on `stream`
+ * (pageable host memory makes it effectively synchronous). */
+int GB300VertexBufferUpdateData(GB300VertexBuffer *buffer, const float *src, int startVertex,
+                                int numVertices, void *stream);
+float *GB300VertexBufferBindCudaBuffer(GB300VertexBuffer *buffer);
+int GB300VertexBufferGetNumElements(const GB300VertexBuffer *buffer);
+int GB300VertexBufferGetNumVertices(const GB300VertexBuffer *buffer);
+
+/* ---- kernel accounting -------------------------------------------------------------------- */
+
+/* Number of this library's kernels launched since load (for launch-count reporting). */
+uint64_t GB300GetLaunchCount(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OSD_GB300_H */

@@ -1,0 +1,78 @@
+// Shared host/device helpers for libosd_gb300.so: status reporting, launch accounting and
+// small PTX wrappers.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/osd_gb300.h"
+
+namespace gb300 {
+
+// ---- status -------------------------------------------------------------------------------
+
+// Records `msg` as the calling thread's last error and returns `code`.
+int fail(int code, const char *fmt, ...);
+// Clears the calling thread's last error and returns GB300_OK.
+int ok();
+// Maps a CUDA error to a status (recording its message); GB300_OK for cudaSuccess.
+int check_cuda(cudaError_t e, const char *what);
+// Checks the launch that was just queued.
+int check_launch(const char *what);
+
+extern std::atomic<uint64_t> g_launches;
+inline void count_launch(uint64_t n = 1) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+// Number of SMs of the current device (cached per device).
+int num_sms();
+
+// ---- device helpers -----------------------------------------------------------------------
+
+// L2 eviction policies (createpolicy) for the cache-hinted loads below.
+__device__ __forceinline__ uint64_t l2_evict_first() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ uint64_t l2_evict_last() {
+    uint64_t p;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+// Streaming (read-once) 32-bit loads for the stencil table: no L1 allocation and an
+// evict-first L2 policy, so the table stream does not push the source rows out of L2.
+__device__ __forceinline__ int ld_stream(const int *p, uint64_t pol) {
+    int v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.b32 %0, [%1], %2;"
+                 : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ float ld_stream(const float *p, uint64_t pol) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;"
+                 : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// Source-row loads: read-only path, kept in L1, evict-last in L2 (the control points are
+// re-read by every stencil that touches them).
+__device__ __forceinline__ float ld_src(const float *p, uint64_t pol) {
+    float v;
+    asm("ld.global.nc.L1::evict_last.L2::cache_hint.f32 %0, [%1], %2;"
+                 : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
+// Streaming stores for outputs (written once, not re-read by this launch).
+__device__ __forceinline__ void st_stream(float *p, float v) {
+    asm volatile("st.global.cs.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");
+}
+
+}  // namespace gb300

@@ -1,0 +1,281 @@
+// Device-resident tables and buffers: the GB300 counterparts of CudaStencilTable
+// (osd/cudaEvaluator.cpp:100-145), CudaPatchTable (osd/cudaPatchTable.cpp:59-162) and
+// CudaVertexBuffer (osd/cudaVertexBuffer.cpp:35-91).  Unlike the reference, a failed
+// allocation or copy frees everything allocated so far and reports a status.
+#include "common.cuh"
+#include "patchmap.h"
+
+#include <new>
+#include <vector>
+
+using namespace gb300;
+
+namespace {
+
+// Allocates `bytes` (rounded up to 16 so bulk copies of the tail stay in bounds) and copies
+// `host` into it; returns false (with the status recorded) on failure.
+bool upload(void **dptr, const void *host, size_t bytes, cudaStream_t s, const char *what) {
+    *dptr = nullptr;
+    if (!host || bytes == 0) return true;
+    size_t padded = (bytes + 15) & ~(size_t)15;
+    if (check_cuda(cudaMalloc(dptr, padded), what) != GB300_OK) {
+        *dptr = nullptr;
+        return false;
+    }
+    if (padded != bytes &&
+        check_cuda(cudaMemsetAsync((char *)*dptr + bytes, 0, padded - bytes, s), what) != GB300_OK)
+        return false;
+    if (check_cuda(cudaMemcpyAsync(*dptr, host, bytes, cudaMemcpyHostToDevice, s), what) !=
+        GB300_OK)
+        return false;
+    return true;
+}
+
+void release(void *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+}  // namespace
+
+struct GB300StencilTable {
+    int numStencils = 0;
+    int64_t nnz = 0;
+    void *buf[9] = {nullptr};  // sizes, offsets, indices, w, du, dv, duu, duv, dvv
+    ~GB300StencilTable() {
+        for (auto &p : buf) release(p);
+    }
+};
+
+struct GB300PatchTable {
+    int numArrays = 0, numPatches = 0;
+    int64_t numIndices = 0;
+    void *arrays = nullptr, *indices = nullptr, *params = nullptr;
+    PatchMapDevice map;
+    ~GB300PatchTable() {
+        release(arrays);
+        release(indices);
+        release(params);
+        release(map.nodes);
+        release(map.handles);
+    }
+};
+
+struct GB300VertexBuffer {
+    int numElements = 0, numVertices = 0;
+    float *mem = nullptr;
+    ~GB300VertexBuffer() {
+        if (mem) cudaFree(mem);
+    }
+};
+
+extern "C" {
+
+GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const int *sizes,
+                                           const int *offsets, const int *indices,
+                                           const float *weights, const float *duWeights,
+                                           const float *dvWeights, const float *duuWeights,
+                                           const float *duvWeights, const float *dvvWeights,
+                                           void *stream) {
+    if (numStencils < 0 || nnz < 0 || (numStencils > 0 && (!sizes || !offsets)) ||
+        (nnz > 0 && (!indices || !weights))) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilTableCreate: bad arguments");
+        return nullptr;
+    }
+    cudaStream_t s = as_stream(stream);
+    GB300StencilTable *t = new (std::nothrow) GB300StencilTable;
+    if (!t) {
+        fail(GB300_ERR_OUT_OF_MEMORY, "GB300StencilTableCreate: host allocation");
+        return nullptr;
+    }
+    t->numStencils = numStencils;
+    t->nnz = nnz;
+    const void *host[9] = {sizes, offsets, indices, weights, duWeights,
+                           dvWeights, duuWeights, duvWeights, dvvWeights};
+    const size_t bytes[9] = {(size_t)numStencils * 4, (size_t)numStencils * 4,
+                             (size_t)nnz * 4, (size_t)nnz * 4, (size_t)nnz * 4,
+                             (size_t)nnz * 4, (size_t)nnz * 4, (size_t)nnz * 4,
+                             (size_t)nnz * 4};
+    for (int k = 0; k < 9; ++k) {
+        if (!upload(&t->buf[k], host[k], bytes[k], s, "GB300StencilTableCreate")) {
+            delete t;
+            return nullptr;
+        }
+    }
+    if (check_cuda(cudaStreamSynchronize(s), "GB300StencilTableCreate") != GB300_OK) {
+        delete t;
+        return nullptr;
+    }
+    ok();
+    return t;
+}
+
+void GB300StencilTableDestroy(GB300StencilTable *t) { delete t; }
+
+int GB300StencilTableGetNumStencils(const GB300StencilTable *t) { return t ? t->numStencils : 0; }
+
+int64_t GB300StencilTableGetNumIndices(const GB300StencilTable *t) { return t ? t->nnz : 0; }
+
+void *GB300StencilTableGetBuffer(const GB300StencilTable *t, int which) {
+    if (!t || which < 0 || which > 8) return nullptr;
+    return t->buf[which];
+}
+
+int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *dst, float *du,
+                          float *dv, float *duu, float *duv, float *dvv, int length,
+                          int srcStride, int dstStride, int duStride, int dvStride,
+                          int duuStride, int duvStride, int dvvStride, void *stream) {
+    if (!t) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilTableEval: null table");
+    float *d[6] = {dst, du, dv, duu, duv, dvv};
+    const int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
+    const float *w[6];
+    for (int k = 0; k < 6; ++k) {
+        w[k] = (const float *)t->buf[3 + k];
+        if (d[k] && !w[k])
+            return fail(GB300_ERR_INVALID_ARGUMENT,
+                        "GB300StencilTableEval: output %d requested but the table has no such "
+                        "weights",
+                        k);
+    }
+    return eval_stencils(src, d, st, w, length, srcStride, (const int *)t->buf[0],
+                         (const int *)t->buf[1], (const int *)t->buf[2], 0, t->numStencils,
+                         as_stream(stream), "GB300StencilTableEval");
+}
+
+GB300PatchTable *GB300PatchTableCreate(int numArrays, const void *patchArrays,
+                                       int64_t numIndices, const int *patchIndices,
+                                       int numPatches, const void *patchParams, int triangular,
+                                       void *stream) {
+    if (numArrays < 0 || numIndices < 0 || numPatches < 0 ||
+        (numArrays > 0 && !patchArrays) || (numIndices > 0 && !patchIndices) ||
+        (numPatches > 0 && !patchParams)) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableCreate: bad arguments");
+        return nullptr;
+    }
+    const int *arr = (const int *)patchArrays;
+    for (int a = 0; a < numArrays; ++a) {
+        for (int k = 0; k < 2; ++k) {
+            const int type = arr[6 * a + k];
+            if (type != GB300_PATCH_QUADS && type != GB300_PATCH_TRIANGLES &&
+                type != GB300_PATCH_LOOP && type != GB300_PATCH_REGULAR &&
+                type != GB300_PATCH_GREGORY_BASIS && type != GB300_PATCH_GREGORY_TRIANGLE) {
+                fail(GB300_ERR_UNSUPPORTED, "GB300PatchTableCreate: patch type %d in array %d",
+                     type, a);
+                return nullptr;
+            }
+        }
+        const int64_t last =
+            (int64_t)arr[6 * a + 3] + (int64_t)arr[6 * a + 4] * arr[6 * a + 2];
+        if (last > numIndices || arr[6 * a + 5] < 0 ||
+            arr[6 * a + 5] + (int64_t)arr[6 * a + 2] > numPatches) {
+            fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableCreate: array %d out of range", a);
+            return nullptr;
+        }
+    }
+    PatchMapHost hm;
+    if (build_patch_map(numArrays, arr, numPatches, (const int *)patchParams, triangular, hm) !=
+        GB300_OK)
+        return nullptr;
+    cudaStream_t s = as_stream(stream);
+    GB300PatchTable *t = new (std::nothrow) GB300PatchTable;
+    if (!t) {
+        fail(GB300_ERR_OUT_OF_MEMORY, "GB300PatchTableCreate: host allocation");
+        return nullptr;
+    }
+    t->numArrays = numArrays;
+    t->numPatches = numPatches;
+    t->numIndices = numIndices;
+    const char *w = "GB300PatchTableCreate";
+    if (!upload(&t->arrays, patchArrays, (size_t)numArrays * 24, s, w) ||
+        !upload(&t->indices, patchIndices, (size_t)numIndices * 4, s, w) ||
+        !upload(&t->params, patchParams, (size_t)numPatches * 12, s, w) ||
+        !upload(&t->map.nodes, hm.nodes.data(), hm.nodes.size() * 4, s, w) ||
+        !upload(&t->map.handles, hm.handles.data(), hm.handles.size() * 4, s, w) ||
+        check_cuda(cudaStreamSynchronize(s), w) != GB300_OK) {
+        delete t;
+        return nullptr;
+    }
+    t->map.triangular = triangular;
+    t->map.minFace = hm.minFace;
+    t->map.maxFace = hm.maxFace;
+    t->map.maxDepth = hm.maxDepth;
+    t->map.numPatches = numPatches;
+    ok();
+    return t;
+}
+
+void GB300PatchTableDestroy(GB300PatchTable *t) { delete t; }
+
+void *GB300PatchTableGetBuffer(const GB300PatchTable *t, int which) {
+    if (!t) return nullptr;
+    return which == 0 ? t->arrays : which == 1 ? t->indices : which == 2 ? t->params : nullptr;
+}
+
+int GB300PatchTableGetNumArrays(const GB300PatchTable *t) { return t ? t->numArrays : 0; }
+
+int GB300PatchTableGetNumPatches(const GB300PatchTable *t) { return t ? t->numPatches : 0; }
+
+int GB300PatchTableFindPatches(const GB300PatchTable *t, int n, const int *faces, const float *u,
+                               const float *v, void *coordsOut, void *stream) {
+    if (!t) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableFindPatches: null table");
+    return find_patches(t->map, n, faces, u, v, coordsOut, as_stream(stream));
+}
+
+int GB300PatchTableEval(const GB300PatchTable *t, const float *src, float *dst, float *du,
+                        float *dv, float *duu, float *duv, float *dvv, int length,
+                        int srcStride, int dstStride, int duStride, int dvStride,
+                        int duuStride, int duvStride, int dvvStride, int numPatchCoords,
+                        const void *patchCoords, void *stream) {
+    if (!t) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableEval: null table");
+    float *d[6] = {dst, du, dv, duu, duv, dvv};
+    const int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
+    return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, t->arrays,
+                        (const int *)t->indices, t->params, as_stream(stream),
+                        "GB300PatchTableEval");
+}
+
+GB300VertexBuffer *GB300VertexBufferCreate(int numElements, int numVertices) {
+    if (numElements <= 0 || numVertices < 0) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "GB300VertexBufferCreate: bad size");
+        return nullptr;
+    }
+    GB300VertexBuffer *b = new (std::nothrow) GB300VertexBuffer;
+    if (!b) {
+        fail(GB300_ERR_OUT_OF_MEMORY, "GB300VertexBufferCreate: host allocation");
+        return nullptr;
+    }
+    b->numElements = numElements;
+    b->numVertices = numVertices;
+    const size_t bytes = (size_t)numElements * (size_t)numVertices * sizeof(float);
+    if (bytes > 0 && check_cuda(cudaMalloc((void **)&b->mem, bytes), "GB300VertexBufferCreate") !=
+                         GB300_OK) {
+        b->mem = nullptr;
+        delete b;
+        return nullptr;
+    }
+    ok();
+    return b;
+}
+
+void GB300VertexBufferDestroy(GB300VertexBuffer *b) { delete b; }
+
+int GB300VertexBufferUpdateData(GB300VertexBuffer *b, const float *src, int startVertex,
+                                int numVertices, void *stream) {
+    if (!b || !src || startVertex < 0 || numVertices < 0 ||
+        (int64_t)startVertex + numVertices > b->numVertices)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "GB300VertexBufferUpdateData: bad range");
+    if (numVertices == 0) return ok();
+    const size_t off = (size_t)startVertex * b->numElements;
+    const size_t bytes = (size_t)numVertices * b->numElements * sizeof(float);
+    return check_cuda(cudaMemcpyAsync(b->mem + off, src, bytes, cudaMemcpyHostToDevice,
+                                      as_stream(stream)),
+                      "GB300VertexBufferUpdateData");
+}
+
+float *GB300VertexBufferBindCudaBuffer(GB300VertexBuffer *b) { return b ? b->mem : nullptr; }
+
+int GB300VertexBufferGetNumElements(const GB300VertexBuffer *b) { return b ? b->numElements : 0; }
+
+int GB300VertexBufferGetNumVertices(const GB300VertexBuffer *b) { return b ? b->numVertices : 0; }
+
+}  // extern "C"

@@ -1,0 +1,140 @@
+// EvalPatches for sm_103a: one thread per patch coordinate; PatchParam decode, basis and the
+// gather of up to 20 control points are fused and kept in registers, and all requested
+// outputs (P, dPdu, dPdv, dPduu, dPduv, dPdvv) come out of one pass.  Replaces
+// computePatches (osd/cudaKernel.cu:244-328), which spills six float[20] weight arrays and
+// accumulates each output in global memory.
+#include "common.cuh"
+#include "patch_basis.cuh"
+
+namespace gb300 {
+
+struct Coord {
+    int arrayIndex, patchIndex, vertIndex;
+    float s, t;
+};
+struct Array {
+    int regDesc, desc, numPatches, indexBase, stride, primitiveIdBase;
+};
+struct ParamRec {
+    int field0, field1;
+    float sharpness;
+};
+
+struct PatchArgs {
+    const float *src;
+    float *dst[6];
+    int dstStride[6];
+    int active;
+    int length;
+    int srcStride;
+    int numCoords;
+    const Coord *coords;
+    const Array *arrays;
+    const int *indices;
+    const ParamRec *params;
+};
+
+template <int LC>
+__global__ void __launch_bounds__(128) k_eval_patches(const PatchArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.numCoords; i += stride) {
+        const Coord c = a.coords[i];
+        for (int e0 = 0; e0 < a.length; e0 += LC) {
+            Acc6<LC> acc;
+            acc.zero();
+            float d1 = 1.0f, d2 = 1.0f;
+            if (c.arrayIndex >= 0) {
+                const Array arr = a.arrays[c.arrayIndex];
+                const ParamRec pr = a.params[c.patchIndex];
+                const Param p{pr.field0, pr.field1};
+                const int type = p.regular() ? arr.regDesc : arr.desc;
+                const int *cvs =
+                    a.indices + arr.indexBase + arr.stride * (c.patchIndex - arr.primitiveIdBase);
+                if (!eval_patch_point<LC>(type, p, c.s, c.t, cvs, a.src, a.srcStride, e0,
+                                          a.length, acc, d1, d2))
+                    acc.zero();
+            }
+            const float scale[6] = {1.0f, d1, d1, d2, d2, d2};
+#pragma unroll
+            for (int k = 0; k < 6; ++k) {
+                if (!(a.active & (1 << k))) continue;
+                float *out = a.dst[k] + (size_t)i * a.dstStride[k] + e0;
+#pragma unroll
+                for (int q = 0; q < LC; ++q)
+                    if (e0 + q < a.length) st_stream(out + q, acc.v[k][q] * scale[k]);
+            }
+        }
+    }
+}
+
+int eval_patches(const float *src, float *const *dst, const int *strides, int length,
+                 int srcStride, int numCoords, const void *coords, const void *arrays,
+                 const int *indices, const void *params, cudaStream_t s, const char *who) {
+    if (numCoords <= 0) return ok();
+    if (!src || !coords || !arrays || !indices || !params)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: null source, coord or table pointer", who);
+    if (length <= 0 || srcStride < length)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad length %d / source stride %d", who,
+                    length, srcStride);
+    PatchArgs a{};
+    a.src = src;
+    a.length = length;
+    a.srcStride = srcStride;
+    a.numCoords = numCoords;
+    a.coords = (const Coord *)coords;
+    a.arrays = (const Array *)arrays;
+    a.indices = indices;
+    a.params = (const ParamRec *)params;
+    for (int k = 0; k < 6; ++k) {
+        if (!dst[k]) continue;
+        if (strides[k] < length)
+            return fail(GB300_ERR_INVALID_ARGUMENT, "%s: output %d stride %d < length %d", who, k,
+                        strides[k], length);
+        a.dst[k] = dst[k];
+        a.dstStride[k] = strides[k];
+        a.active |= 1 << k;
+    }
+    if (!a.active) return ok();
+    const int threads = 128;
+    long long blocks = ((long long)numCoords + threads - 1) / threads;
+    long long cap = (long long)num_sms() * 32;
+    const int grid = (int)(blocks < cap ? blocks : cap);
+    switch (length) {
+        case 1: k_eval_patches<1><<<grid, threads, 0, s>>>(a); break;
+        case 2: k_eval_patches<2><<<grid, threads, 0, s>>>(a); break;
+        case 3: k_eval_patches<3><<<grid, threads, 0, s>>>(a); break;
+        default: k_eval_patches<4><<<grid, threads, 0, s>>>(a); break;
+    }
+    count_launch();
+    return check_launch(who);
+}
+
+}  // namespace gb300
+
+using namespace gb300;
+
+extern "C" {
+
+int GB300EvalPatches(const float *src, float *dst, int length, int srcStride, int dstStride,
+                     int numPatchCoords, const void *patchCoords, const void *patchArrays,
+                     const int *patchIndices, const void *patchParams, void *stream) {
+    if (!dst) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300EvalPatches: null destination");
+    float *d[6] = {dst, 0, 0, 0, 0, 0};
+    int st[6] = {dstStride, 0, 0, 0, 0, 0};
+    return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, patchArrays,
+                        patchIndices, patchParams, as_stream(stream), "GB300EvalPatches");
+}
+
+int GB300EvalPatchesWithDerivatives(
+    const float *src, float *dst, float *du, float *dv, float *duu, float *duv, float *dvv,
+    int length, int srcStride, int dstStride, int duStride, int dvStride, int duuStride,
+    int duvStride, int dvvStride, int numPatchCoords, const void *patchCoords,
+    const void *patchArrays, const int *patchIndices, const void *patchParams, void *stream) {
+    float *d[6] = {dst, du, dv, duu, duv, dvv};
+    int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
+    return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, patchArrays,
+                        patchIndices, patchParams, as_stream(stream),
+                        "GB300EvalPatchesWithDerivatives");
+}
+
+}  // extern "C"

@@ -1,0 +1,40 @@
+// Host-side PatchMap quadtree (built from patch params) and its device mirror.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+namespace gb300 {
+
+struct PatchMapHost {
+    int triangular = 0, minFace = 0, maxFace = -1, maxDepth = 0;
+    std::vector<uint32_t> nodes;  // 4 packed children per node; roots first (one per face)
+    std::vector<int> handles;     // 4 ints per patch: array, patch, vert, pad
+};
+
+struct PatchMapDevice {
+    void *nodes = nullptr;
+    void *handles = nullptr;
+    int triangular = 0, minFace = 0, maxFace = -1, maxDepth = 0, numPatches = 0;
+};
+
+// Builds the quadtree of far/patchMap.cpp:89-202 from host arrays (6 ints per patch array,
+// 3 x 32-bit per patch param).
+int build_patch_map(int numArrays, const int *arrays, int numPatches, const int *params,
+                    int triangular, PatchMapHost &out);
+
+int find_patches(const PatchMapDevice &m, int n, const int *faces, const float *u,
+                 const float *v, void *coordsOut, cudaStream_t s);
+
+int eval_stencils(const float *src, float *const *dst, const int *strides,
+                  const float *const *w, int length, int srcStride, const int *sizes,
+                  const int *offsets, const int *indices, int start, int end, cudaStream_t s,
+                  const char *who);
+
+int eval_patches(const float *src, float *const *dst, const int *strides, int length,
+                 int srcStride, int numCoords, const void *coords, const void *arrays,
+                 const int *indices, const void *params, cudaStream_t s, const char *who);
+
+}  // namespace gb300

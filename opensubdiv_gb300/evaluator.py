@@ -1,0 +1,289 @@
+"""Python mirror of the Osd evaluator interface over libosd_gb300.so.
+
+Names and argument meanings follow the reference's static evaluator API
+(osd/cudaEvaluator.h:94-1262, osd/cpuEvaluator.h:39+) and its device-object wrappers
+(CudaStencilTable osd/cudaEvaluator.h:52-92, CudaPatchTable osd/cudaPatchTable.h:51-110,
+CudaVertexBuffer osd/cudaVertexBuffer.h:42-79):
+
+* raw pointers (or CUDA tensors) exclude the BufferDescriptor offset; the evaluator adds it
+  (cudaEvaluator.cpp:159-162);
+* ``EvalStencils`` / ``EvalPatches`` return ``True`` on success and ``False`` on an invalid
+  request (mismatched lengths, null table ...), like the reference's bool; the reason is in
+  :func:`last_error`.  CUDA failures raise :class:`GB300Error`;
+* work is queued on ``stream`` (a ``torch.cuda.Stream``, a raw ``cudaStream_t`` int or
+  ``None`` for the legacy default stream); call :meth:`GB300Evaluator.Synchronize`.
+
+Device memory is plain CUDA memory; torch tensors are accepted as a convenience.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from ._lib import GB300Error, check, last_error  # noqa: F401
+
+# Far::PatchDescriptor::Type values (far/patchDescriptor.h:48-63)
+QUADS, TRIANGLES, LOOP, REGULAR, GREGORY_BASIS, GREGORY_TRIANGLE = 3, 4, 5, 6, 9, 10
+
+
+@dataclass
+class BufferDescriptor:
+    """(offset, length, stride) of one primvar in an interleaved float buffer
+    (osd/bufferDescriptor.h:61-103)."""
+
+    offset: int = 0
+    length: int = 0
+    stride: int = 0
+
+    def GetLocalOffset(self) -> int:
+        return self.offset % self.stride if self.stride > 0 else 0
+
+    def IsValid(self) -> bool:
+        return self.length > 0 and self.length <= self.stride - self.GetLocalOffset()
+
+
+def _ptr(x, offset_floats: int = 0):
+    """Device address of x (+ offset in 4-byte elements) or None."""
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x + 4 * offset_floats
+    if hasattr(x, "data_ptr"):
+        if not x.is_cuda:
+            raise ValueError("GB300 evaluator buffers must live in device memory")
+        return x.data_ptr() + 4 * offset_floats
+    if hasattr(x, "BindCudaBuffer"):
+        return x.BindCudaBuffer() + 4 * offset_floats
+    raise TypeError(f"cannot take a device address of {type(x).__name__}")
+
+
+def _stream(s):
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream  # torch.cuda.Stream
+
+
+def _status_to_bool(status: int) -> bool:
+    if status == 0:
+        return True
+    if status == 1:  # GB300_ERR_INVALID_ARGUMENT: the reference's `return false`
+        return False
+    raise GB300Error(status, last_error())
+
+
+def _desc(d):
+    return d if d is not None else BufferDescriptor()
+
+
+class GB300Evaluator:
+    """Static, stateless evaluator (drop-in beside CpuEvaluator / CudaEvaluator)."""
+
+    @staticmethod
+    def EvalStencils(src, srcDesc, dst, dstDesc, sizes, offsets, indices, weights,
+                     start=0, end=None, du=None, duDesc=None, dv=None, dvDesc=None,
+                     duWeights=None, dvWeights=None, duu=None, duuDesc=None, duv=None,
+                     duvDesc=None, dvv=None, dvvDesc=None, duuWeights=None, duvWeights=None,
+                     dvvWeights=None, stream=None) -> bool:
+        """dst[i] = sum_j w_j src[idx_j] for stencils [start, end)
+        (CudaEvaluator::EvalStencils, osd/cudaEvaluator.cpp:150-292).  The derivative forms
+        run in the same single pass."""
+        lib = _lib.load()
+        if end is None:
+            end = int(sizes.shape[0]) if hasattr(sizes, "shape") else 0
+        outs = [(dst, dstDesc), (du, duDesc), (dv, dvDesc), (duu, duuDesc), (duv, duvDesc),
+                (dvv, dvvDesc)]
+        for o, d in outs:
+            if o is not None and _desc(d).length != srcDesc.length:
+                return False  # cpuEvaluator.cpp:46-47
+        ws = [weights, duWeights, dvWeights, duuWeights, duvWeights, dvvWeights]
+        if all(o is None for o, _ in outs[1:]):
+            st = lib.GB300EvalStencils(_ptr(src, srcDesc.offset), _ptr(dst, dstDesc.offset),
+                                       srcDesc.length, srcDesc.stride, dstDesc.stride,
+                                       _ptr(sizes), _ptr(offsets), _ptr(indices), _ptr(weights),
+                                       start, end, _stream(stream))
+        else:
+            ptrs = [_ptr(o, _desc(d).offset) if o is not None else None for o, d in outs]
+            strides = [_desc(d).stride for _, d in outs]
+            st = lib.GB300EvalStencilsWithDerivatives(
+                _ptr(src, srcDesc.offset), *ptrs, srcDesc.length, srcDesc.stride, *strides,
+                _ptr(sizes), _ptr(offsets), _ptr(indices),
+                *[_ptr(w) if o is not None else None for w, (o, _) in zip(ws, outs)],
+                start, end, _stream(stream))
+        return _status_to_bool(st)
+
+    @staticmethod
+    def EvalStencilsTable(src, srcDesc, dst, dstDesc, table, du=None, duDesc=None, dv=None,
+                          dvDesc=None, duu=None, duuDesc=None, duv=None, duvDesc=None,
+                          dvv=None, dvvDesc=None, stream=None) -> bool:
+        """Template form over a device table (osd/cudaEvaluator.h:125-142)."""
+        outs = [(dst, dstDesc), (du, duDesc), (dv, dvDesc), (duu, duuDesc), (duv, duvDesc),
+                (dvv, dvvDesc)]
+        for o, d in outs:
+            if o is not None and _desc(d).length != srcDesc.length:
+                return False
+        ptrs = [_ptr(o, _desc(d).offset) if o is not None else None for o, d in outs]
+        strides = [_desc(d).stride for _, d in outs]
+        st = _lib.load().GB300StencilTableEval(table.handle, _ptr(src, srcDesc.offset), *ptrs,
+                                               srcDesc.length, srcDesc.stride, *strides,
+                                               _stream(stream))
+        return _status_to_bool(st)
+
+    @staticmethod
+    def EvalPatches(src, srcDesc, dst, dstDesc, numPatchCoords, patchCoords, patchArrays,
+                    patchIndices, patchParams, du=None, duDesc=None, dv=None, dvDesc=None,
+                    duu=None, duuDesc=None, duv=None, duvDesc=None, dvv=None, dvvDesc=None,
+                    stream=None) -> bool:
+        """Limit evaluation at patch coordinates (CudaEvaluator::EvalPatches,
+        osd/cudaEvaluator.cpp:295-372)."""
+        lib = _lib.load()
+        outs = [(dst, dstDesc), (du, duDesc), (dv, dvDesc), (duu, duuDesc), (duv, duvDesc),
+                (dvv, dvvDesc)]
+        for o, d in outs:
+            if o is not None and _desc(d).length != srcDesc.length:
+                return False
+        if all(o is None for o, _ in outs[1:]):
+            st = lib.GB300EvalPatches(_ptr(src, srcDesc.offset), _ptr(dst, dstDesc.offset),
+                                      srcDesc.length, srcDesc.stride, dstDesc.stride,
+                                      numPatchCoords, _ptr(patchCoords), _ptr(patchArrays),
+                                      _ptr(patchIndices), _ptr(patchParams), _stream(stream))
+        else:
+            ptrs = [_ptr(o, _desc(d).offset) if o is not None else None for o, d in outs]
+            strides = [_desc(d).stride for _, d in outs]
+            st = lib.GB300EvalPatchesWithDerivatives(
+                _ptr(src, srcDesc.offset), *ptrs, srcDesc.length, srcDesc.stride, *strides,
+                numPatchCoords, _ptr(patchCoords), _ptr(patchArrays), _ptr(patchIndices),
+                _ptr(patchParams), _stream(stream))
+        return _status_to_bool(st)
+
+    @staticmethod
+    def EvalPatchesTable(src, srcDesc, dst, dstDesc, numPatchCoords, patchCoords, table,
+                         du=None, duDesc=None, dv=None, dvDesc=None, duu=None, duuDesc=None,
+                         duv=None, duvDesc=None, dvv=None, dvvDesc=None, stream=None) -> bool:
+        """Template form over a device patch table (osd/cudaEvaluator.h:502-525)."""
+        outs = [(dst, dstDesc), (du, duDesc), (dv, dvDesc), (duu, duuDesc), (duv, duvDesc),
+                (dvv, dvvDesc)]
+        for o, d in outs:
+            if o is not None and _desc(d).length != srcDesc.length:
+                return False
+        ptrs = [_ptr(o, _desc(d).offset) if o is not None else None for o, d in outs]
+        strides = [_desc(d).stride for _, d in outs]
+        st = _lib.load().GB300PatchTableEval(table.handle, _ptr(src, srcDesc.offset), *ptrs,
+                                             srcDesc.length, srcDesc.stride, *strides,
+                                             numPatchCoords, _ptr(patchCoords), _stream(stream))
+        return _status_to_bool(st)
+
+    @staticmethod
+    def Synchronize(stream=None):
+        check(_lib.load().GB300Synchronize(_stream(stream)))
+
+
+class GB300StencilTable:
+    """Device copy of a Far::StencilTable / LimitStencilTable (CudaStencilTable)."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    @classmethod
+    def Create(cls, sizes, offsets, indices, weights, duWeights=None, dvWeights=None,
+               duuWeights=None, duvWeights=None, dvvWeights=None, stream=None):
+        """From host (numpy) arrays in Far layout; int32 sizes/offsets/indices, float32
+        weights."""
+        arrs = [np.ascontiguousarray(a, np.int32) for a in (sizes, offsets, indices)]
+        ws = [np.ascontiguousarray(w, np.float32) if w is not None else None
+              for w in (weights, duWeights, dvWeights, duuWeights, duvWeights, dvvWeights)]
+        h = _lib.load().GB300StencilTableCreate(
+            len(arrs[0]), len(arrs[2]), *[a.ctypes.data for a in arrs],
+            *[w.ctypes.data if w is not None else None for w in ws], _stream(stream))
+        if not h:
+            raise GB300Error(3, last_error())
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            _lib.load().GB300StencilTableDestroy(self.handle)
+            self.handle = None
+
+    def GetNumStencils(self):
+        return _lib.load().GB300StencilTableGetNumStencils(self.handle)
+
+    def _buf(self, k):
+        return _lib.load().GB300StencilTableGetBuffer(self.handle, k)
+
+    def GetSizesBuffer(self): return self._buf(0)
+    def GetOffsetsBuffer(self): return self._buf(1)
+    def GetIndicesBuffer(self): return self._buf(2)
+    def GetWeightsBuffer(self): return self._buf(3)
+    def GetDuWeightsBuffer(self): return self._buf(4)
+    def GetDvWeightsBuffer(self): return self._buf(5)
+    def GetDuuWeightsBuffer(self): return self._buf(6)
+    def GetDuvWeightsBuffer(self): return self._buf(7)
+    def GetDvvWeightsBuffer(self): return self._buf(8)
+
+
+class GB300PatchTable:
+    """Device copy of a flattened Far::PatchTable plus its device PatchMap (CudaPatchTable)."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    @classmethod
+    def Create(cls, arrays, indices, params, triangular=False, stream=None):
+        """From host arrays in Osd::CpuPatchTable layout: int32 [nArrays, 6] patch arrays,
+        int32 index buffer, int32 [nPatches, 3] params (field0, field1, sharpness bits)."""
+        a = np.ascontiguousarray(arrays, np.int32)
+        i = np.ascontiguousarray(indices, np.int32)
+        p = np.ascontiguousarray(params, np.int32)
+        h = _lib.load().GB300PatchTableCreate(len(a), a.ctypes.data, len(i), i.ctypes.data,
+                                              len(p), p.ctypes.data, int(bool(triangular)),
+                                              _stream(stream))
+        if not h:
+            raise GB300Error(1, last_error())
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            _lib.load().GB300PatchTableDestroy(self.handle)
+            self.handle = None
+
+    def GetPatchArrayBuffer(self): return _lib.load().GB300PatchTableGetBuffer(self.handle, 0)
+    def GetPatchIndexBuffer(self): return _lib.load().GB300PatchTableGetBuffer(self.handle, 1)
+    def GetPatchParamBuffer(self): return _lib.load().GB300PatchTableGetBuffer(self.handle, 2)
+
+    def FindPatches(self, n, faces, u, v, coords_out, stream=None):
+        """Device PatchMap lookup: writes n OsdPatchCoord records to coords_out."""
+        check(_lib.load().GB300PatchTableFindPatches(self.handle, n, _ptr(faces), _ptr(u),
+                                                     _ptr(v), _ptr(coords_out), _stream(stream)))
+
+
+class GB300VertexBuffer:
+    """Owning device float buffer of numVertices x numElements (CudaVertexBuffer)."""
+
+    def __init__(self, handle):
+        self.handle = handle
+
+    @classmethod
+    def Create(cls, numElements, numVertices, deviceContext=None):
+        h = _lib.load().GB300VertexBufferCreate(numElements, numVertices)
+        if not h:
+            raise GB300Error(3, last_error())
+        return cls(h)
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            _lib.load().GB300VertexBufferDestroy(self.handle)
+            self.handle = None
+
+    def UpdateData(self, src, startVertex, numVertices, stream=None):
+        src = np.ascontiguousarray(src, np.float32)
+        check(_lib.load().GB300VertexBufferUpdateData(self.handle, src.ctypes.data, startVertex,
+                                                      numVertices, _stream(stream)))
+
+    def BindCudaBuffer(self) -> int:
+        return _lib.load().GB300VertexBufferBindCudaBuffer(self.handle)
+
+    def GetNumElements(self): return _lib.load().GB300VertexBufferGetNumElements(self.handle)
+    def GetNumVertices(self): return _lib.load().GB300VertexBufferGetNumVertices(self.handle)

@@ -64,15 +64,39 @@ def eval_stencils(src, src_desc, dsts, dst_descs, sizes, offsets, indices, weigh
 
 
 def eval_patches(src, src_desc, dsts, dst_descs, coords, arrays, indices, params, threads=1,
-                 fp64=False):
+                 fp64=False, absolute=False):
     """Restated EvalPatches (osd/cpuEvaluator.cpp:157-381).  coords: int32 [n, 5] view of
-    PatchCoord records (s, t stored as float bits)."""
-    fn = lib().orc_eval_patches_d if fp64 else lib().orc_eval_patches_f
+    PatchCoord records (s, t stored as float bits).  absolute=True writes sum_j |w_j x_j|
+    (double) instead: the scale of the float rounding error of each output."""
+    if absolute:
+        fn = lib().orc_eval_patches_abs
+    else:
+        fn = lib().orc_eval_patches_d if fp64 else lib().orc_eval_patches_f
     ok = fn(_p(np.ascontiguousarray(src, np.float32)), _p(np.asarray(src_desc, np.int32)),
             C.c_int(len(dsts)), _ptrs(dsts), _p(np.asarray(dst_descs, np.int32).ravel()),
             C.c_int(coords.shape[0]), _p(coords), _p(arrays), _p(indices), _p(params),
             C.c_int(threads))
     return bool(ok)
+
+
+def abs_scale(src, src_desc, length, coords, arrays, indices, params):
+    """[6, n*length] array of sum_j |w_j x_j| for the six EvalPatches outputs."""
+    m = coords.shape[0]
+    outs = [np.zeros(m * length) for _ in range(6)]
+    eval_patches(src, src_desc, outs, [(0, length, length)] * 6, coords, arrays, indices, params,
+                 threads=4, absolute=True)
+    return np.stack(outs)
+
+
+def stencil_abs_scale(src, src_desc, sizes, offsets, indices, weights, threads=4):
+    """sum_j |w_j x_j| per stencil and element (double), for tolerance statements."""
+    n = len(sizes)
+    length = src_desc[1]
+    out = np.zeros(n * length)
+    eval_stencils(np.abs(np.asarray(src, np.float32)), src_desc, [out], [(0, length, length)],
+                  sizes, offsets, indices, [np.abs(np.asarray(weights, np.float32))],
+                  threads=threads, fp64=True)
+    return out
 
 
 def patch_basis(ptype, field0, field1, s, t, fp64=False):

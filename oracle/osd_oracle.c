@@ -198,6 +198,41 @@ int orc_eval_patches_d(const float *src, const int *srcDesc, int nout, double *c
     return 1;
 }
 
+/* Magnitude of the summands, sum_j |w_j| |x_j|, per output: the natural scale of the float
+ * rounding error of a (possibly cancelling) weighted sum.  Used by tests to state tolerances
+ * for derivative outputs. */
+int orc_eval_patches_abs(const float *src, const int *srcDesc, int nout, double *const *dst,
+                         const int *dstDesc, int ncoords, const void *coords, const int *arrays,
+                         const int *patchIndices, const void *params, int nthreads) {
+    if (!src) return 0;
+    const int len = srcDesc[1], sstride = srcDesc[2];
+    if (len > MAX_LEN) return 0;
+    const float *s0 = src + srcDesc[0];
+    const orc_coord *pc = (const orc_coord *)coords;
+    const orc_param *pp = (const orc_param *)params;
+#pragma omp parallel for schedule(static, 1024) num_threads(nthreads > 0 ? nthreads : 1)
+    for (int i = 0; i < ncoords; ++i) {
+        double w[6 * 20];
+        double acc[MAX_LEN];
+        const orc_coord *c = pc + i;
+        const orc_param *p = pp + c->patchIndex;
+        int type = coord_patch_type(arrays, pp, c);
+        int n = orc_patch_basis_d(type, p->field0, p->field1, (double)c->s, (double)c->t, w);
+        const int *cvs = coord_cvs(arrays, patchIndices, c);
+        for (int k = 0; k < nout; ++k) {
+            if (!dst[k]) continue;
+            for (int e = 0; e < len; ++e) acc[e] = 0.0;
+            for (int j = 0; j < n; ++j) {
+                const float *row = s0 + (size_t)cvs[j] * sstride;
+                for (int e = 0; e < len; ++e) acc[e] += fabs((double)row[e] * w[20 * k + j]);
+            }
+            double *d = dst[k] + dstDesc[3 * k] + (size_t)i * dstDesc[3 * k + 2];
+            memcpy(d, acc, sizeof(double) * len);
+        }
+    }
+    return 1;
+}
+
 /* ---- PatchMap (far/patchMap.h:49-231, far/patchMap.cpp:89-202) ------------------------ */
 
 /* A quadtree child: set / leaf flags and an index into the node or handle list. */

@@ -53,6 +53,11 @@ int orc_eval_patches_d(const float *src, const int *srcDesc, int nout, double *c
                        const int *dstDesc, int ncoords, const void *coords, const int *arrays,
                        const int *patchIndices, const void *params, int nthreads);
 
+/* sum_j |w_j x_j| per output and element (double): the scale of float rounding error. */
+int orc_eval_patches_abs(const float *src, const int *srcDesc, int nout, double *const *dst,
+                         const int *dstDesc, int ncoords, const void *coords, const int *arrays,
+                         const int *patchIndices, const void *params, int nthreads);
+
 /* PatchMap (far/patchMap.h, far/patchMap.cpp).  params: 3 x 32-bit per patch (only
  * field0/field1 are read); arrays: 6 ints per patch array; triangular: 1 when the table's
  * varying patches have 3 CVs (tri patch layout). */

@@ -1,0 +1,150 @@
+"""EvalPatches and the device PatchMap on the GB300 through the C ABI.
+
+Fixtures cover every patch type the Osd evaluator supports: REGULAR (B-spline, with boundary
+masks on the open grid), GREGORY_BASIS end caps, LOOP (box spline, with boundary masks),
+GREGORY_TRIANGLE, and the linear QUADS / TRIANGLES of uniform tables.  PatchMap handles must
+be bit-exact with Far::PatchMap (integer work); float outputs must match Osd::CpuEvaluator
+within 1e-5 x bbox diagonal, scaled for derivatives by their magnitude relative to the cage.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import bbox_diag, dev, host, max_err, torch_cuda
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+STENCIL_FIXTURES = set(glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz")))
+FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*.npz"))) - STENCIL_FIXTURES)
+REL_TOL = 1e-5
+NAMES = ("P", "du", "dv", "duu", "duv", "dvv")
+
+
+def _table(z):
+    from opensubdiv_gb300.evaluator import GB300PatchTable
+    return GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"],
+                                  triangular=bool(z["triangular"]))
+
+
+def _tol(z, abs_k):
+    """1e-5 x bbox diagonal, scaled up when the output is a cancelling sum whose summands
+    sum_j |w_j x_j| (abs_k, from the oracle) exceed the diagonal -- second derivatives carry
+    a 4^depth factor, and float rounding error grows with the summands, not the result."""
+    diag = bbox_diag(z["positions"])
+    return REL_TOL * diag * max(1.0, float(np.max(abs_k)) / diag)
+
+
+def _abs(z, src=None, length=3, desc=(0, 3, 3)):
+    src = z["src"] if src is None else src
+    return oracle.abs_scale(src, desc, length, z["coords"], z["arrays"], z["patch_indices"],
+                            z["params"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FIXTURES, ids=os.path.basename)
+def test_device_patchmap_bit_exact(path):
+    torch = torch_cuda()
+    z = np.load(path)
+    t = _table(z)
+    n = len(z["q_face"])
+    out = torch.zeros(n * 5, dtype=torch.int32, device="cuda")
+    t.FindPatches(n, dev(z["q_face"]), dev(z["q_u"]), dev(z["q_v"]), out)
+    torch.cuda.synchronize()
+    o = host(out).reshape(n, 5)
+    assert np.array_equal(o[:, :3], z["q_handles"])
+    assert np.array_equal(o[:, 3].view(np.float32), z["q_u"])
+    assert np.array_equal(o[:, 4].view(np.float32), z["q_v"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FIXTURES, ids=os.path.basename)
+def test_eval_patches_all_outputs(path):
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
+    z = np.load(path)
+    m = z["coords"].shape[0]
+    t = _table(z)
+    src = dev(z["src"])
+    coords = dev(z["coords"])
+    outs = [torch.zeros(m * 3, device="cuda") for _ in range(6)]
+    A = _abs(z)
+    d = BD(0, 3, 3)
+    assert Ev.EvalPatchesTable(src, d, outs[0], d, m, coords, t, du=outs[1], duDesc=d,
+                               dv=outs[2], dvDesc=d, duu=outs[3], duuDesc=d, duv=outs[4],
+                               duvDesc=d, dvv=outs[5], dvvDesc=d)
+    Ev.Synchronize()
+    for k in range(6):
+        g = host(outs[k])
+        ref = z["out6"][k].ravel()
+        f64 = z["out6_fp64"][k].ravel()
+        err, tol = max_err(g, ref), _tol(z, A[k])
+        print(f"{os.path.basename(path)} {NAMES[k]}: |gpu-cpu|={err:.2e} tol={tol:.2e} "
+              f"|gpu-fp64|={max_err(g, f64):.2e} |cpu-fp64|={max_err(ref, f64):.2e}")
+        assert err <= tol, NAMES[k]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FIXTURES, ids=os.path.basename)
+def test_eval_patches_raw_api_and_partial_outputs(path):
+    """Raw-pointer API (CudaEvalPatches / ...WithDerivatives) with 1 and 3 outputs, and an
+    interleaved 8-wide source evaluated at descriptor offsets."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
+    z = np.load(path)
+    m = z["coords"].shape[0]
+    t = _table(z)
+    arrays, idx, params = (t.GetPatchArrayBuffer(), t.GetPatchIndexBuffer(),
+                           t.GetPatchParamBuffer())
+    coords = dev(z["coords"])
+    src = dev(z["src"])
+    p = torch.zeros(m * 3, device="cuda")
+    assert Ev.EvalPatches(src, BD(0, 3, 3), p, BD(0, 3, 3), m, coords, arrays, idx, params)
+    Ev.Synchronize()
+    A = _abs(z)
+    assert max_err(host(p), z["out6"][0]) <= _tol(z, A[0])
+    # 8 interleaved primvars: xyz in lanes 2..4 of a stride-8 source, outputs stride 4
+    nsrc = len(z["src"]) // 3
+    rng = np.random.default_rng(5)
+    s8 = rng.uniform(-1, 1, (nsrc, 8)).astype(np.float32)
+    s8[:, 2:5] = z["src"].reshape(-1, 3)
+    d = [torch.zeros(m * 4, device="cuda") for _ in range(3)]
+    assert Ev.EvalPatches(dev(s8.ravel()), BD(2, 3, 8), d[0], BD(1, 3, 4), m, coords, arrays,
+                          idx, params, du=d[1], duDesc=BD(0, 3, 4), dv=d[2], dvDesc=BD(1, 3, 4))
+    Ev.Synchronize()
+    o0 = host(d[0]).reshape(m, 4)[:, 1:4]
+    o1 = host(d[1]).reshape(m, 4)[:, 0:3]
+    o2 = host(d[2]).reshape(m, 4)[:, 1:4]
+    for k, o in enumerate((o0, o1, o2)):
+        assert max_err(o, z["out6"][k]) <= _tol(z, A[k]), NAMES[k]
+    # full 8-wide evaluation against the oracle
+    out8 = [torch.zeros(m * 8, device="cuda") for _ in range(6)]
+    b8 = BD(0, 8, 8)
+    assert Ev.EvalPatches(dev(s8.ravel()), b8, out8[0], b8, m, coords, arrays, idx, params,
+                          du=out8[1], duDesc=b8, dv=out8[2], dvDesc=b8, duu=out8[3],
+                          duuDesc=b8, duv=out8[4], duvDesc=b8, dvv=out8[5], dvvDesc=b8)
+    Ev.Synchronize()
+    ref8 = [np.zeros(m * 8, np.float32) for _ in range(6)]
+    oracle.eval_patches(s8.ravel(), (0, 8, 8), ref8, [(0, 8, 8)] * 6, z["coords"], z["arrays"],
+                        z["patch_indices"], z["params"])
+    A8 = _abs(z, s8.ravel(), 8, (0, 8, 8))
+    for k in range(6):
+        assert max_err(host(out8[k]), ref8[k]) <= _tol(z, A8[k]), NAMES[k]
+
+
+@pytest.mark.gpu
+def test_patchmap_misses_evaluate_to_zero():
+    """Coords with a negative array index (PatchMap misses) produce zeros."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
+    z = np.load(FIXTURES[0])
+    t = _table(z)
+    c = z["coords"][:4].copy()
+    c[1, :3] = -1
+    out = torch.full((12,), 5.0, device="cuda")
+    assert Ev.EvalPatchesTable(dev(z["src"]), BD(0, 3, 3), out, BD(0, 3, 3), 4, dev(c), t)
+    Ev.Synchronize()
+    o = host(out).reshape(4, 3)
+    assert np.all(o[1] == 0)
+    assert max_err(o[[0, 2, 3]], z["out6"][0][[0, 2, 3]]) <= _tol(z, _abs(z)[0])
