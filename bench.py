@@ -1,0 +1,412 @@
+"""Benchmark of the Osd evaluation hot path on GB300 (one JSON line on stdout).
+
+Workload (one "step" = one pass of the hot path over one batch): the plain-method torus --
+512 x 256 quads, 5% split into triangles, 2% semi-sharp creases, Catmull-Clark uniform level 3
+(8,598,400 factorized stencils, 112M entries), 8 interleaved float32 primvars -- EvalStencils
+over every level-3 point, then limit EvalStencils (P, du, dv fused) at 1M seeded locations.
+Metric: stencil evaluations per second (refined + limit points per step / step time).
+
+  value  -- tables, source and outputs resident in HBM, CUDA events on the launch stream;
+  e2e    -- through the public C-ABI with host buffers: per step the deformed control points
+            are copied from pinned host memory into the GB300 vertex buffer, both evaluations
+            run, and all outputs are copied back to pinned host memory.
+The per-step working set (1.4 GB of tables and outputs) exceeds the 129 MB L2, so no
+explicit flush is needed between steps.
+
+--impl reference times the CPU evaluator of the path on this host's cores (the oracle port
+of Osd::CpuEvaluator / OmpEvaluator; the reference library itself is not available on the
+GPU host) on the same workload, one bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0,
+                    help="bounded CPU-baseline sample length")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--nu", type=int, default=512, help="torus cage resolution (u)")
+    ap.add_argument("--nv", type=int, default=256, help="torus cage resolution (v)")
+    ap.add_argument("--n-limit", type=int, default=1_000_000, help="limit locations")
+    return ap.parse_args()
+
+
+METRIC = "stencil evals per s (EvalStencils refine L3 + limit du/dv)"
+UNIT = "stencils/s"
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_key):
+    """Per-launch DRAM bytes of the kernel from the committed ncu summary, if any."""
+    d = os.path.join(ROOT, "profiles")
+    if not os.path.isdir(d):
+        return None
+    for f in sorted(os.listdir(d)):
+        if not f.endswith(".md"):
+            continue
+        for line in open(os.path.join(d, f)):
+            m = re.match(r"\s*dram_bytes_per_launch\[(\S+)\]:\s*([0-9.eE+]+)", line)
+            if m and m.group(1) == kernel_key:
+                return float(m.group(2))
+    return None
+
+
+class NvmlClocks:
+    """Read-only NVML polling (SM clock, max clock, clock-event reasons) every 2 ms in a
+    thread, so even a short timed region gets samples.  Reasons bits per nvml.h:
+    0x4 sw_power_cap, 0x8 hw_slowdown, 0x20 sw_thermal_slowdown, 0x40 hw_thermal_slowdown."""
+
+    BITS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+            0x40: "hw_thermal_slowdown"}
+
+    def __init__(self, index=0):
+        import ctypes
+
+        self.C = ctypes
+        self.nv = ctypes.CDLL("libnvidia-ml.so.1")
+        if self.nv.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = ctypes.c_void_p()
+        if self.nv.nvmlDeviceGetHandleByIndex_v2(index, ctypes.byref(self.h)) != 0:
+            raise OSError("no NVML handle")
+        self.sm, self.reasons, self.stop = [], 0, False
+        mx = ctypes.c_uint()
+        self.nv.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx))
+        self.max = float(mx.value)
+
+    def _loop(self):
+        C = self.C
+        mhz, r = C.c_uint(), C.c_ulonglong()
+        get_r = getattr(self.nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            self.nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        while not self.stop:
+            if self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0:
+                self.sm.append(float(mhz.value))
+            if get_r(self.h, C.byref(r)) == 0:
+                self.reasons |= int(r.value)
+            time.sleep(0.002)
+
+    def __enter__(self):
+        self.t = threading.Thread(target=self._loop, daemon=True)
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop = True
+        self.t.join(timeout=2)
+
+    def summary(self):
+        return {"sm_mhz": float(np.median(self.sm)) if self.sm else None, "sm_max_mhz": self.max,
+                "reasons": sorted(n for b, n in self.BITS.items() if self.reasons & b),
+                "samples": len(self.sm), "source": "nvml"}
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle sampling during the timed region (fallback when NVML
+    cannot be loaded)."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if len(r) >= 8 and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) >= 8 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) < 8:
+                continue
+            for k, n in enumerate(names):
+                if r[4 + k].lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_rate(w, seconds, threads):
+    """Oracle port of CpuEvaluator/OmpEvaluator on the same workload for ~`seconds`."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    L = w["length"]
+    r, l = w["refine"], w["limit"]
+    out = np.zeros(len(r["sizes"]) * L, np.float32)
+    outs = [np.zeros(len(l["sizes"]) * L, np.float32) for _ in range(3)]
+    d = (0, L, L)
+    done = 0
+    t0 = time.perf_counter()
+    while True:
+        oracle.eval_stencils(w["src"], d, [out], [d], r["sizes"], r["offsets"], r["indices"],
+                             [r["weights"]], threads=threads)
+        oracle.eval_stencils(w["src"], d, outs, [d] * 3, l["sizes"], l["offsets"], l["indices"],
+                             [l["weights"], l["du_weights"], l["dv_weights"]], threads=threads)
+        done += len(r["sizes"]) + len(l["sizes"])
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            return done / el, el
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    from opensubdiv_gb300 import workloads
+
+    w = workloads.refine_and_limit_torus(args.nu, args.nv, n_limit=args.n_limit)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_rate(w, 0.0, threads)
+    rates, total = [], 0.0
+    for _ in range(args.steps):
+        r, el = cpu_rate(w, per_step, threads)
+        rates.append(r)
+        total += el
+    value = float(np.median(rates))
+    n_step = len(w["refine"]["sizes"]) + len(w["limit"]["sizes"])
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * n_step / value, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded torus cage)",
+            "config": {"workload": w["name"], "stencils_per_step": n_step},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{args.steps} steps x >= {per_step:.1f}s of full "
+                                       "refine+limit passes, OpenMP over all host threads"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world):
+    import torch
+
+    from opensubdiv_gb300 import _lib, workloads
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300StencilTable, GB300VertexBuffer)
+
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    torch.cuda.set_device(local)
+    _lib.load()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    w = workloads.refine_and_limit_torus(args.nu, args.nv, n_limit=args.n_limit)
+    L = w["length"]
+    r, lim = w["refine"], w["limit"]
+    ncv = w["cage"].num_vertices
+    n_ref, n_lim = len(r["sizes"]), len(lim["sizes"])
+    stream = torch.cuda.Stream()
+    t_ref = GB300StencilTable.Create(r["sizes"], r["offsets"], r["indices"], r["weights"])
+    t_lim = GB300StencilTable.Create(lim["sizes"], lim["offsets"], lim["indices"],
+                                     lim["weights"], lim["du_weights"], lim["dv_weights"])
+    vb = GB300VertexBuffer.Create(L, ncv)
+    vb.UpdateData(w["src"], 0, ncv)
+    src = vb.BindCudaBuffer()
+    out = torch.empty(n_ref * L, device="cuda")
+    lo = [torch.empty(n_lim * L, device="cuda") for _ in range(3)]
+    d = BD(0, L, L)
+
+    def step():
+        ok1 = Ev.EvalStencilsTable(src, d, out, d, t_ref, stream=stream)
+        ok2 = Ev.EvalStencilsTable(src, d, lo[0], d, t_lim, du=lo[1], duDesc=d, dv=lo[2],
+                                   dvDesc=d, stream=stream)
+        assert ok1 and ok2, _lib.last_error()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    # ---- device-resident timing (value) + per-launch events for the roofline ----
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    launches0 = _lib.launch_count()
+    try:
+        sampler = NvmlClocks(local)
+    except OSError:
+        sampler = ClockSampler(local)
+    with sampler as clk:
+        t_start = torch.cuda.Event(enable_timing=True)
+        t_end = torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            t_start.record(stream)
+            for k in range(args.steps):
+                ev[k][0].record(stream)
+                assert Ev.EvalStencilsTable(src, d, out, d, t_ref, stream=stream)
+                ev[k][1].record(stream)
+                assert Ev.EvalStencilsTable(src, d, lo[0], d, t_lim, du=lo[1], duDesc=d,
+                                            dv=lo[2], dvDesc=d, stream=stream)
+                ev[k][2].record(stream)
+            t_end.record(stream)
+        barrier()
+    launches = _lib.launch_count() - launches0
+    ms = t_start.elapsed_time(t_end)
+    ref_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in ev]))
+    lim_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in ev]))
+    if dist:
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    n_step = n_ref + n_lim
+    value = world * n_step * args.steps / (ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers ----
+    host_src = torch.from_numpy(w["src"].copy()).pin_memory()
+    host_out = torch.empty(n_ref * L, pin_memory=True)
+    host_lo = [torch.empty(n_lim * L, pin_memory=True) for _ in range(3)]
+    phase = np.random.default_rng(7).uniform(0, 2 * np.pi)
+    base = w["src"].reshape(ncv, L)
+
+    def e2e_step(k):
+        vb.UpdateData(host_src.numpy(), 0, ncv, stream=stream)  # pinned -> HBM
+        step()
+        with torch.cuda.stream(stream):
+            host_out.copy_(out, non_blocking=True)
+            for a, b in zip(host_lo, lo):
+                a.copy_(b, non_blocking=True)
+
+    # per-frame deformation of the control points (host side, outside the copy/eval timing)
+    host_src.numpy().reshape(ncv, L)[:, :3] = base[:, :3] * (1.0 + 0.01 * np.sin(phase))
+    for k in range(args.warmup):
+        e2e_step(k)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for k in range(args.steps):
+        e2e_step(k)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1)
+    if dist:
+        t = torch.tensor([e2e_ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_value = world * n_step * args.steps / (e2e_ms / 1e3)
+    h2d = ncv * L * 4
+    d2h = (n_ref + 3 * n_lim) * L * 4
+
+    # correctness spot check against the oracle on a slice (cheap, outside timing)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    k0, k1 = n_ref // 2, n_ref // 2 + 20000
+    refv = np.zeros(n_ref * L, np.float32)
+    oracle.eval_stencils(host_src.numpy(), (0, L, L), [refv], [(0, L, L)], r["sizes"],
+                         r["offsets"], r["indices"], [r["weights"]], k0, k1, threads=4)
+    spot = float(np.abs(host_out.numpy()[k0 * L:k1 * L] - refv[k0 * L:k1 * L]).max())
+    diag = w["cage"].bbox_diagonal()
+
+    if rank != 0:
+        return
+    peak, peak_kind = peaks()
+    b_ref = workloads.stencil_bytes(n_ref, len(r["indices"]), L, ncv)
+    b_lim = workloads.stencil_bytes(n_lim, len(lim["indices"]), L, ncv, n_weight_arrays=3,
+                                    n_outputs=3)
+    achieved = b_ref / (ref_ms / 1e3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded torus cage, stencils from the native uniform refiner)",
+        "config": {"workload": w["name"], "stencils_per_step": n_step, "refine_stencils": n_ref,
+                   "refine_nnz": int(len(r["indices"])), "limit_stencils": n_lim,
+                   "limit_nnz": int(len(lim["indices"])), "primvars": L,
+                   "l2": "per-step working set 1.4 GB > 129 MB L2 (no flush needed)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "kernel": "k_stencils_tma<1,true> (refine EvalStencils, staged)",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": b_ref, "launch_ms": ref_ms,
+                     "traffic": ncu_traffic("refine"),
+                     "limit_kernel": {"launch_ms": lim_ms, "algorithmic_bytes": b_lim,
+                                      "achieved": b_lim / (lim_ms / 1e3) / 1e9}},
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_ms / args.steps},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "accuracy": {"max_abs_err_vs_oracle_slice": spot, "bbox_diag": diag,
+                     "rel": spot / diag},
+    }
+    if not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, el = cpu_rate(w, args.cpu_seconds, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{el:.1f}s of full refine+limit passes (oracle "
+                                          "port of CpuEvaluator, OpenMP, all host threads)"}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gb300(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

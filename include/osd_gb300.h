@@ -186,6 +186,11 @@ float *GB300VertexBufferBindCudaBuffer(GB300VertexBuffer *buffer);
 int GB300VertexBufferGetNumElements(const GB300VertexBuffer *buffer);
 int GB300VertexBufferGetNumVertices(const GB300VertexBuffer *buffer);
 
+/* Reads and clears the device-side status word of the current device: GB300_OK, or
+ * GB300_ERR_DEVICE_TIMEOUT if a bounded wait inside a staged kernel gave up (the kernel then
+ * left its outputs incomplete).  Synchronises the device. */
+int GB300GetDeviceStatus(void);
+
 /* ---- kernel accounting -------------------------------------------------------------------- */
 
 /* Number of this library's kernels launched since load (for launch-count reporting). */

@@ -13,6 +13,11 @@
 
 namespace gb300 {
 
+int eval_stencils_staged(const float *src, float *const *dst, const int *strides,
+                         const float *const *w, int length, int srcStride, const int *sizes,
+                         const int *offsets, const int *indices, int start, int end,
+                         cudaStream_t s);
+
 struct StencilArgs {
     const float *src;
     float *dst[6];
@@ -140,6 +145,11 @@ int eval_stencils(const float *src, float *const *dst, const int *strides,
         last = k;
     }
     if (last < 0) return ok();
+    // staged kernel first (16-byte aligned tables); the group kernel covers everything else
+    const int staged = eval_stencils_staged(src, a.dst, a.dstStride, a.w, length, srcStride,
+                                            sizes, offsets, indices, start, end, s);
+    if (staged == GB300_OK) return check_launch(who);
+    if (staged != GB300_ERR_UNSUPPORTED) return staged;
     const int G = group_width(length);
     if (last == 0)
         launch_group<1>(a, G, s);

@@ -1,0 +1,438 @@
+// EvalStencils, staged kernel for sm_103a.
+//
+// A persistent CTA = 1 producer warp + 8 consumer warps.  The stencil range is cut into tiles
+// of TS consecutive stencils.  For each tile the producer streams the tile's slice of every
+// table array -- sizes, offsets, control indices and the 1, 3 or 6 weight arrays -- from HBM
+// into one stage of a 3-deep shared-memory ring with bulk asynchronous copies
+// (cp.async.bulk ... mbarrier::complete_tx), so the table stream runs at full memory-level
+// parallelism independently of the consumers' dependent gathers.  Consumers take one stencil
+// per thread, read its entries from shared memory, gather the source rows (float4 when the
+// layout allows) from L1/L2 and accumulate every requested output in registers; outputs are
+// written with streaming stores.
+//
+// Bulk copies need 16-byte aligned addresses and sizes: the copied window is the tile's range
+// rounded down to 4 entries at the start and the last partial 16-byte chunk is loaded with
+// plain loads by the producer lanes, so nothing outside [0, nnz) / [0, numStencils) is read.
+// A tile whose entries do not fit the stage (or whose offsets are not monotone) is processed
+// straight from global memory.  Every mbarrier wait is bounded by a %globaltimer deadline; on
+// expiry the CTA records GB300_ERR_DEVICE_TIMEOUT in g_status and leaves.
+#include "common.cuh"
+
+namespace gb300 {
+
+__device__ int g_status = 0;
+
+namespace tma {
+
+constexpr int kStages = 3;
+constexpr int kConsumers = 256;  // 8 warps
+constexpr int kThreads = kConsumers + 32;
+constexpr unsigned long long kWaitNs = 4000000000ull;  // 4 s per wait
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(uint64_t *b, int count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(b)), "r"(count));
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(b)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long now_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait: false (and g_status set) when the deadline passes.
+__device__ __forceinline__ bool mbar_wait(uint64_t *b, uint32_t parity) {
+    if (mbar_try_wait(b, parity)) return true;
+    const unsigned long long t0 = now_ns();
+    while (!mbar_try_wait(b, parity)) {
+        if (now_ns() - t0 > kWaitNs) {
+            atomicExch(&g_status, GB300_ERR_DEVICE_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes,
+                                         uint64_t *bar, uint64_t policy) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+        " [%0], [%1], %2, [%3], %4;" ::"r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
+struct Meta {
+    int s0, s1, s0a, e0a, e1, staged;
+};
+
+template <int NW>
+struct Cfg {
+    static constexpr int kCap = NW == 1 ? 4096 : NW == 3 ? 2048 : 1024;  // entries per stage
+    static constexpr int kTile = kCap / 16;                               // stencils per tile
+    static constexpr int kMeta = kTile + 8;  // sizes/offsets slots (window starts 4-aligned)
+    static constexpr size_t kStageBytes = (size_t)kCap * 4 * (1 + NW) + (size_t)kMeta * 8;
+    static constexpr size_t kSmem = kStages * kStageBytes + 256;
+};
+
+struct Args {
+    const float *src;
+    float *dst[6];
+    const float *w[6];  // compacted: the NW weight arrays in output order
+    int dstStride[6];
+    int outOf[6];       // weight array k feeds output outOf[k]
+    const int *sizes;
+    const int *offsets;
+    const int *indices;
+    int length, srcStride, start, end, numTiles;
+    int vecSrc, vecDst[6];
+};
+
+template <int NW>
+__device__ __forceinline__ void stage_ptrs(char *base, int stage, int **idx, float **w,
+                                           int **sz, int **of) {
+    char *p = base + (size_t)stage * Cfg<NW>::kStageBytes;
+    *idx = (int *)p;
+    p += (size_t)Cfg<NW>::kCap * 4;
+    *w = (float *)p;
+    p += (size_t)Cfg<NW>::kCap * 4 * NW;
+    *sz = (int *)p;
+    p += (size_t)Cfg<NW>::kMeta * 4;
+    *of = (int *)p;
+}
+
+// Elements [c0, c0 + 8) of source row `id` (zeros past the primvar length): one 256-bit load
+// for 32-byte aligned rows, two 128-bit loads for 16-byte aligned rows, else scalar loads.
+template <int VW>
+__device__ __forceinline__ void gather_row(const Args &a, int id, int c0, uint64_t pol_src,
+                                           float (&x)[8]) {
+    const float *row = a.src + (size_t)id * a.srcStride + c0;
+    if (VW == 8) {
+        asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+            : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(x[3]), "=f"(x[4]), "=f"(x[5]),
+              "=f"(x[6]), "=f"(x[7])
+            : "l"(row));
+    } else if (VW == 4) {
+        const float4 *r4 = reinterpret_cast<const float4 *>(row);
+        const float4 v0 = __ldg(r4);
+        x[0] = v0.x; x[1] = v0.y; x[2] = v0.z; x[3] = v0.w;
+        if (c0 + 4 < a.length) {
+            const float4 v1 = __ldg(r4 + 1);
+            x[4] = v1.x; x[5] = v1.y; x[6] = v1.z; x[7] = v1.w;
+        } else {
+            x[4] = x[5] = x[6] = x[7] = 0.0f;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = (c0 + c < a.length) ? ld_src(row + c, pol_src) : 0.0f;
+    }
+}
+
+template <int NW>
+__device__ __forceinline__ void fma_row(const float (&wk)[NW], const float (&x)[8],
+                                        float (&acc)[NW][8]) {
+#pragma unroll
+    for (int k = 0; k < NW; ++k)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) acc[k][c] = fmaf(wk[k], x[c], acc[k][c]);
+}
+
+// One stencil, all requested outputs, elements [c0, c0 + 8) of the primvar; entries come from
+// shared memory (lidx/lw at local offset o) or straight from global memory (when lidx null).
+template <int NW, int VW>
+__device__ __forceinline__ void eval_one(const Args &a, int i, int n, const int *lidx,
+                                         const float *lw, int lstride, int o, uint64_t pol_src,
+                                         uint64_t pol_stream) {
+    for (int c0 = 0; c0 < a.length; c0 += 8) {
+        float acc[NW][8];
+#pragma unroll
+        for (int k = 0; k < NW; ++k)
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[k][c] = 0.0f;
+        if (lidx) {
+            // entries from shared memory: scalar up to a 16-byte boundary, then 4 entries per
+            // 128-bit shared load (four independent row gathers in flight), then the tail
+            int j = 0;
+            for (; j < n && ((o + j) & 3); ++j) {
+                float wk[NW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = lw[k * lstride + o + j];
+                float x[8];
+                gather_row<VW>(a, lidx[o + j], c0, pol_src, x);
+                fma_row<NW>(wk, x, acc);
+            }
+            for (; j + 4 <= n; j += 4) {
+                const int4 id4 = *reinterpret_cast<const int4 *>(lidx + o + j);
+                float4 w4[NW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k)
+                    w4[k] = *reinterpret_cast<const float4 *>(lw + k * lstride + o + j);
+                float x0[8], x1[8], x2[8], x3[8];
+                gather_row<VW>(a, id4.x, c0, pol_src, x0);
+                gather_row<VW>(a, id4.y, c0, pol_src, x1);
+                gather_row<VW>(a, id4.z, c0, pol_src, x2);
+                gather_row<VW>(a, id4.w, c0, pol_src, x3);
+                float wk[NW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = w4[k].x;
+                fma_row<NW>(wk, x0, acc);
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = w4[k].y;
+                fma_row<NW>(wk, x1, acc);
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = w4[k].z;
+                fma_row<NW>(wk, x2, acc);
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = w4[k].w;
+                fma_row<NW>(wk, x3, acc);
+            }
+            for (; j < n; ++j) {
+                float wk[NW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = lw[k * lstride + o + j];
+                float x[8];
+                gather_row<VW>(a, lidx[o + j], c0, pol_src, x);
+                fma_row<NW>(wk, x, acc);
+            }
+        } else {
+            for (int j = 0; j < n; ++j) {
+                float wk[NW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k) wk[k] = ld_stream(a.w[k] + o + j, pol_stream);
+                float x[8];
+                gather_row<VW>(a, ld_stream(a.indices + o + j, pol_stream), c0, pol_src, x);
+                fma_row<NW>(wk, x, acc);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < NW; ++k) {
+            float *d = a.dst[a.outOf[k]] + (size_t)i * a.dstStride[a.outOf[k]] + c0;
+            const int rem = a.length - c0;
+            if (a.vecDst[a.outOf[k]] == 8 && rem >= 8) {
+                asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
+                             "f"(acc[k][0]), "f"(acc[k][1]), "f"(acc[k][2]), "f"(acc[k][3]),
+                             "f"(acc[k][4]), "f"(acc[k][5]), "f"(acc[k][6]), "f"(acc[k][7])
+                             : "memory");
+            } else if (a.vecDst[a.outOf[k]] && rem >= 8) {
+                asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d),
+                             "f"(acc[k][0]), "f"(acc[k][1]), "f"(acc[k][2]), "f"(acc[k][3])
+                             : "memory");
+                asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d + 4),
+                             "f"(acc[k][4]), "f"(acc[k][5]), "f"(acc[k][6]), "f"(acc[k][7])
+                             : "memory");
+            } else {
+#pragma unroll
+                for (int c = 0; c < 8; ++c)
+                    if (c < rem) st_stream(d + c, acc[k][c]);
+            }
+        }
+    }
+}
+
+template <int NW, int VW>
+__global__ void __launch_bounds__(kThreads, 1) k_stencils_tma(const Args a) {
+    extern __shared__ __align__(128) char smem[];
+    using C = Cfg<NW>;
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+    __shared__ Meta meta[kStages];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            mbar_init(&full[s], 32);
+            mbar_init(&empty[s], kConsumers / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const uint64_t pol_stream = l2_evict_first(), pol_src = l2_evict_last();
+
+    if (warp == kConsumers / 32) {
+        // ---------------- producer warp ----------------
+        int it = 0;
+        for (int t = blockIdx.x; t < a.numTiles; t += gridDim.x, ++it) {
+            const int stage = it % kStages;
+            const uint32_t use = (uint32_t)(it / kStages);
+            if (use > 0 && !mbar_wait(&empty[stage], (use - 1) & 1)) return;
+            int *sidx, *ssz, *sof;
+            float *sw;
+            stage_ptrs<NW>(smem, stage, &sidx, &sw, &ssz, &sof);
+            const int s0 = a.start + t * C::kTile;
+            const int s1 = min(s0 + C::kTile, a.end);
+            int e0 = 0, e1 = 0;
+            if (lane == 0) {
+                e0 = __ldg(a.offsets + s0);
+                e1 = __ldg(a.offsets + s1 - 1) + __ldg(a.sizes + s1 - 1);
+            }
+            e0 = __shfl_sync(0xffffffffu, e0, 0);
+            e1 = __shfl_sync(0xffffffffu, e1, 0);
+            const int s0a = s0 & ~3, s1t = s1 & ~3;
+            const int e0a = e0 & ~3, e1t = e1 & ~3;
+            const bool staged = e1 >= e0 && (e1 - e0a) <= C::kCap;
+            if (lane == 0) meta[stage] = Meta{s0, s1, s0a, e0a, e1, staged ? 1 : 0};
+            uint32_t bytes = 0;
+            if (s1t > s0a) bytes += (uint32_t)(s1t - s0a) * 8;
+            if (staged && e1t > e0a) bytes += (uint32_t)(e1t - e0a) * 4 * (1 + NW);
+            if (lane == 0) {
+                mbar_arrive_expect_tx(&full[stage], bytes);
+                if (s1t > s0a) {
+                    bulk_g2s(ssz, a.sizes + s0a, (uint32_t)(s1t - s0a) * 4, &full[stage], pol_stream);
+                    bulk_g2s(sof, a.offsets + s0a, (uint32_t)(s1t - s0a) * 4, &full[stage], pol_stream);
+                }
+                if (staged && e1t > e0a) {
+                    const uint32_t nb = (uint32_t)(e1t - e0a) * 4;
+                    bulk_g2s(sidx, a.indices + e0a, nb, &full[stage], pol_stream);
+#pragma unroll
+                    for (int k = 0; k < NW; ++k)
+                        bulk_g2s(sw + (size_t)k * C::kCap, a.w[k] + e0a, nb, &full[stage], pol_stream);
+                }
+            }
+            // ragged tails (fewer than 4 entries each) with plain loads
+            const int st0 = max(s1t, s0a);
+            if (lane < s1 - st0) {
+                ssz[st0 - s0a + lane] = __ldg(a.sizes + st0 + lane);
+                sof[st0 - s0a + lane] = __ldg(a.offsets + st0 + lane);
+            }
+            if (staged) {
+                const int et0 = max(e1t, e0a);
+                if (lane < e1 - et0) {
+                    sidx[et0 - e0a + lane] = __ldg(a.indices + et0 + lane);
+#pragma unroll
+                    for (int k = 0; k < NW; ++k)
+                        sw[(size_t)k * C::kCap + et0 - e0a + lane] = __ldg(a.w[k] + et0 + lane);
+                }
+            }
+            __syncwarp();
+            if (lane != 0) mbar_arrive(&full[stage]);
+        }
+        return;
+    }
+
+    // ---------------- consumer warps ----------------
+    int it = 0;
+    for (int t = blockIdx.x; t < a.numTiles; t += gridDim.x, ++it) {
+        const int stage = it % kStages;
+        const uint32_t use = (uint32_t)(it / kStages);
+        if (!mbar_wait(&full[stage], use & 1)) return;
+        int *sidx, *ssz, *sof;
+        float *sw;
+        stage_ptrs<NW>(smem, stage, &sidx, &sw, &ssz, &sof);
+        const Meta m = meta[stage];
+        for (int i = m.s0 + (int)threadIdx.x; i < m.s1; i += kConsumers) {
+            const int n = ssz[i - m.s0a];
+            const int o = sof[i - m.s0a];
+            if (m.staged && o >= m.e0a && o + n <= m.e1)
+                eval_one<NW, VW>(a, i, n, sidx, sw, C::kCap, o - m.e0a, pol_src, pol_stream);
+            else
+                eval_one<NW, VW>(a, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[stage]);
+    }
+}
+
+template <int NW, int VW>
+static int launch(const Args &a, cudaStream_t s) {
+    using C = Cfg<NW>;
+    auto kern = k_stencils_tma<NW, VW>;
+    static bool attr = false;  // per-process: the attribute is per function
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)C::kSmem);
+        if (e != cudaSuccess) return check_cuda(e, "stencils (staged): smem attribute");
+        attr = true;
+    }
+    static int perSm = 0;
+    if (perSm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kThreads, C::kSmem) !=
+                cudaSuccess || perSm < 1)
+            perSm = 1;
+    }
+    Args b = a;
+    b.numTiles = (a.end - a.start + C::kTile - 1) / C::kTile;
+    const int grid = min(b.numTiles, num_sms() * perSm);
+    kern<<<grid, kThreads, C::kSmem, s>>>(b);
+    count_launch();
+    return GB300_OK;
+}
+
+}  // namespace tma
+
+// Staged path; returns GB300_ERR_UNSUPPORTED when the arguments do not meet its alignment
+// preconditions (the caller then uses the group kernel).
+int eval_stencils_staged(const float *src, float *const *dst, const int *strides,
+                         const float *const *w, int length, int srcStride, const int *sizes,
+                         const int *offsets, const int *indices, int start, int end,
+                         cudaStream_t s) {
+    auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+    auto al32 = [](const void *p) { return ((uintptr_t)p & 31) == 0; };
+    if (!al16(sizes) || !al16(offsets) || !al16(indices)) return GB300_ERR_UNSUPPORTED;
+    tma::Args a{};
+    a.src = src;
+    a.sizes = sizes;
+    a.offsets = offsets;
+    a.indices = indices;
+    a.length = length;
+    a.srcStride = srcStride;
+    a.start = start;
+    a.end = end;
+    int nw = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (!dst[k]) continue;
+        if (!al16(w[k])) return GB300_ERR_UNSUPPORTED;
+        a.dst[k] = dst[k];
+        a.dstStride[k] = strides[k];
+        a.vecDst[k] = (al32(dst[k]) && strides[k] % 8 == 0) ? 8
+                      : (al16(dst[k]) && strides[k] % 4 == 0) ? 4 : 0;
+        a.w[nw] = w[k];
+        a.outOf[nw] = k;
+        ++nw;
+    }
+    // source row loads: 256-bit when rows are 32-byte aligned, 128-bit when 16-byte aligned
+    a.vecSrc = (al32(src) && srcStride % 8 == 0) ? 8 : (al16(src) && srcStride % 4 == 0) ? 4 : 1;
+    switch (nw * 10 + a.vecSrc) {
+        case 18: return tma::launch<1, 8>(a, s);
+        case 14: return tma::launch<1, 4>(a, s);
+        case 11: return tma::launch<1, 1>(a, s);
+        case 38: return tma::launch<3, 8>(a, s);
+        case 34: return tma::launch<3, 4>(a, s);
+        case 31: return tma::launch<3, 1>(a, s);
+        case 68: return tma::launch<6, 8>(a, s);
+        case 64: return tma::launch<6, 4>(a, s);
+        case 61: return tma::launch<6, 1>(a, s);
+        default: return GB300_ERR_UNSUPPORTED;  // 2, 4 or 5 outputs: group kernel
+    }
+}
+
+}  // namespace gb300
+
+extern "C" int GB300GetDeviceStatus(void) {
+    using namespace gb300;
+    int v = 0;
+    int st = check_cuda(cudaDeviceSynchronize(), "GB300GetDeviceStatus");
+    if (st != GB300_OK) return st;
+    st = check_cuda(cudaMemcpyFromSymbol(&v, g_status, sizeof(int)), "GB300GetDeviceStatus");
+    if (st != GB300_OK) return st;
+    if (v != 0) {
+        const int zero = 0;
+        cudaMemcpyToSymbol(g_status, &zero, sizeof(int));
+        return fail(v, "a staged kernel's bounded wait expired");
+    }
+    return ok();
+}

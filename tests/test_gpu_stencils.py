@@ -182,6 +182,49 @@ def test_random_tables_all_lengths_and_pole_sized_stencils(length):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("layout", ["reversed_blocks", "gapped", "misaligned_views"])
+def test_non_factory_table_layouts(layout):
+    """Tables the factories never produce still evaluate correctly: stencil entry blocks
+    stored in reverse order (offsets not monotone), gaps between blocks, and table pointers
+    that are not 16-byte aligned (sub-array views)."""
+    torch = torch_cuda()
+    Ev, BD = _ev()
+    z = np.load(FIXTURES[0])
+    sizes, offsets, idx, w = z["sizes"], z["offsets"], z["indices"], z["weights"]
+    n = len(sizes)
+    if layout == "reversed_blocks":
+        order = np.arange(n)[::-1]
+        new_off = np.zeros(n, np.int32)
+        new_off[order] = np.concatenate([[0], np.cumsum(sizes[order])[:-1]]).astype(np.int32)
+        gather = np.concatenate([np.arange(offsets[i], offsets[i] + sizes[i]) for i in order])
+        offsets, idx, w = new_off, idx[gather], w[gather]
+    elif layout == "gapped":
+        gap = 3
+        new_off = (offsets + gap * np.arange(n)).astype(np.int32)
+        idx2 = np.zeros(len(idx) + gap * n, np.int32)
+        w2 = np.full(len(idx) + gap * n, np.nan, np.float32)  # gap entries must never be read
+        for i in range(n):
+            idx2[new_off[i]:new_off[i] + sizes[i]] = idx[offsets[i]:offsets[i] + sizes[i]]
+            w2[new_off[i]:new_off[i] + sizes[i]] = w[offsets[i]:offsets[i] + sizes[i]]
+        offsets, idx, w = new_off, idx2, w2
+    tbl = [dev(a) for a in (sizes, offsets, idx, w)]
+    if layout == "misaligned_views":
+        # one extra leading element, then a view starting at element 1 (4-byte aligned only)
+        tbl = [dev(np.concatenate([a[:1], a]))[1:] for a in (sizes, offsets, idx, w)]
+    out = torch.zeros(n * 3, device="cuda")
+    assert Ev.EvalStencils(dev(z["positions"].ravel()), BD(0, 3, 3), out, BD(0, 3, 3), *tbl,
+                           0, n)
+    Ev.Synchronize()
+    assert max_err(host(out), z["out3"]) <= REL_TOL * bbox_diag(z["positions"])
+
+
+@pytest.mark.gpu
+def test_device_status_word_is_clear_after_runs():
+    from opensubdiv_gb300 import _lib
+    assert _lib.load().GB300GetDeviceStatus() == 0
+
+
+@pytest.mark.gpu
 def test_invalid_requests_return_false_and_empty_ranges_are_noops():
     torch = torch_cuda()
     Ev, BD = _ev()
