@@ -5,7 +5,9 @@
 #include "common.cuh"
 #include "patchmap.h"
 
+#include <algorithm>
 #include <new>
+#include <thread>
 #include <vector>
 
 using namespace gb300;
@@ -34,6 +36,56 @@ bool upload(void **dptr, const void *host, size_t bytes, cudaStream_t s, const c
 void release(void *&p) {
     if (p) cudaFree(p);
     p = nullptr;
+}
+
+// Device layout of an owned stencil table: the entries of every stencil are stored in
+// ascending control-vertex order (weights permuted alongside).  The stencil -- a weighted
+// sum -- is unchanged; neighbouring stencils then touch the same source rows at the same
+// entry position, which cuts the distinct rows per warp-wide gather.  Applied only when the
+// stencils' entry ranges are disjoint and inside [0, nnz); returns false otherwise.
+bool sort_entries(int numStencils, int64_t nnz, const int *sizes, const int *offsets,
+                  const int *indices, const float *const *w, std::vector<int> &idxOut,
+                  std::vector<std::vector<float>> &wOut) {
+    int64_t prevEnd = 0;
+    for (int i = 0; i < numStencils; ++i) {
+        if (sizes[i] < 0 || offsets[i] < prevEnd || (int64_t)offsets[i] + sizes[i] > nnz)
+            return false;
+        prevEnd = (int64_t)offsets[i] + sizes[i];
+    }
+    idxOut.assign(indices, indices + nnz);
+    wOut.assign(9, {});
+    for (int k = 0; k < 6; ++k)
+        if (w[k]) wOut[k].assign(w[k], w[k] + nnz);
+    const int nth = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nth; ++t) {
+        pool.emplace_back([&, t]() {
+            const int lo = (int)((int64_t)numStencils * t / nth);
+            const int hi = (int)((int64_t)numStencils * (t + 1) / nth);
+            for (int i = lo; i < hi; ++i) {
+                const int o = offsets[i], n = sizes[i];
+                // insertion sort of (index, weights) pairs by index: stencils are short
+                for (int a = o + 1; a < o + n; ++a) {
+                    const int key = idxOut[a];
+                    float wk[6] = {0, 0, 0, 0, 0, 0};
+                    for (int k = 0; k < 6; ++k)
+                        if (!wOut[k].empty()) wk[k] = wOut[k][a];
+                    int b = a - 1;
+                    while (b >= o && idxOut[b] > key) {
+                        idxOut[b + 1] = idxOut[b];
+                        for (int k = 0; k < 6; ++k)
+                            if (!wOut[k].empty()) wOut[k][b + 1] = wOut[k][b];
+                        --b;
+                    }
+                    idxOut[b + 1] = key;
+                    for (int k = 0; k < 6; ++k)
+                        if (!wOut[k].empty()) wOut[k][b + 1] = wk[k];
+                }
+            }
+        });
+    }
+    for (auto &th : pool) th.join();
+    return true;
 }
 
 }  // namespace
@@ -90,8 +142,16 @@ GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const i
     }
     t->numStencils = numStencils;
     t->nnz = nnz;
-    const void *host[9] = {sizes, offsets, indices, weights, duWeights,
-                           dvWeights, duuWeights, duvWeights, dvvWeights};
+    const float *wsrc[6] = {weights, duWeights, dvWeights, duuWeights, duvWeights, dvvWeights};
+    std::vector<int> sortedIdx;
+    std::vector<std::vector<float>> sortedW;
+    if (sort_entries(numStencils, nnz, sizes, offsets, indices, wsrc, sortedIdx, sortedW)) {
+        indices = sortedIdx.data();
+        for (int k = 0; k < 6; ++k)
+            if (wsrc[k]) wsrc[k] = sortedW[k].data();
+    }
+    const void *host[9] = {sizes, offsets, indices, wsrc[0], wsrc[1],
+                           wsrc[2], wsrc[3], wsrc[4], wsrc[5]};
     const size_t bytes[9] = {(size_t)numStencils * 4, (size_t)numStencils * 4,
                              (size_t)nnz * 4, (size_t)nnz * 4, (size_t)nnz * 4,
                              (size_t)nnz * 4, (size_t)nnz * 4, (size_t)nnz * 4,

@@ -167,49 +167,30 @@ __device__ __forceinline__ void eval_one(const Args &a, int i, int n, const int 
 #pragma unroll
             for (int c = 0; c < 8; ++c) acc[k][c] = 0.0f;
         if (lidx) {
-            // entries from shared memory: scalar up to a 16-byte boundary, then 4 entries per
-            // 128-bit shared load (four independent row gathers in flight), then the tail
-            int j = 0;
-            for (; j < n && ((o + j) & 3); ++j) {
-                float wk[NW];
-#pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = lw[k * lstride + o + j];
-                float x[8];
-                gather_row<VW>(a, lidx[o + j], c0, pol_src, x);
-                fma_row<NW>(wk, x, acc);
-            }
-            for (; j + 4 <= n; j += 4) {
-                const int4 id4 = *reinterpret_cast<const int4 *>(lidx + o + j);
+            // entries from shared memory in aligned chunks of 4 (one 128-bit shared load per
+            // array and chunk); entries of the chunk outside [o, o + n) are skipped, so the
+            // row gathers stay exact while every thread runs the same simple loop
+            const int end = o + n;
+            for (int q = o & ~3; q < end; q += 4) {
+                const int4 id4 = *reinterpret_cast<const int4 *>(lidx + q);
                 float4 w4[NW];
 #pragma unroll
                 for (int k = 0; k < NW; ++k)
-                    w4[k] = *reinterpret_cast<const float4 *>(lw + k * lstride + o + j);
-                float x0[8], x1[8], x2[8], x3[8];
-                gather_row<VW>(a, id4.x, c0, pol_src, x0);
-                gather_row<VW>(a, id4.y, c0, pol_src, x1);
-                gather_row<VW>(a, id4.z, c0, pol_src, x2);
-                gather_row<VW>(a, id4.w, c0, pol_src, x3);
-                float wk[NW];
+                    w4[k] = *reinterpret_cast<const float4 *>(lw + k * lstride + q);
+                const int ids[4] = {id4.x, id4.y, id4.z, id4.w};
+                float x[4][8];
 #pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = w4[k].x;
-                fma_row<NW>(wk, x0, acc);
+                for (int m = 0; m < 4; ++m)
+                    if (q + m >= o && q + m < end) gather_row<VW>(a, ids[m], c0, pol_src, x[m]);
 #pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = w4[k].y;
-                fma_row<NW>(wk, x1, acc);
+                for (int m = 0; m < 4; ++m) {
+                    if (q + m < o || q + m >= end) continue;
+                    float wk[NW];
 #pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = w4[k].z;
-                fma_row<NW>(wk, x2, acc);
-#pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = w4[k].w;
-                fma_row<NW>(wk, x3, acc);
-            }
-            for (; j < n; ++j) {
-                float wk[NW];
-#pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = lw[k * lstride + o + j];
-                float x[8];
-                gather_row<VW>(a, lidx[o + j], c0, pol_src, x);
-                fma_row<NW>(wk, x, acc);
+                    for (int k = 0; k < NW; ++k)
+                        wk[k] = m == 0 ? w4[k].x : m == 1 ? w4[k].y : m == 2 ? w4[k].z : w4[k].w;
+                    fma_row<NW>(wk, x[m], acc);
+                }
             }
         } else {
             for (int j = 0; j < n; ++j) {
@@ -247,7 +228,7 @@ __device__ __forceinline__ void eval_one(const Args &a, int i, int n, const int 
 }
 
 template <int NW, int VW>
-__global__ void __launch_bounds__(kThreads, 1) k_stencils_tma(const Args a) {
+__global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(const Args a) {
     extern __shared__ __align__(128) char smem[];
     using C = Cfg<NW>;
     __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
