@@ -46,7 +46,78 @@ def parse():
     ap.add_argument("--nu", type=int, default=512, help="torus cage resolution (u)")
     ap.add_argument("--nv", type=int, default=256, help="torus cage resolution (v)")
     ap.add_argument("--n-limit", type=int, default=1_000_000, help="limit locations")
+    ap.add_argument("--no-patches", action="store_true", help="skip the EvalPatches section")
+    ap.add_argument("--patch-points", type=int, default=4_000_000)
     return ap.parse_args()
+
+
+def bench_patches(args, stream, peak):
+    """Secondary measurement: device PatchMap lookup + EvalPatches (P and all five
+    derivatives) at 4M uniform points on a table of the 512 x 256 torus's adaptive level-4
+    size (see workloads.eval_patches_torus)."""
+    import torch
+
+    from opensubdiv_gb300 import workloads
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300PatchTable)
+
+    w = workloads.eval_patches_torus(args.patch_points)
+    n = len(w["face"])
+    table = GB300PatchTable.Create(w["arrays"], w["indices"], w["params"], w["triangular"])
+    src = torch.from_numpy(w["src"]).cuda()
+    face = torch.from_numpy(w["face"]).cuda()
+    u = torch.from_numpy(w["u"]).cuda()
+    v = torch.from_numpy(w["v"]).cuda()
+    coords = torch.empty(n * 5, dtype=torch.int32, device="cuda")
+    outs = [torch.empty(n * 3, device="cuda") for _ in range(6)]
+    d = BD(0, 3, 3)
+
+    def step(ev=None):
+        if ev:
+            ev[0].record(stream)
+        table.FindPatches(n, face, u, v, coords, stream=stream)
+        if ev:
+            ev[1].record(stream)
+        ok = Ev.EvalPatchesTable(src, d, outs[0], d, n, coords, table, du=outs[1], duDesc=d,
+                                 dv=outs[2], dvDesc=d, duu=outs[3], duuDesc=d, duv=outs[4],
+                                 duvDesc=d, dvv=outs[5], dvvDesc=d, stream=stream)
+        assert ok
+        if ev:
+            ev[2].record(stream)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3))
+           for _ in range(args.steps)]
+    with torch.cuda.stream(stream):
+        for k in range(args.steps):
+            step(evs[k])
+    torch.cuda.synchronize()
+    find_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+    eval_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+    c = coords.view(n, 5)[:, 1].cpu().numpy()
+    touched = int(len(np.unique(c[c >= 0])))
+    cvs = float(np.average(w["arrays"][:, 4], weights=w["arrays"][:, 2]))
+    b = workloads.patch_bytes(n, 3, 6, len(w["src"]) // 3, touched, cvs)
+    # spot check against the oracle on a slice (outside timing)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    k = 20000
+    ch = coords[: k * 5].view(k, 5).cpu().numpy()
+    ref = [np.zeros(k * 3, np.float32) for _ in range(6)]
+    oracle.eval_patches(w["src"], (0, 3, 3), ref, [(0, 3, 3)] * 6, ch, w["arrays"],
+                        w["indices"], w["params"], threads=8)
+    err_p = float(np.abs(outs[0][: k * 3].cpu().numpy() - ref[0]).max())
+    return {"workload": w["name"], "points": n, "patch_evals_per_s": n / ((find_ms + eval_ms) / 1e3),
+            "find_patches_ms": find_ms, "eval_patches_ms": eval_ms, "outputs": 6,
+            "patches_touched": touched,
+            "roofline": {"bound": "hbm", "kernel": "k_eval_patches (P + 5 derivatives)",
+                         "algorithmic_bytes": b, "achieved": b / (eval_ms / 1e3) / 1e9,
+                         "peak": peak, "unit": "GB/s",
+                         "frac": b / (eval_ms / 1e3) / 1e9 / peak,
+                         "traffic": ncu_traffic("patches")},
+            "max_abs_err_P_vs_oracle_slice": err_p}
 
 
 METRIC = "stencil evals per s (EvalStencils refine L3 + limit du/dv)"
@@ -373,7 +444,7 @@ def run_gb300(args, rank, world):
                    "limit_nnz": int(len(lim["indices"])), "primvars": L,
                    "l2": "per-step working set 1.4 GB > 129 MB L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "k_stencils_tma<1,true> (refine EvalStencils, staged)",
+        "roofline": {"bound": "hbm", "kernel": "k_stencils_tma<1,8> (refine EvalStencils, staged)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": b_ref, "launch_ms": ref_ms,
@@ -387,6 +458,8 @@ def run_gb300(args, rank, world):
         "accuracy": {"max_abs_err_vs_oracle_slice": spot, "bbox_diag": diag,
                      "rel": spot / diag},
     }
+    if not args.no_patches:
+        line["eval_patches"] = bench_patches(args, stream, peak)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, el = cpu_rate(w, args.cpu_seconds, threads)

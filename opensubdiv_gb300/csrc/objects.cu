@@ -94,13 +94,73 @@ struct GB300StencilTable {
     int numStencils = 0;
     int64_t nnz = 0;
     void *buf[9] = {nullptr};  // sizes, offsets, indices, w, du, dv, duu, duv, dvv
+    // Evaluation order for tables whose consecutive stencils are scattered over the control
+    // points (limit stencils at random locations): the same stencils sorted by their lowest
+    // control index, each writing back to its original destination row (outRow).
+    void *ebuf[9] = {nullptr};
+    void *outRow = nullptr;
     ~GB300StencilTable() {
         for (auto &p : buf) release(p);
+        for (auto &p : ebuf) release(p);
+        release(outRow);
     }
 };
 
+namespace {
+
+// Builds the locality-sorted evaluation layout when consecutive stencils' lowest control
+// indices jump by more than 1% of the index range on average.  Entries must already be
+// sorted per stencil (index[offset] is the lowest).  Returns false when not worthwhile.
+bool evaluation_order(int n, int64_t nnz, const int *sizes, const int *offsets,
+                      const int *indices, const float *const *w, std::vector<int> &order,
+                      std::vector<int> &esz,
+                      std::vector<int> &eoff, std::vector<int> &eidx,
+                      std::vector<std::vector<float>> &ew) {
+    if (n < 4096) return false;
+    int maxIdx = 1;
+    double jump = 0.0;
+    int prev = -1;
+    for (int i = 0; i < n; ++i) {
+        const int key = sizes[i] > 0 ? indices[offsets[i]] : 0;
+        maxIdx = std::max(maxIdx, key);
+        if (prev >= 0) jump += std::abs(key - prev);
+        prev = key;
+    }
+    if (jump / (n - 1) < 0.01 * maxIdx) return false;
+    order.resize(n);
+    for (int i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+        const int ka = sizes[a] > 0 ? indices[offsets[a]] : -1;
+        const int kb = sizes[b] > 0 ? indices[offsets[b]] : -1;
+        return ka < kb;
+    });
+    esz.resize(n);
+    eoff.resize(n);
+    int64_t z = 0;
+    for (int j = 0; j < n; ++j) {
+        esz[j] = sizes[order[j]];
+        eoff[j] = (int)z;
+        z += esz[j];
+    }
+    // arrays keep the original entry count (a table with gaps packs into fewer entries)
+    eidx.assign(std::max<int64_t>(z, nnz), 0);
+    ew.assign(6, {});
+    for (int k = 0; k < 6; ++k)
+        if (w[k]) ew[k].assign(std::max<int64_t>(z, nnz), 0.0f);
+    for (int j = 0; j < n; ++j) {
+        const int o = offsets[order[j]];
+        std::copy(indices + o, indices + o + esz[j], eidx.begin() + eoff[j]);
+        for (int k = 0; k < 6; ++k)
+            if (w[k]) std::copy(w[k] + o, w[k] + o + esz[j], ew[k].begin() + eoff[j]);
+    }
+    return true;
+}
+
+}  // namespace
+
 struct GB300PatchTable {
     int numArrays = 0, numPatches = 0;
+    int quadFamily = 0;  // all arrays REGULAR / GREGORY_BASIS / QUADS
     int64_t numIndices = 0;
     void *arrays = nullptr, *indices = nullptr, *params = nullptr;
     PatchMapDevice map;
@@ -162,6 +222,27 @@ GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const i
             return nullptr;
         }
     }
+    std::vector<int> order, esz, eoff, eidx;
+    std::vector<std::vector<float>> ew;
+    if (!sortedIdx.empty() &&
+        evaluation_order(numStencils, nnz, sizes, offsets, indices, wsrc, order, esz, eoff, eidx,
+                         ew)) {
+        const void *eh[9] = {esz.data(), eoff.data(), eidx.data(), nullptr, nullptr,
+                             nullptr, nullptr, nullptr, nullptr};
+        for (int k = 0; k < 6; ++k)
+            if (wsrc[k]) eh[3 + k] = ew[k].data();
+        for (int k = 0; k < 9; ++k) {
+            if (!upload(&t->ebuf[k], eh[k], bytes[k], s, "GB300StencilTableCreate")) {
+                delete t;
+                return nullptr;
+            }
+        }
+        if (!upload(&t->outRow, order.data(), (size_t)numStencils * 4, s,
+                    "GB300StencilTableCreate")) {
+            delete t;
+            return nullptr;
+        }
+    }
     if (check_cuda(cudaStreamSynchronize(s), "GB300StencilTableCreate") != GB300_OK) {
         delete t;
         return nullptr;
@@ -196,6 +277,15 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
                         "GB300StencilTableEval: output %d requested but the table has no such "
                         "weights",
                         k);
+    }
+    if (t->outRow) {
+        const float *ew[6];
+        for (int k = 0; k < 6; ++k) ew[k] = (const float *)t->ebuf[3 + k];
+        const int r = eval_stencils(src, d, st, ew, length, srcStride, (const int *)t->ebuf[0],
+                                    (const int *)t->ebuf[1], (const int *)t->ebuf[2], 0,
+                                    t->numStencils, as_stream(stream), "GB300StencilTableEval",
+                                    (const int *)t->outRow);
+        if (r != GB300_ERR_UNSUPPORTED) return r;
     }
     return eval_stencils(src, d, st, w, length, srcStride, (const int *)t->buf[0],
                          (const int *)t->buf[1], (const int *)t->buf[2], 0, t->numStencils,
@@ -245,6 +335,14 @@ GB300PatchTable *GB300PatchTableCreate(int numArrays, const void *patchArrays,
     t->numArrays = numArrays;
     t->numPatches = numPatches;
     t->numIndices = numIndices;
+    t->quadFamily = numArrays > 0;
+    for (int a = 0; a < numArrays; ++a)
+        for (int k = 0; k < 2; ++k) {
+            const int type = arr[6 * a + k];
+            if (type != GB300_PATCH_REGULAR && type != GB300_PATCH_GREGORY_BASIS &&
+                type != GB300_PATCH_QUADS)
+                t->quadFamily = 0;
+        }
     const char *w = "GB300PatchTableCreate";
     if (!upload(&t->arrays, patchArrays, (size_t)numArrays * 24, s, w) ||
         !upload(&t->indices, patchIndices, (size_t)numIndices * 4, s, w) ||
@@ -291,7 +389,7 @@ int GB300PatchTableEval(const GB300PatchTable *t, const float *src, float *dst, 
     const int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
     return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, t->arrays,
                         (const int *)t->indices, t->params, as_stream(stream),
-                        "GB300PatchTableEval");
+                        "GB300PatchTableEval", t->quadFamily);
 }
 
 GB300VertexBuffer *GB300VertexBufferCreate(int numElements, int numVertices) {

@@ -54,6 +54,22 @@ __device__ __forceinline__ void load_row(const float *__restrict__ src, int stri
     for (int c = 0; c < LC; ++c) x[c] = (e0 + c < length) ? __ldg(p + c) : 0.0f;
 }
 
+// N control-point indices of a patch: 128-bit loads when the index row is 16-byte aligned
+// (REGULAR rows are 64 B, GREGORY_BASIS rows 80 B), scalar loads otherwise.
+template <int N>
+__device__ __forceinline__ void load_indices(const int *__restrict__ cvs, int (&idx)[N]) {
+    if ((N % 4) == 0 && (reinterpret_cast<uintptr_t>(cvs) & 15) == 0) {
+#pragma unroll
+        for (int j = 0; j < N / 4; ++j) {
+            const int4 v = __ldg(reinterpret_cast<const int4 *>(cvs) + j);
+            idx[4 * j] = v.x; idx[4 * j + 1] = v.y; idx[4 * j + 2] = v.z; idx[4 * j + 3] = v.w;
+        }
+    } else {
+#pragma unroll
+        for (int j = 0; j < N; ++j) idx[j] = __ldg(cvs + j);
+    }
+}
+
 __device__ __forceinline__ void bspline_curve(float t, float *p, float *d, float *dd) {
     const float sixth = 1.0f / 6.0f;
     float t2 = t * t, t3 = t * t2;
@@ -131,8 +147,7 @@ __device__ void eval_bspline(float s, float t, int boundary, const int *__restri
     if (boundary & 4) { fold_last(tp); fold_last(td); fold_last(tdd); }
     if (boundary & 8) { fold_first(sp); fold_first(sd); fold_first(sdd); }
     int idx[16];
-#pragma unroll
-    for (int j = 0; j < 16; ++j) idx[j] = __ldg(cvs + j);
+    load_indices<16>(cvs, idx);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         float x[4][LC];
@@ -159,8 +174,7 @@ __device__ void eval_gregory(float s, float t, const int *__restrict__ cvs,
     float d3 = s + tc;  d3 = (d3 <= 0.0f) ? 1.0f : (1.0f / d3);
     const float g0 = s * d0, g2 = t * d1, g4 = sc * d2, g6 = tc * d3;
     int idx[20];
-#pragma unroll
-    for (int j = 0; j < 20; ++j) idx[j] = __ldg(cvs + j);
+    load_indices<20>(cvs, idx);
     // rows of the Bezier grid; interior entries are blended pairs
     constexpr int kGrid[4][4] = {{0, 1, 7, 5}, {2, -1, -2, 6}, {16, -4, -3, 12}, {15, 17, 11, 10}};
 #pragma unroll
@@ -378,8 +392,7 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
     m[6] = m[3] * s; m[7] = m[4] * s; m[8] = m[4] * t; m[9] = m[5] * t;
     m[10] = m[6] * s; m[11] = m[7] * s; m[12] = m[3] * m[5]; m[13] = m[8] * t; m[14] = m[9] * t;
     int idx[12];
-#pragma unroll
-    for (int j = 0; j < 12; ++j) idx[j] = __ldg(cvs + j);
+    load_indices<12>(cvs, idx);
     const float k12 = 1.0f / 12.0f, k6 = 1.0f / 6.0f;
     // one derivative order at a time keeps 12 weights live instead of 72
 #pragma unroll
@@ -449,7 +462,7 @@ __device__ void eval_linear_tri(float s, float t, const int *__restrict__ cvs,
 // OsdEvaluatePatchBasis + gather for one point: normalises (s,t) into the patch, evaluates
 // the basis of `type`, accumulates into acc and returns the derivative scales d1, d2
 // (patchBasis.h:1558-1610).  Returns false for an unknown type.
-template <int LC>
+template <int LC, bool QUAD_ONLY = false>
 __device__ bool eval_patch_point(int type, Param p, float s, float t,
                                  const int *__restrict__ cvs, const float *__restrict__ src,
                                  int stride, int e0, int length, Acc6<LC> &acc, float &d1,
@@ -468,14 +481,23 @@ __device__ bool eval_patch_point(int type, Param p, float s, float t,
         s = s * fracInv - (float)p.u();
         t = t * fracInv - (float)p.v();
     }
-    switch (type) {
-        case 6: eval_bspline<LC>(s, t, p.boundary(), cvs, src, stride, e0, length, acc); break;
-        case 9: eval_gregory<LC>(s, t, cvs, src, stride, e0, length, acc); break;
-        case 5: eval_box_tri<LC>(s, t, p.boundary(), cvs, src, stride, e0, length, acc); break;
-        case 10: eval_gregory_tri<LC>(s, t, cvs, src, stride, e0, length, acc); break;
-        case 3: eval_linear_quad<LC>(s, t, cvs, src, stride, e0, length, acc); break;
-        case 4: eval_linear_tri<LC>(s, t, cvs, src, stride, e0, length, acc); break;
-        default: return false;
+    if (QUAD_ONLY) {  // Catmull-Clark tables: REGULAR, GREGORY_BASIS, QUADS
+        switch (type) {
+            case 6: eval_bspline<LC>(s, t, p.boundary(), cvs, src, stride, e0, length, acc); break;
+            case 9: eval_gregory<LC>(s, t, cvs, src, stride, e0, length, acc); break;
+            case 3: eval_linear_quad<LC>(s, t, cvs, src, stride, e0, length, acc); break;
+            default: return false;
+        }
+    } else {
+        switch (type) {
+            case 6: eval_bspline<LC>(s, t, p.boundary(), cvs, src, stride, e0, length, acc); break;
+            case 9: eval_gregory<LC>(s, t, cvs, src, stride, e0, length, acc); break;
+            case 5: eval_box_tri<LC>(s, t, p.boundary(), cvs, src, stride, e0, length, acc); break;
+            case 10: eval_gregory_tri<LC>(s, t, cvs, src, stride, e0, length, acc); break;
+            case 3: eval_linear_quad<LC>(s, t, cvs, src, stride, e0, length, acc); break;
+            case 4: eval_linear_tri<LC>(s, t, cvs, src, stride, e0, length, acc); break;
+            default: return false;
+        }
     }
     d1 = sign * (float)(1 << depth);
     d2 = sign * d1 * d1;

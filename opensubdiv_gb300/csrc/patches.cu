@@ -67,9 +67,56 @@ __global__ void __launch_bounds__(128) k_eval_patches(const PatchArgs a) {
     }
 }
 
+// G lanes per point, lane l owning primvar elements l, l + G, ...: one source-row fetch is a
+// single coalesced access for the whole group, the accumulators are per element (6 per
+// lane) and no cross-lane reduction is needed.  The basis is evaluated by every lane of the
+// group (cheap for the separable quad-family bases this kernel is used for).
+template <int G>
+__global__ void __launch_bounds__(256, 4) k_eval_patches_lanes(const PatchArgs a) {
+    // G need not be a power of two: a warp holds floor(32 / G) groups (3 lanes per point
+    // for xyz: 10 points per warp) and its remaining lanes stay idle
+    constexpr int kPerWarp = 32 / G;
+    const int wl = threadIdx.x & 31;
+    const int slot = wl / G;
+    if (slot >= kPerWarp) return;
+    const int lane = wl - slot * G;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    const int group = warp * kPerWarp + slot;
+    const int ngroups = nwarps * kPerWarp;
+    for (int i = group; i < a.numCoords; i += ngroups) {
+        const Coord c = a.coords[i];
+        for (int e0 = 0; e0 < a.length; e0 += G) {
+            const int e = e0 + lane;
+            Acc6<1> acc;
+            acc.zero();
+            float d1 = 1.0f, d2 = 1.0f;
+            if (c.arrayIndex >= 0) {
+                const Array arr = a.arrays[c.arrayIndex];
+                const ParamRec pr = a.params[c.patchIndex];
+                const Param p{pr.field0, pr.field1};
+                const int type = p.regular() ? arr.regDesc : arr.desc;
+                const int *cvs =
+                    a.indices + arr.indexBase + arr.stride * (c.patchIndex - arr.primitiveIdBase);
+                if (!eval_patch_point<1, true>(type, p, c.s, c.t, cvs, a.src, a.srcStride, e,
+                                               a.length, acc, d1, d2))
+                    acc.zero();
+            }
+            if (e < a.length) {
+                const float scale[6] = {1.0f, d1, d1, d2, d2, d2};
+#pragma unroll
+                for (int k = 0; k < 6; ++k)
+                    if (a.active & (1 << k))
+                        st_stream(a.dst[k] + (size_t)i * a.dstStride[k] + e, acc.v[k][0] * scale[k]);
+            }
+        }
+    }
+}
+
 int eval_patches(const float *src, float *const *dst, const int *strides, int length,
                  int srcStride, int numCoords, const void *coords, const void *arrays,
-                 const int *indices, const void *params, cudaStream_t s, const char *who) {
+                 const int *indices, const void *params, cudaStream_t s, const char *who,
+                 int quadFamily) {
     if (numCoords <= 0) return ok();
     if (!src || !coords || !arrays || !indices || !params)
         return fail(GB300_ERR_INVALID_ARGUMENT, "%s: null source, coord or table pointer", who);
@@ -95,6 +142,28 @@ int eval_patches(const float *src, float *const *dst, const int *strides, int le
         a.active |= 1 << k;
     }
     if (!a.active) return ok();
+    if (quadFamily) {
+        // element-lane kernel: G = length lanes per point for the common widths, else 32
+        // lanes looping over element chunks
+        const int G = (length <= 4 || length == 6 || length == 8) ? length : 32;
+        const int perWarp = 32 / G;
+        const int threads = 256;
+        long long warps = ((long long)numCoords + perWarp - 1) / perWarp;
+        long long blocks = (warps * 32 + threads - 1) / threads;
+        long long cap = (long long)num_sms() * 16;
+        const int grid = (int)(blocks < cap ? blocks : cap);
+        switch (G) {
+            case 1: k_eval_patches_lanes<1><<<grid, threads, 0, s>>>(a); break;
+            case 2: k_eval_patches_lanes<2><<<grid, threads, 0, s>>>(a); break;
+            case 3: k_eval_patches_lanes<3><<<grid, threads, 0, s>>>(a); break;
+            case 4: k_eval_patches_lanes<4><<<grid, threads, 0, s>>>(a); break;
+            case 6: k_eval_patches_lanes<6><<<grid, threads, 0, s>>>(a); break;
+            case 8: k_eval_patches_lanes<8><<<grid, threads, 0, s>>>(a); break;
+            default: k_eval_patches_lanes<32><<<grid, threads, 0, s>>>(a); break;
+        }
+        count_launch();
+        return check_launch(who);
+    }
     const int threads = 128;
     long long blocks = ((long long)numCoords + threads - 1) / threads;
     long long cap = (long long)num_sms() * 32;
@@ -122,7 +191,7 @@ int GB300EvalPatches(const float *src, float *dst, int length, int srcStride, in
     float *d[6] = {dst, 0, 0, 0, 0, 0};
     int st[6] = {dstStride, 0, 0, 0, 0, 0};
     return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, patchArrays,
-                        patchIndices, patchParams, as_stream(stream), "GB300EvalPatches");
+                        patchIndices, patchParams, as_stream(stream), "GB300EvalPatches", 0);
 }
 
 int GB300EvalPatchesWithDerivatives(
@@ -134,7 +203,7 @@ int GB300EvalPatchesWithDerivatives(
     int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
     return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, patchArrays,
                         patchIndices, patchParams, as_stream(stream),
-                        "GB300EvalPatchesWithDerivatives");
+                        "GB300EvalPatchesWithDerivatives", 0);
 }
 
 }  // extern "C"

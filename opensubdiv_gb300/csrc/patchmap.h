@@ -31,10 +31,13 @@ int find_patches(const PatchMapDevice &m, int n, const int *faces, const float *
 int eval_stencils(const float *src, float *const *dst, const int *strides,
                   const float *const *w, int length, int srcStride, const int *sizes,
                   const int *offsets, const int *indices, int start, int end, cudaStream_t s,
-                  const char *who);
+                  const char *who, const int *outRow = nullptr);
 
+// quadFamily: every patch array holds only REGULAR / GREGORY_BASIS / QUADS patches, which
+// selects the element-lane kernel (known for device tables; raw-pointer calls pass 0).
 int eval_patches(const float *src, float *const *dst, const int *strides, int length,
                  int srcStride, int numCoords, const void *coords, const void *arrays,
-                 const int *indices, const void *params, cudaStream_t s, const char *who);
+                 const int *indices, const void *params, cudaStream_t s, const char *who,
+                 int quadFamily);
 
 }  // namespace gb300

@@ -101,6 +101,7 @@ struct Args {
     const int *sizes;
     const int *offsets;
     const int *indices;
+    const int *outRow;  // optional: stencil i writes destination element outRow[i]
     int length, srcStride, start, end, numTiles;
     int vecSrc, vecDst[6];
 };
@@ -204,7 +205,8 @@ __device__ __forceinline__ void eval_one(const Args &a, int i, int n, const int 
         }
 #pragma unroll
         for (int k = 0; k < NW; ++k) {
-            float *d = a.dst[a.outOf[k]] + (size_t)i * a.dstStride[a.outOf[k]] + c0;
+            const int row = a.outRow ? __ldg(a.outRow + i) : i;
+            float *d = a.dst[a.outOf[k]] + (size_t)row * a.dstStride[a.outOf[k]] + c0;
             const int rem = a.length - c0;
             if (a.vecDst[a.outOf[k]] == 8 && rem >= 8) {
                 asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
@@ -360,11 +362,12 @@ static int launch(const Args &a, cudaStream_t s) {
 int eval_stencils_staged(const float *src, float *const *dst, const int *strides,
                          const float *const *w, int length, int srcStride, const int *sizes,
                          const int *offsets, const int *indices, int start, int end,
-                         cudaStream_t s) {
+                         cudaStream_t s, const int *outRow) {
     auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
     auto al32 = [](const void *p) { return ((uintptr_t)p & 31) == 0; };
     if (!al16(sizes) || !al16(offsets) || !al16(indices)) return GB300_ERR_UNSUPPORTED;
     tma::Args a{};
+    a.outRow = outRow;
     a.src = src;
     a.sizes = sizes;
     a.offsets = offsets;

@@ -42,6 +42,66 @@ def refine_and_limit_torus(nu=512, nv=256, level=3, n_limit=1_000_000, length=8,
                 limit=limit, level=level)
 
 
+def instanced_patch_table(fixture, copies):
+    """`copies` disjoint instances of a flattened Far patch table (Osd::CpuPatchTable layout)
+    stored in a fixture: arrays stay grouped by patch type, every copy's control indices are
+    offset by the source size and its ptex faces by the ptex count.  Returns arrays, indices,
+    params, the source points (copy c displaced by c along x) and the ptex face count."""
+    z = np.load(fixture)
+    arr, idx, par, src = z["arrays"], z["patch_indices"], z["params"], z["src"].reshape(-1, 3)
+    nsrc, nptex = len(src), int(z["num_ptex"])
+    arrays, indices, params = [], [], []
+    ibase = pbase = 0
+    for a in arr:
+        t_reg, t_irr, npatch, ib, stride, pb = (int(x) for x in a)
+        block = idx[ib: ib + npatch * stride]
+        pblock = par[pb: pb + npatch]
+        arrays.append([t_reg, t_irr, npatch * copies, ibase, stride, pbase])
+        for c in range(copies):
+            indices.append(block + c * nsrc)
+            p = pblock.copy()
+            face = (p[:, 0] & 0xFFFFFFF) + c * nptex
+            p[:, 0] = (p[:, 0] & ~0xFFFFFFF) | face
+            params.append(p)
+        ibase += npatch * stride * copies
+        pbase += npatch * copies
+    shift = np.zeros((copies, 1, 3), np.float32)
+    shift[:, 0, 0] = np.arange(copies, dtype=np.float32) * 3.0
+    srcs = (src[None, :, :] + shift).reshape(-1)
+    return (np.asarray(arrays, np.int32), np.concatenate(indices).astype(np.int32),
+            np.concatenate(params).astype(np.int32), np.ascontiguousarray(srcs, np.float32),
+            nptex * copies, bool(z["triangular"]))
+
+
+def eval_patches_torus(n_points=4_000_000, target_patches=1_284_866, seed=7):
+    """EvalPatches workload at the size of the 512 x 256 torus's adaptive level-4 table with
+    Gregory-basis end caps (1,181,550 regular + 103,316 Gregory patches, 5.42M source points):
+    the reference's own adaptive level-4 Gregory-basis table of the 32 x 16 triangle/crease
+    torus (tests/golden/torus32x16_patches_L4.npz), instanced to that patch count, evaluated
+    at n_points uniform (ptex face, u, v) locations."""
+    import os
+    fixture = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "tests", "golden", "torus32x16_patches_L4.npz")
+    per = int(np.load(fixture)["arrays"][:, 2].sum())
+    copies = max(1, round(target_patches / per))
+    arrays, indices, params, src, nptex, tri = instanced_patch_table(fixture, copies)
+    rng = np.random.default_rng(seed)
+    face = rng.integers(0, nptex, n_points).astype(np.int32)
+    u = rng.random(n_points).astype(np.float32)
+    v = rng.random(n_points).astype(np.float32)
+    return dict(name=f"torus32x16_adaptiveL4_gregory_x{copies}_{n_points // 1000000}Mpts",
+                arrays=arrays, indices=indices, params=params, src=src, length=3,
+                num_ptex=nptex, triangular=tri, face=face, u=u, v=v, copies=copies)
+
+
+def patch_bytes(n_points, length, n_outputs, n_src, touched_patches, cvs_per_patch):
+    """Unique-bytes model of one EvalPatches pass: coords (20 B per point), outputs
+    (4 B x length x outputs per point), touched patches' index rows and params
+    (4 B x CVs + 12 B) and the source once (4 B x length per point)."""
+    return (20 * n_points + 4 * length * n_outputs * n_points
+            + touched_patches * (4 * cvs_per_patch + 12) + 4 * length * n_src)
+
+
 def refine_cube(n=8, level=4, seed=1):
     cage = shapes.cube(n, noise=0.01, seed=seed)
     refine = UniformRefiner(cage, level).stencil_table()

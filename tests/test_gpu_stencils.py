@@ -219,6 +219,46 @@ def test_non_factory_table_layouts(layout):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("outputs", [("P", "du", "dv"), ("P",), ("du", "dv")])
+def test_device_table_random_location_limit_stencils(outputs):
+    """A limit table at random locations gets a locality-sorted evaluation order inside the
+    device table; results must land in the caller's order for every output subset."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import shapes, topology
+    from opensubdiv_gb300.evaluator import GB300StencilTable
+    Ev, BD = _ev()
+    cage = shapes.torus(48, 24, tri_fraction=0.05, crease_fraction=0.02, seed=9)
+    face, u, v = shapes.uniform_locations(cage, 20000, seed=10)
+    lt = topology.UniformRefiner(cage, 2).limit_stencil_table(face, u, v)
+    m = len(lt["sizes"])
+    table = GB300StencilTable.Create(lt["sizes"], lt["offsets"], lt["indices"], lt["weights"],
+                                     lt["du_weights"], lt["dv_weights"])
+    src = np.random.default_rng(1).uniform(-1, 1, cage.num_vertices * 8).astype(np.float32)
+    d = BD(0, 8, 8)
+    outs = {k: torch.zeros(m * 8, device="cuda") for k in ("P", "du", "dv")}
+    kw = {}
+    for k in ("du", "dv"):
+        if k in outputs:
+            kw[k], kw[k + "Desc"] = outs[k], d
+    dst = outs["P"] if "P" in outputs else None
+    assert Ev.EvalStencilsTable(dev(src), d, dst, d if dst is not None else None, table, **kw)
+    Ev.Synchronize()
+    refs = [np.zeros(m * 8, np.float32) for _ in range(3)]
+    oracle.eval_stencils(src, (0, 8, 8), refs, [(0, 8, 8)] * 3, lt["sizes"], lt["offsets"],
+                         lt["indices"], [lt["weights"], lt["du_weights"], lt["dv_weights"]],
+                         threads=4)
+    for k, name in enumerate(("P", "du", "dv")):
+        got = host(outs[name])
+        if name in outputs:
+            A = oracle.stencil_abs_scale(src, (0, 8, 8), lt["sizes"], lt["offsets"],
+                                         lt["indices"], [lt["weights"], lt["du_weights"],
+                                                         lt["dv_weights"]][k])
+            assert np.all(np.abs(got - refs[k]) <= 1e-6 * np.maximum(A, 1.0)), name
+        else:
+            assert float(np.abs(got).max()) == 0.0
+
+
+@pytest.mark.gpu
 def test_device_status_word_is_clear_after_runs():
     from opensubdiv_gb300 import _lib
     assert _lib.load().GB300GetDeviceStatus() == 0
