@@ -1,0 +1,409 @@
+//
+// gb300Evaluator.h -- Osd::GB300Evaluator, a drop-in beside Osd::CpuEvaluator and
+// Osd::CudaEvaluator for NVIDIA GB300 (sm_103a), plus its device objects.
+//
+// Header-only C++ layer over the C ABI of libosd_gb300.so (include/osd_gb300.h).  It mirrors
+// the reference interfaces member for member:
+//   GB300StencilTable   <-> Osd::CudaStencilTable   (opensubdiv/osd/cudaEvaluator.h:52-92)
+//   GB300PatchTable     <-> Osd::CudaPatchTable     (opensubdiv/osd/cudaPatchTable.h:51-110)
+//   GB300VertexBuffer   <-> Osd::CudaVertexBuffer   (opensubdiv/osd/cudaVertexBuffer.h:42-79)
+//   GB300Evaluator      <-> Osd::CudaEvaluator      (opensubdiv/osd/cudaEvaluator.h:94-1262)
+// Differences: `deviceContext`, ignored by CudaEvaluator, may carry a cudaStream_t (cast to
+// void*) on which the work is queued; the bool results are false on invalid requests (as
+// CpuEvaluator's) and on device errors, with the reason in GB300GetLastErrorString().
+//
+// Build: compile with -I<repo>/include and, when OpenSubdiv's headers are on the include
+// path, the real Osd::BufferDescriptor / PatchCoord / PatchArray / PatchParam types are
+// used; otherwise layout-identical stand-ins are declared here.  Link libosd_gb300.so.
+//
+#ifndef OPENSUBDIV_GB300_OSD_GB300_EVALUATOR_H
+#define OPENSUBDIV_GB300_OSD_GB300_EVALUATOR_H
+
+#include <cstddef>
+#include <vector>
+
+#include "../../osd_gb300.h"
+
+#if defined(__has_include)
+#if __has_include(<opensubdiv/osd/types.h>) && !defined(OSD_GB300_NO_OPENSUBDIV)
+#define OSD_GB300_HAVE_OPENSUBDIV 1
+#include <opensubdiv/osd/bufferDescriptor.h>
+#include <opensubdiv/osd/types.h>
+#include <opensubdiv/osd/cpuPatchTable.h>
+#endif
+#endif
+
+#ifdef OSD_GB300_HAVE_OPENSUBDIV
+#define OSD_GB300_NAMESPACE_BEGIN \
+    namespace OpenSubdiv {        \
+    namespace OPENSUBDIV_VERSION {  \
+    namespace Osd {
+#define OSD_GB300_NAMESPACE_END \
+    }                           \
+    }                           \
+    }
+#else
+#define OSD_GB300_NAMESPACE_BEGIN \
+    namespace OpenSubdiv {        \
+    namespace Osd {
+#define OSD_GB300_NAMESPACE_END \
+    }                           \
+    }
+#endif
+
+#ifndef OSD_GB300_HAVE_OPENSUBDIV
+// Layout-identical stand-ins for the Osd types the evaluator signatures use
+// (osd/bufferDescriptor.h:61-103, osd/types.h:42-130).
+namespace OpenSubdiv {
+namespace Osd {
+struct BufferDescriptor {
+    BufferDescriptor() : offset(0), length(0), stride(0) {}
+    BufferDescriptor(int o, int l, int s) : offset(o), length(l), stride(s) {}
+    int GetLocalOffset() const { return stride > 0 ? offset % stride : 0; }
+    bool IsValid() const { return length > 0 && length <= stride - GetLocalOffset(); }
+    int offset, length, stride;
+};
+struct PatchHandle { int arrayIndex, patchIndex, vertIndex; };
+struct PatchCoord {
+    PatchCoord() : s(0), t(0) { handle.arrayIndex = handle.patchIndex = handle.vertIndex = 0; }
+    PatchCoord(PatchHandle h, float s_, float t_) : handle(h), s(s_), t(t_) {}
+    PatchHandle handle;
+    float s, t;
+};
+struct PatchArray { int regDesc, desc, numPatches, indexBase, stride, primitiveIdBase; };
+struct PatchParam { unsigned int field0, field1; float sharpness; };
+}  // namespace Osd
+}  // namespace OpenSubdiv
+#endif
+
+OSD_GB300_NAMESPACE_BEGIN
+
+namespace gb300_detail {
+inline void *stream_of(void *deviceContext) { return deviceContext; }
+inline bool ok(int status) { return status == GB300_OK; }
+
+// Picks LimitStencilTable weight arrays when the table type has them.
+template <class T>
+auto du_of(T const *t, int) -> decltype(&t->GetDuWeights()[0]) {
+    return t->GetDuWeights().empty() ? nullptr : &t->GetDuWeights()[0];
+}
+template <class T>
+const float *du_of(T const *, long) { return nullptr; }
+template <class T>
+auto dv_of(T const *t, int) -> decltype(&t->GetDvWeights()[0]) {
+    return t->GetDvWeights().empty() ? nullptr : &t->GetDvWeights()[0];
+}
+template <class T>
+const float *dv_of(T const *, long) { return nullptr; }
+template <class T>
+auto duu_of(T const *t, int) -> decltype(&t->GetDuuWeights()[0]) {
+    return t->GetDuuWeights().empty() ? nullptr : &t->GetDuuWeights()[0];
+}
+template <class T>
+const float *duu_of(T const *, long) { return nullptr; }
+template <class T>
+auto duv_of(T const *t, int) -> decltype(&t->GetDuvWeights()[0]) {
+    return t->GetDuvWeights().empty() ? nullptr : &t->GetDuvWeights()[0];
+}
+template <class T>
+const float *duv_of(T const *, long) { return nullptr; }
+template <class T>
+auto dvv_of(T const *t, int) -> decltype(&t->GetDvvWeights()[0]) {
+    return t->GetDvvWeights().empty() ? nullptr : &t->GetDvvWeights()[0];
+}
+template <class T>
+const float *dvv_of(T const *, long) { return nullptr; }
+}  // namespace gb300_detail
+
+/// Device copy of a Far::StencilTable or Far::LimitStencilTable (CudaStencilTable).
+class GB300StencilTable {
+public:
+    /// FAR_TABLE: Far::StencilTable or Far::LimitStencilTable (or any type with the same
+    /// GetSizes / GetOffsets / GetControlIndices / GetWeights [/ GetDu..DvvWeights] members).
+    template <class FAR_TABLE>
+    static GB300StencilTable *Create(FAR_TABLE const *table, void *deviceContext = NULL) {
+        using namespace gb300_detail;
+        const int n = table->GetNumStencils();
+        const int64_t nnz = (int64_t)table->GetControlIndices().size();
+        ::GB300StencilTable *h = GB300StencilTableCreate(
+            n, nnz, n ? &table->GetSizes()[0] : nullptr, n ? &table->GetOffsets()[0] : nullptr,
+            nnz ? &table->GetControlIndices()[0] : nullptr,
+            nnz ? &table->GetWeights()[0] : nullptr, du_of(table, 0), dv_of(table, 0),
+            duu_of(table, 0), duv_of(table, 0), dvv_of(table, 0), stream_of(deviceContext));
+        return h ? new GB300StencilTable(h) : nullptr;
+    }
+    ~GB300StencilTable() { GB300StencilTableDestroy(_h); }
+
+    void *GetSizesBuffer() const { return GB300StencilTableGetBuffer(_h, 0); }
+    void *GetOffsetsBuffer() const { return GB300StencilTableGetBuffer(_h, 1); }
+    void *GetIndicesBuffer() const { return GB300StencilTableGetBuffer(_h, 2); }
+    void *GetWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 3); }
+    void *GetDuWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 4); }
+    void *GetDvWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 5); }
+    void *GetDuuWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 6); }
+    void *GetDuvWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 7); }
+    void *GetDvvWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 8); }
+    int GetNumStencils() const { return GB300StencilTableGetNumStencils(_h); }
+    ::GB300StencilTable *GetHandle() const { return _h; }
+
+private:
+    explicit GB300StencilTable(::GB300StencilTable *h) : _h(h) {}
+    GB300StencilTable(GB300StencilTable const &) = delete;
+    GB300StencilTable &operator=(GB300StencilTable const &) = delete;
+    ::GB300StencilTable *_h;
+};
+
+/// Device copy of a flattened Far::PatchTable plus its device PatchMap (CudaPatchTable).
+class GB300PatchTable {
+public:
+#ifdef OSD_GB300_HAVE_OPENSUBDIV
+    /// Flattens like CpuPatchTable (osd/cpuPatchTable.cpp:35-158) and uploads.
+    static GB300PatchTable *Create(Far::PatchTable const *farTable, void *deviceContext = NULL) {
+        CpuPatchTable cpu(farTable);
+        const bool tri = farTable->GetVaryingPatchDescriptor().GetNumControlVertices() == 3;
+        return Create((int)cpu.GetNumPatchArrays(), cpu.GetPatchArrayBuffer(),
+                      (int64_t)cpu.GetPatchIndexSize(), cpu.GetPatchIndexBuffer(),
+                      (int)cpu.GetPatchParamSize(), cpu.GetPatchParamBuffer(), tri,
+                      deviceContext);
+    }
+#endif
+    /// From a flattened host table (Osd::CpuPatchTable layout).
+    static GB300PatchTable *Create(int numArrays, PatchArray const *arrays, int64_t numIndices,
+                                   int const *indices, int numPatches, PatchParam const *params,
+                                   bool triangular, void *deviceContext = NULL) {
+        ::GB300PatchTable *h = GB300PatchTableCreate(numArrays, arrays, numIndices, indices,
+                                                     numPatches, params, triangular ? 1 : 0,
+                                                     gb300_detail::stream_of(deviceContext));
+        return h ? new GB300PatchTable(h) : nullptr;
+    }
+    ~GB300PatchTable() { GB300PatchTableDestroy(_h); }
+
+    void *GetPatchArrayBuffer() const { return GB300PatchTableGetBuffer(_h, 0); }
+    void *GetPatchIndexBuffer() const { return GB300PatchTableGetBuffer(_h, 1); }
+    void *GetPatchParamBuffer() const { return GB300PatchTableGetBuffer(_h, 2); }
+    int GetNumPatchArrays() const { return GB300PatchTableGetNumArrays(_h); }
+
+    /// Device Far::PatchMap::FindPatch for n device-resident (face, u, v) queries, writing
+    /// PatchCoords (s, t = u, v) to device memory; misses get handle (-1, -1, -1).
+    bool FindPatches(int n, int const *faces, float const *u, float const *v,
+                     PatchCoord *coordsOut, void *deviceContext = NULL) const {
+        return gb300_detail::ok(GB300PatchTableFindPatches(
+            _h, n, faces, u, v, coordsOut, gb300_detail::stream_of(deviceContext)));
+    }
+    ::GB300PatchTable *GetHandle() const { return _h; }
+
+private:
+    explicit GB300PatchTable(::GB300PatchTable *h) : _h(h) {}
+    GB300PatchTable(GB300PatchTable const &) = delete;
+    GB300PatchTable &operator=(GB300PatchTable const &) = delete;
+    ::GB300PatchTable *_h;
+};
+
+/// Owning device float buffer (CudaVertexBuffer), sizes computed in 64 bits.
+class GB300VertexBuffer {
+public:
+    static GB300VertexBuffer *Create(int numElements, int numVertices,
+                                     void *deviceContext = NULL) {
+        (void)deviceContext;
+        ::GB300VertexBuffer *h = GB300VertexBufferCreate(numElements, numVertices);
+        return h ? new GB300VertexBuffer(h) : nullptr;
+    }
+    ~GB300VertexBuffer() { GB300VertexBufferDestroy(_h); }
+    void UpdateData(const float *src, int startVertex, int numVertices,
+                    void *deviceContext = NULL) {
+        GB300VertexBufferUpdateData(_h, src, startVertex, numVertices,
+                                    gb300_detail::stream_of(deviceContext));
+    }
+    int GetNumElements() const { return GB300VertexBufferGetNumElements(_h); }
+    int GetNumVertices() const { return GB300VertexBufferGetNumVertices(_h); }
+    float *BindCudaBuffer() { return GB300VertexBufferBindCudaBuffer(_h); }
+
+private:
+    explicit GB300VertexBuffer(::GB300VertexBuffer *h) : _h(h) {}
+    GB300VertexBuffer(GB300VertexBuffer const &) = delete;
+    GB300VertexBuffer &operator=(GB300VertexBuffer const &) = delete;
+    ::GB300VertexBuffer *_h;
+};
+
+/// Static, stateless evaluator with CudaEvaluator's interface.
+class GB300Evaluator {
+public:
+    // ---- EvalStencils, raw device pointers (offsets applied here, cudaEvaluator.cpp:159) ----
+    static bool EvalStencils(const float *src, BufferDescriptor const &srcDesc, float *dst,
+                             BufferDescriptor const &dstDesc, const int *sizes,
+                             const int *offsets, const int *indices, const float *weights,
+                             int start, int end, void *deviceContext = NULL) {
+        if (!dst || srcDesc.length != dstDesc.length) return false;
+        return gb300_detail::ok(GB300EvalStencils(
+            src + srcDesc.offset, dst + dstDesc.offset, srcDesc.length, srcDesc.stride,
+            dstDesc.stride, sizes, offsets, indices, weights, start, end,
+            gb300_detail::stream_of(deviceContext)));
+    }
+    static bool EvalStencils(const float *src, BufferDescriptor const &srcDesc, float *dst,
+                             BufferDescriptor const &dstDesc, float *du,
+                             BufferDescriptor const &duDesc, float *dv,
+                             BufferDescriptor const &dvDesc, const int *sizes,
+                             const int *offsets, const int *indices, const float *weights,
+                             const float *duWeights, const float *dvWeights, int start, int end,
+                             void *deviceContext = NULL) {
+        return EvalStencils(src, srcDesc, dst, dstDesc, du, duDesc, dv, dvDesc, nullptr,
+                            BufferDescriptor(), nullptr, BufferDescriptor(), nullptr,
+                            BufferDescriptor(), sizes, offsets, indices, weights, duWeights,
+                            dvWeights, nullptr, nullptr, nullptr, start, end, deviceContext);
+    }
+    static bool EvalStencils(const float *src, BufferDescriptor const &srcDesc, float *dst,
+                             BufferDescriptor const &dstDesc, float *du,
+                             BufferDescriptor const &duDesc, float *dv,
+                             BufferDescriptor const &dvDesc, float *duu,
+                             BufferDescriptor const &duuDesc, float *duv,
+                             BufferDescriptor const &duvDesc, float *dvv,
+                             BufferDescriptor const &dvvDesc, const int *sizes,
+                             const int *offsets, const int *indices, const float *weights,
+                             const float *duWeights, const float *dvWeights,
+                             const float *duuWeights, const float *duvWeights,
+                             const float *dvvWeights, int start, int end,
+                             void *deviceContext = NULL) {
+        BufferDescriptor const *d[6] = {&dstDesc, &duDesc, &dvDesc, &duuDesc, &duvDesc, &dvvDesc};
+        float *o[6] = {dst, du, dv, duu, duv, dvv};
+        for (int k = 0; k < 6; ++k) {
+            if (o[k]) {
+                if (d[k]->length != srcDesc.length) return false;
+                o[k] += d[k]->offset;
+            }
+        }
+        return gb300_detail::ok(GB300EvalStencilsWithDerivatives(
+            src + srcDesc.offset, o[0], o[1], o[2], o[3], o[4], o[5], srcDesc.length,
+            srcDesc.stride, dstDesc.stride, duDesc.stride, dvDesc.stride, duuDesc.stride,
+            duvDesc.stride, dvvDesc.stride, sizes, offsets, indices, weights, duWeights,
+            dvWeights, duuWeights, duvWeights, dvvWeights, start, end,
+            gb300_detail::stream_of(deviceContext)));
+    }
+
+    // ---- EvalStencils over a device table (template forms, cudaEvaluator.h:125-142) ----------
+    template <typename SRC_BUFFER, typename DST_BUFFER>
+    static bool EvalStencils(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                             DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                             GB300StencilTable const *table, const void *instance = NULL,
+                             void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length) return false;
+        return gb300_detail::ok(GB300StencilTableEval(
+            table->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
+            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
+            gb300_detail::stream_of(deviceContext)));
+    }
+    template <typename SRC_BUFFER, typename DST_BUFFER>
+    static bool EvalStencils(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                             DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                             DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
+                             DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
+                             GB300StencilTable const *table, const void *instance = NULL,
+                             void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
+            srcDesc.length != dvDesc.length)
+            return false;
+        return gb300_detail::ok(GB300StencilTableEval(
+            table->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset,
+            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
+            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
+            duDesc.stride, dvDesc.stride, 0, 0, 0, gb300_detail::stream_of(deviceContext)));
+    }
+
+    // ---- EvalPatches, raw device pointers (cudaEvaluator.cpp:295-372) -----------------------
+    static bool EvalPatches(const float *src, BufferDescriptor const &srcDesc, float *dst,
+                            BufferDescriptor const &dstDesc, int numPatchCoords,
+                            const PatchCoord *patchCoords, const PatchArray *patchArrays,
+                            const int *patchIndices, const PatchParam *patchParams,
+                            void *deviceContext = NULL) {
+        if (!dst || srcDesc.length != dstDesc.length) return false;
+        return gb300_detail::ok(GB300EvalPatches(
+            src + srcDesc.offset, dst + dstDesc.offset, srcDesc.length, srcDesc.stride,
+            dstDesc.stride, numPatchCoords, patchCoords, patchArrays, patchIndices, patchParams,
+            gb300_detail::stream_of(deviceContext)));
+    }
+    static bool EvalPatches(const float *src, BufferDescriptor const &srcDesc, float *dst,
+                            BufferDescriptor const &dstDesc, float *du,
+                            BufferDescriptor const &duDesc, float *dv,
+                            BufferDescriptor const &dvDesc, int numPatchCoords,
+                            const PatchCoord *patchCoords, const PatchArray *patchArrays,
+                            const int *patchIndices, const PatchParam *patchParams,
+                            void *deviceContext = NULL) {
+        return EvalPatches(src, srcDesc, dst, dstDesc, du, duDesc, dv, dvDesc, nullptr,
+                           BufferDescriptor(), nullptr, BufferDescriptor(), nullptr,
+                           BufferDescriptor(), numPatchCoords, patchCoords, patchArrays,
+                           patchIndices, patchParams, deviceContext);
+    }
+    static bool EvalPatches(const float *src, BufferDescriptor const &srcDesc, float *dst,
+                            BufferDescriptor const &dstDesc, float *du,
+                            BufferDescriptor const &duDesc, float *dv,
+                            BufferDescriptor const &dvDesc, float *duu,
+                            BufferDescriptor const &duuDesc, float *duv,
+                            BufferDescriptor const &duvDesc, float *dvv,
+                            BufferDescriptor const &dvvDesc, int numPatchCoords,
+                            const PatchCoord *patchCoords, const PatchArray *patchArrays,
+                            const int *patchIndices, const PatchParam *patchParams,
+                            void *deviceContext = NULL) {
+        BufferDescriptor const *d[6] = {&dstDesc, &duDesc, &dvDesc, &duuDesc, &duvDesc, &dvvDesc};
+        float *o[6] = {dst, du, dv, duu, duv, dvv};
+        for (int k = 0; k < 6; ++k) {
+            if (o[k]) {
+                if (d[k]->length != srcDesc.length) return false;
+                o[k] += d[k]->offset;
+            }
+        }
+        return gb300_detail::ok(GB300EvalPatchesWithDerivatives(
+            src + srcDesc.offset, o[0], o[1], o[2], o[3], o[4], o[5], srcDesc.length,
+            srcDesc.stride, dstDesc.stride, duDesc.stride, dvDesc.stride, duuDesc.stride,
+            duvDesc.stride, dvvDesc.stride, numPatchCoords, patchCoords, patchArrays,
+            patchIndices, patchParams, gb300_detail::stream_of(deviceContext)));
+    }
+
+    // ---- EvalPatches over a device table (template forms, cudaEvaluator.h:502-525) ----------
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
+    static bool EvalPatches(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                            DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                            int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
+                            GB300PatchTable const *patchTable, const void *instance = NULL,
+                            void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length) return false;
+        return gb300_detail::ok(GB300PatchTableEval(
+            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
+            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
+            numPatchCoords, (const void *)patchCoords->BindCudaBuffer(),
+            gb300_detail::stream_of(deviceContext)));
+    }
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
+    static bool EvalPatches(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                            DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                            DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
+                            DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
+                            int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
+                            GB300PatchTable const *patchTable, const void *instance = NULL,
+                            void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
+            srcDesc.length != dvDesc.length)
+            return false;
+        return gb300_detail::ok(GB300PatchTableEval(
+            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset,
+            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
+            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
+            duDesc.stride, dvDesc.stride, 0, 0, 0, numPatchCoords,
+            (const void *)patchCoords->BindCudaBuffer(), gb300_detail::stream_of(deviceContext)));
+    }
+
+    /// Waits for the work queued on deviceContext's stream (CudaEvaluator::Synchronize).
+    static void Synchronize(void *deviceContext = NULL) {
+        GB300Synchronize(gb300_detail::stream_of(deviceContext));
+    }
+};
+
+OSD_GB300_NAMESPACE_END
+
+#endif  // OPENSUBDIV_GB300_OSD_GB300_EVALUATOR_H
