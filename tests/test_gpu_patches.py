@@ -134,6 +134,47 @@ def test_eval_patches_raw_api_and_partial_outputs(path):
 
 
 @pytest.mark.gpu
+def test_large_random_request_on_instanced_table():
+    """300k random (face, u, v) on a 74k-patch table (the Gregory-basis torus fixture
+    instanced 12x), including out-of-range faces: device PatchMap + EvalPatches against the
+    oracle point by point."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import workloads
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
+    from opensubdiv_gb300.evaluator import GB300PatchTable
+    fixture = os.path.join(GOLDEN, "torus32x16_patches_L4.npz")
+    arrays, indices, params, src, nptex, tri = workloads.instanced_patch_table(fixture, 12)
+    assert arrays[:, 2].sum() >= 1 << 16
+    t = GB300PatchTable.Create(arrays, indices, params, tri)
+    n = 300_000
+    rng = np.random.default_rng(3)
+    face = rng.integers(-2, nptex + 2, n).astype(np.int32)  # a few misses at both ends
+    u = rng.random(n).astype(np.float32)
+    v = rng.random(n).astype(np.float32)
+    coords = torch.zeros(n * 5, dtype=torch.int32, device="cuda")
+    t.FindPatches(n, dev(face), dev(u), dev(v), coords)
+    d = BD(0, 3, 3)
+    outs = [torch.full((n * 3,), 9.0, device="cuda") for _ in range(3)]
+    assert Ev.EvalPatchesTable(dev(src), d, outs[0], d, n, coords, t, du=outs[1], duDesc=d,
+                               dv=outs[2], dvDesc=d)
+    Ev.Synchronize()
+    ch = host(coords).reshape(n, 5)
+    hit = ch[:, 0] >= 0
+    assert 0 < (~hit).sum() < n // 100
+    chh = np.ascontiguousarray(ch[hit])  # the oracle (like CpuEvaluator) takes hits only
+    m = len(chh)
+    refs = [np.zeros(m * 3, np.float32) for _ in range(3)]
+    oracle.eval_patches(src, (0, 3, 3), refs, [(0, 3, 3)] * 3, chh, arrays, indices, params,
+                        threads=8)
+    A = oracle.abs_scale(src, (0, 3, 3), 3, chh, arrays, indices, params)
+    for k in range(3):
+        g = host(outs[k]).reshape(n, 3)
+        assert np.all(g[~hit] == 0)
+        bound = 1e-6 * np.maximum(A[k].reshape(m, 3), 1.0) + 1e-6
+        assert np.all(np.abs(g[hit] - refs[k].reshape(m, 3)) <= bound), NAMES[k]
+
+
+@pytest.mark.gpu
 def test_patchmap_misses_evaluate_to_zero():
     """Coords with a negative array index (PatchMap misses) produce zeros."""
     torch = torch_cuda()
