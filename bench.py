@@ -48,6 +48,10 @@ def parse():
     ap.add_argument("--n-limit", type=int, default=1_000_000, help="limit locations")
     ap.add_argument("--no-patches", action="store_true", help="skip the EvalPatches section")
     ap.add_argument("--patch-points", type=int, default=4_000_000)
+    ap.add_argument("--no-batch", action="store_true", help="skip the batching section")
+    ap.add_argument("--batch-meshes", type=int, default=256)
+    ap.add_argument("--batch-cv-max", type=int, default=25_000,
+                    help="upper end of the log-uniform CV range of the batched meshes")
     return ap.parse_args()
 
 
@@ -118,6 +122,120 @@ def bench_patches(args, stream, peak):
                          "frac": b / (eval_ms / 1e3) / 1e9 / peak,
                          "traffic": ncu_traffic("patches")},
             "max_abs_err_P_vs_oracle_slice": err_p}
+
+
+def bench_batch(args, stream, peak):
+    """Batching: a population of meshes of uneven size (workloads.batch_population) evaluated
+    per frame as ONE persistent launch replayed from a CUDA graph (GB300StencilBatch, tuned),
+    against one plain EvalStencilsTable call per mesh.  A frame = sinusoidal deformation of
+    every control value (one elementwise pass over all meshes' sources, same in both arms) +
+    evaluation of every mesh."""
+    import torch
+
+    from opensubdiv_gb300 import workloads
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300StencilBatch, GB300StencilTable)
+
+    t0 = time.time()
+    pop = workloads.batch_population(n_meshes=args.batch_meshes, cv_max=args.batch_cv_max)
+    gen_s = time.time() - t0
+    # one concatenated source / base / phase buffer and one destination buffer, every mesh's
+    # slice starting on a 32-byte boundary
+    al = lambda x: (x + 7) // 8 * 8  # noqa: E731
+    s_off, d_off, so, do = [], [], 0, 0
+    for m in pop:
+        s_off.append(so)
+        d_off.append(do)
+        so += al(m["n_cv"] * m["length"])
+        do += al(len(m["table"]["sizes"]) * m["length"])
+    base_h = np.zeros(so, np.float32)
+    phase_h = np.zeros(so, np.float32)
+    for m, o in zip(pop, s_off):
+        base_h[o:o + len(m["src"])] = m["src"]
+        phase_h[o:o + len(m["src"])] = m["phase"]
+    base = torch.from_numpy(base_h).cuda()
+    phase = torch.from_numpy(phase_h).cuda()
+    src = base.clone()
+    dst = torch.zeros(do, device="cuda")
+    tables = [GB300StencilTable.Create(**m["table"]) for m in pop]
+    descs = [BD(0, m["length"], m["length"]) for m in pop]
+    sp = [src.data_ptr() + 4 * o for o in s_off]
+    dp = [dst.data_ptr() + 4 * o for o in d_off]
+    n_st = sum(len(m["table"]["sizes"]) for m in pop)
+    nnz = sum(len(m["table"]["indices"]) for m in pop)
+    b_alg = sum(workloads.stencil_bytes(len(m["table"]["sizes"]), len(m["table"]["indices"]),
+                                        m["length"], m["n_cv"]) for m in pop)
+    batch = GB300StencilBatch(list(zip(tables, sp, descs, dp, descs)), stream=stream)
+    with torch.cuda.stream(stream):
+        batch.Tune(iterations=3, stream=stream)
+    cfg = batch.GetConfig()
+
+    def deform(frame):
+        torch.add(base, torch.sin(0.1 * frame + phase + 7.0 * base), alpha=0.01, out=src)
+
+    def plain_eval():
+        for t, s, d, de in zip(tables, sp, dp, descs):
+            assert Ev.EvalStencilsTable(s, de, d, de, t, stream=stream)
+
+    def batched_eval():
+        batch.EvalGraph(stream=stream)
+
+    def run(fn):
+        for f in range(args.warmup):
+            deform(f)
+            fn()
+        torch.cuda.synchronize()
+        ev = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3))
+              for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for f in range(args.steps):
+                ev[f][0].record(stream)
+                deform(f)
+                ev[f][1].record(stream)
+                fn()
+                ev[f][2].record(stream)
+        torch.cuda.synchronize()
+        frame = np.array([e[0].elapsed_time(e[2]) for e in ev])
+        evals = np.array([e[1].elapsed_time(e[2]) for e in ev])
+        return frame, evals
+
+    with torch.cuda.stream(stream):
+        fp, ep = run(plain_eval)
+        deform(0)
+        plain_eval()
+        torch.cuda.synchronize()
+        ref = dst.clone()
+        dst.zero_()
+        fb, eb = run(batched_eval)
+        deform(0)
+        batched_eval()
+        torch.cuda.synchronize()
+    identical = bool(torch.equal(dst, ref))
+    del ref
+    status = batch.GetDeviceStatus()
+    ms_b, ms_p = float(eb.mean()), float(ep.mean())
+    return {
+        "workload": f"{len(pop)} meshes, CVs log-uniform [500, {args.batch_cv_max}], 70% "
+                    "Catmull-Clark / 30% Loop tori and cubes, uniform L1-4, 3-12 primvars",
+        "meshes": len(pop), "stencils_per_frame": n_st, "nnz": nnz,
+        "generation_s": gen_s, "tuned": cfg,
+        "batched": {"frame_ms": float(fb.mean()), "eval_ms": ms_b,
+                    "stencils_per_s": n_st / (ms_b / 1e3),
+                    "frame_ms_p50": float(np.percentile(fb, 50)),
+                    "frame_ms_p99": float(np.percentile(fb, 99)),
+                    "launches_per_frame": 1},
+        "plain_per_mesh": {"frame_ms": float(fp.mean()), "eval_ms": ms_p,
+                           "stencils_per_s": n_st / (ms_p / 1e3),
+                           "frame_ms_p50": float(np.percentile(fp, 50)),
+                           "frame_ms_p99": float(np.percentile(fp, 99)),
+                           "launches_per_frame": len(pop)},
+        "speedup_eval": ms_p / ms_b, "speedup_frame": float(fp.mean() / fb.mean()),
+        "bit_identical_to_plain": identical, "device_status": status,
+        "roofline": {"bound": "hbm", "kernel": "k_stencils_batch (persistent, graph replay)",
+                     "algorithmic_bytes": b_alg, "achieved": b_alg / (ms_b / 1e3) / 1e9,
+                     "peak": peak, "unit": "GB/s", "frac": b_alg / (ms_b / 1e3) / 1e9 / peak,
+                     "plain_frac": b_alg / (ms_p / 1e3) / 1e9 / peak},
+    }
 
 
 METRIC = "stencil evals per s (EvalStencils refine L3 + limit du/dv)"
@@ -460,6 +578,8 @@ def run_gb300(args, rank, world):
     }
     if not args.no_patches:
         line["eval_patches"] = bench_patches(args, stream, peak)
+    if not args.no_batch:
+        line["batching"] = bench_batch(args, stream, peak)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, el = cpu_rate(w, args.cpu_seconds, threads)

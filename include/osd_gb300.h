@@ -190,6 +190,42 @@ float *GB300VertexBufferBindCudaBuffer(GB300VertexBuffer *buffer);
 int GB300VertexBufferGetNumElements(const GB300VertexBuffer *buffer);
 int GB300VertexBufferGetNumVertices(const GB300VertexBuffer *buffer);
 
+/* ---- batched EvalStencils (no counterpart in the reference) ------------------------------ */
+
+/* A batch evaluates many meshes' device stencil tables in ONE persistent launch, instead of one
+ * GB300StencilTableEval (CudaEvaluator::EvalStencils, osd/cudaEvaluator.h:125-142) per mesh:
+ * job i computes dst[i][k*dstStride[i] + e] = sum_j w_j * src[i][idx_j*srcStride[i] + e] for
+ * every stencil k of tables[i] and element e < length[i] (pointers already include the
+ * BufferDescriptor offset, as in the raw EvalStencils forms).  Results are those of the
+ * per-mesh call (bit-identical for stencils evaluated one per thread, within float rounding
+ * for warp-evaluated large stencils).  The batch keeps the pointers: tables and buffers must
+ * outlive it, and the source / destination contents may change between evaluations. */
+typedef struct GB300StencilBatch GB300StencilBatch;
+
+/* Builds the job table and the concatenated tile list on the device (synchronous on
+ * `stream`).  Uses the tuned configuration cached for batches with the same work histogram,
+ * if any.  Returns NULL on failure (error string set). */
+GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const *tables,
+                                           const float *const *src, float *const *dst,
+                                           const int *length, const int *srcStride,
+                                           const int *dstStride, void *stream);
+void GB300StencilBatchDestroy(GB300StencilBatch *batch);
+/* One evaluation of every job: a counter reset and one kernel on `stream`. */
+int GB300StencilBatchEval(GB300StencilBatch *batch, void *stream);
+/* The same, replayed from a CUDA graph captured on the first call (on a private stream) and
+ * launched on `stream`.  The graph is dropped and recaptured after GB300StencilBatchTune. */
+int GB300StencilBatchEvalGraph(GB300StencilBatch *batch, void *stream);
+/* Autotuner: times each candidate (stencils per tile, CTAs per SM, mean stencil size above
+ * which a job switches to one warp per stencil) over `iterations` evaluations on the batch
+ * itself, keeps the fastest, and caches it for later batches with the same histogram of work
+ * over (stencil size, job size, primvar width) classes.  Writes the outputs as Eval does. */
+int GB300StencilBatchTune(GB300StencilBatch *batch, int iterations, void *stream);
+int GB300StencilBatchGetConfig(const GB300StencilBatch *batch, int *tileStencils,
+                               int *ctasPerSm, int *warpThreshold, int *numTiles);
+/* Reads and clears the batch kernel's status word (GB300_OK or GB300_ERR_DEVICE_TIMEOUT);
+ * synchronous. */
+int GB300StencilBatchGetDeviceStatus(GB300StencilBatch *batch, int *status);
+
 /* Reads and clears the device-side status word of the current device: GB300_OK, or
  * GB300_ERR_DEVICE_TIMEOUT if a bounded wait inside a staged kernel gave up (the kernel then
  * left its outputs incomplete).  Synchronises the device. */

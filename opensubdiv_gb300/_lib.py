@@ -48,6 +48,13 @@ _PROTOS = {
     "GB300VertexBufferBindCudaBuffer": (vp, [vp]),
     "GB300VertexBufferGetNumElements": (i32, [vp]),
     "GB300VertexBufferGetNumVertices": (i32, [vp]),
+    "GB300StencilBatchCreate": (vp, [i32, vp, vp, vp, vp, vp, vp, vp]),
+    "GB300StencilBatchDestroy": (None, [vp]),
+    "GB300StencilBatchEval": (i32, [vp, vp]),
+    "GB300StencilBatchEvalGraph": (i32, [vp, vp]),
+    "GB300StencilBatchTune": (i32, [vp, i32, vp]),
+    "GB300StencilBatchGetConfig": (i32, [vp, vp, vp, vp, vp]),
+    "GB300StencilBatchGetDeviceStatus": (i32, [vp, vp]),
 }
 
 

@@ -413,6 +413,10 @@ extern "C" {
 
 const char *GB300TopologyGetLastError(void) { return t_err.c_str(); }
 
+// Worker threads used by this calling thread's refinement and table copies (OpenMP
+// nthreads-var of the calling thread); 1 when many meshes are generated concurrently.
+void GB300TopologySetNumThreads(int n) { omp_set_num_threads(n > 0 ? n : 1); }
+
 void *GB300TopologyCreate(int scheme, int nverts, int nfaces, const int *vertsPerFace,
                           const int *faceVerts, int ncreases, const int *creaseVerts,
                           const float *creaseSharpness) {

@@ -1,0 +1,599 @@
+// Batched EvalStencils: many meshes of uneven sizes in ONE persistent launch.
+//
+// A launch is a device job table (one job per mesh: its stencil table arrays, source and
+// destination with the descriptor offset applied, primvar length and strides) plus the prefix
+// of the jobs' tile counts.  CTAs of 1 producer warp + 8 consumer warps claim global tile
+// numbers from a device work counter (dynamic scheduling absorbs the uneven tile costs); the
+// producer maps the tile to its job by a warp-wide forward scan of the prefix (claims only
+// grow, so each CTA's scan position only moves forward), stages the tile's sizes / offsets /
+// indices / weights with bulk copies into a 3-stage shared-memory ring, and the consumers
+// evaluate it with the staged EvalStencils kernel's own per-stencil code (tma::eval_one: one
+// stencil per thread, vector row gathers where the layout allows), or one stencil per warp
+// with a shuffle reduction for jobs whose stencils are large (high-valence poles).  Tile size,
+// CTAs per SM and the large-stencil threshold come from the autotuner
+// (GB300StencilBatchTune), which times candidates on the batch itself and caches the winner by
+// the batch's histogram of work.  The counter reset is a memset on the launch stream, so the
+// pair is graph-capturable (GB300StencilBatchEvalGraph).
+#include "common.cuh"
+#include "stencil_eval.cuh"
+#include "stencils_batch.h"
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <new>
+#include <vector>
+
+namespace gb300 {
+namespace batch {
+
+constexpr int kStages = 3;
+constexpr int kConsumers = 256;
+constexpr int kThreads = kConsumers + 32;
+constexpr int kCap = 4096;        // entries per stage
+constexpr int kMaxTile = 256;     // stencils per tile (upper bound)
+constexpr int kMeta = kMaxTile + 8;
+constexpr size_t kStageBytes = (size_t)kCap * 8 + (size_t)kMeta * 8;
+constexpr size_t kSmem = kStages * kStageBytes + 256;
+constexpr unsigned long long kWaitNs = 4000000000ull;
+
+struct Meta {
+    int job, s0, s1, s0a, e0a, e1, staged, done;
+};
+
+__device__ __forceinline__ uint32_t su32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void bar_init(uint64_t *b, int n) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(n));
+}
+__device__ __forceinline__ void bar_arrive(uint64_t *b) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ void bar_arrive_tx(uint64_t *b, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)),
+                 "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t *b, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(su32(b)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+__device__ __forceinline__ unsigned long long gtime() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %globaltimer;" : "=l"(t));
+    return t;
+}
+// Bounded wait; sets *status to GB300_ERR_DEVICE_TIMEOUT and returns false on expiry.
+__device__ __forceinline__ bool bar_wait(uint64_t *b, uint32_t parity, int *status) {
+    if (bar_try(b, parity)) return true;
+    const unsigned long long t0 = gtime();
+    while (!bar_try(b, parity)) {
+        if (gtime() - t0 > kWaitNs) {
+            atomicExch(status, GB300_ERR_DEVICE_TIMEOUT);
+            return false;
+        }
+    }
+    return true;
+}
+__device__ __forceinline__ void bulk(void *dst, const void *src, uint32_t bytes, uint64_t *bar,
+                                     uint64_t pol) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint"
+        " [%0], [%1], %2, [%3], %4;" ::"r"(su32(dst)),
+        "l"(src), "r"(bytes), "r"(su32(bar)), "l"(pol)
+        : "memory");
+}
+
+// One (large) stencil by one warp: lanes split the entries, then a butterfly reduction.
+__device__ __forceinline__ void stencil_warp(const Job &j, int i, int n, int o, const int *lidx,
+                                             const float *lw, int lane, uint64_t pol_src) {
+    for (int c0 = 0; c0 < j.length; c0 += 8) {
+        float acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+        for (int k = lane; k < n; k += 32) {
+            const int id = lidx ? lidx[o + k] : __ldg(j.indices + o + k);
+            const float w = lidx ? lw[o + k] : __ldg(j.w[0] + o + k);
+            float x[8];
+            tma::gather_row<0>(j, id, c0, pol_src, x);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) acc[c] = fmaf(w, x[c], acc[c]);
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+#pragma unroll
+            for (int d = 16; d > 0; d >>= 1) acc[c] += __shfl_xor_sync(0xffffffffu, acc[c], d);
+        if (lane == 0) {
+            float *d = j.dst[0] + (size_t)i * j.dstStride[0] + c0;
+#pragma unroll
+            for (int c = 0; c < 8; ++c)
+                if (c0 + c < j.length) st_stream(d + c, acc[c]);
+        }
+    }
+}
+
+// Consumers' work on one staged tile (VW = 0: the job's row width chosen per gather).
+template <int VW>
+__device__ __forceinline__ void tile_threads(const Job &j, const Meta &m, const int *sidx,
+                                             const float *sw, const int *ssz, const int *sof,
+                                             uint64_t pol_src, uint64_t pol_stream) {
+    for (int i = m.s0 + (int)threadIdx.x; i < m.s1; i += kConsumers) {
+        const int n = ssz[i - m.s0a], o = sof[i - m.s0a];
+        if (m.staged && o >= m.e0a && o + n <= m.e1)
+            tma::eval_one<1, VW>(j, i, n, sidx, sw, kCap, o - m.e0a, pol_src, pol_stream);
+        else
+            tma::eval_one<1, VW>(j, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
+    }
+}
+
+struct Args {
+    const Job *jobs;
+    const int *tileBase;  // numJobs + 1 entries
+    int numJobs, numTiles;
+    int *counter;         // work counter, zeroed before the launch
+    int *status;
+};
+
+__global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
+    extern __shared__ __align__(128) char smem[];
+    __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
+    __shared__ Meta meta[kStages];
+    __shared__ __align__(16) Job sjob[kStages];  // the staged tile's job, read by consumers
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < kStages; ++s) {
+            bar_init(&full[s], 32);
+            bar_init(&empty[s], kConsumers / 32);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const uint64_t pol_stream = l2_evict_first(), pol_src = l2_evict_last();
+    auto stage_ptr = [&](int s, int **idx, float **w, int **sz, int **of) {
+        char *p = smem + (size_t)s * kStageBytes;
+        *idx = (int *)p;
+        *w = (float *)(p + (size_t)kCap * 4);
+        *sz = (int *)(p + (size_t)kCap * 8);
+        *of = *sz + kMeta;
+    };
+
+    if (warp == kConsumers / 32) {
+        // producer: claim tiles until the list is exhausted, then post one "done" stage
+        int jc = 0;  // job of the last claimed tile (claims only grow)
+        for (int it = 0;; ++it) {
+            const int stage = it % kStages;
+            const uint32_t use = (uint32_t)(it / kStages);
+            if (use > 0 && !bar_wait(&empty[stage], (use - 1) & 1, a.status)) return;
+            int t = 0;
+            if (lane == 0) t = atomicAdd(a.counter, 1);
+            t = __shfl_sync(0xffffffffu, t, 0);
+            int *sidx, *ssz, *sof;
+            float *sw;
+            stage_ptr(stage, &sidx, &sw, &ssz, &sof);
+            if (t >= a.numTiles) {
+                if (lane == 0) meta[stage] = Meta{0, 0, 0, 0, 0, 0, 0, 1};
+                __syncwarp();
+                bar_arrive(&full[stage]);  // all 32 lanes: completes the phase without tx
+                return;
+            }
+            // advance jc to the last job whose first tile is <= t (tileBase is non-decreasing,
+            // so the lanes that pass form a prefix)
+            for (;;) {
+                const int q = jc + 1 + lane;
+                const bool pass = q < a.numJobs && __ldg(a.tileBase + q) <= t;
+                const int cnt = __popc(__ballot_sync(0xffffffffu, pass));
+                jc += cnt;
+                if (cnt < 32) break;
+            }
+            const Job &j = a.jobs[jc];
+            static_assert(sizeof(Job) % 4 == 0 && sizeof(Job) / 4 <= 64, "Job copy");
+            for (int q = lane; q < (int)(sizeof(Job) / 4); q += 32)
+                reinterpret_cast<int *>(&sjob[stage])[q] =
+                    __ldg(reinterpret_cast<const int *>(&j) + q);
+            const int s0 = (t - __ldg(a.tileBase + jc)) * j.tileStencils;
+            const int s1 = min(s0 + j.tileStencils, j.numStencils);
+            int e0 = 0, e1 = 0;
+            if (lane == 0) {
+                e0 = __ldg(j.offsets + s0);
+                e1 = __ldg(j.offsets + s1 - 1) + __ldg(j.sizes + s1 - 1);
+            }
+            e0 = __shfl_sync(0xffffffffu, e0, 0);
+            e1 = __shfl_sync(0xffffffffu, e1, 0);
+            const int s0a = s0 & ~3, s1t = s1 & ~3, e0a = e0 & ~3, e1t = e1 & ~3;
+            const bool staged = e1 >= e0 && (e1 - e0a) <= kCap;
+            if (lane == 0) meta[stage] = Meta{jc, s0, s1, s0a, e0a, e1, staged ? 1 : 0, 0};
+            uint32_t bytes = 0;
+            if (s1t > s0a) bytes += (uint32_t)(s1t - s0a) * 8;
+            if (staged && e1t > e0a) bytes += (uint32_t)(e1t - e0a) * 8;
+            if (lane == 0) {
+                bar_arrive_tx(&full[stage], bytes);
+                if (s1t > s0a) {
+                    bulk(ssz, j.sizes + s0a, (uint32_t)(s1t - s0a) * 4, &full[stage], pol_stream);
+                    bulk(sof, j.offsets + s0a, (uint32_t)(s1t - s0a) * 4, &full[stage],
+                         pol_stream);
+                }
+                if (staged && e1t > e0a) {
+                    bulk(sidx, j.indices + e0a, (uint32_t)(e1t - e0a) * 4, &full[stage],
+                         pol_stream);
+                    bulk(sw, j.w[0] + e0a, (uint32_t)(e1t - e0a) * 4, &full[stage], pol_stream);
+                }
+            }
+            // the last partial 16-byte chunks with plain loads (nothing past the arrays' ends)
+            const int st0 = max(s1t, s0a);
+            if (lane < s1 - st0) {
+                ssz[st0 - s0a + lane] = __ldg(j.sizes + st0 + lane);
+                sof[st0 - s0a + lane] = __ldg(j.offsets + st0 + lane);
+            }
+            if (staged) {
+                const int et0 = max(e1t, e0a);
+                if (lane < e1 - et0) {
+                    sidx[et0 - e0a + lane] = __ldg(j.indices + et0 + lane);
+                    sw[et0 - e0a + lane] = __ldg(j.w[0] + et0 + lane);
+                }
+            }
+            __syncwarp();
+            if (lane != 0) bar_arrive(&full[stage]);
+        }
+    }
+
+    // consumers
+    for (int it = 0;; ++it) {
+        const int stage = it % kStages;
+        const uint32_t use = (uint32_t)(it / kStages);
+        if (!bar_wait(&full[stage], use & 1, a.status)) return;
+        const Meta m = meta[stage];
+        if (m.done) return;
+        int *sidx, *ssz, *sof;
+        float *sw;
+        stage_ptr(stage, &sidx, &sw, &ssz, &sof);
+        const Job &j = sjob[stage];
+        if (j.mode == 0) {
+            // one code path for every row width (three inlined widths spill registers)
+            tile_threads<0>(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
+        } else {
+            for (int i = m.s0 + warp; i < m.s1; i += kConsumers / 32) {
+                const int n = ssz[i - m.s0a], o = sof[i - m.s0a];
+                if (m.staged && o >= m.e0a && o + n <= m.e1)
+                    stencil_warp(j, i, n, o - m.e0a, sidx, sw, lane, pol_src);
+                else
+                    stencil_warp(j, i, n, o, nullptr, nullptr, lane, pol_src);
+            }
+        }
+        __syncwarp();
+        if (lane == 0) bar_arrive(&empty[stage]);
+    }
+}
+
+bool make_job(const GB300StencilTable *t, const float *src, float *dst, int length,
+              int srcStride, int dstStride, Job &j, double &meanSize, const char *who) {
+    auto al = [](const void *p, uintptr_t m) { return ((uintptr_t)p & (m - 1)) == 0; };
+    if (!t || !src || !dst || length <= 0 || srcStride < length || dstStride < length) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad table, buffer, length or stride", who);
+        return false;
+    }
+    j = Job{};
+    j.src = src;
+    j.dst[0] = dst;
+    j.sizes = (const int *)GB300StencilTableGetBuffer(t, 0);
+    j.offsets = (const int *)GB300StencilTableGetBuffer(t, 1);
+    j.indices = (const int *)GB300StencilTableGetBuffer(t, 2);
+    j.w[0] = (const float *)GB300StencilTableGetBuffer(t, 3);
+    j.length = length;
+    j.srcStride = srcStride;
+    j.dstStride[0] = dstStride;
+    j.vw = (al(src, 32) && srcStride % 8 == 0) ? 8 : (al(src, 16) && srcStride % 4 == 0) ? 4 : 1;
+    j.vecDst[0] = (al(dst, 32) && dstStride % 8 == 0) ? 8
+                  : (al(dst, 16) && dstStride % 4 == 0) ? 4 : 0;
+    j.numStencils = GB300StencilTableGetNumStencils(t);
+    const int64_t nnz = GB300StencilTableGetNumIndices(t);
+    meanSize = j.numStencils ? (double)nnz / j.numStencils : 0.0;
+    return true;
+}
+
+int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int warpThreshold,
+               int *tileBase) {
+    long long total = 0;
+    for (int k = 0; k < n; ++k) {
+        Job &j = jobs[k];
+        j.mode = meanSize[k] > warpThreshold ? 1 : 0;
+        j.tileStencils = j.mode == 1 ? 32 : tileStencils;
+        tileBase[k] = (int)total;
+        total += (j.numStencils + j.tileStencils - 1) / j.tileStencils;
+    }
+    tileBase[n] = (int)total;
+    return (int)total;
+}
+
+int set_smem_attribute() {
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_stencils_batch,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kSmem);
+        if (e != cudaSuccess) return check_cuda(e, "batch smem attribute");
+        attr = true;
+    }
+    return GB300_OK;
+}
+
+int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
+                int *dStatus, int ctasPerSm, cudaStream_t s) {
+    int st = set_smem_attribute();
+    if (st != GB300_OK) return st;
+    if (numTiles == 0) return ok();
+    st = check_cuda(cudaMemsetAsync(dCounter, 0, sizeof(int), s), "batch counter");
+    if (st != GB300_OK) return st;
+    Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus};
+    const int grid = std::min(numTiles, num_sms() * ctasPerSm);
+    k_stencils_batch<<<grid, kThreads, kSmem, s>>>(a);
+    count_launch();
+    return check_launch("batched EvalStencils");
+}
+
+struct Config {
+    int tileStencils = 256;  // stencils per tile
+    int ctasPerSm = 2;       // persistent CTAs per SM
+    int warpThreshold = 64;  // mean stencil size above which a job uses warp-per-stencil
+};
+
+// Tuner key: the batch's work (stencil entries x primvar width) as a histogram over classes
+// of (log2 mean stencil size, log2 stencils per job, primvar width / 4), each bin's share
+// quantized to 1/16, hashed.  Batches with the same shape of work share a tuned config.
+uint64_t work_signature(const std::vector<Job> &jobs, const std::vector<double> &mean) {
+    std::map<int, double> bins;
+    double total = 0.0;
+    for (size_t k = 0; k < jobs.size(); ++k) {
+        const int sc = (int)std::log2(mean[k] + 1.0);
+        const int jc = (int)std::log2((double)jobs[k].numStencils + 1.0);
+        const int key = (sc << 16) | (jc << 8) | ((jobs[k].length + 3) / 4);
+        const double w = mean[k] * jobs[k].numStencils * jobs[k].length;
+        bins[key] += w;
+        total += w;
+    }
+    uint64_t sig = 1469598103934665603ull;
+    for (auto &kv : bins) {
+        const uint64_t q = total > 0 ? (uint64_t)std::lround(16.0 * kv.second / total) : 0;
+        if (!q) continue;
+        sig = (sig ^ (((uint64_t)kv.first << 8) | q)) * 1099511628211ull;
+    }
+    return sig;
+}
+
+}  // namespace batch
+}  // namespace gb300
+
+using namespace gb300;
+using namespace gb300::batch;
+
+struct GB300StencilBatch {
+    std::vector<Job> jobs;     // in launch order: largest first
+    std::vector<double> mean;  // mean stencil size per job (same order)
+    Config cfg;
+    Job *dJobs = nullptr;      // jobs, then numJobs + 1 ints of tile prefix
+    int *dTileBase = nullptr;
+    int *dCounter = nullptr;   // [0] work counter, [1] status word
+    int numTiles = 0;
+    uint64_t signature = 0;
+    cudaGraphExec_t graph = nullptr;  // counter reset + kernel, instantiated on first use
+    cudaStream_t capture = nullptr;
+    void drop_graph() {
+        if (graph) cudaGraphExecDestroy(graph);
+        graph = nullptr;
+    }
+    ~GB300StencilBatch() {
+        drop_graph();
+        if (capture) cudaStreamDestroy(capture);
+        if (dJobs) cudaFree(dJobs);
+        if (dCounter) cudaFree(dCounter);
+    }
+};
+
+namespace {
+
+std::mutex g_tuneLock;
+std::map<uint64_t, Config> g_tuned;  // work signature -> best config
+
+// Applies b->cfg: job modes, tile sizes and the tile prefix, uploaded to the device.
+int upload_plan(GB300StencilBatch *b, cudaStream_t s) {
+    const int n = (int)b->jobs.size();
+    std::vector<int> base(n + 1);
+    b->numTiles = plan_tiles(b->jobs.data(), b->mean.data(), n, b->cfg.tileStencils,
+                             b->cfg.warpThreshold, base.data());
+    int st = check_cuda(cudaMemcpyAsync(b->dJobs, b->jobs.data(), n * sizeof(Job),
+                                        cudaMemcpyHostToDevice, s), "batch jobs");
+    if (st != GB300_OK) return st;
+    st = check_cuda(cudaMemcpyAsync(b->dTileBase, base.data(), (n + 1) * sizeof(int),
+                                    cudaMemcpyHostToDevice, s), "batch jobs");
+    if (st != GB300_OK) return st;
+    return check_cuda(cudaStreamSynchronize(s), "batch jobs");
+}
+
+int launch_batch(GB300StencilBatch *b, cudaStream_t s) {
+    return launch_jobs(b->dJobs, b->dTileBase, (int)b->jobs.size(), b->numTiles, b->dCounter,
+                       b->dCounter + 1, b->cfg.ctasPerSm, s);
+}
+
+}  // namespace
+
+extern "C" {
+
+GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const *tables,
+                                           const float *const *src, float *const *dst,
+                                           const int *length, const int *srcStride,
+                                           const int *dstStride, void *stream) {
+    if (numJobs <= 0 || !tables || !src || !dst || !length || !srcStride || !dstStride) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchCreate: bad arguments");
+        return nullptr;
+    }
+    GB300StencilBatch *b = new (std::nothrow) GB300StencilBatch;
+    if (!b) {
+        fail(GB300_ERR_OUT_OF_MEMORY, "GB300StencilBatchCreate: host allocation");
+        return nullptr;
+    }
+    cudaStream_t s = as_stream(stream);
+    std::vector<Job> jobs(numJobs);
+    std::vector<double> mean(numJobs);
+    for (int i = 0; i < numJobs; ++i) {
+        if (!make_job(tables[i], src[i], dst[i], length[i], srcStride[i], dstStride[i], jobs[i],
+                      mean[i], "GB300StencilBatchCreate")) {
+            delete b;
+            return nullptr;
+        }
+    }
+    // launch order: largest jobs first, so the small ones fill the tail of the launch
+    std::vector<int> order(numJobs);
+    for (int i = 0; i < numJobs; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) {
+        return mean[x] * jobs[x].numStencils * jobs[x].length >
+               mean[y] * jobs[y].numStencils * jobs[y].length;
+    });
+    for (int i : order) {
+        b->jobs.push_back(jobs[i]);
+        b->mean.push_back(mean[i]);
+    }
+    b->signature = work_signature(b->jobs, b->mean);
+    {
+        std::lock_guard<std::mutex> lock(g_tuneLock);
+        auto it = g_tuned.find(b->signature);
+        if (it != g_tuned.end()) b->cfg = it->second;
+    }
+    const size_t jobBytes = ((numJobs * sizeof(Job) + 255) / 256) * 256;
+    if (check_cuda(cudaMalloc((void **)&b->dJobs, jobBytes + (numJobs + 1) * sizeof(int)),
+                   "batch jobs") != GB300_OK) {
+        b->dJobs = nullptr;
+        delete b;
+        return nullptr;
+    }
+    b->dTileBase = (int *)((char *)b->dJobs + jobBytes);
+    if (check_cuda(cudaMalloc((void **)&b->dCounter, 2 * sizeof(int)), "batch counter") !=
+            GB300_OK ||
+        check_cuda(cudaMemsetAsync(b->dCounter, 0, 2 * sizeof(int), s), "batch counter") !=
+            GB300_OK ||
+        upload_plan(b, s) != GB300_OK) {
+        delete b;
+        return nullptr;
+    }
+    ok();
+    return b;
+}
+
+void GB300StencilBatchDestroy(GB300StencilBatch *b) { delete b; }
+
+int GB300StencilBatchEval(GB300StencilBatch *b, void *stream) {
+    if (!b) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchEval: null batch");
+    return launch_batch(b, as_stream(stream));
+}
+
+int GB300StencilBatchEvalGraph(GB300StencilBatch *b, void *stream) {
+    if (!b) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchEvalGraph: null batch");
+    cudaStream_t s = as_stream(stream);
+    if (!b->graph) {
+        int st = set_smem_attribute();
+        if (st != GB300_OK) return st;
+        if (!b->capture &&
+            (st = check_cuda(cudaStreamCreateWithFlags(&b->capture, cudaStreamNonBlocking),
+                             "batch capture stream")) != GB300_OK)
+            return st;
+        cudaGraph_t g = nullptr;
+        st = check_cuda(cudaStreamBeginCapture(b->capture, cudaStreamCaptureModeThreadLocal),
+                        "batch graph capture");
+        if (st != GB300_OK) return st;
+        const uint64_t before = g_launches.load();
+        const int lst = launch_batch(b, b->capture);
+        const cudaError_t ce = cudaStreamEndCapture(b->capture, &g);
+        g_launches.store(before);  // captured, not launched
+        if (lst != GB300_OK) {
+            if (g) cudaGraphDestroy(g);
+            return lst;
+        }
+        if ((st = check_cuda(ce, "batch graph capture")) != GB300_OK) return st;
+        st = check_cuda(cudaGraphInstantiate(&b->graph, g, 0), "batch graph instantiate");
+        cudaGraphDestroy(g);
+        if (st != GB300_OK) {
+            b->graph = nullptr;
+            return st;
+        }
+    }
+    int st = check_cuda(cudaGraphLaunch(b->graph, s), "GB300StencilBatchEvalGraph");
+    if (st != GB300_OK) return st;
+    if (b->numTiles) count_launch();
+    return ok();
+}
+
+int GB300StencilBatchGetDeviceStatus(GB300StencilBatch *b, int *status) {
+    if (!b || !status)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchGetDeviceStatus: null argument");
+    int st = check_cuda(cudaMemcpy(status, b->dCounter + 1, sizeof(int), cudaMemcpyDeviceToHost),
+                        "batch status");
+    if (st != GB300_OK) return st;
+    if (*status) st = check_cuda(cudaMemset(b->dCounter + 1, 0, sizeof(int)), "batch status");
+    return st != GB300_OK ? st : ok();
+}
+
+int GB300StencilBatchGetConfig(const GB300StencilBatch *b, int *tileStencils, int *ctasPerSm,
+                               int *warpThreshold, int *numTiles) {
+    if (!b) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchGetConfig: null batch");
+    if (tileStencils) *tileStencils = b->cfg.tileStencils;
+    if (ctasPerSm) *ctasPerSm = b->cfg.ctasPerSm;
+    if (warpThreshold) *warpThreshold = b->cfg.warpThreshold;
+    if (numTiles) *numTiles = b->numTiles;
+    return ok();
+}
+
+int GB300StencilBatchTune(GB300StencilBatch *b, int iterations, void *stream) {
+    if (!b) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchTune: null batch");
+    cudaStream_t s = as_stream(stream);
+    if (iterations < 1) iterations = 3;
+    b->drop_graph();
+    const int tiles[] = {64, 128, 256};
+    const int ctas[] = {1, 2};
+    const int thresholds[] = {32, 96, 1 << 30};
+    // a threshold only matters when some job's mean stencil size lies between candidates
+    bool anyLarge = false;
+    for (double m : b->mean) anyLarge |= m > 32;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    Config best = b->cfg;
+    float bestMs = 1e30f;
+    int st = GB300_OK;
+    for (int ts : tiles)
+        for (int c : ctas)
+            for (int th : thresholds) {
+                if (!anyLarge && th != thresholds[0]) continue;
+                b->cfg = Config{ts, c, th};
+                if ((st = upload_plan(b, s)) != GB300_OK) goto done;
+                if ((st = launch_batch(b, s)) != GB300_OK) goto done;  // warm-up
+                cudaEventRecord(e0, s);
+                for (int k = 0; k < iterations; ++k)
+                    if ((st = launch_batch(b, s)) != GB300_OK) goto done;
+                cudaEventRecord(e1, s);
+                cudaEventSynchronize(e1);
+                float ms = 0.0f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < bestMs) {
+                    bestMs = ms;
+                    best = b->cfg;
+                }
+            }
+done:
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->cfg = best;
+    const int rb = upload_plan(b, s);
+    if (st != GB300_OK) return st;
+    if (rb != GB300_OK) return rb;
+    {
+        std::lock_guard<std::mutex> lock(g_tuneLock);
+        g_tuned[b->signature] = best;
+    }
+    return ok();
+}
+
+}  // extern "C"

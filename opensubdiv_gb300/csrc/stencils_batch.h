@@ -1,0 +1,49 @@
+// Batched EvalStencils: the job descriptor and launch interface shared by GB300StencilBatch
+// (stencils_batch.cu) and the serving loop (server.cu).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../../include/osd_gb300.h"
+
+namespace gb300 {
+namespace batch {
+
+// One mesh's EvalStencils inside a batched launch.  The first fields are the argument view of
+// tma::eval_one (one weight array, one output): src / dst include the descriptor offset.
+struct Job {
+    const float *src;
+    float *dst[1];
+    const float *w[1];
+    int dstStride[1];
+    int outOf[1];       // always 0
+    int vecDst[1];      // 8: 32-byte aligned rows, 4: 16-byte aligned rows, 0: scalar stores
+    const int *indices;
+    const int *outRow;  // always null: stencil i writes row i
+    const int *sizes, *offsets;
+    int length, srcStride;
+    int vw;             // source rows: 8 = 256-bit loads, 4 = 128-bit loads, 1 = scalar
+    int mode;           // 0: one stencil per thread, 1: one stencil per warp
+    int numStencils;
+    int tileStencils;   // stencils per tile of this job
+};
+
+// Describes job k = (table, src, dst, length, strides); false (error recorded) on bad input.
+// meanSize receives nnz / numStencils.
+bool make_job(const GB300StencilTable *table, const float *src, float *dst, int length,
+              int srcStride, int dstStride, Job &job, double &meanSize, const char *who);
+
+// Chooses each job's mode and tile size and writes the tile prefix tileBase[0..n] (tileBase[n]
+// = total tiles).  Jobs keep their order: tiles are handed out in job order.
+int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int warpThreshold,
+               int *tileBase);
+
+// One persistent launch over n jobs (device arrays dJobs[n], dTileBase[n + 1]); resets the
+// work counter on `s` first.  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.
+int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
+                int *dStatus, int ctasPerSm, cudaStream_t s);
+
+}  // namespace batch
+}  // namespace gb300

@@ -17,6 +17,7 @@
 // straight from global memory.  Every mbarrier wait is bounded by a %globaltimer deadline; on
 // expiry the CTA records GB300_ERR_DEVICE_TIMEOUT in g_status and leaves.
 #include "common.cuh"
+#include "stencil_eval.cuh"
 
 namespace gb300 {
 
@@ -117,116 +118,6 @@ __device__ __forceinline__ void stage_ptrs(char *base, int stage, int **idx, flo
     *sz = (int *)p;
     p += (size_t)Cfg<NW>::kMeta * 4;
     *of = (int *)p;
-}
-
-// Elements [c0, c0 + 8) of source row `id` (zeros past the primvar length): one 256-bit load
-// for 32-byte aligned rows, two 128-bit loads for 16-byte aligned rows, else scalar loads.
-template <int VW>
-__device__ __forceinline__ void gather_row(const Args &a, int id, int c0, uint64_t pol_src,
-                                           float (&x)[8]) {
-    const float *row = a.src + (size_t)id * a.srcStride + c0;
-    if (VW == 8) {
-        asm("ld.global.nc.v8.f32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
-            : "=f"(x[0]), "=f"(x[1]), "=f"(x[2]), "=f"(x[3]), "=f"(x[4]), "=f"(x[5]),
-              "=f"(x[6]), "=f"(x[7])
-            : "l"(row));
-    } else if (VW == 4) {
-        const float4 *r4 = reinterpret_cast<const float4 *>(row);
-        const float4 v0 = __ldg(r4);
-        x[0] = v0.x; x[1] = v0.y; x[2] = v0.z; x[3] = v0.w;
-        if (c0 + 4 < a.length) {
-            const float4 v1 = __ldg(r4 + 1);
-            x[4] = v1.x; x[5] = v1.y; x[6] = v1.z; x[7] = v1.w;
-        } else {
-            x[4] = x[5] = x[6] = x[7] = 0.0f;
-        }
-    } else {
-#pragma unroll
-        for (int c = 0; c < 8; ++c) x[c] = (c0 + c < a.length) ? ld_src(row + c, pol_src) : 0.0f;
-    }
-}
-
-template <int NW>
-__device__ __forceinline__ void fma_row(const float (&wk)[NW], const float (&x)[8],
-                                        float (&acc)[NW][8]) {
-#pragma unroll
-    for (int k = 0; k < NW; ++k)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) acc[k][c] = fmaf(wk[k], x[c], acc[k][c]);
-}
-
-// One stencil, all requested outputs, elements [c0, c0 + 8) of the primvar; entries come from
-// shared memory (lidx/lw at local offset o) or straight from global memory (when lidx null).
-template <int NW, int VW>
-__device__ __forceinline__ void eval_one(const Args &a, int i, int n, const int *lidx,
-                                         const float *lw, int lstride, int o, uint64_t pol_src,
-                                         uint64_t pol_stream) {
-    for (int c0 = 0; c0 < a.length; c0 += 8) {
-        float acc[NW][8];
-#pragma unroll
-        for (int k = 0; k < NW; ++k)
-#pragma unroll
-            for (int c = 0; c < 8; ++c) acc[k][c] = 0.0f;
-        if (lidx) {
-            // entries from shared memory in aligned chunks of 4 (one 128-bit shared load per
-            // array and chunk); entries of the chunk outside [o, o + n) are skipped, so the
-            // row gathers stay exact while every thread runs the same simple loop
-            const int end = o + n;
-            for (int q = o & ~3; q < end; q += 4) {
-                const int4 id4 = *reinterpret_cast<const int4 *>(lidx + q);
-                float4 w4[NW];
-#pragma unroll
-                for (int k = 0; k < NW; ++k)
-                    w4[k] = *reinterpret_cast<const float4 *>(lw + k * lstride + q);
-                const int ids[4] = {id4.x, id4.y, id4.z, id4.w};
-                float x[4][8];
-#pragma unroll
-                for (int m = 0; m < 4; ++m)
-                    if (q + m >= o && q + m < end) gather_row<VW>(a, ids[m], c0, pol_src, x[m]);
-#pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    if (q + m < o || q + m >= end) continue;
-                    float wk[NW];
-#pragma unroll
-                    for (int k = 0; k < NW; ++k)
-                        wk[k] = m == 0 ? w4[k].x : m == 1 ? w4[k].y : m == 2 ? w4[k].z : w4[k].w;
-                    fma_row<NW>(wk, x[m], acc);
-                }
-            }
-        } else {
-            for (int j = 0; j < n; ++j) {
-                float wk[NW];
-#pragma unroll
-                for (int k = 0; k < NW; ++k) wk[k] = ld_stream(a.w[k] + o + j, pol_stream);
-                float x[8];
-                gather_row<VW>(a, ld_stream(a.indices + o + j, pol_stream), c0, pol_src, x);
-                fma_row<NW>(wk, x, acc);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < NW; ++k) {
-            const int row = a.outRow ? __ldg(a.outRow + i) : i;
-            float *d = a.dst[a.outOf[k]] + (size_t)row * a.dstStride[a.outOf[k]] + c0;
-            const int rem = a.length - c0;
-            if (a.vecDst[a.outOf[k]] == 8 && rem >= 8) {
-                asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
-                             "f"(acc[k][0]), "f"(acc[k][1]), "f"(acc[k][2]), "f"(acc[k][3]),
-                             "f"(acc[k][4]), "f"(acc[k][5]), "f"(acc[k][6]), "f"(acc[k][7])
-                             : "memory");
-            } else if (a.vecDst[a.outOf[k]] && rem >= 8) {
-                asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d),
-                             "f"(acc[k][0]), "f"(acc[k][1]), "f"(acc[k][2]), "f"(acc[k][3])
-                             : "memory");
-                asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d + 4),
-                             "f"(acc[k][4]), "f"(acc[k][5]), "f"(acc[k][6]), "f"(acc[k][7])
-                             : "memory");
-            } else {
-#pragma unroll
-                for (int c = 0; c < 8; ++c)
-                    if (c < rem) st_stream(d + c, acc[k][c]);
-            }
-        }
-    }
 }
 
 template <int NW, int VW>

@@ -224,6 +224,63 @@ class GB300StencilTable:
     def GetDvvWeightsBuffer(self): return self._buf(8)
 
 
+class GB300StencilBatch:
+    """Many meshes' EvalStencils in one persistent launch (no counterpart in the reference;
+    the per-mesh equivalent is one EvalStencilsTable call per job).
+
+    ``jobs`` is a sequence of ``(table, src, srcDesc, dst, dstDesc)``: a
+    :class:`GB300StencilTable` and device buffers with their descriptors, as for
+    :meth:`GB300Evaluator.EvalStencilsTable`.  Tables and buffers must outlive the batch."""
+
+    def __init__(self, jobs, stream=None):
+        import ctypes as C
+        n = len(jobs)
+        tabs = (C.c_void_p * n)()
+        srcs = (C.c_void_p * n)()
+        dsts = (C.c_void_p * n)()
+        lens, sst, dst_ = (C.c_int * n)(), (C.c_int * n)(), (C.c_int * n)()
+        for i, (table, src, sd, dst, dd) in enumerate(jobs):
+            sd, dd = _desc(sd), _desc(dd)
+            if sd.length != dd.length or not sd.IsValid() or not dd.IsValid():
+                raise ValueError(f"job {i}: mismatched or invalid buffer descriptors")
+            tabs[i] = table.handle
+            srcs[i] = _ptr(src, sd.offset)
+            dsts[i] = _ptr(dst, dd.offset)
+            lens[i], sst[i], dst_[i] = sd.length, sd.stride, dd.stride
+        self._keep = [j[0] for j in jobs]  # tables stay alive while the batch exists
+        self.handle = _lib.load().GB300StencilBatchCreate(n, tabs, srcs, dsts, lens, sst, dst_,
+                                                          _stream(stream))
+        if not self.handle:
+            raise GB300Error(1, last_error())
+
+    def __del__(self):
+        if getattr(self, "handle", None):
+            _lib.load().GB300StencilBatchDestroy(self.handle)
+            self.handle = None
+
+    def Eval(self, stream=None):
+        check(_lib.load().GB300StencilBatchEval(self.handle, _stream(stream)))
+
+    def EvalGraph(self, stream=None):
+        check(_lib.load().GB300StencilBatchEvalGraph(self.handle, _stream(stream)))
+
+    def Tune(self, iterations=3, stream=None):
+        check(_lib.load().GB300StencilBatchTune(self.handle, iterations, _stream(stream)))
+
+    def GetConfig(self):
+        import ctypes as C
+        v = [C.c_int(0) for _ in range(4)]
+        check(_lib.load().GB300StencilBatchGetConfig(self.handle, *[C.byref(x) for x in v]))
+        return dict(tile_stencils=v[0].value, ctas_per_sm=v[1].value,
+                    warp_threshold=v[2].value, num_tiles=v[3].value)
+
+    def GetDeviceStatus(self):
+        import ctypes as C
+        s = C.c_int(0)
+        check(_lib.load().GB300StencilBatchGetDeviceStatus(self.handle, C.byref(s)))
+        return s.value
+
+
 class GB300PatchTable:
     """Device copy of a flattened Far::PatchTable plus its device PatchMap (CudaPatchTable)."""
 

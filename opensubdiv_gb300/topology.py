@@ -39,6 +39,8 @@ def load():
         lib.GB300TopologyLimitStencilNnz.argtypes = [vp]
         lib.GB300TopologyLimitStencilCopy.argtypes = [vp, vp, vp, vp, vp, vp, vp]
         lib.GB300TopologyGetLastError.restype = C.c_char_p
+        lib.GB300TopologySetNumThreads.argtypes = [i32]
+        lib.GB300TopologySetNumThreads.restype = None
         _lib = lib
     return _lib
 

@@ -108,3 +108,60 @@ def refine_cube(n=8, level=4, seed=1):
     return dict(name=f"cube{n}_catmark_L{level}_xyz", cage=cage,
                 src=np.ascontiguousarray(cage.positions.ravel()), length=3, refine=refine,
                 level=level)
+
+
+def batch_population(n_meshes=256, cv_min=500, cv_max=200_000, seed=4096, threads=None):
+    """Meshes of uneven size for batched evaluation: procedural noisy tori or cubes (50/50)
+    with control-vertex counts log-uniform in [cv_min, cv_max], 70% Catmull-Clark and 30%
+    Loop (every quad split along a random diagonal), uniform refinement level uniform in
+    {1, 2, 3, 4} (stencils of the finest level only) and 3-12 float32 primvars (xyz + U[-1, 1]
+    channels), each with a seeded deformation phase.  Tables are generated on `threads` host
+    threads (default: all cores), one mesh per thread.
+
+    Returns a list of dicts: name, scheme, level, length, phase, n_cv, src (float32 n_cv x
+    length, flattened), table (Far-layout arrays)."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+
+    from .topology import load as _topo_load
+
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_meshes):
+        loop = bool(rng.random() < 0.3)
+        kind = "torus" if rng.random() < 0.5 else "cube"
+        cv = float(np.exp(rng.uniform(np.log(cv_min), np.log(cv_max))))
+        specs.append(dict(index=i, loop=loop, kind=kind, cv=cv, level=int(rng.integers(1, 5)),
+                          length=int(rng.integers(3, 13)),
+                          phase=float(rng.uniform(0.0, 2.0 * np.pi))))
+
+    def build(sp):
+        _topo_load().GB300TopologySetNumThreads(1)
+        scheme = shapes.LOOP if sp["loop"] else shapes.CATMARK
+        s = seed * 1000 + sp["index"]
+        if sp["kind"] == "torus":
+            nv = max(3, int(round(np.sqrt(sp["cv"] / 2.0))))
+            nu = max(3, int(round(sp["cv"] / nv)))
+            cage = shapes.torus(nu, nv, noise=0.005, seed=s, scheme=scheme)
+        else:
+            n = max(1, int(round(np.sqrt(max(sp["cv"] - 2.0, 6.0) / 6.0))))
+            cage = shapes.cube(n, noise=0.01, seed=s, scheme=scheme)
+        table = UniformRefiner(cage, sp["level"]).stencil_table()
+        r = np.random.default_rng(s + 1)
+        ncv = cage.num_vertices
+        src = np.concatenate([cage.positions,
+                              r.uniform(-1, 1, (ncv, sp["length"] - 3)).astype(np.float32)], 1)
+        return dict(name=f"{cage.name}_{'loop' if sp['loop'] else 'catmark'}_L{sp['level']}",
+                    scheme=scheme, level=sp["level"], length=sp["length"], phase=sp["phase"],
+                    n_cv=ncv, src=np.ascontiguousarray(src.ravel()), table=table)
+
+    _topo_load()  # load once before the workers start
+    with ThreadPoolExecutor(threads or os.cpu_count()) as ex:
+        return list(ex.map(build, specs))
+
+
+def deform(base, phase, frame, amplitude=0.01):
+    """Per-frame sinusoidal displacement of every control value: base + a sin(0.1 frame +
+    phase + 7 base), with the mesh's phase (works on numpy arrays and torch tensors)."""
+    lib = np if isinstance(base, np.ndarray) else __import__("torch")
+    return base + amplitude * lib.sin(0.1 * frame + phase + 7.0 * base)
