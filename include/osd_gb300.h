@@ -226,6 +226,30 @@ int GB300StencilBatchGetConfig(const GB300StencilBatch *batch, int *tileStencils
  * synchronous. */
 int GB300StencilBatchGetDeviceStatus(GB300StencilBatch *batch, int *status);
 
+/* ---- batched EvalStencils that allocates nothing (no counterpart in the reference) -------- */
+
+/* For callers that cannot allocate: a renderer running under a fixed device-memory budget or
+ * a pool it does not own, or code that must not call cudaMalloc / cudaFree (they synchronise
+ * the device) inside its frame loop.  Evaluates numJobs raw-pointer EvalStencils jobs (the
+ * arguments of GB300EvalStencils per job, over stencils [0, numStencils[k]); every array
+ * argument is a HOST array indexed by job, holding device pointers or ints) in one batched
+ * launch, like GB300StencilBatchEval with one stencil per thread.  It allocates no device or
+ * host memory: its scratch (work counter, status word, job table, tile prefix) is a fixed
+ * 26,112-byte device array inside the library, so at most 256 jobs per call (more are
+ * rejected with GB300_ERR_INVALID_ARGUMENT and a message).  The job table is copied into that
+ * array from the host stack with cudaMemcpyAsync on `stream`, and the counter and status word
+ * are cleared on `stream` before the kernel.  Table arrays must be 16-byte aligned.
+ * The first call on each device looks up the array's device address (cudaGetSymbolAddress,
+ * with that device current): make that first call before any stream capture.  There is one
+ * array per device, so calls that can overlap on a device (different streams, or different
+ * host threads without ordering) race: serialise them on one stream. */
+int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float *const *dst,
+                                    const int *length, const int *srcStride,
+                                    const int *dstStride, const int *numStencils,
+                                    const int *const *sizes, const int *const *offsets,
+                                    const int *const *indices, const float *const *weights,
+                                    void *stream);
+
 /* Reads and clears the device-side status word of the current device: GB300_OK, or
  * GB300_ERR_DEVICE_TIMEOUT if a bounded wait inside a staged kernel gave up (the kernel then
  * left its outputs incomplete).  Synchronises the device. */

@@ -55,6 +55,7 @@ _PROTOS = {
     "GB300StencilBatchTune": (i32, [vp, i32, vp]),
     "GB300StencilBatchGetConfig": (i32, [vp, vp, vp, vp, vp]),
     "GB300StencilBatchGetDeviceStatus": (i32, [vp, vp]),
+    "GB300EvalStencilsBatchedNoAlloc": (i32, [i32] + [vp] * 11),
 }
 
 

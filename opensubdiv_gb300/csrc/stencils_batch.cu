@@ -421,6 +421,33 @@ int launch_batch(GB300StencilBatch *b, cudaStream_t s) {
 
 }  // namespace
 
+
+// ---- batched EvalStencils without allocation ------------------------------------------------
+//
+// The same kernel with all of its scratch -- work counter, status word, job table and tile
+// prefix -- in one fixed file-scope device array, so a call allocates no memory: the job table
+// is built on the host stack and copied into the array, the counter and status word are cleared
+// by a memset, and the kernel runs every job one stencil per thread (jobs' mean stencil sizes
+// are not known without reading the device tables).  One array per device means calls that
+// overlap on the device (two streams, two host threads) race on it.
+namespace {
+
+constexpr int kNoAllocMaxJobs = 256;
+constexpr size_t kNoAllocJobOffset = 256;  // [0] counter, [1] status
+constexpr size_t kNoAllocBaseOffset =
+    kNoAllocJobOffset + ((kNoAllocMaxJobs * sizeof(Job) + 255) / 256) * 256;
+constexpr size_t kNoAllocScratchBytes =
+    kNoAllocBaseOffset + (((kNoAllocMaxJobs + 1) * sizeof(int) + 255) / 256) * 256;
+constexpr int kNoAllocMaxDevices = 64;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noallocLock;
+unsigned char *g_noallocAddr[kNoAllocMaxDevices];  // scratch address per device
+int g_noallocSms[kNoAllocMaxDevices];
+
+}  // namespace
+
 extern "C" {
 
 GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const *tables,
@@ -594,6 +621,105 @@ done:
         g_tuned[b->signature] = best;
     }
     return ok();
+}
+
+
+int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float *const *dst,
+                                    const int *length, const int *srcStride,
+                                    const int *dstStride, const int *numStencils,
+                                    const int *const *sizes, const int *const *offsets,
+                                    const int *const *indices, const float *const *weights,
+                                    void *stream) {
+    static const char *who = "GB300EvalStencilsBatchedNoAlloc";
+    if (numJobs < 1 || numJobs > kNoAllocMaxJobs)
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "%s: %d jobs; between 1 and %d jobs fit its fixed %zu-byte device scratch",
+                    who, numJobs, kNoAllocMaxJobs, kNoAllocScratchBytes);
+    if (!src || !dst || !length || !srcStride || !dstStride || !numStencils || !sizes ||
+        !offsets || !indices || !weights)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: null argument array", who);
+    // job table and tile prefix on the host stack (no heap allocation)
+    Job jobs[kNoAllocMaxJobs];
+    int base[kNoAllocMaxJobs + 1];
+    auto al = [](const void *p, uintptr_t m) { return ((uintptr_t)p & (m - 1)) == 0; };
+    long long tiles = 0;
+    for (int k = 0; k < numJobs; ++k) {
+        const int n = numStencils[k];
+        if (n < 0 || length[k] <= 0 || srcStride[k] < length[k] || dstStride[k] < length[k] ||
+            (n > 0 && (!src[k] || !dst[k] || !sizes[k] || !offsets[k] || !indices[k] ||
+                       !weights[k])))
+            return fail(GB300_ERR_INVALID_ARGUMENT,
+                        "%s: job %d has a bad count, length, stride or null pointer", who, k);
+        if (n > 0 && (!al(sizes[k], 16) || !al(offsets[k], 16) || !al(indices[k], 16) ||
+                      !al(weights[k], 16)))
+            return fail(GB300_ERR_INVALID_ARGUMENT,
+                        "%s: job %d table arrays must be 16-byte aligned (bulk copies)", who, k);
+        Job &j = jobs[k];
+        j = Job{};
+        j.src = src[k];
+        j.dst[0] = dst[k];
+        j.w[0] = weights[k];
+        j.sizes = sizes[k];
+        j.offsets = offsets[k];
+        j.indices = indices[k];
+        j.length = length[k];
+        j.srcStride = srcStride[k];
+        j.dstStride[0] = dstStride[k];
+        j.vw = (al(src[k], 32) && srcStride[k] % 8 == 0)   ? 8
+               : (al(src[k], 16) && srcStride[k] % 4 == 0) ? 4 : 1;
+        j.vecDst[0] = (al(dst[k], 32) && dstStride[k] % 8 == 0)   ? 8
+                      : (al(dst[k], 16) && dstStride[k] % 4 == 0) ? 4 : 0;
+        j.numStencils = n;
+        j.mode = 0;
+        j.tileStencils = kMaxTile;
+        base[k] = (int)tiles;
+        tiles += (n + kMaxTile - 1) / kMaxTile;
+        if (tiles > INT32_MAX)
+            return fail(GB300_ERR_INVALID_ARGUMENT, "%s: more than 2^31 tiles", who);
+    }
+    base[numJobs] = (int)tiles;
+    // scratch address and SM count, once per device (with that device current)
+    int dev = 0;
+    int st = check_cuda(cudaGetDevice(&dev), who);
+    if (st != GB300_OK) return st;
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return fail(GB300_ERR_UNSUPPORTED, "%s: device %d beyond the first %d", who, dev,
+                    kNoAllocMaxDevices);
+    unsigned char *scratch = nullptr;
+    int sms = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_noallocLock);
+        if (!g_noallocAddr[dev]) {
+            void *p = nullptr;
+            st = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), who);
+            if (st != GB300_OK) return st;
+            int n = 0;
+            st = check_cuda(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), who);
+            if (st != GB300_OK) return st;
+            g_noallocSms[dev] = n > 0 ? n : 1;
+            g_noallocAddr[dev] = (unsigned char *)p;
+        }
+        scratch = g_noallocAddr[dev];
+        sms = g_noallocSms[dev];
+    }
+    if ((st = set_smem_attribute()) != GB300_OK) return st;
+    if (tiles == 0) return ok();
+    cudaStream_t s = as_stream(stream);
+    int *counter = (int *)scratch;
+    Job *dJobs = (Job *)(scratch + kNoAllocJobOffset);
+    int *dBase = (int *)(scratch + kNoAllocBaseOffset);
+    // pageable host -> device: the stack buffers are consumed before the calls return
+    if ((st = check_cuda(cudaMemcpyAsync(dJobs, jobs, numJobs * sizeof(Job),
+                                         cudaMemcpyHostToDevice, s), who)) != GB300_OK ||
+        (st = check_cuda(cudaMemcpyAsync(dBase, base, (numJobs + 1) * sizeof(int),
+                                         cudaMemcpyHostToDevice, s), who)) != GB300_OK ||
+        (st = check_cuda(cudaMemsetAsync(counter, 0, 2 * sizeof(int), s), who)) != GB300_OK)
+        return st;
+    Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1};
+    const int grid = (int)std::min<long long>(tiles, 2LL * sms);
+    k_stencils_batch<<<grid, kThreads, kSmem, s>>>(a);
+    count_launch();
+    return check_launch(who);
 }
 
 }  // extern "C"
