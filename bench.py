@@ -52,6 +52,14 @@ def parse():
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--batch-cv-max", type=int, default=25_000,
                     help="upper end of the log-uniform CV range of the batched meshes")
+    ap.add_argument("--no-serving", action="store_true", help="skip the serving section")
+    ap.add_argument("--serve-topologies", type=int, default=1000)
+    ap.add_argument("--serve-requests", type=int, default=4000, help="requests per rate")
+    ap.add_argument("--serve-rates", type=lambda s: [float(x) for x in s.split(",")],
+                    default=[2000.0, 5000.0, 10000.0, 20000.0])
+    ap.add_argument("--serve-budget-gb", type=float, default=40.0)
+    ap.add_argument("--serve-ring-mb", type=int, default=4096,
+                    help="pinned host ring for request outputs")
     return ap.parse_args()
 
 
@@ -235,6 +243,120 @@ def bench_batch(args, stream, peak):
                      "algorithmic_bytes": b_alg, "achieved": b_alg / (ms_b / 1e3) / 1e9,
                      "peak": peak, "unit": "GB/s", "frac": b_alg / (ms_b / 1e3) / 1e9 / peak,
                      "plain_frac": b_alg / (ms_p / 1e3) / 1e9 / peak},
+    }
+
+
+def bench_serving(args):
+    """Serving: a pool of resident topologies under a device-memory budget (LRU), an open-loop
+    Poisson request stream with Zipf(1.1) topology popularity, half refine requests (uniform
+    level 1-4 of the topology) and half limit requests (10k-1M uniform (face, u, v) points,
+    P + dPdu + dPdv); latency = submit -> results in pinned host memory.  The continuous-
+    batching server vs the same server serving one request at a time through the plain entry
+    points, on the same traces."""
+    import torch
+
+    from opensubdiv_gb300 import workloads
+    from opensubdiv_gb300.server import LIMIT, REFINE, GB300Server
+
+    t0 = time.time()
+    pool = workloads.serving_pool(n_topologies=args.serve_topologies,
+                                  cv_max=args.batch_cv_max)
+    gen_s = time.time() - t0
+    rng = np.random.default_rng(31337)
+    # host inputs: per-topology control values, shared query windows, an output ring
+    cvs = [torch.from_numpy(workloads.serving_control_values(t, seed=t["id"])).pin_memory()
+           for t in pool]
+    max_pts = 1_000_000
+    uq, vq = (torch.from_numpy(rng.random(max_pts).astype(np.float32)).pin_memory()
+              for _ in range(2))
+    ut, vt = uq.clone().pin_memory(), vq.clone().pin_memory()
+    fold = (ut + vt) > 1.0
+    ut[fold], vt[fold] = 1.0 - ut[fold], 1.0 - vt[fold]
+    faces = {}
+    for t in pool:
+        key = (t["scheme"], t["copies"])
+        if key not in faces:
+            faces[key] = torch.from_numpy(rng.integers(0, t["num_ptex"], max_pts)
+                                          .astype(np.int32)).pin_memory()
+    ring = torch.empty(args.serve_ring_mb << 18, pin_memory=True)  # floats
+    ring_pos = [0]
+
+    def out_slot(n):
+        if ring_pos[0] + n > ring.numel():
+            ring_pos[0] = 0
+        s = ring[ring_pos[0]:ring_pos[0] + n]
+        ring_pos[0] += (n + 63) // 64 * 64
+        return s
+
+    zipf = 1.0 / np.arange(1, len(pool) + 1) ** 1.1
+    zipf /= zipf.sum()
+    rank_to_topo = rng.permutation(len(pool))
+
+    def trace(n, rate, seed):
+        r = np.random.default_rng(seed)
+        arrivals = np.cumsum(r.exponential(1.0 / rate, n))
+        arrivals -= arrivals[0]
+        topo = rank_to_topo[r.choice(len(pool), n, p=zipf)]
+        kinds = np.where(r.random(n) < 0.5, REFINE, LIMIT)
+        pts = np.exp(r.uniform(np.log(10_000), np.log(max_pts), n)).astype(np.int64)
+        reqs, work = [], 0
+        for k in range(n):
+            t = pool[topo[k]]
+            if kinds[k] == REFINE:
+                out = out_slot(len(t["refine"]["sizes"]) * t["length"])
+                reqs.append(GB300Server.request(t["id"], REFINE, cvs[t["id"]], out))
+                work += len(t["refine"]["sizes"])
+            else:
+                m = int(pts[k])
+                tri = t["base"].triangular
+                f = faces[(t["scheme"], t["copies"])][:m]
+                u = (ut if tri else uq)[:m]
+                v = (vt if tri else vq)[:m]
+                reqs.append(GB300Server.request(t["id"], LIMIT, cvs[t["id"]], out_slot(9 * m),
+                                                f, u, v))
+                work += m
+        return reqs, arrivals, work
+
+    def serve(plain):
+        srv = GB300Server(int(args.serve_budget_gb * (1 << 30)), 16 << 30,
+                          streams=1 if plain else 4, max_requests_per_round=64, plain=plain,
+                          pin_host_tables=True)
+        for t in pool:
+            srv.add_topology(t["id"], t["num_control"], t["length"], t["refine"], t["limit"])
+        reqs, arr, _ = trace(args.serve_requests // 2, 5000.0, 7)  # warm-up: hot set resident
+        srv.replay(reqs, arr)
+        s0 = srv.stats()
+        res = []
+        for rate in args.serve_rates:
+            reqs, arr, work = trace(args.serve_requests, rate, 1000 + int(rate))
+            t1 = time.perf_counter()
+            lat = srv.replay(reqs, arr)
+            wall = time.perf_counter() - t1
+            res.append({"offered_req_per_s": rate, "requests": len(reqs),
+                        "achieved_req_per_s": len(reqs) / wall,
+                        "evals_per_s": work / wall,
+                        "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3),
+                                       "p99": float(np.percentile(lat, 99) * 1e3),
+                                       "mean": float(lat.mean() * 1e3)}})
+        s1 = srv.stats()
+        srv.close()
+        return res, {k: s1[k] - s0[k] for k in ("rounds", "uploads", "evictions",
+                                                 "completed", "failed")} | {
+            "peak_resident_gb": s1["peakResidentBytes"] / 1e9}
+
+    batched, bstats = serve(False)
+    plain, pstats = serve(True)
+    table_gb = sum(len(t["refine"]["indices"]) * 8 + len(t["limit"]["pp_indices"]) * 8
+                   + len(t["limit"]["patch_indices"]) * 4 for t in pool) / 1e9
+    return {
+        "workload": f"{len(pool)} topologies (CVs log-uniform [500, {args.batch_cv_max}], "
+                    "70% Catmull-Clark / 30% Loop, refine level 1-4, 3-12 primvars), "
+                    f"Zipf(1.1) popularity, Poisson arrivals, 50% refine / 50% limit "
+                    f"(10k-1M points, P+du+dv), {args.serve_budget_gb} GB table budget",
+        "pool_table_gb": table_gb, "generation_s": gen_s,
+        "latency_definition": "submit -> results in pinned host memory",
+        "batched": {"per_rate": batched, "stats": bstats},
+        "plain_one_at_a_time": {"per_rate": plain, "stats": pstats},
     }
 
 
@@ -580,6 +702,8 @@ def run_gb300(args, rank, world):
         line["eval_patches"] = bench_patches(args, stream, peak)
     if not args.no_batch:
         line["batching"] = bench_batch(args, stream, peak)
+    if not args.no_serving:
+        line["serving"] = bench_serving(args)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, el = cpu_rate(w, args.cpu_seconds, threads)

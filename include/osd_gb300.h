@@ -226,6 +226,89 @@ int GB300StencilBatchGetConfig(const GB300StencilBatch *batch, int *tileStencils
  * synchronous. */
 int GB300StencilBatchGetDeviceStatus(GB300StencilBatch *batch, int *status);
 
+/* ---- serving loop (no counterpart in the reference) --------------------------------------- */
+
+/* A request server for many topologies: keeps their stencil and patch tables resident in a
+ * fixed device-memory budget (least-recently-used topologies are evicted and re-uploaded on
+ * demand), batches the refine and limit-evaluation requests that are pending when a stream
+ * frees up into one round (one batched stencil launch + PatchMap/EvalPatches per limit
+ * request), and overlaps rounds on several streams.  Requests carry HOST control values and
+ * receive HOST results; pinned host memory keeps the copies asynchronous.  All device memory
+ * (table pool + request arena) is allocated by GB300ServerCreate. */
+typedef struct GB300Server GB300Server;
+
+enum { GB300_REQUEST_REFINE = 0, GB300_REQUEST_LIMIT = 1 };
+
+typedef struct {
+    size_t tableBudgetBytes;  /* device bytes for resident topologies (LRU-evicted) */
+    size_t arenaBytes;        /* device bytes for the inputs/outputs of requests in flight */
+    int streams;              /* rounds in flight, one stream each */
+    int maxRequestsPerRound;
+    int plain;                /* 1: one request at a time through the plain entry points */
+    int pinHostTables;        /* 1: page-lock each topology's host arrays when it is added
+                                 (cudaHostRegister), so uploads after an eviction are
+                                 asynchronous; arrays shared by several topologies are
+                                 registered once */
+} GB300ServerConfig;
+
+/* A topology's tables, as HOST arrays that must stay valid while the server exists (they are
+ * re-uploaded after an eviction).  Refine: a Far-layout stencil table over the numControl
+ * control vertices (each `length` floats).  Limit (optional, numPatchArrays = 0 disables it):
+ * the patch points -- every point the patch table indexes -- as stencils over the control
+ * vertices' first 3 floats (patch point k = stencil k), and the flattened patch table
+ * (Osd::CpuPatchTable layout, as GB300PatchTableCreate takes it). */
+typedef struct {
+    int numControl;
+    int length;
+    int numStencils;
+    int64_t nnz;
+    const int *sizes, *offsets, *indices;
+    const float *weights;
+    int numPatchPoints;
+    int64_t patchPointNnz;
+    const int *ppSizes, *ppOffsets, *ppIndices;
+    const float *ppWeights;
+    int numPatchArrays;
+    const void *patchArrays;
+    int64_t numPatchIndices;
+    const int *patchIndices;
+    int numPatches;
+    const void *patchParams;
+    int triangular;
+} GB300TopologyDesc;
+
+/* One request.  REFINE: out = numStencils x length floats (the refined points).  LIMIT:
+ * numPoints (ptex face, u, v) queries; out = P, dPdu, dPdv, each numPoints x 3 floats, one
+ * after the other (a query that misses the patch map gives zeros). */
+typedef struct {
+    int topology;
+    int kind;
+    const float *controlValues;
+    float *out;
+    int numPoints;
+    const int *faces;
+    const float *u, *v;
+} GB300Request;
+
+typedef struct {
+    uint64_t submitted, completed, failed, rounds, uploads, evictions;
+    uint64_t bytesUploaded, residentBytes, peakResidentBytes;
+} GB300ServerStats;
+
+GB300Server *GB300ServerCreate(const GB300ServerConfig *config);
+/* Finishes every submitted request, then frees the server. */
+void GB300ServerDestroy(GB300Server *server);
+int GB300ServerAddTopology(GB300Server *server, int id, const GB300TopologyDesc *desc);
+/* Queues a request (thread-safe); its buffers must stay valid until it completes. */
+int GB300ServerSubmit(GB300Server *server, const GB300Request *request, uint64_t *ticket);
+/* Blocks until the request completed; latency = submit -> results in host memory. */
+int GB300ServerWait(GB300Server *server, uint64_t ticket, double *latencySeconds);
+/* Open-loop load: submits request i at arrivalSeconds[i] after the call starts, waits for
+ * all, and writes each request's latency. */
+int GB300ServerReplay(GB300Server *server, int n, const GB300Request *requests,
+                      const double *arrivalSeconds, double *latencySeconds);
+int GB300ServerGetStats(GB300Server *server, GB300ServerStats *stats);
+
 /* ---- batched EvalStencils that allocates nothing (no counterpart in the reference) -------- */
 
 /* For callers that cannot allocate: a renderer running under a fixed device-memory budget or

@@ -56,6 +56,13 @@ _PROTOS = {
     "GB300StencilBatchGetConfig": (i32, [vp, vp, vp, vp, vp]),
     "GB300StencilBatchGetDeviceStatus": (i32, [vp, vp]),
     "GB300EvalStencilsBatchedNoAlloc": (i32, [i32] + [vp] * 11),
+    "GB300ServerCreate": (vp, [vp]),
+    "GB300ServerDestroy": (None, [vp]),
+    "GB300ServerAddTopology": (i32, [vp, i32, vp]),
+    "GB300ServerSubmit": (i32, [vp, vp, vp]),
+    "GB300ServerWait": (i32, [vp, u64, vp]),
+    "GB300ServerReplay": (i32, [vp, i32, vp, vp, vp]),
+    "GB300ServerGetStats": (i32, [vp, vp]),
 }
 
 

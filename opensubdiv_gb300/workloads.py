@@ -165,3 +165,140 @@ def deform(base, phase, frame, amplitude=0.01):
     phase + 7 base), with the mesh's phase (works on numpy arrays and torch tensors)."""
     lib = np if isinstance(base, np.ndarray) else __import__("torch")
     return base + amplitude * lib.sin(0.1 * frame + phase + 7.0 * base)
+
+
+# ---- serving pool ----------------------------------------------------------------------------
+
+SERVING_BASES = {shapes.CATMARK: "torus32x16_patches_L4.npz", shapes.LOOP: "icosphere2_patches_L3.npz"}
+
+
+def _golden(name):
+    import os
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests",
+                        "golden", name)
+
+
+def sort_entries(table):
+    """Far-layout table with every stencil's entries in ascending control-index order (the
+    device layout GB300StencilTableCreate uses; same stencils, better gather locality)."""
+    sizes, offsets = table["sizes"], table["offsets"]
+    row = np.repeat(np.arange(len(sizes)), sizes)
+    pos = np.concatenate([np.arange(o, o + s) for o, s in zip(offsets, sizes)]) if len(sizes) \
+        else np.zeros(0, np.int64)
+    order = np.lexsort((table["indices"][pos], row))
+    pos = pos[order]
+    new_off = np.concatenate([[0], np.cumsum(sizes)[:-1]]).astype(np.int32)
+    return dict(sizes=sizes.astype(np.int32), offsets=new_off,
+                indices=table["indices"][pos].astype(np.int32),
+                weights=table["weights"][pos].astype(np.float32))
+
+
+def instance_table(table, copies, src_per_copy):
+    """`copies` disjoint copies of a stencil table: copy c reads source rows offset by
+    c * src_per_copy and produces rows c * numStencils + i."""
+    n, nnz = len(table["sizes"]), len(table["indices"])
+    c = np.arange(copies, dtype=np.int64)
+    return dict(sizes=np.tile(table["sizes"], copies),
+                offsets=(table["offsets"][None, :] + (c * nnz)[:, None]).astype(np.int32).ravel(),
+                indices=(table["indices"][None, :] + (c * src_per_copy)[:, None])
+                .astype(np.int32).ravel(),
+                weights=np.tile(table["weights"], copies))
+
+
+class ServingBase:
+    """One base shape of the serving pool: the reference's adaptive patch table of a small
+    cage (tests/golden fixture) with its patch points' stencils over the cage, and uniform
+    refinement tables of the same cage from the native generator (one per level, cached)."""
+
+    def __init__(self, scheme):
+        z = np.load(_golden(SERVING_BASES[scheme]))
+        self.scheme = scheme
+        self.fixture = _golden(SERVING_BASES[scheme])
+        self.cage = shapes.Cage(z["positions"], z["verts_per_face"], z["face_verts"],
+                                scheme=int(z["scheme"]), name=f"base{int(z['scheme'])}")
+        self.cage.crease_verts = z["crease_verts"]
+        self.cage.crease_sharpness = z["crease_sharpness"]
+        self.nc = len(z["positions"])
+        self.ns = len(z["ps_sizes"])
+        self.nptex = int(z["num_ptex"])
+        self.triangular = bool(z["triangular"])
+        # patch source of one copy = [cage points (identity stencils); patch points]
+        eye = dict(sizes=np.ones(self.nc, np.int32), offsets=np.arange(self.nc, dtype=np.int32),
+                   indices=np.arange(self.nc, dtype=np.int32), weights=np.ones(self.nc, np.float32))
+        ps = dict(sizes=z["ps_sizes"], offsets=z["ps_offsets"] + self.nc, indices=z["ps_indices"],
+                  weights=z["ps_weights"])
+        self.pp = sort_entries({k: np.concatenate([eye[k], ps[k]]) for k in eye})
+        self._refine = {}
+        self._patch = {}
+
+    def refine(self, level):
+        if level not in self._refine:
+            self._refine[level] = sort_entries(UniformRefiner(self.cage, level).stencil_table())
+        return self._refine[level]
+
+    def patch_table(self, copies):
+        if copies not in self._patch:
+            arrays, indices, params, _, nptex, tri = instanced_patch_table(self.fixture, copies)
+            self._patch[copies] = (arrays, indices, params, nptex)
+        return self._patch[copies]
+
+
+def serving_pool(n_topologies=1000, cv_min=500, cv_max=25_000, seed=5150):
+    """Topologies for the serving loop, drawn like the batching population: CV counts
+    log-uniform in [cv_min, cv_max], 70% Catmull-Clark / 30% Loop, uniform refinement level
+    uniform in {1..4}, 3-12 float32 primvars.  Topology = `copies` instances of a base cage
+    (ServingBase: the 512-CV crease/triangle torus for Catmull-Clark, the 162-CV icosphere for
+    Loop) with copies = CV target / base CVs rounded to a log-spaced set (so host tables are
+    shared between topologies of the same (base, copies, level); every topology still has its
+    own device copy when resident).  Each has a refine table at its level and limit tables
+    (patch points as stencils over the cage's xyz + the instanced adaptive patch table)."""
+    rng = np.random.default_rng(seed)
+    steps = np.array([1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192], np.int64)
+    bases = {s: ServingBase(s) for s in SERVING_BASES}
+    cache = {}
+    pool = []
+    for t in range(n_topologies):
+        scheme = shapes.LOOP if rng.random() < 0.3 else shapes.CATMARK
+        b = bases[scheme]
+        cv = float(np.exp(rng.uniform(np.log(cv_min), np.log(cv_max))))
+        copies = int(steps[np.argmin(np.abs(np.log(steps) - np.log(max(cv / b.nc, 1.0))))])
+        level = int(rng.integers(1, 5))
+        length = int(rng.integers(3, 13))
+        key = (scheme, copies, level)
+        if key not in cache:
+            refine = instance_table(b.refine(level), copies, b.nc)
+            arrays, pidx, params, nptex = b.patch_table(copies)
+            pp = instance_table(b.pp, copies, b.nc)
+            cache[key] = dict(refine=refine, limit=dict(
+                pp_sizes=pp["sizes"], pp_offsets=pp["offsets"], pp_indices=pp["indices"],
+                pp_weights=pp["weights"], arrays=arrays, patch_indices=pidx, params=params,
+                triangular=b.triangular), num_ptex=nptex)
+        c = cache[key]
+        pool.append(dict(id=t, scheme=scheme, copies=copies, level=level, length=length,
+                         num_control=copies * b.nc, refine=c["refine"], limit=c["limit"],
+                         num_ptex=c["num_ptex"], base=b))
+    return pool
+
+
+def serving_control_values(topo, seed):
+    """Deformed control values of a pool topology: the base cage positions of every copy
+    (copy c shifted by 3c along x) plus U[-1, 1] channels, float32 [numControl x length]."""
+    b = topo["base"]
+    rng = np.random.default_rng(seed)
+    pos = np.tile(b.cage.positions, (topo["copies"], 1)).astype(np.float64)
+    pos[:, 0] += np.repeat(np.arange(topo["copies"]) * 3.0, b.nc)
+    pos += rng.normal(0.0, 0.002, pos.shape)
+    extra = rng.uniform(-1, 1, (len(pos), topo["length"] - 3))
+    return np.ascontiguousarray(np.concatenate([pos, extra], 1).astype(np.float32).ravel())
+
+
+def serving_queries(topo, n, seed):
+    """n uniform (ptex face, u, v) queries (Loop: folded into u + v <= 1)."""
+    rng = np.random.default_rng(seed)
+    face = rng.integers(0, topo["num_ptex"], n).astype(np.int32)
+    u = rng.random(n).astype(np.float32)
+    v = rng.random(n).astype(np.float32)
+    if topo["base"].triangular:
+        f = u + v > 1.0
+        u[f], v[f] = 1.0 - u[f], 1.0 - v[f]
+    return face, u, v

@@ -153,6 +153,10 @@ def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3):
     out.update(level=np.int32(level), adaptive=np.int32(adaptive), endcap=np.int32(endcap),
                arrays=p.arrays, patch_indices=p.indices, params=p.params,
                num_local_points=np.int32(p.num_local_points), src=buf,
+               # the patch points' stencils over the cage (all refinement levels + local
+               # points): src[nc:] = these stencils applied to src[:nc]
+               ps_sizes=p.st["sizes"], ps_offsets=p.st["offsets"], ps_indices=p.st["indices"],
+               ps_weights=p.st["weights"],
                num_ptex=np.int32(nptex), q_face=faces, q_u=u, q_v=v, q_handles=handles,
                q_found=found, coords=coords, out6=np.stack(outs).reshape(6, -1, 3),
                out6_fp64=fp64.transpose(1, 0, 2).copy(),
