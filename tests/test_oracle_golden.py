@@ -105,6 +105,21 @@ def test_eval_patches_bitwise_and_fp64(path):
         assert np.array_equal(outd[k], z["out6_fp64"][k].ravel()), k
 
 
+@pytest.mark.parametrize("path", PATCH_FIXTURES, ids=os.path.basename)
+def test_patch_point_stencils_reproduce_the_patch_source(path):
+    """The patch points' stencils over the cage (stored with each patch fixture) reproduce the
+    patch source the reference computed in place: src[nc:] = stencils applied to src[:nc]."""
+    z = np.load(path)
+    nc = len(z["positions"])
+    n = len(z["ps_sizes"])
+    assert len(z["src"]) == 3 * (nc + n)
+    assert n == 0 or int(z["ps_indices"].max()) < nc  # factorized to the cage
+    out = np.zeros(n * 3, np.float32)
+    oracle.eval_stencils(z["src"][: nc * 3], (0, 3, 3), [out], [(0, 3, 3)], z["ps_sizes"],
+                         z["ps_offsets"], z["ps_indices"], [z["ps_weights"]])
+    assert np.array_equal(out, z["src"][nc * 3:])
+
+
 def test_descriptor_length_mismatch_is_rejected():
     """CpuEvaluator returns false when a destination length differs from the source's
     (osd/cpuEvaluator.cpp:46-47)."""
