@@ -70,6 +70,19 @@ __device__ __forceinline__ float ld_src(const float *p, uint64_t pol) {
     return v;
 }
 
+__device__ __forceinline__ int ld_keep(const int *p, uint64_t pol) {
+    int v;
+    asm("ld.global.nc.L2::cache_hint.b32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int4 ld_keep4(const int *p, uint64_t pol) {
+    int4 v;
+    asm("ld.global.nc.L2::cache_hint.v4.b32 {%0, %1, %2, %3}, [%4], %5;"
+        : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+        : "l"(p), "l"(pol));
+    return v;
+}
+
 // Streaming stores for outputs (written once, not re-read by this launch).
 __device__ __forceinline__ void st_stream(float *p, float v) {
     asm volatile("st.global.cs.f32 [%0], %1;" ::"l"(p), "f"(v) : "memory");

@@ -45,28 +45,34 @@ struct Acc6 {
     }
 };
 
+// Source points, patch index rows and params are gathered at random and re-read by every
+// query that lands on the same patch: they are loaded with an evict-last L2 policy, so the
+// streams read or written once (query coords, outputs) do not push them out of L2.
+
 // Loads LC elements [e0, e0+LC) of control point `cv` (elements >= length read as 0).
 template <int LC>
 __device__ __forceinline__ void load_row(const float *__restrict__ src, int stride, int cv,
                                          int e0, int length, float (&x)[LC]) {
     const float *p = src + (size_t)cv * stride + e0;
+    const uint64_t pol = l2_evict_last();
 #pragma unroll
-    for (int c = 0; c < LC; ++c) x[c] = (e0 + c < length) ? __ldg(p + c) : 0.0f;
+    for (int c = 0; c < LC; ++c) x[c] = (e0 + c < length) ? ld_src(p + c, pol) : 0.0f;
 }
 
 // N control-point indices of a patch: 128-bit loads when the index row is 16-byte aligned
 // (REGULAR rows are 64 B, GREGORY_BASIS rows 80 B), scalar loads otherwise.
 template <int N>
 __device__ __forceinline__ void load_indices(const int *__restrict__ cvs, int (&idx)[N]) {
+    const uint64_t pol = l2_evict_last();
     if ((N % 4) == 0 && (reinterpret_cast<uintptr_t>(cvs) & 15) == 0) {
 #pragma unroll
         for (int j = 0; j < N / 4; ++j) {
-            const int4 v = __ldg(reinterpret_cast<const int4 *>(cvs) + j);
+            const int4 v = ld_keep4(cvs + 4 * j, pol);
             idx[4 * j] = v.x; idx[4 * j + 1] = v.y; idx[4 * j + 2] = v.z; idx[4 * j + 3] = v.w;
         }
     } else {
 #pragma unroll
-        for (int j = 0; j < N; ++j) idx[j] = __ldg(cvs + j);
+        for (int j = 0; j < N; ++j) idx[j] = ld_keep(cvs + j, pol);
     }
 }
 

@@ -20,6 +20,24 @@ struct ParamRec {
     float sharpness;
 };
 
+// A query's patch coordinate (read once: evict-first) and its patch's param (evict-last).
+__device__ __forceinline__ Coord load_coord(const Coord *p) {
+    const int *q = reinterpret_cast<const int *>(p);
+    const uint64_t pol = l2_evict_first();
+    Coord c;
+    c.arrayIndex = ld_stream(q, pol);
+    c.patchIndex = ld_stream(q + 1, pol);
+    c.vertIndex = ld_stream(q + 2, pol);
+    c.s = __int_as_float(ld_stream(q + 3, pol));
+    c.t = __int_as_float(ld_stream(q + 4, pol));
+    return c;
+}
+__device__ __forceinline__ ParamRec load_param(const ParamRec *p) {
+    const int *q = reinterpret_cast<const int *>(p);
+    const uint64_t pol = l2_evict_last();
+    return ParamRec{ld_keep(q, pol), ld_keep(q + 1, pol), __int_as_float(ld_keep(q + 2, pol))};
+}
+
 struct PatchArgs {
     const float *src;
     float *dst[6];
@@ -38,14 +56,14 @@ template <int LC>
 __global__ void __launch_bounds__(128) k_eval_patches(const PatchArgs a) {
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.numCoords; i += stride) {
-        const Coord c = a.coords[i];
+        const Coord c = load_coord(a.coords + i);
         for (int e0 = 0; e0 < a.length; e0 += LC) {
             Acc6<LC> acc;
             acc.zero();
             float d1 = 1.0f, d2 = 1.0f;
             if (c.arrayIndex >= 0) {
                 const Array arr = a.arrays[c.arrayIndex];
-                const ParamRec pr = a.params[c.patchIndex];
+                const ParamRec pr = load_param(a.params + c.patchIndex);
                 const Param p{pr.field0, pr.field1};
                 const int type = p.regular() ? arr.regDesc : arr.desc;
                 const int *cvs =
@@ -60,8 +78,8 @@ __global__ void __launch_bounds__(128) k_eval_patches(const PatchArgs a) {
                 if (!(a.active & (1 << k))) continue;
                 float *out = a.dst[k] + (size_t)i * a.dstStride[k] + e0;
 #pragma unroll
-                for (int q = 0; q < LC; ++q)
-                    if (e0 + q < a.length) st_stream(out + q, acc.v[k][q] * scale[k]);
+                for (int m = 0; m < LC; ++m)
+                    if (e0 + m < a.length) st_stream(out + m, acc.v[k][m] * scale[k]);
             }
         }
     }
@@ -85,7 +103,7 @@ __global__ void __launch_bounds__(256, 4) k_eval_patches_lanes(const PatchArgs a
     const int group = warp * kPerWarp + slot;
     const int ngroups = nwarps * kPerWarp;
     for (int i = group; i < a.numCoords; i += ngroups) {
-        const Coord c = a.coords[i];
+        const Coord c = load_coord(a.coords + i);
         for (int e0 = 0; e0 < a.length; e0 += G) {
             const int e = e0 + lane;
             Acc6<1> acc;
@@ -93,7 +111,7 @@ __global__ void __launch_bounds__(256, 4) k_eval_patches_lanes(const PatchArgs a
             float d1 = 1.0f, d2 = 1.0f;
             if (c.arrayIndex >= 0) {
                 const Array arr = a.arrays[c.arrayIndex];
-                const ParamRec pr = a.params[c.patchIndex];
+                const ParamRec pr = load_param(a.params + c.patchIndex);
                 const Param p{pr.field0, pr.field1};
                 const int type = p.regular() ? arr.regDesc : arr.desc;
                 const int *cvs =
