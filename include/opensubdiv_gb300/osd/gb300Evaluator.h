@@ -161,10 +161,31 @@ public:
     static GB300PatchTable *Create(Far::PatchTable const *farTable, void *deviceContext = NULL) {
         CpuPatchTable cpu(farTable);
         const bool tri = farTable->GetVaryingPatchDescriptor().GetNumControlVertices() == 3;
-        return Create((int)cpu.GetNumPatchArrays(), cpu.GetPatchArrayBuffer(),
-                      (int64_t)cpu.GetPatchIndexSize(), cpu.GetPatchIndexBuffer(),
-                      (int)cpu.GetPatchParamSize(), cpu.GetPatchParamBuffer(), tri,
-                      deviceContext);
+        GB300PatchTable *t = Create((int)cpu.GetNumPatchArrays(), cpu.GetPatchArrayBuffer(),
+                                    (int64_t)cpu.GetPatchIndexSize(), cpu.GetPatchIndexBuffer(),
+                                    (int)cpu.GetPatchParamSize(), cpu.GetPatchParamBuffer(), tri,
+                                    deviceContext);
+        if (!t) return nullptr;
+        void *s = gb300_detail::stream_of(deviceContext);
+        // varying and face-varying tables (osd/cpuPatchTable.cpp:75-114)
+        bool good = cpu.GetVaryingPatchIndexSize() == 0 ||
+                    GB300PatchTableSetVarying(t->_h, (int)cpu.GetNumPatchArrays(),
+                                              cpu.GetVaryingPatchArrayBuffer(),
+                                              (int64_t)cpu.GetVaryingPatchIndexSize(),
+                                              cpu.GetVaryingPatchIndexBuffer(), s) == GB300_OK;
+        for (int c = 0; good && c < cpu.GetNumFVarChannels(); ++c) {
+            int ch = -1;
+            good = GB300PatchTableAddFVarChannel(
+                       t->_h, (int)cpu.GetNumPatchArrays(), cpu.GetFVarPatchArrayBuffer(c),
+                       (int64_t)cpu.GetFVarPatchIndexSize(c), cpu.GetFVarPatchIndexBuffer(c),
+                       (int)cpu.GetFVarPatchParamSize(c), cpu.GetFVarPatchParamBuffer(c), &ch,
+                       s) == GB300_OK;
+        }
+        if (!good) {
+            delete t;
+            return nullptr;
+        }
+        return t;
     }
 #endif
     /// From a flattened host table (Osd::CpuPatchTable layout).
@@ -182,6 +203,18 @@ public:
     void *GetPatchIndexBuffer() const { return GB300PatchTableGetBuffer(_h, 1); }
     void *GetPatchParamBuffer() const { return GB300PatchTableGetBuffer(_h, 2); }
     int GetNumPatchArrays() const { return GB300PatchTableGetNumArrays(_h); }
+    void *GetVaryingPatchArrayBuffer() const { return GB300PatchTableGetVaryingBuffer(_h, 0); }
+    void *GetVaryingPatchIndexBuffer() const { return GB300PatchTableGetVaryingBuffer(_h, 1); }
+    int GetNumFVarChannels() const { return GB300PatchTableGetNumFVarChannels(_h); }
+    void *GetFVarPatchArrayBuffer(int fvarChannel = 0) const {
+        return GB300PatchTableGetFVarBuffer(_h, fvarChannel, 0);
+    }
+    void *GetFVarPatchIndexBuffer(int fvarChannel = 0) const {
+        return GB300PatchTableGetFVarBuffer(_h, fvarChannel, 1);
+    }
+    void *GetFVarPatchParamBuffer(int fvarChannel = 0) const {
+        return GB300PatchTableGetFVarBuffer(_h, fvarChannel, 2);
+    }
 
     /// Device Far::PatchMap::FindPatch for n device-resident (face, u, v) queries, writing
     /// PatchCoords (s, t = u, v) to device memory; misses get handle (-1, -1, -1).
@@ -391,6 +424,80 @@ public:
             return false;
         return gb300_detail::ok(GB300PatchTableEval(
             patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset,
+            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
+            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
+            duDesc.stride, dvDesc.stride, 0, 0, 0, numPatchCoords,
+            (const void *)patchCoords->BindCudaBuffer(), gb300_detail::stream_of(deviceContext)));
+    }
+
+    // ---- EvalPatchesVarying / EvalPatchesFaceVarying (cudaEvaluator.h:859-1255) -------------
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
+    static bool EvalPatchesVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                                   DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                                   int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
+                                   GB300PatchTable const *patchTable,
+                                   const void *instance = NULL, void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length) return false;
+        return gb300_detail::ok(GB300PatchTableEvalVarying(
+            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
+            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
+            numPatchCoords, (const void *)patchCoords->BindCudaBuffer(),
+            gb300_detail::stream_of(deviceContext)));
+    }
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
+    static bool EvalPatchesVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                                   DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                                   DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
+                                   DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
+                                   int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
+                                   GB300PatchTable const *patchTable,
+                                   const void *instance = NULL, void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
+            srcDesc.length != dvDesc.length)
+            return false;
+        return gb300_detail::ok(GB300PatchTableEvalVarying(
+            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset,
+            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
+            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
+            duDesc.stride, dvDesc.stride, 0, 0, 0, numPatchCoords,
+            (const void *)patchCoords->BindCudaBuffer(), gb300_detail::stream_of(deviceContext)));
+    }
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
+    static bool EvalPatchesFaceVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                                       DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                                       int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
+                                       GB300PatchTable const *patchTable, int fvarChannel = 0,
+                                       const void *instance = NULL,
+                                       void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length) return false;
+        return gb300_detail::ok(GB300PatchTableEvalFaceVarying(
+            patchTable->GetHandle(), fvarChannel, srcBuffer->BindCudaBuffer() + srcDesc.offset,
+            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
+            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
+            numPatchCoords, (const void *)patchCoords->BindCudaBuffer(),
+            gb300_detail::stream_of(deviceContext)));
+    }
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
+    static bool EvalPatchesFaceVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                                       DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                                       DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
+                                       DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
+                                       int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
+                                       GB300PatchTable const *patchTable, int fvarChannel = 0,
+                                       const void *instance = NULL,
+                                       void *deviceContext = NULL) {
+        (void)instance;
+        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
+            srcDesc.length != dvDesc.length)
+            return false;
+        return gb300_detail::ok(GB300PatchTableEvalFaceVarying(
+            patchTable->GetHandle(), fvarChannel, srcBuffer->BindCudaBuffer() + srcDesc.offset,
             dstBuffer->BindCudaBuffer() + dstDesc.offset,
             duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
             nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,

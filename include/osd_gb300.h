@@ -173,6 +173,39 @@ int GB300PatchTableEval(const GB300PatchTable *table, const float *src, float *d
                         int duuStride, int duvStride, int dvvStride, int numPatchCoords,
                         const void *patchCoords, void *stream);
 
+/* Varying and face-varying patch tables (CudaPatchTable's varying / fvar buffers,
+ * osd/cudaPatchTable.h:51-110, flattened as osd/cpuPatchTable.cpp:75-114).  Both describe the
+ * vertex table's patches -- the same arrays with the same patch counts and first patches -- so
+ * the vertex PatchMap's coords index them.  Varying patches use the vertex patch params; each
+ * face-varying channel has its own params (numParams = the vertex table's numPatches).
+ * HOST arrays in, as for GB300PatchTableCreate.  AddFVarChannel writes the channel index. */
+int GB300PatchTableSetVarying(GB300PatchTable *table, int numArrays, const void *patchArrays,
+                              int64_t numIndices, const int *patchIndices, void *stream);
+int GB300PatchTableAddFVarChannel(GB300PatchTable *table, int numArrays, const void *patchArrays,
+                                  int64_t numIndices, const int *patchIndices, int numParams,
+                                  const void *patchParams, int *channel, void *stream);
+int GB300PatchTableGetNumFVarChannels(const GB300PatchTable *table);
+/* which: 0 patch arrays, 1 patch indices (NULL when no varying table was set). */
+void *GB300PatchTableGetVaryingBuffer(const GB300PatchTable *table, int which);
+/* which: 0 patch arrays, 1 patch indices, 2 patch params of face-varying `channel`. */
+void *GB300PatchTableGetFVarBuffer(const GB300PatchTable *table, int channel, int which);
+
+/* CudaEvaluator::EvalPatchesVarying (osd/cudaEvaluator.h:859-1060): EvalPatches over the
+ * varying arrays / indices with the vertex patch params. */
+int GB300PatchTableEvalVarying(const GB300PatchTable *table, const float *src, float *dst,
+                               float *du, float *dv, float *duu, float *duv, float *dvv,
+                               int length, int srcStride, int dstStride, int duStride,
+                               int dvStride, int duuStride, int duvStride, int dvvStride,
+                               int numPatchCoords, const void *patchCoords, void *stream);
+/* CudaEvaluator::EvalPatchesFaceVarying (osd/cudaEvaluator.h:1070-1255): EvalPatches over
+ * face-varying channel `channel` (its arrays, indices and params). */
+int GB300PatchTableEvalFaceVarying(const GB300PatchTable *table, int channel, const float *src,
+                                   float *dst, float *du, float *dv, float *duu, float *duv,
+                                   float *dvv, int length, int srcStride, int dstStride,
+                                   int duStride, int dvStride, int duuStride, int duvStride,
+                                   int dvvStride, int numPatchCoords, const void *patchCoords,
+                                   void *stream);
+
 /* ---- vertex buffer (CudaVertexBuffer, osd/cudaVertexBuffer.h:42-79) ---------------------- */
 
 typedef struct GB300VertexBuffer GB300VertexBuffer;

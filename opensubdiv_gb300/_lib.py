@@ -42,6 +42,13 @@ _PROTOS = {
     "GB300PatchTableGetNumPatches": (i32, [vp]),
     "GB300PatchTableFindPatches": (i32, [vp, i32, vp, vp, vp, vp, vp]),
     "GB300PatchTableEval": (i32, [vp, vp] + [vp] * 6 + [i32] * 8 + [i32, vp, vp]),
+    "GB300PatchTableSetVarying": (i32, [vp, i32, vp, i64, vp, vp]),
+    "GB300PatchTableAddFVarChannel": (i32, [vp, i32, vp, i64, vp, i32, vp, vp, vp]),
+    "GB300PatchTableGetNumFVarChannels": (i32, [vp]),
+    "GB300PatchTableGetVaryingBuffer": (vp, [vp, i32]),
+    "GB300PatchTableGetFVarBuffer": (vp, [vp, i32, i32]),
+    "GB300PatchTableEvalVarying": (i32, [vp, vp] + [vp] * 6 + [i32] * 8 + [i32, vp, vp]),
+    "GB300PatchTableEvalFaceVarying": (i32, [vp, i32, vp] + [vp] * 6 + [i32] * 8 + [i32, vp, vp]),
     "GB300VertexBufferCreate": (vp, [i32, i32]),
     "GB300VertexBufferDestroy": (None, [vp]),
     "GB300VertexBufferUpdateData": (i32, [vp, vp, i32, i32, vp]),

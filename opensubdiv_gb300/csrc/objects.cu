@@ -158,18 +158,38 @@ bool evaluation_order(int n, int64_t nnz, const int *sizes, const int *offsets,
 
 }  // namespace
 
+// A varying or face-varying (arrays, indices[, params]) set evaluated with the vertex table's
+// patch handles (osd/cpuPatchTable.cpp:75-114).
+struct PatchSet {
+    int numArrays = 0, numParams = 0;
+    int quadFamily = 0;
+    int64_t numIndices = 0;
+    void *arrays = nullptr, *indices = nullptr, *params = nullptr;
+    void free() {
+        release(arrays);
+        release(indices);
+        release(params);
+        numArrays = 0;
+    }
+};
+
 struct GB300PatchTable {
     int numArrays = 0, numPatches = 0;
     int quadFamily = 0;  // all arrays REGULAR / GREGORY_BASIS / QUADS
     int64_t numIndices = 0;
     void *arrays = nullptr, *indices = nullptr, *params = nullptr;
     PatchMapDevice map;
+    std::vector<int> hostArrays;  // 6 ints per array (validation of varying / fvar sets)
+    PatchSet varying;
+    std::vector<PatchSet> fvar;
     ~GB300PatchTable() {
         release(arrays);
         release(indices);
         release(params);
         release(map.nodes);
         release(map.handles);
+        varying.free();
+        for (PatchSet &f : fvar) f.free();
     }
 };
 
@@ -292,6 +312,90 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
                          as_stream(stream), "GB300StencilTableEval");
 }
 
+namespace {
+
+// Patch arrays reference only evaluable types and stay inside the index / param buffers.
+int check_patch_arrays(const char *who, int numArrays, const int *arr, int64_t numIndices,
+                       int numPatches) {
+    for (int a = 0; a < numArrays; ++a) {
+        for (int k = 0; k < 2; ++k) {
+            const int type = arr[6 * a + k];
+            if (type != GB300_PATCH_QUADS && type != GB300_PATCH_TRIANGLES &&
+                type != GB300_PATCH_LOOP && type != GB300_PATCH_REGULAR &&
+                type != GB300_PATCH_GREGORY_BASIS && type != GB300_PATCH_GREGORY_TRIANGLE)
+                return fail(GB300_ERR_UNSUPPORTED, "%s: patch type %d in array %d", who, type, a);
+        }
+        const int64_t last =
+            (int64_t)arr[6 * a + 3] + (int64_t)arr[6 * a + 4] * arr[6 * a + 2];
+        if (last > numIndices || arr[6 * a + 5] < 0 ||
+            arr[6 * a + 5] + (int64_t)arr[6 * a + 2] > numPatches)
+            return fail(GB300_ERR_INVALID_ARGUMENT, "%s: array %d out of range", who, a);
+    }
+    return GB300_OK;
+}
+
+int quad_family(int numArrays, const int *arr) {
+    int q = numArrays > 0;
+    for (int a = 0; a < numArrays; ++a)
+        for (int k = 0; k < 2; ++k) {
+            const int type = arr[6 * a + k];
+            if (type != GB300_PATCH_REGULAR && type != GB300_PATCH_GREGORY_BASIS &&
+                type != GB300_PATCH_QUADS)
+                q = 0;
+        }
+    return q;
+}
+
+// A varying / face-varying set must describe the vertex table's patches: same arrays, same
+// patch counts and first patch of each array, so the vertex patch handles index it.
+int make_set(GB300PatchTable *t, const char *who, int numArrays, const void *patchArrays,
+             int64_t numIndices, const int *patchIndices, int numParams, const void *params,
+             cudaStream_t s, PatchSet &out) {
+    if (!t || numArrays != t->numArrays || numIndices < 0 ||
+        (numArrays > 0 && (!patchArrays || (numIndices > 0 && !patchIndices))))
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
+    const int *arr = (const int *)patchArrays;
+    for (int a = 0; a < numArrays; ++a)
+        if (arr[6 * a + 2] != t->hostArrays[6 * a + 2] ||
+            arr[6 * a + 5] != t->hostArrays[6 * a + 5])
+            return fail(GB300_ERR_INVALID_ARGUMENT,
+                        "%s: array %d does not match the vertex patch array", who, a);
+    const int patches = params ? numParams : t->numPatches;
+    if (params && numParams != t->numPatches)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: %d params for %d patches", who, numParams,
+                    t->numPatches);
+    int st = check_patch_arrays(who, numArrays, arr, numIndices, patches);
+    if (st != GB300_OK) return st;
+    PatchSet set;
+    set.numArrays = numArrays;
+    set.numIndices = numIndices;
+    set.numParams = params ? numParams : 0;
+    set.quadFamily = quad_family(numArrays, arr);
+    if (!upload(&set.arrays, patchArrays, (size_t)numArrays * 24, s, who) ||
+        !upload(&set.indices, patchIndices, (size_t)numIndices * 4, s, who) ||
+        (params && !upload(&set.params, params, (size_t)numParams * 12, s, who)) ||
+        check_cuda(cudaStreamSynchronize(s), who) != GB300_OK) {
+        set.free();
+        return GB300_ERR_OUT_OF_MEMORY;
+    }
+    out = set;
+    return ok();
+}
+
+int eval_set(const GB300PatchTable *t, const PatchSet &set, const void *params,
+             const float *src, float *dst, float *du, float *dv, float *duu, float *duv,
+             float *dvv, int length, int srcStride, int dstStride, int duStride, int dvStride,
+             int duuStride, int duvStride, int dvvStride, int n, const void *coords,
+             void *stream, const char *who) {
+    float *d[6] = {dst, du, dv, duu, duv, dvv};
+    const int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
+    return eval_patches(src, d, st, length, srcStride, n, coords, set.arrays,
+                        (const int *)set.indices, params, as_stream(stream), who,
+                        set.quadFamily);
+}
+
+}  // namespace
+
 GB300PatchTable *GB300PatchTableCreate(int numArrays, const void *patchArrays,
                                        int64_t numIndices, const int *patchIndices,
                                        int numPatches, const void *patchParams, int triangular,
@@ -303,25 +407,9 @@ GB300PatchTable *GB300PatchTableCreate(int numArrays, const void *patchArrays,
         return nullptr;
     }
     const int *arr = (const int *)patchArrays;
-    for (int a = 0; a < numArrays; ++a) {
-        for (int k = 0; k < 2; ++k) {
-            const int type = arr[6 * a + k];
-            if (type != GB300_PATCH_QUADS && type != GB300_PATCH_TRIANGLES &&
-                type != GB300_PATCH_LOOP && type != GB300_PATCH_REGULAR &&
-                type != GB300_PATCH_GREGORY_BASIS && type != GB300_PATCH_GREGORY_TRIANGLE) {
-                fail(GB300_ERR_UNSUPPORTED, "GB300PatchTableCreate: patch type %d in array %d",
-                     type, a);
-                return nullptr;
-            }
-        }
-        const int64_t last =
-            (int64_t)arr[6 * a + 3] + (int64_t)arr[6 * a + 4] * arr[6 * a + 2];
-        if (last > numIndices || arr[6 * a + 5] < 0 ||
-            arr[6 * a + 5] + (int64_t)arr[6 * a + 2] > numPatches) {
-            fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableCreate: array %d out of range", a);
-            return nullptr;
-        }
-    }
+    if (check_patch_arrays("GB300PatchTableCreate", numArrays, arr, numIndices, numPatches) !=
+        GB300_OK)
+        return nullptr;
     PatchMapHost hm;
     if (build_patch_map(numArrays, arr, numPatches, (const int *)patchParams, triangular, hm) !=
         GB300_OK)
@@ -335,14 +423,8 @@ GB300PatchTable *GB300PatchTableCreate(int numArrays, const void *patchArrays,
     t->numArrays = numArrays;
     t->numPatches = numPatches;
     t->numIndices = numIndices;
-    t->quadFamily = numArrays > 0;
-    for (int a = 0; a < numArrays; ++a)
-        for (int k = 0; k < 2; ++k) {
-            const int type = arr[6 * a + k];
-            if (type != GB300_PATCH_REGULAR && type != GB300_PATCH_GREGORY_BASIS &&
-                type != GB300_PATCH_QUADS)
-                t->quadFamily = 0;
-        }
+    t->quadFamily = quad_family(numArrays, arr);
+    t->hostArrays.assign(arr, arr + 6 * (size_t)numArrays);
     const char *w = "GB300PatchTableCreate";
     if (!upload(&t->arrays, patchArrays, (size_t)numArrays * 24, s, w) ||
         !upload(&t->indices, patchIndices, (size_t)numIndices * 4, s, w) ||
@@ -390,6 +472,75 @@ int GB300PatchTableEval(const GB300PatchTable *t, const float *src, float *dst, 
     return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, t->arrays,
                         (const int *)t->indices, t->params, as_stream(stream),
                         "GB300PatchTableEval", t->quadFamily);
+}
+
+int GB300PatchTableSetVarying(GB300PatchTable *t, int numArrays, const void *patchArrays,
+                              int64_t numIndices, const int *patchIndices, void *stream) {
+    PatchSet set;
+    const int st = make_set(t, "GB300PatchTableSetVarying", numArrays, patchArrays, numIndices,
+                            patchIndices, 0, nullptr, as_stream(stream), set);
+    if (st != GB300_OK) return st;
+    t->varying.free();
+    t->varying = set;
+    return ok();
+}
+
+int GB300PatchTableAddFVarChannel(GB300PatchTable *t, int numArrays, const void *patchArrays,
+                                  int64_t numIndices, const int *patchIndices, int numParams,
+                                  const void *patchParams, int *channel, void *stream) {
+    if (!patchParams || !channel)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableAddFVarChannel: null params");
+    PatchSet set;
+    const int st = make_set(t, "GB300PatchTableAddFVarChannel", numArrays, patchArrays,
+                            numIndices, patchIndices, numParams, patchParams, as_stream(stream),
+                            set);
+    if (st != GB300_OK) return st;
+    t->fvar.push_back(set);
+    *channel = (int)t->fvar.size() - 1;
+    return ok();
+}
+
+int GB300PatchTableGetNumFVarChannels(const GB300PatchTable *t) {
+    return t ? (int)t->fvar.size() : 0;
+}
+
+void *GB300PatchTableGetVaryingBuffer(const GB300PatchTable *t, int which) {
+    if (!t || !t->varying.arrays) return nullptr;
+    return which == 0 ? t->varying.arrays : which == 1 ? t->varying.indices : nullptr;
+}
+
+void *GB300PatchTableGetFVarBuffer(const GB300PatchTable *t, int channel, int which) {
+    if (!t || channel < 0 || channel >= (int)t->fvar.size()) return nullptr;
+    const PatchSet &f = t->fvar[channel];
+    return which == 0 ? f.arrays : which == 1 ? f.indices : which == 2 ? f.params : nullptr;
+}
+
+int GB300PatchTableEvalVarying(const GB300PatchTable *t, const float *src, float *dst,
+                               float *du, float *dv, float *duu, float *duv, float *dvv,
+                               int length, int srcStride, int dstStride, int duStride,
+                               int dvStride, int duuStride, int duvStride, int dvvStride,
+                               int numPatchCoords, const void *patchCoords, void *stream) {
+    if (!t || !t->varying.arrays)
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "GB300PatchTableEvalVarying: table without varying patches");
+    return eval_set(t, t->varying, t->params, src, dst, du, dv, duu, duv, dvv, length,
+                    srcStride, dstStride, duStride, dvStride, duuStride, duvStride, dvvStride,
+                    numPatchCoords, patchCoords, stream, "GB300PatchTableEvalVarying");
+}
+
+int GB300PatchTableEvalFaceVarying(const GB300PatchTable *t, int channel, const float *src,
+                                   float *dst, float *du, float *dv, float *duu, float *duv,
+                                   float *dvv, int length, int srcStride, int dstStride,
+                                   int duStride, int dvStride, int duuStride, int duvStride,
+                                   int dvvStride, int numPatchCoords, const void *patchCoords,
+                                   void *stream) {
+    if (!t || channel < 0 || channel >= (int)t->fvar.size())
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "GB300PatchTableEvalFaceVarying: no face-varying channel %d", channel);
+    const PatchSet &f = t->fvar[channel];
+    return eval_set(t, f, f.params, src, dst, du, dv, duu, duv, dvv, length, srcStride,
+                    dstStride, duStride, dvStride, duuStride, duvStride, dvvStride,
+                    numPatchCoords, patchCoords, stream, "GB300PatchTableEvalFaceVarying");
 }
 
 GB300VertexBuffer *GB300VertexBufferCreate(int numElements, int numVertices) {

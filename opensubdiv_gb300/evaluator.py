@@ -177,6 +177,41 @@ class GB300Evaluator:
         return _status_to_bool(st)
 
     @staticmethod
+    def _eval_table_set(fn, lead, src, srcDesc, outs, numPatchCoords, patchCoords, stream):
+        for o, d in outs:
+            if o is not None and _desc(d).length != srcDesc.length:
+                return False
+        ptrs = [_ptr(o, _desc(d).offset) if o is not None else None for o, d in outs]
+        strides = [_desc(d).stride for _, d in outs]
+        st = fn(*lead, _ptr(src, srcDesc.offset), *ptrs, srcDesc.length, srcDesc.stride,
+                *strides, numPatchCoords, _ptr(patchCoords), _stream(stream))
+        return _status_to_bool(st)
+
+    @staticmethod
+    def EvalPatchesVarying(src, srcDesc, dst, dstDesc, numPatchCoords, patchCoords, table,
+                           du=None, duDesc=None, dv=None, dvDesc=None, duu=None, duuDesc=None,
+                           duv=None, duvDesc=None, dvv=None, dvvDesc=None, stream=None) -> bool:
+        """Varying primvars at patch coords (osd/cudaEvaluator.h:859-1060)."""
+        outs = [(dst, dstDesc), (du, duDesc), (dv, dvDesc), (duu, duuDesc), (duv, duvDesc),
+                (dvv, dvvDesc)]
+        return GB300Evaluator._eval_table_set(_lib.load().GB300PatchTableEvalVarying,
+                                              (table.handle,), src, srcDesc, outs,
+                                              numPatchCoords, patchCoords, stream)
+
+    @staticmethod
+    def EvalPatchesFaceVarying(src, srcDesc, dst, dstDesc, numPatchCoords, patchCoords, table,
+                               fvarChannel=0, du=None, duDesc=None, dv=None, dvDesc=None,
+                               duu=None, duuDesc=None, duv=None, duvDesc=None, dvv=None,
+                               dvvDesc=None, stream=None) -> bool:
+        """Face-varying primvars of channel fvarChannel at patch coords
+        (osd/cudaEvaluator.h:1070-1255)."""
+        outs = [(dst, dstDesc), (du, duDesc), (dv, dvDesc), (duu, duuDesc), (duv, duvDesc),
+                (dvv, dvvDesc)]
+        return GB300Evaluator._eval_table_set(_lib.load().GB300PatchTableEvalFaceVarying,
+                                              (table.handle, int(fvarChannel)), src, srcDesc,
+                                              outs, numPatchCoords, patchCoords, stream)
+
+    @staticmethod
     def Synchronize(stream=None):
         check(_lib.load().GB300Synchronize(_stream(stream)))
 
@@ -309,6 +344,45 @@ class GB300PatchTable:
     def GetPatchArrayBuffer(self): return _lib.load().GB300PatchTableGetBuffer(self.handle, 0)
     def GetPatchIndexBuffer(self): return _lib.load().GB300PatchTableGetBuffer(self.handle, 1)
     def GetPatchParamBuffer(self): return _lib.load().GB300PatchTableGetBuffer(self.handle, 2)
+
+    def SetVarying(self, arrays, indices, stream=None):
+        """Varying patch arrays / indices (CpuPatchTable's varying tables), evaluated with the
+        vertex patch params."""
+        a = np.ascontiguousarray(arrays, np.int32)
+        i = np.ascontiguousarray(indices, np.int32)
+        check(_lib.load().GB300PatchTableSetVarying(self.handle, len(a), a.ctypes.data, len(i),
+                                                    i.ctypes.data, _stream(stream)))
+
+    def AddFVarChannel(self, arrays, indices, params, stream=None):
+        """Face-varying channel tables; returns the channel index."""
+        import ctypes as C
+        a = np.ascontiguousarray(arrays, np.int32)
+        i = np.ascontiguousarray(indices, np.int32)
+        p = np.ascontiguousarray(params, np.int32)
+        ch = C.c_int(-1)
+        check(_lib.load().GB300PatchTableAddFVarChannel(self.handle, len(a), a.ctypes.data,
+                                                        len(i), i.ctypes.data, len(p),
+                                                        p.ctypes.data, C.byref(ch),
+                                                        _stream(stream)))
+        return ch.value
+
+    def GetNumFVarChannels(self):
+        return _lib.load().GB300PatchTableGetNumFVarChannels(self.handle)
+
+    def GetVaryingPatchArrayBuffer(self):
+        return _lib.load().GB300PatchTableGetVaryingBuffer(self.handle, 0)
+
+    def GetVaryingPatchIndexBuffer(self):
+        return _lib.load().GB300PatchTableGetVaryingBuffer(self.handle, 1)
+
+    def GetFVarPatchArrayBuffer(self, channel=0):
+        return _lib.load().GB300PatchTableGetFVarBuffer(self.handle, channel, 0)
+
+    def GetFVarPatchIndexBuffer(self, channel=0):
+        return _lib.load().GB300PatchTableGetFVarBuffer(self.handle, channel, 1)
+
+    def GetFVarPatchParamBuffer(self, channel=0):
+        return _lib.load().GB300PatchTableGetFVarBuffer(self.handle, channel, 2)
 
     def FindPatches(self, n, faces, u, v, coords_out, stream=None):
         """Device PatchMap lookup: writes n OsdPatchCoord records to coords_out."""

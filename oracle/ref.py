@@ -27,6 +27,7 @@ def lib():
         _lib = C.CDLL(LIB_PATH)
         vp = C.c_void_p
         _lib.ref_refiner_create.restype = vp
+        _lib.ref_refiner_create_fvar.restype = vp
         _lib.ref_stencils_create.restype = vp
         _lib.ref_limit_stencils_create.restype = vp
         _lib.ref_patches_create.restype = vp
@@ -38,7 +39,7 @@ def lib():
                      "ref_stencils_destroy", "ref_patches_destroy", "ref_patches_counts",
                      "ref_patches_copy", "ref_patches_copy_stencils", "ref_find_patches",
                      "ref_cpu_eval_stencils", "ref_cpu_eval_patches", "ref_eval_patches_fp64",
-                     "ref_omp_set_threads"):
+                     "ref_omp_set_threads", "ref_patches_varying", "ref_patches_fvar"):
             getattr(_lib, name).argtypes = None
     return _lib
 
@@ -50,16 +51,27 @@ def _p(a):
 class Refiner:
     """Far::TopologyRefiner built from a shapes.Cage (far/topologyRefinerFactory.h)."""
 
-    def __init__(self, cage, boundary: int = 1):
+    def __init__(self, cage, boundary: int = 1, fvar=None):
+        """fvar: optional (num_values, value index per face-vertex, linear) face-varying
+        channel."""
         self.cage = cage
         L = lib()
         cv = np.ascontiguousarray(cage.crease_verts, np.int32).ravel()
         cs = np.ascontiguousarray(cage.crease_sharpness, np.float32)
         self._keep = (cage.verts_per_face, cage.face_verts, cv, cs)
-        self.h = L.ref_refiner_create(
-            C.c_int(cage.scheme), C.c_int(cage.num_vertices), C.c_int(cage.num_faces),
-            _p(cage.verts_per_face), _p(cage.face_verts), C.c_int(len(cs)), _p(cv), _p(cs),
-            C.c_int(0), None, None, C.c_int(boundary))
+        if fvar is None:
+            self.h = L.ref_refiner_create(
+                C.c_int(cage.scheme), C.c_int(cage.num_vertices), C.c_int(cage.num_faces),
+                _p(cage.verts_per_face), _p(cage.face_verts), C.c_int(len(cs)), _p(cv), _p(cs),
+                C.c_int(0), None, None, C.c_int(boundary))
+        else:
+            nvals, fidx, linear = fvar
+            fidx = np.ascontiguousarray(fidx, np.int32)
+            self._keep += (fidx,)
+            self.h = L.ref_refiner_create_fvar(
+                C.c_int(cage.scheme), C.c_int(cage.num_vertices), C.c_int(cage.num_faces),
+                _p(cage.verts_per_face), _p(cage.face_verts), C.c_int(len(cs)), _p(cv), _p(cs),
+                C.c_int(boundary), C.c_int(nvals), _p(fidx), C.c_int(int(bool(linear))))
         if not self.h:
             raise RuntimeError("TopologyRefinerFactory::Create failed")
         self.h = C.c_void_p(self.h)
@@ -161,6 +173,26 @@ class Patches:
         if getattr(self, "h", None):
             lib().ref_patches_destroy(self.h)
             self.h = None
+
+    def varying(self):
+        """(arrays [n, 6], indices) of Osd::CpuPatchTable's varying tables."""
+        counts = np.zeros(2, np.int64)
+        lib().ref_patches_varying(self.h, _p(counts), None, None)
+        arrays = np.zeros((int(counts[0]), 6), np.int32)
+        indices = np.zeros(int(counts[1]), np.int32)
+        lib().ref_patches_varying(self.h, _p(counts), _p(arrays), _p(indices))
+        return arrays, indices
+
+    def fvar(self, channel=0):
+        """(arrays [n, 6], indices, params [n, 3]) of face-varying channel `channel`."""
+        counts = np.zeros(4, np.int64)
+        lib().ref_patches_fvar(self.h, C.c_int(channel), _p(counts), None, None, None)
+        arrays = np.zeros((int(counts[1]), 6), np.int32)
+        indices = np.zeros(int(counts[2]), np.int32)
+        params = np.zeros((int(counts[3]), 3), np.int32)
+        lib().ref_patches_fvar(self.h, C.c_int(channel), _p(counts), _p(arrays), _p(indices),
+                               _p(params))
+        return arrays, indices, params
 
     def find_patches(self, faces, u, v):
         faces = np.ascontiguousarray(faces, np.int32)

@@ -90,6 +90,38 @@ void *ref_refiner_create(int scheme, int nverts, int nfaces, const int *vertsPer
     return h;
 }
 
+// As ref_refiner_create, plus one face-varying channel (Far::TopologyDescriptor::FVarChannel,
+// far/topologyDescriptor.h:73-82): fvarIndices holds one value index per face-vertex.
+void *ref_refiner_create_fvar(int scheme, int nverts, int nfaces, const int *vertsPerFace,
+                              const int *faceVerts, int ncreases, const int *creaseVerts,
+                              const float *creaseSharp, int boundary, int fvarNumValues,
+                              const int *fvarIndices, int fvarLinear) {
+    Far::TopologyDescriptor desc;
+    desc.numVertices = nverts;
+    desc.numFaces = nfaces;
+    desc.numVertsPerFace = vertsPerFace;
+    desc.vertIndicesPerFace = faceVerts;
+    desc.numCreases = ncreases;
+    desc.creaseVertexIndexPairs = creaseVerts;
+    desc.creaseWeights = creaseSharp;
+    Far::TopologyDescriptor::FVarChannel ch;
+    ch.numValues = fvarNumValues;
+    ch.valueIndices = fvarIndices;
+    desc.numFVarChannels = 1;
+    desc.fvarChannels = &ch;
+    Sdc::SchemeType type = scheme == 0 ? Sdc::SCHEME_BILINEAR
+                         : scheme == 1 ? Sdc::SCHEME_CATMARK : Sdc::SCHEME_LOOP;
+    Sdc::Options opts;
+    opts.SetVtxBoundaryInterpolation((Sdc::Options::VtxBoundaryInterpolation)boundary);
+    opts.SetFVarLinearInterpolation(fvarLinear ? Sdc::Options::FVAR_LINEAR_ALL
+                                               : Sdc::Options::FVAR_LINEAR_NONE);
+    Far::TopologyRefinerFactory<Far::TopologyDescriptor>::Options fo(type, opts);
+    Refiner *h = new Refiner;
+    h->r = Far::TopologyRefinerFactory<Far::TopologyDescriptor>::Create(desc, fo);
+    if (!h->r) { delete h; return nullptr; }
+    return h;
+}
+
 void ref_refiner_destroy(void *p) {
     Refiner *h = (Refiner *)p;
     if (!h) return;
@@ -109,6 +141,12 @@ void ref_refine_adaptive(void *p, int isolation, int useSingleCrease, int useInf
     Far::PatchTableFactory::Options po(isolation);
     po.useSingleCreasePatch = useSingleCrease;
     po.useInfSharpPatch = useInfSharp;
+    if (((Refiner *)p)->r->GetNumFVarChannels() > 0) {
+        // non-linear face-varying patches need isolation of the face-varying topology
+        // (far/patchTableFactory.h:105-106)
+        po.generateFVarTables = true;
+        po.generateFVarLegacyLinearPatches = false;
+    }
     ((Refiner *)p)->r->RefineAdaptive(po.GetRefineAdaptiveOptions());
 }
 
@@ -310,6 +348,10 @@ void *ref_patches_create(void *p, int endcap, int maxIsolation, int useSingleCre
     po.useSingleCreasePatch = useSingleCrease;
     po.useInfSharpPatch = useInfSharp;
     po.shareEndCapPatchPoints = shareEndCapPoints;
+    if (r->GetNumFVarChannels() > 0) {
+        po.generateFVarTables = true;
+        po.generateFVarLegacyLinearPatches = !r->IsUniform() ? false : true;
+    }
     Patches *h = new Patches;
     h->pt = Far::PatchTableFactory::Create(*r, po);
     h->cpu = Osd::CpuPatchTable::Create(h->pt, nullptr);
@@ -371,6 +413,37 @@ void ref_patches_copy_stencils(void *p, int *sizes, int *offsets, int *indices, 
     copyVec(h->all->GetOffsets(), offsets);
     copyVec(h->all->GetControlIndices(), indices);
     copyN(h->all->GetWeights(), w, h->all->GetControlIndices().size());
+}
+
+// Varying tables of Osd::CpuPatchTable (osd/cpuPatchTable.cpp:75-86): counts[0] = arrays,
+// counts[1] = indices; arrays/indices may be NULL to query the counts.
+void ref_patches_varying(void *p, long *counts, int *arrays, int *indices) {
+    Patches *h = (Patches *)p;
+    counts[0] = h->pt->GetNumPatchArrays();
+    counts[1] = (long)h->cpu->GetVaryingPatchIndexSize();
+    if (arrays)
+        std::memcpy(arrays, h->cpu->GetVaryingPatchArrayBuffer(), counts[0] * 6 * sizeof(int));
+    if (indices)
+        std::memcpy(indices, h->cpu->GetVaryingPatchIndexBuffer(), counts[1] * sizeof(int));
+}
+
+// Face-varying tables of one channel (osd/cpuPatchTable.cpp:88-114): counts[0] = channels,
+// counts[1] = arrays, counts[2] = indices, counts[3] = params (3 x 32-bit each).
+void ref_patches_fvar(void *p, int channel, long *counts, int *arrays, int *indices,
+                      int *params) {
+    Patches *h = (Patches *)p;
+    counts[0] = h->cpu->GetNumFVarChannels();
+    if (channel >= counts[0]) { counts[1] = counts[2] = counts[3] = 0; return; }
+    counts[1] = h->pt->GetNumPatchArrays();
+    counts[2] = (long)h->cpu->GetFVarPatchIndexSize(channel);
+    counts[3] = (long)h->cpu->GetFVarPatchParamSize(channel);
+    if (arrays)
+        std::memcpy(arrays, h->cpu->GetFVarPatchArrayBuffer(channel),
+                    counts[1] * 6 * sizeof(int));
+    if (indices)
+        std::memcpy(indices, h->cpu->GetFVarPatchIndexBuffer(channel), counts[2] * sizeof(int));
+    if (params)
+        std::memcpy(params, h->cpu->GetFVarPatchParamBuffer(channel), counts[3] * 12);
 }
 
 // Far::PatchMap::FindPatch (far/patchMap.h:192-231).  handles: 3 ints per query

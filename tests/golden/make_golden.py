@@ -108,10 +108,30 @@ def edge_queries(nptex, rng, n):
     return face, u, v
 
 
-def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3):
+def uv_seams(cage, nu, nv):
+    """A face-varying UV channel with seams for a shapes.torus(nu, nv) cage: values on an
+    (nu + 1) x (nv + 1) grid, so faces across the wrap use the duplicated seam values."""
+    fidx = []
+    start = 0
+    for n in cage.verts_per_face:
+        vs = cage.face_verts[start:start + n]
+        start += n
+        i, j = vs // nv, vs % nv
+        if i.max() - i.min() > 1:
+            i = np.where(i == 0, nu, i)
+        if j.max() - j.min() > 1:
+            j = np.where(j == 0, nv, j)
+        fidx.extend((i * (nv + 1) + j).tolist())
+    return (nu + 1) * (nv + 1), np.asarray(fidx, np.int32)
+
+
+def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3, fvar=None):
+    """fvar: (num_values, indices per face-vertex) of a face-varying channel; the fixture then
+    also holds the reference's varying and face-varying patch tables with CpuEvaluator
+    outputs over random sources (EvalPatchesVarying / EvalPatchesFaceVarying)."""
     rng = np.random.default_rng(seed)
     out = dict(cage_arrays(cage))
-    r = ref.Refiner(cage)
+    r = ref.Refiner(cage, fvar=None if fvar is None else (fvar[0], fvar[1], False))
     if adaptive:
         r.refine_adaptive(level)
     else:
@@ -161,6 +181,23 @@ def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3):
                q_found=found, coords=coords, out6=np.stack(outs).reshape(6, -1, 3),
                out6_fp64=fp64.transpose(1, 0, 2).copy(),
                triangular=np.int32(cage.scheme == shapes.LOOP))
+    if fvar is not None:
+        # varying: the vertex patch params with the varying arrays / indices, 4 primvars
+        va, vi = p.varying()
+        vsrc = rng.uniform(-1, 1, (int(vi.max()) + 1, 4)).astype(np.float32).ravel()
+        vouts = [np.zeros(len(sel) * 4, np.float32) for _ in range(3)]
+        assert ref.cpu_eval_patches(vsrc, (0, 4, 4), vouts, [(0, 4, 4)] * 3, coords, va, vi,
+                                    p.params)
+        # face-varying channel 0: its own arrays / indices / params, 2 primvars (uv)
+        fa, fi, fp = p.fvar(0)
+        fsrc = rng.uniform(0, 1, (int(fi.max()) + 1, 2)).astype(np.float32).ravel()
+        fouts = [np.zeros(len(sel) * 2, np.float32) for _ in range(6)]
+        assert ref.cpu_eval_patches(fsrc, (0, 2, 2), fouts, [(0, 2, 2)] * 6, coords, fa, fi, fp)
+        out.update(fvar_num_values=np.int32(fvar[0]), fvar_value_indices=fvar[1],
+                   varying_arrays=va, varying_indices=vi, varying_src=vsrc,
+                   varying_out3=np.stack(vouts).reshape(3, -1, 4),
+                   fvar_arrays=fa, fvar_indices=fi, fvar_params=fp, fvar_src=fsrc,
+                   fvar_out6=np.stack(fouts).reshape(6, -1, 2))
     np.savez_compressed(path, **out)
     return out
 
@@ -185,6 +222,13 @@ def main():
     # Config-3 family: adaptive patch tables with Gregory-basis end caps.
     patch_fixture(os.path.join(g, "torus32x16_patches_L4.npz"), tor, 4, seed=21)
     patch_fixture(os.path.join(g, "icosphere2_patches_L3.npz"), ico, 3, seed=22)
+    # Varying and face-varying tables: tori with UV seams (non-linear face-varying patches)
+    ftor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=31, noise=0.01)
+    patch_fixture(os.path.join(g, "torus12x8_fvar_patches_L3.npz"), ftor, 3, seed=32,
+                  nq=1500, fvar=uv_seams(ftor, 12, 8))
+    fltor = shapes.torus(12, 8, seed=33, noise=0.01, scheme=shapes.LOOP)
+    patch_fixture(os.path.join(g, "looptorus12x8_fvar_patches_L3.npz"), fltor, 3, seed=34,
+                  nq=1500, fvar=uv_seams(fltor, 12, 8))
     # Boundaries: open grids (B-spline and box-spline boundary masks).
     patch_fixture(os.path.join(g, "grid6_patches_L3.npz"), shapes.grid(6, 6, seed=5), 3,
                   seed=23, nq=1500)

@@ -189,3 +189,52 @@ def test_patchmap_misses_evaluate_to_zero():
     o = host(out).reshape(4, 3)
     assert np.all(o[1] == 0)
     assert max_err(o[[0, 2, 3]], z["out6"][0][[0, 2, 3]]) <= _tol(z, _abs(z)[0])
+
+
+FVAR_FIXTURES = [p for p in FIXTURES if "fvar_arrays" in np.load(p)]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", FVAR_FIXTURES, ids=os.path.basename)
+def test_eval_patches_varying_and_face_varying(path):
+    """EvalPatchesVarying / EvalPatchesFaceVarying over the reference's varying and
+    face-varying tables (non-linear face-varying patches with seams), against CpuEvaluator."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
+    z = np.load(path)
+    m = z["coords"].shape[0]
+    t = _table(z)
+    t.SetVarying(z["varying_arrays"], z["varying_indices"])
+    ch = t.AddFVarChannel(z["fvar_arrays"], z["fvar_indices"], z["fvar_params"])
+    assert ch == 0 and t.GetNumFVarChannels() == 1
+    assert t.GetVaryingPatchIndexBuffer() and t.GetFVarPatchParamBuffer(0)
+    coords = dev(z["coords"])
+    # varying: 4 primvars, P + du + dv, with the vertex patch params
+    d4 = BD(0, 4, 4)
+    vo = [torch.zeros(m * 4, device="cuda") for _ in range(3)]
+    assert Ev.EvalPatchesVarying(dev(z["varying_src"]), d4, vo[0], d4, m, coords, t, du=vo[1],
+                                 duDesc=d4, dv=vo[2], dvDesc=d4)
+    # face-varying: 2 primvars (uv), all six outputs
+    d2 = BD(0, 2, 2)
+    fo = [torch.zeros(m * 2, device="cuda") for _ in range(6)]
+    assert Ev.EvalPatchesFaceVarying(dev(z["fvar_src"]), d2, fo[0], d2, m, coords, t, ch,
+                                     du=fo[1], duDesc=d2, dv=fo[2], dvDesc=d2, duu=fo[3],
+                                     duuDesc=d2, duv=fo[4], duvDesc=d2, dvv=fo[5], dvvDesc=d2)
+    Ev.Synchronize()
+    Av = oracle.abs_scale(z["varying_src"], (0, 4, 4), 4, z["coords"], z["varying_arrays"],
+                          z["varying_indices"], z["params"])
+    for k in range(3):
+        bound = 1e-6 * np.maximum(Av[k], 1.0)
+        assert np.all(np.abs(host(vo[k]) - z["varying_out3"][k].ravel()) <= bound), NAMES[k]
+    Af = oracle.abs_scale(z["fvar_src"], (0, 2, 2), 2, z["coords"], z["fvar_arrays"],
+                          z["fvar_indices"], z["fvar_params"])
+    for k in range(6):
+        bound = 1e-6 * np.maximum(Af[k], 1.0)
+        assert np.all(np.abs(host(fo[k]) - z["fvar_out6"][k].ravel()) <= bound), NAMES[k]
+    # a varying set that does not describe the vertex patches is rejected
+    from opensubdiv_gb300.evaluator import GB300Error
+    bad = z["varying_arrays"].copy()
+    bad[0, 2] -= 1
+    with pytest.raises(GB300Error):
+        t.SetVarying(bad, z["varying_indices"])
+    assert not Ev.EvalPatchesFaceVarying(dev(z["fvar_src"]), d2, fo[0], d2, m, coords, t, 3)

@@ -120,6 +120,28 @@ def test_patch_point_stencils_reproduce_the_patch_source(path):
     assert np.array_equal(out, z["src"][nc * 3:])
 
 
+FVAR_FIXTURES = [p for p in PATCH_FIXTURES if "fvar_arrays" in np.load(p)]
+
+
+@pytest.mark.parametrize("path", FVAR_FIXTURES, ids=os.path.basename)
+def test_varying_and_face_varying_patches_bitwise(path):
+    """EvalPatchesVarying (vertex params with the varying arrays/indices) and
+    EvalPatchesFaceVarying (the channel's own arrays/indices/params) restated, against
+    Osd::CpuEvaluator on the reference's own varying / face-varying tables."""
+    z = np.load(path)
+    m = z["coords"].shape[0]
+    vo = [np.zeros(m * 4, np.float32) for _ in range(3)]
+    oracle.eval_patches(z["varying_src"], (0, 4, 4), vo, [(0, 4, 4)] * 3, z["coords"],
+                        z["varying_arrays"], z["varying_indices"], z["params"])
+    for k in range(3):
+        assert np.array_equal(vo[k], z["varying_out3"][k].ravel()), k
+    fo = [np.zeros(m * 2, np.float32) for _ in range(6)]
+    oracle.eval_patches(z["fvar_src"], (0, 2, 2), fo, [(0, 2, 2)] * 6, z["coords"],
+                        z["fvar_arrays"], z["fvar_indices"], z["fvar_params"])
+    for k in range(6):
+        assert np.array_equal(fo[k], z["fvar_out6"][k].ravel()), k
+
+
 def test_descriptor_length_mismatch_is_rejected():
     """CpuEvaluator returns false when a destination length differs from the source's
     (osd/cpuEvaluator.cpp:46-47)."""
