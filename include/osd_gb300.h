@@ -235,8 +235,10 @@ int GB300VertexBufferGetNumVertices(const GB300VertexBuffer *buffer);
  * outlive it, and the source / destination contents may change between evaluations. */
 typedef struct GB300StencilBatch GB300StencilBatch;
 
-/* Builds the job table and the concatenated tile list on the device (synchronous on
- * `stream`).  Uses the tuned configuration cached for batches with the same work histogram,
+/* Builds the job table and the tile prefix on the device (synchronous on `stream`).  Jobs
+ * whose source rows are unaligned (no 16-byte vector loads) and at most 8 floats wide get a
+ * device buffer for a padded copy of their source (rows of 8 floats), refreshed by every
+ * evaluation.  Uses the tuned configuration cached for batches with the same work histogram,
  * if any.  Returns NULL on failure (error string set). */
 GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const *tables,
                                            const float *const *src, float *const *dst,
@@ -249,12 +251,14 @@ int GB300StencilBatchEval(GB300StencilBatch *batch, void *stream);
  * launched on `stream`.  The graph is dropped and recaptured after GB300StencilBatchTune. */
 int GB300StencilBatchEvalGraph(GB300StencilBatch *batch, void *stream);
 /* Autotuner: times each candidate (stencils per tile, CTAs per SM, mean stencil size above
- * which a job switches to one warp per stencil) over `iterations` evaluations on the batch
- * itself, keeps the fastest, and caches it for later batches with the same histogram of work
- * over (stencil size, job size, primvar width) classes.  Writes the outputs as Eval does. */
+ * which a job switches to one warp per stencil, tiles claimed from a work counter or assigned
+ * round-robin) over `iterations` evaluations on the batch itself, keeps the fastest, and
+ * caches it for later batches with the same histogram of work over (stencil size, job size,
+ * primvar width) classes.  Writes the outputs as Eval does. */
 int GB300StencilBatchTune(GB300StencilBatch *batch, int iterations, void *stream);
 int GB300StencilBatchGetConfig(const GB300StencilBatch *batch, int *tileStencils,
-                               int *ctasPerSm, int *warpThreshold, int *numTiles);
+                               int *ctasPerSm, int *warpThreshold, int *numTiles,
+                               int *dynamicClaims);
 /* Reads and clears the batch kernel's status word (GB300_OK or GB300_ERR_DEVICE_TIMEOUT);
  * synchronous. */
 int GB300StencilBatchGetDeviceStatus(GB300StencilBatch *batch, int *status);

@@ -60,7 +60,7 @@ _PROTOS = {
     "GB300StencilBatchEval": (i32, [vp, vp]),
     "GB300StencilBatchEvalGraph": (i32, [vp, vp]),
     "GB300StencilBatchTune": (i32, [vp, i32, vp]),
-    "GB300StencilBatchGetConfig": (i32, [vp, vp, vp, vp, vp]),
+    "GB300StencilBatchGetConfig": (i32, [vp, vp, vp, vp, vp, vp]),
     "GB300StencilBatchGetDeviceStatus": (i32, [vp, vp]),
     "GB300EvalStencilsBatchedNoAlloc": (i32, [i32] + [vp] * 11),
     "GB300ServerCreate": (vp, [vp]),

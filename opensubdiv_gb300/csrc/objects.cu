@@ -4,6 +4,7 @@
 // allocation or copy frees everything allocated so far and reports a status.
 #include "common.cuh"
 #include "patchmap.h"
+#include "stencils_batch.h"
 
 #include <algorithm>
 #include <new>
@@ -93,6 +94,7 @@ bool sort_entries(int numStencils, int64_t nnz, const int *sizes, const int *off
 struct GB300StencilTable {
     int numStencils = 0;
     int64_t nnz = 0;
+    int numControl = 0;  // largest control index + 1 (rows of the source the table reads)
     void *buf[9] = {nullptr};  // sizes, offsets, indices, w, du, dv, duu, duv, dvv
     // Evaluation order for tables whose consecutive stencils are scattered over the control
     // points (limit stencils at random locations): the same stencils sorted by their lowest
@@ -222,6 +224,11 @@ GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const i
     }
     t->numStencils = numStencils;
     t->nnz = nnz;
+    {
+        int mx = -1;
+        for (int64_t e = 0; e < nnz; ++e) mx = std::max(mx, indices[e]);
+        t->numControl = mx + 1;
+    }
     const float *wsrc[6] = {weights, duWeights, dvWeights, duuWeights, duvWeights, dvvWeights};
     std::vector<int> sortedIdx;
     std::vector<std::vector<float>> sortedW;
@@ -282,6 +289,23 @@ void *GB300StencilTableGetBuffer(const GB300StencilTable *t, int which) {
     return t->buf[which];
 }
 
+}  // extern "C"
+
+namespace gb300 {
+namespace batch {
+int stencil_table_num_control(const GB300StencilTable *t) { return t ? t->numControl : 0; }
+}  // namespace batch
+}  // namespace gb300
+
+extern "C" {
+
+namespace {
+
+int table_eval(const GB300StencilTable *t, const float *src, float *const *d, const int *st,
+               int length, int srcStride, cudaStream_t s);
+
+}  // namespace
+
 int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *dst, float *du,
                           float *dv, float *duu, float *duv, float *dvv, int length,
                           int srcStride, int dstStride, int duStride, int dvStride,
@@ -289,6 +313,32 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
     if (!t) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilTableEval: null table");
     float *d[6] = {dst, du, dv, duu, duv, dvv};
     const int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
+    cudaStream_t s = as_stream(stream);
+    // Unaligned source rows (no vector gathers) of a large table: gather from a padded copy
+    // (rows of 8 floats, 256-bit loads) made on the same stream in stream-ordered memory.
+    auto al = [](const void *p, uintptr_t m) { return ((uintptr_t)p & (m - 1)) == 0; };
+    const bool unaligned = src && !((al(src, 32) && srcStride % 8 == 0) ||
+                                    (al(src, 16) && srcStride % 4 == 0));
+    if (unaligned && length > 0 && length <= 8 && srcStride >= length &&
+        t->nnz >= (int64_t)t->numControl * 4 && t->nnz >= (1 << 20) && t->numControl > 0) {
+        float *padded = nullptr;
+        if (cudaMallocAsync((void **)&padded, (size_t)t->numControl * 32, s) == cudaSuccess) {
+            batch::PadJob j{src, padded, srcStride, length, t->numControl};
+            int r = batch::launch_pad_one(j, s);
+            if (r == GB300_OK) r = table_eval(t, padded, d, st, length, 8, s);
+            const int f = check_cuda(cudaFreeAsync(padded, s), "GB300StencilTableEval");
+            return r != GB300_OK ? r : f;
+        }
+        cudaGetLastError();  // no stream-ordered memory: evaluate in place
+    }
+    return table_eval(t, src, d, st, length, srcStride, s);
+}
+
+namespace {
+
+int table_eval(const GB300StencilTable *t, const float *src, float *const *dIn, const int *st,
+               int length, int srcStride, cudaStream_t s) {
+    float *d[6] = {dIn[0], dIn[1], dIn[2], dIn[3], dIn[4], dIn[5]};
     const float *w[6];
     for (int k = 0; k < 6; ++k) {
         w[k] = (const float *)t->buf[3 + k];
@@ -303,14 +353,16 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
         for (int k = 0; k < 6; ++k) ew[k] = (const float *)t->ebuf[3 + k];
         const int r = eval_stencils(src, d, st, ew, length, srcStride, (const int *)t->ebuf[0],
                                     (const int *)t->ebuf[1], (const int *)t->ebuf[2], 0,
-                                    t->numStencils, as_stream(stream), "GB300StencilTableEval",
+                                    t->numStencils, s, "GB300StencilTableEval",
                                     (const int *)t->outRow);
         if (r != GB300_ERR_UNSUPPORTED) return r;
     }
     return eval_stencils(src, d, st, w, length, srcStride, (const int *)t->buf[0],
-                         (const int *)t->buf[1], (const int *)t->buf[2], 0, t->numStencils,
-                         as_stream(stream), "GB300StencilTableEval");
+                         (const int *)t->buf[1], (const int *)t->buf[2], 0, t->numStencils, s,
+                         "GB300StencilTableEval");
 }
+
+}  // namespace
 
 namespace {
 

@@ -138,6 +138,7 @@ struct Args {
     int numJobs, numTiles;
     int *counter;         // work counter, zeroed before the launch
     int *status;
+    int dynamic;          // 1: tiles claimed from the counter, 0: CTA b takes b, b + grid, ...
 };
 
 __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
@@ -170,9 +171,11 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
             const int stage = it % kStages;
             const uint32_t use = (uint32_t)(it / kStages);
             if (use > 0 && !bar_wait(&empty[stage], (use - 1) & 1, a.status)) return;
-            int t = 0;
-            if (lane == 0) t = atomicAdd(a.counter, 1);
-            t = __shfl_sync(0xffffffffu, t, 0);
+            int t = (int)blockIdx.x + it * (int)gridDim.x;
+            if (a.dynamic) {
+                if (lane == 0) t = atomicAdd(a.counter, 1);
+                t = __shfl_sync(0xffffffffu, t, 0);
+            }
             int *sidx, *ssz, *sof;
             float *sw;
             stage_ptr(stage, &sidx, &sw, &ssz, &sof);
@@ -270,6 +273,67 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
     }
 }
 
+__global__ void __launch_bounds__(256) k_pad_rows(const PadJob *jobs, const long long *rowBase,
+                                                  int count, long long totalRows) {
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < totalRows;
+         r += step) {
+        int lo = 0, hi = count - 1;  // last job whose first row is <= r
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (__ldg(rowBase + mid) <= r)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        const PadJob j = jobs[lo];
+        const long long i = r - __ldg(rowBase + lo);
+        const float *row = j.src + i * j.srcStride;
+        float x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = c < j.length ? __ldg(row + c) : 0.0f;
+        float *d = j.dst + i * 8;
+        asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
+                     "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]), "f"(x[4]), "f"(x[5]),
+                     "f"(x[6]), "f"(x[7])
+                     : "memory");
+    }
+}
+
+__global__ void __launch_bounds__(256) k_pad_one(const PadJob j) {
+    const long long step = (long long)gridDim.x * blockDim.x;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < j.numRows;
+         i += step) {
+        const float *row = j.src + i * j.srcStride;
+        float x[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) x[c] = c < j.length ? __ldg(row + c) : 0.0f;
+        asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(j.dst + i * 8),
+                     "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]), "f"(x[4]), "f"(x[5]),
+                     "f"(x[6]), "f"(x[7])
+                     : "memory");
+    }
+}
+
+int launch_pad_one(const PadJob &j, cudaStream_t s) {
+    if (j.numRows <= 0) return GB300_OK;
+    const long long blocks = (j.numRows + 255) / 256;
+    const int grid = (int)std::min<long long>(blocks, (long long)num_sms() * 16);
+    k_pad_one<<<grid, 256, 0, s>>>(j);
+    count_launch();
+    return check_launch("padded source copy");
+}
+
+int launch_pad(const PadJob *dJobs, const long long *dRowBase, int count, long long totalRows,
+               cudaStream_t s) {
+    if (count <= 0 || totalRows <= 0) return GB300_OK;
+    const long long blocks = (totalRows + 255) / 256;
+    const int grid = (int)std::min<long long>(blocks, (long long)num_sms() * 16);
+    k_pad_rows<<<grid, 256, 0, s>>>(dJobs, dRowBase, count, totalRows);
+    count_launch();
+    return check_launch("padded source copy");
+}
+
 bool make_job(const GB300StencilTable *t, const float *src, float *dst, int length,
               int srcStride, int dstStride, Job &j, double &meanSize, const char *who) {
     auto al = [](const void *p, uintptr_t m) { return ((uintptr_t)p & (m - 1)) == 0; };
@@ -323,13 +387,15 @@ int set_smem_attribute() {
 }
 
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s) {
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic) {
     int st = set_smem_attribute();
     if (st != GB300_OK) return st;
     if (numTiles == 0) return ok();
-    st = check_cuda(cudaMemsetAsync(dCounter, 0, sizeof(int), s), "batch counter");
-    if (st != GB300_OK) return st;
-    Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus};
+    if (dynamic) {
+        st = check_cuda(cudaMemsetAsync(dCounter, 0, sizeof(int), s), "batch counter");
+        if (st != GB300_OK) return st;
+    }
+    Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus, dynamic};
     const int grid = std::min(numTiles, num_sms() * ctasPerSm);
     k_stencils_batch<<<grid, kThreads, kSmem, s>>>(a);
     count_launch();
@@ -340,6 +406,7 @@ struct Config {
     int tileStencils = 256;  // stencils per tile
     int ctasPerSm = 2;       // persistent CTAs per SM
     int warpThreshold = 64;  // mean stencil size above which a job uses warp-per-stencil
+    int dynamic = 1;         // tiles claimed from a work counter (else round-robin)
 };
 
 // Tuner key: the batch's work (stencil entries x primvar width) as a histogram over classes
@@ -380,8 +447,14 @@ struct GB300StencilBatch {
     int *dCounter = nullptr;   // [0] work counter, [1] status word
     int numTiles = 0;
     uint64_t signature = 0;
-    cudaGraphExec_t graph = nullptr;  // counter reset + kernel, instantiated on first use
+    cudaGraphExec_t graph = nullptr;  // pad copy + counter reset + kernel, on first use
     cudaStream_t capture = nullptr;
+    // padded copies of unaligned sources (rows of 8 floats), refreshed by every evaluation
+    float *dPadded = nullptr;
+    PadJob *dPad = nullptr;
+    long long *dPadBase = nullptr;
+    int numPad = 0;
+    long long padRows = 0;
     void drop_graph() {
         if (graph) cudaGraphExecDestroy(graph);
         graph = nullptr;
@@ -391,6 +464,8 @@ struct GB300StencilBatch {
         if (capture) cudaStreamDestroy(capture);
         if (dJobs) cudaFree(dJobs);
         if (dCounter) cudaFree(dCounter);
+        if (dPadded) cudaFree(dPadded);
+        if (dPad) cudaFree(dPad);
     }
 };
 
@@ -415,8 +490,56 @@ int upload_plan(GB300StencilBatch *b, cudaStream_t s) {
 }
 
 int launch_batch(GB300StencilBatch *b, cudaStream_t s) {
+    const int st = launch_pad(b->dPad, b->dPadBase, b->numPad, b->padRows, s);
+    if (st != GB300_OK) return st;
     return launch_jobs(b->dJobs, b->dTileBase, (int)b->jobs.size(), b->numTiles, b->dCounter,
-                       b->dCounter + 1, b->cfg.ctasPerSm, s);
+                       b->dCounter + 1, b->cfg.ctasPerSm, s, b->cfg.dynamic);
+}
+
+// Jobs whose source rows are unaligned (scalar gathers) and at most 8 floats wide read a
+// padded copy instead: one device buffer for all of them, rows of 8 floats.
+int setup_padding(GB300StencilBatch *b, const std::vector<int> &tableRows, cudaStream_t s) {
+    std::vector<PadJob> pads;
+    std::vector<long long> base(1, 0);
+    std::vector<int> which;
+    for (size_t k = 0; k < b->jobs.size(); ++k) {
+        const Job &j = b->jobs[k];
+        if (j.vw != 1 || j.length > 8 || tableRows[k] <= 0 || j.numStencils == 0) continue;
+        pads.push_back(PadJob{j.src, nullptr, j.srcStride, j.length, tableRows[k]});
+        base.push_back(base.back() + tableRows[k]);
+        which.push_back((int)k);
+    }
+    if (pads.empty()) return GB300_OK;
+    const long long rows = base.back();
+    int st = check_cuda(cudaMalloc((void **)&b->dPadded, (size_t)rows * 32), "batch padding");
+    if (st != GB300_OK) {
+        b->dPadded = nullptr;
+        return st;
+    }
+    for (size_t p = 0; p < pads.size(); ++p) {
+        pads[p].dst = b->dPadded + base[p] * 8;
+        Job &j = b->jobs[which[p]];
+        j.src = pads[p].dst;
+        j.srcStride = 8;
+        j.vw = 8;
+    }
+    const size_t padBytes = ((pads.size() * sizeof(PadJob) + 255) / 256) * 256;
+    st = check_cuda(cudaMalloc((void **)&b->dPad, padBytes + base.size() * sizeof(long long)),
+                    "batch padding");
+    if (st != GB300_OK) {
+        b->dPad = nullptr;
+        return st;
+    }
+    b->dPadBase = (long long *)((char *)b->dPad + padBytes);
+    b->numPad = (int)pads.size();
+    b->padRows = rows;
+    st = check_cuda(cudaMemcpyAsync(b->dPad, pads.data(), pads.size() * sizeof(PadJob),
+                                    cudaMemcpyHostToDevice, s), "batch padding");
+    if (st == GB300_OK)
+        st = check_cuda(cudaMemcpyAsync(b->dPadBase, base.data(), base.size() * sizeof(long long),
+                                        cudaMemcpyHostToDevice, s), "batch padding");
+    if (st == GB300_OK) st = check_cuda(cudaStreamSynchronize(s), "batch padding");
+    return st;
 }
 
 }  // namespace
@@ -480,9 +603,15 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
         return mean[x] * jobs[x].numStencils * jobs[x].length >
                mean[y] * jobs[y].numStencils * jobs[y].length;
     });
+    std::vector<int> rows;
     for (int i : order) {
         b->jobs.push_back(jobs[i]);
         b->mean.push_back(mean[i]);
+        rows.push_back(stencil_table_num_control(tables[i]));
+    }
+    if (setup_padding(b, rows, s) != GB300_OK) {
+        delete b;
+        return nullptr;
     }
     b->signature = work_signature(b->jobs, b->mean);
     {
@@ -564,12 +693,13 @@ int GB300StencilBatchGetDeviceStatus(GB300StencilBatch *b, int *status) {
 }
 
 int GB300StencilBatchGetConfig(const GB300StencilBatch *b, int *tileStencils, int *ctasPerSm,
-                               int *warpThreshold, int *numTiles) {
+                               int *warpThreshold, int *numTiles, int *dynamicClaims) {
     if (!b) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilBatchGetConfig: null batch");
     if (tileStencils) *tileStencils = b->cfg.tileStencils;
     if (ctasPerSm) *ctasPerSm = b->cfg.ctasPerSm;
     if (warpThreshold) *warpThreshold = b->cfg.warpThreshold;
     if (numTiles) *numTiles = b->numTiles;
+    if (dynamicClaims) *dynamicClaims = b->cfg.dynamic;
     return ok();
 }
 
@@ -592,9 +722,10 @@ int GB300StencilBatchTune(GB300StencilBatch *b, int iterations, void *stream) {
     int st = GB300_OK;
     for (int ts : tiles)
         for (int c : ctas)
-            for (int th : thresholds) {
+            for (int th : thresholds)
+            for (int dyn = 0; dyn < 2; ++dyn) {
                 if (!anyLarge && th != thresholds[0]) continue;
-                b->cfg = Config{ts, c, th};
+                b->cfg = Config{ts, c, th, dyn};
                 if ((st = upload_plan(b, s)) != GB300_OK) goto done;
                 if ((st = launch_batch(b, s)) != GB300_OK) goto done;  // warm-up
                 cudaEventRecord(e0, s);
@@ -715,7 +846,7 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
                                          cudaMemcpyHostToDevice, s), who)) != GB300_OK ||
         (st = check_cuda(cudaMemsetAsync(counter, 0, 2 * sizeof(int), s), who)) != GB300_OK)
         return st;
-    Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1};
+    Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1, 1};
     const int grid = (int)std::min<long long>(tiles, 2LL * sms);
     k_stencils_batch<<<grid, kThreads, kSmem, s>>>(a);
     count_launch();

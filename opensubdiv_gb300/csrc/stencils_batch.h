@@ -40,10 +40,32 @@ bool make_job(const GB300StencilTable *table, const float *src, float *dst, int 
 int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int warpThreshold,
                int *tileBase);
 
-// One persistent launch over n jobs (device arrays dJobs[n], dTileBase[n + 1]); resets the
-// work counter on `s` first.  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.
+// One persistent launch over n jobs (device arrays dJobs[n], dTileBase[n + 1]).  dynamic: tiles
+// are claimed from the work counter (reset on `s` first), else CTA b takes tiles b, b + grid,
+// ...  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s);
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1);
+
+// Padded copy of one source: rows [0, numRows) of `src` (length <= 8 floats, srcStride apart)
+// written to `dst` with a stride of 8 floats (elements >= length are 0), so the gathers of an
+// unaligned layout become 256-bit loads.  Values are copied, so results do not change.
+struct PadJob {
+    const float *src;
+    float *dst;
+    int srcStride, length;
+    long long numRows;
+};
+
+// One launch over `count` pad jobs (device arrays: jobs, rowBase[count + 1] = prefix of their
+// numRows).  Nothing is launched when totalRows is 0.
+int launch_pad(const PadJob *dJobs, const long long *dRowBase, int count, long long totalRows,
+               cudaStream_t s);
+
+// The same for one source, the job passed by value.
+int launch_pad_one(const PadJob &job, cudaStream_t s);
+
+// Rows a stencil table's indices address (its largest control index + 1).
+int stencil_table_num_control(const GB300StencilTable *table);
 
 }  // namespace batch
 }  // namespace gb300

@@ -304,10 +304,11 @@ class GB300StencilBatch:
 
     def GetConfig(self):
         import ctypes as C
-        v = [C.c_int(0) for _ in range(4)]
+        v = [C.c_int(0) for _ in range(5)]
         check(_lib.load().GB300StencilBatchGetConfig(self.handle, *[C.byref(x) for x in v]))
         return dict(tile_stencils=v[0].value, ctas_per_sm=v[1].value,
-                    warp_threshold=v[2].value, num_tiles=v[3].value)
+                    warp_threshold=v[2].value, num_tiles=v[3].value,
+                    dynamic_claims=v[4].value)
 
     def GetDeviceStatus(self):
         import ctypes as C

@@ -280,3 +280,39 @@ def test_invalid_requests_return_false_and_empty_ranges_are_noops():
     assert Ev.EvalStencils(src, BD(0, 3, 3), out, BD(0, 3, 3), *tbl, 5, 5)
     Ev.Synchronize()
     assert float(host(out).max()) == 0.0
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("length,stride,offset", [(3, 3, 0), (5, 7, 2), (8, 9, 1), (1, 1, 0)])
+def test_device_table_unaligned_rows_on_a_large_table(length, stride, offset):
+    """Device tables of >= 1M entries gather unaligned source rows from a padded copy: results
+    must be bit-identical to the raw entry point (which gathers in place) and match the
+    oracle."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import shapes
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
+    from opensubdiv_gb300.evaluator import GB300StencilTable
+    from opensubdiv_gb300.topology import UniformRefiner
+    cage = shapes.torus(96, 48, tri_fraction=0.05, crease_fraction=0.02, seed=8)
+    r = UniformRefiner(cage, 3).stencil_table()
+    n, ncv = len(r["sizes"]), cage.num_vertices
+    assert len(r["indices"]) >= 1 << 20
+    rng = np.random.default_rng(length)
+    src = rng.uniform(-1, 1, ncv * stride + offset).astype(np.float32)
+    t = GB300StencilTable.Create(r["sizes"], r["offsets"], r["indices"], r["weights"])
+    sd, dd = BD(offset, length, stride), BD(0, length, length)
+    a = torch.zeros(n * length, device="cuda")
+    b = torch.zeros(n * length, device="cuda")
+    s = dev(src)
+    assert Ev.EvalStencilsTable(s, sd, a, dd, t)
+    # the raw entry point over the table's own device arrays (entries sorted per stencil)
+    assert Ev.EvalStencils(s, sd, b, dd, t.GetSizesBuffer(), t.GetOffsetsBuffer(),
+                           t.GetIndicesBuffer(), t.GetWeightsBuffer(), 0, n)
+    Ev.Synchronize()
+    assert torch.equal(a, b)
+    out = np.zeros(n * length, np.float32)
+    oracle.eval_stencils(src, (offset, length, stride), [out], [(0, length, length)],
+                         r["sizes"], r["offsets"], r["indices"], [r["weights"]], threads=8)
+    bound = 1e-6 * oracle.stencil_abs_scale(src, (offset, length, stride), r["sizes"],
+                                            r["offsets"], r["indices"], r["weights"]) + 1e-6
+    assert np.all(np.abs(host(a) - out) <= bound)
