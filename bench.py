@@ -14,8 +14,10 @@ The per-step working set (1.4 GB of tables and outputs) exceeds the 129 MB L2, s
 explicit flush is needed between steps.
 
 --impl reference times the CPU evaluator of the path on this host's cores (the oracle port
-of Osd::CpuEvaluator / OmpEvaluator; the reference library itself is not available on the
-GPU host) on the same workload, one bounded sample per step.
+of Osd::CpuEvaluator / OmpEvaluator; the reference's C++ library is compiled for the build
+host only) on the same workload, one bounded sample per step, and adds `reference_cuda`: the
+reference's own CUDA evaluator kernels (osd/cudaKernel.cu, compiled for sm_103a by the oracle
+recipe) launched with its own launch logic on the same GPU and workloads.
 """
 from __future__ import annotations
 
@@ -513,6 +515,74 @@ def cpu_rate(w, seconds, threads):
             return done / el, el
 
 
+def reference_cuda(args, w):
+    """The reference's own CUDA evaluator kernels (osd/cudaKernel.cu built for sm_103a into
+    oracle/_ref by the oracle recipe) with its own launch logic, on the same workloads: refine
+    EvalStencils, limit EvalStencils with du/dv (one CudaEvalStencils per weight array, as
+    CudaEvaluator does), and EvalPatches with all derivatives at the bench's query points (patch
+    coords from the oracle's PatchMap on the host).  CUDA events per launch group."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    try:
+        import refcuda
+        import torch
+    except ImportError as e:
+        return {"unavailable": str(e)}
+    if not refcuda.available():
+        return {"unavailable": "oracle/_ref/osd_cudaKernel.cubin not built (reference sources "
+                               "absent where build() ran)"}
+    if not torch.cuda.is_available():
+        return {"unavailable": "no CUDA device"}
+    import oracle
+    L = w["length"]
+    r, lim = w["refine"], w["limit"]
+    dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    src = dev(w["src"])
+    rt = [dev(r[k]) for k in ("sizes", "offsets", "indices", "weights")]
+    lt = [dev(lim[k]) for k in ("sizes", "offsets", "indices")]
+    lw = [dev(lim[k]) for k in ("weights", "du_weights", "dv_weights")]
+    n_ref, n_lim = len(r["sizes"]), len(lim["sizes"])
+    out = torch.empty(n_ref * L, device="cuda")
+    lo = [torch.empty(n_lim * L, device="cuda") for _ in range(3)]
+
+    def timed(fn):
+        for _ in range(args.warmup):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            fn()
+        e1.record()
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / args.steps
+
+    refine_ms = timed(lambda: refcuda.eval_stencils(
+        src.data_ptr(), out.data_ptr(), L, L, L, *[t.data_ptr() for t in rt], 0, n_ref))
+    limit_ms = timed(lambda: refcuda.eval_stencils_derivatives(
+        src.data_ptr(), [o.data_ptr() for o in lo], L, L, [L] * 3, *[t.data_ptr() for t in lt],
+        [x.data_ptr() for x in lw], 0, n_lim))
+    res = {"kernels": "osd/cudaKernel.cu (computeStencils<<<512,32>>> for L=8; "
+                      "computePatches<<<512,32>>>)",
+           "refine_ms": refine_ms, "limit_ms": limit_ms,
+           "stencils_per_s": (n_ref + n_lim) / ((refine_ms + limit_ms) / 1e3)}
+    if not args.no_patches:
+        from opensubdiv_gb300 import workloads
+        pw = workloads.eval_patches_torus(args.patch_points)
+        handles = oracle.PatchMap(pw["arrays"], pw["params"], pw["triangular"]).find(
+            pw["face"], pw["u"], pw["v"])
+        coords = dev(oracle.make_coords(handles, pw["u"], pw["v"]))
+        n = len(pw["face"])
+        psrc = dev(pw["src"])
+        pa, pi, pp = dev(pw["arrays"]), dev(pw["indices"]), dev(pw["params"])
+        outs = [torch.empty(n * 3, device="cuda") for _ in range(6)]
+        patches_ms = timed(lambda: refcuda.eval_patches(
+            psrc.data_ptr(), [o.data_ptr() for o in outs], 3, 3, [3] * 6, n, coords.data_ptr(),
+            pa.data_ptr(), pi.data_ptr(), pp.data_ptr()))
+        res.update(eval_patches_ms=patches_ms, patch_points=n,
+                   patch_evals_per_s=n / (patches_ms / 1e3))
+    return res
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -539,7 +609,8 @@ def run_reference(args, rank, world):
                              "sample": f"{args.steps} steps x >= {per_step:.1f}s of full "
                                        "refine+limit passes, OpenMP over all host threads"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0}}
+                    "d2h_bytes_per_step": 0},
+            "reference_cuda": reference_cuda(args, w)}
     print(json.dumps(line), flush=True)
 
 
