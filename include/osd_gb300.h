@@ -332,10 +332,25 @@ typedef struct {
     uint64_t bytesUploaded, residentBytes, peakResidentBytes;
 } GB300ServerStats;
 
+/* ---- table cache (no counterpart in the reference) --------------------------------------- */
+
+/* Writes a topology's tables (the arrays a GB300TopologyDesc points at) to one file: a 256-byte
+ * header with counts, array offsets and an FNV-1a checksum, then the arrays, 64-byte aligned.
+ * Written to `<path>.tmp` and renamed, so readers never see a partial file. */
+int GB300TableCacheWrite(const char *path, const GB300TopologyDesc *desc);
+/* Maps a table cache read-only and fills `desc` with pointers into the mapping (valid until
+ * GB300TableCacheClose(*handle)).  verify = 1 checks the payload checksum (reads the file). */
+int GB300TableCacheOpen(const char *path, int verify, GB300TopologyDesc *desc, void **handle);
+void GB300TableCacheClose(void *handle);
+
 GB300Server *GB300ServerCreate(const GB300ServerConfig *config);
 /* Finishes every submitted request, then frees the server. */
 void GB300ServerDestroy(GB300Server *server);
 int GB300ServerAddTopology(GB300Server *server, int id, const GB300TopologyDesc *desc);
+/* The same from a table cache file: the server keeps the file mapped and uploads from the
+ * mapping, so a topology evicted from device memory is re-read from the file (through the page
+ * cache) instead of being held in host memory. */
+int GB300ServerAddTopologyFromCache(GB300Server *server, int id, const char *path);
 /* Queues a request (thread-safe); its buffers must stay valid until it completes. */
 int GB300ServerSubmit(GB300Server *server, const GB300Request *request, uint64_t *ticket);
 /* Blocks until the request completed; latency = submit -> results in host memory. */

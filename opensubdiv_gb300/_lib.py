@@ -70,6 +70,10 @@ _PROTOS = {
     "GB300ServerWait": (i32, [vp, u64, vp]),
     "GB300ServerReplay": (i32, [vp, i32, vp, vp, vp]),
     "GB300ServerGetStats": (i32, [vp, vp]),
+    "GB300ServerAddTopologyFromCache": (i32, [vp, i32, C.c_char_p]),
+    "GB300TableCacheWrite": (i32, [C.c_char_p, vp]),
+    "GB300TableCacheOpen": (i32, [C.c_char_p, i32, vp, vp]),
+    "GB300TableCacheClose": (None, [vp]),
 }
 
 

@@ -182,6 +182,7 @@ struct GB300Server {
     bool stop = false;
     std::thread worker;
     std::vector<void *> registered;  // host ranges this server page-locked
+    std::vector<void *> caches;      // table-cache mappings of topologies added from files
 };
 
 namespace gb300 {
@@ -606,6 +607,7 @@ void GB300ServerDestroy(GB300Server *s) {
     for (auto &kv : s->topos)
         if (kv.second->ready) cudaEventDestroy(kv.second->ready);
     for (void *p : s->registered) cudaHostUnregister(p);
+    for (void *c : s->caches) GB300TableCacheClose(c);
     delete s;
 }
 
@@ -696,6 +698,22 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
         return fail(GB300_ERR_INVALID_ARGUMENT, "%s: topology %d already registered", who, id);
     }
     s->topos[id] = std::move(t);
+    return ok();
+}
+
+int GB300ServerAddTopologyFromCache(GB300Server *s, int id, const char *path) {
+    if (!s) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300ServerAddTopologyFromCache: null server");
+    GB300TopologyDesc d;
+    void *h = nullptr;
+    int st = GB300TableCacheOpen(path, 1, &d, &h);
+    if (st != GB300_OK) return st;
+    st = GB300ServerAddTopology(s, id, &d);
+    if (st != GB300_OK) {
+        GB300TableCacheClose(h);
+        return st;
+    }
+    std::lock_guard<std::mutex> lock(s->m);
+    s->caches.push_back(h);
     return ok();
 }
 

@@ -76,18 +76,27 @@ __device__ __forceinline__ void eval_one(const A &a, int i, int n, const int *li
                 for (int k = 0; k < NW; ++k)
                     w4[k] = *reinterpret_cast<const float4 *>(lw + k * lstride + q);
                 const int ids[4] = {id4.x, id4.y, id4.z, id4.w};
-                float x[4][8];
+                // rows gathered G at a time before they are accumulated: all 4 for one output,
+                // 2 when the NW accumulators need the registers
+                constexpr int G = NW == 1 ? 4 : 2;
 #pragma unroll
-                for (int m = 0; m < 4; ++m)
-                    if (q + m >= o && q + m < end) gather_row<VW>(a, ids[m], c0, pol_src, x[m]);
+                for (int g = 0; g < 4; g += G) {
+                    float x[G][8];
 #pragma unroll
-                for (int m = 0; m < 4; ++m) {
-                    if (q + m < o || q + m >= end) continue;
-                    float wk[NW];
+                    for (int m = 0; m < G; ++m)
+                        if (q + g + m >= o && q + g + m < end)
+                            gather_row<VW>(a, ids[g + m], c0, pol_src, x[m]);
 #pragma unroll
-                    for (int k = 0; k < NW; ++k)
-                        wk[k] = m == 0 ? w4[k].x : m == 1 ? w4[k].y : m == 2 ? w4[k].z : w4[k].w;
-                    fma_row<NW>(wk, x[m], acc);
+                    for (int m = 0; m < G; ++m) {
+                        const int e = g + m;
+                        if (q + e < o || q + e >= end) continue;
+                        float wk[NW];
+#pragma unroll
+                        for (int k = 0; k < NW; ++k)
+                            wk[k] = e == 0 ? w4[k].x : e == 1 ? w4[k].y : e == 2 ? w4[k].z
+                                                                         : w4[k].w;
+                        fma_row<NW>(wk, x[m], acc);
+                    }
                 }
             }
         } else {

@@ -61,6 +61,77 @@ def _addr(a):
     return a.ctypes.data
 
 
+def topology_desc(num_control, length, refine, limit=None):
+    """A TopologyDesc over contiguous copies of the arrays; returns (desc, arrays to keep)."""
+    r = {k: np.ascontiguousarray(refine[k], np.int32 if k != "weights" else np.float32)
+         for k in ("sizes", "offsets", "indices", "weights")}
+    d = TopologyDesc()
+    d.numControl, d.length = int(num_control), int(length)
+    d.numStencils, d.nnz = len(r["sizes"]), len(r["indices"])
+    d.sizes, d.offsets, d.indices, d.weights = (_addr(r[k]) for k in
+                                                ("sizes", "offsets", "indices", "weights"))
+    keep = [r]
+    if limit is not None:
+        lm = {k: np.ascontiguousarray(limit[k], np.float32 if k == "pp_weights" else np.int32)
+              for k in ("pp_sizes", "pp_offsets", "pp_indices", "pp_weights", "arrays",
+                        "patch_indices", "params")}
+        d.numPatchPoints, d.patchPointNnz = len(lm["pp_sizes"]), len(lm["pp_indices"])
+        d.ppSizes, d.ppOffsets, d.ppIndices, d.ppWeights = (
+            _addr(lm[k]) for k in ("pp_sizes", "pp_offsets", "pp_indices", "pp_weights"))
+        d.numPatchArrays = lm["arrays"].shape[0]
+        d.patchArrays = _addr(lm["arrays"])
+        d.numPatchIndices = len(lm["patch_indices"])
+        d.patchIndices = _addr(lm["patch_indices"])
+        d.numPatches = lm["params"].shape[0]
+        d.patchParams = _addr(lm["params"])
+        d.triangular = int(bool(limit["triangular"]))
+        keep.append(lm)
+    return d, keep
+
+
+def write_table_cache(path, num_control, length, refine, limit=None):
+    """Write one topology's tables to a table-cache file (GB300TableCacheWrite)."""
+    d, _keep = topology_desc(num_control, length, refine, limit)
+    check(_lib.load().GB300TableCacheWrite(str(path).encode(), C.byref(d)))
+
+
+def read_table_cache(path, verify=True):
+    """Map a table-cache file and return copies of its arrays:
+    (num_control, length, refine dict, limit dict or None)."""
+    d = TopologyDesc()
+    h = C.c_void_p()
+    check(_lib.load().GB300TableCacheOpen(str(path).encode(), int(bool(verify)), C.byref(d),
+                                          C.byref(h)))
+
+    def arr(ptr, n, dtype, shape=None):
+        if n == 0:
+            return np.zeros(shape or (0,), dtype)
+        ct = C.c_int32 if dtype == np.int32 else C.c_float
+        a = np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ct)), shape=(n,)).copy()
+        return a.view(dtype).reshape(shape) if shape else a.view(dtype)
+
+    try:
+        refine = dict(sizes=arr(d.sizes, d.numStencils, np.int32),
+                      offsets=arr(d.offsets, d.numStencils, np.int32),
+                      indices=arr(d.indices, d.nnz, np.int32),
+                      weights=arr(d.weights, d.nnz, np.float32))
+        limit = None
+        if d.numPatchArrays > 0:
+            limit = dict(pp_sizes=arr(d.ppSizes, d.numPatchPoints, np.int32),
+                         pp_offsets=arr(d.ppOffsets, d.numPatchPoints, np.int32),
+                         pp_indices=arr(d.ppIndices, d.patchPointNnz, np.int32),
+                         pp_weights=arr(d.ppWeights, d.patchPointNnz, np.float32),
+                         arrays=arr(d.patchArrays, 6 * d.numPatchArrays, np.int32,
+                                    (d.numPatchArrays, 6)),
+                         patch_indices=arr(d.patchIndices, d.numPatchIndices, np.int32),
+                         params=arr(d.patchParams, 3 * d.numPatches, np.int32,
+                                    (d.numPatches, 3)),
+                         triangular=bool(d.triangular))
+        return d.numControl, d.length, refine, limit
+    finally:
+        _lib.load().GB300TableCacheClose(h)
+
+
 class GB300Server:
     def __init__(self, table_budget_bytes, arena_bytes, streams=4, max_requests_per_round=64,
                  plain=False, pin_host_tables=False):
@@ -84,31 +155,14 @@ class GB300Server:
         """refine: dict(sizes, offsets, indices, weights) over the control vertices.
         limit: dict(pp_sizes, pp_offsets, pp_indices, pp_weights, arrays, patch_indices,
         params, triangular) or None."""
-        r = {k: np.ascontiguousarray(refine[k], np.int32 if k != "weights" else np.float32)
-             for k in ("sizes", "offsets", "indices", "weights")}
-        d = TopologyDesc()
-        d.numControl, d.length = int(num_control), int(length)
-        d.numStencils, d.nnz = len(r["sizes"]), len(r["indices"])
-        d.sizes, d.offsets, d.indices, d.weights = (_addr(r[k]) for k in
-                                                    ("sizes", "offsets", "indices", "weights"))
-        keep = [r]
-        if limit is not None:
-            lm = {k: np.ascontiguousarray(limit[k], np.float32 if k == "pp_weights" else np.int32)
-                  for k in ("pp_sizes", "pp_offsets", "pp_indices", "pp_weights", "arrays",
-                            "patch_indices", "params")}
-            d.numPatchPoints, d.patchPointNnz = len(lm["pp_sizes"]), len(lm["pp_indices"])
-            d.ppSizes, d.ppOffsets, d.ppIndices, d.ppWeights = (
-                _addr(lm[k]) for k in ("pp_sizes", "pp_offsets", "pp_indices", "pp_weights"))
-            d.numPatchArrays = lm["arrays"].shape[0]
-            d.patchArrays = _addr(lm["arrays"])
-            d.numPatchIndices = len(lm["patch_indices"])
-            d.patchIndices = _addr(lm["patch_indices"])
-            d.numPatches = lm["params"].shape[0]
-            d.patchParams = _addr(lm["params"])
-            d.triangular = int(bool(limit["triangular"]))
-            keep.append(lm)
+        d, keep = topology_desc(num_control, length, refine, limit)
         check(_lib.load().GB300ServerAddTopology(self.handle, int(tid), C.byref(d)))
         self._keep[int(tid)] = keep
+
+    def add_topology_from_cache(self, tid, path):
+        """Register a topology stored with write_table_cache (the server maps the file)."""
+        check(_lib.load().GB300ServerAddTopologyFromCache(self.handle, int(tid),
+                                                          str(path).encode()))
 
     @staticmethod
     def request(tid, kind, control_values, out, faces=None, u=None, v=None):

@@ -195,3 +195,29 @@ def test_server_rejects_bad_requests():
         t = pool[0]
         small.add_topology(t["id"], t["num_control"], t["length"], t["refine"], t["limit"])
     s.close()
+
+
+@pytest.mark.gpu
+def test_server_topologies_from_table_cache_files(tmp_path):
+    """Topologies registered from table-cache files (mapped, re-read on re-admission) give the
+    results of topologies registered from host arrays, under a budget that forces evictions."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.server import GB300Server, write_table_cache
+    pool = _pool()[:5]
+    reqs = _work(pool)
+    ref_srv = _server(pool, budget=sum(_table_bytes(t) for t in pool) * 2)
+    expect = _run_alone(ref_srv, reqs, torch)
+    ref_srv.close()
+    srv = GB300Server(max(_table_bytes(t) for t in pool) * 2, 1 << 30, streams=3,
+                      max_requests_per_round=16, pin_host_tables=True)
+    for t in pool:
+        path = tmp_path / f"topo{t['id']}.gbtc"
+        write_table_cache(path, t["num_control"], t["length"], t["refine"], t["limit"])
+        srv.add_topology_from_cache(t["id"], path)
+    for _ in range(2):  # twice round: the second pass re-admits evicted topologies
+        got = _run_alone(srv, reqs, torch)
+        for q, a, b in zip(reqs, expect, got):
+            assert np.array_equal(a, b), (q["topo"]["id"], q["kind"])
+    st = srv.stats()
+    srv.close()
+    assert st["evictions"] > 0 and st["failed"] == 0
