@@ -118,17 +118,37 @@ __device__ __forceinline__ void stencil_warp(const Job &j, int i, int n, int o, 
     }
 }
 
+// eval_one's view of a staged job: the fields every gather uses are held in registers, the
+// ones used once per stencil (outputs, weights for the unstaged path) stay in the shared-memory
+// copy of the descriptor and are reached through references.
+struct JobView {
+    const float *src;
+    int srcStride, length, vw;
+    const float *const (&w)[1];
+    float *const (&dst)[1];
+    const int (&dstStride)[1];
+    const int (&outOf)[1];
+    const int (&vecDst)[1];
+    const int *const &indices;
+    const int *const &outRow;
+    __device__ explicit JobView(const Job &j)
+        : src(j.src), srcStride(j.srcStride), length(j.length), vw(j.vw), w(j.w), dst(j.dst),
+          dstStride(j.dstStride), outOf(j.outOf), vecDst(j.vecDst), indices(j.indices),
+          outRow(j.outRow) {}
+};
+
 // Consumers' work on one staged tile (VW = 0: the job's row width chosen per gather).
 template <int VW>
 __device__ __forceinline__ void tile_threads(const Job &j, const Meta &m, const int *sidx,
                                              const float *sw, const int *ssz, const int *sof,
                                              uint64_t pol_src, uint64_t pol_stream) {
+    const JobView v(j);
     for (int i = m.s0 + (int)threadIdx.x; i < m.s1; i += kConsumers) {
         const int n = ssz[i - m.s0a], o = sof[i - m.s0a];
         if (m.staged && o >= m.e0a && o + n <= m.e1)
-            tma::eval_one<1, VW>(j, i, n, sidx, sw, kCap, o - m.e0a, pol_src, pol_stream);
+            tma::eval_one<1, VW>(v, i, n, sidx, sw, kCap, o - m.e0a, pol_src, pol_stream);
         else
-            tma::eval_one<1, VW>(j, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
+            tma::eval_one<1, VW>(v, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
     }
 }
 
