@@ -621,13 +621,12 @@ def run_gb300(args, rank, world):
     from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
                                             GB300StencilTable, GB300VertexBuffer)
 
-    local = int(os.environ.get("LOCAL_RANK", 0))
+    from opensubdiv_gb300 import replicas
+
+    local = replicas.world()[1]
     torch.cuda.set_device(local)
     _lib.load()
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
+    dist = replicas.init("nccl")
 
     w = workloads.refine_and_limit_torus(args.nu, args.nv, n_limit=args.n_limit)
     L = w["length"]
@@ -685,12 +684,9 @@ def run_gb300(args, rank, world):
     ms = t_start.elapsed_time(t_end)
     ref_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in ev]))
     lim_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in ev]))
-    if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = replicas.max_over_ranks(dist, ms, device="cuda")
     n_step = n_ref + n_lim
-    value = world * n_step * args.steps / (ms / 1e3)
+    value = replicas.job_rate(n_step * args.steps, world, ms / 1e3)
 
     # ---- end to end through the C ABI with host buffers ----
     host_src = torch.from_numpy(w["src"].copy()).pin_memory()
@@ -720,11 +716,8 @@ def run_gb300(args, rank, world):
     e1.record(stream)
     barrier()
     e2e_ms = e0.elapsed_time(e1)
-    if dist:
-        t = torch.tensor([e2e_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
-    e2e_value = world * n_step * args.steps / (e2e_ms / 1e3)
+    e2e_ms = replicas.max_over_ranks(dist, e2e_ms, device="cuda")
+    e2e_value = replicas.job_rate(n_step * args.steps, world, e2e_ms / 1e3)
     h2d = ncv * L * 4
     d2h = (n_ref + 3 * n_lim) * L * 4
 
@@ -788,8 +781,8 @@ def run_gb300(args, rank, world):
 
 def main():
     args = parse()
-    rank = int(os.environ.get("RANK", 0))
-    world = int(os.environ.get("WORLD_SIZE", 1))
+    from opensubdiv_gb300 import replicas
+    rank, _, world = replicas.world()
     if args.impl == "reference":
         run_reference(args, rank, world)
     else:

@@ -199,6 +199,24 @@ public:
     }
     ~GB300PatchTable() { GB300PatchTableDestroy(_h); }
 
+    /// Varying and face-varying tables for a table created from flattened arrays (Create from
+    /// a Far::PatchTable fills them itself).  AddFVarChannel returns the channel or -1.
+    bool SetVarying(int numArrays, PatchArray const *arrays, int64_t numIndices,
+                    int const *indices, void *deviceContext = NULL) {
+        return gb300_detail::ok(GB300PatchTableSetVarying(
+            _h, numArrays, arrays, numIndices, indices, gb300_detail::stream_of(deviceContext)));
+    }
+    int AddFVarChannel(int numArrays, PatchArray const *arrays, int64_t numIndices,
+                       int const *indices, int numParams, PatchParam const *params,
+                       void *deviceContext = NULL) {
+        int ch = -1;
+        return gb300_detail::ok(GB300PatchTableAddFVarChannel(
+                   _h, numArrays, arrays, numIndices, indices, numParams, params, &ch,
+                   gb300_detail::stream_of(deviceContext)))
+                   ? ch
+                   : -1;
+    }
+
     void *GetPatchArrayBuffer() const { return GB300PatchTableGetBuffer(_h, 0); }
     void *GetPatchIndexBuffer() const { return GB300PatchTableGetBuffer(_h, 1); }
     void *GetPatchParamBuffer() const { return GB300PatchTableGetBuffer(_h, 2); }

@@ -57,6 +57,10 @@ struct Topology {
     std::vector<Level> levels;
     std::vector<Rows> rows;  // rows[l] = stencils of level-l vertices (rows[0] identity)
     std::vector<int> ptexOff;
+    // masks of one level, between GB300TopologyMaskCounts and GB300TopologyMaskCopy
+    std::vector<int64_t> maskOff;
+    std::vector<int> maskIdx;
+    std::vector<double> maskW;
     // limit stencils produced by the last GB300TopologyLimitStencils call
     std::vector<int> lsizes, loffsets, lidx;
     std::vector<float> lw[3];
@@ -451,20 +455,83 @@ void *GB300TopologyCreate(int scheme, int nverts, int nfaces, const int *vertsPe
 void GB300TopologyDestroy(void *p) { delete (Topology *)p; }
 
 // Refines uniformly up to `level` (1..10), building factorized rows for every level.
+// Topology of levels 1..level (no stencils).
+int GB300TopologyRefineTopology(void *p, int level) {
+    Topology *t = (Topology *)p;
+    if (!t || level < 1 || level > 10) return fail("GB300TopologyRefineTopology: bad level");
+    while ((int)t->levels.size() <= level) {
+        Level child;
+        refine_topology(t->scheme, t->levels.back(), child);
+        std::string err;
+        if (!finish_level(child, err)) return fail(err.c_str());
+        t->levels.push_back(std::move(child));
+    }
+    return 0;
+}
+
+// Topology and factorized stencils of levels 1..level.
 int GB300TopologyRefineUniform(void *p, int level) {
     Topology *t = (Topology *)p;
     if (!t || level < 1 || level > 10) return fail("GB300TopologyRefineUniform: bad level");
-    while ((int)t->levels.size() <= level) {
-        Level child;
-        const Level &par = t->levels.back();
-        refine_topology(t->scheme, par, child);
-        std::string err;
-        if (!finish_level(child, err)) return fail(err.c_str());
+    if (GB300TopologyRefineTopology(p, level)) return 1;
+    while ((int)t->rows.size() <= level) {
+        const size_t l = t->rows.size();  // compose level l from level l - 1
         Rows r;
-        compose(t->scheme, par, t->rows.back(), t->levels[0].nv, r, child.nv);
-        t->levels.push_back(std::move(child));
+        compose(t->scheme, t->levels[l - 1], t->rows.back(), t->levels[0].nv, r,
+                t->levels[l].nv);
         t->rows.push_back(std::move(r));
     }
+    return 0;
+}
+
+// Subdivision masks of the level-`level` vertices over the level-(level - 1) vertices, in
+// the order compose() applies them (CSR: offsets[nChild + 1], parents, double weights).
+// MaskCounts computes them and keeps them until MaskCopy hands them out.
+int GB300TopologyMaskCounts(void *p, int level, int *nChild, int64_t *nnz) {
+    Topology *t = (Topology *)p;
+    if (!t || level < 1 || level >= (int)t->levels.size())
+        return fail("GB300TopologyMaskCounts: level not refined");
+    const Level &P = t->levels[level - 1];
+    const int nc = t->levels[level].nv;
+    const bool cat = t->scheme == kCatmark;
+    const int vFace = cat ? P.nv : -1, vEdge = cat ? P.nv + P.nf : P.nv;
+    auto mask_of = [&](int c, Mask &m) {
+        if (c < P.nv) vertex_mask(t->scheme, P, c, m);
+        else if (cat && c < vEdge) add_face_point(P, c - vFace, 1.0, m);
+        else edge_mask(t->scheme, P, c - vEdge, m);
+    };
+    // two passes (sizes, then the masks again into place): no per-child staging buffer
+    t->maskOff.assign(nc + 1, 0);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+        Mask m;
+        mask_of(c, m);
+        t->maskOff[c + 1] = m.n;
+    }
+    for (int c = 0; c < nc; ++c) t->maskOff[c + 1] += t->maskOff[c];
+    t->maskIdx.resize(t->maskOff[nc]);
+    t->maskW.resize(t->maskOff[nc]);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < nc; ++c) {
+        Mask m;
+        mask_of(c, m);
+        std::copy(m.idx, m.idx + m.n, t->maskIdx.begin() + t->maskOff[c]);
+        std::copy(m.w, m.w + m.n, t->maskW.begin() + t->maskOff[c]);
+    }
+    *nChild = nc;
+    *nnz = t->maskOff[nc];
+    return 0;
+}
+
+int GB300TopologyMaskCopy(void *p, int64_t *offsets, int *parents, double *weights) {
+    Topology *t = (Topology *)p;
+    if (!t || t->maskOff.empty()) return fail("GB300TopologyMaskCopy: no masks computed");
+    std::copy(t->maskOff.begin(), t->maskOff.end(), offsets);
+    std::copy(t->maskIdx.begin(), t->maskIdx.end(), parents);
+    std::copy(t->maskW.begin(), t->maskW.end(), weights);
+    std::vector<int64_t>().swap(t->maskOff);
+    std::vector<int>().swap(t->maskIdx);
+    std::vector<double>().swap(t->maskW);
     return 0;
 }
 

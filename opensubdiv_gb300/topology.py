@@ -41,6 +41,9 @@ def load():
         lib.GB300TopologyGetLastError.restype = C.c_char_p
         lib.GB300TopologySetNumThreads.argtypes = [i32]
         lib.GB300TopologySetNumThreads.restype = None
+        lib.GB300TopologyRefineTopology.argtypes = [vp, i32]
+        lib.GB300TopologyMaskCounts.argtypes = [vp, i32, vp, vp]
+        lib.GB300TopologyMaskCopy.argtypes = [vp, vp, vp, vp]
         _lib = lib
     return _lib
 
@@ -52,7 +55,8 @@ def _err():
 class UniformRefiner:
     """Uniform refinement of a shapes.Cage (Catmull-Clark or Loop, closed, with creases)."""
 
-    def __init__(self, cage, level: int):
+    def __init__(self, cage, level: int, stencils: bool = True):
+        """stencils=False refines the topology only (for masks() / the GPU factory)."""
         lib = load()
         self.cage = cage
         self.level = level
@@ -66,7 +70,8 @@ class UniformRefiner:
                                          cs.ctypes.data if len(cs) else None)
         if not self.h:
             raise ValueError(_err())
-        if lib.GB300TopologyRefineUniform(self.h, level) != 0:
+        refine = lib.GB300TopologyRefineUniform if stencils else lib.GB300TopologyRefineTopology
+        if refine(self.h, level) != 0:
             raise ValueError(_err())
 
     def __del__(self):
@@ -96,6 +101,19 @@ class UniformRefiner:
         lib.GB300TopologyStencilCopy(self.h, first, last, sizes.ctypes.data, offsets.ctypes.data,
                                      idx.ctypes.data, w.ctypes.data)
         return dict(sizes=sizes, offsets=offsets, indices=idx, weights=w)
+
+    def masks(self, level):
+        """Subdivision masks of the level-`level` vertices over level - 1 (CSR: int64 offsets,
+        int32 parents, float64 weights), in the order the stencils compose them."""
+        lib = load()
+        n, nnz = C.c_int(0), C.c_int64(0)
+        if lib.GB300TopologyMaskCounts(self.h, level, C.byref(n), C.byref(nnz)):
+            raise ValueError(_err())
+        off = np.empty(n.value + 1, np.int64)
+        idx = np.empty(nnz.value, np.int32)
+        w = np.empty(nnz.value, np.float64)
+        lib.GB300TopologyMaskCopy(self.h, off.ctypes.data, idx.ctypes.data, w.ctypes.data)
+        return off, idx, w
 
     def limit_stencil_table(self, faces, u, v):
         """Bilinear limit stencils with du/dv weights at (ptex face, u, v) locations."""
