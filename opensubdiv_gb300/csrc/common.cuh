@@ -32,6 +32,19 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // Number of SMs of the current device (cached per device).
 int num_sms();
 
+// Runs `fn` (returning a status) once per device for one call site: `done` is that call site's
+// bitmask of devices it already succeeded on (devices >= 64 run it every time).
+template <class F>
+int once_per_device(std::atomic<uint64_t> &done, F fn) {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fn();
+    const uint64_t bit = 1ull << dev;
+    if (done.load(std::memory_order_acquire) & bit) return GB300_OK;
+    const int st = fn();
+    if (st == GB300_OK) done.fetch_or(bit, std::memory_order_release);
+    return st;
+}
+
 // ---- device helpers -----------------------------------------------------------------------
 
 // L2 eviction policies (createpolicy) for the cache-hinted loads below.

@@ -190,12 +190,13 @@ namespace serve {
 
 void on_round_done(void *p) {
     Round *r = (Round *)p;
+    GB300Server *srv = r->srv;  // the scheduler may free r as soon as done is set
     r->tDone = Clock::now();
     {
-        std::lock_guard<std::mutex> lock(r->srv->m);
+        std::lock_guard<std::mutex> lock(srv->m);
         r->done.store(true);
     }
-    r->srv->cv.notify_all();
+    srv->cv.notify_all();
 }
 
 // Arena bytes of one request (its device inputs, outputs and scratch).
@@ -320,9 +321,11 @@ batch::Job stencil_job(const int *sizes, const int *offsets, const int *indices,
 int launch_round(GB300Server *s, Round *r) {
     cudaStream_t st = s->streams[r->stream];
     int err = GB300_OK;
-    auto chk = [&](cudaError_t e, const char *w) {
-        if (err == GB300_OK) err = check_cuda(e, w);
-    };
+    // after the first failure nothing more is queued (the scheduler then drains the stream)
+#define chk(call, what)                                    \
+    do {                                                   \
+        if (err == GB300_OK) err = check_cuda((call), what); \
+    } while (0)
     for (Topology *t : r->uploads)
         if (err == GB300_OK) err = upload_tables(s, t, st);
     // tables uploaded by rounds on other streams
@@ -443,6 +446,7 @@ int launch_round(GB300Server *s, Round *r) {
                                 cudaMemcpyDeviceToHost, st), "GB300Server output copy");
     }
     chk(cudaLaunchHostFunc(st, on_round_done, r), "GB300Server completion callback");
+#undef chk
     return err;
 }
 
@@ -663,7 +667,7 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
                     who, id, L.total, s->tables.capacity());
     int st = check_cuda(cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming), who);
     if (st != GB300_OK) return st;
-    std::lock_guard<std::mutex> lock(s->m);
+    std::vector<void *> pinned;  // CUDA calls stay outside the server lock
     if (s->cfg.pinHostTables) {
         // page-lock the arrays uploads read from; ranges another topology already registered
         // (shared tables) are left as they are, and a range that cannot be registered stays
@@ -673,7 +677,7 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
             const cudaError_t e = cudaHostRegister(const_cast<void *>(p), bytes,
                                                    cudaHostRegisterDefault);
             if (e == cudaSuccess)
-                s->registered.push_back(const_cast<void *>(p));
+                pinned.push_back(const_cast<void *>(p));
             else
                 cudaGetLastError();
         };
@@ -692,6 +696,8 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
             pin(t->map.handles.data(), t->map.handles.size() * 4);
         }
     }
+    std::lock_guard<std::mutex> lock(s->m);
+    s->registered.insert(s->registered.end(), pinned.begin(), pinned.end());
     auto it = s->topos.find(id);
     if (it != s->topos.end()) {
         cudaEventDestroy(t->ready);
@@ -770,7 +776,9 @@ int GB300ServerReplay(GB300Server *s, int n, const GB300Request *reqs,
     std::vector<uint64_t> tickets(n);
     const Clock::time_point t0 = Clock::now();
     int first = GB300_OK;
-    for (int i = 0; i < n; ++i) {
+    int submitted = 0;
+    for (; submitted < n; ++submitted) {
+        const int i = submitted;
         // open loop: submit at the trace's arrival time (spin for the last 50 us)
         for (;;) {
             const double wait = arrivalSeconds[i] - seconds_since(t0);
@@ -779,12 +787,19 @@ int GB300ServerReplay(GB300Server *s, int n, const GB300Request *reqs,
                 std::this_thread::sleep_for(std::chrono::duration<double>(wait - 50e-6));
         }
         const int st = GB300ServerSubmit(s, &reqs[i], &tickets[i]);
-        if (st != GB300_OK) return st;
+        if (st != GB300_OK) {
+            first = st;
+            break;
+        }
     }
+    // wait for everything submitted, even after a rejected request: the requests' buffers
+    // belong to the caller, who may free them once this returns
     for (int i = 0; i < n; ++i) {
         double lat = -1;
-        const int st = GB300ServerWait(s, tickets[i], &lat);
-        if (st != GB300_OK && first == GB300_OK) first = st;
+        if (i < submitted) {
+            const int st = GB300ServerWait(s, tickets[i], &lat);
+            if (st != GB300_OK && first == GB300_OK) first = st;
+        }
         if (latencySeconds) latencySeconds[i] = lat;
     }
     return first == GB300_OK ? ok() : first;

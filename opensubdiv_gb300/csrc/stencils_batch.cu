@@ -395,15 +395,13 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 }
 
 int set_smem_attribute() {
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_stencils_batch,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmem);
-        if (e != cudaSuccess) return check_cuda(e, "batch smem attribute");
-        attr = true;
-    }
-    return GB300_OK;
+    static std::atomic<uint64_t> attr{0};  // devices whose function attribute is set
+    return once_per_device(attr, [] {
+        return check_cuda(cudaFuncSetAttribute(k_stencils_batch,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmem),
+                          "batch smem attribute");
+    });
 }
 
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,

@@ -225,13 +225,13 @@ template <int NW, int VW>
 static int launch(const Args &a, cudaStream_t s) {
     using C = Cfg<NW>;
     auto kern = k_stencils_tma<NW, VW>;
-    static bool attr = false;  // per-process: the attribute is per function
-    if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)C::kSmem);
-        if (e != cudaSuccess) return check_cuda(e, "stencils (staged): smem attribute");
-        attr = true;
-    }
+    static std::atomic<uint64_t> attr{0};  // devices whose function attribute is set
+    const int st = once_per_device(attr, [&] {
+        return check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)C::kSmem),
+                          "stencils (staged): smem attribute");
+    });
+    if (st != GB300_OK) return st;
     static int perSm = 0;
     if (perSm == 0) {
         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kThreads, C::kSmem) !=
