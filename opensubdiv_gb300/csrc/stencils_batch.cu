@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
         stage_ptr(stage, &sidx, &sw, &ssz, &sof);
         const Job &j = sjob[stage];
         if (j.mode == 0) {
-            // one code path for every row width (three inlined widths spill registers)
+            // one code path for every row width (inlined width-specific paths spill registers)
             tile_threads<0>(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
         } else {
             for (int i = m.s0 + warp; i < m.s1; i += kConsumers / 32) {
@@ -290,6 +290,18 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
         }
         __syncwarp();
         if (lane == 0) bar_arrive(&empty[stage]);
+    }
+}
+
+// Row i of a pad job: 8, 12 or 16 floats, 128-bit stores.
+__device__ __forceinline__ void pad_row(const PadJob &j, long long i) {
+    const float *row = j.src + i * j.srcStride;
+    float *d = j.dst + i * j.dstStride;
+    for (int c0 = 0; c0 < j.dstStride; c0 += 4) {
+        float x[4];
+#pragma unroll
+        for (int c = 0; c < 4; ++c) x[c] = c0 + c < j.length ? __ldg(row + c0 + c) : 0.0f;
+        *reinterpret_cast<float4 *>(d + c0) = make_float4(x[0], x[1], x[2], x[3]);
     }
 }
 
@@ -307,32 +319,15 @@ __global__ void __launch_bounds__(256) k_pad_rows(const PadJob *jobs, const long
                 hi = mid - 1;
         }
         const PadJob j = jobs[lo];
-        const long long i = r - __ldg(rowBase + lo);
-        const float *row = j.src + i * j.srcStride;
-        float x[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) x[c] = c < j.length ? __ldg(row + c) : 0.0f;
-        float *d = j.dst + i * 8;
-        asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
-                     "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]), "f"(x[4]), "f"(x[5]),
-                     "f"(x[6]), "f"(x[7])
-                     : "memory");
+        pad_row(j, r - __ldg(rowBase + lo));
     }
 }
 
 __global__ void __launch_bounds__(256) k_pad_one(const PadJob j) {
     const long long step = (long long)gridDim.x * blockDim.x;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < j.numRows;
-         i += step) {
-        const float *row = j.src + i * j.srcStride;
-        float x[8];
-#pragma unroll
-        for (int c = 0; c < 8; ++c) x[c] = c < j.length ? __ldg(row + c) : 0.0f;
-        asm volatile("st.global.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(j.dst + i * 8),
-                     "f"(x[0]), "f"(x[1]), "f"(x[2]), "f"(x[3]), "f"(x[4]), "f"(x[5]),
-                     "f"(x[6]), "f"(x[7])
-                     : "memory");
-    }
+         i += step)
+        pad_row(j, i);
 }
 
 int launch_pad_one(const PadJob &j, cudaStream_t s) {
@@ -522,24 +517,34 @@ int setup_padding(GB300StencilBatch *b, const std::vector<int> &tableRows, cudaS
     std::vector<int> which;
     for (size_t k = 0; k < b->jobs.size(); ++k) {
         const Job &j = b->jobs[k];
-        if (j.vw != 1 || j.length > 8 || tableRows[k] <= 0 || j.numStencils == 0) continue;
-        pads.push_back(PadJob{j.src, nullptr, j.srcStride, j.length, tableRows[k]});
-        base.push_back(base.back() + tableRows[k]);
+        // unaligned rows (scalar gathers), up to 16 floats wide
+        if (j.vw != 1 || padded_stride(j.length) == 0 || tableRows[k] <= 0 ||
+            j.numStencils == 0)
+            continue;
+        pads.push_back(PadJob{j.src, nullptr, j.srcStride, j.length, tableRows[k],
+                              padded_stride(j.length), 0});
         which.push_back((int)k);
     }
     if (pads.empty()) return GB300_OK;
+    long long floats = 0;
+    std::vector<long long> at;
+    for (const PadJob &p : pads) {
+        at.push_back(floats);
+        floats += p.numRows * p.dstStride;
+        base.push_back(base.back() + p.numRows);
+    }
     const long long rows = base.back();
-    int st = check_cuda(cudaMalloc((void **)&b->dPadded, (size_t)rows * 32), "batch padding");
+    int st = check_cuda(cudaMalloc((void **)&b->dPadded, (size_t)floats * 4), "batch padding");
     if (st != GB300_OK) {
         b->dPadded = nullptr;
         return st;
     }
     for (size_t p = 0; p < pads.size(); ++p) {
-        pads[p].dst = b->dPadded + base[p] * 8;
+        pads[p].dst = b->dPadded + at[p];
         Job &j = b->jobs[which[p]];
         j.src = pads[p].dst;
-        j.srcStride = 8;
-        j.vw = 8;
+        j.srcStride = pads[p].dstStride;
+        j.vw = pads[p].dstStride == 12 ? 4 : 8;
     }
     const size_t padBytes = ((pads.size() * sizeof(PadJob) + 255) / 256) * 256;
     st = check_cuda(cudaMalloc((void **)&b->dPad, padBytes + base.size() * sizeof(long long)),

@@ -46,15 +46,23 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
                 int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1);
 
-// Padded copy of one source: rows [0, numRows) of `src` (length <= 8 floats, srcStride apart)
-// written to `dst` with a stride of 8 floats (elements >= length are 0), so the gathers of an
-// unaligned layout become 256-bit loads.  Values are copied, so results do not change.
+// Padded copy of one source: rows [0, numRows) of `src` (length <= 16 floats, srcStride
+// apart) written to `dst` with a stride of dstStride = 8, 12 or 16 floats (elements >= length
+// are 0), so the gathers of an unaligned layout become vector loads: 256-bit rows of 8, three
+// 128-bit chunks for 9-12 floats (only the bytes used), 256-bit pairs for 13-16.  Values are
+// copied, so results do not change.
 struct PadJob {
     const float *src;
     float *dst;
     int srcStride, length;
     long long numRows;
+    int dstStride, pad;
 };
+
+// Row stride of the padded copy of a source `length` floats wide (0: not padded).
+inline int padded_stride(int length) {
+    return length <= 8 ? 8 : length <= 12 ? 12 : length <= 16 ? 16 : 0;
+}
 
 // One launch over `count` pad jobs (device arrays: jobs, rowBase[count + 1] = prefix of their
 // numRows).  Nothing is launched when totalRows is 0.

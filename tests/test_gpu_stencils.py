@@ -283,11 +283,12 @@ def test_invalid_requests_return_false_and_empty_ranges_are_noops():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("length,stride,offset", [(3, 3, 0), (5, 7, 2), (8, 9, 1), (1, 1, 0)])
+@pytest.mark.parametrize("length,stride,offset", [(3, 3, 0), (5, 7, 2), (8, 9, 1), (1, 1, 0),
+                                                   (12, 12, 0), (11, 13, 3), (16, 16, 0)])
 def test_device_table_unaligned_rows_on_a_large_table(length, stride, offset):
-    """Device tables of >= 1M entries gather unaligned source rows from a padded copy: results
-    must be bit-identical to the raw entry point (which gathers in place) and match the
-    oracle."""
+    """Device tables of >= 1M entries gather unaligned source rows from a padded copy (rows of
+    8, 12 or 16 floats, gathered with vector loads): results must be bit-identical to the
+    raw entry point (which gathers in place) and match the oracle."""
     torch = torch_cuda()
     from opensubdiv_gb300 import shapes
     from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
