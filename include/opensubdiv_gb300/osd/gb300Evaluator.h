@@ -145,6 +145,10 @@ public:
     void *GetDvvWeightsBuffer() const { return GB300StencilTableGetBuffer(_h, 8); }
     int GetNumStencils() const { return GB300StencilTableGetNumStencils(_h); }
     ::GB300StencilTable *GetHandle() const { return _h; }
+    /// Takes ownership of a table made by the C ABI (e.g. GB300StencilTableFactoryCreate).
+    static GB300StencilTable *Adopt(::GB300StencilTable *h) {
+        return h ? new GB300StencilTable(h) : nullptr;
+    }
 
 private:
     explicit GB300StencilTable(::GB300StencilTable *h) : _h(h) {}

@@ -141,6 +141,59 @@ int GB300StencilTableEval(const GB300StencilTable *table, const float *src, floa
                           int srcStride, int dstStride, int duStride, int dvStride,
                           int duuStride, int duvStride, int dvvStride, void *stream);
 
+/* Copies device buffer `which` (as GB300StencilTableGetBuffer) of a table to HOST memory:
+ * numStencils ints for sizes / offsets, numIndices elements otherwise.  Synchronous. */
+int GB300StencilTableCopyBuffer(const GB300StencilTable *table, int which, void *hostDst,
+                                void *stream);
+
+/* ---- GPU stencil-table factory (Far::StencilTableFactory, far/stencilTableFactory.cpp) ---- */
+
+/* The subdivision masks of one refinement level, in HOST memory: for each vertex of the level
+ * (row order), the (source, weight) pairs that Far::PrimvarRefiner::Interpolate /
+ * InterpolateVarying / InterpolateFaceVarying passes to StencilBuilder::Index::AddWithWeight
+ * (far/primvarRefiner.h:475-650, far/stencilBuilder.cpp:509-518), in call order, zero weights
+ * left out.  Sources are global vertex indices: control vertices [0, numControl), then the
+ * vertices of level 1, 2, ... concatenated.  A level's masks refer to the previous level and
+ * to vertices of their own level (Catmark face points feed edge and vertex points). */
+typedef struct GB300StencilMasks {
+    int numRows;
+    int64_t nnz;
+    const int64_t *offsets; /* numRows + 1 */
+    const int *sources;     /* nnz */
+    const float *weights;   /* nnz */
+} GB300StencilMasks;
+
+/* Far::StencilTableFactory::Create (far/stencilTableFactory.cpp:78-151) with
+ * factorizeIntermediateLevels, merging on the device: each row is the merge, in first-touch
+ * order with float products and sums, of its mask weights times the factorized rows of its
+ * sources (control vertices are rows of one entry of weight 1), exactly as WeightTable::merge
+ * (far/stencilBuilder.cpp:164-198,310-385).  The table holds the rows of every level
+ * (generateIntermediateLevels) or of the last level only, preceded by one identity stencil per
+ * control vertex when generateControlVerts is set.  sortEntries = 0 keeps each stencil's
+ * entries in Far's order (the table then equals Far's bit for bit); 1 sorts them by control
+ * index (the GB300StencilTableCreate layout).  Returns NULL on failure (status recorded). */
+GB300StencilTable *GB300StencilTableFactoryCreate(int numControl, int numLevels,
+                                                  const GB300StencilMasks *levels,
+                                                  int generateIntermediateLevels,
+                                                  int generateControlVerts, int sortEntries,
+                                                  void *stream);
+
+/* Stencils composed from the stencils of a DEVICE table given by its arrays in Far's layout
+ * (baseSizes / baseOffsets per stencil, baseIndices, baseWeights): row i merges, over its mask
+ * entries k (HOST arrays offsets[numRows + 1], sources, weights[c] for c < numChannels), the
+ * products weights[c][k] * w of the entries (index, w) of base stencil sources[k], zero w
+ * skipped, first-touch order, float arithmetic -- StencilBuilder::Index::AddWithWeight with a
+ * StencilReal source (far/stencilBuilder.cpp:520-598).  numChannels 1, 3 (P, du, dv) or
+ * 6 (+ duu, duv, dvv).  appendBase = 1 puts the base stencils first (AppendLocalPointStencilTable,
+ * far/stencilTableFactory.cpp:255-407, with local-point stencils as the masks); 0 returns the
+ * composed rows alone (LimitStencilTableFactory's per-location stencils,
+ * far/stencilTableFactory.cpp:560-640, with patch CVs and basis weights as the masks). */
+GB300StencilTable *GB300StencilTableComposeRows(
+    int baseNumStencils, int64_t baseNumIndices, const int *baseSizes, const int *baseOffsets,
+    const int *baseIndices, const float *baseWeights, int numRows, int64_t nnz,
+    const int64_t *offsets, const int *sources, int numChannels, const float *const *weights,
+    int appendBase, int sortEntries, void *stream);
+
 /* ---- device patch table (CudaPatchTable, osd/cudaPatchTable.h:51-110) -------------------- */
 
 typedef struct GB300PatchTable GB300PatchTable;

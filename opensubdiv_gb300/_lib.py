@@ -35,6 +35,10 @@ _PROTOS = {
     "GB300StencilTableGetNumIndices": (i64, [vp]),
     "GB300StencilTableGetBuffer": (vp, [vp, i32]),
     "GB300StencilTableEval": (i32, [vp, vp] + [vp] * 6 + [i32] * 8 + [vp]),
+    "GB300StencilTableCopyBuffer": (i32, [vp, i32, vp, vp]),
+    "GB300StencilTableFactoryCreate": (vp, [i32, i32, vp, i32, i32, i32, vp]),
+    "GB300StencilTableComposeRows": (vp, [i32, i64, vp, vp, vp, vp, i32, i64, vp, vp, i32, vp,
+                                          i32, i32, vp]),
     "GB300PatchTableCreate": (vp, [i32, vp, i64, vp, i32, vp, i32, vp]),
     "GB300PatchTableDestroy": (None, [vp]),
     "GB300PatchTableGetBuffer": (vp, [vp, i32]),

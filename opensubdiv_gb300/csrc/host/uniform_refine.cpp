@@ -234,13 +234,17 @@ void refine_topology(int scheme, const Level &P, Level &C) {
 }
 
 // A child vertex as a small combination of parent vertices.
+// At most 64 distinct parents (a Catmark vertex of valence up to 31 over quads); a mask that
+// would need more sets `overflow` and the refinement reports an error.
 struct Mask {
     int n = 0;
+    bool overflow = false;
     int idx[64];
     double w[64];
     void add(int i, double x) {
         for (int k = 0; k < n; ++k)
             if (idx[k] == i) { w[k] += x; return; }
+        if (n == 64) { overflow = true; return; }
         idx[n] = i; w[n] = x; ++n;
     }
 };
@@ -340,8 +344,8 @@ void vertex_mask(int scheme, const Level &P, int v, Mask &m) {
     rule_mask(scheme, P, v, cr, cEnds, 1.0 - pw, m);
 }
 
-// Composes child masks with the parent's factorized rows.
-void compose(int scheme, const Level &P, const Rows &prow, int nControl, Rows &crow,
+// Composes child masks with the parent's factorized rows; false when a mask overflowed.
+bool compose(int scheme, const Level &P, const Rows &prow, int nControl, Rows &crow,
              int nChild) {
     const bool cat = scheme == kCatmark;
     const int vFace = cat ? P.nv : -1, vEdge = cat ? P.nv + P.nf : P.nv;
@@ -358,7 +362,8 @@ void compose(int scheme, const Level &P, const Rows &prow, int nControl, Rows &c
     std::vector<std::vector<double>> lw(nth);
     std::vector<int64_t> chunkStart(nth + 1, 0);
     const int chunk = (nChild + nth - 1) / nth;
-#pragma omp parallel num_threads(nth)
+    int overflow = 0;
+#pragma omp parallel num_threads(nth) reduction(| : overflow)
     {
         int t = 0;
 #ifdef _OPENMP
@@ -376,6 +381,7 @@ void compose(int scheme, const Level &P, const Rows &prow, int nControl, Rows &c
             if (c < P.nv) vertex_mask(scheme, P, c, m);
             else if (cat && c < vEdge) add_face_point(P, c - vFace, 1.0, m);
             else edge_mask(scheme, P, c - vEdge, m);
+            overflow |= m.overflow ? 1 : 0;
             touched.clear();
             for (int k = 0; k < m.n; ++k) {
                 const int p = m.idx[k];
@@ -404,6 +410,7 @@ void compose(int scheme, const Level &P, const Rows &prow, int nControl, Rows &c
         std::copy(lw[t].begin(), lw[t].end(), crow.w.begin() + pos);
         pos += (int64_t)lidx[t].size();
     }
+    return !overflow;
 }
 
 int fail(const char *msg) {
@@ -477,8 +484,10 @@ int GB300TopologyRefineUniform(void *p, int level) {
     while ((int)t->rows.size() <= level) {
         const size_t l = t->rows.size();  // compose level l from level l - 1
         Rows r;
-        compose(t->scheme, t->levels[l - 1], t->rows.back(), t->levels[0].nv, r,
-                t->levels[l].nv);
+        if (!compose(t->scheme, t->levels[l - 1], t->rows.back(), t->levels[0].nv, r,
+                     t->levels[l].nv))
+            return fail("GB300TopologyRefineUniform: a vertex valence or face size beyond "
+                        "the generator's 64-parent masks");
         t->rows.push_back(std::move(r));
     }
     return 0;
@@ -502,11 +511,18 @@ int GB300TopologyMaskCounts(void *p, int level, int *nChild, int64_t *nnz) {
     };
     // two passes (sizes, then the masks again into place): no per-child staging buffer
     t->maskOff.assign(nc + 1, 0);
-#pragma omp parallel for schedule(static)
+    int overflow = 0;
+#pragma omp parallel for schedule(static) reduction(| : overflow)
     for (int c = 0; c < nc; ++c) {
         Mask m;
         mask_of(c, m);
         t->maskOff[c + 1] = m.n;
+        overflow |= m.overflow ? 1 : 0;
+    }
+    if (overflow) {
+        std::vector<int64_t>().swap(t->maskOff);
+        return fail("GB300TopologyMaskCounts: a vertex valence or face size beyond the "
+                    "generator's 64-parent masks");
     }
     for (int c = 0; c < nc; ++c) t->maskOff[c + 1] += t->maskOff[c];
     t->maskIdx.resize(t->maskOff[nc]);

@@ -5,6 +5,7 @@
 #include "common.cuh"
 #include "patchmap.h"
 #include "stencils_batch.h"
+#include "tables.h"
 
 #include <algorithm>
 #include <new>
@@ -295,7 +296,33 @@ namespace gb300 {
 namespace batch {
 int stencil_table_num_control(const GB300StencilTable *t) { return t ? t->numControl : 0; }
 }  // namespace batch
+
+GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
+                                       void *const buf[9]) {
+    GB300StencilTable *t = new (std::nothrow) GB300StencilTable;
+    if (!t) return nullptr;
+    t->numStencils = numStencils;
+    t->nnz = nnz;
+    t->numControl = numControl;
+    for (int k = 0; k < 9; ++k) t->buf[k] = buf[k];
+    return t;
+}
 }  // namespace gb300
+
+extern "C" int GB300StencilTableCopyBuffer(const GB300StencilTable *t, int which, void *hostDst,
+                                           void *stream) {
+    if (!t || which < 0 || which > 8 || !hostDst)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilTableCopyBuffer: bad arguments");
+    const size_t n = which < 2 ? (size_t)t->numStencils : (size_t)t->nnz;
+    if (!t->buf[which] || n == 0) return ok();
+    cudaStream_t s = as_stream(stream);
+    if (check_cuda(cudaMemcpyAsync(hostDst, t->buf[which], n * 4, cudaMemcpyDeviceToHost, s),
+                   "GB300StencilTableCopyBuffer") != GB300_OK)
+        return GB300_ERR_CUDA;
+    if (check_cuda(cudaStreamSynchronize(s), "GB300StencilTableCopyBuffer") != GB300_OK)
+        return GB300_ERR_CUDA;
+    return ok();
+}
 
 extern "C" {
 

@@ -17,6 +17,7 @@ Device memory is plain CUDA memory; torch tensors are accepted as a convenience.
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass
 
 import numpy as np
@@ -248,6 +249,47 @@ class GB300StencilTable:
     def _buf(self, k):
         return _lib.load().GB300StencilTableGetBuffer(self.handle, k)
 
+    def GetNumIndices(self):
+        return _lib.load().GB300StencilTableGetNumIndices(self.handle)
+
+    def CopyToHost(self, stream=None):
+        """The table's device arrays as numpy arrays (Far names: sizes, offsets, indices,
+        weights and, where present, du_weights ... dvv_weights)."""
+        n, nnz = self.GetNumStencils(), self.GetNumIndices()
+        names = ("sizes", "offsets", "indices", "weights", "du_weights", "dv_weights",
+                 "duu_weights", "duv_weights", "dvv_weights")
+        out = {}
+        for k, name in enumerate(names):
+            if not self._buf(k):
+                continue
+            a = np.zeros(n if k < 2 else nnz, np.int32 if k < 3 else np.float32)
+            check(_lib.load().GB300StencilTableCopyBuffer(self.handle, k, a.ctypes.data,
+                                                          _stream(stream)))
+            out[name] = a
+        return out
+
+    @classmethod
+    def ComposeRows(cls, base, offsets, sources, weights, appendBase=False, sortEntries=True,
+                    stream=None):
+        """Stencils composed over the rows of a device table `base` (a GB300StencilTable
+        whose entries are in Far's order, e.g. from GB300StencilTableFactory.Create with
+        sortEntries=False): row i merges weights[c][k] * w over the entries (index, w) of base
+        stencil sources[k] (StencilBuilder::Index::AddWithWeight with a StencilReal source,
+        far/stencilBuilder.cpp:520-598).  weights: list of 1, 3 or 6 host float32 arrays."""
+        off = np.ascontiguousarray(offsets, np.int64)
+        src = np.ascontiguousarray(sources, np.int32)
+        ws = [np.ascontiguousarray(w, np.float32) for w in weights]
+        wp = (C.c_void_p * len(ws))(*[w.ctypes.data for w in ws])
+        L = _lib.load()
+        h = L.GB300StencilTableComposeRows(
+            base.GetNumStencils(), base.GetNumIndices(), base.GetSizesBuffer(),
+            base.GetOffsetsBuffer(), base.GetIndicesBuffer(), base.GetWeightsBuffer(),
+            len(off) - 1, len(src), off.ctypes.data, src.ctypes.data if len(src) else None,
+            len(ws), wp, int(bool(appendBase)), int(bool(sortEntries)), _stream(stream))
+        if not h:
+            raise GB300Error(1, last_error())
+        return cls(h)
+
     def GetSizesBuffer(self): return self._buf(0)
     def GetOffsetsBuffer(self): return self._buf(1)
     def GetIndicesBuffer(self): return self._buf(2)
@@ -257,6 +299,41 @@ class GB300StencilTable:
     def GetDuuWeightsBuffer(self): return self._buf(6)
     def GetDuvWeightsBuffer(self): return self._buf(7)
     def GetDvvWeightsBuffer(self): return self._buf(8)
+
+
+class _StencilMasks(C.Structure):
+    _fields_ = [("numRows", C.c_int), ("nnz", C.c_int64), ("offsets", C.c_void_p),
+                ("sources", C.c_void_p), ("weights", C.c_void_p)]
+
+
+class GB300StencilTableFactory:
+    """Far::StencilTableFactory::Create (factorized) with the merging on the GPU, from the
+    per-level masks Far::PrimvarRefiner produces (as recorded by GB300MaskRecorder in
+    include/opensubdiv_gb300/far/gb300StencilTableFactory.h)."""
+
+    @staticmethod
+    def Create(numControl, levels, generateIntermediateLevels=True, generateControlVerts=False,
+               sortEntries=True, stream=None):
+        """levels: per refinement level a dict of host arrays offsets (int64, rows + 1),
+        sources (int32, global vertex indices) and weights (float32).  sortEntries=False keeps
+        each stencil's entries in Far's order (the table then equals Far's bit for bit)."""
+        keep = []
+        views = (_StencilMasks * max(1, len(levels)))()
+        for i, d in enumerate(levels):
+            off = np.ascontiguousarray(d["offsets"], np.int64)
+            src = np.ascontiguousarray(d["sources"], np.int32)
+            w = np.ascontiguousarray(d["weights"], np.float32)
+            keep += [off, src, w]
+            views[i] = _StencilMasks(len(off) - 1, len(src), off.ctypes.data,
+                                     src.ctypes.data if len(src) else None,
+                                     w.ctypes.data if len(w) else None)
+        h = _lib.load().GB300StencilTableFactoryCreate(
+            int(numControl), len(levels), C.cast(views, C.c_void_p),
+            int(bool(generateIntermediateLevels)), int(bool(generateControlVerts)),
+            int(bool(sortEntries)), _stream(stream))
+        if not h:
+            raise GB300Error(1, last_error())
+        return GB300StencilTable(h)
 
 
 class GB300StencilBatch:

@@ -192,6 +192,21 @@ def icosphere(subdivisions: int = 6, noise: float = 0.005, seed: int = 0) -> Cag
                 np.asarray(tris, np.int32).ravel(), scheme=LOOP, name=f"icosphere{subdivisions}")
 
 
+def bipyramid(n: int = 360, height: float = 1.0, scheme: int = CATMARK) -> Cage:
+    """A closed double cone: a ring of n vertices and two poles of valence n joined by 2n
+    triangles -- the extraordinary-vertex stress case (rows of hundreds of entries)."""
+    a = np.arange(n) * (2.0 * np.pi / n)
+    ring = np.stack([np.cos(a), np.sin(a), np.zeros(n)], 1)
+    pos = np.concatenate([ring, [[0.0, 0.0, height], [0.0, 0.0, -height]]])
+    top, bot = n, n + 1
+    i = np.arange(n)
+    j = (i + 1) % n
+    tris = np.concatenate([np.stack([np.full(n, top), i, j], 1),
+                           np.stack([np.full(n, bot), j, i], 1)])
+    return Cage(pos.astype(np.float32), np.full(2 * n, 3, np.int32),
+                tris.astype(np.int32).ravel(), scheme=scheme, name=f"bipyramid{n}")
+
+
 def grid(nx: int = 6, ny: int = 6, noise: float = 0.02, seed: int = 0,
          scheme: int = CATMARK) -> Cage:
     """Open (nx x ny)-quad planar grid with a height field; has boundary edges and corners.

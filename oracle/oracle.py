@@ -138,3 +138,70 @@ def make_coords(handles, s, t):
     out[:, 3] = np.asarray(s, np.float32).view(np.int32)
     out[:, 4] = np.asarray(t, np.float32).view(np.int32)
     return out
+
+
+class _OrcTable(C.Structure):
+    _fields_ = [("numStencils", C.c_int), ("numChannels", C.c_int), ("nnz", C.c_longlong),
+                ("sizes", C.POINTER(C.c_int)), ("offsets", C.POINTER(C.c_int)),
+                ("indices", C.POINTER(C.c_int)), ("w", C.POINTER(C.c_float) * 6)]
+
+
+def _take_table(ptr):
+    if not ptr:
+        raise ValueError("malformed masks")
+    t = ptr.contents
+    n, nnz = t.numStencils, t.nnz
+    out = dict(sizes=np.ctypeslib.as_array(t.sizes, (max(n, 1),))[:n].copy(),
+               offsets=np.ctypeslib.as_array(t.offsets, (max(n, 1),))[:n].copy(),
+               indices=np.ctypeslib.as_array(t.indices, (max(nnz, 1),))[:nnz].copy())
+    names = ("weights", "du_weights", "dv_weights", "duu_weights", "duv_weights",
+             "dvv_weights")
+    for c in range(t.numChannels):
+        out[names[c]] = np.ctypeslib.as_array(t.w[c], (max(nnz, 1),))[:nnz].copy()
+    lib().orc_table_free(ptr)
+    return out
+
+
+def _factory_protos():
+    L = lib()
+    if getattr(L, "_factory_protos", False):
+        return L
+    L.orc_factory_create.restype = C.POINTER(_OrcTable)
+    L.orc_compose_rows.restype = C.POINTER(_OrcTable)
+    L.orc_table_free.argtypes = [C.POINTER(_OrcTable)]
+    L._factory_protos = True
+    return L
+
+
+def factory_create(num_control, levels, intermediate=True, control=False):
+    """Restated Far::StencilTableFactory::Create (factorized) from per-level masks
+    (dicts of offsets int64, sources int32, weights float32), as far/stencilBuilder.cpp
+    merges them.  Returns dict(sizes, offsets, indices, weights)."""
+    L = _factory_protos()
+    offs = [np.ascontiguousarray(d["offsets"], np.int64) for d in levels]
+    srcs = [np.ascontiguousarray(d["sources"], np.int32) for d in levels]
+    ws = [np.ascontiguousarray(d["weights"], np.float32) for d in levels]
+    nrows = np.array([len(o) - 1 for o in offs], np.int32)
+    ptr = L.orc_factory_create(
+        C.c_int(num_control), C.c_int(len(offs)), _p(nrows), _ptrs(offs) if offs else None,
+        _ptrs(srcs) if offs else None, _ptrs(ws) if offs else None,
+        C.c_int(int(intermediate)), C.c_int(int(control)))
+    return _take_table(ptr)
+
+
+def compose_rows(base, offsets, sources, weights, append_base=False):
+    """Restated StencilBuilder::Index::AddWithWeight(StencilReal, ...) composition of rows
+    over a base table (dict of sizes, offsets, indices, weights); weights is a list of 1, 3
+    or 6 float32 arrays (P, du, dv[, duu, duv, dvv])."""
+    L = _factory_protos()
+    bs = np.ascontiguousarray(base["sizes"], np.int32)
+    bo = np.ascontiguousarray(base["offsets"], np.int32)
+    bi = np.ascontiguousarray(base["indices"], np.int32)
+    bw = np.ascontiguousarray(base["weights"], np.float32)
+    off = np.ascontiguousarray(offsets, np.int64)
+    src = np.ascontiguousarray(sources, np.int32)
+    ws = [np.ascontiguousarray(w, np.float32) for w in weights]
+    ptr = L.orc_compose_rows(C.c_int(len(bs)), _p(bs), _p(bo), _p(bi), _p(bw),
+                             C.c_int(len(off) - 1), _p(off), _p(src), C.c_int(len(ws)),
+                             _ptrs(ws), C.c_int(int(append_base)))
+    return _take_table(ptr)

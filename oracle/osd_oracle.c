@@ -404,3 +404,250 @@ int orc_find_patches(const void *p, int n, const int *faces, const double *uu,
     }
     return found;
 }
+
+/* ---- stencil-table factory ----------------------------------------------------------------
+ * A restatement of Far's StencilBuilder (far/stencilBuilder.cpp): a row is built by merging
+ * (index, weight) terms; a term whose index is already in the row is added to that entry
+ * (WeightTable::merge, :310-346), otherwise appended (WeightTable::add, :348-385).  A mask
+ * entry (source s, weight m) contributes m itself for a control vertex and w * m for every
+ * entry (i, w) of s's factorized row otherwise (WeightTable::AddWithWeight, :164-198). */
+
+typedef struct {
+    int *idx;
+    float *w[6];
+    long long n, cap;
+    int nc;
+} orc_arena;
+
+static int arena_grow(orc_arena *a, long long need) {
+    if (need <= a->cap) return 1;
+    long long cap = a->cap ? a->cap : 1024;
+    while (cap < need) cap *= 2;
+    int *ni = (int *)realloc(a->idx, (size_t)cap * sizeof(int));
+    if (!ni) return 0;
+    a->idx = ni;
+    for (int c = 0; c < a->nc; ++c) {
+        float *nw = (float *)realloc(a->w[c], (size_t)cap * sizeof(float));
+        if (!nw) return 0;
+        a->w[c] = nw;
+    }
+    a->cap = cap;
+    return 1;
+}
+
+static void arena_free(orc_arena *a) {
+    free(a->idx);
+    for (int c = 0; c < 6; ++c) free(a->w[c]);
+}
+
+/* merges term (q, x[0..nc)) into the row that starts at `start` (the arena's last row) */
+static int row_merge(orc_arena *a, long long start, int q, const float *x) {
+    for (long long i = start; i < a->n; ++i)
+        if (a->idx[i] == q) {
+            for (int c = 0; c < a->nc; ++c) a->w[c][i] += x[c];
+            return 1;
+        }
+    if (!arena_grow(a, a->n + 1)) return 0;
+    a->idx[a->n] = q;
+    for (int c = 0; c < a->nc; ++c) a->w[c][a->n] = x[c];
+    ++a->n;
+    return 1;
+}
+
+void orc_table_free(orc_table *t) {
+    if (!t) return;
+    free(t->sizes);
+    free(t->offsets);
+    free(t->indices);
+    for (int c = 0; c < 6; ++c) free(t->w[c]);
+    free(t);
+}
+
+static orc_table *table_alloc(int n, long long nnz, int nc) {
+    orc_table *t = (orc_table *)calloc(1, sizeof(orc_table));
+    if (!t) return NULL;
+    t->numStencils = n;
+    t->numChannels = nc;
+    t->nnz = nnz;
+    t->sizes = (int *)malloc((size_t)(n ? n : 1) * sizeof(int));
+    t->offsets = (int *)malloc((size_t)(n ? n : 1) * sizeof(int));
+    t->indices = (int *)malloc((size_t)(nnz ? nnz : 1) * sizeof(int));
+    int good = t->sizes && t->offsets && t->indices;
+    for (int c = 0; c < nc; ++c) {
+        t->w[c] = (float *)malloc((size_t)(nnz ? nnz : 1) * sizeof(float));
+        good = good && t->w[c];
+    }
+    if (!good) {
+        orc_table_free(t);
+        return NULL;
+    }
+    return t;
+}
+
+orc_table *orc_factory_create(int numControl, int numLevels, const int *numRows,
+                              const long long *const *offsets, const int *const *sources,
+                              const float *const *weights, int generateIntermediateLevels,
+                              int generateControlVerts) {
+    if (numControl < 0 || numLevels < 0) return NULL;
+    long long total = 0;
+    for (int l = 0; l < numLevels; ++l) total += numRows[l];
+    long long *rowOff = (long long *)malloc((size_t)(total ? total : 1) * sizeof(long long));
+    int *rowSize = (int *)malloc((size_t)(total ? total : 1) * sizeof(int));
+    char *done = (char *)calloc((size_t)(total ? total : 1), 1);
+    orc_arena a;
+    memset(&a, 0, sizeof(a));
+    a.nc = 1;
+    orc_table *t = NULL;
+    int good = rowOff && rowSize && done;
+    long long first = numControl; /* global index of the current level's row 0 */
+    for (int l = 0; l < numLevels && good; ++l) {
+        const long long prevFirst = l ? first - numRows[l - 1] : 0;
+        const long long *mo = offsets[l];
+        const int *ms = sources[l];
+        const float *mw = weights[l];
+        long long left = numRows[l];
+        while (left > 0 && good) {
+            long long progress = 0;
+            for (int r = 0; r < numRows[l] && good; ++r) {
+                const long long g = first + r - numControl;
+                if (done[g]) continue;
+                int ready = 1;
+                for (long long k = mo[r]; k < mo[r + 1]; ++k) {
+                    const long long s = ms[k];
+                    if (s < 0 || s >= first + numRows[l] ||
+                        (s >= numControl && s < (l ? prevFirst : numControl))) {
+                        good = 0; /* a source outside the previous level and this one */
+                        break;
+                    }
+                    if (s >= first && !done[s - numControl]) ready = 0;
+                }
+                if (!good || !ready) continue;
+                const long long start = a.n;
+                for (long long k = mo[r]; k < mo[r + 1] && good; ++k) {
+                    const int s = ms[k];
+                    const float m = mw[k];
+                    if (m == 0.0f) continue;
+                    if (s < numControl) {
+                        const float x = m * 1.0f;
+                        good = row_merge(&a, start, s, &x);
+                        continue;
+                    }
+                    const long long o = rowOff[s - numControl];
+                    const int n = rowSize[s - numControl];
+                    for (int j = 0; j < n && good; ++j) {
+                        const float x = a.w[0][o + j] * m;
+                        good = row_merge(&a, start, a.idx[o + j], &x);
+                    }
+                }
+                rowOff[g] = start;
+                rowSize[g] = (int)(a.n - start);
+                done[g] = 1;
+                ++progress;
+                --left;
+            }
+            if (!progress) good = 0; /* rows that wait on each other */
+        }
+        first += numRows[l];
+    }
+    if (good) {
+        const int firstLevel = generateIntermediateLevels ? 0 : (numLevels ? numLevels - 1 : 0);
+        long long firstRow = 0;
+        for (int l = 0; l < firstLevel; ++l) firstRow += numRows[l];
+        const int nc = generateControlVerts ? numControl : 0;
+        const long long nr = numLevels ? total - firstRow : 0;
+        long long nnz = nc;
+        for (long long g = firstRow; g < firstRow + nr; ++g) nnz += rowSize[g];
+        t = table_alloc((int)(nc + nr), nnz, 1);
+        if (t) {
+            long long e = 0;
+            int i = 0;
+            for (int v = 0; v < nc; ++v, ++i) {
+                t->sizes[i] = 1;
+                t->offsets[i] = (int)e;
+                t->indices[e] = v;
+                t->w[0][e++] = 1.0f;
+            }
+            for (long long g = firstRow; g < firstRow + nr; ++g, ++i) {
+                t->sizes[i] = rowSize[g];
+                t->offsets[i] = (int)e;
+                memcpy(t->indices + e, a.idx + rowOff[g], (size_t)rowSize[g] * sizeof(int));
+                memcpy(t->w[0] + e, a.w[0] + rowOff[g], (size_t)rowSize[g] * sizeof(float));
+                e += rowSize[g];
+            }
+        }
+    }
+    free(rowOff);
+    free(rowSize);
+    free(done);
+    arena_free(&a);
+    return t;
+}
+
+orc_table *orc_compose_rows(int baseNumStencils, const int *baseSizes, const int *baseOffsets,
+                            const int *baseIndices, const float *baseWeights, int numRows,
+                            const long long *offsets, const int *sources, int numChannels,
+                            const float *const *weights, int appendBase) {
+    if (numChannels != 1 && numChannels != 3 && numChannels != 6) return NULL;
+    orc_arena a;
+    memset(&a, 0, sizeof(a));
+    a.nc = numChannels;
+    long long *rowOff = (long long *)malloc((size_t)(numRows ? numRows : 1) * sizeof(long long));
+    int good = rowOff != NULL;
+    for (int r = 0; r < numRows && good; ++r) {
+        const long long start = a.n;
+        for (long long k = offsets[r]; k < offsets[r + 1] && good; ++k) {
+            const int s = sources[k];
+            if (s < 0 || s >= baseNumStencils) {
+                good = 0;
+                break;
+            }
+            float m[6];
+            int any = 0;
+            for (int c = 0; c < numChannels; ++c) {
+                m[c] = weights[c][k];
+                any |= m[c] != 0.0f;
+            }
+            if (!any) continue;
+            for (int j = 0; j < baseSizes[s] && good; ++j) {
+                const float w = baseWeights[baseOffsets[s] + j];
+                if (w == 0.0f) continue;
+                float x[6];
+                for (int c = 0; c < numChannels; ++c) x[c] = m[c] * w;
+                good = row_merge(&a, start, baseIndices[baseOffsets[s] + j], x);
+            }
+        }
+        rowOff[r] = start;
+    }
+    orc_table *t = NULL;
+    if (good) {
+        long long baseNnz = 0;
+        const int nb = appendBase ? baseNumStencils : 0;
+        for (int i = 0; i < nb; ++i) baseNnz += baseSizes[i];
+        t = table_alloc(nb + numRows, baseNnz + a.n, numChannels);
+        if (t) {
+            long long e = 0;
+            int i = 0;
+            for (int b = 0; b < nb; ++b, ++i) {
+                t->sizes[i] = baseSizes[b];
+                t->offsets[i] = (int)e;
+                for (int j = 0; j < baseSizes[b]; ++j, ++e) {
+                    t->indices[e] = baseIndices[baseOffsets[b] + j];
+                    t->w[0][e] = baseWeights[baseOffsets[b] + j];
+                    for (int c = 1; c < numChannels; ++c) t->w[c][e] = 0.0f;
+                }
+            }
+            for (int r = 0; r < numRows; ++r, ++i) {
+                const long long end = r + 1 < numRows ? rowOff[r + 1] : a.n;
+                t->sizes[i] = (int)(end - rowOff[r]);
+                t->offsets[i] = (int)e;
+                for (long long j = rowOff[r]; j < end; ++j, ++e) {
+                    t->indices[e] = a.idx[j];
+                    for (int c = 0; c < numChannels; ++c) t->w[c][e] = a.w[c][j];
+                }
+            }
+        }
+    }
+    free(rowOff);
+    arena_free(&a);
+    return t;
+}

@@ -68,6 +68,39 @@ void orc_patchmap_free(void *map);
 int orc_find_patches(const void *map, int n, const int *faces, const double *u,
                      const double *v, int *handles);
 
+/* ---- stencil-table factory (far/stencilTableFactory.cpp, far/stencilBuilder.cpp) ---------- */
+
+/* A stencil table produced by the factory restatements below (malloc'ed; free with
+ * orc_table_free).  w[c] for c < numChannels. */
+typedef struct orc_table {
+    int numStencils, numChannels;
+    long long nnz;
+    int *sizes, *offsets, *indices;
+    float *w[6];
+} orc_table;
+
+void orc_table_free(orc_table *t);
+
+/* Far::StencilTableFactory::Create with factorizeIntermediateLevels from recorded per-level
+ * masks (levels[l]: numRows[l], offsets[l][numRows + 1], sources[l], weights[l]; sources are
+ * global vertex indices).  Rows are merged as far/stencilBuilder.cpp:164-198 (AddWithWeight)
+ * and :310-385 (merge / add) do: first-touch entry order, float products and sums; rows of a
+ * level are processed after the same-level rows their masks refer to (the order PrimvarRefiner
+ * interpolates in).  Returns NULL on malformed masks. */
+orc_table *orc_factory_create(int numControl, int numLevels, const int *numRows,
+                              const long long *const *offsets, const int *const *sources,
+                              const float *const *weights, int generateIntermediateLevels,
+                              int generateControlVerts);
+
+/* Rows composed from a base table with StencilBuilder::Index::AddWithWeight(StencilReal, ...)
+ * (far/stencilBuilder.cpp:520-598): row i merges weights[c][k] * w over the entries (index, w)
+ * of base stencil sources[k], zero w skipped.  appendBase puts the base stencils first
+ * (AppendLocalPointStencilTable, far/stencilTableFactory.cpp:255-407). */
+orc_table *orc_compose_rows(int baseNumStencils, const int *baseSizes, const int *baseOffsets,
+                            const int *baseIndices, const float *baseWeights, int numRows,
+                            const long long *offsets, const int *sources, int numChannels,
+                            const float *const *weights, int appendBase);
+
 #ifdef __cplusplus
 }
 #endif

@@ -32,6 +32,8 @@ def lib():
         _lib.ref_limit_stencils_create.restype = vp
         _lib.ref_patches_create.restype = vp
         _lib.ref_stencils_nnz.restype = C.c_long
+        _lib.ref_stencils_create_mode.restype = vp
+        _lib.ref_masks_record.restype = vp
         for name in ("ref_refiner_destroy", "ref_refine_uniform", "ref_refine_adaptive",
                      "ref_num_vertices_total", "ref_level_num_vertices", "ref_max_level",
                      "ref_num_ptex_faces", "ref_ptex_face_ids", "ref_stencils_num",
@@ -39,7 +41,9 @@ def lib():
                      "ref_stencils_destroy", "ref_patches_destroy", "ref_patches_counts",
                      "ref_patches_copy", "ref_patches_copy_stencils", "ref_find_patches",
                      "ref_cpu_eval_stencils", "ref_cpu_eval_patches", "ref_eval_patches_fp64",
-                     "ref_omp_set_threads", "ref_patches_varying", "ref_patches_fvar"):
+                     "ref_omp_set_threads", "ref_patches_varying", "ref_patches_fvar",
+                     "ref_masks_num_levels", "ref_masks_num_control", "ref_masks_level_counts",
+                     "ref_masks_level_copy", "ref_masks_destroy"):
             getattr(_lib, name).argtypes = None
     return _lib
 
@@ -132,6 +136,40 @@ def stencil_table(refiner, use_double=False, intermediate=True, factorize=True,
                                              C.c_int(int(intermediate)), C.c_int(int(factorize)),
                                              C.c_int(int(control)), C.c_int(max_level)))
     return _copy_stencils(h, False, use_double)
+
+
+INTERPOLATE_VERTEX, INTERPOLATE_VARYING, INTERPOLATE_FACE_VARYING = 0, 1, 2
+
+
+def stencil_table_mode(refiner, mode=INTERPOLATE_VERTEX, channel=0, intermediate=True,
+                       control=False, max_level=10):
+    """Far::StencilTableFactory::Create (float) in interpolation mode `mode`."""
+    h = C.c_void_p(lib().ref_stencils_create_mode(refiner.h, C.c_int(mode), C.c_int(channel),
+                                                  C.c_int(int(intermediate)),
+                                                  C.c_int(int(control)), C.c_int(max_level)))
+    return _copy_stencils(h, False, False)
+
+
+def record_masks(refiner, mode=INTERPOLATE_VERTEX, channel=0, max_level=10):
+    """Per-level masks recorded from Far::PrimvarRefiner by the product's GB300MaskRecorder:
+    (num_control, [dict(offsets int64, sources int32, weights float32), ...])."""
+    L = lib()
+    h = L.ref_masks_record(refiner.h, C.c_int(mode), C.c_int(channel), C.c_int(max_level))
+    if not h:
+        raise RuntimeError("mask recording failed")
+    h = C.c_void_p(h)
+    levels = []
+    for lv in range(L.ref_masks_num_levels(h)):
+        n, nnz = C.c_int(), C.c_long()
+        L.ref_masks_level_counts(h, C.c_int(lv), C.byref(n), C.byref(nnz))
+        off = np.zeros(n.value + 1, np.int64)
+        src = np.zeros(nnz.value, np.int32)
+        w = np.zeros(nnz.value, np.float32)
+        L.ref_masks_level_copy(h, C.c_int(lv), _p(off), _p(src), _p(w))
+        levels.append(dict(offsets=off, sources=src, weights=w))
+    nc = L.ref_masks_num_control(h)
+    L.ref_masks_destroy(h)
+    return nc, levels
 
 
 def limit_stencil_table(refiner, ptex, s, t, use_double=False, d1=True, d2=False):

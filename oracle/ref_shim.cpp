@@ -18,6 +18,8 @@
 #include <opensubdiv/osd/cpuPatchTable.h>
 #include <opensubdiv/osd/bufferDescriptor.h>
 
+#include <opensubdiv_gb300/far/gb300StencilTableFactory.h>
+
 #include <cstring>
 #include <vector>
 
@@ -231,6 +233,57 @@ void *ref_limit_stencils_create(void *p, int useDouble, int n, const int *ptex,
     }
     return s;
 }
+
+// Far::StencilTableFactory::Create (float) in any interpolation mode.
+void *ref_stencils_create_mode(void *p, int mode, int channel, int genIntermediate,
+                               int genCtrl, int maxLevel) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    Stencils *s = new Stencils;
+    Far::StencilTableFactory::Options o;
+    o.interpolationMode = mode;
+    o.fvarChannel = channel;
+    o.generateIntermediateLevels = genIntermediate;
+    o.generateControlVerts = genCtrl;
+    o.generateOffsets = true;
+    o.maxLevel = maxLevel;
+    s->f = Far::StencilTableFactory::Create(*r, o);
+    return s;
+}
+
+// The per-level masks the GPU factory consumes, recorded from Far::PrimvarRefiner by the
+// product's own recorder (include/opensubdiv_gb300/far/gb300StencilTableFactory.h).
+struct MaskSet {
+    std::vector<Osd::GB300LevelMasks> levels;
+    int numControl = 0;
+};
+
+void *ref_masks_record(void *p, int mode, int channel, int maxLevel) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    Far::StencilTableFactory::Options o;
+    o.interpolationMode = mode;
+    o.fvarChannel = channel;
+    o.maxLevel = maxLevel;
+    MaskSet *m = new MaskSet;
+    if (!Osd::GB300StencilTableFactory::RecordMasks(*r, o, m->levels, &m->numControl)) {
+        delete m;
+        return nullptr;
+    }
+    return m;
+}
+int ref_masks_num_levels(void *p) { return (int)((MaskSet *)p)->levels.size(); }
+int ref_masks_num_control(void *p) { return ((MaskSet *)p)->numControl; }
+void ref_masks_level_counts(void *p, int level, int *numRows, long *nnz) {
+    Osd::GB300LevelMasks const &L = ((MaskSet *)p)->levels[level];
+    *numRows = L.numRows;
+    *nnz = (long)L.sources.size();
+}
+void ref_masks_level_copy(void *p, int level, int64_t *offsets, int *sources, float *weights) {
+    Osd::GB300LevelMasks const &L = ((MaskSet *)p)->levels[level];
+    copyVec(L.offsets, offsets);
+    copyVec(L.sources, sources);
+    copyVec(L.weights, weights);
+}
+void ref_masks_destroy(void *p) { delete (MaskSet *)p; }
 
 void ref_stencils_destroy(void *p) {
     Stencils *s = (Stencils *)p;

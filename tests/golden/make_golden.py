@@ -4,7 +4,7 @@ Run in a container that has the reference sources (it builds oracle/_ref/libosdr
 reference's own Far + Osd CPU code compiled from source, and drives it through
 oracle/ref_shim.cpp):
 
-    make -C oracle ref && python tests/golden/make_golden.py
+    make -C oracle ref && python tests/golden/make_golden.py [factory]
 
 Every array written here comes out of the reference: Far factories build the tables,
 Osd::CpuEvaluator produces the float outputs, Far::PatchMap the handles and
@@ -202,7 +202,48 @@ def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3, fva
     return out
 
 
+def factory_fixture(path):
+    """Per-level masks recorded from Far::PrimvarRefiner (by the product's GB300MaskRecorder)
+    and the tables Far::StencilTableFactory builds from the same refiners: the inputs and the
+    expected outputs of the GPU stencil-table factory."""
+    out = {}
+    ftor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=31, noise=0.01)
+    cases = [
+        ("cube", shapes.cube(4, noise=0.01, seed=41), 3, ref.INTERPOLATE_VERTEX, None),
+        ("torus", shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=42), 3,
+         ref.INTERPOLATE_VERTEX, None),
+        ("loop", shapes.torus(12, 8, crease_fraction=0.05, seed=43, scheme=shapes.LOOP), 3,
+         ref.INTERPOLATE_VERTEX, None),
+        ("varying", shapes.torus(12, 8, tri_fraction=0.1, seed=44), 2,
+         ref.INTERPOLATE_VARYING, None),
+        ("fvar", ftor, 2, ref.INTERPOLATE_FACE_VARYING, uv_seams(ftor, 12, 8)),
+        ("pole", shapes.bipyramid(300), 1, ref.INTERPOLATE_VERTEX, None),
+        ("looppole", shapes.bipyramid(300, scheme=shapes.LOOP), 1, ref.INTERPOLATE_VERTEX,
+         None),
+    ]
+    names = []
+    for name, cage, level, mode, fvar in cases:
+        r = ref.Refiner(cage, fvar=None if fvar is None else (fvar[0], fvar[1], False))
+        r.refine_uniform(level)
+        nc, levels = ref.record_masks(r, mode)
+        out[f"{name}_num_control"] = np.int32(nc)
+        out[f"{name}_mode"] = np.int32(mode)
+        out[f"{name}_mask_rows"] = np.array([len(d["offsets"]) - 1 for d in levels], np.int32)
+        for k in ("offsets", "sources", "weights"):
+            out[f"{name}_mask_{k}"] = np.concatenate([d[k] for d in levels])
+        for tag, inter, ctrl in (("all", True, False), ("last_ctrl", False, True)):
+            t = ref.stencil_table_mode(r, mode, intermediate=inter, control=ctrl)
+            for k in ("sizes", "offsets", "indices", "weights"):
+                out[f"{name}_{tag}_{k}"] = t[k]
+        names.append(name)
+    out["cases"] = np.array(names)
+    np.savez_compressed(path, **out)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "factory":
+        factory_fixture(os.path.join(HERE, "factory_masks.npz"))
+        return
     if not ref.available():
         raise SystemExit("oracle/_ref/libosdref.so missing: run `make -C oracle ref` first")
     g = HERE
@@ -241,6 +282,7 @@ def main():
                   adaptive=False)
     patch_fixture(os.path.join(g, "icosphere2_uniform_tris_L1.npz"), ico, 1, seed=27,
                   nq=1500, adaptive=False)
+    factory_fixture(os.path.join(g, "factory_masks.npz"))
     for f in sorted(os.listdir(g)):
         if f.endswith(".npz"):
             print(f"{f:40s} {os.path.getsize(os.path.join(g, f)) / 1024:8.1f} KiB")

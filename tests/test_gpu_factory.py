@@ -1,0 +1,140 @@
+"""The GPU stencil-table factory (GB300StencilTableFactoryCreate, GB300StencilTableComposeRows)
+against the reference's own tables and the oracle.
+
+The masks in tests/golden/factory_masks.npz were recorded from Far::PrimvarRefiner; the device
+factory must rebuild Far::StencilTableFactory's tables from them bit for bit (entries in Far's
+order), and with sorted entries must hold the same stencils.  Compositions over a base table
+(limit-stencil and local-point forms) must equal the oracle's restatement bit for bit."""
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import dev, torch_cuda
+from test_factory_oracle import GOLDEN, cases, far_table, load_case, same_table
+
+
+def sorted_rows(t):
+    """The table with each stencil's entries sorted by control index (stable)."""
+    idx = t["indices"].copy()
+    w = t["weights"].copy()
+    for i, (o, n) in enumerate(zip(t["offsets"], t["sizes"])):
+        p = np.argsort(idx[o:o + n], kind="stable")
+        idx[o:o + n] = idx[o:o + n][p]
+        w[o:o + n] = w[o:o + n][p]
+    return dict(sizes=t["sizes"], offsets=t["offsets"], indices=idx, weights=w)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", cases())
+@pytest.mark.parametrize("tag,inter,ctrl", [("all", True, False), ("last_ctrl", False, True)])
+def test_factory_rebuilds_far_tables(name, tag, inter, ctrl):
+    torch_cuda()
+    from opensubdiv_gb300.evaluator import GB300StencilTableFactory as F
+    z = np.load(GOLDEN)
+    nc, levels = load_case(z, name)
+    far = far_table(z, name, tag)
+    t = F.Create(nc, levels, generateIntermediateLevels=inter, generateControlVerts=ctrl,
+                 sortEntries=False)
+    assert same_table(t.CopyToHost(), far)
+    s = F.Create(nc, levels, generateIntermediateLevels=inter, generateControlVerts=ctrl,
+                 sortEntries=True)
+    assert same_table(s.CopyToHost(), sorted_rows(far))
+
+
+@pytest.mark.gpu
+def test_factory_table_evaluates_like_the_uploaded_far_table():
+    """EvalStencils over the factory's table (sorted layout) and over GB300StencilTable.Create
+    of Far's arrays: the same device layout, so bit-identical results."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300StencilTable, GB300StencilTableFactory as F)
+    z = np.load(GOLDEN)
+    nc, levels = load_case(z, "torus")
+    far = far_table(z, "torus", "all")
+    a = F.Create(nc, levels)
+    b = GB300StencilTable.Create(far["sizes"], far["offsets"], far["indices"], far["weights"])
+    n = a.GetNumStencils()
+    src = dev(np.random.default_rng(5).normal(size=nc * 4).astype(np.float32))
+    d = BD(0, 4, 4)
+    ya = torch.zeros(n * 4, device="cuda")
+    yb = torch.zeros(n * 4, device="cuda")
+    assert Ev.EvalStencilsTable(src, d, ya, d, a)
+    assert Ev.EvalStencilsTable(src, d, yb, d, b)
+    torch.cuda.synchronize()
+    assert torch.equal(ya, yb)
+
+
+def _device_base(rng, n_ctrl, n_rows, max_size):
+    """A device table in Far's entry order, built by ComposeRows over identity rows: each row
+    gets distinct control indices, and some rows an extra entry that cancels one weight to an
+    exact 0.0 (zero entries stay in the row, as Far's merges keep them)."""
+    from opensubdiv_gb300.evaluator import GB300StencilTable
+    ident = np.arange(n_ctrl, dtype=np.int32)
+    idt = GB300StencilTable.Create(np.ones(n_ctrl, np.int32), ident, ident,
+                                   np.ones(n_ctrl, np.float32))
+    off, src, w = [0], [], []
+    for _ in range(n_rows):
+        q = rng.choice(n_ctrl, int(rng.integers(1, max_size + 1)), replace=False)
+        x = rng.normal(size=len(q)).astype(np.float32)
+        src += q.tolist()
+        w += x.tolist()
+        if rng.random() < 0.1:
+            j = int(rng.integers(len(q)))
+            src.append(int(q[j]))
+            w.append(-float(x[j]))
+        off.append(len(src))
+    b = GB300StencilTable.ComposeRows(idt, np.array(off, np.int64), np.array(src, np.int32),
+                                      [np.array(w, np.float32)], sortEntries=False)
+    return b, b.CopyToHost()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nch,append", [(1, False), (3, False), (6, False), (1, True)])
+def test_compose_rows_matches_oracle(nch, append):
+    """Limit-stencil form (patch CVs x basis weights, 1 / 3 / 6 channels) and the local-point
+    append form over a base table whose rows overlap heavily (merges hit existing entries),
+    with zero base entries (skipped), zero mask weights, masks longer than a warp and rows
+    longer than the 256-entry shared-memory list."""
+    torch_cuda()
+    from opensubdiv_gb300.evaluator import GB300StencilTable
+    rng = np.random.default_rng(100 + nch)
+    b, base = _device_base(rng, 400, 3000, 24)
+    assert (base["weights"] == 0).any()
+    n = 2000
+    cnt = rng.integers(1, 21, n)
+    cnt[:3] = [60, 200, 40]  # long masks: rows of hundreds of entries
+    off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    src = rng.integers(0, 3000, int(off[-1])).astype(np.int32)
+    ws = [rng.normal(size=len(src)).astype(np.float32) for _ in range(nch)]
+    zero = rng.random(len(src)) < 0.05
+    for w in ws:
+        w[zero] = 0.0
+    want = oracle.compose_rows(base, off, src, ws, append_base=append)
+    assert want["sizes"].max() > 256
+    got = GB300StencilTable.ComposeRows(b, off, src, ws, appendBase=append, sortEntries=False)
+    h = got.CopyToHost()
+    names = ("weights", "du_weights", "dv_weights", "duu_weights", "duv_weights",
+             "dvv_weights")
+    for k in ("sizes", "offsets", "indices"):
+        assert np.array_equal(h[k], want[k]), k
+    for c in range(nch):
+        assert np.array_equal(h[names[c]].view(np.uint32), want[names[c]].view(np.uint32))
+
+
+@pytest.mark.gpu
+def test_factory_rejects_malformed_masks():
+    torch_cuda()
+    from opensubdiv_gb300.evaluator import GB300Error, GB300StencilTableFactory as F
+    z = np.load(GOLDEN)
+    nc, levels = load_case(z, "cube")
+    bad = [dict(d) for d in levels]
+    bad[2] = dict(bad[2], sources=bad[2]["sources"].copy())
+    bad[2]["sources"][5] = nc + 3  # an older level: not allowed with factorized levels
+    with pytest.raises(GB300Error):
+        F.Create(nc, bad)
+    bad[2]["sources"][5] = 1 << 30  # beyond every vertex
+    with pytest.raises(GB300Error):
+        F.Create(nc, bad)
+    # the device is still usable afterwards
+    t = F.Create(nc, levels)
+    assert t.GetNumStencils() == sum(len(d["offsets"]) - 1 for d in levels)

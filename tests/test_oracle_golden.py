@@ -15,7 +15,9 @@ import oracle
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STENCIL_FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz")))
-PATCH_FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*.npz"))) - set(STENCIL_FIXTURES))
+PATCH_FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*_patches_*.npz"))) |
+                        set(glob.glob(os.path.join(GOLDEN, "*_uniform_quads_*.npz"))) |
+                        set(glob.glob(os.path.join(GOLDEN, "*_uniform_tris_*.npz"))))
 
 
 def bits(a):
