@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--batch-cv-max", type=int, default=25_000,
                     help="upper end of the log-uniform CV range of the batched meshes")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section")
+    ap.add_argument("--no-factory", action="store_true",
+                    help="skip the stencil-table factory section")
     ap.add_argument("--serve-topologies", type=int, default=1000)
     ap.add_argument("--serve-requests", type=int, default=4000, help="requests per rate")
     ap.add_argument("--serve-rates", type=lambda s: [float(x) for x in s.split(",")],
@@ -365,6 +367,83 @@ def bench_serving(args):
 
 METRIC = "stencil evals per s (EvalStencils refine L3 + limit du/dv)"
 UNIT = "stencils/s"
+
+
+def bench_factory(args, w):
+    """Stencil-table construction for the refine workload's cage (the step before the path):
+    the GPU factory (host topology + Far-form masks, then GB300StencilTableFactory: mask upload
+    and device merge, table left on the device) against the host generator (topology + OpenMP
+    composition in double + upload of the finished table), plus the oracle's restatement of
+    Far's single-threaded StencilBuilder merge on a bounded sample."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    from opensubdiv_gb300 import shapes, topology
+    from opensubdiv_gb300.evaluator import GB300StencilTable, GB300StencilTableFactory as F
+
+    cage, level = w["cage"], w["level"]
+    reps = 3
+    t0 = time.perf_counter()
+    topo = topology.UniformRefiner(cage, level, stencils=False)
+    t_topo = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    nc, levels = topo.factory_masks()
+    t_masks = time.perf_counter() - t0
+    mask_nnz = sum(len(d["sources"]) for d in levels)
+    F.Create(nc, levels, generateIntermediateLevels=False)  # warm-up (module, pools)
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        tab = F.Create(nc, levels, generateIntermediateLevels=False)
+        times.append(time.perf_counter() - t0)
+        del tab
+    t_gpu = float(np.median(times))
+    launches0 = _lib_launches()
+    tab = F.Create(nc, levels, generateIntermediateLevels=False)
+    launches = _lib_launches() - launches0
+    n, nnz = tab.GetNumStencils(), tab.GetNumIndices()
+    # host generator path for the same table (its tables are what the refine bench uses)
+    r = w["refine"]
+    t0 = time.perf_counter()
+    gen = topology.UniformRefiner(cage, level)
+    g = gen.stencil_table()
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    up = GB300StencilTable.Create(g["sizes"], g["offsets"], g["indices"], g["weights"])
+    t_up = time.perf_counter() - t0
+    # same stencils: sizes identical, weights within 2 float ulps of 1 (float vs double sums)
+    a, b = tab.CopyToHost(), up.CopyToHost()
+    same = bool(np.array_equal(a["sizes"], b["sizes"]) and np.array_equal(a["indices"],
+                                                                        b["indices"]))
+    werr = float(np.abs(a["weights"] - b["weights"]).max()) if same else None
+    del up, gen, g
+    # Far's merge restated (oracle, one thread) on a bounded sample: a smaller torus
+    sn, sv = max(8, args.nu // 4), max(8, args.nv // 4)
+    scage = shapes.torus(sn, sv, tri_fraction=0.05, crease_fraction=0.02, seed=2024)
+    snc, slev = topology.UniformRefiner(scage, level, stencils=False).factory_masks()
+    t0 = time.perf_counter()
+    st = oracle.factory_create(snc, slev, intermediate=False)
+    t_orc = time.perf_counter() - t0
+    return {
+        "workload": f"{w['name'].split('_')[0]} Catmark L{level}: {n} stencils, {nnz} entries "
+                    f"from {mask_nnz} mask entries",
+        "stencils": n, "entries": int(nnz), "mask_entries": int(mask_nnz),
+        "host_topology_ms": t_topo * 1e3, "host_masks_ms": t_masks * 1e3,
+        "gpu_factory_ms": t_gpu * 1e3, "gpu_factory_launches": int(launches),
+        "gpu_path_ms": (t_topo + t_masks + t_gpu) * 1e3,
+        "host_generator_ms": t_gen * 1e3, "host_upload_ms": t_up * 1e3,
+        "host_path_ms": (t_gen + t_up) * 1e3,
+        "speedup_path": (t_gen + t_up) / (t_topo + t_masks + t_gpu),
+        "gpu_factory_stencils_per_s": n / t_gpu,
+        "matches_host_generator": same, "max_weight_diff": werr,
+        "far_merge_port": {"stencils_per_s": len(st["sizes"]) / t_orc, "cores": 1,
+                           "sample": f"torus {sn}x{sv} L{level} ({len(st['sizes'])} stencils, "
+                                     "oracle restatement of StencilBuilder's merge)"},
+    }
+
+
+def _lib_launches():
+    from opensubdiv_gb300 import _lib
+    return int(_lib.load().GB300GetLaunchCount())
 
 
 def peaks():
@@ -787,6 +866,8 @@ def run_gb300(args, rank, world):
         line["batching"] = bench_batch(args, stream, peak)
     if not args.no_serving:
         line["serving"] = bench_serving(args)
+    if not args.no_factory:
+        line["factory"] = bench_factory(args, w)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, el = cpu_rate(w, args.cpu_seconds, threads)

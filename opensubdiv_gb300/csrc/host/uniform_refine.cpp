@@ -60,7 +60,7 @@ struct Topology {
     // masks of one level, between GB300TopologyMaskCounts and GB300TopologyMaskCopy
     std::vector<int64_t> maskOff;
     std::vector<int> maskIdx;
-    std::vector<double> maskW;
+    std::vector<float> maskW;
     // limit stencils produced by the last GB300TopologyLimitStencils call
     std::vector<int> lsizes, loffsets, lidx;
     std::vector<float> lw[3];
@@ -493,45 +493,153 @@ int GB300TopologyRefineUniform(void *p, int level) {
     return 0;
 }
 
-// Subdivision masks of the level-`level` vertices over the level-(level - 1) vertices, in
-// the order compose() applies them (CSR: offsets[nChild + 1], parents, double weights).
-// MaskCounts computes them and keeps them until MaskCopy hands them out.
+// Subdivision masks of the level-`level` vertices in the form Far::PrimvarRefiner feeds a
+// stencil builder (far/primvarRefiner.h:475-650): per child vertex, (source, float weight)
+// pairs in call order -- face points: the face's vertices; edge points: both ends, then (Catmark)
+// the adjacent face points of the same level or (Loop) the opposite vertices; vertex points:
+// (Catmark) the incident face points, then the edge neighbours, then the vertex itself.  Zero
+// weights are left out.  Sources are global indices (control vertices, then each level's
+// vertices), so a level's masks name the previous level and its own face points.  These are
+// the inputs of the GPU stencil-table factory (GB300StencilTableFactoryCreate).
+struct FarMask {
+    static constexpr int kMax = 160;
+    int n = 0;
+    bool overflow = false;
+    int src[kMax];
+    float w[kMax];
+    void add(int s, double x) {
+        const float f = (float)x;
+        if (f == 0.0f) return;
+        if (n == kMax) { overflow = true; return; }
+        src[n] = s; w[n] = f; ++n;
+    }
+};
+
+// per-slot weights of a vertex rule (incident faces / edges in vFace / vEdge order)
+void vertex_slots(int scheme, const Level &P, int v, Rule r, const std::vector<int> &sharpEnds,
+                  double scale, double *fw, double *ew, double &vw) {
+    const int b = P.vOff[v], n = P.vOff[v + 1] - b;
+    if (r == kCorner) { vw += scale; return; }
+    if (r == kCrease) {
+        vw += 0.75 * scale;
+        for (int k = 0; k < n; ++k) {
+            const int o = other_end(P, P.vEdge[b + k], v);
+            if (o == sharpEnds[0] || o == sharpEnds[1]) ew[k] += 0.125 * scale;
+        }
+        return;
+    }
+    if (scheme == kCatmark) {
+        const double dn = n;
+        vw += scale * (dn - 2.0) / dn;
+        for (int k = 0; k < n; ++k) {
+            ew[k] += scale / (dn * dn);
+            fw[k] += scale / (dn * dn);
+        }
+    } else {
+        double e = 0.0625, c = 0.625;
+        if (n != 6) {
+            const double inv = 1.0 / n;
+            const double beta = 0.25 * std::cos(M_PI * 2.0 * inv) + 0.375;
+            e = (0.625 - beta * beta) * inv;
+            c = 1.0 - e * n;
+        }
+        vw += scale * c;
+        for (int k = 0; k < n; ++k) ew[k] += scale * e;
+    }
+}
+
+void far_mask(int scheme, const Level &P, int c, int64_t parentBase, int64_t childBase,
+              FarMask &m) {
+    const bool cat = scheme == kCatmark;
+    const int vFace = P.nv, vEdge = cat ? P.nv + P.nf : P.nv;
+    auto faceChild = [&](int f) { return (int)(childBase + vFace + f); };
+    if (c < P.nv) {  // vertex point
+        const int v = c, b = P.vOff[v], n = P.vOff[v + 1] - b;
+        if (2 * n + 1 > FarMask::kMax) { m.overflow = true; return; }
+        double fw[FarMask::kMax] = {0}, ew[FarMask::kMax] = {0}, vw = 0.0;
+        int psharp = 0, csharp = 0, tcount = 0;
+        double tsum = 0.0;
+        std::vector<int> pEnds, cEnds;
+        for (int k = 0; k < n; ++k) {
+            const int e = P.vEdge[b + k];
+            const float s = P.sharp[e];
+            if (s > 0.0f) { ++psharp; pEnds.push_back(other_end(P, e, v)); }
+            if (decrement(s) > 0.0f) { ++csharp; cEnds.push_back(other_end(P, e, v)); }
+            if (s > 0.0f && s <= 1.0f) { tsum += s; ++tcount; }
+        }
+        auto rule = [](int k) { return k <= 1 ? kSmooth : k == 2 ? kCrease : kCorner; };
+        const Rule pr = rule(psharp), cr = rule(csharp);
+        if (pr == kSmooth || pr == cr) {
+            vertex_slots(scheme, P, v, pr, pEnds, 1.0, fw, ew, vw);
+        } else {
+            double pw = tcount ? tsum / tcount : 0.0;
+            if (pw > 1.0) pw = 1.0;
+            vertex_slots(scheme, P, v, pr, pEnds, pw, fw, ew, vw);
+            vertex_slots(scheme, P, v, cr, cEnds, 1.0 - pw, fw, ew, vw);
+        }
+        if (cat)
+            for (int k = 0; k < n; ++k) m.add(faceChild(P.vFace[b + k]), fw[k]);
+        for (int k = 0; k < n; ++k) m.add((int)(parentBase + other_end(P, P.vEdge[b + k], v)), ew[k]);
+        m.add((int)(parentBase + v), vw);
+    } else if (cat && c < vEdge) {  // face point
+        const int f = c - vFace, b = P.fOff[f], n = P.fOff[f + 1] - b;
+        const float w = 1.0f / (float)n;
+        for (int i = 0; i < n; ++i) m.add((int)(parentBase + P.fv[b + i]), w);
+    } else {  // edge point
+        const int e = c - vEdge;
+        const int a = P.ev[2 * e], bb = P.ev[2 * e + 1];
+        const float s = P.sharp[e];
+        if (s >= 1.0f) {
+            m.add((int)(parentBase + a), 0.5);
+            m.add((int)(parentBase + bb), 0.5);
+            return;
+        }
+        const double pw = s > 0.0f ? (double)s : 0.0, cw = 1.0 - pw;
+        const int f0 = P.ef[2 * (size_t)e], f1 = P.ef[2 * (size_t)e + 1];
+        const double vwt = pw * 0.5 + cw * (cat ? 0.25 : 0.375);
+        m.add((int)(parentBase + a), vwt);
+        m.add((int)(parentBase + bb), vwt);
+        if (cat) {
+            m.add(faceChild(f0), 0.25 * cw);
+            m.add(faceChild(f1), 0.25 * cw);
+        } else {
+            m.add((int)(parentBase + opposite(P, f0, e)), 0.125 * cw);
+            m.add((int)(parentBase + opposite(P, f1, e)), 0.125 * cw);
+        }
+    }
+}
+
 int GB300TopologyMaskCounts(void *p, int level, int *nChild, int64_t *nnz) {
     Topology *t = (Topology *)p;
     if (!t || level < 1 || level >= (int)t->levels.size())
         return fail("GB300TopologyMaskCounts: level not refined");
     const Level &P = t->levels[level - 1];
     const int nc = t->levels[level].nv;
-    const bool cat = t->scheme == kCatmark;
-    const int vFace = cat ? P.nv : -1, vEdge = cat ? P.nv + P.nf : P.nv;
-    auto mask_of = [&](int c, Mask &m) {
-        if (c < P.nv) vertex_mask(t->scheme, P, c, m);
-        else if (cat && c < vEdge) add_face_point(P, c - vFace, 1.0, m);
-        else edge_mask(t->scheme, P, c - vEdge, m);
-    };
+    int64_t parentBase = 0;
+    for (int l = 0; l < level - 1; ++l) parentBase += t->levels[l].nv;
+    const int64_t childBase = parentBase + P.nv;
     // two passes (sizes, then the masks again into place): no per-child staging buffer
     t->maskOff.assign(nc + 1, 0);
     int overflow = 0;
 #pragma omp parallel for schedule(static) reduction(| : overflow)
     for (int c = 0; c < nc; ++c) {
-        Mask m;
-        mask_of(c, m);
+        FarMask m;
+        far_mask(t->scheme, P, c, parentBase, childBase, m);
         t->maskOff[c + 1] = m.n;
         overflow |= m.overflow ? 1 : 0;
     }
     if (overflow) {
         std::vector<int64_t>().swap(t->maskOff);
-        return fail("GB300TopologyMaskCounts: a vertex valence or face size beyond the "
-                    "generator's 64-parent masks");
+        return fail("GB300TopologyMaskCounts: a vertex valence beyond the generator's masks");
     }
     for (int c = 0; c < nc; ++c) t->maskOff[c + 1] += t->maskOff[c];
     t->maskIdx.resize(t->maskOff[nc]);
     t->maskW.resize(t->maskOff[nc]);
 #pragma omp parallel for schedule(static)
     for (int c = 0; c < nc; ++c) {
-        Mask m;
-        mask_of(c, m);
-        std::copy(m.idx, m.idx + m.n, t->maskIdx.begin() + t->maskOff[c]);
+        FarMask m;
+        far_mask(t->scheme, P, c, parentBase, childBase, m);
+        std::copy(m.src, m.src + m.n, t->maskIdx.begin() + t->maskOff[c]);
         std::copy(m.w, m.w + m.n, t->maskW.begin() + t->maskOff[c]);
     }
     *nChild = nc;
@@ -539,15 +647,15 @@ int GB300TopologyMaskCounts(void *p, int level, int *nChild, int64_t *nnz) {
     return 0;
 }
 
-int GB300TopologyMaskCopy(void *p, int64_t *offsets, int *parents, double *weights) {
+int GB300TopologyMaskCopy(void *p, int64_t *offsets, int *sources, float *weights) {
     Topology *t = (Topology *)p;
     if (!t || t->maskOff.empty()) return fail("GB300TopologyMaskCopy: no masks computed");
     std::copy(t->maskOff.begin(), t->maskOff.end(), offsets);
-    std::copy(t->maskIdx.begin(), t->maskIdx.end(), parents);
+    std::copy(t->maskIdx.begin(), t->maskIdx.end(), sources);
     std::copy(t->maskW.begin(), t->maskW.end(), weights);
     std::vector<int64_t>().swap(t->maskOff);
     std::vector<int>().swap(t->maskIdx);
-    std::vector<double>().swap(t->maskW);
+    std::vector<float>().swap(t->maskW);
     return 0;
 }
 

@@ -103,17 +103,23 @@ class UniformRefiner:
         return dict(sizes=sizes, offsets=offsets, indices=idx, weights=w)
 
     def masks(self, level):
-        """Subdivision masks of the level-`level` vertices over level - 1 (CSR: int64 offsets,
-        int32 parents, float64 weights), in the order the stencils compose them."""
+        """Subdivision masks of the level-`level` vertices in Far::PrimvarRefiner's form
+        (per child: (global source, float32 weight) in call order; Catmark edge and vertex
+        points name the level's own face points): dict of int64 offsets, int32 sources,
+        float32 weights -- the input of GB300StencilTableFactory."""
         lib = load()
         n, nnz = C.c_int(0), C.c_int64(0)
         if lib.GB300TopologyMaskCounts(self.h, level, C.byref(n), C.byref(nnz)):
             raise ValueError(_err())
         off = np.empty(n.value + 1, np.int64)
         idx = np.empty(nnz.value, np.int32)
-        w = np.empty(nnz.value, np.float64)
+        w = np.empty(nnz.value, np.float32)
         lib.GB300TopologyMaskCopy(self.h, off.ctypes.data, idx.ctypes.data, w.ctypes.data)
-        return off, idx, w
+        return dict(offsets=off, sources=idx, weights=w)
+
+    def factory_masks(self):
+        """(number of control vertices, masks of levels 1..level)."""
+        return self.cage.num_vertices, [self.masks(l) for l in range(1, self.level + 1)]
 
     def limit_stencil_table(self, faces, u, v):
         """Bilinear limit stencils with du/dv weights at (ptex face, u, v) locations."""

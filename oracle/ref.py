@@ -34,6 +34,8 @@ def lib():
         _lib.ref_stencils_nnz.restype = C.c_long
         _lib.ref_stencils_create_mode.restype = vp
         _lib.ref_masks_record.restype = vp
+        _lib.ref_limit_record.restype = vp
+        _lib.ref_limit_array_size.restype = C.c_long
         for name in ("ref_refiner_destroy", "ref_refine_uniform", "ref_refine_adaptive",
                      "ref_num_vertices_total", "ref_level_num_vertices", "ref_max_level",
                      "ref_num_ptex_faces", "ref_ptex_face_ids", "ref_stencils_num",
@@ -43,7 +45,8 @@ def lib():
                      "ref_cpu_eval_stencils", "ref_cpu_eval_patches", "ref_eval_patches_fp64",
                      "ref_omp_set_threads", "ref_patches_varying", "ref_patches_fvar",
                      "ref_masks_num_levels", "ref_masks_num_control", "ref_masks_level_counts",
-                     "ref_masks_level_copy", "ref_masks_destroy"):
+                     "ref_masks_level_copy", "ref_masks_destroy", "ref_limit_array_size",
+                     "ref_limit_array_copy", "ref_limit_info", "ref_limit_destroy"):
             getattr(_lib, name).argtypes = None
     return _lib
 
@@ -170,6 +173,39 @@ def record_masks(refiner, mode=INTERPOLATE_VERTEX, channel=0, max_level=10):
     nc = L.ref_masks_num_control(h)
     L.ref_masks_destroy(h)
     return nc, levels
+
+
+def limit_record(refiner, ptex, s, t, mode=INTERPOLATE_VERTEX, channel=0, d1=True, d2=False):
+    """Inputs and outputs of the GPU limit-stencil factory for these locations, recorded with
+    GB300LimitStencilTableFactory's helpers, plus Far::LimitStencilTableFactory's own table."""
+    L = lib()
+    ptex = np.ascontiguousarray(ptex, np.int32)
+    s = np.ascontiguousarray(s, np.float32)
+    t = np.ascontiguousarray(t, np.float32)
+    h = L.ref_limit_record(refiner.h, C.c_int(mode), C.c_int(channel), C.c_int(len(ptex)),
+                           _p(ptex), _p(s), _p(t), C.c_int(int(d1)), C.c_int(int(d2)))
+    if not h:
+        raise RuntimeError("limit recording failed")
+    h = C.c_void_p(h)
+    types = {0: np.int32, 1: np.int64, 2: np.int32, 3: np.float32, 4: np.int64, 5: np.int32,
+             6: np.float32, 7: np.int64, 8: np.int32, 15: np.int32, 16: np.int32, 17: np.int32}
+    names = {0: "level_rows", 1: "level_offsets", 2: "level_sources", 3: "level_weights",
+             4: "local_offsets", 5: "local_sources", 6: "local_weights", 7: "loc_offsets",
+             8: "loc_sources", 15: "far_sizes", 16: "far_offsets", 17: "far_indices"}
+    out = {}
+    for key in range(24):
+        typ = types.get(key, np.float32)
+        name = names.get(key, f"loc_w{key - 9}" if key < 15 else f"far_w{key - 18}")
+        a = np.zeros(L.ref_limit_array_size(h, C.c_int(key)), typ)
+        if len(a):
+            L.ref_limit_array_copy(h, C.c_int(key), _p(a))
+        out[name] = a
+    info = np.zeros(4, np.int32)
+    L.ref_limit_info(h, _p(info))
+    out.update(num_control=int(info[0]), num_channels=int(info[1]), spliced=int(info[2]),
+               cv_intermediate=int(info[3]))
+    L.ref_limit_destroy(h)
+    return out
 
 
 def limit_stencil_table(refiner, ptex, s, t, use_double=False, d1=True, d2=False):

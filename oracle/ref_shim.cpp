@@ -285,6 +285,128 @@ void ref_masks_level_copy(void *p, int level, int64_t *offsets, int *sources, fl
 }
 void ref_masks_destroy(void *p) { delete (MaskSet *)p; }
 
+// Everything the GPU limit-stencil factory consumes and produces for one refiner and set of
+// locations, recorded with the product's header (GB300LimitStencilTableFactory's helpers), plus
+// the table Far::LimitStencilTableFactory builds itself.  Arrays are exported by key.
+struct LimitRecord {
+    std::vector<int> levelRows, levelSrc, locSrc, localSrc, farSizes, farOffsets, farIndices;
+    std::vector<int64_t> levelOff, locOff, localOff;
+    std::vector<float> levelW, localW, locW[6], farW[6];
+    int numControl = 0, numChannels = 0, spliced = 0, cvIntermediate = 0;
+};
+
+void *ref_limit_record(void *p, int mode, int channel, int n, const int *ptex, const float *su,
+                       const float *tv, int d1, int d2) {
+    Far::TopologyRefiner *r = ((Refiner *)p)->r;
+    typedef Osd::GB300LimitStencilTableFactory LF;
+    LF::Options o;
+    o.interpolationMode = mode;
+    o.fvarChannel = channel;
+    o.generate1stDerivatives = d1;
+    o.generate2ndDerivatives = d2;
+    LimitRecord *rec = new LimitRecord;
+    LF::LocationArrayVec locs(n);
+    for (int i = 0; i < n; ++i) {
+        locs[i].ptexIdx = ptex[i];
+        locs[i].numLocations = 1;
+        locs[i].s = su + i;
+        locs[i].t = tv + i;
+    }
+    // refined-vertex stencil masks
+    Osd::GB300StencilTableFactory::Options co = LF::CvOptions(*r, o);
+    rec->cvIntermediate = co.generateIntermediateLevels;
+    std::vector<Osd::GB300LevelMasks> levels;
+    if (!Osd::GB300StencilTableFactory::RecordMasks(*r, co, levels, &rec->numControl)) {
+        delete rec;
+        return nullptr;
+    }
+    for (auto const &L : levels) {
+        rec->levelRows.push_back(L.numRows);
+        rec->levelOff.insert(rec->levelOff.end(), L.offsets.begin(), L.offsets.end());
+        rec->levelSrc.insert(rec->levelSrc.end(), L.sources.begin(), L.sources.end());
+        rec->levelW.insert(rec->levelW.end(), L.weights.begin(), L.weights.end());
+    }
+    Far::PatchTable const *pt = LF::CreatePatchTable(*r, o);
+    const bool fvar = mode == Far::LimitStencilTableFactory::INTERPOLATE_FACE_VARYING;
+    const int nRefined = r->IsUniform()
+        ? (fvar ? r->GetLevel(r->GetMaxLevel()).GetNumFVarValues(channel)
+                : r->GetLevel(r->GetMaxLevel()).GetNumVertices())
+        : (fvar ? r->GetNumFVarValuesTotal(channel) : r->GetNumVerticesTotal());
+    int cvCount = rec->numControl;
+    for (size_t l = co.generateIntermediateLevels ? 0 : (levels.empty() ? 0 : levels.size() - 1);
+         l < levels.size(); ++l)
+        cvCount += levels[l].numRows;
+    rec->spliced = cvCount == nRefined &&
+                   LF::LocalPointMasks(*pt, o, rec->localOff, rec->localSrc, rec->localW);
+    rec->numChannels = LF::LocationMasks(*r, *pt, locs, o, rec->locOff, rec->locSrc, rec->locW);
+    delete pt;
+    // the reference's own table
+    Far::LimitStencilTable const *far = Far::LimitStencilTableFactory::Create(*r, locs, nullptr,
+                                                                             nullptr, o);
+    if (far) {
+        const size_t nnz = far->GetControlIndices().size();
+        rec->farSizes = far->GetSizes();
+        rec->farOffsets = far->GetOffsets();
+        rec->farIndices = far->GetControlIndices();
+        std::vector<float> const *fw[6] = {&far->GetWeights(), &far->GetDuWeights(),
+                                           &far->GetDvWeights(), &far->GetDuuWeights(),
+                                           &far->GetDuvWeights(), &far->GetDvvWeights()};
+        for (int c = 0; c < rec->numChannels; ++c)
+            rec->farW[c].assign(fw[c]->begin(), fw[c]->begin() + std::min(nnz, fw[c]->size()));
+        delete far;
+    }
+    return rec;
+}
+
+// keys: 0 levelRows 1 levelOff 2 levelSrc 3 levelW 4 localOff 5 localSrc 6 localW 7 locOff
+// 8 locSrc 9..14 locW[c] 15 farSizes 16 farOffsets 17 farIndices 18..23 farW[c]
+static void limit_array(LimitRecord *r, int key, const void **ptr, long *n, int *esize) {
+    *ptr = nullptr;
+    *n = 0;
+    *esize = 4;
+    auto set = [&](auto const &v) {
+        *ptr = v.data();
+        *n = (long)v.size();
+        *esize = (int)sizeof(v[0]);
+    };
+    if (key == 0) set(r->levelRows);
+    else if (key == 1) set(r->levelOff);
+    else if (key == 2) set(r->levelSrc);
+    else if (key == 3) set(r->levelW);
+    else if (key == 4) set(r->localOff);
+    else if (key == 5) set(r->localSrc);
+    else if (key == 6) set(r->localW);
+    else if (key == 7) set(r->locOff);
+    else if (key == 8) set(r->locSrc);
+    else if (key >= 9 && key < 15) set(r->locW[key - 9]);
+    else if (key == 15) set(r->farSizes);
+    else if (key == 16) set(r->farOffsets);
+    else if (key == 17) set(r->farIndices);
+    else if (key >= 18 && key < 24) set(r->farW[key - 18]);
+}
+long ref_limit_array_size(void *p, int key) {
+    const void *ptr;
+    long n;
+    int es;
+    limit_array((LimitRecord *)p, key, &ptr, &n, &es);
+    return n;
+}
+void ref_limit_array_copy(void *p, int key, void *dst) {
+    const void *ptr;
+    long n;
+    int es;
+    limit_array((LimitRecord *)p, key, &ptr, &n, &es);
+    if (n) std::memcpy(dst, ptr, (size_t)n * es);
+}
+void ref_limit_info(void *p, int *info) {
+    LimitRecord *r = (LimitRecord *)p;
+    info[0] = r->numControl;
+    info[1] = r->numChannels;
+    info[2] = r->spliced;
+    info[3] = r->cvIntermediate;
+}
+void ref_limit_destroy(void *p) { delete (LimitRecord *)p; }
+
 void ref_stencils_destroy(void *p) {
     Stencils *s = (Stencils *)p;
     if (!s) return;

@@ -240,9 +240,40 @@ def factory_fixture(path):
     np.savez_compressed(path, **out)
 
 
+def factory_limit_fixture(path):
+    """GPU LimitStencilTableFactory inputs recorded with GB300LimitStencilTableFactory's helpers
+    (refined-vertex level masks, local-point masks, per-location patch points and basis
+    weights from Far's own PatchMap and EvaluateBasis) and Far::LimitStencilTableFactory's
+    table for the same locations."""
+    out = {}
+    tor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=45)
+    cases = [("adaptive", tor, 3, True, True, False, ref.INTERPOLATE_VERTEX),
+             ("adaptive2nd", tor, 3, True, True, True, ref.INTERPOLATE_VERTEX),
+             ("uniform", tor, 2, False, False, False, ref.INTERPOLATE_VERTEX),
+             ("loop", shapes.icosphere(1, seed=46), 3, True, True, False,
+              ref.INTERPOLATE_VERTEX),
+             ("varying", shapes.cube(3, seed=47), 3, True, True, False,
+              ref.INTERPOLATE_VARYING)]
+    for name, cage, level, adaptive, d1, d2, mode in cases:
+        r = ref.Refiner(cage)
+        if adaptive:
+            r.refine_adaptive(level)
+        else:
+            r.refine_uniform(level)
+        ptex, u, v = shapes.uniform_locations(cage, 400, seed=48)
+        rec = ref.limit_record(r, ptex, u, v, mode=mode, d1=d1, d2=d2)
+        for k, a in rec.items():
+            if isinstance(a, np.ndarray) and a.size == 0:
+                continue
+            out[f"{name}_{k}"] = np.asarray(a)
+    out["cases"] = np.array([c[0] for c in cases])
+    np.savez_compressed(path, **out)
+
+
 def main():
     if len(sys.argv) > 1 and sys.argv[1] == "factory":
         factory_fixture(os.path.join(HERE, "factory_masks.npz"))
+        factory_limit_fixture(os.path.join(HERE, "factory_limit.npz"))
         return
     if not ref.available():
         raise SystemExit("oracle/_ref/libosdref.so missing: run `make -C oracle ref` first")
@@ -283,6 +314,7 @@ def main():
     patch_fixture(os.path.join(g, "icosphere2_uniform_tris_L1.npz"), ico, 1, seed=27,
                   nq=1500, adaptive=False)
     factory_fixture(os.path.join(g, "factory_masks.npz"))
+    factory_limit_fixture(os.path.join(g, "factory_limit.npz"))
     for f in sorted(os.listdir(g)):
         if f.endswith(".npz"):
             print(f"{f:40s} {os.path.getsize(os.path.join(g, f)) / 1024:8.1f} KiB")

@@ -45,8 +45,63 @@ def same_table(a, b):
                           np.asarray(b["weights"], np.float32).view(np.uint32))
 
 
+LIMIT = os.path.join(ROOT, "tests", "golden", "factory_limit.npz")
+CHANNELS = ("weights", "du_weights", "dv_weights", "duu_weights", "duv_weights", "dvv_weights")
+
+
 def cases():
     return [str(c) for c in np.load(GOLDEN)["cases"]]
+
+
+def limit_cases():
+    return [str(c) for c in np.load(LIMIT)["cases"]]
+
+
+def limit_case(z, name):
+    """The recorded inputs of one GPU LimitStencilTableFactory case as plain arrays."""
+    g = lambda k, d=None: z[f"{name}_{k}"] if f"{name}_{k}" in z else d  # noqa: E731
+    rows = g("level_rows")
+    off, src, w = g("level_offsets"), g("level_sources"), g("level_weights")
+    levels, base, o = [], 0, 0
+    for n in rows:
+        lo = off[o:o + n + 1].astype(np.int64)
+        o += n + 1
+        nnz = int(lo[-1])
+        levels.append(dict(offsets=lo, sources=src[base:base + nnz], weights=w[base:base + nnz]))
+        base += nnz
+    nc = int(g("num_channels"))
+    rec = dict(num_control=int(g("num_control")), levels=levels, num_channels=nc,
+               spliced=bool(int(g("spliced"))), intermediate=bool(int(g("cv_intermediate"))),
+               local=(g("local_offsets"), g("local_sources"), g("local_weights")),
+               loc=(g("loc_offsets"), g("loc_sources"), [g(f"loc_w{c}") for c in range(nc)]))
+    far = dict(sizes=g("far_sizes"), offsets=g("far_offsets"), indices=g("far_indices"))
+    for c in range(nc):
+        far[CHANNELS[c]] = g(f"far_w{c}")
+    return rec, far
+
+
+def same_limit_table(a, b, nc):
+    for k in ("sizes", "offsets", "indices"):
+        if not np.array_equal(a[k], b[k]):
+            return False
+    return all(np.array_equal(np.asarray(a[CHANNELS[c]], np.float32).view(np.uint32),
+                              np.asarray(b[CHANNELS[c]], np.float32).view(np.uint32))
+               for c in range(nc))
+
+
+@pytest.mark.parametrize("name", limit_cases())
+def test_oracle_limit_pipeline_rebuilds_far_limit_tables(name):
+    """Refined-vertex table, local-point splice (AppendLocalPointStencilTable) and per-location
+    merges from the recorded masks equal Far::LimitStencilTableFactory's table bit for bit."""
+    rec, far = limit_case(np.load(LIMIT), name)
+    cv = oracle.factory_create(rec["num_control"], rec["levels"], intermediate=rec["intermediate"],
+                               control=True)
+    if rec["spliced"]:
+        o, s, w = rec["local"]
+        cv = oracle.compose_rows(cv, o, s, [w], append_base=True)
+    o, s, ws = rec["loc"]
+    got = oracle.compose_rows(cv, o, s, ws)
+    assert same_limit_table(got, far, rec["num_channels"])
 
 
 @pytest.mark.parametrize("name", cases())

@@ -10,7 +10,8 @@ import pytest
 
 import oracle
 from gpu_util import dev, torch_cuda
-from test_factory_oracle import GOLDEN, cases, far_table, load_case, same_table
+from test_factory_oracle import (CHANNELS, GOLDEN, LIMIT, cases, far_table, limit_case,
+                                 limit_cases, load_case, same_limit_table, same_table)
 
 
 def sorted_rows(t):
@@ -138,3 +139,23 @@ def test_factory_rejects_malformed_masks():
     # the device is still usable afterwards
     t = F.Create(nc, levels)
     assert t.GetNumStencils() == sum(len(d["offsets"]) - 1 for d in levels)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", limit_cases())
+def test_limit_pipeline_rebuilds_far_limit_tables(name):
+    """The device LimitStencilTableFactory pipeline (GB300LimitStencilTableFactory::Create's
+    steps through the C ABI): refined-vertex table, local-point splice, per-location merges with
+    Far's basis weights -- bit for bit Far::LimitStencilTableFactory's table."""
+    torch_cuda()
+    from opensubdiv_gb300.evaluator import GB300StencilTable, GB300StencilTableFactory as F
+    rec, far = limit_case(np.load(LIMIT), name)
+    cv = F.Create(rec["num_control"], rec["levels"],
+                  generateIntermediateLevels=rec["intermediate"], generateControlVerts=True,
+                  sortEntries=False)
+    if rec["spliced"]:
+        o, s, w = rec["local"]
+        cv = GB300StencilTable.ComposeRows(cv, o, s, [w], appendBase=True, sortEntries=False)
+    o, s, ws = rec["loc"]
+    lim = GB300StencilTable.ComposeRows(cv, o, s, ws, sortEntries=False)
+    assert same_limit_table(lim.CopyToHost(), far, rec["num_channels"])

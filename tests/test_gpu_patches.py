@@ -18,7 +18,7 @@ from gpu_util import bbox_diag, dev, host, max_err, torch_cuda
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 STENCIL_FIXTURES = set(glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz")))
 FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*.npz"))) - STENCIL_FIXTURES -
-                  {os.path.join(GOLDEN, "factory_masks.npz")})
+                  set(glob.glob(os.path.join(GOLDEN, "factory_*.npz"))))
 REL_TOL = 1e-5
 NAMES = ("P", "du", "dv", "duu", "duv", "dvv")
 

@@ -72,3 +72,30 @@ def test_generator_limit_stencils_are_bilinear_partitions():
 def test_generator_rejects_open_cages():
     with pytest.raises(ValueError):
         topology.UniformRefiner(shapes.grid(3, 3), 1)
+
+
+@pytest.mark.parametrize("scheme", ["catmark", "loop"])
+def test_generator_far_form_masks_compose_to_its_tables(scheme):
+    """The generator's masks in Far::PrimvarRefiner form (the GPU factory's input), merged as
+    Far's StencilBuilder does (the oracle), give the generator's own tables: same stencils and
+    supports, weights within 2 float ulps of 1 (float vs double accumulation)."""
+    import oracle
+    if scheme == "catmark":
+        cage = shapes.torus(16, 8, tri_fraction=0.1, crease_fraction=0.05, seed=3)
+    else:
+        cage = shapes.torus(12, 8, crease_fraction=0.05, seed=4, scheme=shapes.LOOP)
+    r = topology.UniformRefiner(cage, 3)
+    mine = r.stencil_table()
+    nc, levels = r.factory_masks()
+    first = nc
+    for d in levels:
+        n = len(d["offsets"]) - 1
+        assert d["sources"].min() >= 0 and d["sources"].max() < first + n
+        assert (d["sources"] >= first).any() == (scheme == "catmark")  # face points
+        first += n
+    t = oracle.factory_create(nc, levels, intermediate=False)
+    assert np.array_equal(t["sizes"], mine["sizes"])
+    for i in range(len(t["sizes"])):
+        a, b = _row(t, i), _row(mine, i)
+        assert set(a) == set(b)
+        assert max(abs(a[k] - b[k]) for k in a) <= 2.4e-7
