@@ -526,9 +526,12 @@ int setup_padding(GB300StencilBatch *b, const std::vector<int> &tableRows, cudaS
         which.push_back((int)k);
     }
     if (pads.empty()) return GB300_OK;
+    // every job's region starts on a 64-byte boundary: rows of 8 / 16 floats are then 32-byte
+    // aligned (256-bit gathers) and rows of 12 floats 16-byte aligned (128-bit gathers)
     long long floats = 0;
     std::vector<long long> at;
     for (const PadJob &p : pads) {
+        floats = (floats + 15) & ~15LL;
         at.push_back(floats);
         floats += p.numRows * p.dstStride;
         base.push_back(base.back() + p.numRows);
@@ -635,6 +638,17 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
     if (setup_padding(b, rows, s) != GB300_OK) {
         delete b;
         return nullptr;
+    }
+    // every job's vector width must match its rows' alignment (the gathers assume it)
+    for (const Job &j : b->jobs) {
+        const uintptr_t a = (uintptr_t)j.src;
+        if ((j.vw == 8 && ((a & 31) || j.srcStride % 8)) ||
+            (j.vw == 4 && ((a & 15) || j.srcStride % 4))) {
+            fail(GB300_ERR_CUDA, "GB300StencilBatchCreate: internal error: job rows not "
+                                 "aligned for %d-wide gathers", j.vw);
+            delete b;
+            return nullptr;
+        }
     }
     b->signature = work_signature(b->jobs, b->mean);
     {

@@ -192,3 +192,34 @@ def test_batch_invalid_requests():
     lib = _lib.load()
     assert lib.GB300StencilBatchEval(None, None) == 1
     assert lib.GB300StencilBatchEvalGraph(None, None) == 1
+
+
+@pytest.mark.gpu
+def test_batch_mixed_padded_widths_with_odd_row_counts():
+    """Unaligned jobs of every padded width (rows of 8, 12 and 16 floats) with an odd number of
+    source rows, side by side in one batch: each job's padded region starts on a 64-byte
+    boundary, so the 256-bit and 128-bit gathers stay aligned; results equal plain calls."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import shapes, topology
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD
+    from opensubdiv_gb300.evaluator import GB300StencilBatch, GB300StencilTable
+    cage = shapes.torus(7, 5, tri_fraction=0.1, seed=3)
+    ncv = cage.num_vertices
+    assert ncv % 2 == 1
+    t = topology.UniformRefiner(cage, 2).stencil_table()
+    table = GB300StencilTable.Create(**t)
+    n = len(t["sizes"])
+    rng = np.random.default_rng(12)
+    widths = [9, 3, 11, 5, 10, 13, 7, 6, 15, 12, 14]
+    srcs, dsts, plain, descs = [], [], [], []
+    for L in widths:
+        srcs.append(dev(rng.uniform(-1, 1, ncv * L).astype(np.float32)))
+        dsts.append(torch.zeros(n * L, device="cuda"))
+        plain.append(torch.zeros(n * L, device="cuda"))
+        descs.append(BD(0, L, L))
+    batch = GB300StencilBatch([(table, s, d, o, d) for s, o, d in zip(srcs, dsts, descs)])
+    batch.Eval()
+    _plain(torch, [table] * len(widths), srcs, descs, plain, descs)
+    for L, a, b in zip(widths, dsts, plain):
+        assert torch.equal(a, b), L
+    assert batch.GetDeviceStatus() == 0
