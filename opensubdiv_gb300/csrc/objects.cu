@@ -299,12 +299,21 @@ int stencil_table_num_control(const GB300StencilTable *t) { return t ? t->numCon
 
 GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
                                        void *const buf[9]) {
+    return adopt_stencil_table(numStencils, nnz, numControl, buf, nullptr, nullptr);
+}
+
+GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
+                                       void *const buf[9], void *const ebuf[9], void *outRow) {
     GB300StencilTable *t = new (std::nothrow) GB300StencilTable;
     if (!t) return nullptr;
     t->numStencils = numStencils;
     t->nnz = nnz;
     t->numControl = numControl;
-    for (int k = 0; k < 9; ++k) t->buf[k] = buf[k];
+    for (int k = 0; k < 9; ++k) {
+        t->buf[k] = buf[k];
+        t->ebuf[k] = ebuf ? ebuf[k] : nullptr;
+    }
+    t->outRow = outRow;
     return t;
 }
 }  // namespace gb300

@@ -24,6 +24,7 @@
 #include "common.cuh"
 #include "tables.h"
 
+#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -237,6 +238,65 @@ __global__ void __launch_bounds__(warps_of<NC>() * 32) k_fill(Pass<NC> p) {
     }
 }
 
+// Term bounds of the pass's rows (0 for rows of other waves); element n is 0.
+template <int NC>
+__global__ void k_bounds(Pass<NC> p, long long *out) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r <= p.numRows;
+         r += gridDim.x * blockDim.x) {
+        long long t = 0;
+        if (r < p.numRows && (!p.wave || p.wave[r] == p.waveId)) {
+            for (long long k = p.moff[r]; k < p.moff[r + 1]; ++k) {
+                int s;
+                float m[NC];
+                if (!mask_entry(p, k, s, m)) continue;
+                int n;
+                const int *i;
+                const float *w;
+                source_row(p.rows, s, n, i, w);
+                t += n;
+            }
+        }
+        out[r] = t;
+    }
+}
+
+// Single merge pass: row r owns bound[r] entries of the arena from metaOff; it is built in
+// shared memory when that bound fits (then copied out) and in place otherwise.  Writes the
+// row's entry count.
+template <int NC>
+__global__ void __launch_bounds__(warps_of<NC>() * 32) k_merge1(Pass<NC> p,
+                                                                const long long *bound) {
+    constexpr int W = warps_of<NC>();
+    __shared__ int skeys[W][kCap];
+    __shared__ float svals[W][NC][kCap];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    for (int r = blockIdx.x * W + wib; r < p.numRows; r += gridDim.x * W) {
+        if (p.wave && p.wave[r] != p.waveId) continue;
+        const long long cap = bound[r];
+        const long long o = p.metaOff[p.metaBase + r];
+        int n;
+        if (cap <= kCap) {
+            float *v[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = svals[wib][c];
+            n = merge_row<NC, true>(p, r, skeys[wib], v, (int)cap, lane);
+            for (int i = lane; i < n; i += 32) {
+                p.arenaIdx[o + i] = skeys[wib][i];
+#pragma unroll
+                for (int c = 0; c < NC; ++c) p.arenaW[c][o + i] = svals[wib][c][i];
+            }
+        } else {
+            float *v[NC];
+#pragma unroll
+            for (int c = 0; c < NC; ++c) v[c] = p.arenaW[c] + o;
+            n = merge_row<NC, true>(p, r, p.arenaIdx + o, v,
+                                    (int)min(cap, (long long)0x7fffffff), lane);
+        }
+        if (lane == 0) p.metaSize[p.metaBase + r] = n;
+        __syncwarp();
+    }
+}
+
 // Dependency waves of one level's rows: 0 when no source lies in the level itself, -1 (to be
 // assigned) otherwise.  Also checks every source: a control vertex, a vertex of the previous
 // level [prevFirst, levelFirst) or of this level.
@@ -396,6 +456,58 @@ __global__ void k_out_copy(Assemble a, int n, const long long *off, int *outSize
     if (lane == 0 && mx >= 0) atomicMax(maxIdx, mx);
 }
 
+// Evaluation order of a finished table (the layout GB300StencilTableCreate keeps for tables
+// whose consecutive stencils jump across the control points): per stencil its lowest index
+// (entries sorted: the first; -1 when empty) and the sum / max of the jumps between
+// consecutive stencils' keys (empty stencils count as 0 there).
+__global__ void k_order_keys(const int *sizes, const int *offsets, const int *idx, int n,
+                             int *keys, int *iota, unsigned long long *jump, int *maxKey) {
+    unsigned long long j = 0;
+    int mx = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int k = sizes[i] > 0 ? idx[offsets[i]] : -1;
+        keys[i] = k;
+        iota[i] = i;
+        const int a = max(k, 0);
+        mx = max(mx, a);
+        if (i > 0) {
+            const int b = sizes[i - 1] > 0 ? idx[offsets[i - 1]] : 0;
+            j += (unsigned long long)(a > b ? a - b : b - a);
+        }
+    }
+    for (int d = 16; d; d >>= 1) {
+        j += __shfl_xor_sync(kFull, j, d);
+        mx = max(mx, __shfl_xor_sync(kFull, mx, d));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(jump, j);
+        atomicMax(maxKey, mx);
+    }
+}
+
+__global__ void k_order_sizes(const int *sizes, const int *order, int n, int *esz) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        esz[j] = sizes[order[j]];
+}
+
+// warp per evaluation row j: copies stencil order[j] to eoff[j]
+__global__ void k_order_copy(const int *sizes, const int *offsets, const int *idx,
+                             const float *w0, const float *w1, const float *w2, const float *w3,
+                             const float *w4, const float *w5, int nc, const int *order,
+                             const int *eoff, int n, int *eidx, float *e0, float *e1, float *e2,
+                             float *e3, float *e4, float *e5) {
+    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
+    const float *w[6] = {w0, w1, w2, w3, w4, w5};
+    float *e[6] = {e0, e1, e2, e3, e4, e5};
+    for (int j = blockIdx.x * warps + (threadIdx.x >> 5); j < n; j += gridDim.x * warps) {
+        const int i = order[j], sz = sizes[i], o = offsets[i], d = eoff[j];
+        for (int k = lane; k < sz; k += 32) {
+            eidx[d + k] = idx[o + k];
+            for (int c = 0; c < nc; ++c) e[c][d + k] = w[c][o + k];
+        }
+    }
+}
+
 // ---- host side --------------------------------------------------------------------------
 
 int grid_for(long long items, int perBlock) {
@@ -479,8 +591,11 @@ bool arena_reserve(Arena<NC> &a, long long need, Scratch &sc, const char *who) {
     return true;
 }
 
-// Count, scan and fill the rows of one pass (one wave); p.metaSize / metaOff / arena are
-// updated.  Returns false with the status recorded on failure.
+// Builds the rows of one pass (one wave); p.metaSize / metaOff / arena are updated.  When the
+// rows' term bounds fit in half the free device memory every row gets room for its bound and
+// ONE merge pass writes it (rows then leave gaps in the arena; the table assembly compacts);
+// otherwise a COUNT pass sizes the rows exactly before the FILL pass.  Returns false with the
+// status recorded on failure.
 template <int NC>
 bool run_pass(Pass<NC> p, Arena<NC> &arena, long long *sizesTmp, long long *scanTmp,
               void *cubTmp, size_t cubBytes, int *dStatus, unsigned long long *dUsed,
@@ -495,6 +610,44 @@ bool run_pass(Pass<NC> p, Arena<NC> &arena, long long *sizesTmp, long long *scan
     if (p.rowsInArena) {
         p.rows.idx = arena.idx;
         p.rows.w = arena.w[0];
+    }
+    {
+        const int g1 = grid_for(p.numRows + 1, 256);
+        k_bounds<NC><<<g1, 256, 0, s>>>(p, sizesTmp);
+        count_launch();
+        size_t bytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, bytes, sizesTmp, scanTmp, p.numRows + 1, s);
+        if (bytes > cubBytes && !(cubTmp = sc.alloc<char>(bytes, who))) return false;
+        if (check_cuda(cub::DeviceScan::ExclusiveSum(cubTmp, bytes, sizesTmp, scanTmp,
+                                                     p.numRows + 1, s),
+                       who) != GB300_OK)
+            return false;
+        count_launch();
+        long long bound = 0;
+        if (!d2h(&bound, scanTmp + p.numRows, 1, s, who)) return false;
+        size_t freeB = 0, totalB = 0;
+        if (check_cuda(cudaMemGetInfo(&freeB, &totalB), who) != GB300_OK) return false;
+        // a growing arena is reallocated (old copy alive until the move is done)
+        const long long need = arena.fill + bound;
+        const long long newCap = need > arena.cap ? std::max(need, arena.cap + arena.cap / 2) : 0;
+        if ((double)newCap * 4.0 * (1 + NC) < 0.5 * (double)freeB) {
+            if (!arena_reserve(arena, arena.fill + bound, sc, who)) return false;
+            k_wave_offsets<<<g1, 256, 0, s>>>(scanTmp, p.wave, p.waveId, p.numRows, arena.fill,
+                                              const_cast<long long *>(p.metaOff), p.metaBase);
+            count_launch();
+            if (p.rowsInArena) {
+                p.rows.idx = arena.idx;
+                p.rows.w = arena.w[0];
+            }
+            p.arenaIdx = arena.idx;
+            for (int c = 0; c < NC; ++c) p.arenaW[c] = arena.w[c];
+            // the bounds are needed by the merge: keep them apart from the scan's inputs
+            k_merge1<NC><<<grid, W * 32, 0, s>>>(p, sizesTmp);
+            count_launch();
+            if (check_launch(who) != GB300_OK) return false;
+            arena.fill += bound;
+            return true;
+        }
     }
     // count (rerun once with a larger scratch pool when long rows need it)
     for (int attempt = 0; attempt < 2; ++attempt) {
@@ -561,6 +714,71 @@ bool run_pass(Pass<NC> p, Arena<NC> &arena, long long *sizesTmp, long long *scan
     return true;
 }
 
+// Builds the evaluation layout of a finished table with sorted entries (ebuf / outRow) when its
+// consecutive stencils' lowest indices jump by more than 1% of the index range on average --
+// the criterion and the stable order GB300StencilTableCreate uses.  Leaves ebuf / outRow null
+// when the table does not qualify.  False (status recorded) on failure.
+bool evaluation_order(void *const buf[9], int n, long long nnz, int nc, Scratch &sc,
+                      void *ebuf[9], void **outRow, const char *who) {
+    cudaStream_t s = sc.s;
+    int *keys = sc.alloc<int>((size_t)n, who), *keys2 = sc.alloc<int>((size_t)n, who);
+    int *iota = sc.alloc<int>((size_t)n, who);
+    unsigned long long *jump = sc.alloc<unsigned long long>(1, who);
+    int *maxKey = sc.alloc<int>(1, who);
+    if (!keys || !keys2 || !iota || !jump || !maxKey) return false;
+    if (check_cuda(cudaMemsetAsync(jump, 0, 8, s), who) != GB300_OK ||
+        check_cuda(cudaMemsetAsync(maxKey, 0, 4, s), who) != GB300_OK)
+        return false;
+    k_order_keys<<<grid_for(n, 256), 256, 0, s>>>((const int *)buf[0], (const int *)buf[1],
+                                                  (const int *)buf[2], n, keys, iota, jump,
+                                                  maxKey);
+    count_launch();
+    unsigned long long j = 0;
+    int mk = 0;
+    if (check_launch(who) != GB300_OK || !d2h(&j, jump, 1, s, who) || !d2h(&mk, maxKey, 1, s, who))
+        return false;
+    if ((double)j / (n - 1) < 0.01 * std::max(1, mk)) return true;  // already local
+    void *order = nullptr;
+    if (check_cuda(cudaMalloc(&order, ((size_t)n * 4 + 15) & ~size_t(15)), who) != GB300_OK)
+        return false;
+    *outRow = order;
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, keys, keys2, iota, (int *)order, n, 0, 32, s);
+    void *tmp = sc.alloc<char>(bytes, who);
+    if (!tmp ||
+        check_cuda(cub::DeviceRadixSort::SortPairs(tmp, bytes, keys, keys2, iota, (int *)order,
+                                                   n, 0, 32, s),
+                   who) != GB300_OK)
+        return false;
+    count_launch();
+    const size_t eb[9] = {(size_t)n * 4, (size_t)n * 4, (size_t)nnz * 4};
+    for (int k = 0; k < 3 + nc; ++k) {
+        const size_t b = k < 3 ? eb[k] : (size_t)nnz * 4;
+        if (check_cuda(cudaMalloc(&ebuf[k], (std::max<size_t>(b, 4) + 15) & ~size_t(15)), who) !=
+            GB300_OK)
+            return false;
+    }
+    k_order_sizes<<<grid_for(n, 256), 256, 0, s>>>((const int *)buf[0], (const int *)order, n,
+                                                   (int *)ebuf[0]);
+    count_launch();
+    bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, bytes, (int *)ebuf[0], (int *)ebuf[1], n, s);
+    void *tmp2 = sc.alloc<char>(bytes, who);
+    if (!tmp2 || check_cuda(cub::DeviceScan::ExclusiveSum(tmp2, bytes, (int *)ebuf[0],
+                                                          (int *)ebuf[1], n, s),
+                            who) != GB300_OK)
+        return false;
+    count_launch();
+    k_order_copy<<<grid_for(n, 8), 256, 0, s>>>(
+        (const int *)buf[0], (const int *)buf[1], (const int *)buf[2], (const float *)buf[3],
+        (const float *)buf[4], (const float *)buf[5], (const float *)buf[6],
+        (const float *)buf[7], (const float *)buf[8], nc, (const int *)order,
+        (const int *)ebuf[1], n, (int *)ebuf[2], (float *)ebuf[3], (float *)ebuf[4],
+        (float *)ebuf[5], (float *)ebuf[6], (float *)ebuf[7], (float *)ebuf[8]);
+    count_launch();
+    return check_launch(who) == GB300_OK;
+}
+
 // Copies the assembled rows into a new table object.
 GB300StencilTable *assemble(Assemble a, int n, Scratch &sc, void *cubTmp, size_t cubBytes,
                             const char *who) {
@@ -615,9 +833,22 @@ GB300StencilTable *assemble(Assemble a, int n, Scratch &sc, void *cubTmp, size_t
         cleanup();
         return nullptr;
     }
-    GB300StencilTable *t = adopt_stencil_table(n, nnz, mx + 1, buf);
-    if (!t) {
+    void *ebuf[9] = {nullptr};
+    void *outRow = nullptr;
+    auto cleanupAll = [&]() {
         cleanup();
+        for (void *&b : ebuf)
+            if (b) cudaFree(b), b = nullptr;
+        if (outRow) cudaFree(outRow), outRow = nullptr;
+    };
+    if (a.sort && n >= 4096 &&
+        !evaluation_order(buf, n, nnz, a.nc, sc, ebuf, &outRow, who)) {
+        cleanupAll();
+        return nullptr;
+    }
+    GB300StencilTable *t = adopt_stencil_table(n, nnz, mx + 1, buf, ebuf, outRow);
+    if (!t) {
+        cleanupAll();
         fail(GB300_ERR_OUT_OF_MEMORY, "%s: host allocation", who);
     }
     return t;

@@ -159,3 +159,42 @@ def test_limit_pipeline_rebuilds_far_limit_tables(name):
     o, s, ws = rec["loc"]
     lim = GB300StencilTable.ComposeRows(cv, o, s, ws, sortEntries=False)
     assert same_limit_table(lim.CopyToHost(), far, rec["num_channels"])
+
+
+@pytest.mark.gpu
+def test_composed_scattered_table_evaluates_like_an_uploaded_one():
+    """Limit-like stencils at scattered locations (consecutive stencils far apart): the device
+    assembly builds the same locality-sorted evaluation layout GB300StencilTable.Create keeps,
+    so EvalStencils results are bit-identical to the uploaded copy of the same arrays, and
+    within float rounding of the oracle."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300StencilTable)
+    rng = np.random.default_rng(77)
+    b, base = _device_base(rng, 5000, 20000, 12)
+    n = 6000
+    cnt = np.full(n, 16)
+    off = np.concatenate([[0], np.cumsum(cnt)]).astype(np.int64)
+    # each location reads 16 rows around a random centre: scattered from one stencil to the next
+    centre = rng.integers(0, 20000 - 64, n)
+    src = (centre[:, None] + rng.integers(0, 64, (n, 16))).astype(np.int32).ravel()
+    ws = [rng.normal(size=len(src)).astype(np.float32) for _ in range(3)]
+    t = GB300StencilTable.ComposeRows(b, off, src, ws)  # sorted entries + evaluation order
+    h = t.CopyToHost()
+    u = GB300StencilTable.Create(h["sizes"], h["offsets"], h["indices"], h["weights"],
+                                 h["du_weights"], h["dv_weights"])
+    L = 4
+    x = rng.uniform(-1, 1, 5000 * L).astype(np.float32)
+    d = BD(0, L, L)
+    outs = [[torch.zeros(n * L, device="cuda") for _ in range(3)] for _ in range(2)]
+    for tab, o in zip((t, u), outs):
+        assert Ev.EvalStencilsTable(dev(x), d, o[0], d, tab, du=o[1], duDesc=d, dv=o[2],
+                                    dvDesc=d)
+    torch.cuda.synchronize()
+    for a, c in zip(*outs):
+        assert torch.equal(a, c)
+    ref = [np.zeros(n * L, np.float32) for _ in range(3)]
+    oracle.eval_stencils(x, (0, L, L), ref, [(0, L, L)] * 3, h["sizes"], h["offsets"],
+                         h["indices"], [h["weights"], h["du_weights"], h["dv_weights"]])
+    for a, r in zip(outs[0], ref):
+        assert np.abs(a.cpu().numpy() - r).max() <= 1e-4 * max(1.0, np.abs(r).max())
