@@ -79,6 +79,7 @@ __device__ __forceinline__ void eval_one(const A &a, int i, int n, const int *li
                 // rows gathered G at a time before they are accumulated: all 4 for one output,
                 // 2 when the NW accumulators need the registers
                 constexpr int G = NW == 1 ? 4 : 2;
+                static_assert(4 % G == 0, "rows are gathered in groups that tile the chunk");
 #pragma unroll
                 for (int g = 0; g < 4; g += G) {
                     float x[G][8];
