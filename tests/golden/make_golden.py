@@ -247,15 +247,18 @@ def factory_limit_fixture(path):
     table for the same locations."""
     out = {}
     tor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=45)
-    cases = [("adaptive", tor, 3, True, True, False, ref.INTERPOLATE_VERTEX),
-             ("adaptive2nd", tor, 3, True, True, True, ref.INTERPOLATE_VERTEX),
-             ("uniform", tor, 2, False, False, False, ref.INTERPOLATE_VERTEX),
+    ftor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=31, noise=0.01)
+    seams = uv_seams(ftor, 12, 8)
+    cases = [("adaptive", tor, 3, True, True, False, ref.INTERPOLATE_VERTEX, None),
+             ("adaptive2nd", tor, 3, True, True, True, ref.INTERPOLATE_VERTEX, None),
+             ("uniform", tor, 2, False, False, False, ref.INTERPOLATE_VERTEX, None),
              ("loop", shapes.icosphere(1, seed=46), 3, True, True, False,
-              ref.INTERPOLATE_VERTEX),
+              ref.INTERPOLATE_VERTEX, None),
              ("varying", shapes.cube(3, seed=47), 3, True, True, False,
-              ref.INTERPOLATE_VARYING)]
-    for name, cage, level, adaptive, d1, d2, mode in cases:
-        r = ref.Refiner(cage)
+              ref.INTERPOLATE_VARYING, None),
+             ("fvar", ftor, 3, True, True, False, ref.INTERPOLATE_FACE_VARYING, seams)]
+    for name, cage, level, adaptive, d1, d2, mode, fvar in cases:
+        r = ref.Refiner(cage, fvar=None if fvar is None else (fvar[0], fvar[1], False))
         if adaptive:
             r.refine_adaptive(level)
         else:
