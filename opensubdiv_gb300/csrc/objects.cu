@@ -351,7 +351,7 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
     const int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
     cudaStream_t s = as_stream(stream);
     // Unaligned source rows (no vector gathers) of a large table: gather from a padded copy
-    // (rows of 8, 12 or 16 floats: vector loads) made on the same stream in stream-ordered
+    // (rows of 4, 8, 12 or 16 floats: vector loads) made on the same stream in stream-ordered
     // memory.
     auto al = [](const void *p, uintptr_t m) { return ((uintptr_t)p & (m - 1)) == 0; };
     const bool unaligned = src && !((al(src, 32) && srcStride % 8 == 0) ||

@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
     }
 }
 
-// Row i of a pad job: 8, 12 or 16 floats, 128-bit stores.
+// Row i of a pad job: 4, 8, 12 or 16 floats, 128-bit stores.
 __device__ __forceinline__ void pad_row(const PadJob &j, long long i) {
     const float *row = j.src + i * j.srcStride;
     float *d = j.dst + i * j.dstStride;
@@ -527,7 +527,7 @@ int setup_padding(GB300StencilBatch *b, const std::vector<int> &tableRows, cudaS
     }
     if (pads.empty()) return GB300_OK;
     // every job's region starts on a 64-byte boundary: rows of 8 / 16 floats are then 32-byte
-    // aligned (256-bit gathers) and rows of 12 floats 16-byte aligned (128-bit gathers)
+    // aligned (256-bit gathers) and rows of 4 / 12 floats 16-byte aligned (128-bit gathers)
     long long floats = 0;
     std::vector<long long> at;
     for (const PadJob &p : pads) {
@@ -547,7 +547,7 @@ int setup_padding(GB300StencilBatch *b, const std::vector<int> &tableRows, cudaS
         Job &j = b->jobs[which[p]];
         j.src = pads[p].dst;
         j.srcStride = pads[p].dstStride;
-        j.vw = pads[p].dstStride == 12 ? 4 : 8;
+        j.vw = (pads[p].dstStride == 4 || pads[p].dstStride == 12) ? 4 : 8;
     }
     const size_t padBytes = ((pads.size() * sizeof(PadJob) + 255) / 256) * 256;
     st = check_cuda(cudaMalloc((void **)&b->dPad, padBytes + base.size() * sizeof(long long)),

@@ -47,10 +47,10 @@ int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int
                 int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1);
 
 // Padded copy of one source: rows [0, numRows) of `src` (length <= 16 floats, srcStride
-// apart) written to `dst` with a stride of dstStride = 8, 12 or 16 floats (elements >= length
-// are 0), so the gathers of an unaligned layout become vector loads: 256-bit rows of 8, three
-// 128-bit chunks for 9-12 floats (only the bytes used), 256-bit pairs for 13-16.  Values are
-// copied, so results do not change.
+// apart) written to `dst` with a stride of dstStride = 4, 8, 12 or 16 floats (elements >=
+// length are 0), so the gathers of an unaligned layout become vector loads: one 128-bit load
+// for up to 4 floats, one 256-bit load for 5-8, three 128-bit loads for 9-12 (only the bytes
+// used), two 256-bit loads for 13-16.  Values are copied, so results do not change.
 struct PadJob {
     const float *src;
     float *dst;
@@ -61,7 +61,7 @@ struct PadJob {
 
 // Row stride of the padded copy of a source `length` floats wide (0: not padded).
 inline int padded_stride(int length) {
-    return length <= 8 ? 8 : length <= 12 ? 12 : length <= 16 ? 16 : 0;
+    return length <= 4 ? 4 : length <= 8 ? 8 : length <= 12 ? 12 : length <= 16 ? 16 : 0;
 }
 
 // One launch over `count` pad jobs (device arrays: jobs, rowBase[count + 1] = prefix of their

@@ -287,7 +287,7 @@ def test_invalid_requests_return_false_and_empty_ranges_are_noops():
                                                    (12, 12, 0), (11, 13, 3), (16, 16, 0)])
 def test_device_table_unaligned_rows_on_a_large_table(length, stride, offset):
     """Device tables of >= 1M entries gather unaligned source rows from a padded copy (rows of
-    8, 12 or 16 floats, gathered with vector loads): results must be bit-identical to the
+    4, 8, 12 or 16 floats, gathered with vector loads): results must be bit-identical to the
     raw entry point (which gathers in place) and match the oracle."""
     torch = torch_cuda()
     from opensubdiv_gb300 import shapes
