@@ -211,10 +211,16 @@ __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(cons
         for (int i = m.s0 + (int)threadIdx.x; i < m.s1; i += kConsumers) {
             const int n = ssz[i - m.s0a];
             const int o = sof[i - m.s0a];
-            if (m.staged && o >= m.e0a && o + n <= m.e1)
+            if constexpr (VW == 12) {  // one output, 9-12 floats: single 12-wide pass
+                if (m.staged && o >= m.e0a && o + n <= m.e1)
+                    eval_one12(a, i, n, sidx, sw, o - m.e0a);
+                else
+                    eval_one<NW, 4>(a, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
+            } else if (m.staged && o >= m.e0a && o + n <= m.e1) {
                 eval_one<NW, VW>(a, i, n, sidx, sw, C::kCap, o - m.e0a, pol_src, pol_stream);
-            else
+            } else {
                 eval_one<NW, VW>(a, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
+            }
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[stage]);
@@ -281,6 +287,8 @@ int eval_stencils_staged(const float *src, float *const *dst, const int *strides
     }
     // source row loads: 256-bit when rows are 32-byte aligned, 128-bit when 16-byte aligned
     a.vecSrc = (al32(src) && srcStride % 8 == 0) ? 8 : (al16(src) && srcStride % 4 == 0) ? 4 : 1;
+    // one output 9-12 floats wide over 16-byte aligned rows (stride >= 12): single 12-wide pass
+    if (nw == 1 && a.vecSrc >= 4 && length > 8 && length <= 12) return tma::launch<1, 12>(a, s);
     switch (nw * 10 + a.vecSrc) {
         case 18: return tma::launch<1, 8>(a, s);
         case 14: return tma::launch<1, 4>(a, s);
