@@ -74,7 +74,10 @@ int GB300Synchronize(void *stream);
  * Replaces CudaEvalStencils (osd/cudaKernel.cu:351-383).  `sizes`, `offsets`, `indices`,
  * `weights` are device arrays of the Far::StencilTable (far/stencilTable.h:263-268).
  * Source and destination may be the same buffer (Osd::Mesh::Refine, osd/mesh.h:501-540) as
- * long as no destination element is also read as a source by another stencil. */
+ * long as no destination element is also read as a source by another stencil.  Source rows
+ * whose start and stride allow it are read with 128-/256-bit loads that may touch the row's
+ * elements up to its stride: the source buffer must span every row's full stride (as Osd
+ * vertex buffers of numVertices x stride floats do). */
 int GB300EvalStencils(const float *src, float *dst, int length, int srcStride, int dstStride,
                       const int *sizes, const int *offsets, const int *indices,
                       const float *weights, int start, int end, void *stream);
