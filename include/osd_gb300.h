@@ -43,7 +43,8 @@ enum {
     GB300_ERR_CUDA = 2,             /* a CUDA runtime call or launch failed */
     GB300_ERR_OUT_OF_MEMORY = 3,    /* device allocation failed; nothing was left allocated */
     GB300_ERR_UNSUPPORTED = 4,      /* e.g. an unknown patch type in a patch array */
-    GB300_ERR_DEVICE_TIMEOUT = 5    /* a bounded device-side wait gave up (see DESIGN) */
+    GB300_ERR_DEVICE_TIMEOUT = 5    /* a bounded device-side wait (4 s) gave up; the kernel
+                                       recorded it and returned instead of waiting longer */
 };
 
 /* Patch types (Far::PatchDescriptor::Type, far/patchDescriptor.h:48-63). */
