@@ -127,10 +127,16 @@ __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(cons
     __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
     __shared__ Meta meta[kStages];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    // Consumer groups: a tile holds kTile stencils (one per thread), fewer than the consumers
+    // when every stencil carries 3 or 6 weight arrays; the consumers then split into two
+    // groups that take alternate tiles of the ring, so all of them have a stencil to work on.
+    constexpr int G = NW == 1 ? 1 : 2;
+    constexpr int GT = kConsumers / G;  // threads per group
+    constexpr int GW = GT / 32;         // warps per group
     if (threadIdx.x == 0) {
         for (int s = 0; s < kStages; ++s) {
             mbar_init(&full[s], 32);
-            mbar_init(&empty[s], kConsumers / 32);
+            mbar_init(&empty[s], GW);  // one group consumes each tile
         }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
@@ -199,8 +205,11 @@ __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(cons
     }
 
     // ---------------- consumer warps ----------------
-    int it = 0;
-    for (int t = blockIdx.x; t < a.numTiles; t += gridDim.x, ++it) {
+    // group g takes this CTA's tiles it = g, g + G, g + 2G, ... (tile t = blockIdx.x + it * grid)
+    const int grp = warp / GW;
+    const int gtid = (int)threadIdx.x - grp * GT;
+    int it = grp;
+    for (int t = blockIdx.x + grp * gridDim.x; t < a.numTiles; t += G * gridDim.x, it += G) {
         const int stage = it % kStages;
         const uint32_t use = (uint32_t)(it / kStages);
         if (!mbar_wait(&full[stage], use & 1)) return;
@@ -208,7 +217,7 @@ __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(cons
         float *sw;
         stage_ptrs<NW>(smem, stage, &sidx, &sw, &ssz, &sof);
         const Meta m = meta[stage];
-        for (int i = m.s0 + (int)threadIdx.x; i < m.s1; i += kConsumers) {
+        for (int i = m.s0 + gtid; i < m.s1; i += GT) {
             const int n = ssz[i - m.s0a];
             const int o = sof[i - m.s0a];
             if constexpr (VW == 12) {  // one output, 9-12 floats: single 12-wide pass

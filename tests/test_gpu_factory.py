@@ -198,3 +198,28 @@ def test_composed_scattered_table_evaluates_like_an_uploaded_one():
                          h["indices"], [h["weights"], h["du_weights"], h["dv_weights"]])
     for a, r in zip(outs[0], ref):
         assert np.abs(a.cpu().numpy() - r).max() <= 1e-4 * max(1.0, np.abs(r).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("cage_id", ["torus_creases_L3", "cube_L4", "loop_L3", "pole30_L3"])
+def test_factory_on_generator_masks_matches_oracle(cage_id):
+    """Larger tables from the host generator's masks (Far::PrimvarRefiner form): the device
+    factory equals the oracle's restatement of StencilBuilder's merge bit for bit, for every
+    level (intermediate levels kept) and for the last level with control vertices."""
+    torch_cuda()
+    from opensubdiv_gb300 import shapes, topology
+    from opensubdiv_gb300.evaluator import GB300StencilTableFactory as F
+    cage, level = {
+        "torus_creases_L3": (shapes.torus(64, 32, tri_fraction=0.1, crease_fraction=0.05,
+                                          seed=21), 3),
+        "cube_L4": (shapes.cube(6, seed=22), 4),
+        "loop_L3": (shapes.torus(32, 16, crease_fraction=0.05, seed=23,
+                                 scheme=shapes.LOOP), 3),
+        "pole30_L3": (shapes.bipyramid(30), 3),
+    }[cage_id]
+    nc, levels = topology.UniformRefiner(cage, level, stencils=False).factory_masks()
+    for inter, ctrl in ((True, False), (False, True)):
+        want = oracle.factory_create(nc, levels, intermediate=inter, control=ctrl)
+        got = F.Create(nc, levels, generateIntermediateLevels=inter, generateControlVerts=ctrl,
+                       sortEntries=False).CopyToHost()
+        assert same_table(got, want), (inter, ctrl)
