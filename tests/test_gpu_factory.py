@@ -223,3 +223,47 @@ def test_factory_on_generator_masks_matches_oracle(cage_id):
         got = F.Create(nc, levels, generateIntermediateLevels=inter, generateControlVerts=ctrl,
                        sortEntries=False).CopyToHost()
         assert same_table(got, want), (inter, ctrl)
+
+
+def _random_levels(rng, nc, rows, fan=6, same_level=0.3, zero=0.05):
+    """Random masks: each row names sources of the previous level (or control vertices) and,
+    with probability `same_level`, earlier rows of its own level, so dependency chains run
+    several waves deep; some weights are 0 (dropped) and some rows end up empty."""
+    levels, first, prev_first, prev_n = [], nc, 0, nc
+    for n in rows:
+        off, src, w = [0], [], []
+        for r in range(n):
+            k = int(rng.integers(0, fan + 1))
+            for _ in range(k):
+                if r > 0 and rng.random() < same_level:
+                    src.append(first + int(rng.integers(0, r)))
+                else:
+                    src.append(prev_first + int(rng.integers(0, prev_n)))
+                w.append(0.0 if rng.random() < zero else float(rng.normal()))
+            off.append(len(src))
+        levels.append(dict(offsets=np.array(off, np.int64), sources=np.array(src, np.int32),
+                           weights=np.array(w, np.float32)))
+        prev_first, prev_n, first = first, n, first + n
+    return levels
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_factory_random_masks_match_oracle(seed):
+    """Synthetic masks with deep same-level chains (many dependency waves), zero weights,
+    empty rows, an empty level and mixed row lengths: device factory == oracle, bit for bit;
+    a factory with no levels gives one identity stencil per control vertex."""
+    torch_cuda()
+    from opensubdiv_gb300.evaluator import GB300StencilTableFactory as F
+    rng = np.random.default_rng(seed)
+    nc = 50
+    levels = _random_levels(rng, nc, [200, 400, 900, 0] if seed == 2 else [200, 400, 900])
+    for inter, ctrl in ((True, False), (False, True)):
+        want = oracle.factory_create(nc, levels, intermediate=inter, control=ctrl)
+        got = F.Create(nc, levels, generateIntermediateLevels=inter, generateControlVerts=ctrl,
+                       sortEntries=False).CopyToHost()
+        assert same_table(got, want), (inter, ctrl)
+    ident = F.Create(nc, [], generateControlVerts=True, sortEntries=False).CopyToHost()
+    assert np.array_equal(ident["sizes"], np.ones(nc, np.int32))
+    assert np.array_equal(ident["indices"], np.arange(nc, dtype=np.int32))
+    assert np.array_equal(ident["weights"], np.ones(nc, np.float32))
