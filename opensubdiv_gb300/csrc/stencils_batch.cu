@@ -137,6 +137,21 @@ struct JobView {
           outRow(j.outRow) {}
 };
 
+// Consumers' work on one staged tile of a job 9-12 floats wide over 16-byte aligned rows
+// (stride >= 12): the single 12-wide pass (the wide instantiation of the kernel only).
+__device__ __forceinline__ void tile_threads12(const Job &j, const Meta &m, const int *sidx,
+                                               const float *sw, const int *ssz, const int *sof,
+                                               uint64_t pol_src, uint64_t pol_stream) {
+    const JobView v(j);
+    for (int i = m.s0 + (int)threadIdx.x; i < m.s1; i += kConsumers) {
+        const int n = ssz[i - m.s0a], o = sof[i - m.s0a];
+        if (m.staged && o >= m.e0a && o + n <= m.e1)
+            tma::eval_one12(v, i, n, sidx, sw, o - m.e0a);
+        else
+            tma::eval_one<1, 4>(v, i, n, nullptr, nullptr, 0, o, pol_src, pol_stream);
+    }
+}
+
 // Consumers' work on one staged tile (VW = 0: the job's row width chosen per gather).
 template <int VW>
 __device__ __forceinline__ void tile_threads(const Job &j, const Meta &m, const int *sidx,
@@ -161,6 +176,9 @@ struct Args {
     int dynamic;          // 1: tiles claimed from the counter, 0: CTA b takes b, b + grid, ...
 };
 
+// WIDE: every job of the launch is 9-12 floats wide over 16-byte aligned rows (single 12-wide
+// pass); otherwise any job (one run-time-width path).
+template <bool WIDE>
 __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
     extern __shared__ __align__(128) char smem[];
     __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
@@ -278,7 +296,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
         const Job &j = sjob[stage];
         if (j.mode == 0) {
             // one code path for every row width (inlined width-specific paths spill registers)
-            tile_threads<0>(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
+            if constexpr (WIDE)
+                tile_threads12(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
+            else
+                tile_threads<0>(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
         } else {
             for (int i = m.s0 + warp; i < m.s1; i += kConsumers / 32) {
                 const int n = ssz[i - m.s0a], o = sof[i - m.s0a];
@@ -392,15 +413,21 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 int set_smem_attribute() {
     static std::atomic<uint64_t> attr{0};  // devices whose function attribute is set
     return once_per_device(attr, [] {
-        return check_cuda(cudaFuncSetAttribute(k_stencils_batch,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kSmem),
-                          "batch smem attribute");
+        int st = check_cuda(cudaFuncSetAttribute(k_stencils_batch<false>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kSmem),
+                            "batch smem attribute");
+        if (st == GB300_OK)
+            st = check_cuda(cudaFuncSetAttribute(k_stencils_batch<true>,
+                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                 (int)kSmem),
+                            "batch smem attribute");
+        return st;
     });
 }
 
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic) {
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic, bool wide) {
     int st = set_smem_attribute();
     if (st != GB300_OK) return st;
     if (numTiles == 0) return ok();
@@ -410,7 +437,10 @@ int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int
     }
     Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus, dynamic};
     const int grid = std::min(numTiles, num_sms() * ctasPerSm);
-    k_stencils_batch<<<grid, kThreads, kSmem, s>>>(a);
+    if (wide)
+        k_stencils_batch<true><<<grid, kThreads, kSmem, s>>>(a);
+    else
+        k_stencils_batch<false><<<grid, kThreads, kSmem, s>>>(a);
     count_launch();
     return check_launch("batched EvalStencils");
 }
@@ -452,13 +482,16 @@ using namespace gb300;
 using namespace gb300::batch;
 
 struct GB300StencilBatch {
-    std::vector<Job> jobs;     // in launch order: largest first
+    // in launch order: the general jobs, then the jobs 9-12 floats wide over 16-byte aligned
+    // rows (the kernel's 12-wide instantiation), each part largest first
+    std::vector<Job> jobs;
     std::vector<double> mean;  // mean stencil size per job (same order)
+    int numWide = 0;           // jobs at the end run by the 12-wide launch
     Config cfg;
-    Job *dJobs = nullptr;      // jobs, then numJobs + 1 ints of tile prefix
-    int *dTileBase = nullptr;
-    int *dCounter = nullptr;   // [0] work counter, [1] status word
-    int numTiles = 0;
+    Job *dJobs = nullptr;      // jobs, then the tile prefixes: general (n - numWide + 1 ints)
+    int *dTileBase = nullptr;  // and wide (numWide + 1 ints)
+    int *dCounter = nullptr;   // [0] work counter, [1] status word, [2] wide work counter
+    int numTiles = 0, numTilesWide = 0;
     uint64_t signature = 0;
     cudaGraphExec_t graph = nullptr;  // pad copy + counter reset + kernel, on first use
     cudaStream_t capture = nullptr;
@@ -489,24 +522,32 @@ std::map<uint64_t, Config> g_tuned;  // work signature -> best config
 
 // Applies b->cfg: job modes, tile sizes and the tile prefix, uploaded to the device.
 int upload_plan(GB300StencilBatch *b, cudaStream_t s) {
-    const int n = (int)b->jobs.size();
-    std::vector<int> base(n + 1);
-    b->numTiles = plan_tiles(b->jobs.data(), b->mean.data(), n, b->cfg.tileStencils,
+    const int n = (int)b->jobs.size(), ng = n - b->numWide;
+    std::vector<int> base(n + 2);
+    b->numTiles = plan_tiles(b->jobs.data(), b->mean.data(), ng, b->cfg.tileStencils,
                              b->cfg.warpThreshold, base.data());
+    b->numTilesWide = plan_tiles(b->jobs.data() + ng, b->mean.data() + ng, b->numWide,
+                                 b->cfg.tileStencils, b->cfg.warpThreshold,
+                                 base.data() + ng + 1);
     int st = check_cuda(cudaMemcpyAsync(b->dJobs, b->jobs.data(), n * sizeof(Job),
                                         cudaMemcpyHostToDevice, s), "batch jobs");
     if (st != GB300_OK) return st;
-    st = check_cuda(cudaMemcpyAsync(b->dTileBase, base.data(), (n + 1) * sizeof(int),
+    st = check_cuda(cudaMemcpyAsync(b->dTileBase, base.data(), (n + 2) * sizeof(int),
                                     cudaMemcpyHostToDevice, s), "batch jobs");
     if (st != GB300_OK) return st;
     return check_cuda(cudaStreamSynchronize(s), "batch jobs");
 }
 
 int launch_batch(GB300StencilBatch *b, cudaStream_t s) {
-    const int st = launch_pad(b->dPad, b->dPadBase, b->numPad, b->padRows, s);
+    int st = launch_pad(b->dPad, b->dPadBase, b->numPad, b->padRows, s);
     if (st != GB300_OK) return st;
-    return launch_jobs(b->dJobs, b->dTileBase, (int)b->jobs.size(), b->numTiles, b->dCounter,
-                       b->dCounter + 1, b->cfg.ctasPerSm, s, b->cfg.dynamic);
+    const int ng = (int)b->jobs.size() - b->numWide;
+    st = launch_jobs(b->dJobs, b->dTileBase, ng, b->numTiles, b->dCounter, b->dCounter + 1,
+                     b->cfg.ctasPerSm, s, b->cfg.dynamic, false);
+    if (st != GB300_OK) return st;
+    return launch_jobs(b->dJobs + ng, b->dTileBase + ng + 1, b->numWide, b->numTilesWide,
+                       b->dCounter + 2, b->dCounter + 1, b->cfg.ctasPerSm, s, b->cfg.dynamic,
+                       true);
 }
 
 // Jobs whose source rows are unaligned (scalar gathers) and at most 8 floats wide read a
@@ -639,6 +680,22 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
         delete b;
         return nullptr;
     }
+    // jobs one output 9-12 floats wide over 16-byte aligned rows (stride >= 12) go last, to
+    // the 12-wide launch (order within each part kept: largest first)
+    {
+        auto wide = [](const Job &j) { return j.vw >= 4 && j.length > 8 && j.length <= 12; };
+        std::vector<Job> gj, wj;
+        std::vector<double> gm, wm;
+        for (size_t k = 0; k < b->jobs.size(); ++k) {
+            (wide(b->jobs[k]) ? wj : gj).push_back(b->jobs[k]);
+            (wide(b->jobs[k]) ? wm : gm).push_back(b->mean[k]);
+        }
+        b->numWide = (int)wj.size();
+        gj.insert(gj.end(), wj.begin(), wj.end());
+        gm.insert(gm.end(), wm.begin(), wm.end());
+        b->jobs.swap(gj);
+        b->mean.swap(gm);
+    }
     // every job's vector width must match its rows' alignment (the gathers assume it)
     for (const Job &j : b->jobs) {
         const uintptr_t a = (uintptr_t)j.src;
@@ -657,16 +714,16 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
         if (it != g_tuned.end()) b->cfg = it->second;
     }
     const size_t jobBytes = ((numJobs * sizeof(Job) + 255) / 256) * 256;
-    if (check_cuda(cudaMalloc((void **)&b->dJobs, jobBytes + (numJobs + 1) * sizeof(int)),
+    if (check_cuda(cudaMalloc((void **)&b->dJobs, jobBytes + (numJobs + 2) * sizeof(int)),
                    "batch jobs") != GB300_OK) {
         b->dJobs = nullptr;
         delete b;
         return nullptr;
     }
     b->dTileBase = (int *)((char *)b->dJobs + jobBytes);
-    if (check_cuda(cudaMalloc((void **)&b->dCounter, 2 * sizeof(int)), "batch counter") !=
+    if (check_cuda(cudaMalloc((void **)&b->dCounter, 3 * sizeof(int)), "batch counter") !=
             GB300_OK ||
-        check_cuda(cudaMemsetAsync(b->dCounter, 0, 2 * sizeof(int), s), "batch counter") !=
+        check_cuda(cudaMemsetAsync(b->dCounter, 0, 3 * sizeof(int), s), "batch counter") !=
             GB300_OK ||
         upload_plan(b, s) != GB300_OK) {
         delete b;
@@ -716,6 +773,7 @@ int GB300StencilBatchEvalGraph(GB300StencilBatch *b, void *stream) {
     int st = check_cuda(cudaGraphLaunch(b->graph, s), "GB300StencilBatchEvalGraph");
     if (st != GB300_OK) return st;
     if (b->numTiles) count_launch();
+    if (b->numTilesWide) count_launch();
     return ok();
 }
 
@@ -735,7 +793,7 @@ int GB300StencilBatchGetConfig(const GB300StencilBatch *b, int *tileStencils, in
     if (tileStencils) *tileStencils = b->cfg.tileStencils;
     if (ctasPerSm) *ctasPerSm = b->cfg.ctasPerSm;
     if (warpThreshold) *warpThreshold = b->cfg.warpThreshold;
-    if (numTiles) *numTiles = b->numTiles;
+    if (numTiles) *numTiles = b->numTiles + b->numTilesWide;
     if (dynamicClaims) *dynamicClaims = b->cfg.dynamic;
     return ok();
 }
@@ -885,7 +943,7 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
         return st;
     Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1, 1};
     const int grid = (int)std::min<long long>(tiles, 2LL * sms);
-    k_stencils_batch<<<grid, kThreads, kSmem, s>>>(a);
+    k_stencils_batch<false><<<grid, kThreads, kSmem, s>>>(a);
     count_launch();
     return check_launch(who);
 }

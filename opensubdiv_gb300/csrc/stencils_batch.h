@@ -42,9 +42,10 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 
 // One persistent launch over n jobs (device arrays dJobs[n], dTileBase[n + 1]).  dynamic: tiles
 // are claimed from the work counter (reset on `s` first), else CTA b takes tiles b, b + grid,
-// ...  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.
+// ...  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.  wide: every job is one
+// output 9-12 floats wide over 16-byte aligned rows (the kernel's single 12-wide pass).
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1);
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1, bool wide = false);
 
 // Padded copy of one source: rows [0, numRows) of `src` (length <= 16 floats, srcStride
 // apart) written to `dst` with a stride of dstStride = 4, 8, 12 or 16 floats (elements >=
