@@ -68,17 +68,19 @@ def parse():
     return ap.parse_args()
 
 
-def bench_patches(args, stream, peak):
+def bench_patches(args, stream, peak, loop=False):
     """Secondary measurement: device PatchMap lookup + EvalPatches (P and all five
     derivatives) at 4M uniform points on a table of the 512 x 256 torus's adaptive level-4
-    size (see workloads.eval_patches_torus)."""
+    size (workloads.eval_patches_torus) or, with `loop`, of the level-6 icosphere's adaptive
+    Loop table (workloads.eval_patches_icosphere)."""
     import torch
 
     from opensubdiv_gb300 import workloads
     from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
                                             GB300PatchTable)
 
-    w = workloads.eval_patches_torus(args.patch_points)
+    w = (workloads.eval_patches_icosphere if loop else workloads.eval_patches_torus)(
+        args.patch_points)
     n = len(w["face"])
     table = GB300PatchTable.Create(w["arrays"], w["indices"], w["params"], w["triangular"])
     src = torch.from_numpy(w["src"]).cuda()
@@ -133,7 +135,7 @@ def bench_patches(args, stream, peak):
                          "algorithmic_bytes": b, "achieved": b / (eval_ms / 1e3) / 1e9,
                          "peak": peak, "unit": "GB/s",
                          "frac": b / (eval_ms / 1e3) / 1e9 / peak,
-                         "traffic": ncu_traffic("patches")},
+                         "traffic": ncu_traffic("patches_loop" if loop else "patches")},
             "max_abs_err_P_vs_oracle_slice": err_p}
 
 
@@ -862,6 +864,7 @@ def run_gb300(args, rank, world):
     }
     if not args.no_patches:
         line["eval_patches"] = bench_patches(args, stream, peak)
+        line["eval_patches_loop"] = bench_patches(args, stream, peak, loop=True)
     if not args.no_batch:
         line["batching"] = bench_batch(args, stream, peak)
     if not args.no_serving:

@@ -397,10 +397,17 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
     m[3] = s * s; m[4] = s * t; m[5] = t * t;
     m[6] = m[3] * s; m[7] = m[4] * s; m[8] = m[4] * t; m[9] = m[5] * t;
     m[10] = m[6] * s; m[11] = m[7] * s; m[12] = m[3] * m[5]; m[13] = m[8] * t; m[14] = m[9] * t;
-    int idx[12];
-    load_indices<12>(cvs, idx);
+    // the 12 control points once (every index of a Loop patch is valid, phantom boundary
+    // points included, as the reference's own gather of all 12 relies on), then one
+    // derivative order at a time: 12 weights live instead of 72, no reloads
+    float x[12][LC];
+    {
+        int idx[12];
+        load_indices<12>(cvs, idx);
+#pragma unroll
+        for (int j = 0; j < 12; ++j) load_row<LC>(src, stride, idx[j], e0, length, x[j]);
+    }
     const float k12 = 1.0f / 12.0f, k6 = 1.0f / 6.0f;
-    // one derivative order at a time keeps 12 weights live instead of 72
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         float w[12];
@@ -417,10 +424,8 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
 #pragma unroll
         for (int j = 0; j < 12; ++j) {
             if (w[j] == 0.0f) continue;
-            float x[LC];
-            load_row<LC>(src, stride, idx[j], e0, length, x);
 #pragma unroll
-            for (int c = 0; c < LC; ++c) acc.v[k][c] = fmaf(w[j], x[c], acc.v[k][c]);
+            for (int c = 0; c < LC; ++c) acc.v[k][c] = fmaf(w[j], x[j][c], acc.v[k][c]);
         }
     }
 }

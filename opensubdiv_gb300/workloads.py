@@ -94,6 +94,30 @@ def eval_patches_torus(n_points=4_000_000, target_patches=1_284_866, seed=7):
                 num_ptex=nptex, triangular=tri, face=face, u=u, v=v, copies=copies)
 
 
+def eval_patches_icosphere(n_points=4_000_000, target_loop_patches=82_580, seed=8):
+    """EvalPatches workload at the size of the level-6 icosphere's adaptive Loop table
+    (82,580 LOOP patches): the reference's own adaptive level-3 Loop table of the level-2
+    icosphere (tests/golden/icosphere2_patches_L3.npz: LOOP + GREGORY_TRIANGLE end caps),
+    instanced to that LOOP patch count, evaluated at n_points uniform (ptex face, u, v)
+    locations folded into the triangle (u + v <= 1)."""
+    import os
+    fixture = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                           "tests", "golden", "icosphere2_patches_L3.npz")
+    arr = np.load(fixture)["arrays"]
+    per_loop = int(arr[arr[:, 0] == 5, 2].sum())
+    copies = max(1, round(target_loop_patches / per_loop))
+    arrays, indices, params, src, nptex, tri = instanced_patch_table(fixture, copies)
+    rng = np.random.default_rng(seed)
+    face = rng.integers(0, nptex, n_points).astype(np.int32)
+    u = rng.random(n_points).astype(np.float32)
+    v = rng.random(n_points).astype(np.float32)
+    fold = u + v > 1.0
+    u[fold], v[fold] = 1.0 - u[fold], 1.0 - v[fold]
+    return dict(name=f"icosphere2_adaptiveL3_loop_x{copies}_{n_points // 1000000}Mpts",
+                arrays=arrays, indices=indices, params=params, src=src, length=3,
+                num_ptex=nptex, triangular=tri, face=face, u=u, v=v, copies=copies)
+
+
 def patch_bytes(n_points, length, n_outputs, n_src, touched_patches, cvs_per_patch):
     """Unique-bytes model of one EvalPatches pass: coords (20 B per point), outputs
     (4 B x length x outputs per point), touched patches' index rows and params
