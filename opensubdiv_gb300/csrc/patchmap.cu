@@ -6,7 +6,8 @@
 // (bit 31 set, bit 30 leaf, bits 0..29 node or handle index).  Quad tables walk in float:
 // every step subtracts a power of two `median` from a value in [median, 2*median], which is
 // exact (Sterbenz), so the float walk takes the reference's double-precision decisions.
-// Triangle tables test u+v against the median and walk in double like the reference.
+// Triangle tables walk the same way and form only their u + v tests in double, as the
+// reference rounds them.
 #include "common.cuh"
 #include "patchmap.h"
 
@@ -157,14 +158,18 @@ __global__ void __launch_bounds__(256) k_find_patches(const FindArgs a) {
                         node = __ldg(a.nodes + (c & kIndex));
                     }
                 } else {
-                    double u = fu, v = fv, median = 0.5;
+                    // every subtraction takes the power-of-two median from a value in
+                    // [median, 2 * median] (exact in float, Sterbenz), so u and v hold the
+                    // reference's double values exactly; only the sums u + v, which the
+                    // reference rounds in double, are formed in double
+                    float u = fu, v = fv, median = 0.5f;
                     bool rot = false;
-                    for (int d = 0; d <= a.maxDepth; ++d, median *= 0.5) {
+                    for (int d = 0; d <= a.maxDepth; ++d, median *= 0.5f) {
                         int q;
                         if (!rot) {
                             if (u >= median) { u -= median; q = 1; }
                             else if (v >= median) { v -= median; q = 2; }
-                            else if ((u + v) >= median) { rot = true; q = 3; }
+                            else if (((double)u + (double)v) >= (double)median) { rot = true; q = 3; }
                             else q = 0;
                         } else {
                             if (u < median) { v -= median; q = 1; }
@@ -172,7 +177,7 @@ __global__ void __launch_bounds__(256) k_find_patches(const FindArgs a) {
                             else {
                                 u -= median;
                                 v -= median;
-                                if ((u + v) < median) { rot = false; q = 3; }
+                                if (((double)u + (double)v) < (double)median) { rot = false; q = 3; }
                                 else q = 0;
                             }
                         }

@@ -239,3 +239,43 @@ def test_eval_patches_varying_and_face_varying(path):
     with pytest.raises(GB300Error):
         t.SetVarying(bad, z["varying_indices"])
     assert not Ev.EvalPatchesFaceVarying(dev(z["fvar_src"]), d2, fo[0], d2, m, coords, t, 3)
+
+
+@pytest.mark.gpu
+def test_triangle_patchmap_sums_at_the_median():
+    """Triangle quadtree walks decide on u + v against the median, which the reference rounds
+    in double: queries whose sum lies within an ulp of a median (and sums of very different
+    magnitudes) must take the reference's decisions (oracle PatchMap, pinned to Far)."""
+    torch = torch_cuda()
+    z = np.load(os.path.join(GOLDEN, "icosphere2_patches_L3.npz"))
+    t = _table(z)
+    rng = np.random.default_rng(31)
+    nptex = int(z["num_ptex"])
+    us, vs = [], []
+    for m in (0.5, 0.25, 0.125, 0.0625):
+        u = (rng.random(2000) * m).astype(np.float32)
+        v = (np.float32(m) - u).astype(np.float32)
+        for dv in (v, np.nextafter(v, np.float32(0)), np.nextafter(v, np.float32(1))):
+            us.append(u)
+            vs.append(dv)
+        # one tiny operand next to a value just below the median
+        us.append(np.full(500, np.nextafter(np.float32(m), np.float32(0)), np.float32))
+        vs.append((rng.random(500) * 2.0 ** -40).astype(np.float32))
+    # the same queries inside rotated sub-triangles (offset by the parent's median)
+    u = np.concatenate(us)
+    v = np.concatenate(vs)
+    u2 = np.clip(np.float32(1.0) - u, 0, 1).astype(np.float32)
+    v2 = np.clip(np.float32(1.0) - v, 0, 1).astype(np.float32)
+    u = np.concatenate([u, np.float32(0.5) - u * np.float32(0.5), u2 * np.float32(0.5)])
+    v = np.concatenate([v, np.float32(0.5) - v * np.float32(0.5), v2 * np.float32(0.5)])
+    u = np.clip(u, 0, 1).astype(np.float32)
+    v = np.clip(v, 0, 1).astype(np.float32)
+    face = rng.integers(0, nptex, len(u)).astype(np.int32)
+    n = len(face)
+    out = torch.zeros(n * 5, dtype=torch.int32, device="cuda")
+    t.FindPatches(n, dev(face), dev(u), dev(v), out)
+    torch.cuda.synchronize()
+    got = host(out).reshape(n, 5)[:, :3]
+    pm = oracle.PatchMap(z["arrays"], z["params"], True)
+    want = pm.find(face, u.astype(np.float64), v.astype(np.float64))
+    assert np.array_equal(got, want)
