@@ -223,3 +223,34 @@ def test_batch_mixed_padded_widths_with_odd_row_counts():
     for L, a, b in zip(widths, dsts, plain):
         assert torch.equal(a, b), L
     assert batch.GetDeviceStatus() == 0
+
+
+@pytest.mark.gpu
+def test_batch_of_only_wide_jobs():
+    """Every job 9-12 floats wide (aligned and padded rows): the general launch has no jobs and
+    the 12-wide launch does all the work; graph replay included; results equal plain calls."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import shapes, topology
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD
+    from opensubdiv_gb300.evaluator import GB300StencilBatch, GB300StencilTable
+    cage = shapes.torus(9, 7, tri_fraction=0.1, seed=5)
+    t = topology.UniformRefiner(cage, 2).stencil_table()
+    table = GB300StencilTable.Create(**t)
+    n, ncv = len(t["sizes"]), cage.num_vertices
+    rng = np.random.default_rng(13)
+    widths = [(12, 12), (9, 9), (10, 12), (11, 11), (12, 16)]
+    srcs, dsts, plain, sds, dds = [], [], [], [], []
+    for L, stride in widths:
+        srcs.append(dev(rng.uniform(-1, 1, ncv * stride).astype(np.float32)))
+        dsts.append(torch.zeros(n * L, device="cuda"))
+        plain.append(torch.zeros(n * L, device="cuda"))
+        sds.append(BD(0, L, stride))
+        dds.append(BD(0, L, L))
+    batch = GB300StencilBatch([(table, s, sd, o, dd)
+                               for s, sd, o, dd in zip(srcs, sds, dsts, dds)])
+    assert batch.GetConfig()["num_tiles"] > 0
+    batch.EvalGraph()
+    _plain(torch, [table] * len(widths), srcs, sds, plain, dds)
+    for (L, stride), a, b in zip(widths, dsts, plain):
+        assert torch.equal(a, b), (L, stride)
+    assert batch.GetDeviceStatus() == 0
