@@ -90,7 +90,9 @@ struct Cfg {
     static constexpr int kTile = kCap / 16;                               // stencils per tile
     static constexpr int kMeta = kTile + 8;  // sizes/offsets slots (window starts 4-aligned)
     static constexpr size_t kStageBytes = (size_t)kCap * 4 * (1 + NW) + (size_t)kMeta * 8;
-    static constexpr size_t kSmem = kStages * kStageBytes + 256;
+    // ring depth: 4 stages for 6 outputs (one CTA per SM, small stages), else 3
+    static constexpr int kRing = NW == 6 ? 4 : kStages;
+    static constexpr size_t kSmem = kRing * kStageBytes + 256;
 };
 
 struct Args {
@@ -124,17 +126,20 @@ template <int NW, int VW>
 __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(const Args a) {
     extern __shared__ __align__(128) char smem[];
     using C = Cfg<NW>;
-    __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
-    __shared__ Meta meta[kStages];
+    constexpr int S = C::kRing;
+    __shared__ __align__(8) uint64_t full[S], empty[S];
+    __shared__ Meta meta[S];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     // Consumer groups: a tile holds kTile stencils (one per thread), fewer than the consumers
-    // when every stencil carries 3 or 6 weight arrays; the consumers then split into two
-    // groups that take alternate tiles of the ring, so all of them have a stencil to work on.
-    constexpr int G = NW == 1 ? 1 : 2;
+    // when every stencil carries 3 or 6 weight arrays; the consumers then split into groups
+    // of kTile threads that take turns on the tiles of the ring, so all of them have a
+    // stencil to work on (2 groups for 3 outputs, 4 for 6 with a 4-stage ring).
+    constexpr int G = kConsumers / C::kTile;
+    static_assert(G >= 1 && G <= S && kConsumers % G == 0, "consumer groups");
     constexpr int GT = kConsumers / G;  // threads per group
     constexpr int GW = GT / 32;         // warps per group
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             mbar_init(&full[s], 32);
             mbar_init(&empty[s], GW);  // one group consumes each tile
         }
@@ -147,8 +152,8 @@ __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(cons
         // ---------------- producer warp ----------------
         int it = 0;
         for (int t = blockIdx.x; t < a.numTiles; t += gridDim.x, ++it) {
-            const int stage = it % kStages;
-            const uint32_t use = (uint32_t)(it / kStages);
+            const int stage = it % S;
+            const uint32_t use = (uint32_t)(it / S);
             if (use > 0 && !mbar_wait(&empty[stage], (use - 1) & 1)) return;
             int *sidx, *ssz, *sof;
             float *sw;
@@ -210,8 +215,8 @@ __global__ void __launch_bounds__(kThreads, NW == 6 ? 1 : 2) k_stencils_tma(cons
     const int gtid = (int)threadIdx.x - grp * GT;
     int it = grp;
     for (int t = blockIdx.x + grp * gridDim.x; t < a.numTiles; t += G * gridDim.x, it += G) {
-        const int stage = it % kStages;
-        const uint32_t use = (uint32_t)(it / kStages);
+        const int stage = it % S;
+        const uint32_t use = (uint32_t)(it / S);
         if (!mbar_wait(&full[stage], use & 1)) return;
         int *sidx, *ssz, *sof;
         float *sw;
