@@ -92,7 +92,7 @@ def test_eval_stencils_device_table_and_fp64(path):
 @pytest.mark.gpu
 @pytest.mark.parametrize("path", [p for p in FIXTURES if "limit_sizes" in np.load(p)],
                          ids=os.path.basename)
-@pytest.mark.parametrize("nout", [1, 3, 6])
+@pytest.mark.parametrize("nout", [1, 2, 3, 4, 5, 6])
 def test_limit_stencils_fused_derivatives(path, nout):
     torch = torch_cuda()
     Ev, BD = _ev()
