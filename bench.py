@@ -846,7 +846,7 @@ def run_gb300(args, rank, world):
                    "limit_nnz": int(len(lim["indices"])), "primvars": L,
                    "l2": "per-step working set 1.4 GB > 129 MB L2 (no flush needed)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
-        "roofline": {"bound": "hbm", "kernel": "k_stencils_tma<1,8> (refine EvalStencils, staged)",
+        "roofline": {"bound": "hbm", "kernel": "k_stencils_sell<1,8> (refine EvalStencils, sliced layout, staged ring)",
                      "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": b_ref, "launch_ms": ref_ms,

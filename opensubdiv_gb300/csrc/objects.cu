@@ -4,6 +4,7 @@
 // allocation or copy frees everything allocated so far and reports a status.
 #include "common.cuh"
 #include "patchmap.h"
+#include "sell.h"
 #include "stencils_batch.h"
 #include "tables.h"
 
@@ -97,69 +98,14 @@ struct GB300StencilTable {
     int64_t nnz = 0;
     int numControl = 0;  // largest control index + 1 (rows of the source the table reads)
     void *buf[9] = {nullptr};  // sizes, offsets, indices, w, du, dv, duu, duv, dvv
-    // Evaluation order for tables whose consecutive stencils are scattered over the control
-    // points (limit stencils at random locations): the same stencils sorted by their lowest
-    // control index, each writing back to its original destination row (outRow).
-    void *ebuf[9] = {nullptr};
-    void *outRow = nullptr;
+    // Sliced evaluation layout (sell.h): sz, sliceSlot, idx, w x 6, outRow
+    gb300::SellTable sell;
+    void *sbuf[10] = {nullptr};
     ~GB300StencilTable() {
         for (auto &p : buf) release(p);
-        for (auto &p : ebuf) release(p);
-        release(outRow);
+        for (auto &p : sbuf) release(p);
     }
 };
-
-namespace {
-
-// Builds the locality-sorted evaluation layout when consecutive stencils' lowest control
-// indices jump by more than 1% of the index range on average.  Entries must already be
-// sorted per stencil (index[offset] is the lowest).  Returns false when not worthwhile.
-bool evaluation_order(int n, int64_t nnz, const int *sizes, const int *offsets,
-                      const int *indices, const float *const *w, std::vector<int> &order,
-                      std::vector<int> &esz,
-                      std::vector<int> &eoff, std::vector<int> &eidx,
-                      std::vector<std::vector<float>> &ew) {
-    if (n < 4096) return false;
-    int maxIdx = 1;
-    double jump = 0.0;
-    int prev = -1;
-    for (int i = 0; i < n; ++i) {
-        const int key = sizes[i] > 0 ? indices[offsets[i]] : 0;
-        maxIdx = std::max(maxIdx, key);
-        if (prev >= 0) jump += std::abs(key - prev);
-        prev = key;
-    }
-    if (jump / (n - 1) < 0.01 * maxIdx) return false;
-    order.resize(n);
-    for (int i = 0; i < n; ++i) order[i] = i;
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-        const int ka = sizes[a] > 0 ? indices[offsets[a]] : -1;
-        const int kb = sizes[b] > 0 ? indices[offsets[b]] : -1;
-        return ka < kb;
-    });
-    esz.resize(n);
-    eoff.resize(n);
-    int64_t z = 0;
-    for (int j = 0; j < n; ++j) {
-        esz[j] = sizes[order[j]];
-        eoff[j] = (int)z;
-        z += esz[j];
-    }
-    // arrays keep the original entry count (a table with gaps packs into fewer entries)
-    eidx.assign(std::max<int64_t>(z, nnz), 0);
-    ew.assign(6, {});
-    for (int k = 0; k < 6; ++k)
-        if (w[k]) ew[k].assign(std::max<int64_t>(z, nnz), 0.0f);
-    for (int j = 0; j < n; ++j) {
-        const int o = offsets[order[j]];
-        std::copy(indices + o, indices + o + esz[j], eidx.begin() + eoff[j]);
-        for (int k = 0; k < 6; ++k)
-            if (w[k]) std::copy(w[k] + o, w[k] + o + esz[j], ew[k].begin() + eoff[j]);
-    }
-    return true;
-}
-
-}  // namespace
 
 // A varying or face-varying (arrays, indices[, params]) set evaluated with the vertex table's
 // patch handles (osd/cpuPatchTable.cpp:75-114).
@@ -217,6 +163,14 @@ GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const i
         fail(GB300_ERR_INVALID_ARGUMENT, "GB300StencilTableCreate: bad arguments");
         return nullptr;
     }
+    for (int i = 0; i < numStencils; ++i) {
+        if (sizes[i] < 0 || offsets[i] < 0 || (int64_t)offsets[i] + sizes[i] > nnz) {
+            fail(GB300_ERR_INVALID_ARGUMENT,
+                 "GB300StencilTableCreate: stencil %d's entries [%d, %d + %d) outside [0, %lld)",
+                 i, offsets[i], offsets[i], sizes[i], (long long)nnz);
+            return nullptr;
+        }
+    }
     cudaStream_t s = as_stream(stream);
     GB300StencilTable *t = new (std::nothrow) GB300StencilTable;
     if (!t) {
@@ -250,26 +204,12 @@ GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const i
             return nullptr;
         }
     }
-    std::vector<int> order, esz, eoff, eidx;
-    std::vector<std::vector<float>> ew;
-    if (!sortedIdx.empty() &&
-        evaluation_order(numStencils, nnz, sizes, offsets, indices, wsrc, order, esz, eoff, eidx,
-                         ew)) {
-        const void *eh[9] = {esz.data(), eoff.data(), eidx.data(), nullptr, nullptr,
-                             nullptr, nullptr, nullptr, nullptr};
-        for (int k = 0; k < 6; ++k)
-            if (wsrc[k]) eh[3 + k] = ew[k].data();
-        for (int k = 0; k < 9; ++k) {
-            if (!upload(&t->ebuf[k], eh[k], bytes[k], s, "GB300StencilTableCreate")) {
-                delete t;
-                return nullptr;
-            }
-        }
-        if (!upload(&t->outRow, order.data(), (size_t)numStencils * 4, s,
-                    "GB300StencilTableCreate")) {
-            delete t;
-            return nullptr;
-        }
+    const int r = gb300::build_sell(numStencils, (const int *)t->buf[0], (const int *)t->buf[1],
+                                    (const int *)t->buf[2], (const float *const *)(t->buf + 3), s,
+                                    t->sell, t->sbuf, "GB300StencilTableCreate");
+    if (r != GB300_OK && r != GB300_ERR_UNSUPPORTED) {
+        delete t;
+        return nullptr;
     }
     if (check_cuda(cudaStreamSynchronize(s), "GB300StencilTableCreate") != GB300_OK) {
         delete t;
@@ -298,22 +238,23 @@ int stencil_table_num_control(const GB300StencilTable *t) { return t ? t->numCon
 }  // namespace batch
 
 GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
-                                       void *const buf[9]) {
-    return adopt_stencil_table(numStencils, nnz, numControl, buf, nullptr, nullptr);
-}
-
-GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
-                                       void *const buf[9], void *const ebuf[9], void *outRow) {
+                                       void *const buf[9], cudaStream_t s, const char *who) {
     GB300StencilTable *t = new (std::nothrow) GB300StencilTable;
-    if (!t) return nullptr;
+    if (!t) {
+        fail(GB300_ERR_OUT_OF_MEMORY, "%s: host allocation", who);
+        return nullptr;
+    }
     t->numStencils = numStencils;
     t->nnz = nnz;
     t->numControl = numControl;
-    for (int k = 0; k < 9; ++k) {
-        t->buf[k] = buf[k];
-        t->ebuf[k] = ebuf ? ebuf[k] : nullptr;
+    const int r = build_sell(numStencils, (const int *)buf[0], (const int *)buf[1],
+                             (const int *)buf[2], (const float *const *)buf + 3, s, t->sell,
+                             t->sbuf, who);
+    if (r != GB300_OK && r != GB300_ERR_UNSUPPORTED) {
+        delete t;  // buffers not yet owned
+        return nullptr;
     }
-    t->outRow = outRow;
+    for (int k = 0; k < 9; ++k) t->buf[k] = buf[k];
     return t;
 }
 }  // namespace gb300
@@ -387,14 +328,11 @@ int table_eval(const GB300StencilTable *t, const float *src, float *const *dIn, 
                         "weights",
                         k);
     }
-    if (t->outRow) {
-        const float *ew[6];
-        for (int k = 0; k < 6; ++k) ew[k] = (const float *)t->ebuf[3 + k];
-        const int r = eval_stencils(src, d, st, ew, length, srcStride, (const int *)t->ebuf[0],
-                                    (const int *)t->ebuf[1], (const int *)t->ebuf[2], 0,
-                                    t->numStencils, s, "GB300StencilTableEval",
-                                    (const int *)t->outRow);
-        if (r != GB300_ERR_UNSUPPORTED) return r;
+    if (t->sell.numSlices > 0 && t->sell.idx) {
+        const float *sw[6];
+        for (int k = 0; k < 6; ++k) sw[k] = d[k] ? t->sell.w[k] : nullptr;
+        return eval_stencils_sell(t->sell, src, d, st, sw, length, srcStride, s,
+                                  "GB300StencilTableEval");
     }
     return eval_stencils(src, d, st, w, length, srcStride, (const int *)t->buf[0],
                          (const int *)t->buf[1], (const int *)t->buf[2], 0, t->numStencils, s,

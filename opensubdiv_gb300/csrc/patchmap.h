@@ -31,7 +31,7 @@ int find_patches(const PatchMapDevice &m, int n, const int *faces, const float *
 int eval_stencils(const float *src, float *const *dst, const int *strides,
                   const float *const *w, int length, int srcStride, const int *sizes,
                   const int *offsets, const int *indices, int start, int end, cudaStream_t s,
-                  const char *who, const int *outRow = nullptr);
+                  const char *who);
 
 // quadFamily: every patch array holds only REGULAR / GREGORY_BASIS / QUADS patches, which
 // selects the element-lane kernel (known for device tables; raw-pointer calls pass 0).

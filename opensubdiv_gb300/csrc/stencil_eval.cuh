@@ -1,6 +1,6 @@
 // Per-stencil evaluation shared by the staged EvalStencils kernel (stencils_tma.cu) and the
 // batched kernel (stencils_batch.cu).  `A` is the launch's argument view: it provides src,
-// srcStride, length, indices, w[k], dst[k], dstStride[k], outOf[k], vecDst[k] and outRow.
+// srcStride, length, indices, w[k], dst[k], dstStride[k], outOf[k] and vecDst[k].
 #pragma once
 
 #include "common.cuh"
@@ -112,8 +112,7 @@ __device__ __forceinline__ void eval_one(const A &a, int i, int n, const int *li
         }
 #pragma unroll
         for (int k = 0; k < NW; ++k) {
-            const int row = a.outRow ? __ldg(a.outRow + i) : i;
-            float *d = a.dst[a.outOf[k]] + (size_t)row * a.dstStride[a.outOf[k]] + c0;
+            float *d = a.dst[a.outOf[k]] + (size_t)i * a.dstStride[a.outOf[k]] + c0;
             const int rem = a.length - c0;
             if (a.vecDst[a.outOf[k]] == 8 && rem >= 8) {
                 asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
@@ -178,9 +177,8 @@ __device__ __forceinline__ void eval_one12(const A &a, int i, int n, const int *
             }
         }
     }
-    const int row = a.outRow ? __ldg(a.outRow + i) : i;
     const int k = a.outOf[0];
-    float *d = a.dst[k] + (size_t)row * a.dstStride[k];
+    float *d = a.dst[k] + (size_t)i * a.dstStride[k];
     if (a.vecDst[k]) {
 #pragma unroll
         for (int v = 0; v < 3; ++v) {

@@ -24,7 +24,6 @@
 #include "common.cuh"
 #include "tables.h"
 
-#include <cub/device/device_radix_sort.cuh>
 #include <cub/device/device_scan.cuh>
 
 #include <algorithm>
@@ -456,58 +455,6 @@ __global__ void k_out_copy(Assemble a, int n, const long long *off, int *outSize
     if (lane == 0 && mx >= 0) atomicMax(maxIdx, mx);
 }
 
-// Evaluation order of a finished table (the layout GB300StencilTableCreate keeps for tables
-// whose consecutive stencils jump across the control points): per stencil its lowest index
-// (entries sorted: the first; -1 when empty) and the sum / max of the jumps between
-// consecutive stencils' keys (empty stencils count as 0 there).
-__global__ void k_order_keys(const int *sizes, const int *offsets, const int *idx, int n,
-                             int *keys, int *iota, unsigned long long *jump, int *maxKey) {
-    unsigned long long j = 0;
-    int mx = 0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const int k = sizes[i] > 0 ? idx[offsets[i]] : -1;
-        keys[i] = k;
-        iota[i] = i;
-        const int a = max(k, 0);
-        mx = max(mx, a);
-        if (i > 0) {
-            const int b = sizes[i - 1] > 0 ? idx[offsets[i - 1]] : 0;
-            j += (unsigned long long)(a > b ? a - b : b - a);
-        }
-    }
-    for (int d = 16; d; d >>= 1) {
-        j += __shfl_xor_sync(kFull, j, d);
-        mx = max(mx, __shfl_xor_sync(kFull, mx, d));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(jump, j);
-        atomicMax(maxKey, mx);
-    }
-}
-
-__global__ void k_order_sizes(const int *sizes, const int *order, int n, int *esz) {
-    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
-        esz[j] = sizes[order[j]];
-}
-
-// warp per evaluation row j: copies stencil order[j] to eoff[j]
-__global__ void k_order_copy(const int *sizes, const int *offsets, const int *idx,
-                             const float *w0, const float *w1, const float *w2, const float *w3,
-                             const float *w4, const float *w5, int nc, const int *order,
-                             const int *eoff, int n, int *eidx, float *e0, float *e1, float *e2,
-                             float *e3, float *e4, float *e5) {
-    const int lane = threadIdx.x & 31, warps = blockDim.x >> 5;
-    const float *w[6] = {w0, w1, w2, w3, w4, w5};
-    float *e[6] = {e0, e1, e2, e3, e4, e5};
-    for (int j = blockIdx.x * warps + (threadIdx.x >> 5); j < n; j += gridDim.x * warps) {
-        const int i = order[j], sz = sizes[i], o = offsets[i], d = eoff[j];
-        for (int k = lane; k < sz; k += 32) {
-            eidx[d + k] = idx[o + k];
-            for (int c = 0; c < nc; ++c) e[c][d + k] = w[c][o + k];
-        }
-    }
-}
-
 // ---- host side --------------------------------------------------------------------------
 
 int grid_for(long long items, int perBlock) {
@@ -714,71 +661,6 @@ bool run_pass(Pass<NC> p, Arena<NC> &arena, long long *sizesTmp, long long *scan
     return true;
 }
 
-// Builds the evaluation layout of a finished table with sorted entries (ebuf / outRow) when its
-// consecutive stencils' lowest indices jump by more than 1% of the index range on average --
-// the criterion and the stable order GB300StencilTableCreate uses.  Leaves ebuf / outRow null
-// when the table does not qualify.  False (status recorded) on failure.
-bool evaluation_order(void *const buf[9], int n, long long nnz, int nc, Scratch &sc,
-                      void *ebuf[9], void **outRow, const char *who) {
-    cudaStream_t s = sc.s;
-    int *keys = sc.alloc<int>((size_t)n, who), *keys2 = sc.alloc<int>((size_t)n, who);
-    int *iota = sc.alloc<int>((size_t)n, who);
-    unsigned long long *jump = sc.alloc<unsigned long long>(1, who);
-    int *maxKey = sc.alloc<int>(1, who);
-    if (!keys || !keys2 || !iota || !jump || !maxKey) return false;
-    if (check_cuda(cudaMemsetAsync(jump, 0, 8, s), who) != GB300_OK ||
-        check_cuda(cudaMemsetAsync(maxKey, 0, 4, s), who) != GB300_OK)
-        return false;
-    k_order_keys<<<grid_for(n, 256), 256, 0, s>>>((const int *)buf[0], (const int *)buf[1],
-                                                  (const int *)buf[2], n, keys, iota, jump,
-                                                  maxKey);
-    count_launch();
-    unsigned long long j = 0;
-    int mk = 0;
-    if (check_launch(who) != GB300_OK || !d2h(&j, jump, 1, s, who) || !d2h(&mk, maxKey, 1, s, who))
-        return false;
-    if ((double)j / (n - 1) < 0.01 * std::max(1, mk)) return true;  // already local
-    void *order = nullptr;
-    if (check_cuda(cudaMalloc(&order, ((size_t)n * 4 + 15) & ~size_t(15)), who) != GB300_OK)
-        return false;
-    *outRow = order;
-    size_t bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, bytes, keys, keys2, iota, (int *)order, n, 0, 32, s);
-    void *tmp = sc.alloc<char>(bytes, who);
-    if (!tmp ||
-        check_cuda(cub::DeviceRadixSort::SortPairs(tmp, bytes, keys, keys2, iota, (int *)order,
-                                                   n, 0, 32, s),
-                   who) != GB300_OK)
-        return false;
-    count_launch();
-    const size_t eb[9] = {(size_t)n * 4, (size_t)n * 4, (size_t)nnz * 4};
-    for (int k = 0; k < 3 + nc; ++k) {
-        const size_t b = k < 3 ? eb[k] : (size_t)nnz * 4;
-        if (check_cuda(cudaMalloc(&ebuf[k], (std::max<size_t>(b, 4) + 15) & ~size_t(15)), who) !=
-            GB300_OK)
-            return false;
-    }
-    k_order_sizes<<<grid_for(n, 256), 256, 0, s>>>((const int *)buf[0], (const int *)order, n,
-                                                   (int *)ebuf[0]);
-    count_launch();
-    bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, bytes, (int *)ebuf[0], (int *)ebuf[1], n, s);
-    void *tmp2 = sc.alloc<char>(bytes, who);
-    if (!tmp2 || check_cuda(cub::DeviceScan::ExclusiveSum(tmp2, bytes, (int *)ebuf[0],
-                                                          (int *)ebuf[1], n, s),
-                            who) != GB300_OK)
-        return false;
-    count_launch();
-    k_order_copy<<<grid_for(n, 8), 256, 0, s>>>(
-        (const int *)buf[0], (const int *)buf[1], (const int *)buf[2], (const float *)buf[3],
-        (const float *)buf[4], (const float *)buf[5], (const float *)buf[6],
-        (const float *)buf[7], (const float *)buf[8], nc, (const int *)order,
-        (const int *)ebuf[1], n, (int *)ebuf[2], (float *)ebuf[3], (float *)ebuf[4],
-        (float *)ebuf[5], (float *)ebuf[6], (float *)ebuf[7], (float *)ebuf[8]);
-    count_launch();
-    return check_launch(who) == GB300_OK;
-}
-
 // Copies the assembled rows into a new table object.
 GB300StencilTable *assemble(Assemble a, int n, Scratch &sc, void *cubTmp, size_t cubBytes,
                             const char *who) {
@@ -833,24 +715,8 @@ GB300StencilTable *assemble(Assemble a, int n, Scratch &sc, void *cubTmp, size_t
         cleanup();
         return nullptr;
     }
-    void *ebuf[9] = {nullptr};
-    void *outRow = nullptr;
-    auto cleanupAll = [&]() {
-        cleanup();
-        for (void *&b : ebuf)
-            if (b) cudaFree(b), b = nullptr;
-        if (outRow) cudaFree(outRow), outRow = nullptr;
-    };
-    if (a.sort && n >= 4096 &&
-        !evaluation_order(buf, n, nnz, a.nc, sc, ebuf, &outRow, who)) {
-        cleanupAll();
-        return nullptr;
-    }
-    GB300StencilTable *t = adopt_stencil_table(n, nnz, mx + 1, buf, ebuf, outRow);
-    if (!t) {
-        cleanupAll();
-        fail(GB300_ERR_OUT_OF_MEMORY, "%s: host allocation", who);
-    }
+    GB300StencilTable *t = adopt_stencil_table(n, nnz, mx + 1, buf, s, who);
+    if (!t) cleanup();
     return t;
 }
 

@@ -17,7 +17,7 @@ namespace gb300 {
 int eval_stencils_staged(const float *src, float *const *dst, const int *strides,
                          const float *const *w, int length, int srcStride, const int *sizes,
                          const int *offsets, const int *indices, int start, int end,
-                         cudaStream_t s, const int *outRow);
+                         cudaStream_t s);
 
 struct StencilArgs {
     const float *src;
@@ -111,13 +111,11 @@ static int group_width(int length) {
     return g;
 }
 
-// Validates and launches.  outputs/strides/weights hold 6 slots (NULL = absent).  With
-// outRow, stencil i writes destination element outRow[i]; only the staged kernel supports
-// that, so GB300_ERR_UNSUPPORTED comes back when it cannot take the request.
+// Validates and launches.  outputs/strides/weights hold 6 slots (NULL = absent).
 int eval_stencils(const float *src, float *const *dst, const int *strides,
                   const float *const *w, int length, int srcStride, const int *sizes,
                   const int *offsets, const int *indices, int start, int end, cudaStream_t s,
-                  const char *who, const int *outRow) {
+                  const char *who) {
     if (end <= start) return ok();
     if (start < 0) return fail(GB300_ERR_INVALID_ARGUMENT, "%s: start < 0", who);
     if (!src || !sizes || !offsets || !indices)
@@ -150,9 +148,9 @@ int eval_stencils(const float *src, float *const *dst, const int *strides,
     if (last < 0) return ok();
     // staged kernel first (16-byte aligned tables); the group kernel covers everything else
     const int staged = eval_stencils_staged(src, a.dst, a.dstStride, a.w, length, srcStride,
-                                            sizes, offsets, indices, start, end, s, outRow);
+                                            sizes, offsets, indices, start, end, s);
     if (staged == GB300_OK) return check_launch(who);
-    if (staged != GB300_ERR_UNSUPPORTED || outRow) return staged;
+    if (staged != GB300_ERR_UNSUPPORTED) return staged;
     const int G = group_width(length);
     if (last == 0)
         launch_group<1>(a, G, s);

@@ -130,11 +130,9 @@ struct JobView {
     const int (&outOf)[1];
     const int (&vecDst)[1];
     const int *const &indices;
-    const int *const &outRow;
     __device__ explicit JobView(const Job &j)
         : src(j.src), srcStride(j.srcStride), length(j.length), vw(j.vw), w(j.w), dst(j.dst),
-          dstStride(j.dstStride), outOf(j.outOf), vecDst(j.vecDst), indices(j.indices),
-          outRow(j.outRow) {}
+          dstStride(j.dstStride), outOf(j.outOf), vecDst(j.vecDst), indices(j.indices) {}
 };
 
 // Consumers' work on one staged tile of a job 9-12 floats wide over 16-byte aligned rows

@@ -21,7 +21,6 @@ struct Job {
     int outOf[1];       // always 0
     int vecDst[1];      // 8: 32-byte aligned rows, 4: 16-byte aligned rows, 0: scalar stores
     const int *indices;
-    const int *outRow;  // always null: stencil i writes row i
     const int *sizes, *offsets;
     int length, srcStride;
     int vw;             // source rows: 8 = 256-bit loads, 4 = 128-bit loads, 1 = scalar

@@ -17,6 +17,7 @@
 // straight from global memory.  Every mbarrier wait is bounded by a %globaltimer deadline; on
 // expiry the CTA records GB300_ERR_DEVICE_TIMEOUT in g_status and leaves.
 #include "common.cuh"
+#include "sell.h"
 #include "stencil_eval.cuh"
 
 namespace gb300 {
@@ -104,7 +105,6 @@ struct Args {
     const int *sizes;
     const int *offsets;
     const int *indices;
-    const int *outRow;  // optional: stencil i writes destination element outRow[i]
     int length, srcStride, start, end, numTiles;
     int vecSrc, vecDst[6];
 };
@@ -268,6 +268,244 @@ static int launch(const Args &a, cudaStream_t s) {
     return GB300_OK;
 }
 
+// ---- sliced layout (sell.h): the same producer / ring / consumer-group scheme ----------------
+// A tile is SPT consecutive slices (one warp each, one stencil per lane); the producer copies
+// the tile's positions (sizes, destination rows) and its contiguous slot range (indices and
+// weights, 128-byte multiples) into a stage; a consumer warp steps through entry j of its 32
+// stencils together, reading index and weights with one conflict-free shared load each.
+template <int NW>
+struct SellCfg {
+    static constexpr int kSlots = NW == 1 ? 4096 : NW <= 3 ? 2048 : 1024;  // slots per stage
+    static constexpr int kSpt = kSlots / 512;  // slices per tile (staged up to width 16)
+    static constexpr size_t kStageBytes = (size_t)kSpt * 32 * 8 + (size_t)kSlots * 4 * (1 + NW);
+    static constexpr int kRing = NW >= 4 ? 4 : kStages;
+    static constexpr size_t kSmem = kRing * kStageBytes + 256;
+};
+
+struct SellArgs {
+    const float *src;
+    int srcStride, length;
+    const int *sz, *sliceSlot, *idx, *outRow;
+    const float *w[6];  // compacted
+    int numSlices, numTiles;
+    float *dst[6];
+    int dstStride[6];
+    int outOf[6];
+    int vecDst[6];
+};
+
+struct SellMeta {
+    int s0, s1, slot0, staged;
+};
+
+// Columns [c0, c0 + 8) of source row `id`, or all 12 columns of a 9-12 wide row (VW = 12:
+// three 16-byte loads; the row stride is a multiple of 4 floats, at least 12).
+template <int VW>
+__device__ __forceinline__ void gather_cols(const SellArgs &a, int id, int c0, uint64_t pol_src,
+                                            float (&x)[VW == 12 ? 12 : 8]) {
+    if constexpr (VW == 12) {
+        const float4 *r = reinterpret_cast<const float4 *>(a.src + (size_t)id * a.srcStride);
+#pragma unroll
+        for (int v = 0; v < 3; ++v) {
+            const float4 q = __ldg(r + v);
+            x[4 * v] = q.x;
+            x[4 * v + 1] = q.y;
+            x[4 * v + 2] = q.z;
+            x[4 * v + 3] = q.w;
+        }
+    } else {
+        gather_row<VW>(a, id, c0, pol_src, x);
+    }
+}
+
+// Elements [c0, c0 + CW) (those below the primvar length) of output `o`'s row `row`:
+// 256-bit or 128-bit streaming stores where the output layout allows, else scalar ones.
+template <int CW>
+__device__ __forceinline__ void store_cols(const SellArgs &a, int o, int row, int c0,
+                                           const float (&acc)[CW]) {
+    float *d = a.dst[o] + (size_t)row * a.dstStride[o] + c0;
+    const int rem = a.length - c0;
+    if (CW == 8 && a.vecDst[o] == 8 && rem >= 8) {
+        asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
+                     "f"(acc[0]), "f"(acc[1]), "f"(acc[2]), "f"(acc[3]), "f"(acc[4]),
+                     "f"(acc[5]), "f"(acc[6]), "f"(acc[7])
+                     : "memory");
+        return;
+    }
+#pragma unroll
+    for (int v = 0; v < CW / 4; ++v) {
+        if (a.vecDst[o] && 4 * v + 4 <= rem) {
+            asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d + 4 * v),
+                         "f"(acc[4 * v]), "f"(acc[4 * v + 1]), "f"(acc[4 * v + 2]),
+                         "f"(acc[4 * v + 3])
+                         : "memory");
+        } else {
+#pragma unroll
+            for (int c = 4 * v; c < 4 * v + 4; ++c)
+                if (c < rem) st_stream(d + c, acc[c]);
+        }
+    }
+}
+
+template <int NW, int VW>
+__global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : 2) k_stencils_sell(const SellArgs a) {
+    extern __shared__ __align__(128) char smem[];
+    using C = SellCfg<NW>;
+    constexpr int S = C::kRing, SPT = C::kSpt;
+    constexpr int G = 8 / SPT;          // consumer groups (one warp per slice of a tile)
+    constexpr int GT = kConsumers / G;  // threads per group
+    constexpr int GW = GT / 32;         // warps per group (= SPT)
+    static_assert(G >= 1 && G <= S && GW == SPT, "consumer groups");
+    __shared__ __align__(8) uint64_t full[S], empty[S];
+    __shared__ SellMeta meta[S];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) {
+        for (int st = 0; st < S; ++st) {
+            mbar_init(&full[st], 32);
+            mbar_init(&empty[st], GW);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const uint64_t pol_stream = l2_evict_first(), pol_src = l2_evict_last();
+    auto stage = [&](int st, int **sz, int **orow, int **idx, float **w) {
+        char *p = smem + (size_t)st * C::kStageBytes;
+        *sz = (int *)p;
+        *orow = *sz + SPT * 32;
+        *idx = *orow + SPT * 32;
+        *w = (float *)(*idx + C::kSlots);
+    };
+    if (warp == kConsumers / 32) {
+        // producer
+        int it = 0;
+        for (int t = blockIdx.x; t < a.numTiles; t += gridDim.x, ++it) {
+            const int st = it % S;
+            const uint32_t use = (uint32_t)(it / S);
+            if (use > 0 && !mbar_wait(&empty[st], (use - 1) & 1)) return;
+            int *ssz, *sor, *sidx;
+            float *sw;
+            stage(st, &ssz, &sor, &sidx, &sw);
+            const int s0 = t * SPT, s1 = min(s0 + SPT, a.numSlices);
+            const int slot0 = __ldg(a.sliceSlot + s0), slot1 = __ldg(a.sliceSlot + s1);
+            const int nslots = slot1 - slot0;
+            const bool staged = nslots <= C::kSlots;
+            if (lane == 0) {
+                meta[st] = SellMeta{s0, s1, slot0, staged ? 1 : 0};
+                const uint32_t pb = (uint32_t)(s1 - s0) * 128;
+                const uint32_t eb = staged ? (uint32_t)nslots * 4 : 0;
+                mbar_arrive_expect_tx(&full[st], 2 * pb + eb * (1 + NW));
+                bulk_g2s(ssz, a.sz + (size_t)s0 * 32, pb, &full[st], pol_stream);
+                bulk_g2s(sor, a.outRow + (size_t)s0 * 32, pb, &full[st], pol_stream);
+                if (eb) {
+                    bulk_g2s(sidx, a.idx + slot0, eb, &full[st], pol_stream);
+#pragma unroll
+                    for (int k = 0; k < NW; ++k)
+                        bulk_g2s(sw + (size_t)k * C::kSlots, a.w[k] + slot0, eb, &full[st],
+                                 pol_stream);
+                }
+            }
+            __syncwarp();
+            if (lane != 0) mbar_arrive(&full[st]);
+        }
+        return;
+    }
+    // consumers: group g takes this CTA's tiles it = g, g + G, ...; warp wg of the group takes
+    // slice wg of the tile
+    const int grp = warp / GW, wg = warp - grp * GW;
+    constexpr int R = NW <= 3 ? 4 : 2;  // entry steps gathered together
+    constexpr int CW = VW == 12 ? 12 : 8;  // columns per pass
+    int it = grp;
+    for (int t = blockIdx.x + grp * gridDim.x; t < a.numTiles; t += G * gridDim.x, it += G) {
+        const int st = it % S;
+        const uint32_t use = (uint32_t)(it / S);
+        if (!mbar_wait(&full[st], use & 1)) return;
+        int *ssz, *sor, *sidx;
+        float *sw;
+        stage(st, &ssz, &sor, &sidx, &sw);
+        const SellMeta m = meta[st];
+        const int slice = m.s0 + wg;
+        if (slice < m.s1) {
+            const int n = ssz[wg * 32 + lane];
+            const int row = sor[wg * 32 + lane];
+            const int b0 = __ldg(a.sliceSlot + slice);
+            const int width = (__ldg(a.sliceSlot + slice + 1) - b0) >> 5;
+            const int base = b0 - m.slot0 + lane;  // this lane's slot of entry 0 in the stage
+            for (int c0 = 0; c0 < a.length; c0 += CW) {
+                float acc[NW][CW];
+#pragma unroll
+                for (int k = 0; k < NW; ++k)
+#pragma unroll
+                    for (int c = 0; c < CW; ++c) acc[k][c] = 0.0f;
+                for (int j0 = 0; j0 < width; j0 += R) {
+                    int ids[R];
+                    float wk[R][NW];
+#pragma unroll
+                    for (int q = 0; q < R; ++q) {
+                        const int j = j0 + q;
+                        if (j < n) {
+                            if (m.staged) {
+                                ids[q] = sidx[base + j * 32];
+#pragma unroll
+                                for (int k = 0; k < NW; ++k)
+                                    wk[q][k] = sw[(size_t)k * C::kSlots + base + j * 32];
+                            } else {
+                                ids[q] = ld_stream(a.idx + b0 + lane + (size_t)j * 32, pol_stream);
+#pragma unroll
+                                for (int k = 0; k < NW; ++k)
+                                    wk[q][k] = ld_stream(a.w[k] + b0 + lane + (size_t)j * 32,
+                                                         pol_stream);
+                            }
+                        }
+                    }
+                    float x[R][CW];
+#pragma unroll
+                    for (int q = 0; q < R; ++q)
+                        if (j0 + q < n) gather_cols<VW>(a, ids[q], c0, pol_src, x[q]);
+#pragma unroll
+                    for (int q = 0; q < R; ++q)
+                        if (j0 + q < n)
+#pragma unroll
+                            for (int k = 0; k < NW; ++k)
+#pragma unroll
+                                for (int c = 0; c < CW; ++c)
+                                    acc[k][c] = fmaf(wk[q][k], x[q][c], acc[k][c]);
+                }
+                if (row >= 0) {
+#pragma unroll
+                    for (int k = 0; k < NW; ++k) store_cols(a, a.outOf[k], row, c0, acc[k]);
+                }
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+    }
+}
+
+template <int NW, int VW>
+static int launch_sell(const SellArgs &a, cudaStream_t s) {
+    using C = SellCfg<NW>;
+    auto kern = k_stencils_sell<NW, VW>;
+    static std::atomic<uint64_t> attr{0};
+    const int st = once_per_device(attr, [&] {
+        return check_cuda(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)C::kSmem),
+                          "stencils (sliced): smem attribute");
+    });
+    if (st != GB300_OK) return st;
+    static int perSm = 0;
+    if (perSm == 0) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, kern, kThreads, C::kSmem) !=
+                cudaSuccess || perSm < 1)
+            perSm = 1;
+    }
+    SellArgs b = a;
+    b.numTiles = (a.numSlices + C::kSpt - 1) / C::kSpt;
+    const int grid = min(b.numTiles, num_sms() * perSm);
+    kern<<<grid, kThreads, C::kSmem, s>>>(b);
+    count_launch();
+    return GB300_OK;
+}
+
 }  // namespace tma
 
 // Staged path; returns GB300_ERR_UNSUPPORTED when the arguments do not meet its alignment
@@ -275,12 +513,11 @@ static int launch(const Args &a, cudaStream_t s) {
 int eval_stencils_staged(const float *src, float *const *dst, const int *strides,
                          const float *const *w, int length, int srcStride, const int *sizes,
                          const int *offsets, const int *indices, int start, int end,
-                         cudaStream_t s, const int *outRow) {
+                         cudaStream_t s) {
     auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
     auto al32 = [](const void *p) { return ((uintptr_t)p & 31) == 0; };
     if (!al16(sizes) || !al16(offsets) || !al16(indices)) return GB300_ERR_UNSUPPORTED;
     tma::Args a{};
-    a.outRow = outRow;
     a.src = src;
     a.sizes = sizes;
     a.offsets = offsets;
@@ -326,6 +563,60 @@ int eval_stencils_staged(const float *src, float *const *dst, const int *strides
         case 61: return tma::launch<6, 1>(a, s);
         default: return GB300_ERR_UNSUPPORTED;
     }
+}
+
+int eval_stencils_sell(const SellTable &t, const float *src, float *const *dst,
+                       const int *strides, const float *const *w, int length, int srcStride,
+                       cudaStream_t s, const char *who) {
+    if (t.numSlices == 0) return ok();
+    if (!src || length <= 0 || srcStride < length)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad source", who);
+    auto al16 = [](const void *p) { return ((uintptr_t)p & 15) == 0; };
+    auto al32 = [](const void *p) { return ((uintptr_t)p & 31) == 0; };
+    tma::SellArgs a{};
+    a.src = src;
+    a.srcStride = srcStride;
+    a.length = length;
+    a.sz = t.sz;
+    a.sliceSlot = t.sliceSlot;
+    a.idx = t.idx;
+    a.outRow = t.outRow;
+    a.numSlices = t.numSlices;
+    int nw = 0;
+    for (int k = 0; k < 6; ++k) {
+        if (!dst[k]) continue;
+        if (!w[k] || strides[k] < length)
+            return fail(GB300_ERR_INVALID_ARGUMENT, "%s: output %d stride / weights", who, k);
+        a.dst[k] = dst[k];
+        a.dstStride[k] = strides[k];
+        a.vecDst[k] = (al32(dst[k]) && strides[k] % 8 == 0) ? 8
+                      : (al16(dst[k]) && strides[k] % 4 == 0) ? 4 : 0;
+        a.w[nw] = w[k];
+        a.outOf[nw] = k;
+        ++nw;
+    }
+    if (nw == 0) return ok();
+    const int vw = (al32(src) && srcStride % 8 == 0) ? 8 : (al16(src) && srcStride % 4 == 0) ? 4 : 1;
+    int r;
+    if (nw == 1 && vw >= 4 && length > 8 && length <= 12) {
+        r = tma::launch_sell<1, 12>(a, s);
+    } else {
+        switch (nw * 10 + vw) {
+#define GB300_SELL_CASES(NW)                                   \
+    case NW * 10 + 8: r = tma::launch_sell<NW, 8>(a, s); break; \
+    case NW * 10 + 4: r = tma::launch_sell<NW, 4>(a, s); break; \
+    case NW * 10 + 1: r = tma::launch_sell<NW, 1>(a, s); break;
+            GB300_SELL_CASES(1)
+            GB300_SELL_CASES(2)
+            GB300_SELL_CASES(3)
+            GB300_SELL_CASES(4)
+            GB300_SELL_CASES(5)
+            GB300_SELL_CASES(6)
+#undef GB300_SELL_CASES
+            default: return fail(GB300_ERR_INVALID_ARGUMENT, "%s: %d outputs", who, nw);
+        }
+    }
+    return r != GB300_OK ? r : check_launch(who);
 }
 
 }  // namespace gb300

@@ -3,19 +3,18 @@
 
 #include <cstdint>
 
+#include <cuda_runtime.h>
+
 struct GB300StencilTable;
 
 namespace gb300 {
 
 // Wraps device buffers (sizes, offsets, indices, w, du, dv, duu, duv, dvv; unused = null, all
-// allocated with cudaMalloc) in a table object that owns them.  numControl = largest control
-// index + 1.  Returns null (buffers untouched) when out of host memory.
+// allocated with cudaMalloc) in a table object that owns them, and builds its sliced
+// evaluation layout on stream `s`.  numControl = largest control index + 1.  Returns null
+// (buffers untouched, status recorded) when out of host memory or when the layout build
+// fails.
 GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
-                                       void *const buf[9]);
-
-// Also hands over an evaluation layout (the same stencils sorted by lowest control index:
-// sizes, offsets, indices, weights..., as buf) and its outRow map (either may be null).
-GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
-                                       void *const buf[9], void *const ebuf[9], void *outRow);
+                                       void *const buf[9], cudaStream_t s, const char *who);
 
 }  // namespace gb300
