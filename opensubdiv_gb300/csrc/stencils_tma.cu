@@ -275,7 +275,7 @@ static int launch(const Args &a, cudaStream_t s) {
 // stencils together, reading index and weights with one conflict-free shared load each.
 template <int NW>
 struct SellCfg {
-    static constexpr int kSlots = NW == 1 ? 4096 : NW <= 3 ? 2048 : 1024;  // slots per stage
+    static constexpr int kSlots = NW <= 3 ? 2048 : 1024;  // slots per stage
     static constexpr int kSpt = kSlots / 512;  // slices per tile (staged up to width 16)
     static constexpr size_t kStageBytes = (size_t)kSpt * 32 * 8 + (size_t)kSlots * 4 * (1 + NW);
     static constexpr int kRing = NW >= 4 ? 4 : kStages;
@@ -347,8 +347,12 @@ __device__ __forceinline__ void store_cols(const SellArgs &a, int o, int row, in
     }
 }
 
+// Three CTAs per SM for one output over vector rows (72 registers, 53 KB of ring each: the
+// gathers are latency-bound and the smaller carve-out leaves more L1 for source rows;
+// 0.267 -> 0.238 ms on the refine pass), two otherwise (more would spill), one for 6 outputs.
 template <int NW, int VW>
-__global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : 2) k_stencils_sell(const SellArgs a) {
+__global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : (NW == 1 && (VW == 8 || VW == 4)) ? 3 : 2)
+    k_stencils_sell(const SellArgs a) {
     extern __shared__ __align__(128) char smem[];
     using C = SellCfg<NW>;
     constexpr int S = C::kRing, SPT = C::kSpt;
