@@ -17,12 +17,13 @@ using namespace gb300;
 
 namespace {
 
-// Allocates `bytes` (rounded up to 16 so bulk copies of the tail stay in bounds) and copies
-// `host` into it; returns false (with the status recorded) on failure.
+// Allocates `bytes` (rounded up to 16 so bulk copies of the tail stay in bounds; 16 zero bytes
+// for an empty array, so a present array is never null) and copies `host` into it; returns
+// false (with the status recorded) on failure.  A null `host` leaves *dptr null.
 bool upload(void **dptr, const void *host, size_t bytes, cudaStream_t s, const char *what) {
     *dptr = nullptr;
-    if (!host || bytes == 0) return true;
-    size_t padded = (bytes + 15) & ~(size_t)15;
+    if (!host) return true;
+    size_t padded = std::max<size_t>(16, (bytes + 15) & ~(size_t)15);
     if (check_cuda(cudaMalloc(dptr, padded), what) != GB300_OK) {
         *dptr = nullptr;
         return false;
@@ -30,8 +31,8 @@ bool upload(void **dptr, const void *host, size_t bytes, cudaStream_t s, const c
     if (padded != bytes &&
         check_cuda(cudaMemsetAsync((char *)*dptr + bytes, 0, padded - bytes, s), what) != GB300_OK)
         return false;
-    if (check_cuda(cudaMemcpyAsync(*dptr, host, bytes, cudaMemcpyHostToDevice, s), what) !=
-        GB300_OK)
+    if (bytes && check_cuda(cudaMemcpyAsync(*dptr, host, bytes, cudaMemcpyHostToDevice, s),
+                            what) != GB300_OK)
         return false;
     return true;
 }
@@ -187,7 +188,8 @@ GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const i
     const float *wsrc[6] = {weights, duWeights, dvWeights, duuWeights, duvWeights, dvvWeights};
     std::vector<int> sortedIdx;
     std::vector<std::vector<float>> sortedW;
-    if (sort_entries(numStencils, nnz, sizes, offsets, indices, wsrc, sortedIdx, sortedW)) {
+    if (nnz > 0 && sort_entries(numStencils, nnz, sizes, offsets, indices, wsrc, sortedIdx,
+                                sortedW)) {
         indices = sortedIdx.data();
         for (int k = 0; k < 6; ++k)
             if (wsrc[k]) wsrc[k] = sortedW[k].data();
