@@ -119,12 +119,17 @@ typedef struct GB300StencilTable GB300StencilTable;
 
 /* Copies a stencil table from HOST arrays (Far::StencilTable::GetSizes/GetOffsets/
  * GetControlIndices/GetWeights and, for limit tables, GetDu..DvvWeights; pass NULL for absent
- * derivative arrays) into device memory.  nnz = number of control indices.  On failure
- * returns NULL and frees anything partially allocated.
+ * derivative arrays) into device memory.  nnz = number of control indices.  Every stencil's
+ * entries [offsets[i], offsets[i] + sizes[i]) must lie inside [0, nnz)
+ * (GB300_ERR_INVALID_ARGUMENT otherwise).  On failure returns NULL and frees anything
+ * partially allocated.
  * Device layout: when the stencils' entry ranges are disjoint (as Far builds them), the
  * entries of each stencil are stored in ascending control-index order with their weights
  * permuted alongside -- the same stencils, reordered so that neighbouring stencils gather the
- * same source rows together.  The Get*Buffer arrays hold that layout. */
+ * same source rows together.  The Get*Buffer arrays hold that layout.  The table also keeps a
+ * second, evaluation-only copy built on the device (32-stencil slices stored entry-major, in
+ * locality order), which GB300StencilTableEval reads; it takes about as much device memory
+ * as the Get*Buffer arrays. */
 GB300StencilTable *GB300StencilTableCreate(int numStencils, int64_t nnz, const int *sizes,
                                            const int *offsets, const int *indices,
                                            const float *weights, const float *duWeights,
