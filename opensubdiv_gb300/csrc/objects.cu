@@ -239,6 +239,8 @@ namespace batch {
 int stencil_table_num_control(const GB300StencilTable *t) { return t ? t->numControl : 0; }
 }  // namespace batch
 
+const SellTable *stencil_table_sell(const GB300StencilTable *t) { return t ? &t->sell : nullptr; }
+
 GB300StencilTable *adopt_stencil_table(int numStencils, int64_t nnz, int numControl,
                                        void *const buf[9], cudaStream_t s, const char *who) {
     GB300StencilTable *t = new (std::nothrow) GB300StencilTable;

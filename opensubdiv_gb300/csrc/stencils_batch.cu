@@ -15,8 +15,10 @@
 // the batch's histogram of work.  The counter reset is a memset on the launch stream, so the
 // pair is graph-capturable (GB300StencilBatchEvalGraph).
 #include "common.cuh"
+#include "sell.h"
 #include "stencil_eval.cuh"
 #include "stencils_batch.h"
+#include "tables.h"
 
 #include <algorithm>
 #include <cmath>
@@ -150,6 +152,92 @@ __device__ __forceinline__ void tile_threads12(const Job &j, const Meta &m, cons
     }
 }
 
+// One slice of a sliced job by one warp (lane = stencil): entry j of the 32 stencils at a time,
+// index and weight from the stage (slot base `slot0`) or, for a slice wider than the stage,
+// from global memory; WIDE: the single 12-wide pass over 16-byte aligned rows.
+template <bool WIDE>
+__device__ __forceinline__ void slice_warp(const Job &j, const Meta &m, int wl, const int *sidx,
+                                           const float *sw, const int *ssz, const int *srow,
+                                           int lane, uint64_t pol_src, uint64_t pol_stream) {
+    constexpr int CW = WIDE ? 12 : 8;  // columns per pass
+    constexpr int R = 4;               // entry steps gathered together
+    const JobView v(j);
+    const int slice = m.s0 + wl;
+    const int n = ssz[wl * 32 + lane], row = srow[wl * 32 + lane];
+    const int b0 = __ldg(j.slSlot + slice);
+    const int width = (__ldg(j.slSlot + slice + 1) - b0) >> 5;
+    const int base = b0 - m.e0a + lane;
+    for (int c0 = 0; c0 < j.length; c0 += CW) {
+        float acc[CW];
+#pragma unroll
+        for (int c = 0; c < CW; ++c) acc[c] = 0.0f;
+        for (int j0 = 0; j0 < width; j0 += R) {
+            int ids[R];
+            float wk[R];
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                const int e = j0 + q;
+                if (e < n) {
+                    if (m.staged) {
+                        ids[q] = sidx[base + e * 32];
+                        wk[q] = sw[base + e * 32];
+                    } else {
+                        ids[q] = ld_stream(j.slIdx + b0 + lane + (size_t)e * 32, pol_stream);
+                        wk[q] = ld_stream(j.slW + b0 + lane + (size_t)e * 32, pol_stream);
+                    }
+                }
+            }
+            float x[R][CW];
+#pragma unroll
+            for (int q = 0; q < R; ++q) {
+                if (j0 + q >= n) continue;
+                if constexpr (WIDE) {
+                    const float4 *r =
+                        reinterpret_cast<const float4 *>(v.src + (size_t)ids[q] * v.srcStride);
+#pragma unroll
+                    for (int u = 0; u < 3; ++u) {
+                        const float4 f = __ldg(r + u);
+                        x[q][4 * u] = f.x;
+                        x[q][4 * u + 1] = f.y;
+                        x[q][4 * u + 2] = f.z;
+                        x[q][4 * u + 3] = f.w;
+                    }
+                } else {
+                    tma::gather_row<0>(v, ids[q], c0, pol_src, x[q]);
+                }
+            }
+#pragma unroll
+            for (int q = 0; q < R; ++q)
+                if (j0 + q < n)
+#pragma unroll
+                    for (int c = 0; c < CW; ++c) acc[c] = fmaf(wk[q], x[q][c], acc[c]);
+        }
+        if (row < 0) continue;
+        float *d = j.dst[0] + (size_t)row * j.dstStride[0] + c0;
+        const int rem = j.length - c0;
+        if (CW == 8 && j.vecDst[0] == 8 && rem >= 8) {
+            asm volatile("st.global.cs.v8.f32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"l"(d),
+                         "f"(acc[0]), "f"(acc[1]), "f"(acc[2]), "f"(acc[3]), "f"(acc[4]),
+                         "f"(acc[5]), "f"(acc[6]), "f"(acc[7])
+                         : "memory");
+            continue;
+        }
+#pragma unroll
+        for (int u = 0; u < CW / 4; ++u) {
+            if (j.vecDst[0] && 4 * u + 4 <= rem) {
+                asm volatile("st.global.cs.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(d + 4 * u),
+                             "f"(acc[4 * u]), "f"(acc[4 * u + 1]), "f"(acc[4 * u + 2]),
+                             "f"(acc[4 * u + 3])
+                             : "memory");
+            } else {
+#pragma unroll
+                for (int c = 4 * u; c < 4 * u + 4; ++c)
+                    if (c < rem) st_stream(d + c, acc[c]);
+            }
+        }
+    }
+}
+
 // Consumers' work on one staged tile (VW = 0: the job's row width chosen per gather).
 template <int VW>
 __device__ __forceinline__ void tile_threads(const Job &j, const Meta &m, const int *sidx,
@@ -175,8 +263,10 @@ struct Args {
 };
 
 // WIDE: every job of the launch is 9-12 floats wide over 16-byte aligned rows (single 12-wide
-// pass); otherwise any job (one run-time-width path).
-template <bool WIDE>
+// pass); otherwise any job (one run-time-width path).  SLICED: every job of the launch reads
+// its table's sliced layout (mode 2; a separate instantiation: both tile paths in one kernel
+// spill registers).
+template <bool WIDE, bool SLICED>
 __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
     extern __shared__ __align__(128) char smem[];
     __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
@@ -235,6 +325,29 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
             for (int q = lane; q < (int)(sizeof(Job) / 4); q += 32)
                 reinterpret_cast<int *>(&sjob[stage])[q] =
                     __ldg(reinterpret_cast<const int *>(&j) + q);
+            if constexpr (SLICED) {
+                // sliced: the tile's positions (sizes, destination rows: 128 B per slice) and
+                // its contiguous slot range (128-byte multiples) when it fits the stage
+                const int s0 = (t - __ldg(a.tileBase + jc)) * kSliceTile;
+                const int s1 = min(s0 + kSliceTile, j.numSlices);
+                const int slot0 = __ldg(j.slSlot + s0), slot1 = __ldg(j.slSlot + s1);
+                const bool staged = slot1 - slot0 <= kCap;
+                const uint32_t pb = (uint32_t)(s1 - s0) * 128;
+                const uint32_t eb = staged ? (uint32_t)(slot1 - slot0) * 4 : 0;
+                if (lane == 0) {
+                    meta[stage] = Meta{jc, s0, s1, 0, slot0, 0, staged ? 1 : 0, 0};
+                    bar_arrive_tx(&full[stage], 2 * pb + 2 * eb);
+                    bulk(ssz, j.slSz + (size_t)s0 * 32, pb, &full[stage], pol_stream);
+                    bulk(sof, j.slRow + (size_t)s0 * 32, pb, &full[stage], pol_stream);
+                    if (eb) {
+                        bulk(sidx, j.slIdx + slot0, eb, &full[stage], pol_stream);
+                        bulk(sw, j.slW + slot0, eb, &full[stage], pol_stream);
+                    }
+                }
+                __syncwarp();
+                if (lane != 0) bar_arrive(&full[stage]);
+                continue;
+            }
             const int s0 = (t - __ldg(a.tileBase + jc)) * j.tileStencils;
             const int s1 = min(s0 + j.tileStencils, j.numStencils);
             int e0 = 0, e1 = 0;
@@ -292,7 +405,10 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
         float *sw;
         stage_ptr(stage, &sidx, &sw, &ssz, &sof);
         const Job &j = sjob[stage];
-        if (j.mode == 0) {
+        if constexpr (SLICED) {
+            if (m.s0 + warp < m.s1)
+                slice_warp<WIDE>(j, m, warp, sidx, sw, ssz, sof, lane, pol_src, pol_stream);
+        } else if (j.mode == 0) {
             // one code path for every row width (inlined width-specific paths spill registers)
             if constexpr (WIDE)
                 tile_threads12(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
@@ -389,6 +505,15 @@ bool make_job(const GB300StencilTable *t, const float *src, float *dst, int leng
     j.vecDst[0] = (al(dst, 32) && dstStride % 8 == 0) ? 8
                   : (al(dst, 16) && dstStride % 4 == 0) ? 4 : 0;
     j.numStencils = GB300StencilTableGetNumStencils(t);
+    const SellTable *sl = stencil_table_sell(t);
+    if (sl && sl->numSlices > 0 && sl->w[0]) {
+        j.slSz = sl->sz;
+        j.slSlot = sl->sliceSlot;
+        j.slIdx = sl->idx;
+        j.slRow = sl->outRow;
+        j.slW = sl->w[0];
+        j.numSlices = sl->numSlices;
+    }
     const int64_t nnz = GB300StencilTableGetNumIndices(t);
     meanSize = j.numStencils ? (double)nnz / j.numStencils : 0.0;
     return true;
@@ -399,9 +524,15 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
     long long total = 0;
     for (int k = 0; k < n; ++k) {
         Job &j = jobs[k];
+        tileBase[k] = (int)total;
+        if (j.slSz) {
+            j.mode = 2;
+            j.tileStencils = kSliceTile * 32;
+            total += (j.numSlices + kSliceTile - 1) / kSliceTile;
+            continue;
+        }
         j.mode = meanSize[k] > warpThreshold ? 1 : 0;
         j.tileStencils = j.mode == 1 ? 32 : tileStencils;
-        tileBase[k] = (int)total;
         total += (j.numStencils + j.tileStencils - 1) / j.tileStencils;
     }
     tileBase[n] = (int)total;
@@ -411,12 +542,13 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 int set_smem_attribute() {
     static std::atomic<uint64_t> attr{0};  // devices whose function attribute is set
     return once_per_device(attr, [] {
-        int st = check_cuda(cudaFuncSetAttribute(k_stencils_batch<false>,
-                                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)kSmem),
-                            "batch smem attribute");
-        if (st == GB300_OK)
-            st = check_cuda(cudaFuncSetAttribute(k_stencils_batch<true>,
+        void (*const kernels[4])(Args) = {k_stencils_batch<false, false>,
+                                          k_stencils_batch<true, false>,
+                                          k_stencils_batch<false, true>,
+                                          k_stencils_batch<true, true>};
+        int st = GB300_OK;
+        for (int k = 0; k < 4 && st == GB300_OK; ++k)
+            st = check_cuda(cudaFuncSetAttribute(kernels[k],
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)kSmem),
                             "batch smem attribute");
@@ -425,7 +557,8 @@ int set_smem_attribute() {
 }
 
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic, bool wide) {
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic, bool wide,
+                bool sliced) {
     int st = set_smem_attribute();
     if (st != GB300_OK) return st;
     if (numTiles == 0) return ok();
@@ -435,10 +568,17 @@ int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int
     }
     Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus, dynamic};
     const int grid = std::min(numTiles, num_sms() * ctasPerSm);
-    if (wide)
-        k_stencils_batch<true><<<grid, kThreads, kSmem, s>>>(a);
-    else
-        k_stencils_batch<false><<<grid, kThreads, kSmem, s>>>(a);
+    if (sliced) {
+        if (wide)
+            k_stencils_batch<true, true><<<grid, kThreads, kSmem, s>>>(a);
+        else
+            k_stencils_batch<false, true><<<grid, kThreads, kSmem, s>>>(a);
+    } else {
+        if (wide)
+            k_stencils_batch<true, false><<<grid, kThreads, kSmem, s>>>(a);
+        else
+            k_stencils_batch<false, false><<<grid, kThreads, kSmem, s>>>(a);
+    }
     count_launch();
     return check_launch("batched EvalStencils");
 }
@@ -485,6 +625,7 @@ struct GB300StencilBatch {
     std::vector<Job> jobs;
     std::vector<double> mean;  // mean stencil size per job (same order)
     int numWide = 0;           // jobs at the end run by the 12-wide launch
+    bool sliced = false;       // every job reads its table's sliced layout (mode 2)
     Config cfg;
     Job *dJobs = nullptr;      // jobs, then the tile prefixes: general (n - numWide + 1 ints)
     int *dTileBase = nullptr;  // and wide (numWide + 1 ints)
@@ -541,11 +682,11 @@ int launch_batch(GB300StencilBatch *b, cudaStream_t s) {
     if (st != GB300_OK) return st;
     const int ng = (int)b->jobs.size() - b->numWide;
     st = launch_jobs(b->dJobs, b->dTileBase, ng, b->numTiles, b->dCounter, b->dCounter + 1,
-                     b->cfg.ctasPerSm, s, b->cfg.dynamic, false);
+                     b->cfg.ctasPerSm, s, b->cfg.dynamic, false, b->sliced);
     if (st != GB300_OK) return st;
     return launch_jobs(b->dJobs + ng, b->dTileBase + ng + 1, b->numWide, b->numTilesWide,
                        b->dCounter + 2, b->dCounter + 1, b->cfg.ctasPerSm, s, b->cfg.dynamic,
-                       true);
+                       true, b->sliced);
 }
 
 // Jobs whose source rows are unaligned (scalar gathers) and at most 8 floats wide read a
@@ -674,6 +815,11 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
         b->mean.push_back(mean[i]);
         rows.push_back(stencil_table_num_control(tables[i]));
     }
+    // one tile path per launch: the sliced one when every table has its sliced layout
+    b->sliced = true;
+    for (const Job &j : b->jobs) b->sliced = b->sliced && j.slSz;
+    if (!b->sliced)
+        for (Job &j : b->jobs) j.slSz = nullptr;
     if (setup_padding(b, rows, s) != GB300_OK) {
         delete b;
         return nullptr;
@@ -818,6 +964,8 @@ int GB300StencilBatchTune(GB300StencilBatch *b, int iterations, void *stream) {
             for (int th : thresholds)
             for (int dyn = 0; dyn < 2; ++dyn) {
                 if (!anyLarge && th != thresholds[0]) continue;
+                // sliced jobs have fixed tiles and no warp-per-stencil mode
+                if (b->sliced && (ts != tiles[0] || th != thresholds[0])) continue;
                 b->cfg = Config{ts, c, th, dyn};
                 if ((st = upload_plan(b, s)) != GB300_OK) goto done;
                 if ((st = launch_batch(b, s)) != GB300_OK) goto done;  // warm-up
@@ -941,7 +1089,7 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
         return st;
     Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1, 1};
     const int grid = (int)std::min<long long>(tiles, 2LL * sms);
-    k_stencils_batch<false><<<grid, kThreads, kSmem, s>>>(a);
+    k_stencils_batch<false, false><<<grid, kThreads, kSmem, s>>>(a);
     count_launch();
     return check_launch(who);
 }

@@ -24,10 +24,17 @@ struct Job {
     const int *sizes, *offsets;
     int length, srcStride;
     int vw;             // source rows: 8 = 256-bit loads, 4 = 128-bit loads, 1 = scalar
-    int mode;           // 0: one stencil per thread, 1: one stencil per warp
+    int mode;           // 0: one stencil per thread, 1: one stencil per warp, 2: sliced
     int numStencils;
     int tileStencils;   // stencils per tile of this job
+    // the table's sliced layout (sell.h), null when absent: mode 2 tiles are kSliceTile slices
+    // (one per consumer warp, one stencil per lane) read from it
+    const int *slSz, *slSlot, *slIdx, *slRow;
+    const float *slW;
+    int numSlices;
 };
+
+constexpr int kSliceTile = 8;  // slices per tile of a sliced job
 
 // Describes job k = (table, src, dst, length, strides); false (error recorded) on bad input.
 // meanSize receives nnz / numStencils.
@@ -35,7 +42,8 @@ bool make_job(const GB300StencilTable *table, const float *src, float *dst, int 
               int srcStride, int dstStride, Job &job, double &meanSize, const char *who);
 
 // Chooses each job's mode and tile size and writes the tile prefix tileBase[0..n] (tileBase[n]
-// = total tiles).  Jobs keep their order: tiles are handed out in job order.
+// = total tiles).  Jobs with a sliced layout take mode 2.  Jobs keep their order: tiles are
+// handed out in job order.
 int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int warpThreshold,
                int *tileBase);
 
@@ -43,8 +51,10 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 // are claimed from the work counter (reset on `s` first), else CTA b takes tiles b, b + grid,
 // ...  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.  wide: every job is one
 // output 9-12 floats wide over 16-byte aligned rows (the kernel's single 12-wide pass).
+// sliced: every job is mode 2 (plan_tiles of jobs that all carry a sliced layout).
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1, bool wide = false);
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1, bool wide = false,
+                bool sliced = false);
 
 // Padded copy of one source: rows [0, numRows) of `src` (length <= 16 floats, srcStride
 // apart) written to `dst` with a stride of dstStride = 4, 8, 12 or 16 floats (elements >=

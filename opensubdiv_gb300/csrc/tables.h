@@ -9,6 +9,11 @@ struct GB300StencilTable;
 
 namespace gb300 {
 
+struct SellTable;
+
+// The table's sliced evaluation layout (numSlices 0 when it has none).
+const SellTable *stencil_table_sell(const GB300StencilTable *table);
+
 // Wraps device buffers (sizes, offsets, indices, w, du, dv, duu, duv, dvv; unused = null, all
 // allocated with cudaMalloc) in a table object that owns them, and builds its sliced
 // evaluation layout on stream `s`.  numControl = largest control index + 1.  Returns null
