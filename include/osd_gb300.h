@@ -297,10 +297,12 @@ int GB300VertexBufferGetNumVertices(const GB300VertexBuffer *buffer);
  * outlive it, and the source / destination contents may change between evaluations. */
 typedef struct GB300StencilBatch GB300StencilBatch;
 
-/* Builds the job table and the tile prefix on the device (synchronous on `stream`).  Jobs
- * whose source rows are unaligned (no 16-byte vector loads) and at most 8 floats wide get a
- * device buffer for a padded copy of their source (rows of 8 floats), refreshed by every
- * evaluation.  Uses the tuned configuration cached for batches with the same work histogram,
+/* Builds the job table and the tile prefix on the device (synchronous on `stream`).  When
+ * every table has its sliced evaluation layout (tables from GB300StencilTableCreate and the
+ * factories), the batch reads those: tiles of 8 slices, one warp per 32-stencil slice;
+ * otherwise the Far-layout arrays.  Jobs whose source rows are unaligned (no 16-byte vector
+ * loads) and at most 8 floats wide get a device buffer for a padded copy of their source
+ * (rows of 8 floats), refreshed by every evaluation.  Uses the tuned configuration cached for batches with the same work histogram,
  * if any.  Returns NULL on failure (error string set). */
 GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const *tables,
                                            const float *const *src, float *const *dst,
@@ -312,9 +314,10 @@ int GB300StencilBatchEval(GB300StencilBatch *batch, void *stream);
 /* The same, replayed from a CUDA graph captured on the first call (on a private stream) and
  * launched on `stream`.  The graph is dropped and recaptured after GB300StencilBatchTune. */
 int GB300StencilBatchEvalGraph(GB300StencilBatch *batch, void *stream);
-/* Autotuner: times each candidate (stencils per tile, CTAs per SM, mean stencil size above
- * which a job switches to one warp per stencil, tiles claimed from a work counter or assigned
- * round-robin) over `iterations` evaluations on the batch itself, keeps the fastest, and
+/* Autotuner: times each candidate (stencils per tile, CTAs per SM (1-3, capped by what the
+ * kernel keeps resident), mean stencil size above which a job switches to one warp per
+ * stencil, tiles claimed from a work counter or assigned round-robin; sliced batches only try
+ * the CTA counts and the claim order) over `iterations` evaluations on the batch itself, keeps the fastest, and
  * caches it for later batches with the same histogram of work over (stencil size, job size,
  * primvar width) classes.  Writes the outputs as Eval does. */
 int GB300StencilBatchTune(GB300StencilBatch *batch, int iterations, void *stream);

@@ -37,7 +37,18 @@ constexpr int kCap = 4096;        // entries per stage
 constexpr int kMaxTile = 256;     // stencils per tile (upper bound)
 constexpr int kMeta = kMaxTile + 8;
 constexpr size_t kStageBytes = (size_t)kCap * 8 + (size_t)kMeta * 8;
-constexpr size_t kSmem = kStages * kStageBytes + 256;
+
+// Ring depth and CTAs per SM of an instantiation: the sliced kernel for jobs up to 8 floats
+// wide runs a 2-stage ring at three CTAs per SM (72 registers; its gathers are
+// latency-bound, so resident warps matter more than a third stage); the others 3 stages, two
+// CTAs per SM.
+template <bool WIDE, bool SLICED>
+struct Ring {
+    static constexpr bool kThin = SLICED && !WIDE;
+    static constexpr int kDepth = kThin ? 2 : kStages;
+    static constexpr int kMinBlocks = kThin ? 3 : 2;
+    static constexpr size_t kSmem = kDepth * kStageBytes + 256;
+};
 constexpr unsigned long long kWaitNs = 4000000000ull;
 
 struct Meta {
@@ -267,14 +278,16 @@ struct Args {
 // its table's sliced layout (mode 2; a separate instantiation: both tile paths in one kernel
 // spill registers).
 template <bool WIDE, bool SLICED>
-__global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
+__global__ void __launch_bounds__(kThreads, (Ring<WIDE, SLICED>::kMinBlocks))
+    k_stencils_batch(const Args a) {
+    constexpr int S = Ring<WIDE, SLICED>::kDepth;
     extern __shared__ __align__(128) char smem[];
-    __shared__ __align__(8) uint64_t full[kStages], empty[kStages];
-    __shared__ Meta meta[kStages];
-    __shared__ __align__(16) Job sjob[kStages];  // the staged tile's job, read by consumers
+    __shared__ __align__(8) uint64_t full[S], empty[S];
+    __shared__ Meta meta[S];
+    __shared__ __align__(16) Job sjob[S];  // the staged tile's job, read by consumers
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     if (threadIdx.x == 0) {
-        for (int s = 0; s < kStages; ++s) {
+        for (int s = 0; s < S; ++s) {
             bar_init(&full[s], 32);
             bar_init(&empty[s], kConsumers / 32);
         }
@@ -294,8 +307,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
         // producer: claim tiles until the list is exhausted, then post one "done" stage
         int jc = 0;  // job of the last claimed tile (claims only grow)
         for (int it = 0;; ++it) {
-            const int stage = it % kStages;
-            const uint32_t use = (uint32_t)(it / kStages);
+            const int stage = it % S;
+            const uint32_t use = (uint32_t)(it / S);
             if (use > 0 && !bar_wait(&empty[stage], (use - 1) & 1, a.status)) return;
             int t = (int)blockIdx.x + it * (int)gridDim.x;
             if (a.dynamic) {
@@ -396,8 +409,8 @@ __global__ void __launch_bounds__(kThreads, 2) k_stencils_batch(const Args a) {
 
     // consumers
     for (int it = 0;; ++it) {
-        const int stage = it % kStages;
-        const uint32_t use = (uint32_t)(it / kStages);
+        const int stage = it % S;
+        const uint32_t use = (uint32_t)(it / S);
         if (!bar_wait(&full[stage], use & 1, a.status)) return;
         const Meta m = meta[stage];
         if (m.done) return;
@@ -546,11 +559,13 @@ int set_smem_attribute() {
                                           k_stencils_batch<true, false>,
                                           k_stencils_batch<false, true>,
                                           k_stencils_batch<true, true>};
+        const size_t bytes[4] = {Ring<false, false>::kSmem, Ring<true, false>::kSmem,
+                                 Ring<false, true>::kSmem, Ring<true, true>::kSmem};
         int st = GB300_OK;
         for (int k = 0; k < 4 && st == GB300_OK; ++k)
             st = check_cuda(cudaFuncSetAttribute(kernels[k],
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                 (int)kSmem),
+                                                 (int)bytes[k]),
                             "batch smem attribute");
         return st;
     });
@@ -567,17 +582,20 @@ int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int
         if (st != GB300_OK) return st;
     }
     Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus, dynamic};
-    const int grid = std::min(numTiles, num_sms() * ctasPerSm);
+    // at most the CTAs per SM the instantiation can keep resident
+    const int perSm = std::min(ctasPerSm, sliced && !wide ? Ring<false, true>::kMinBlocks
+                                                          : Ring<false, false>::kMinBlocks);
+    const int grid = std::min(numTiles, num_sms() * std::max(1, perSm));
     if (sliced) {
         if (wide)
-            k_stencils_batch<true, true><<<grid, kThreads, kSmem, s>>>(a);
+            k_stencils_batch<true, true><<<grid, kThreads, Ring<true, true>::kSmem, s>>>(a);
         else
-            k_stencils_batch<false, true><<<grid, kThreads, kSmem, s>>>(a);
+            k_stencils_batch<false, true><<<grid, kThreads, Ring<false, true>::kSmem, s>>>(a);
     } else {
         if (wide)
-            k_stencils_batch<true, false><<<grid, kThreads, kSmem, s>>>(a);
+            k_stencils_batch<true, false><<<grid, kThreads, Ring<true, false>::kSmem, s>>>(a);
         else
-            k_stencils_batch<false, false><<<grid, kThreads, kSmem, s>>>(a);
+            k_stencils_batch<false, false><<<grid, kThreads, Ring<false, false>::kSmem, s>>>(a);
     }
     count_launch();
     return check_launch("batched EvalStencils");
@@ -948,7 +966,7 @@ int GB300StencilBatchTune(GB300StencilBatch *b, int iterations, void *stream) {
     if (iterations < 1) iterations = 3;
     b->drop_graph();
     const int tiles[] = {64, 128, 256};
-    const int ctas[] = {1, 2};
+    const int ctas[] = {1, 2, 3};
     const int thresholds[] = {32, 96, 1 << 30};
     // a threshold only matters when some job's mean stencil size lies between candidates
     bool anyLarge = false;
@@ -1089,7 +1107,7 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
         return st;
     Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1, 1};
     const int grid = (int)std::min<long long>(tiles, 2LL * sms);
-    k_stencils_batch<false, false><<<grid, kThreads, kSmem, s>>>(a);
+    k_stencils_batch<false, false><<<grid, kThreads, Ring<false, false>::kSmem, s>>>(a);
     count_launch();
     return check_launch(who);
 }

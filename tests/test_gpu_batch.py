@@ -123,7 +123,7 @@ def test_batch_graph_replay_tune_and_deformation():
             assert torch.equal(d, p), f"frame {frame}"
     batch.Tune(iterations=2)
     cfg = batch.GetConfig()
-    assert cfg["tile_stencils"] in (64, 128, 256) and cfg["ctas_per_sm"] in (1, 2)
+    assert cfg["tile_stencils"] in (64, 128, 256) and cfg["ctas_per_sm"] in (1, 2, 3)
     for d in dsts:
         d.zero_()
     batch.EvalGraph()
