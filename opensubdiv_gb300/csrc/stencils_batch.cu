@@ -38,13 +38,13 @@ constexpr int kMaxTile = 256;     // stencils per tile (upper bound)
 constexpr int kMeta = kMaxTile + 8;
 constexpr size_t kStageBytes = (size_t)kCap * 8 + (size_t)kMeta * 8;
 
-// Ring depth and CTAs per SM of an instantiation: the sliced kernel for jobs up to 8 floats
-// wide runs a 2-stage ring at three CTAs per SM (72 registers; its gathers are
-// latency-bound, so resident warps matter more than a third stage); the others 3 stages, two
-// CTAs per SM.
+// Ring depth and CTAs per SM of an instantiation: the sliced kernels run a 2-stage ring at
+// three CTAs per SM (72 registers; their gathers are latency-bound, so resident warps matter
+// more than a third stage; the 12-wide one gathers 2 rows per step to fit: 3 spilled and ran
+// 5% slower); the Far-layout ones 3 stages, two CTAs per SM.
 template <bool WIDE, bool SLICED>
 struct Ring {
-    static constexpr bool kThin = SLICED && !WIDE;
+    static constexpr bool kThin = SLICED;
     static constexpr int kDepth = kThin ? 2 : kStages;
     static constexpr int kMinBlocks = kThin ? 3 : 2;
     static constexpr size_t kSmem = kDepth * kStageBytes + 256;
@@ -171,7 +171,7 @@ __device__ __forceinline__ void slice_warp(const Job &j, const Meta &m, int wl, 
                                            const float *sw, const int *ssz, const int *srow,
                                            int lane, uint64_t pol_src, uint64_t pol_stream) {
     constexpr int CW = WIDE ? 12 : 8;  // columns per pass
-    constexpr int R = 4;               // entry steps gathered together
+    constexpr int R = WIDE ? 2 : 4;    // entry steps gathered together (72 registers)
     const JobView v(j);
     const int slice = m.s0 + wl;
     const int n = ssz[wl * 32 + lane], row = srow[wl * 32 + lane];
@@ -583,8 +583,8 @@ int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int
     }
     Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus, dynamic};
     // at most the CTAs per SM the instantiation can keep resident
-    const int perSm = std::min(ctasPerSm, sliced && !wide ? Ring<false, true>::kMinBlocks
-                                                          : Ring<false, false>::kMinBlocks);
+    const int perSm = std::min(ctasPerSm, sliced ? Ring<false, true>::kMinBlocks
+                                                 : Ring<false, false>::kMinBlocks);
     const int grid = std::min(numTiles, num_sms() * std::max(1, perSm));
     if (sliced) {
         if (wide)
