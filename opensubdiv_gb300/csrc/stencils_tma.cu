@@ -298,12 +298,23 @@ struct SellMeta {
     int s0, s1, slot0, staged;
 };
 
-// Columns [c0, c0 + 8) of source row `id`, or all 12 columns of a 9-12 wide row (VW = 12:
-// three 16-byte loads; the row stride is a multiple of 4 floats, at least 12).
+// VW of the pass over rows of at most 4 floats at 16-byte aligned rows: one 128-bit load per
+// entry and 4 columns per pass, so more rows fit in registers per entry step.
+constexpr int kNarrow = 44;
+
+// Columns [c0, c0 + 8) of source row `id`, all 12 columns of a 9-12 wide row (VW = 12: three
+// 16-byte loads; the row stride is a multiple of 4 floats, at least 12), or the 4 columns of a
+// row of at most 4 floats (VW = kNarrow: one 16-byte load, stride a multiple of 4).
 template <int VW>
 __device__ __forceinline__ void gather_cols(const SellArgs &a, int id, int c0, uint64_t pol_src,
-                                            float (&x)[VW == 12 ? 12 : 8]) {
-    if constexpr (VW == 12) {
+                                            float (&x)[VW == 12 ? 12 : VW == kNarrow ? 4 : 8]) {
+    if constexpr (VW == kNarrow) {
+        const float4 q = __ldg(reinterpret_cast<const float4 *>(a.src + (size_t)id * a.srcStride));
+        x[0] = q.x;
+        x[1] = q.y;
+        x[2] = q.z;
+        x[3] = q.w;
+    } else if constexpr (VW == 12) {
         const float4 *r = reinterpret_cast<const float4 *>(a.src + (size_t)id * a.srcStride);
 #pragma unroll
         for (int v = 0; v < 3; ++v) {
@@ -347,11 +358,12 @@ __device__ __forceinline__ void store_cols(const SellArgs &a, int o, int row, in
     }
 }
 
-// Three CTAs per SM for one output over vector rows (72 registers, 53 KB of ring each: the
-// gathers are latency-bound and the smaller carve-out leaves more L1 for source rows;
-// 0.267 -> 0.238 ms on the refine pass), two otherwise (more would spill), one for 6 outputs.
+// Three CTAs per SM for one output (72 registers, 53 KB of ring each: the gathers are
+// latency-bound and the smaller carve-out leaves more L1 for source rows; 0.267 -> 0.238 ms on
+// the refine pass, 12-wide rows 0.372 -> 0.356 ms), and for 3 outputs over rows of up to 4
+// floats; two otherwise (more would spill), one for 6 outputs.
 template <int NW, int VW>
-__global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : (NW == 1 && (VW == 8 || VW == 4)) ? 3 : 2)
+__global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : (NW == 1 || VW == kNarrow) ? 3 : 2)
     k_stencils_sell(const SellArgs a) {
     extern __shared__ __align__(128) char smem[];
     using C = SellCfg<NW>;
@@ -416,8 +428,9 @@ __global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : (NW == 1 && (VW == 8 |
     // consumers: group g takes this CTA's tiles it = g, g + G, ...; warp wg of the group takes
     // slice wg of the tile
     const int grp = warp / GW, wg = warp - grp * GW;
-    constexpr int R = NW <= 3 ? 4 : 2;  // entry steps gathered together
-    constexpr int CW = VW == 12 ? 12 : 8;  // columns per pass
+    // entry steps gathered together, columns per pass
+    constexpr int R = VW == kNarrow ? (NW == 1 ? 6 : 4) : VW == 12 ? 2 : NW <= 3 ? 4 : 2;
+    constexpr int CW = VW == 12 ? 12 : VW == kNarrow ? 4 : 8;
     int it = grp;
     for (int t = blockIdx.x + grp * gridDim.x; t < a.numTiles; t += G * gridDim.x, it += G) {
         const int st = it % S;
@@ -604,6 +617,8 @@ int eval_stencils_sell(const SellTable &t, const float *src, float *const *dst,
     int r;
     if (nw == 1 && vw >= 4 && length > 8 && length <= 12) {
         r = tma::launch_sell<1, 12>(a, s);
+    } else if ((nw == 1 || nw == 3) && vw >= 4 && length <= 4) {
+        r = nw == 1 ? tma::launch_sell<1, tma::kNarrow>(a, s) : tma::launch_sell<3, tma::kNarrow>(a, s);
     } else {
         switch (nw * 10 + vw) {
 #define GB300_SELL_CASES(NW)                                   \

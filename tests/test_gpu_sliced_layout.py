@@ -92,7 +92,7 @@ def test_partial_last_slice_and_small_tables(n):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("length", [1, 3, 4, 8, 11, 12, 33])
+@pytest.mark.parametrize("length", [1, 2, 3, 4, 8, 11, 12, 33])
 def test_empty_and_pole_stencils(length):
     """Empty stencils (every 7th and the last) write zeros; valence-360 poles make slices
     wider than a stage, which the kernel reads straight from global memory."""
@@ -135,9 +135,11 @@ def test_scattered_table_every_output_count_and_store_width(nout):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("src_desc", [(0, 8, 8), (4, 8, 12), (0, 10, 12), (2, 6, 9)])
+@pytest.mark.parametrize("src_desc", [(0, 8, 8), (4, 8, 12), (0, 10, 12), (2, 6, 9), (0, 3, 4),
+                                      (4, 4, 8)])
 def test_source_layouts(src_desc):
-    """Source rows gathered with 256-bit, 128-bit, 12-wide and scalar loads."""
+    """Source rows gathered with 256-bit, 128-bit, 12-wide, scalar and 4-column (rows of at
+    most 4 floats) loads."""
     torch = torch_cuda()
     rng = np.random.default_rng(300 + src_desc[2])
     n, ncv = 9000, 2500
