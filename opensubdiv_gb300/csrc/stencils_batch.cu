@@ -42,7 +42,7 @@ constexpr size_t kStageBytes = (size_t)kCap * 8 + (size_t)kMeta * 8;
 // three CTAs per SM (72 registers; their gathers are latency-bound, so resident warps matter
 // more than a third stage; the 12-wide one gathers 2 rows per step to fit: 3 spilled and ran
 // 5% slower); the Far-layout ones 3 stages, two CTAs per SM.
-template <bool WIDE, bool SLICED>
+template <int CLS, bool SLICED>
 struct Ring {
     static constexpr bool kThin = SLICED;
     static constexpr int kDepth = kThin ? 2 : kStages;
@@ -163,15 +163,21 @@ __device__ __forceinline__ void tile_threads12(const Job &j, const Meta &m, cons
     }
 }
 
+// Job classes of a launch: any width (run-time row width, 8 columns per pass), 9-12 floats
+// wide over 16-byte aligned rows (one 12-column pass), at most 4 floats over 16-byte aligned
+// rows (one 4-column pass; sliced batches only).
+constexpr int kAny = 0, kWide = 1, kNarrow = 2;
+
 // One slice of a sliced job by one warp (lane = stencil): entry j of the 32 stencils at a time,
 // index and weight from the stage (slot base `slot0`) or, for a slice wider than the stage,
-// from global memory; WIDE: the single 12-wide pass over 16-byte aligned rows.
-template <bool WIDE>
+// from global memory; columns per pass by job class.
+template <int CLS>
 __device__ __forceinline__ void slice_warp(const Job &j, const Meta &m, int wl, const int *sidx,
                                            const float *sw, const int *ssz, const int *srow,
                                            int lane, uint64_t pol_src, uint64_t pol_stream) {
-    constexpr int CW = WIDE ? 12 : 8;  // columns per pass
-    constexpr int R = WIDE ? 2 : 4;    // entry steps gathered together (72 registers)
+    constexpr bool WIDE = CLS == kWide;
+    constexpr int CW = WIDE ? 12 : CLS == kNarrow ? 4 : 8;  // columns per pass
+    constexpr int R = WIDE ? 2 : CLS == kNarrow ? 6 : 4;    // rows per step (72 registers)
     const JobView v(j);
     const int slice = m.s0 + wl;
     const int n = ssz[wl * 32 + lane], row = srow[wl * 32 + lane];
@@ -202,7 +208,14 @@ __device__ __forceinline__ void slice_warp(const Job &j, const Meta &m, int wl, 
 #pragma unroll
             for (int q = 0; q < R; ++q) {
                 if (j0 + q >= n) continue;
-                if constexpr (WIDE) {
+                if constexpr (CLS == kNarrow) {
+                    const float4 f = __ldg(
+                        reinterpret_cast<const float4 *>(v.src + (size_t)ids[q] * v.srcStride));
+                    x[q][0] = f.x;
+                    x[q][1] = f.y;
+                    x[q][2] = f.z;
+                    x[q][3] = f.w;
+                } else if constexpr (WIDE) {
                     const float4 *r =
                         reinterpret_cast<const float4 *>(v.src + (size_t)ids[q] * v.srcStride);
 #pragma unroll
@@ -273,14 +286,14 @@ struct Args {
     int dynamic;          // 1: tiles claimed from the counter, 0: CTA b takes b, b + grid, ...
 };
 
-// WIDE: every job of the launch is 9-12 floats wide over 16-byte aligned rows (single 12-wide
-// pass); otherwise any job (one run-time-width path).  SLICED: every job of the launch reads
-// its table's sliced layout (mode 2; a separate instantiation: both tile paths in one kernel
-// spill registers).
-template <bool WIDE, bool SLICED>
-__global__ void __launch_bounds__(kThreads, (Ring<WIDE, SLICED>::kMinBlocks))
+// CLS: the class of every job of the launch (kAny, kWide: single 12-wide pass, kNarrow: single
+// 4-column pass, sliced launches only).  SLICED: every job of the launch reads its table's
+// sliced layout (mode 2; a separate instantiation: both tile paths in one kernel spill
+// registers).
+template <int CLS, bool SLICED>
+__global__ void __launch_bounds__(kThreads, (Ring<CLS, SLICED>::kMinBlocks))
     k_stencils_batch(const Args a) {
-    constexpr int S = Ring<WIDE, SLICED>::kDepth;
+    constexpr int S = Ring<CLS, SLICED>::kDepth;
     extern __shared__ __align__(128) char smem[];
     __shared__ __align__(8) uint64_t full[S], empty[S];
     __shared__ Meta meta[S];
@@ -420,10 +433,10 @@ __global__ void __launch_bounds__(kThreads, (Ring<WIDE, SLICED>::kMinBlocks))
         const Job &j = sjob[stage];
         if constexpr (SLICED) {
             if (m.s0 + warp < m.s1)
-                slice_warp<WIDE>(j, m, warp, sidx, sw, ssz, sof, lane, pol_src, pol_stream);
+                slice_warp<CLS>(j, m, warp, sidx, sw, ssz, sof, lane, pol_src, pol_stream);
         } else if (j.mode == 0) {
             // one code path for every row width (inlined width-specific paths spill registers)
-            if constexpr (WIDE)
+            if constexpr (CLS == kWide)
                 tile_threads12(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
             else
                 tile_threads<0>(j, m, sidx, sw, ssz, sof, pol_src, pol_stream);
@@ -555,14 +568,15 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 int set_smem_attribute() {
     static std::atomic<uint64_t> attr{0};  // devices whose function attribute is set
     return once_per_device(attr, [] {
-        void (*const kernels[4])(Args) = {k_stencils_batch<false, false>,
-                                          k_stencils_batch<true, false>,
-                                          k_stencils_batch<false, true>,
-                                          k_stencils_batch<true, true>};
-        const size_t bytes[4] = {Ring<false, false>::kSmem, Ring<true, false>::kSmem,
-                                 Ring<false, true>::kSmem, Ring<true, true>::kSmem};
+        void (*const kernels[5])(Args) = {
+            k_stencils_batch<kAny, false>, k_stencils_batch<kWide, false>,
+            k_stencils_batch<kAny, true>, k_stencils_batch<kWide, true>,
+            k_stencils_batch<kNarrow, true>};
+        const size_t bytes[5] = {Ring<kAny, false>::kSmem, Ring<kWide, false>::kSmem,
+                                 Ring<kAny, true>::kSmem, Ring<kWide, true>::kSmem,
+                                 Ring<kNarrow, true>::kSmem};
         int st = GB300_OK;
-        for (int k = 0; k < 4 && st == GB300_OK; ++k)
+        for (int k = 0; k < 5 && st == GB300_OK; ++k)
             st = check_cuda(cudaFuncSetAttribute(kernels[k],
                                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                  (int)bytes[k]),
@@ -572,30 +586,34 @@ int set_smem_attribute() {
 }
 
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic, bool wide,
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic, int cls,
                 bool sliced) {
     int st = set_smem_attribute();
     if (st != GB300_OK) return st;
     if (numTiles == 0) return ok();
+    if (cls == kNarrow && !sliced)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "batched EvalStencils: narrow class unsliced");
     if (dynamic) {
         st = check_cuda(cudaMemsetAsync(dCounter, 0, sizeof(int), s), "batch counter");
         if (st != GB300_OK) return st;
     }
     Args a{dJobs, dTileBase, n, numTiles, dCounter, dStatus, dynamic};
     // at most the CTAs per SM the instantiation can keep resident
-    const int perSm = std::min(ctasPerSm, sliced ? Ring<false, true>::kMinBlocks
-                                                 : Ring<false, false>::kMinBlocks);
+    const int perSm = std::min(ctasPerSm, sliced ? Ring<kAny, true>::kMinBlocks
+                                                 : Ring<kAny, false>::kMinBlocks);
     const int grid = std::min(numTiles, num_sms() * std::max(1, perSm));
     if (sliced) {
-        if (wide)
-            k_stencils_batch<true, true><<<grid, kThreads, Ring<true, true>::kSmem, s>>>(a);
+        if (cls == kWide)
+            k_stencils_batch<kWide, true><<<grid, kThreads, Ring<kWide, true>::kSmem, s>>>(a);
+        else if (cls == kNarrow)
+            k_stencils_batch<kNarrow, true><<<grid, kThreads, Ring<kNarrow, true>::kSmem, s>>>(a);
         else
-            k_stencils_batch<false, true><<<grid, kThreads, Ring<false, true>::kSmem, s>>>(a);
+            k_stencils_batch<kAny, true><<<grid, kThreads, Ring<kAny, true>::kSmem, s>>>(a);
     } else {
-        if (wide)
-            k_stencils_batch<true, false><<<grid, kThreads, Ring<true, false>::kSmem, s>>>(a);
+        if (cls == kWide)
+            k_stencils_batch<kWide, false><<<grid, kThreads, Ring<kWide, false>::kSmem, s>>>(a);
         else
-            k_stencils_batch<false, false><<<grid, kThreads, Ring<false, false>::kSmem, s>>>(a);
+            k_stencils_batch<kAny, false><<<grid, kThreads, Ring<kAny, false>::kSmem, s>>>(a);
     }
     count_launch();
     return check_launch("batched EvalStencils");
@@ -638,17 +656,20 @@ using namespace gb300;
 using namespace gb300::batch;
 
 struct GB300StencilBatch {
-    // in launch order: the general jobs, then the jobs 9-12 floats wide over 16-byte aligned
-    // rows (the kernel's 12-wide instantiation), each part largest first
+    // in launch order, one launch per part: the general jobs, the jobs at most 4 floats wide
+    // over 16-byte aligned rows (sliced batches: the 4-column instantiation), the jobs 9-12
+    // floats wide over 16-byte aligned rows (the 12-wide instantiation); each part largest
+    // first
     std::vector<Job> jobs;
     std::vector<double> mean;  // mean stencil size per job (same order)
-    int numWide = 0;           // jobs at the end run by the 12-wide launch
+    int part[3] = {0, 0, 0};   // jobs per part
     bool sliced = false;       // every job reads its table's sliced layout (mode 2)
     Config cfg;
-    Job *dJobs = nullptr;      // jobs, then the tile prefixes: general (n - numWide + 1 ints)
-    int *dTileBase = nullptr;  // and wide (numWide + 1 ints)
-    int *dCounter = nullptr;   // [0] work counter, [1] status word, [2] wide work counter
-    int numTiles = 0, numTilesWide = 0;
+    Job *dJobs = nullptr;      // jobs, then the tile prefixes of the parts (part[p] + 1 ints
+    int *dTileBase = nullptr;  // each)
+    int *dCounter = nullptr;   // [1] status word; [0], [2], [3] work counters of the parts
+    int partTiles[3] = {0, 0, 0};
+    int numTiles() const { return partTiles[0] + partTiles[1] + partTiles[2]; }
     uint64_t signature = 0;
     cudaGraphExec_t graph = nullptr;  // pad copy + counter reset + kernel, on first use
     cudaStream_t capture = nullptr;
@@ -677,19 +698,21 @@ namespace {
 std::mutex g_tuneLock;
 std::map<uint64_t, Config> g_tuned;  // work signature -> best config
 
-// Applies b->cfg: job modes, tile sizes and the tile prefix, uploaded to the device.
+constexpr int kPartClass[3] = {kAny, kNarrow, kWide};
+constexpr int kPartCounter[3] = {0, 3, 2};
+
+// Applies b->cfg: job modes, tile sizes and the tile prefixes, uploaded to the device.
 int upload_plan(GB300StencilBatch *b, cudaStream_t s) {
-    const int n = (int)b->jobs.size(), ng = n - b->numWide;
-    std::vector<int> base(n + 2);
-    b->numTiles = plan_tiles(b->jobs.data(), b->mean.data(), ng, b->cfg.tileStencils,
-                             b->cfg.warpThreshold, base.data());
-    b->numTilesWide = plan_tiles(b->jobs.data() + ng, b->mean.data() + ng, b->numWide,
-                                 b->cfg.tileStencils, b->cfg.warpThreshold,
-                                 base.data() + ng + 1);
+    const int n = (int)b->jobs.size();
+    std::vector<int> base(n + 3);
+    for (int p = 0, j0 = 0; p < 3; j0 += b->part[p], ++p)
+        b->partTiles[p] = plan_tiles(b->jobs.data() + j0, b->mean.data() + j0, b->part[p],
+                                     b->cfg.tileStencils, b->cfg.warpThreshold,
+                                     base.data() + j0 + p);
     int st = check_cuda(cudaMemcpyAsync(b->dJobs, b->jobs.data(), n * sizeof(Job),
                                         cudaMemcpyHostToDevice, s), "batch jobs");
     if (st != GB300_OK) return st;
-    st = check_cuda(cudaMemcpyAsync(b->dTileBase, base.data(), (n + 2) * sizeof(int),
+    st = check_cuda(cudaMemcpyAsync(b->dTileBase, base.data(), (n + 3) * sizeof(int),
                                     cudaMemcpyHostToDevice, s), "batch jobs");
     if (st != GB300_OK) return st;
     return check_cuda(cudaStreamSynchronize(s), "batch jobs");
@@ -698,13 +721,13 @@ int upload_plan(GB300StencilBatch *b, cudaStream_t s) {
 int launch_batch(GB300StencilBatch *b, cudaStream_t s) {
     int st = launch_pad(b->dPad, b->dPadBase, b->numPad, b->padRows, s);
     if (st != GB300_OK) return st;
-    const int ng = (int)b->jobs.size() - b->numWide;
-    st = launch_jobs(b->dJobs, b->dTileBase, ng, b->numTiles, b->dCounter, b->dCounter + 1,
-                     b->cfg.ctasPerSm, s, b->cfg.dynamic, false, b->sliced);
-    if (st != GB300_OK) return st;
-    return launch_jobs(b->dJobs + ng, b->dTileBase + ng + 1, b->numWide, b->numTilesWide,
-                       b->dCounter + 2, b->dCounter + 1, b->cfg.ctasPerSm, s, b->cfg.dynamic,
-                       true, b->sliced);
+    for (int p = 0, j0 = 0; p < 3; j0 += b->part[p], ++p) {
+        st = launch_jobs(b->dJobs + j0, b->dTileBase + j0 + p, b->part[p], b->partTiles[p],
+                         b->dCounter + kPartCounter[p], b->dCounter + 1, b->cfg.ctasPerSm, s,
+                         b->cfg.dynamic, kPartClass[p], b->sliced);
+        if (st != GB300_OK) return st;
+    }
+    return GB300_OK;
 }
 
 // Jobs whose source rows are unaligned (scalar gathers) and at most 8 floats wide read a
@@ -842,21 +865,31 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
         delete b;
         return nullptr;
     }
-    // jobs one output 9-12 floats wide over 16-byte aligned rows (stride >= 12) go last, to
-    // the 12-wide launch (order within each part kept: largest first)
+    // parts: jobs one output 9-12 floats wide over 16-byte aligned rows (stride >= 12) go to
+    // the 12-wide launch, jobs at most 4 floats wide over 16-byte aligned rows of a sliced
+    // batch to the 4-column launch, the rest to the general one (order within each part kept:
+    // largest first)
     {
-        auto wide = [](const Job &j) { return j.vw >= 4 && j.length > 8 && j.length <= 12; };
-        std::vector<Job> gj, wj;
-        std::vector<double> gm, wm;
+        const bool sliced = b->sliced;
+        auto part_of = [sliced](const Job &j) {
+            if (j.vw >= 4 && j.length > 8 && j.length <= 12) return 2;
+            if (sliced && j.vw >= 4 && j.length <= 4) return 1;
+            return 0;
+        };
+        std::vector<Job> pj[3];
+        std::vector<double> pm[3];
         for (size_t k = 0; k < b->jobs.size(); ++k) {
-            (wide(b->jobs[k]) ? wj : gj).push_back(b->jobs[k]);
-            (wide(b->jobs[k]) ? wm : gm).push_back(b->mean[k]);
+            const int p = part_of(b->jobs[k]);
+            pj[p].push_back(b->jobs[k]);
+            pm[p].push_back(b->mean[k]);
         }
-        b->numWide = (int)wj.size();
-        gj.insert(gj.end(), wj.begin(), wj.end());
-        gm.insert(gm.end(), wm.begin(), wm.end());
-        b->jobs.swap(gj);
-        b->mean.swap(gm);
+        b->jobs.clear();
+        b->mean.clear();
+        for (int p = 0; p < 3; ++p) {
+            b->part[p] = (int)pj[p].size();
+            b->jobs.insert(b->jobs.end(), pj[p].begin(), pj[p].end());
+            b->mean.insert(b->mean.end(), pm[p].begin(), pm[p].end());
+        }
     }
     // every job's vector width must match its rows' alignment (the gathers assume it)
     for (const Job &j : b->jobs) {
@@ -876,16 +909,16 @@ GB300StencilBatch *GB300StencilBatchCreate(int numJobs, GB300StencilTable *const
         if (it != g_tuned.end()) b->cfg = it->second;
     }
     const size_t jobBytes = ((numJobs * sizeof(Job) + 255) / 256) * 256;
-    if (check_cuda(cudaMalloc((void **)&b->dJobs, jobBytes + (numJobs + 2) * sizeof(int)),
+    if (check_cuda(cudaMalloc((void **)&b->dJobs, jobBytes + (numJobs + 3) * sizeof(int)),
                    "batch jobs") != GB300_OK) {
         b->dJobs = nullptr;
         delete b;
         return nullptr;
     }
     b->dTileBase = (int *)((char *)b->dJobs + jobBytes);
-    if (check_cuda(cudaMalloc((void **)&b->dCounter, 3 * sizeof(int)), "batch counter") !=
+    if (check_cuda(cudaMalloc((void **)&b->dCounter, 4 * sizeof(int)), "batch counter") !=
             GB300_OK ||
-        check_cuda(cudaMemsetAsync(b->dCounter, 0, 3 * sizeof(int), s), "batch counter") !=
+        check_cuda(cudaMemsetAsync(b->dCounter, 0, 4 * sizeof(int), s), "batch counter") !=
             GB300_OK ||
         upload_plan(b, s) != GB300_OK) {
         delete b;
@@ -934,8 +967,8 @@ int GB300StencilBatchEvalGraph(GB300StencilBatch *b, void *stream) {
     }
     int st = check_cuda(cudaGraphLaunch(b->graph, s), "GB300StencilBatchEvalGraph");
     if (st != GB300_OK) return st;
-    if (b->numTiles) count_launch();
-    if (b->numTilesWide) count_launch();
+    for (int p = 0; p < 3; ++p)
+        if (b->partTiles[p]) count_launch();
     return ok();
 }
 
@@ -955,7 +988,7 @@ int GB300StencilBatchGetConfig(const GB300StencilBatch *b, int *tileStencils, in
     if (tileStencils) *tileStencils = b->cfg.tileStencils;
     if (ctasPerSm) *ctasPerSm = b->cfg.ctasPerSm;
     if (warpThreshold) *warpThreshold = b->cfg.warpThreshold;
-    if (numTiles) *numTiles = b->numTiles + b->numTilesWide;
+    if (numTiles) *numTiles = b->numTiles();
     if (dynamicClaims) *dynamicClaims = b->cfg.dynamic;
     return ok();
 }
@@ -1107,7 +1140,7 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
         return st;
     Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1, 1};
     const int grid = (int)std::min<long long>(tiles, 2LL * sms);
-    k_stencils_batch<false, false><<<grid, kThreads, Ring<false, false>::kSmem, s>>>(a);
+    k_stencils_batch<kAny, false><<<grid, kThreads, Ring<kAny, false>::kSmem, s>>>(a);
     count_launch();
     return check_launch(who);
 }

@@ -49,11 +49,13 @@ int plan_tiles(Job *jobs, const double *meanSize, int n, int tileStencils, int w
 
 // One persistent launch over n jobs (device arrays dJobs[n], dTileBase[n + 1]).  dynamic: tiles
 // are claimed from the work counter (reset on `s` first), else CTA b takes tiles b, b + grid,
-// ...  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.  wide: every job is one
-// output 9-12 floats wide over 16-byte aligned rows (the kernel's single 12-wide pass).
-// sliced: every job is mode 2 (plan_tiles of jobs that all carry a sliced layout).
+// ...  dStatus receives GB300_ERR_DEVICE_TIMEOUT if a wait gave up.  cls: 0 any job; 1 every
+// job is one output 9-12 floats wide over 16-byte aligned rows (the kernel's single 12-wide
+// pass); 2 every job is at most 4 floats wide over 16-byte aligned rows (single 4-column pass,
+// sliced launches only).  sliced: every job is mode 2 (plan_tiles of jobs that all carry a
+// sliced layout).
 int launch_jobs(const Job *dJobs, const int *dTileBase, int n, int numTiles, int *dCounter,
-                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1, bool wide = false,
+                int *dStatus, int ctasPerSm, cudaStream_t s, int dynamic = 1, int cls = 0,
                 bool sliced = false);
 
 // Padded copy of one source: rows [0, numRows) of `src` (length <= 16 floats, srcStride
