@@ -309,7 +309,8 @@ template <int VW>
 __device__ __forceinline__ void gather_cols(const SellArgs &a, int id, int c0, uint64_t pol_src,
                                             float (&x)[VW == 12 ? 12 : VW == kNarrow ? 4 : 8]) {
     if constexpr (VW == kNarrow) {
-        const float4 q = __ldg(reinterpret_cast<const float4 *>(a.src + (size_t)id * a.srcStride));
+        const float4 q =
+            __ldg(reinterpret_cast<const float4 *>(a.src + (size_t)id * a.srcStride + c0));
         x[0] = q.x;
         x[1] = q.y;
         x[2] = q.z;
