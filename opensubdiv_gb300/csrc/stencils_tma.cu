@@ -16,6 +16,11 @@
 // A tile whose entries do not fit the stage (or whose offsets are not monotone) is processed
 // straight from global memory.  Every mbarrier wait is bounded by a %globaltimer deadline; on
 // expiry the CTA records GB300_ERR_DEVICE_TIMEOUT in g_status and leaves.
+//
+// Table objects evaluate through their sliced layout (sell.h) with k_stencils_sell: the same
+// producer / ring / consumer-group scheme, tiles of whole 32-stencil slices, one consumer warp
+// per slice stepping through entry j of its 32 stencils together (one conflict-free 32-bit
+// shared load per array per step).  The Far-layout kernel serves raw-pointer calls.
 #include "common.cuh"
 #include "sell.h"
 #include "stencil_eval.cuh"
