@@ -33,3 +33,19 @@ def test_version_and_error_string_without_gpu():
     lib = _lib.load()
     assert lib.GB300GetVersion() >= 100
     assert isinstance(lib.GB300GetLastErrorString(), bytes)
+
+
+def test_stencil_table_create_rejects_entries_outside_the_arrays():
+    """Entry ranges are validated on the host before any device work: a stencil whose
+    [offset, offset + size) leaves [0, nnz) is rejected with GB300_ERR_INVALID_ARGUMENT."""
+    import numpy as np
+    lib = _lib.load()
+    sizes = np.array([2, 3], np.int32)
+    idx = np.zeros(4, np.int32)
+    w = np.ones(4, np.float32)
+    p = lambda a: a.ctypes.data  # noqa: E731
+    for offsets in (np.array([0, 2], np.int32), np.array([-1, 0], np.int32)):
+        h = lib.GB300StencilTableCreate(2, 4, p(sizes), p(offsets), p(idx), p(w), None, None,
+                                        None, None, None, None)
+        assert not h
+        assert b"outside" in lib.GB300GetLastErrorString()
