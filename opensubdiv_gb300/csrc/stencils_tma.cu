@@ -278,12 +278,20 @@ static int launch(const Args &a, cudaStream_t s) {
 // the tile's positions (sizes, destination rows) and its contiguous slot range (indices and
 // weights, 128-byte multiples) into a stage; a consumer warp steps through entry j of its 32
 // stencils together, reading index and weights with one conflict-free shared load each.
-template <int NW>
+// VW of the pass over rows of at most 4 floats at 16-byte aligned rows: one 128-bit load per
+// entry and 4 columns per pass, so more rows fit in registers per entry step.
+constexpr int kNarrow = 44;
+
+// Ring of an instantiation.  One output over rows of at most 4 floats: 2 stages of 8-slice
+// tiles (refine pass at L=4 0.196 -> 0.179 ms; the same ring measured 1-5% slower for 8- and
+// 12-wide rows, which keep 3 stages of 4-slice tiles).
+template <int NW, int VW>
 struct SellCfg {
-    static constexpr int kSlots = NW <= 3 ? 2048 : 1024;  // slots per stage
+    static constexpr bool kTwo = NW == 1 && VW == kNarrow;
+    static constexpr int kSlots = kTwo ? 4096 : NW <= 3 ? 2048 : 1024;  // slots per stage
     static constexpr int kSpt = kSlots / 512;  // slices per tile (staged up to width 16)
     static constexpr size_t kStageBytes = (size_t)kSpt * 32 * 8 + (size_t)kSlots * 4 * (1 + NW);
-    static constexpr int kRing = NW >= 4 ? 4 : kStages;
+    static constexpr int kRing = kTwo ? 2 : NW >= 4 ? 4 : kStages;
     static constexpr size_t kSmem = kRing * kStageBytes + 256;
 };
 
@@ -302,10 +310,6 @@ struct SellArgs {
 struct SellMeta {
     int s0, s1, slot0, staged;
 };
-
-// VW of the pass over rows of at most 4 floats at 16-byte aligned rows: one 128-bit load per
-// entry and 4 columns per pass, so more rows fit in registers per entry step.
-constexpr int kNarrow = 44;
 
 // Columns [c0, c0 + 8) of source row `id`, all 12 columns of a 9-12 wide row (VW = 12: three
 // 16-byte loads; the row stride is a multiple of 4 floats, at least 12), or the 4 columns of a
@@ -372,7 +376,7 @@ template <int NW, int VW>
 __global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : (NW == 1 || VW == kNarrow) ? 3 : 2)
     k_stencils_sell(const SellArgs a) {
     extern __shared__ __align__(128) char smem[];
-    using C = SellCfg<NW>;
+    using C = SellCfg<NW, VW>;
     constexpr int S = C::kRing, SPT = C::kSpt;
     constexpr int G = 8 / SPT;          // consumer groups (one warp per slice of a tile)
     constexpr int GT = kConsumers / G;  // threads per group
@@ -506,7 +510,7 @@ __global__ void __launch_bounds__(kThreads, NW >= 6 ? 1 : (NW == 1 || VW == kNar
 
 template <int NW, int VW>
 static int launch_sell(const SellArgs &a, cudaStream_t s) {
-    using C = SellCfg<NW>;
+    using C = SellCfg<NW, VW>;
     auto kern = k_stencils_sell<NW, VW>;
     static std::atomic<uint64_t> attr{0};
     const int st = once_per_device(attr, [&] {
