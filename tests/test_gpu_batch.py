@@ -254,3 +254,35 @@ def test_batch_of_only_wide_jobs():
     for (L, stride), a, b in zip(widths, dsts, plain):
         assert torch.equal(a, b), (L, stride)
     assert batch.GetDeviceStatus() == 0
+
+
+@pytest.mark.gpu
+def test_sliced_and_far_layout_batches_agree_bit_for_bit():
+    """A batch whose tables all carry their sliced layout runs the sliced tiles (three
+    launches: any width, at most 4 floats, 9-12 floats); one table without stencils (no
+    sliced layout) switches the same jobs to the Far-layout tiles.  Both must write identical
+    bits."""
+    torch = torch_cuda()
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD
+    from opensubdiv_gb300.evaluator import GB300StencilBatch, GB300StencilTable
+    pop = _population(n=20, cv_max=2500, seed=21)
+    tables = [GB300StencilTable.Create(**m["table"]) for m in pop]
+    srcs = [dev(m["src"]) for m in pop]
+    descs = [BD(0, m["length"], m["length"]) for m in pop]
+    a = [torch.zeros(len(m["table"]["sizes"]) * m["length"], device="cuda") for m in pop]
+    b = [torch.zeros_like(x) for x in a]
+    sliced = GB300StencilBatch(list(zip(tables, srcs, descs, a, descs)))
+    # a table without stencils has no sliced layout
+    empty = GB300StencilTable.Create(np.zeros(0, np.int32), np.zeros(0, np.int32),
+                                     np.zeros(0, np.int32), np.zeros(0, np.float32))
+    e_out = torch.full((3,), 9.0, device="cuda")
+    far = GB300StencilBatch(list(zip(tables, srcs, descs, b, descs)) +
+                            [(empty, srcs[0], BD(0, 3, 3), e_out, BD(0, 3, 3))])
+    sliced.Eval()
+    far.Eval()
+    torch.cuda.synchronize()
+    for x, y in zip(a, b):
+        assert torch.equal(x, y)
+    assert float(e_out.min()) == 9.0 and float(e_out.max()) == 9.0
+    lengths = {m["length"] for m in pop}
+    assert lengths & {3, 4} and lengths & {9, 10, 11, 12}
