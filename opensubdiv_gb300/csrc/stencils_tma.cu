@@ -625,8 +625,8 @@ int eval_stencils_sell(const SellTable &t, const float *src, float *const *dst,
     if (nw == 0) return ok();
     const int vw = (al32(src) && srcStride % 8 == 0) ? 8 : (al16(src) && srcStride % 4 == 0) ? 4 : 1;
     int r;
-    if (nw == 1 && vw >= 4 && length > 8 && length <= 12) {
-        r = tma::launch_sell<1, 12>(a, s);
+    if ((nw == 1 || nw == 3) && vw >= 4 && length > 8 && length <= 12) {
+        r = nw == 1 ? tma::launch_sell<1, 12>(a, s) : tma::launch_sell<3, 12>(a, s);
     } else if ((nw == 1 || nw == 3) && vw >= 4 && length <= 4) {
         r = nw == 1 ? tma::launch_sell<1, tma::kNarrow>(a, s) : tma::launch_sell<3, tma::kNarrow>(a, s);
     } else {
