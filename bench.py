@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section")
     ap.add_argument("--no-factory", action="store_true",
                     help="skip the stencil-table factory section")
+    ap.add_argument("--layouts", action="store_true",
+                    help="add the `layouts` section: device-table EvalStencils per primvar "
+                         "layout (L = 3/4/8/12) and per output count (1-6)")
     ap.add_argument("--serve-topologies", type=int, default=1000)
     ap.add_argument("--serve-requests", type=int, default=4000, help="requests per rate")
     ap.add_argument("--serve-rates", type=lambda s: [float(x) for x in s.split(",")],
@@ -369,6 +372,57 @@ def bench_serving(args):
 
 METRIC = "stencil evals per s (EvalStencils refine L3 + limit du/dv)"
 UNIT = "stencils/s"
+
+
+def bench_layouts(w, stream):
+    """Device-table EvalStencils on the headline tables per source layout (refine pass, one
+    output; limit pass, P+du+dv) and, at 8 floats, per output count 1-6 over a limit table
+    carrying 6 weight arrays (du/dv weights reused for the second derivatives: timing only).
+    CUDA events on the launch stream, 20 launches after 3 warm-ups, milliseconds."""
+    import torch
+
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300StencilTable)
+    r, lim = w["refine"], w["limit"]
+    ncv = w["cage"].num_vertices
+    n, m = len(r["sizes"]), len(lim["sizes"])
+    t_ref = GB300StencilTable.Create(r["sizes"], r["offsets"], r["indices"], r["weights"])
+    ws = [lim["weights"], lim["du_weights"], lim["dv_weights"], lim["du_weights"],
+          lim["dv_weights"], lim["du_weights"]]
+    t6 = GB300StencilTable.Create(lim["sizes"], lim["offsets"], lim["indices"], *ws)
+
+    def timeit(fn, k=20):
+        for _ in range(3):
+            assert fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(k):
+            assert fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return round(e0.elapsed_time(e1) / k, 4)
+
+    keys = ("du", "dv", "duu", "duv", "dvv")
+    res = {"refine_ms": {}, "limit_P_du_dv_ms": {}, "limit_L8_ms_by_outputs": {}}
+    for ln, st in ((3, 4), (4, 4), (8, 8), (12, 12)):
+        src = torch.rand(ncv * st, device="cuda")
+        o = [torch.zeros(max(n, m) * ln, device="cuda") for _ in range(6)]
+        sd, dd = BD(0, ln, st), BD(0, ln, ln)
+        res["refine_ms"][f"L{ln}/stride{st}"] = timeit(
+            lambda: Ev.EvalStencilsTable(src, sd, o[0], dd, t_ref, stream=stream))
+        res["limit_P_du_dv_ms"][f"L{ln}/stride{st}"] = timeit(
+            lambda: Ev.EvalStencilsTable(src, sd, o[0], dd, t6, du=o[1], duDesc=dd, dv=o[2],
+                                         dvDesc=dd, stream=stream))
+        if ln == 8:
+            for nout in range(1, 7):
+                kw = {}
+                for k in range(1, nout):
+                    kw[keys[k - 1]], kw[keys[k - 1] + "Desc"] = o[k], dd
+                res["limit_L8_ms_by_outputs"][str(nout)] = timeit(
+                    lambda: Ev.EvalStencilsTable(src, sd, o[0], dd, t6, stream=stream, **kw))
+    res["stencils"] = {"refine": n, "limit": m}
+    return res
 
 
 def bench_factory(args, w):
@@ -871,6 +925,8 @@ def run_gb300(args, rank, world):
         line["serving"] = bench_serving(args)
     if not args.no_factory:
         line["factory"] = bench_factory(args, w)
+    if args.layouts:
+        line["layouts"] = bench_layouts(w, stream)
     if not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         rate, el = cpu_rate(w, args.cpu_seconds, threads)
