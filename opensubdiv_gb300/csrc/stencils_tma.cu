@@ -278,6 +278,7 @@ static int launch(const Args &a, cudaStream_t s) {
 // the tile's positions (sizes, destination rows) and its contiguous slot range (indices and
 // weights, 128-byte multiples) into a stage; a consumer warp steps through entry j of its 32
 // stencils together, reading index and weights with one conflict-free shared load each.
+
 // VW of the pass over rows of at most 4 floats at 16-byte aligned rows: one 128-bit load per
 // entry and 4 columns per pass, so more rows fit in registers per entry step.
 constexpr int kNarrow = 44;
