@@ -16,7 +16,9 @@
 //     boundary points (:666-850) in weight space.
 //   - QUADS / TRIANGLES are the linear bases (:56-97, :496-525).
 // Derivative scaling by +-2^depth and +-4^depth (:1587-1606) is applied to the sums (exact:
-// powers of two).
+// powers of two).  Rows are gathered relative to a corner control point of the patch (see
+// load_row below), which keeps the second-derivative sums accurate to well inside
+// 1e-5 x the cage's size where the reference's absolute-coordinate sums are not.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -57,6 +59,29 @@ __device__ __forceinline__ void load_row(const float *__restrict__ src, int stri
     const uint64_t pol = l2_evict_last();
 #pragma unroll
     for (int c = 0; c < LC; ++c) x[c] = (e0 + c < length) ? ld_src(p + c, pol) : 0.0f;
+}
+
+// Local origin.  Every basis is a partition of unity: its value weights sum to 1 and every
+// derivative's weights sum to 0.  So  sum_j w_j x_j = xc + sum_j w_j (x_j - xc)  for the value
+// and  sum_j w_j (x_j - xc)  for a derivative, for any point xc.  The bases below gather rows
+// relative to one of the patch's own control points (a corner of the patch): the summands
+// then scale with the patch's extent instead of the points' distance from the origin, and
+// the float rounding of the cancelling derivative sums (which carry the 2^depth and 4^depth
+// factors) shrinks by that ratio.  The value output adds xc back at the end.
+template <int LC>
+__device__ __forceinline__ void load_row(const float *__restrict__ src, int stride, int cv,
+                                         int e0, int length, float (&x)[LC],
+                                         const float (&xc)[LC]) {
+    const float *p = src + (size_t)cv * stride + e0;
+    const uint64_t pol = l2_evict_last();
+#pragma unroll
+    for (int c = 0; c < LC; ++c) x[c] = (e0 + c < length) ? ld_src(p + c, pol) - xc[c] : 0.0f;
+}
+
+template <int LC>
+__device__ __forceinline__ void add_origin(const float (&xc)[LC], Acc6<LC> &acc) {
+#pragma unroll
+    for (int c = 0; c < LC; ++c) acc.v[0][c] += xc[c];
 }
 
 // N control-point indices of a patch: 128-bit loads when the index row is 16-byte aligned
@@ -154,13 +179,17 @@ __device__ void eval_bspline(float s, float t, int boundary, const int *__restri
     if (boundary & 8) { fold_first(sp); fold_first(sd); fold_first(sdd); }
     int idx[16];
     load_indices<16>(cvs, idx);
+    float xc[LC];  // point 5: the patch's (0,0) corner, never a phantom
+    load_row<LC>(src, stride, idx[5], e0, length, xc);
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
         float x[4][LC];
 #pragma unroll
-        for (int c = 0; c < 4; ++c) load_row<LC>(src, stride, idx[4 * r + c], e0, length, x[c]);
+        for (int c = 0; c < 4; ++c)
+            load_row<LC>(src, stride, idx[4 * r + c], e0, length, x[c], xc);
         tensor_accumulate<LC>(sp, sd, sdd, tp[r], td[r], tdd[r], x, acc);
     }
+    add_origin<LC>(xc, acc);
 }
 
 // GREGORY_BASIS: 20 points; the Bezier grid is
@@ -181,6 +210,8 @@ __device__ void eval_gregory(float s, float t, const int *__restrict__ cvs,
     const float g0 = s * d0, g2 = t * d1, g4 = sc * d2, g6 = tc * d3;
     int idx[20];
     load_indices<20>(cvs, idx);
+    float xc[LC];  // point 0: the patch's (0,0) corner
+    load_row<LC>(src, stride, idx[0], e0, length, xc);
     // rows of the Bezier grid; interior entries are blended pairs
     constexpr int kGrid[4][4] = {{0, 1, 7, 5}, {2, -1, -2, 6}, {16, -4, -3, 12}, {15, 17, 11, 10}};
 #pragma unroll
@@ -190,20 +221,21 @@ __device__ void eval_gregory(float s, float t, const int *__restrict__ cvs,
         for (int c = 0; c < 4; ++c) {
             const int g = kGrid[r][c];
             if (g >= 0) {
-                load_row<LC>(src, stride, idx[g], e0, length, x[c]);
+                load_row<LC>(src, stride, idx[g], e0, length, x[c], xc);
             } else {
                 // -1: (3,4) by g0; -2: (8,9) by g2; -3: (13,14) by g4; -4: (18,19) by g6
                 const int a = (g == -1) ? 3 : (g == -2) ? 8 : (g == -3) ? 13 : 18;
                 const float ga = (g == -1) ? g0 : (g == -2) ? g2 : (g == -3) ? g4 : g6;
                 float xa[LC], xb[LC];
-                load_row<LC>(src, stride, idx[a], e0, length, xa);
-                load_row<LC>(src, stride, idx[a + 1], e0, length, xb);
+                load_row<LC>(src, stride, idx[a], e0, length, xa, xc);
+                load_row<LC>(src, stride, idx[a + 1], e0, length, xb, xc);
 #pragma unroll
                 for (int k = 0; k < LC; ++k) x[c][k] = ga * xa[k] + (1.0f - ga) * xb[k];
             }
         }
         tensor_accumulate<LC>(bs, bds, bdss, bt[r], bdt[r], bdtt[r], x, acc);
     }
+    add_origin<LC>(xc, acc);
 }
 
 // Quartic Bezier triangle weights for derivative order (ds, dt) (patchBasis.h:924-1044).
@@ -272,19 +304,21 @@ __device__ void eval_gregory_tri(float s, float t, const int *__restrict__ cvs,
     if ((w + u) > 0) { g[4] = w / (w + u); g[5] = u / (w + u); }
     // Bezier point m comes from Gregory point kBez[m] (or a blended pair for 6, 7, 10)
     constexpr int kBez[15] = {0, 1, 15, 7, 5, 2, -1, -2, 6, 17, -3, 16, 11, 12, 10};
+    float xc[LC];  // point 0: the (0,0) corner
+    load_row<LC>(src, stride, __ldg(cvs), e0, length, xc);
     float B[15][LC];
 #pragma unroll
     for (int m = 0; m < 15; ++m) {
         const int gi = kBez[m];
         if (gi >= 0) {
-            load_row<LC>(src, stride, __ldg(cvs + gi), e0, length, B[m]);
+            load_row<LC>(src, stride, __ldg(cvs + gi), e0, length, B[m], xc);
         } else {
             const int a = (gi == -1) ? 3 : (gi == -2) ? 8 : 13;
             const float ga = (gi == -1) ? g[0] : (gi == -2) ? g[2] : g[4];
             const float gb = (gi == -1) ? g[1] : (gi == -2) ? g[3] : g[5];
             float xa[LC], xb[LC];
-            load_row<LC>(src, stride, __ldg(cvs + a), e0, length, xa);
-            load_row<LC>(src, stride, __ldg(cvs + a + 1), e0, length, xb);
+            load_row<LC>(src, stride, __ldg(cvs + a), e0, length, xa, xc);
+            load_row<LC>(src, stride, __ldg(cvs + a + 1), e0, length, xb, xc);
 #pragma unroll
             for (int c = 0; c < LC; ++c) B[m][c] = ga * xa[c] + gb * xb[c];
         }
@@ -299,6 +333,7 @@ __device__ void eval_gregory_tri(float s, float t, const int *__restrict__ cvs,
 #pragma unroll
             for (int c = 0; c < LC; ++c) acc.v[k][c] = fmaf(b[m], B[m][c], acc.v[k][c]);
     }
+    add_origin<LC>(xc, acc);
 }
 
 // Box-spline coefficient rows over the quartic monomials {1, s, t, s2, st, t2, s3, s2t, st2,
@@ -400,12 +435,13 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
     // the 12 control points once (every index of a Loop patch is valid, phantom boundary
     // points included, as the reference's own gather of all 12 relies on), then one
     // derivative order at a time: 12 weights live instead of 72, no reloads
-    float x[12][LC];
+    float x[12][LC], xc[LC];
     {
         int idx[12];
         load_indices<12>(cvs, idx);
+        load_row<LC>(src, stride, idx[4], e0, length, xc);  // point 4: the (0,0) corner
 #pragma unroll
-        for (int j = 0; j < 12; ++j) load_row<LC>(src, stride, idx[j], e0, length, x[j]);
+        for (int j = 0; j < 12; ++j) load_row<LC>(src, stride, idx[j], e0, length, x[j], xc);
     }
     const float k12 = 1.0f / 12.0f, k6 = 1.0f / 6.0f;
 #pragma unroll
@@ -428,6 +464,7 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
             for (int c = 0; c < LC; ++c) acc.v[k][c] = fmaf(w[j], x[j][c], acc.v[k][c]);
         }
     }
+    add_origin<LC>(xc, acc);
 }
 
 template <int LC>
@@ -439,10 +476,12 @@ __device__ void eval_linear_quad(float s, float t, const int *__restrict__ cvs,
     const float ws[4] = {-tc, tc, t, -t};
     const float wt[4] = {-sc, -s, s, sc};
     const float wst[4] = {1.0f, -1.0f, 1.0f, -1.0f};
+    float xc[LC];
+    load_row<LC>(src, stride, __ldg(cvs), e0, length, xc);
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
         float x[LC];
-        load_row<LC>(src, stride, __ldg(cvs + j), e0, length, x);
+        load_row<LC>(src, stride, __ldg(cvs + j), e0, length, x, xc);
 #pragma unroll
         for (int c = 0; c < LC; ++c) {
             acc.v[0][c] = fmaf(wp[j], x[c], acc.v[0][c]);
@@ -451,6 +490,7 @@ __device__ void eval_linear_quad(float s, float t, const int *__restrict__ cvs,
             acc.v[4][c] = fmaf(wst[j], x[c], acc.v[4][c]);
         }
     }
+    add_origin<LC>(xc, acc);
 }
 
 template <int LC>
@@ -459,14 +499,14 @@ __device__ void eval_linear_tri(float s, float t, const int *__restrict__ cvs,
                                 Acc6<LC> &acc) {
     float x0[LC], x1[LC], x2[LC];
     load_row<LC>(src, stride, __ldg(cvs + 0), e0, length, x0);
-    load_row<LC>(src, stride, __ldg(cvs + 1), e0, length, x1);
-    load_row<LC>(src, stride, __ldg(cvs + 2), e0, length, x2);
-    const float w0 = 1.0f - s - t;
+    load_row<LC>(src, stride, __ldg(cvs + 1), e0, length, x1, x0);
+    load_row<LC>(src, stride, __ldg(cvs + 2), e0, length, x2, x0);
+    // relative to point 0: P = x0 + s (x1 - x0) + t (x2 - x0)
 #pragma unroll
     for (int c = 0; c < LC; ++c) {
-        acc.v[0][c] = w0 * x0[c] + s * x1[c] + t * x2[c];
-        acc.v[1][c] = x1[c] - x0[c];
-        acc.v[2][c] = x2[c] - x0[c];
+        acc.v[0][c] = x0[c] + (s * x1[c] + t * x2[c]);
+        acc.v[1][c] = x1[c];
+        acc.v[2][c] = x2[c];
     }
 }
 

@@ -268,6 +268,20 @@ class Patches:
                                _p(params))
         return arrays, indices, params
 
+    def fvar_stencils(self, refiner, channel=0):
+        """Stencils of face-varying channel `channel` over its base values: every refinement
+        level, then the channel's local points (the source buffer of its patches)."""
+        counts = np.zeros(2, np.int64)
+        lib().ref_patches_fvar_stencils(refiner.h, self.h, C.c_int(channel), _p(counts), None,
+                                        None, None, None)
+        n, nnz = int(counts[0]), int(counts[1])
+        st = dict(sizes=np.zeros(n, np.int32), offsets=np.zeros(n, np.int32),
+                  indices=np.zeros(nnz, np.int32), weights=np.zeros(nnz, np.float32))
+        lib().ref_patches_fvar_stencils(refiner.h, self.h, C.c_int(channel), _p(counts),
+                                        _p(st["sizes"]), _p(st["offsets"]), _p(st["indices"]),
+                                        _p(st["weights"]))
+        return st
+
     def find_patches(self, faces, u, v):
         faces = np.ascontiguousarray(faces, np.int32)
         u = np.ascontiguousarray(u, np.float64)

@@ -621,6 +621,40 @@ void ref_patches_fvar(void *p, int channel, long *counts, int *arrays, int *indi
         std::memcpy(params, h->cpu->GetFVarPatchParamBuffer(channel), counts[3] * 12);
 }
 
+// Face-varying values of channel `channel` for every refinement level and the channel's local
+// points, as one stencil table over the channel's base values: Far::StencilTableFactory in
+// INTERPOLATE_FACE_VARYING mode with intermediate levels, plus
+// AppendLocalPointStencilTableFaceVarying (far/stencilTableFactory.h:334-346) with the patch
+// table's face-varying local-point stencils.  counts[0] = stencils, counts[1] = entries; the
+// arrays may be NULL to query the counts.
+void ref_patches_fvar_stencils(void *refiner, void *p, int channel, long *counts, int *sizes,
+                               int *offsets, int *indices, float *w) {
+    Far::TopologyRefiner *r = ((Refiner *)refiner)->r;
+    Patches *h = (Patches *)p;
+    Far::StencilTableFactory::Options so;
+    so.interpolationMode = Far::StencilTableFactory::INTERPOLATE_FACE_VARYING;
+    so.fvarChannel = channel;
+    so.generateOffsets = true;
+    so.generateIntermediateLevels = true;
+    Far::StencilTable const *st = Far::StencilTableFactory::Create(*r, so);
+    Far::StencilTable const *local = h->pt->GetLocalPointFaceVaryingStencilTable(channel);
+    if (local) {
+        Far::StencilTable const *all = Far::StencilTableFactory::
+            AppendLocalPointStencilTableFaceVarying(*r, st, local, channel);
+        delete st;
+        st = all;
+    }
+    counts[0] = st->GetNumStencils();
+    counts[1] = (long)st->GetControlIndices().size();
+    if (sizes) {
+        copyVec(st->GetSizes(), sizes);
+        copyVec(st->GetOffsets(), offsets);
+        copyVec(st->GetControlIndices(), indices);
+        copyN(st->GetWeights(), w, st->GetControlIndices().size());
+    }
+    delete st;
+}
+
 // Far::PatchMap::FindPatch (far/patchMap.h:192-231).  handles: 3 ints per query
 // (arrayIndex, patchIndex, vertIndex); found[i] = 0 when FindPatch returns NULL.
 void ref_find_patches(void *p, int n, const int *faces, const double *u, const double *v,

@@ -18,3 +18,15 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def golden_dir():
     return GOLDEN
+
+
+def pytest_sessionfinish(session, exitstatus):
+    """OSD_GB300_ERROR_REPORT=<path>: write the per-output errors the GPU parity tests saw."""
+    path = os.environ.get("OSD_GB300_ERROR_REPORT")
+    if not path:
+        return
+    import json
+
+    import gpu_util
+    with open(path, "w") as f:
+        json.dump(gpu_util.REPORT, f, indent=0)

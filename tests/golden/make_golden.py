@@ -110,7 +110,8 @@ def edge_queries(nptex, rng, n):
 
 def uv_seams(cage, nu, nv):
     """A face-varying UV channel with seams for a shapes.torus(nu, nv) cage: values on an
-    (nu + 1) x (nv + 1) grid, so faces across the wrap use the duplicated seam values."""
+    (nu + 1) x (nv + 1) grid, so faces across the wrap use the duplicated seam values.
+    Returns (number of values, value index per face-vertex)."""
     fidx = []
     start = 0
     for n in cage.verts_per_face:
@@ -123,6 +124,12 @@ def uv_seams(cage, nu, nv):
             j = np.where(j == 0, nv, j)
         fidx.extend((i * (nv + 1) + j).tolist())
     return (nu + 1) * (nv + 1), np.asarray(fidx, np.int32)
+
+
+def uv_grid(nu, nv):
+    """The texture coordinates of uv_seams' values: value i * (nv + 1) + j = (i / nu, j / nv)."""
+    i, j = np.meshgrid(np.arange(nu + 1), np.arange(nv + 1), indexing="ij")
+    return np.stack([i.ravel() / nu, j.ravel() / nv], 1).astype(np.float32)
 
 
 def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3, fvar=None):
@@ -188,9 +195,18 @@ def patch_fixture(path, cage, level, seed, nq=3000, adaptive=True, endcap=3, fva
         vouts = [np.zeros(len(sel) * 4, np.float32) for _ in range(3)]
         assert ref.cpu_eval_patches(vsrc, (0, 4, 4), vouts, [(0, 4, 4)] * 3, coords, va, vi,
                                     p.params)
-        # face-varying channel 0: its own arrays / indices / params, 2 primvars (uv)
+        # face-varying channel 0: its own arrays / indices / params, 2 primvars (uv).  The
+        # source holds the channel's base values (a uv layout with seams), then its refined
+        # and local-point values (Far's face-varying stencils applied by CpuEvaluator).
         fa, fi, fp = p.fvar(0)
-        fsrc = rng.uniform(0, 1, (int(fi.max()) + 1, 2)).astype(np.float32).ravel()
+        fst = p.fvar_stencils(r, 0)
+        nbase = int(fvar[0])
+        fsrc = np.zeros((nbase + len(fst["sizes"])) * 2, np.float32)
+        fsrc[: nbase * 2] = fvar[2].ravel()
+        assert ref.cpu_eval_stencils(fsrc, (0, 2, 2), [fsrc], [(nbase * 2, 2, 2)],
+                                     fst["sizes"], fst["offsets"], fst["indices"],
+                                     [fst["weights"]], 0, len(fst["sizes"]))
+        assert int(fi.max()) < nbase + len(fst["sizes"])
         fouts = [np.zeros(len(sel) * 2, np.float32) for _ in range(6)]
         assert ref.cpu_eval_patches(fsrc, (0, 2, 2), fouts, [(0, 2, 2)] * 6, coords, fa, fi, fp)
         out.update(fvar_num_values=np.int32(fvar[0]), fvar_value_indices=fvar[1],
@@ -300,10 +316,10 @@ def main():
     # Varying and face-varying tables: tori with UV seams (non-linear face-varying patches)
     ftor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=31, noise=0.01)
     patch_fixture(os.path.join(g, "torus12x8_fvar_patches_L3.npz"), ftor, 3, seed=32,
-                  nq=1500, fvar=uv_seams(ftor, 12, 8))
+                  nq=1500, fvar=uv_seams(ftor, 12, 8) + (uv_grid(12, 8),))
     fltor = shapes.torus(12, 8, seed=33, noise=0.01, scheme=shapes.LOOP)
     patch_fixture(os.path.join(g, "looptorus12x8_fvar_patches_L3.npz"), fltor, 3, seed=34,
-                  nq=1500, fvar=uv_seams(fltor, 12, 8))
+                  nq=1500, fvar=uv_seams(fltor, 12, 8) + (uv_grid(12, 8),))
     # Boundaries: open grids (B-spline and box-spline boundary masks).
     patch_fixture(os.path.join(g, "grid6_patches_L3.npz"), shapes.grid(6, 6, seed=5), 3,
                   seed=23, nq=1500)
