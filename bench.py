@@ -43,8 +43,6 @@ def parse():
     ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=10.0,
-                    help="bounded CPU-baseline sample length")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--nu", type=int, default=512, help="torus cage resolution (u)")
     ap.add_argument("--nv", type=int, default=256, help="torus cage resolution (v)")
@@ -628,27 +626,76 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def cpu_rate(w, seconds, threads):
-    """Oracle port of CpuEvaluator/OmpEvaluator on the same workload for ~`seconds`."""
+def cpu_passes(w, reps, warmup, threads, fraction=1.0):
+    """Seconds of each of `reps` timed passes (after `warmup` untimed ones) of the oracle port
+    of CpuEvaluator / OmpEvaluator (OpenMP over `threads`) over the first `fraction` of the
+    refine and limit tables, and the stencils one pass evaluates."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
     L = w["length"]
     r, l = w["refine"], w["limit"]
+    n_r, n_l = int(len(r["sizes"]) * fraction), int(len(l["sizes"]) * fraction)
     out = np.zeros(len(r["sizes"]) * L, np.float32)
     outs = [np.zeros(len(l["sizes"]) * L, np.float32) for _ in range(3)]
     d = (0, L, L)
-    done = 0
-    t0 = time.perf_counter()
-    while True:
+
+    def one():
         oracle.eval_stencils(w["src"], d, [out], [d], r["sizes"], r["offsets"], r["indices"],
-                             [r["weights"]], threads=threads)
+                             [r["weights"]], 0, n_r, threads=threads)
         oracle.eval_stencils(w["src"], d, outs, [d] * 3, l["sizes"], l["offsets"], l["indices"],
-                             [l["weights"], l["du_weights"], l["dv_weights"]], threads=threads)
-        done += len(r["sizes"]) + len(l["sizes"])
-        el = time.perf_counter() - t0
-        if el >= seconds:
-            return done / el, el
+                             [l["weights"], l["du_weights"], l["dv_weights"]], 0, n_l,
+                             threads=threads)
+
+    for _ in range(warmup):
+        one()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        one()
+        times.append(time.perf_counter() - t0)
+    return times, n_r + n_l
+
+
+def host_cpu():
+    """nproc and the CPU model of this host (lscpu, else /proc/cpuinfo)."""
+    model = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                model = line.split(":", 1)[1].strip()
+                break
+    except (OSError, subprocess.SubprocessError):
+        pass
+    if not model and os.path.exists("/proc/cpuinfo"):
+        for line in open("/proc/cpuinfo"):
+            if line.lower().startswith(("model name", "cpu part")):
+                model = line.split(":", 1)[1].strip()
+                break
+    return {"nproc": os.cpu_count(), "cpu_model": model}
+
+
+def cpu_baseline(w, reps=20, warmup=3, single_fraction=1.0 / 16):
+    """CPU baseline on this host: the median of `reps` timed passes after `warmup` untimed
+    ones, over all host threads (the OmpEvaluator form) and on one thread (the CpuEvaluator
+    form, over the first `single_fraction` of the tables per pass)."""
+    threads = os.cpu_count() or 1
+    t_all, n_all = cpu_passes(w, reps, warmup, threads)
+    t_one, n_one = cpu_passes(w, reps, warmup, 1, single_fraction)
+    med_all, med_one = float(np.median(t_all)), float(np.median(t_one))
+    return {"value": n_all / med_all, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"median of {reps} full refine + limit passes after {warmup} warm-ups "
+                      "(oracle port of OmpEvaluator: OpenMP over all host threads)",
+            "pass_ms": {"median": 1e3 * med_all, "p99": 1e3 * float(np.percentile(t_all, 99))},
+            "single_thread": {
+                "value": n_one / med_one, "unit": UNIT, "cores": 1,
+                "sample": f"median of {reps} passes over the first {single_fraction:.4g} of the "
+                          f"refine and limit tables ({n_one} stencils) after {warmup} warm-ups "
+                          "(oracle port of CpuEvaluator, one thread)",
+                "pass_ms": {"median": 1e3 * med_one,
+                            "p99": 1e3 * float(np.percentile(t_one, 99))}},
+            "host": host_cpu()}
 
 
 def reference_cuda(args, w):
@@ -722,28 +769,37 @@ def reference_cuda(args, w):
 def run_reference(args, rank, world):
     if rank != 0:
         return
-    from opensubdiv_gb300 import workloads
+    # the workload generator built by the oracle recipe: this process maps no library of
+    # the package (oracle/_build and oracle/_ref only)
+    from opensubdiv_gb300 import topology, workloads
+    gen = os.path.join(ROOT, "oracle", "_build", "libworkload_topology.so")
+    if not os.path.exists(gen):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "workload"],
+                       check=True)
+    topology.use_library(gen)
 
     w = workloads.refine_and_limit_torus(args.nu, args.nv, n_limit=args.n_limit)
     threads = os.cpu_count() or 1
-    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
-    for _ in range(args.warmup):
-        cpu_rate(w, 0.0, threads)
-    rates, total = [], 0.0
-    for _ in range(args.steps):
-        r, el = cpu_rate(w, per_step, threads)
-        rates.append(r)
-        total += el
-    value = float(np.median(rates))
-    n_step = len(w["refine"]["sizes"]) + len(w["limit"]["sizes"])
+    # one step = one full refine + limit pass over all host threads; value = the median
+    times, n_step = cpu_passes(w, args.steps, args.warmup, threads)
+    med = float(np.median(times))
+    value = n_step / med
+    base = cpu_baseline(w, reps=max(args.steps, 20), warmup=max(args.warmup, 3))
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
-            "ms_per_step": 1e3 * n_step / value, "higher_is_better": True, "scaling": "weak",
+            "ms_per_step": 1e3 * med, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded torus cage)",
-            "config": {"workload": w["name"], "stencils_per_step": n_step},
+            "config": {"workload": w["name"], "stencils_per_step": n_step,
+                       "refine_stencils": len(w["refine"]["sizes"]),
+                       "refine_nnz": int(len(w["refine"]["indices"])),
+                       "limit_stencils": len(w["limit"]["sizes"]),
+                       "limit_nnz": int(len(w["limit"]["indices"])), "primvars": w["length"],
+                       "parallelism": "host threads"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{args.steps} steps x >= {per_step:.1f}s of full "
-                                       "refine+limit passes, OpenMP over all host threads"},
+                             "sample": f"median of {args.steps} full refine + limit passes "
+                                       f"after {args.warmup} warm-ups (oracle port of "
+                                       "OmpEvaluator: OpenMP over all host threads)",
+                             "single_thread": base["single_thread"], "host": base["host"]},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
             "reference_cuda": reference_cuda(args, w)}
@@ -928,11 +984,7 @@ def run_gb300(args, rank, world):
     if args.layouts:
         line["layouts"] = bench_layouts(w, stream)
     if not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        rate, el = cpu_rate(w, args.cpu_seconds, threads)
-        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
-                                "sample": f"{el:.1f}s of full refine+limit passes (oracle "
-                                          "port of CpuEvaluator, OpenMP, all host threads)"}
+        line["cpu_baseline"] = cpu_baseline(w)
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()

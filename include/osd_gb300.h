@@ -434,11 +434,13 @@ int GB300ServerGetStats(GB300Server *server, GB300ServerStats *stats);
  * arguments of GB300EvalStencils per job, over stencils [0, numStencils[k]); every array
  * argument is a HOST array indexed by job, holding device pointers or ints) in one batched
  * launch, like GB300StencilBatchEval with one stencil per thread.  It allocates no device or
- * host memory: its scratch (work counter, status word, job table, tile prefix) is a fixed
- * 26,112-byte device array inside the library, so at most 256 jobs per call (more are
- * rejected with GB300_ERR_INVALID_ARGUMENT and a message).  The job table is copied into that
- * array from the host stack with cudaMemcpyAsync on `stream`, and the counter and status word
- * are cleared on `stream` before the kernel.  Table arrays must be 16-byte aligned.
+ * host memory: its scratch (work counter, job table, tile prefix) is a fixed 36,352-byte device
+ * array inside the library (256 + 256 job descriptors of 136 bytes + 1,280), so at most 256
+ * jobs per call (more are rejected with GB300_ERR_INVALID_ARGUMENT and a message).  The job
+ * table is copied into that array from the host stack with cudaMemcpyAsync on `stream`, and
+ * the counter is cleared on `stream` before the kernel.  Table arrays must be 16-byte aligned.
+ * A bounded wait that expires inside the kernel leaves outputs incomplete and is reported by
+ * the next GB300GetDeviceStatus(), like every other staged kernel of the library.
  * The first call on each device looks up the array's device address (cudaGetSymbolAddress,
  * with that device current): make that first call before any stream capture.  There is one
  * array per device, so calls that can overlap on a device (different streams, or different

@@ -32,6 +32,10 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // Number of SMs of the current device (cached per device).
 int num_sms();
 
+// Device address of the library's status word on the current device (the word
+// GB300GetDeviceStatus reads and clears; staged kernels record an expired bounded wait there).
+int status_word_address(int **out);
+
 // Runs `fn` (returning a status) once per device for one call site: `done` is that call site's
 // bitmask of devices it already succeeded on (devices >= 64 run it every time).
 template <class F>

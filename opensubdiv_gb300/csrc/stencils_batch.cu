@@ -794,26 +794,31 @@ int setup_padding(GB300StencilBatch *b, const std::vector<int> &tableRows, cudaS
 
 // ---- batched EvalStencils without allocation ------------------------------------------------
 //
-// The same kernel with all of its scratch -- work counter, status word, job table and tile
-// prefix -- in one fixed file-scope device array, so a call allocates no memory: the job table
-// is built on the host stack and copied into the array, the counter and status word are cleared
-// by a memset, and the kernel runs every job one stencil per thread (jobs' mean stencil sizes
-// are not known without reading the device tables).  One array per device means calls that
-// overlap on the device (two streams, two host threads) race on it.
+// The same kernel with all of its scratch -- work counter, job table and tile prefix -- in one
+// fixed file-scope device array, so a call allocates no memory: the job table is built on the
+// host stack and copied into the array, the counter is cleared by a memset, and the kernel runs
+// every job one stencil per thread (jobs' mean stencil sizes are not known without reading the
+// device tables).  An expired bounded wait is recorded in the library's status word (the one
+// GB300GetDeviceStatus reads), which is only cleared by reading it.  One array per device means
+// calls that overlap on the device (two streams, two host threads) race on it.
 namespace {
 
 constexpr int kNoAllocMaxJobs = 256;
-constexpr size_t kNoAllocJobOffset = 256;  // [0] counter, [1] status
+constexpr size_t kNoAllocJobOffset = 256;  // [0] work counter
 constexpr size_t kNoAllocBaseOffset =
     kNoAllocJobOffset + ((kNoAllocMaxJobs * sizeof(Job) + 255) / 256) * 256;
 constexpr size_t kNoAllocScratchBytes =
     kNoAllocBaseOffset + (((kNoAllocMaxJobs + 1) * sizeof(int) + 255) / 256) * 256;
+// the figure the header documents: 256 + 256 job descriptors of 136 bytes + 1,280
+static_assert(sizeof(Job) == 136 && kNoAllocScratchBytes == 36352,
+              "update the scratch size documented for GB300EvalStencilsBatchedNoAlloc");
 constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
 std::mutex g_noallocLock;
 unsigned char *g_noallocAddr[kNoAllocMaxDevices];  // scratch address per device
+int *g_noallocStatus[kNoAllocMaxDevices];          // the library's status word per device
 int g_noallocSms[kNoAllocMaxDevices];
 
 }  // namespace
@@ -1109,6 +1114,7 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
         return fail(GB300_ERR_UNSUPPORTED, "%s: device %d beyond the first %d", who, dev,
                     kNoAllocMaxDevices);
     unsigned char *scratch = nullptr;
+    int *status = nullptr;
     int sms = 0;
     {
         std::lock_guard<std::mutex> lock(g_noallocLock);
@@ -1116,13 +1122,17 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
             void *p = nullptr;
             st = check_cuda(cudaGetSymbolAddress(&p, g_noalloc_scratch), who);
             if (st != GB300_OK) return st;
+            int *sw = nullptr;
+            if ((st = status_word_address(&sw)) != GB300_OK) return st;
             int n = 0;
             st = check_cuda(cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev), who);
             if (st != GB300_OK) return st;
             g_noallocSms[dev] = n > 0 ? n : 1;
+            g_noallocStatus[dev] = sw;
             g_noallocAddr[dev] = (unsigned char *)p;
         }
         scratch = g_noallocAddr[dev];
+        status = g_noallocStatus[dev];
         sms = g_noallocSms[dev];
     }
     if ((st = set_smem_attribute()) != GB300_OK) return st;
@@ -1136,9 +1146,9 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
                                          cudaMemcpyHostToDevice, s), who)) != GB300_OK ||
         (st = check_cuda(cudaMemcpyAsync(dBase, base, (numJobs + 1) * sizeof(int),
                                          cudaMemcpyHostToDevice, s), who)) != GB300_OK ||
-        (st = check_cuda(cudaMemsetAsync(counter, 0, 2 * sizeof(int), s), who)) != GB300_OK)
+        (st = check_cuda(cudaMemsetAsync(counter, 0, sizeof(int), s), who)) != GB300_OK)
         return st;
-    Args a{dJobs, dBase, numJobs, (int)tiles, counter, counter + 1, 1};
+    Args a{dJobs, dBase, numJobs, (int)tiles, counter, status, 1};
     const int grid = (int)std::min<long long>(tiles, 2LL * sms);
     k_stencils_batch<kAny, false><<<grid, kThreads, Ring<kAny, false>::kSmem, s>>>(a);
     count_launch();

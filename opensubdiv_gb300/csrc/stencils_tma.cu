@@ -651,6 +651,17 @@ int eval_stencils_sell(const SellTable &t, const float *src, float *const *dst,
 
 }  // namespace gb300
 
+namespace gb300 {
+
+int status_word_address(int **out) {
+    void *p = nullptr;
+    const int st = check_cuda(cudaGetSymbolAddress(&p, g_status), "status word address");
+    *out = (int *)p;
+    return st;
+}
+
+}  // namespace gb300
+
 extern "C" int GB300GetDeviceStatus(void) {
     using namespace gb300;
     int v = 0;

@@ -17,14 +17,26 @@ import numpy as np
 from . import build as _build
 
 _lib = None
+_path = None
+
+
+def use_library(path: str) -> None:
+    """Loads the generator from `path` instead of the package's own build (a process that
+    must not map this package's libraries -- the CPU reference timing -- builds the same
+    sources elsewhere).  Must be called before the first load()."""
+    global _path
+    if _lib is not None:
+        raise RuntimeError("the generator library is already loaded")
+    _path = path
 
 
 def load():
     global _lib
     if _lib is None:
-        if not os.path.exists(_build.TOPO_LIB):
+        path = _path or _build.TOPO_LIB
+        if _path is None and not os.path.exists(path):
             _build.build_topology()
-        lib = C.CDLL(_build.TOPO_LIB)
+        lib = C.CDLL(path)
         vp, i32, i64 = C.c_void_p, C.c_int, C.c_int64
         lib.GB300TopologyCreate.restype = vp
         lib.GB300TopologyCreate.argtypes = [i32, i32, i32, vp, vp, i32, vp, vp]

@@ -2,8 +2,9 @@
 fixed device array inside the library (no allocation per call).
 
 Two calls in a row, with different source values, must each match the existing
-GB300EvalStencils entry point (one call per job) within the EvalStencils tolerance of
-1e-5 x the cage's bounding-box diagonal.  The file sorts last so that it also runs after every
+GB300EvalStencils entry point (one call per job) and the oracle (Osd::CpuEvaluator restated)
+within the EvalStencils tolerance of 1e-5 x the cage's bounding-box diagonal, and leave the
+library's device status word clear.  The file sorts last so that it also runs after every
 other GPU test in the same process (and it passes alone).
 """
 import ctypes as C
@@ -12,6 +13,7 @@ import os
 import numpy as np
 import pytest
 
+import oracle
 from gpu_util import bbox_diag, dev, host, max_err, torch_cuda
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -34,10 +36,11 @@ def _jobs(torch):
         n = len(z["sizes"])
         diag = bbox_diag(z["positions"])
         src3 = z["src8"].reshape(-1, 8)[:, :3].copy().ravel()
-        jobs.append(dict(tab=tab, n=n, src=src3, length=3, sstride=3, soff=0, dstride=3,
-                         doff=0, diag=diag))
-        jobs.append(dict(tab=tab, n=n, src=z["src8"], length=5, sstride=8, soff=2, dstride=7,
-                         doff=1, diag=diag))
+        host_tab = [z[k] for k in ("sizes", "offsets", "indices", "weights")]
+        jobs.append(dict(tab=tab, host_tab=host_tab, n=n, src=src3, length=3, sstride=3, soff=0,
+                         dstride=3, doff=0, diag=diag))
+        jobs.append(dict(tab=tab, host_tab=host_tab, n=n, src=z["src8"], length=5, sstride=8,
+                         soff=2, dstride=7, doff=1, diag=diag))
     return jobs
 
 
@@ -68,8 +71,9 @@ def test_no_alloc_batch_matches_existing_entry_point_twice():
     rng = np.random.default_rng(17)
     for call in range(2):
         # new source values for every call, so the second call must recompute everything
-        srcs = [dev((j["src"] * (1.0 + 0.1 * call) + 0.01 * call).astype(np.float32))
-                for j in jobs]
+        hsrcs = [(j["src"] * (1.0 + 0.1 * call) + 0.01 * call).astype(np.float32)
+                 for j in jobs]
+        srcs = [dev(h) for h in hsrcs]
         dsts = [torch.full((j["n"] * j["dstride"],), float(rng.integers(2, 9)), device="cuda")
                 for j in jobs]
         refs = [d.clone() for d in dsts]
@@ -91,6 +95,15 @@ def test_no_alloc_batch_matches_existing_entry_point_twice():
             keep = np.ones(j["dstride"], bool)
             keep[j["doff"]:j["doff"] + j["length"]] = False
             assert np.array_equal(gg[:, keep], ee[:, keep])
+            # and the oracle on the same inputs
+            o = np.zeros(j["n"] * j["length"], np.float32)
+            assert oracle.eval_stencils(hsrcs[k], (j["soff"], j["length"], j["sstride"]), [o],
+                                        [(0, j["length"], j["length"])], *j["host_tab"][:3],
+                                        [j["host_tab"][3]], threads=4)
+            got = gg[:, j["doff"]:j["doff"] + j["length"]].ravel()
+            assert max_err(got, o) <= tol, f"call {call} job {k} vs oracle"
+        # no bounded wait expired inside either call
+        assert lib.GB300GetDeviceStatus() == 0, _lib.last_error()
 
 
 @pytest.mark.gpu
