@@ -69,19 +69,53 @@ def parse():
     return ap.parse_args()
 
 
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+# the EvalPatches tables: the reference's own adaptive level-4 tables of the full-size cages
+# (written by tests/golden/make_golden.py large where the reference is available) or, when
+# they are absent, stand-ins of their size instanced from the small fixtures
+PATCH_TABLES = {
+    False: ("torus512x256_adaptiveL4.npz", "torus512x256_adaptiveL4_gregory",
+            "torus32x16_patches_L4.npz", 1_431_592, None, 7),
+    True: ("icosphere6_loop_adaptiveL4.npz", "icosphere6_loop_adaptiveL4",
+           "icosphere2_patches_L3.npz", 82_580, 5, 8),
+}
+
+
+def patch_workload(n_points, loop=False):
+    from opensubdiv_gb300 import workloads
+    large, name, small, target, count_type, seed = PATCH_TABLES[loop]
+    path = os.path.join(GOLDEN, "large", large)
+    if os.path.exists(path):
+        w = workloads.eval_patches_points(np.load(path), name, n_points, seed)
+        w["table_source"] = "the reference's own Far::PatchTableFactory table of the cage"
+        return w
+    w = workloads.instanced_points(np.load(os.path.join(GOLDEN, small)),
+                                   "standin_" + small[:-4], target, n_points, seed, count_type)
+    w["table_source"] = (f"stand-in: {small} instanced {w['copies']}x to the full table's "
+                         "size (the full-size table was not generated where build() ran)")
+    return w
+
+
+def serving_bases():
+    from opensubdiv_gb300 import shapes, workloads
+    return {shapes.CATMARK: workloads.ServingBase(
+                np.load(os.path.join(GOLDEN, "torus32x16_patches_L4.npz"))),
+            shapes.LOOP: workloads.ServingBase(
+                np.load(os.path.join(GOLDEN, "icosphere2_patches_L3.npz")))}
+
+
 def bench_patches(args, stream, peak, loop=False):
     """Secondary measurement: device PatchMap lookup + EvalPatches (P and all five
-    derivatives) at 4M uniform points on a table of the 512 x 256 torus's adaptive level-4
-    size (workloads.eval_patches_torus) or, with `loop`, of the level-6 icosphere's adaptive
-    Loop table (workloads.eval_patches_icosphere)."""
+    derivatives) at 4M uniform points on the 512 x 256 torus's adaptive level-4 table with
+    Gregory-basis end caps or, with `loop`, the level-6 icosphere's adaptive Loop table
+    (patch_workload)."""
     import torch
 
     from opensubdiv_gb300 import workloads
     from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
                                             GB300PatchTable)
 
-    w = (workloads.eval_patches_icosphere if loop else workloads.eval_patches_torus)(
-        args.patch_points)
+    w = patch_workload(args.patch_points, loop)
     n = len(w["face"])
     table = GB300PatchTable.Create(w["arrays"], w["indices"], w["params"], w["triangular"])
     src = torch.from_numpy(w["src"]).cuda()
@@ -129,7 +163,8 @@ def bench_patches(args, stream, peak, loop=False):
     oracle.eval_patches(w["src"], (0, 3, 3), ref, [(0, 3, 3)] * 6, ch, w["arrays"],
                         w["indices"], w["params"], threads=8)
     err_p = float(np.abs(outs[0][: k * 3].cpu().numpy() - ref[0]).max())
-    return {"workload": w["name"], "points": n, "patch_evals_per_s": n / ((find_ms + eval_ms) / 1e3),
+    return {"workload": w["name"], "table": w["table_source"], "points": n,
+            "patch_arrays": w["arrays"].tolist(), "source_points": len(w["src"]) // 3, "patch_evals_per_s": n / ((find_ms + eval_ms) / 1e3),
             "find_patches_ms": find_ms, "eval_patches_ms": eval_ms, "outputs": 6,
             "patches_touched": touched,
             "roofline": {"bound": "hbm", "kernel": "k_eval_patches (P + 5 derivatives)",
@@ -267,7 +302,7 @@ def bench_serving(args):
     from opensubdiv_gb300.server import LIMIT, REFINE, GB300Server
 
     t0 = time.time()
-    pool = workloads.serving_pool(n_topologies=args.serve_topologies,
+    pool = workloads.serving_pool(serving_bases(), n_topologies=args.serve_topologies,
                                   cv_max=args.batch_cv_max)
     gen_s = time.time() - t0
     rng = np.random.default_rng(31337)
@@ -750,7 +785,7 @@ def reference_cuda(args, w):
            "stencils_per_s": (n_ref + n_lim) / ((refine_ms + limit_ms) / 1e3)}
     if not args.no_patches:
         from opensubdiv_gb300 import workloads
-        pw = workloads.eval_patches_torus(args.patch_points)
+        pw = patch_workload(args.patch_points)
         handles = oracle.PatchMap(pw["arrays"], pw["params"], pw["triangular"]).find(
             pw["face"], pw["u"], pw["v"])
         coords = dev(oracle.make_coords(handles, pw["u"], pw["v"]))

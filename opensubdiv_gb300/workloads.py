@@ -42,12 +42,13 @@ def refine_and_limit_torus(nu=512, nv=256, level=3, n_limit=1_000_000, length=8,
                 limit=limit, level=level)
 
 
-def instanced_patch_table(fixture, copies):
-    """`copies` disjoint instances of a flattened Far patch table (Osd::CpuPatchTable layout)
-    stored in a fixture: arrays stay grouped by patch type, every copy's control indices are
-    offset by the source size and its ptex faces by the ptex count.  Returns arrays, indices,
-    params, the source points (copy c displaced by c along x) and the ptex face count."""
-    z = np.load(fixture)
+def instanced_patch_table(table, copies):
+    """`copies` disjoint instances of a flattened Far patch table (Osd::CpuPatchTable layout;
+    `table` maps arrays, patch_indices, params, src, num_ptex, triangular to arrays): arrays
+    stay grouped by patch type, every copy's control indices are offset by the source size and
+    its ptex faces by the ptex count.  Returns arrays, indices, params, the source points (copy
+    c displaced by 3c along x), the ptex face count and whether the table is triangular."""
+    z = table
     arr, idx, par, src = z["arrays"], z["patch_indices"], z["params"], z["src"].reshape(-1, 3)
     nsrc, nptex = len(src), int(z["num_ptex"])
     arrays, indices, params = [], [], []
@@ -73,49 +74,38 @@ def instanced_patch_table(fixture, copies):
             nptex * copies, bool(z["triangular"]))
 
 
-def eval_patches_torus(n_points=4_000_000, target_patches=1_284_866, seed=7):
-    """EvalPatches workload at the size of the 512 x 256 torus's adaptive level-4 table with
-    Gregory-basis end caps (1,181,550 regular + 103,316 Gregory patches, 5.42M source points):
-    the reference's own adaptive level-4 Gregory-basis table of the 32 x 16 triangle/crease
-    torus (tests/golden/torus32x16_patches_L4.npz), instanced to that patch count, evaluated
-    at n_points uniform (ptex face, u, v) locations."""
-    import os
-    fixture = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
-                           "tests", "golden", "torus32x16_patches_L4.npz")
-    per = int(np.load(fixture)["arrays"][:, 2].sum())
+def eval_patches_points(table, name, n_points=4_000_000, seed=7):
+    """EvalPatches workload over a flattened Far patch table (a mapping with arrays,
+    patch_indices, params, src, num_ptex, triangular): n_points uniform (ptex face, u, v)
+    locations, folded into the triangle (u + v <= 1) for triangular tables."""
+    tri = bool(table["triangular"])
+    nptex = int(table["num_ptex"])
+    rng = np.random.default_rng(seed)
+    face = rng.integers(0, nptex, n_points).astype(np.int32)
+    u = rng.random(n_points).astype(np.float32)
+    v = rng.random(n_points).astype(np.float32)
+    if tri:
+        fold = u + v > 1.0
+        u[fold], v[fold] = 1.0 - u[fold], 1.0 - v[fold]
+    return dict(name=f"{name}_{n_points / 1e6:g}Mpts", arrays=np.asarray(table["arrays"]),
+                indices=np.asarray(table["patch_indices"]), params=np.asarray(table["params"]),
+                src=np.ascontiguousarray(table["src"], np.float32), length=3, num_ptex=nptex,
+                triangular=tri, face=face, u=u, v=v)
+
+
+def instanced_points(table, name, target_patches, n_points=4_000_000, seed=7,
+                     count_type=None):
+    """eval_patches_points over `table` instanced to `target_patches` patches (of type
+    `count_type` only, when given): a stand-in of a large table's size built from a small one."""
+    arr = np.asarray(table["arrays"])
+    per = int(arr[:, 2].sum() if count_type is None else arr[arr[:, 0] == count_type, 2].sum())
     copies = max(1, round(target_patches / per))
-    arrays, indices, params, src, nptex, tri = instanced_patch_table(fixture, copies)
-    rng = np.random.default_rng(seed)
-    face = rng.integers(0, nptex, n_points).astype(np.int32)
-    u = rng.random(n_points).astype(np.float32)
-    v = rng.random(n_points).astype(np.float32)
-    return dict(name=f"torus32x16_adaptiveL4_gregory_x{copies}_{n_points // 1000000}Mpts",
-                arrays=arrays, indices=indices, params=params, src=src, length=3,
-                num_ptex=nptex, triangular=tri, face=face, u=u, v=v, copies=copies)
-
-
-def eval_patches_icosphere(n_points=4_000_000, target_loop_patches=82_580, seed=8):
-    """EvalPatches workload at the size of the level-6 icosphere's adaptive Loop table
-    (82,580 LOOP patches): the reference's own adaptive level-3 Loop table of the level-2
-    icosphere (tests/golden/icosphere2_patches_L3.npz: LOOP + GREGORY_TRIANGLE end caps),
-    instanced to that LOOP patch count, evaluated at n_points uniform (ptex face, u, v)
-    locations folded into the triangle (u + v <= 1)."""
-    import os
-    fixture = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
-                           "tests", "golden", "icosphere2_patches_L3.npz")
-    arr = np.load(fixture)["arrays"]
-    per_loop = int(arr[arr[:, 0] == 5, 2].sum())
-    copies = max(1, round(target_loop_patches / per_loop))
-    arrays, indices, params, src, nptex, tri = instanced_patch_table(fixture, copies)
-    rng = np.random.default_rng(seed)
-    face = rng.integers(0, nptex, n_points).astype(np.int32)
-    u = rng.random(n_points).astype(np.float32)
-    v = rng.random(n_points).astype(np.float32)
-    fold = u + v > 1.0
-    u[fold], v[fold] = 1.0 - u[fold], 1.0 - v[fold]
-    return dict(name=f"icosphere2_adaptiveL3_loop_x{copies}_{n_points // 1000000}Mpts",
-                arrays=arrays, indices=indices, params=params, src=src, length=3,
-                num_ptex=nptex, triangular=tri, face=face, u=u, v=v, copies=copies)
+    arrays, indices, params, src, nptex, tri = instanced_patch_table(table, copies)
+    w = eval_patches_points(dict(arrays=arrays, patch_indices=indices, params=params, src=src,
+                                 num_ptex=nptex, triangular=tri), f"{name}_x{copies}",
+                            n_points, seed)
+    w["copies"] = copies
+    return w
 
 
 def patch_bytes(n_points, length, n_outputs, n_src, touched_patches, cvs_per_patch):
@@ -193,15 +183,6 @@ def deform(base, phase, frame, amplitude=0.01):
 
 # ---- serving pool ----------------------------------------------------------------------------
 
-SERVING_BASES = {shapes.CATMARK: "torus32x16_patches_L4.npz", shapes.LOOP: "icosphere2_patches_L3.npz"}
-
-
-def _golden(name):
-    import os
-    return os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests",
-                        "golden", name)
-
-
 def sort_entries(table):
     """Far-layout table with every stencil's entries in ascending control-index order (the
     device layout GB300StencilTableCreate uses; same stencils, better gather locality)."""
@@ -230,14 +211,16 @@ def instance_table(table, copies, src_per_copy):
 
 
 class ServingBase:
-    """One base shape of the serving pool: the reference's adaptive patch table of a small
-    cage (tests/golden fixture) with its patch points' stencils over the cage, and uniform
-    refinement tables of the same cage from the native generator (one per level, cached)."""
+    """One base shape of the serving pool: an adaptive patch table of a small cage (a mapping
+    with the cage -- positions, verts_per_face, face_verts, scheme, crease_verts,
+    crease_sharpness -- the flattened Far patch table and its patch points' stencils over the
+    cage: ps_sizes, ps_offsets, ps_indices, ps_weights), and uniform refinement tables of the
+    same cage from the native generator (one per level, cached)."""
 
-    def __init__(self, scheme):
-        z = np.load(_golden(SERVING_BASES[scheme]))
-        self.scheme = scheme
-        self.fixture = _golden(SERVING_BASES[scheme])
+    def __init__(self, z):
+        self.scheme = int(z["scheme"])
+        self.table = {k: np.asarray(z[k]) for k in ("arrays", "patch_indices", "params", "src",
+                                                     "num_ptex", "triangular")}
         self.cage = shapes.Cage(z["positions"], z["verts_per_face"], z["face_verts"],
                                 scheme=int(z["scheme"]), name=f"base{int(z['scheme'])}")
         self.cage.crease_verts = z["crease_verts"]
@@ -262,23 +245,22 @@ class ServingBase:
 
     def patch_table(self, copies):
         if copies not in self._patch:
-            arrays, indices, params, _, nptex, tri = instanced_patch_table(self.fixture, copies)
+            arrays, indices, params, _, nptex, tri = instanced_patch_table(self.table, copies)
             self._patch[copies] = (arrays, indices, params, nptex)
         return self._patch[copies]
 
 
-def serving_pool(n_topologies=1000, cv_min=500, cv_max=25_000, seed=5150):
+def serving_pool(bases, n_topologies=1000, cv_min=500, cv_max=25_000, seed=5150):
     """Topologies for the serving loop, drawn like the batching population: CV counts
     log-uniform in [cv_min, cv_max], 70% Catmull-Clark / 30% Loop, uniform refinement level
     uniform in {1..4}, 3-12 float32 primvars.  Topology = `copies` instances of a base cage
-    (ServingBase: the 512-CV crease/triangle torus for Catmull-Clark, the 162-CV icosphere for
-    Loop) with copies = CV target / base CVs rounded to a log-spaced set (so host tables are
-    shared between topologies of the same (base, copies, level); every topology still has its
-    own device copy when resident).  Each has a refine table at its level and limit tables
-    (patch points as stencils over the cage's xyz + the instanced adaptive patch table)."""
+    (`bases`: {shapes.CATMARK: ServingBase, shapes.LOOP: ServingBase}) with copies = CV
+    target / base CVs rounded to a log-spaced set (so host tables are shared between
+    topologies of the same (base, copies, level); every topology still has its own device copy
+    when resident).  Each has a refine table at its level and limit tables (patch points as
+    stencils over the cage's xyz + the instanced adaptive patch table)."""
     rng = np.random.default_rng(seed)
     steps = np.array([1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 192], np.int64)
-    bases = {s: ServingBase(s) for s in SERVING_BASES}
     cache = {}
     pool = []
     for t in range(n_topologies):

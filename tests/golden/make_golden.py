@@ -289,7 +289,54 @@ def factory_limit_fixture(path):
     np.savez_compressed(path, **out)
 
 
+LARGE = os.path.join(HERE, "large")
+
+
+def large_patch_workload(path, cage, level):
+    """A full-size EvalPatches workload from the reference's own Far: the adaptive patch table
+    (isolation `level`, Gregory-basis end caps) flattened as Osd::CpuPatchTable, and the source
+    buffer [cage points; refined points of every level; local points] computed with
+    Osd::CpuEvaluator from Far's stencils.  Too large to commit: written under large/ (kept
+    out of git) where the reference is available, for the benchmark and the full-size GPU
+    parity test."""
+    r = ref.Refiner(cage)
+    r.refine_adaptive(level)
+    p = ref.Patches(r, endcap=3, max_isolation=level)
+    nc = cage.num_vertices
+    ns = len(p.st["sizes"])
+    buf = np.zeros((nc + ns) * 3, np.float32)
+    buf[: nc * 3] = cage.positions.reshape(-1)
+    ref.omp_set_threads(os.cpu_count() or 1)
+    assert ref.cpu_eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], p.st["sizes"],
+                                 p.st["offsets"], p.st["indices"], [p.st["weights"]], 0, ns,
+                                 omp=True)
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp.npz"
+    np.savez_compressed(tmp, positions=cage.positions, level=np.int32(level), arrays=p.arrays,
+             patch_indices=p.indices, params=p.params, src=buf,
+             num_ptex=np.int32(r.num_ptex_faces()),
+             triangular=np.int32(cage.scheme == shapes.LOOP))
+    os.replace(tmp, path)
+
+
+def large_workloads():
+    """The EvalPatches benchmark tables: the plain-method torus (512 x 256, R = 1, r = 0.3,
+    seeded 5% triangles and 2% creases U[0, 4]; the cage of the stencil benchmark) and the
+    Loop icosphere subdivided 6 times (40,962 points, N(0, 0.005) noise), both at adaptive
+    isolation level 4 with Gregory-basis end caps."""
+    torus = shapes.torus(512, 256, R=1.0, r=0.3, tri_fraction=0.05, crease_fraction=0.02,
+                         max_sharpness=4.0, seed=2024)
+    large_patch_workload(os.path.join(LARGE, "torus512x256_adaptiveL4.npz"), torus, 4)
+    ico = shapes.icosphere(6, noise=0.005, seed=3)
+    large_patch_workload(os.path.join(LARGE, "icosphere6_loop_adaptiveL4.npz"), ico, 4)
+
+
 def main():
+    if len(sys.argv) > 1 and sys.argv[1] == "large":
+        if not ref.available():
+            raise SystemExit("oracle/_ref/libosdref.so missing: run `make -C oracle ref` first")
+        large_workloads()
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "factory":
         factory_fixture(os.path.join(HERE, "factory_masks.npz"))
         factory_limit_fixture(os.path.join(HERE, "factory_limit.npz"))

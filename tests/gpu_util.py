@@ -100,3 +100,14 @@ def smooth_primvars(xyz, width=8, lane=2):
             out[:, c] = extra[j % len(extra)]
             j += 1
     return out
+
+
+def serving_bases():
+    """The serving pool's base shapes from the fixtures (the reference's adaptive tables of the
+    32 x 16 torus and the level-2 icosphere)."""
+    import os
+
+    from opensubdiv_gb300 import shapes, workloads
+    g = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+    return {shapes.CATMARK: workloads.ServingBase(np.load(os.path.join(g, "torus32x16_patches_L4.npz"))),
+            shapes.LOOP: workloads.ServingBase(np.load(os.path.join(g, "icosphere2_patches_L3.npz")))}

@@ -133,7 +133,7 @@ def test_large_random_request_on_instanced_table():
     from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300Evaluator as Ev
     from opensubdiv_gb300.evaluator import GB300PatchTable
     fixture = os.path.join(GOLDEN, "torus32x16_patches_L4.npz")
-    arrays, indices, params, src, nptex, tri = workloads.instanced_patch_table(fixture, 12)
+    arrays, indices, params, src, nptex, tri = workloads.instanced_patch_table(np.load(fixture), 12)
     assert arrays[:, 2].sum() >= 1 << 16
     t = GB300PatchTable.Create(arrays, indices, params, tri)
     n = 300_000

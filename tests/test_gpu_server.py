@@ -13,14 +13,14 @@ import numpy as np
 import pytest
 
 import oracle
-from gpu_util import torch_cuda
+from gpu_util import serving_bases, torch_cuda
 
 N_POINTS = 4000
 
 
 def _pool():
     from opensubdiv_gb300 import workloads
-    return workloads.serving_pool(n_topologies=8, cv_min=400, cv_max=4000, seed=99)
+    return workloads.serving_pool(serving_bases(), n_topologies=8, cv_min=400, cv_max=4000, seed=99)
 
 
 def _work(pool):

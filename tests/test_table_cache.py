@@ -6,11 +6,13 @@ import os
 import numpy as np
 import pytest
 
+from gpu_util import serving_bases
+
 
 @pytest.fixture(scope="module")
 def topo():
     from opensubdiv_gb300 import workloads
-    return workloads.serving_pool(n_topologies=2, cv_min=400, cv_max=1500, seed=77)[1]
+    return workloads.serving_pool(serving_bases(), n_topologies=2, cv_min=400, cv_max=1500, seed=77)[1]
 
 
 def _write(tmp_path, t, limit=True):
