@@ -81,6 +81,23 @@ PATCH_TABLES = {
 }
 
 
+def fp32_rate(stream):
+    """Measured FP32 FMA rate of this GPU in TFLOP/s (GB300MeasureFp32Rate, once per run)."""
+    global _FP32
+    if _FP32 is None:
+        import ctypes
+
+        from opensubdiv_gb300 import _lib
+        v = ctypes.c_double(0.0)
+        _lib.check(_lib.load().GB300MeasureFp32Rate(ctypes.byref(v),
+                                                      ctypes.c_void_p(stream.cuda_stream)))
+        _FP32 = v.value
+    return _FP32
+
+
+_FP32 = None
+
+
 def patch_workload(n_points, loop=False):
     from opensubdiv_gb300 import workloads
     large, name, small, target, count_type, seed = PATCH_TABLES[loop]
@@ -139,6 +156,7 @@ def bench_patches(args, stream, peak, loop=False):
         if ev:
             ev[2].record(stream)
 
+    fp32_peak = fp32_rate(stream)
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -150,10 +168,14 @@ def bench_patches(args, stream, peak, loop=False):
     torch.cuda.synchronize()
     find_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
     eval_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
-    c = coords.view(n, 5)[:, 1].cpu().numpy()
+    ch_all = coords.view(n, 5).cpu().numpy()
+    c = ch_all[:, 1]
     touched = int(len(np.unique(c[c >= 0])))
     cvs = float(np.average(w["arrays"][:, 4], weights=w["arrays"][:, 2]))
     b = workloads.patch_bytes(n, 3, 6, len(w["src"]) // 3, touched, cvs)
+    types = workloads.point_types(ch_all, w["arrays"], w["params"])
+    flops = workloads.patch_flops(types, 3)
+    gathered = workloads.patch_gathered_bytes(types, 3, 6)
     # spot check against the oracle on a slice (outside timing)
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
@@ -171,7 +193,16 @@ def bench_patches(args, stream, peak, loop=False):
                          "algorithmic_bytes": b, "achieved": b / (eval_ms / 1e3) / 1e9,
                          "peak": peak, "unit": "GB/s",
                          "frac": b / (eval_ms / 1e3) / 1e9 / peak,
-                         "traffic": ncu_traffic("patches_loop" if loop else "patches")},
+                         "traffic": ncu_traffic("patches_loop" if loop else "patches"),
+                         "as_gathered_bytes": gathered,
+                         "as_gathered_gbs": gathered / (eval_ms / 1e3) / 1e9,
+                         "fp32": {"flops_per_launch": flops,
+                                  "achieved_tflops": flops / (eval_ms / 1e3) / 1e12,
+                                  "peak_tflops": fp32_peak,
+                                  "frac": flops / (eval_ms / 1e3) / 1e12 / fp32_peak,
+                                  "peak_kind": "measured (GB300MeasureFp32Rate)"},
+                         "point_types": {str(t): int((types == t).sum())
+                                         for t in np.unique(types)}},
             "max_abs_err_P_vs_oracle_slice": err_p}
 
 

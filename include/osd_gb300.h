@@ -457,6 +457,13 @@ int GB300EvalStencilsBatchedNoAlloc(int numJobs, const float *const *src, float 
  * left its outputs incomplete).  Synchronises the device. */
 int GB300GetDeviceStatus(void);
 
+/* ---- measurement (no counterpart in the reference) ---------------------------------------- */
+
+/* Times a compute-only FP32 fused multiply-add kernel on `stream` (one full-occupancy wave,
+ * 5 timed launches after a warm-up, CUDA events) and writes the rate in TFLOP/s (an FMA counts
+ * as 2).  The compute denominator of the EvalPatches roofline. */
+int GB300MeasureFp32Rate(double *tflops, void *stream);
+
 /* ---- kernel accounting -------------------------------------------------------------------- */
 
 /* Number of this library's kernels launched since load (for launch-count reporting). */

@@ -24,6 +24,7 @@ _PROTOS = {
     "GB300Synchronize": (i32, [vp]),
     "GB300GetLaunchCount": (u64, []),
     "GB300GetDeviceStatus": (i32, []),
+    "GB300MeasureFp32Rate": (i32, [C.POINTER(C.c_double), vp]),
     "GB300EvalStencils": (i32, [vp, vp, i32, i32, i32, vp, vp, vp, vp, i32, i32, vp]),
     "GB300EvalStencilsWithDerivatives": (
         i32, [vp] * 7 + [i32] * 8 + [vp] * 3 + [vp] * 6 + [i32, i32, vp]),

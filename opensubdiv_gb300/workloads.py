@@ -108,6 +108,56 @@ def instanced_points(table, name, target_patches, n_points=4_000_000, seed=7,
     return w
 
 
+# FP32 operations of one EvalPatches point with all six outputs, per basis (an FMA counts 2),
+# counted from the kernels' arithmetic in csrc/patch_basis.cuh: (weights, per primvar element).
+#   REGULAR: two cubic B-spline curves (value, d, dd) ~66 + normalisation 4; per element 16
+#     local-origin subtractions, 4 rows x (3 x 4 FMA row sums + 6 FMA accumulations), the
+#     origin added back, 6 derivative scales: 16 + 144 + 1 + 6.
+#   GREGORY_BASIS: two cubic Bezier curves ~50, 4 rational blend weights ~16; per element 20
+#     subtractions, 4 blended pairs x 4, the same 4 x 36 row sums, origin, scales: 20+16+144+7.
+#   LOOP: 12 monomials, 351 non-zero box-spline coefficients x 2, 48 constant scales; per
+#     element 12 subtractions, 6 x 12 FMA, origin, scales: 12 + 144 + 7.
+#   GREGORY_TRIANGLE: 3 blend pairs ~20, 6 quartic Bezier-triangle weight sets ~270; per element
+#     18 subtractions, 3 blends x 3, 6 x 15 FMA, origin, scales: 18 + 9 + 180 + 7.
+#   QUADS / TRIANGLES: bilinear / linear weights and 4 / 3 rows.
+PATCH_FLOPS = {6: (70, 167), 9: (66, 187), 5: (762, 163), 10: (290, 214), 3: (10, 27),
+               4: (4, 14)}
+PATCH_CVS = {6: 16, 9: 20, 5: 12, 10: 18, 3: 4, 4: 3}
+
+
+def point_types(coords, arrays, params):
+    """Basis type of every evaluated point (-1 for PatchMap misses): the array's regular
+    descriptor when the patch's param marks it regular, its irregular descriptor otherwise."""
+    c = np.asarray(coords).reshape(-1, 5)
+    arrays = np.asarray(arrays).reshape(-1, 6)
+    params = np.asarray(params).reshape(-1, 3)
+    hit = c[:, 0] >= 0
+    t = np.full(len(c), -1, np.int64)
+    ai, pi = c[hit, 0], c[hit, 1]
+    regular = (params[pi, 1] >> 5) & 1
+    t[hit] = np.where(regular == 1, arrays[ai, 0], arrays[ai, 1])
+    return t
+
+
+def patch_flops(types, length):
+    """FP32 operations of one EvalPatches pass with all six outputs (PATCH_FLOPS)."""
+    total = 0
+    for ty, (w, e) in PATCH_FLOPS.items():
+        total += int((types == ty).sum()) * (w + e * length)
+    return total
+
+
+def patch_gathered_bytes(types, length, n_outputs):
+    """As-gathered bytes of one EvalPatches pass: every point's coord (20 B), array record
+    (24 B), param (12 B), index row (4 B per control point), every control point row it
+    reads (4 B x length each, re-reads counted) and its outputs."""
+    total = 0
+    for ty, ncv in PATCH_CVS.items():
+        k = int((types == ty).sum())
+        total += k * (20 + 24 + 12 + 4 * ncv + 4 * length * ncv + 4 * length * n_outputs)
+    return total
+
+
 def patch_bytes(n_points, length, n_outputs, n_src, touched_patches, cvs_per_patch):
     """Unique-bytes model of one EvalPatches pass: coords (20 B per point), outputs
     (4 B x length x outputs per point), touched patches' index rows and params

@@ -13,7 +13,7 @@ HEADER = os.path.join(ROOT, "include", "osd_gb300.h")
 def declared_functions():
     text = open(HEADER).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(GB300[A-Za-z]+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(GB300[A-Za-z0-9]+)\s*\(", text)))
 
 
 def test_header_and_python_bindings_agree():
