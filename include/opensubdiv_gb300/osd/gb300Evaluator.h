@@ -334,37 +334,55 @@ public:
             gb300_detail::stream_of(deviceContext)));
     }
 
-    // ---- EvalStencils over a device table (template forms, cudaEvaluator.h:125-142) ----------
-    template <typename SRC_BUFFER, typename DST_BUFFER>
+    // ---- EvalStencils over a stencil table (template forms, cudaEvaluator.h:125-142,
+    // 219-249, 352-375).  STENCIL_TABLE: GB300StencilTable (evaluated through its own device
+    // layout) or any type with CudaStencilTable's accessors (GetSizesBuffer ... GetDvvWeights-
+    // Buffer, GetNumStencils), evaluated through the raw entry points over those buffers. ----
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename STENCIL_TABLE>
     static bool EvalStencils(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
                              DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                             GB300StencilTable const *table, const void *instance = NULL,
+                             STENCIL_TABLE const *stencilTable, const void *instance = NULL,
                              void *deviceContext = NULL) {
         (void)instance;
-        if (srcDesc.length != dstDesc.length) return false;
-        return gb300_detail::ok(GB300StencilTableEval(
-            table->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
-            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
-            gb300_detail::stream_of(deviceContext)));
+        float *o[6] = {dstBuffer->BindCudaBuffer(), 0, 0, 0, 0, 0};
+        BufferDescriptor const *d[6] = {&dstDesc, &srcDesc, &srcDesc, &srcDesc, &srcDesc,
+                                        &srcDesc};
+        return stencils_over(stencilTable, srcBuffer->BindCudaBuffer(), srcDesc, o, d,
+                             deviceContext);
     }
-    template <typename SRC_BUFFER, typename DST_BUFFER>
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename STENCIL_TABLE>
     static bool EvalStencils(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
                              DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
                              DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
                              DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
-                             GB300StencilTable const *table, const void *instance = NULL,
-                             void *deviceContext = NULL) {
+                             STENCIL_TABLE const *stencilTable,
+                             GB300Evaluator const *instance = NULL, void *deviceContext = NULL) {
         (void)instance;
-        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
-            srcDesc.length != dvDesc.length)
-            return false;
-        return gb300_detail::ok(GB300StencilTableEval(
-            table->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset,
-            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
-            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
-            duDesc.stride, dvDesc.stride, 0, 0, 0, gb300_detail::stream_of(deviceContext)));
+        float *o[6] = {dstBuffer->BindCudaBuffer(), duBuffer->BindCudaBuffer(),
+                       dvBuffer->BindCudaBuffer(), 0, 0, 0};
+        BufferDescriptor const *d[6] = {&dstDesc, &duDesc, &dvDesc, &srcDesc, &srcDesc,
+                                        &srcDesc};
+        return stencils_over(stencilTable, srcBuffer->BindCudaBuffer(), srcDesc, o, d,
+                             deviceContext);
+    }
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename STENCIL_TABLE>
+    static bool EvalStencils(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
+                             DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
+                             DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
+                             DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
+                             DST_BUFFER *duuBuffer, BufferDescriptor const &duuDesc,
+                             DST_BUFFER *duvBuffer, BufferDescriptor const &duvDesc,
+                             DST_BUFFER *dvvBuffer, BufferDescriptor const &dvvDesc,
+                             STENCIL_TABLE const *stencilTable,
+                             GB300Evaluator const *instance = NULL, void *deviceContext = NULL) {
+        (void)instance;
+        float *o[6] = {dstBuffer->BindCudaBuffer(), duBuffer->BindCudaBuffer(),
+                       dvBuffer->BindCudaBuffer(), duuBuffer->BindCudaBuffer(),
+                       duvBuffer->BindCudaBuffer(), dvvBuffer->BindCudaBuffer()};
+        BufferDescriptor const *d[6] = {&dstDesc, &duDesc, &dvDesc, &duuDesc, &duvDesc,
+                                        &dvvDesc};
+        return stencils_over(stencilTable, srcBuffer->BindCudaBuffer(), srcDesc, o, d,
+                             deviceContext);
     }
 
     // ---- EvalPatches, raw device pointers (cudaEvaluator.cpp:295-372) -----------------------
@@ -416,120 +434,157 @@ public:
             patchIndices, patchParams, gb300_detail::stream_of(deviceContext)));
     }
 
-    // ---- EvalPatches over a device table (template forms, cudaEvaluator.h:502-525) ----------
-    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
-    static bool EvalPatches(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
-                            DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                            int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
-                            GB300PatchTable const *patchTable, const void *instance = NULL,
-                            void *deviceContext = NULL) {
-        (void)instance;
-        if (srcDesc.length != dstDesc.length) return false;
-        return gb300_detail::ok(GB300PatchTableEval(
-            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
-            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
-            numPatchCoords, (const void *)patchCoords->BindCudaBuffer(),
-            gb300_detail::stream_of(deviceContext)));
+    // ---- EvalPatches / EvalPatchesVarying / EvalPatchesFaceVarying over a patch table
+    // (template forms, cudaEvaluator.h:502-680, 857-1255).  PATCH_TABLE: GB300PatchTable, or
+    // any type with CudaPatchTable's accessors (GetPatchArrayBuffer, GetPatchIndexBuffer,
+    // GetPatchParamBuffer, the varying and face-varying ones), evaluated through the raw
+    // entry points over those buffers.  PATCHCOORD_BUFFER: any type whose BindCudaBuffer()
+    // returns device PatchCoords. ----
+#define OSD_GB300_PATCH_FORMS(NAME, KIND, CH_PARAM, CH_ARG)                                     \
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER,            \
+              typename PATCH_TABLE>                                                             \
+    static bool NAME(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,                   \
+                     DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,                   \
+                     int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,                       \
+                     PATCH_TABLE *patchTable CH_PARAM, const void *instance = NULL,            \
+                     void *deviceContext = NULL) {                                             \
+        (void)instance;                                                                         \
+        float *o[6] = {dstBuffer->BindCudaBuffer(), 0, 0, 0, 0, 0};                            \
+        BufferDescriptor const *d[6] = {&dstDesc, &srcDesc, &srcDesc, &srcDesc, &srcDesc,      \
+                                        &srcDesc};                                              \
+        return patches_over(patchTable, KIND, CH_ARG, srcBuffer->BindCudaBuffer(), srcDesc, o, \
+                            d, numPatchCoords, patchCoords->BindCudaBuffer(), deviceContext);  \
+    }                                                                                           \
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER,            \
+              typename PATCH_TABLE>                                                             \
+    static bool NAME(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,                   \
+                     DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,                   \
+                     DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,                     \
+                     DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,                     \
+                     int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,                       \
+                     PATCH_TABLE *patchTable CH_PARAM, GB300Evaluator const *instance = NULL,  \
+                     void *deviceContext = NULL) {                                             \
+        (void)instance;                                                                         \
+        float *o[6] = {dstBuffer->BindCudaBuffer(), duBuffer->BindCudaBuffer(),                \
+                       dvBuffer->BindCudaBuffer(), 0, 0, 0};                                    \
+        BufferDescriptor const *d[6] = {&dstDesc, &duDesc, &dvDesc, &srcDesc, &srcDesc,        \
+                                        &srcDesc};                                              \
+        return patches_over(patchTable, KIND, CH_ARG, srcBuffer->BindCudaBuffer(), srcDesc, o, \
+                            d, numPatchCoords, patchCoords->BindCudaBuffer(), deviceContext);  \
+    }                                                                                           \
+    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER,            \
+              typename PATCH_TABLE>                                                             \
+    static bool NAME(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,                   \
+                     DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,                   \
+                     DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,                     \
+                     DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,                     \
+                     DST_BUFFER *duuBuffer, BufferDescriptor const &duuDesc,                   \
+                     DST_BUFFER *duvBuffer, BufferDescriptor const &duvDesc,                   \
+                     DST_BUFFER *dvvBuffer, BufferDescriptor const &dvvDesc,                   \
+                     int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,                       \
+                     PATCH_TABLE *patchTable CH_PARAM, GB300Evaluator const *instance = NULL,  \
+                     void *deviceContext = NULL) {                                             \
+        (void)instance;                                                                         \
+        float *o[6] = {dstBuffer->BindCudaBuffer(), duBuffer->BindCudaBuffer(),                \
+                       dvBuffer->BindCudaBuffer(), duuBuffer->BindCudaBuffer(),                \
+                       duvBuffer->BindCudaBuffer(), dvvBuffer->BindCudaBuffer()};              \
+        BufferDescriptor const *d[6] = {&dstDesc, &duDesc, &dvDesc, &duuDesc, &duvDesc,        \
+                                        &dvvDesc};                                              \
+        return patches_over(patchTable, KIND, CH_ARG, srcBuffer->BindCudaBuffer(), srcDesc, o, \
+                            d, numPatchCoords, patchCoords->BindCudaBuffer(), deviceContext);  \
     }
-    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
-    static bool EvalPatches(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
-                            DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                            DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
-                            DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
-                            int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
-                            GB300PatchTable const *patchTable, const void *instance = NULL,
-                            void *deviceContext = NULL) {
-        (void)instance;
-        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
-            srcDesc.length != dvDesc.length)
-            return false;
-        return gb300_detail::ok(GB300PatchTableEval(
-            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset,
-            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
-            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
-            duDesc.stride, dvDesc.stride, 0, 0, 0, numPatchCoords,
-            (const void *)patchCoords->BindCudaBuffer(), gb300_detail::stream_of(deviceContext)));
-    }
-
-    // ---- EvalPatchesVarying / EvalPatchesFaceVarying (cudaEvaluator.h:859-1255) -------------
-    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
-    static bool EvalPatchesVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
-                                   DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                                   int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
-                                   GB300PatchTable const *patchTable,
-                                   const void *instance = NULL, void *deviceContext = NULL) {
-        (void)instance;
-        if (srcDesc.length != dstDesc.length) return false;
-        return gb300_detail::ok(GB300PatchTableEvalVarying(
-            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
-            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
-            numPatchCoords, (const void *)patchCoords->BindCudaBuffer(),
-            gb300_detail::stream_of(deviceContext)));
-    }
-    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
-    static bool EvalPatchesVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
-                                   DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                                   DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
-                                   DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
-                                   int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
-                                   GB300PatchTable const *patchTable,
-                                   const void *instance = NULL, void *deviceContext = NULL) {
-        (void)instance;
-        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
-            srcDesc.length != dvDesc.length)
-            return false;
-        return gb300_detail::ok(GB300PatchTableEvalVarying(
-            patchTable->GetHandle(), srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset,
-            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
-            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
-            duDesc.stride, dvDesc.stride, 0, 0, 0, numPatchCoords,
-            (const void *)patchCoords->BindCudaBuffer(), gb300_detail::stream_of(deviceContext)));
-    }
-    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
-    static bool EvalPatchesFaceVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
-                                       DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                                       int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
-                                       GB300PatchTable const *patchTable, int fvarChannel = 0,
-                                       const void *instance = NULL,
-                                       void *deviceContext = NULL) {
-        (void)instance;
-        if (srcDesc.length != dstDesc.length) return false;
-        return gb300_detail::ok(GB300PatchTableEvalFaceVarying(
-            patchTable->GetHandle(), fvarChannel, srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset, nullptr, nullptr, nullptr, nullptr,
-            nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride, 0, 0, 0, 0, 0,
-            numPatchCoords, (const void *)patchCoords->BindCudaBuffer(),
-            gb300_detail::stream_of(deviceContext)));
-    }
-    template <typename SRC_BUFFER, typename DST_BUFFER, typename PATCHCOORD_BUFFER>
-    static bool EvalPatchesFaceVarying(SRC_BUFFER *srcBuffer, BufferDescriptor const &srcDesc,
-                                       DST_BUFFER *dstBuffer, BufferDescriptor const &dstDesc,
-                                       DST_BUFFER *duBuffer, BufferDescriptor const &duDesc,
-                                       DST_BUFFER *dvBuffer, BufferDescriptor const &dvDesc,
-                                       int numPatchCoords, PATCHCOORD_BUFFER *patchCoords,
-                                       GB300PatchTable const *patchTable, int fvarChannel = 0,
-                                       const void *instance = NULL,
-                                       void *deviceContext = NULL) {
-        (void)instance;
-        if (srcDesc.length != dstDesc.length || srcDesc.length != duDesc.length ||
-            srcDesc.length != dvDesc.length)
-            return false;
-        return gb300_detail::ok(GB300PatchTableEvalFaceVarying(
-            patchTable->GetHandle(), fvarChannel, srcBuffer->BindCudaBuffer() + srcDesc.offset,
-            dstBuffer->BindCudaBuffer() + dstDesc.offset,
-            duBuffer->BindCudaBuffer() + duDesc.offset, dvBuffer->BindCudaBuffer() + dvDesc.offset,
-            nullptr, nullptr, nullptr, srcDesc.length, srcDesc.stride, dstDesc.stride,
-            duDesc.stride, dvDesc.stride, 0, 0, 0, numPatchCoords,
-            (const void *)patchCoords->BindCudaBuffer(), gb300_detail::stream_of(deviceContext)));
-    }
+#define OSD_GB300_NO_CHANNEL
+#define OSD_GB300_CHANNEL , int fvarChannel = 0
+    OSD_GB300_PATCH_FORMS(EvalPatches, 0, OSD_GB300_NO_CHANNEL, 0)
+    OSD_GB300_PATCH_FORMS(EvalPatchesVarying, 1, OSD_GB300_NO_CHANNEL, 0)
+    OSD_GB300_PATCH_FORMS(EvalPatchesFaceVarying, 2, OSD_GB300_CHANNEL, fvarChannel)
+#undef OSD_GB300_PATCH_FORMS
+#undef OSD_GB300_NO_CHANNEL
+#undef OSD_GB300_CHANNEL
 
     /// Waits for the work queued on deviceContext's stream (CudaEvaluator::Synchronize).
     static void Synchronize(void *deviceContext = NULL) {
         GB300Synchronize(gb300_detail::stream_of(deviceContext));
+    }
+
+private:
+    // Requested outputs o[k] (null = not requested; k = P, du, dv, duu, duv, dvv) with their
+    // descriptors: false when a requested output's length differs from the source's (as
+    // CpuEvaluator), else the pointers with the descriptor offsets applied.
+    static bool apply_offsets(BufferDescriptor const &srcDesc, float *o[6],
+                              BufferDescriptor const *const d[6]) {
+        for (int k = 0; k < 6; ++k) {
+            if (!o[k]) continue;
+            if (d[k]->length != srcDesc.length) return false;
+            o[k] += d[k]->offset;
+        }
+        return true;
+    }
+    // GB300StencilTable: its own evaluation layout.
+    static bool stencils_over(GB300StencilTable const *t, const float *src,
+                              BufferDescriptor const &sd, float *o[6],
+                              BufferDescriptor const *const d[6], void *ctx) {
+        if (!apply_offsets(sd, o, d)) return false;
+        return gb300_detail::ok(GB300StencilTableEval(
+            t->GetHandle(), src + sd.offset, o[0], o[1], o[2], o[3], o[4], o[5], sd.length,
+            sd.stride, d[0]->stride, d[1]->stride, d[2]->stride, d[3]->stride, d[4]->stride,
+            d[5]->stride, gb300_detail::stream_of(ctx)));
+    }
+    // Any other table with CudaStencilTable's accessors: the raw entry points over its device
+    // buffers (weights of outputs not requested are not read).
+    template <class TABLE>
+    static bool stencils_over(TABLE const *t, const float *src, BufferDescriptor const &sd,
+                              float *o[6], BufferDescriptor const *const d[6], void *ctx) {
+        if (!apply_offsets(sd, o, d)) return false;
+        const float *w[6] = {(const float *)t->GetWeightsBuffer(),
+                             o[1] ? (const float *)t->GetDuWeightsBuffer() : nullptr,
+                             o[2] ? (const float *)t->GetDvWeightsBuffer() : nullptr,
+                             o[3] ? (const float *)t->GetDuuWeightsBuffer() : nullptr,
+                             o[4] ? (const float *)t->GetDuvWeightsBuffer() : nullptr,
+                             o[5] ? (const float *)t->GetDvvWeightsBuffer() : nullptr};
+        return gb300_detail::ok(GB300EvalStencilsWithDerivatives(
+            src + sd.offset, o[0], o[1], o[2], o[3], o[4], o[5], sd.length, sd.stride,
+            d[0]->stride, d[1]->stride, d[2]->stride, d[3]->stride, d[4]->stride, d[5]->stride,
+            (const int *)t->GetSizesBuffer(), (const int *)t->GetOffsetsBuffer(),
+            (const int *)t->GetIndicesBuffer(), w[0], w[1], w[2], w[3], w[4], w[5], 0,
+            t->GetNumStencils(), gb300_detail::stream_of(ctx)));
+    }
+    // kind: 0 vertex, 1 varying, 2 face-varying channel `ch`.
+    static bool patches_over(GB300PatchTable const *t, int kind, int ch, const float *src,
+                             BufferDescriptor const &sd, float *o[6],
+                             BufferDescriptor const *const d[6], int n, const void *coords,
+                             void *ctx) {
+        if (!apply_offsets(sd, o, d)) return false;
+        void *s = gb300_detail::stream_of(ctx);
+        if (kind == 2)
+            return gb300_detail::ok(GB300PatchTableEvalFaceVarying(
+                t->GetHandle(), ch, src + sd.offset, o[0], o[1], o[2], o[3], o[4], o[5],
+                sd.length, sd.stride, d[0]->stride, d[1]->stride, d[2]->stride, d[3]->stride,
+                d[4]->stride, d[5]->stride, n, coords, s));
+        return gb300_detail::ok(
+            (kind == 1 ? GB300PatchTableEvalVarying : GB300PatchTableEval)(
+                t->GetHandle(), src + sd.offset, o[0], o[1], o[2], o[3], o[4], o[5], sd.length,
+                sd.stride, d[0]->stride, d[1]->stride, d[2]->stride, d[3]->stride, d[4]->stride,
+                d[5]->stride, n, coords, s));
+    }
+    template <class TABLE>
+    static bool patches_over(TABLE *t, int kind, int ch, const float *src,
+                             BufferDescriptor const &sd, float *o[6],
+                             BufferDescriptor const *const d[6], int n, const void *coords,
+                             void *ctx) {
+        if (!apply_offsets(sd, o, d)) return false;
+        const void *arrays = kind == 2   ? (const void *)t->GetFVarPatchArrayBuffer(ch)
+                             : kind == 1 ? (const void *)t->GetVaryingPatchArrayBuffer()
+                                         : (const void *)t->GetPatchArrayBuffer();
+        const int *indices = kind == 2   ? (const int *)t->GetFVarPatchIndexBuffer(ch)
+                             : kind == 1 ? (const int *)t->GetVaryingPatchIndexBuffer()
+                                         : (const int *)t->GetPatchIndexBuffer();
+        const void *params = kind == 2 ? (const void *)t->GetFVarPatchParamBuffer(ch)
+                                       : (const void *)t->GetPatchParamBuffer();
+        return gb300_detail::ok(GB300EvalPatchesWithDerivatives(
+            src + sd.offset, o[0], o[1], o[2], o[3], o[4], o[5], sd.length, sd.stride,
+            d[0]->stride, d[1]->stride, d[2]->stride, d[3]->stride, d[4]->stride, d[5]->stride,
+            n, coords, arrays, indices, params, gb300_detail::stream_of(ctx)));
     }
 };
 

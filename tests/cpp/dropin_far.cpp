@@ -1,0 +1,71 @@
+// A client written against OpenSubdiv's own headers -- Far::StencilTable, Far::LimitStencilTable
+// (with second-derivative weights) and Far::PatchTable, through the Osd evaluator template
+// forms -- with CudaEvaluator's type names switched to the GB300 ones.  Compiled (not run) by a
+// CPU test with the reference's source tree on the include path; the refine path repeats the
+// calls Osd::Mesh::Refine makes (osd/mesh.h:501-547): the stencil table converted with
+// convertToCompatibleStencilTable, the evaluator looked up in an EvaluatorCacheT (GB300Evaluator,
+// like CudaEvaluator, is not instantiatable, so the lookup yields NULL and the static forms
+// run).
+#include <opensubdiv/far/patchTable.h>
+#include <opensubdiv/far/stencilTable.h>
+#include <opensubdiv/osd/mesh.h>
+#include <opensubdiv_gb300/osd/gb300Evaluator.h>
+
+using namespace OpenSubdiv;
+
+// Device patch coords with the BindCudaBuffer() the template forms call.
+struct PatchCoordBuffer {
+    Osd::PatchCoord *d;
+    Osd::PatchCoord *BindCudaBuffer() { return d; }
+};
+
+bool Refine(Far::StencilTable const *farStencils, Osd::GB300VertexBuffer *vertexBuffer,
+            int numControlVertices, Osd::EvaluatorCacheT<Osd::GB300Evaluator> *cache,
+            void *deviceContext) {
+    Osd::GB300StencilTable const *table =
+        Osd::convertToCompatibleStencilTable<Osd::GB300StencilTable>(farStencils,
+                                                                      deviceContext);
+    Osd::BufferDescriptor srcDesc(0, 3, 3), dstDesc(numControlVertices * 3, 3, 3);
+    Osd::GB300Evaluator const *instance =
+        Osd::GetEvaluator<Osd::GB300Evaluator>(cache, srcDesc, dstDesc, deviceContext);
+    bool ok = Osd::GB300Evaluator::EvalStencils(vertexBuffer, srcDesc, vertexBuffer, dstDesc,
+                                                table, instance, deviceContext);
+    Osd::GB300Evaluator::Synchronize(deviceContext);
+    delete table;
+    return ok;
+}
+
+bool LimitWithSecondDerivatives(Far::LimitStencilTable const *farStencils,
+                                Osd::GB300VertexBuffer *cvs, Osd::GB300VertexBuffer *out[6]) {
+    Osd::GB300StencilTable *table = Osd::GB300StencilTable::Create(farStencils);
+    Osd::BufferDescriptor d(0, 3, 3);
+    bool ok = table && Osd::GB300Evaluator::EvalStencils(cvs, d, out[0], d, out[1], d, out[2], d,
+                                                         out[3], d, out[4], d, out[5], d, table);
+    ok = ok && Osd::GB300Evaluator::EvalStencils(cvs, d, out[0], d, out[1], d, out[2], d, table);
+    delete table;
+    return ok;
+}
+
+bool LimitSurface(Far::PatchTable const *farPatches, Osd::GB300VertexBuffer *src,
+                  Osd::GB300VertexBuffer *fvarSrc, PatchCoordBuffer *coords, int numCoords,
+                  Osd::GB300VertexBuffer *out[6], Osd::GB300VertexBuffer *fvarOut[6]) {
+    Osd::GB300PatchTable *table = Osd::GB300PatchTable::Create(farPatches);
+    Osd::BufferDescriptor d(0, 3, 3), uv(0, 2, 2);
+    bool ok = table &&
+              Osd::GB300Evaluator::EvalPatches(src, d, out[0], d, out[1], d, out[2], d, out[3],
+                                               d, out[4], d, out[5], d, numCoords, coords,
+                                               table) &&
+              Osd::GB300Evaluator::EvalPatches(src, d, out[0], d, out[1], d, out[2], d,
+                                               numCoords, coords, table) &&
+              Osd::GB300Evaluator::EvalPatches(src, d, out[0], d, numCoords, coords, table) &&
+              Osd::GB300Evaluator::EvalPatchesVarying(src, d, out[0], d, out[1], d, out[2], d,
+                                                      out[3], d, out[4], d, out[5], d, numCoords,
+                                                      coords, table) &&
+              Osd::GB300Evaluator::EvalPatchesFaceVarying(
+                  fvarSrc, uv, fvarOut[0], uv, fvarOut[1], uv, fvarOut[2], uv, fvarOut[3], uv,
+                  fvarOut[4], uv, fvarOut[5], uv, numCoords, coords, table, 0);
+    delete table;
+    return ok;
+}
+
+int main() { return 0; }

@@ -9,6 +9,7 @@ import numpy as np
 import pytest
 
 import oracle
+from gpu_util import bbox_diag, bbox_diag_rows, gate
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 GOLDEN = os.path.join(ROOT, "tests", "golden")
@@ -84,15 +85,17 @@ def test_patch_client_header_compiles_standalone():
 
 @pytest.mark.gpu
 def test_cpp_patch_client_through_drop_in_header(tmp_path):
-    """Device PatchMap, EvalPatches (P, du, dv) and EvalPatchesFaceVarying from C++ through
-    the header, on the reference's face-varying torus table."""
+    """Device PatchMap, EvalPatches (P and all five derivatives), EvalPatchesVarying and
+    EvalPatchesFaceVarying (all five derivatives) from C++ through the header's template forms,
+    on the reference's face-varying torus table, and the same EvalPatches over a device table
+    of the client's own type (the PATCH_TABLE type parameter)."""
     import torch
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     z = np.load(os.path.join(GOLDEN, "torus12x8_fvar_patches_L3.npz"))
     for k in ("arrays", "patch_indices", "params", "varying_arrays", "varying_indices",
-              "fvar_arrays", "fvar_indices", "fvar_params", "src", "fvar_src", "q_face", "q_u",
-              "q_v"):
+              "fvar_arrays", "fvar_indices", "fvar_params", "src", "fvar_src", "varying_src",
+              "q_face", "q_u", "q_v"):
         np.ascontiguousarray(z[k]).tofile(tmp_path / f"{k}.bin")
     np.array([int(z["triangular"])], np.int32).tofile(tmp_path / "triangular.bin")
     exe = _build(tmp_path, "dropin_patches")
@@ -102,14 +105,79 @@ def test_cpp_patch_client_through_drop_in_header(tmp_path):
     handles = np.fromfile(tmp_path / "handles.bin", np.int32).reshape(nq, 3)
     assert np.array_equal(handles, z["q_handles"])
     hit = z["q_found"].astype(bool)
-    A = oracle.abs_scale(z["src"], (0, 3, 3), 3, z["coords"], z["arrays"], z["patch_indices"],
-                         z["params"])
-    for k, name in enumerate(("p", "du", "dv")):
-        out = np.fromfile(tmp_path / f"{name}.bin", np.float32).reshape(nq, 3)
-        assert np.all(out[~hit] == 0)
-        bound = 1e-6 * np.maximum(A[k].reshape(-1, 3), 1.0)
-        assert np.all(np.abs(out[hit] - z["out6"][k]) <= bound), name
-    fv = np.fromfile(tmp_path / "fvar.bin", np.float32).reshape(nq, 2)
-    Af = oracle.abs_scale(z["fvar_src"], (0, 2, 2), 2, z["coords"], z["fvar_arrays"],
-                          z["fvar_indices"], z["fvar_params"])
-    assert np.all(np.abs(fv[hit] - z["fvar_out6"][0]) <= 1e-6 * np.maximum(Af[0].reshape(-1, 2), 1.0))
+    diag = bbox_diag(z["positions"])
+    for k in range(6):
+        for tag in ("p", "g"):
+            out = np.fromfile(tmp_path / f"{tag}{k}.bin", np.float32).reshape(nq, 3)
+            assert np.all(out[~hit] == 0)
+            gate(f"C++ client {'table' if tag == 'p' else 'client table'}", k, out[hit],
+                 z["out6"][k], z["out6_fp64"][k], diag)
+    dv_ = bbox_diag_rows(z["varying_src"], 4)
+    for k in range(3):
+        out = np.fromfile(tmp_path / f"var{k}.bin", np.float32).reshape(nq, 4)
+        gate("C++ client varying", k, out[hit], z["varying_out3"][k], None, dv_)
+    m = int(hit.sum())
+    f64 = [np.zeros(m * 2) for _ in range(6)]
+    oracle.eval_patches(z["fvar_src"], (0, 2, 2), f64, [(0, 2, 2)] * 6, z["coords"],
+                        z["fvar_arrays"], z["fvar_indices"], z["fvar_params"], fp64=True)
+    df = bbox_diag_rows(z["fvar_src"], 2)
+    for k in range(6):
+        fv = np.fromfile(tmp_path / f"fvar{k}.bin", np.float32).reshape(nq, 2)
+        gate("C++ client face-varying", k, fv[hit], z["fvar_out6"][k], f64[k], df)
+
+
+@pytest.mark.gpu
+def test_cpp_client_second_derivative_stencils(tmp_path):
+    """Limit stencils with all five derivatives from C++ through the header's six-output
+    EvalStencils template: over a GB300StencilTable made from a Far::LimitStencilTable
+    stand-in, and over a device table of the client's own type (the STENCIL_TABLE type
+    parameter); the three-output form and a rejected descriptor as well."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    z = np.load(os.path.join(GOLDEN, "cube8_uniform_L3.npz"))
+    names = ("weights", "du_weights", "dv_weights", "duu_weights", "duv_weights", "dvv_weights")
+    for k in ("sizes", "offsets", "indices") + names:
+        np.ascontiguousarray(z["limit_" + k]).tofile(tmp_path / f"limit_{k}.bin")
+    z["positions"].astype(np.float32).tofile(tmp_path / "src.bin")
+    exe = _build(tmp_path, "dropin_derivatives")
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    diag = bbox_diag(z["positions"])
+    m = len(z["limit_sizes"])
+    for k in range(6):
+        f64 = np.zeros(m * 3)
+        oracle.eval_stencils(z["positions"].ravel(), (0, 3, 3), [f64], [(0, 3, 3)],
+                             z["limit_sizes"], z["limit_offsets"], z["limit_indices"],
+                             [z["limit_" + names[k]]], fp64=True)
+        for tag in ("a", "b"):
+            out = np.fromfile(tmp_path / f"{tag}{k}.bin", np.float32)
+            gate(f"C++ client limit stencils ({tag})", k, out, z["limit_out6"][k], f64, diag,
+                 all_vs_cpu=True)
+    c0 = np.fromfile(tmp_path / "c0.bin", np.float32)
+    gate("C++ client limit stencils, 3 outputs", 0, c0, z["limit_out6"][0], None, diag)
+
+
+def test_client_compiles_against_the_reference_far_headers(tmp_path):
+    """A client written for CudaEvaluator -- Far::StencilTable, Far::LimitStencilTable with
+    second derivatives and Far::PatchTable through the Osd template forms -- compiles against
+    OpenSubdiv's own headers with only the type names changed (CPU-only check; needs the
+    reference's source tree)."""
+    refroot = os.environ.get("OPENSUBDIV_SOURCE", "/root/reference")
+    if not os.path.isdir(os.path.join(refroot, "opensubdiv", "far")):
+        pytest.skip("OpenSubdiv's headers are not available here")
+    src = os.path.join(ROOT, "tests", "cpp", "dropin_far.cpp")
+    obj = tmp_path / "dropin_far.o"
+    cuda = _cuda_home()
+    r = subprocess.run(["g++", "-std=c++14", "-O1", "-c", f"-I{refroot}", f"-I{ROOT}/include",
+                        f"-I{cuda}/include", src, "-o", str(obj)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    # and links against the reference's CPU library (Far, Osd::CpuPatchTable) and this one
+    refdir = os.path.join(ROOT, "oracle", "_ref")
+    from opensubdiv_gb300 import _lib
+    if os.path.exists(os.path.join(refdir, "libosdref.so")) and os.path.exists(_lib.LIB_PATH):
+        r = subprocess.run(["g++", "-o", str(tmp_path / "dropin_far"), str(obj), f"-L{refdir}",
+                            "-losdref", f"-L{os.path.dirname(_lib.LIB_PATH)}", "-losd_gb300",
+                            f"-L{cuda}/lib64", "-lcudart", "-fopenmp"],
+                           capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
