@@ -48,6 +48,8 @@ def parse():
     ap.add_argument("--nv", type=int, default=256, help="torus cage resolution (v)")
     ap.add_argument("--n-limit", type=int, default=1_000_000, help="limit locations")
     ap.add_argument("--no-patches", action="store_true", help="skip the EvalPatches section")
+    ap.add_argument("--no-config1", action="store_true",
+                    help="skip the CPU-runnable cube section (warm and cold L2)")
     ap.add_argument("--patch-points", type=int, default=4_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batching section")
     ap.add_argument("--batch-meshes", type=int, default=256)
@@ -438,6 +440,82 @@ METRIC = "stencil evals per s (EvalStencils refine L3 + limit du/dv)"
 UNIT = "stencils/s"
 
 
+def bench_config1(args, stream, peak):
+    """The CPU-runnable case: a unit cube with 8 x 8 quads per face (386 control vertices,
+    N(0, 0.01) noise), Catmull-Clark uniform level 4 (98,306 stencils of the last level), xyz
+    at stride 3, through the device table.  Its 13 MB working set fits in L2, so it is timed
+    warm (repeated launches) and cold (a 256 MB buffer written between launches evicts L2),
+    median of 50 launches each, CUDA events around the evaluation only.  Beside it: the oracle
+    port of CpuEvaluator on one host thread and of OmpEvaluator on all of them (median of 20
+    passes after 3 warm-ups) and the error against the oracle."""
+    import torch
+
+    from opensubdiv_gb300 import workloads
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300StencilTable)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+    w = workloads.refine_cube()
+    r = w["refine"]
+    n, nnz, ncv = len(r["sizes"]), len(r["indices"]), w["cage"].num_vertices
+    t = GB300StencilTable.Create(r["sizes"], r["offsets"], r["indices"], r["weights"])
+    src = torch.from_numpy(w["src"]).cuda()
+    out = torch.zeros(n * 3, device="cuda")
+    d = BD(0, 3, 3)
+    flush = torch.empty(64 << 20, device="cuda")
+
+    def one():
+        assert Ev.EvalStencilsTable(src, d, out, d, t, stream=stream)
+
+    def timed(cold, reps=50):
+        ms = []
+        for k in range(reps + 3):
+            if cold:
+                with torch.cuda.stream(stream):
+                    flush.fill_(float(k))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            one()
+            e1.record(stream)
+            e1.synchronize()
+            if k >= 3:
+                ms.append(e0.elapsed_time(e1))
+        return float(np.median(ms)), float(np.percentile(ms, 99))
+
+    warm, warm99 = timed(False)
+    cold, cold99 = timed(True)
+    b = workloads.stencil_bytes(n, nnz, 3, ncv)
+    ref = np.zeros(n * 3, np.float32)
+    oracle.eval_stencils(w["src"], (0, 3, 3), [ref], [(0, 3, 3)], r["sizes"], r["offsets"],
+                         r["indices"], [r["weights"]])
+    err = float(np.abs(out.cpu().numpy() - ref).max())
+    diag = w["cage"].bbox_diagonal()
+
+    def cpu(threads, reps=20):
+        o = np.zeros(n * 3, np.float32)
+        ts = []
+        for k in range(reps + 3):
+            t0 = time.perf_counter()
+            oracle.eval_stencils(w["src"], (0, 3, 3), [o], [(0, 3, 3)], r["sizes"], r["offsets"],
+                                 r["indices"], [r["weights"]], threads=threads)
+            if k >= 3:
+                ts.append(time.perf_counter() - t0)
+        return n / float(np.median(ts))
+
+    return {"workload": w["name"], "stencils": n, "nnz": nnz, "algorithmic_bytes": b,
+            "warm": {"ms": warm, "p99_ms": warm99, "stencils_per_s": n / (warm / 1e3),
+                     "achieved_gbs": b / (warm / 1e3) / 1e9},
+            "cold_l2": {"ms": cold, "p99_ms": cold99, "stencils_per_s": n / (cold / 1e3),
+                        "achieved_gbs": b / (cold / 1e3) / 1e9,
+                        "frac_of_hbm_peak": b / (cold / 1e3) / 1e9 / peak,
+                        "flush": "256 MB buffer written on the stream before each launch"},
+            "accuracy": {"max_abs_err_vs_oracle": err, "bbox_diag": diag,
+                         "in_units_of_1e-5_diag": err / (1e-5 * diag)},
+            "cpu_port_1_thread_stencils_per_s": cpu(1),
+            "cpu_port_all_threads_stencils_per_s": cpu(os.cpu_count() or 1),
+            "cpu_threads": os.cpu_count()}
+
+
 def bench_layouts(w, stream):
     """Device-table EvalStencils on the headline tables per source layout (refine pass, one
     output; limit pass, P+du+dv) and, at 8 floats, per output count 1-6 over a limit table
@@ -782,6 +860,7 @@ def reference_cuda(args, w):
     if not torch.cuda.is_available():
         return {"unavailable": "no CUDA device"}
     import oracle
+    from opensubdiv_gb300 import workloads
     L = w["length"]
     r, lim = w["refine"], w["limit"]
     dev = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
@@ -814,6 +893,17 @@ def reference_cuda(args, w):
                       "computePatches<<<512,32>>>)",
            "refine_ms": refine_ms, "limit_ms": limit_ms,
            "stencils_per_s": (n_ref + n_lim) / ((refine_ms + limit_ms) / 1e3)}
+    # the CPU-runnable cube (xyz, stride 3: computeStencilsNv<3>), warm
+    cw = workloads.refine_cube()
+    cr = cw["refine"]
+    csrc = dev(cw["src"])
+    ct = [dev(cr[k]) for k in ("sizes", "offsets", "indices", "weights")]
+    cout = torch.empty(len(cr["sizes"]) * 3, device="cuda")
+    c_ms = timed(lambda: refcuda.eval_stencils(
+        csrc.data_ptr(), cout.data_ptr(), 3, 3, 3, *[x.data_ptr() for x in ct], 0,
+        len(cr["sizes"])))
+    res["config1_cube"] = {"workload": cw["name"], "refine_ms_warm": c_ms,
+                           "stencils_per_s": len(cr["sizes"]) / (c_ms / 1e3)}
     if not args.no_patches:
         from opensubdiv_gb300 import workloads
         pw = patch_workload(args.patch_points)
@@ -1038,6 +1128,8 @@ def run_gb300(args, rank, world):
         "accuracy": {"max_abs_err_vs_oracle_slice": spot, "bbox_diag": diag,
                      "rel": spot / diag},
     }
+    if not args.no_config1:
+        line["config1_cube"] = bench_config1(args, stream, peak)
     if not args.no_patches:
         line["eval_patches"] = bench_patches(args, stream, peak)
         line["eval_patches_loop"] = bench_patches(args, stream, peak, loop=True)

@@ -38,6 +38,42 @@ int check_launch(const char *what) {
     return ok();
 }
 
+int scratch_alloc(void **p, size_t bytes, cudaStream_t s, const char *who) {
+    static std::mutex m;
+    static std::vector<cudaMemPool_t> pools;
+    int dev = 0;
+    int st = check_cuda(cudaGetDevice(&dev), who);
+    if (st != GB300_OK) return st;
+    cudaMemPool_t pool = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(m);
+        if ((int)pools.size() <= dev) pools.resize(dev + 1, nullptr);
+        if (!pools[dev]) {
+            cudaMemPoolProps props = {};
+            props.allocType = cudaMemAllocationTypePinned;
+            props.location.type = cudaMemLocationTypeDevice;
+            props.location.id = dev;
+            cudaMemPool_t created = nullptr;
+            if ((st = check_cuda(cudaMemPoolCreate(&created, &props), who)) != GB300_OK)
+                return st;
+            uint64_t retain = kScratchRetainBytes;
+            if ((st = check_cuda(cudaMemPoolSetAttribute(
+                                     created, cudaMemPoolAttrReleaseThreshold, &retain),
+                                 who)) != GB300_OK) {
+                cudaMemPoolDestroy(created);
+                return st;
+            }
+            pools[dev] = created;
+        }
+        pool = pools[dev];
+    }
+    return check_cuda(cudaMallocFromPoolAsync(p, bytes < 16 ? 16 : bytes, pool, s), who);
+}
+
+void scratch_free(void *p, cudaStream_t s) {
+    if (p) cudaFreeAsync(p, s);
+}
+
 int num_sms() {
     static std::mutex m;
     static std::vector<int> cache;

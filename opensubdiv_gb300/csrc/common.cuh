@@ -32,6 +32,15 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 // Number of SMs of the current device (cached per device).
 int num_sms();
 
+// Stream-ordered scratch from a memory pool the library keeps per device: allocations and
+// frees are ordered on `s` like cudaMallocAsync / cudaFreeAsync, but up to kScratchRetainBytes
+// of freed memory stay mapped in the pool between calls (the device's default pool returns
+// freed memory at every synchronisation, so a per-call scratch paid a fresh mapping, ~0.1 ms,
+// on every call).
+constexpr size_t kScratchRetainBytes = size_t(512) << 20;
+int scratch_alloc(void **p, size_t bytes, cudaStream_t s, const char *who);
+void scratch_free(void *p, cudaStream_t s);
+
 // Device address of the library's status word on the current device (the word
 // GB300GetDeviceStatus reads and clears; staged kernels record an expired bounded wait there).
 int status_word_address(int **out);

@@ -297,7 +297,7 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
     cudaStream_t s = as_stream(stream);
     // Unaligned source rows (no vector gathers) of a large table: gather from a padded copy
     // (rows of 4, 8, 12 or 16 floats: vector loads) made on the same stream in stream-ordered
-    // memory.
+    // memory from the library's scratch pool.
     auto al = [](const void *p, uintptr_t m) { return ((uintptr_t)p & (m - 1)) == 0; };
     const bool unaligned = src && !((al(src, 32) && srcStride % 8 == 0) ||
                                     (al(src, 16) && srcStride % 4 == 0));
@@ -305,13 +305,13 @@ int GB300StencilTableEval(const GB300StencilTable *t, const float *src, float *d
     if (unaligned && length > 0 && ps > 0 && srcStride >= length &&
         t->nnz >= (int64_t)t->numControl * 4 && t->nnz >= (1 << 20) && t->numControl > 0) {
         float *padded = nullptr;
-        if (cudaMallocAsync((void **)&padded, (size_t)t->numControl * ps * 4, s) ==
-            cudaSuccess) {
+        if (scratch_alloc((void **)&padded, (size_t)t->numControl * ps * 4, s,
+                          "GB300StencilTableEval") == GB300_OK) {
             batch::PadJob j{src, padded, srcStride, length, t->numControl, ps, 0};
             int r = batch::launch_pad_one(j, s);
             if (r == GB300_OK) r = table_eval(t, padded, d, st, length, ps, s);
-            const int f = check_cuda(cudaFreeAsync(padded, s), "GB300StencilTableEval");
-            return r != GB300_OK ? r : f;
+            scratch_free(padded, s);
+            return r != GB300_OK ? r : check_launch("GB300StencilTableEval");
         }
         cudaGetLastError();  // no stream-ordered memory: evaluate in place
     }

@@ -119,14 +119,13 @@ struct Temps {
     template <class T>
     T *get(size_t count, const char *who) {
         void *q = nullptr;
-        if (check_cuda(cudaMallocAsync(&q, std::max<size_t>(count * sizeof(T), 16), s), who) !=
-            GB300_OK)
+        if (scratch_alloc(&q, std::max<size_t>(count * sizeof(T), 16), s, who) != GB300_OK)
             return nullptr;
         p[n++] = q;
         return (T *)q;
     }
     ~Temps() {
-        for (int i = 0; i < n; ++i) cudaFreeAsync(p[i], s);
+        for (int i = 0; i < n; ++i) scratch_free(p[i], s);
     }
 };
 

@@ -468,13 +468,12 @@ struct Scratch {
     std::vector<void *> ptrs;
     explicit Scratch(cudaStream_t st) : s(st) {}
     ~Scratch() {
-        for (void *p : ptrs) cudaFreeAsync(p, s);
+        for (void *p : ptrs) scratch_free(p, s);
     }
     template <class T>
     T *alloc(size_t n, const char *who) {
         void *p = nullptr;
-        if (check_cuda(cudaMallocAsync(&p, std::max<size_t>(n, 1) * sizeof(T), s), who) !=
-            GB300_OK)
+        if (scratch_alloc(&p, std::max<size_t>(n, 1) * sizeof(T), s, who) != GB300_OK)
             return nullptr;
         ptrs.push_back(p);
         return (T *)p;
@@ -482,7 +481,7 @@ struct Scratch {
     void release(void *p) {
         auto it = std::find(ptrs.begin(), ptrs.end(), p);
         if (it != ptrs.end()) {
-            cudaFreeAsync(p, s);
+            scratch_free(p, s);
             ptrs.erase(it);
         }
     }
