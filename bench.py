@@ -53,8 +53,12 @@ def parse():
     ap.add_argument("--patch-points", type=int, default=4_000_000)
     ap.add_argument("--no-batch", action="store_true", help="skip the batching section")
     ap.add_argument("--batch-meshes", type=int, default=256)
-    ap.add_argument("--batch-cv-max", type=int, default=25_000,
+    ap.add_argument("--batch-cv-max", type=int, default=200_000,
                     help="upper end of the log-uniform CV range of the batched meshes")
+    ap.add_argument("--batch-cv-max-scaled", type=int, default=25_000,
+                    help="also run a population with this smaller CV range (0: skip)")
+    ap.add_argument("--serve-cv-max", type=int, default=25_000,
+                    help="upper end of the CV range of the serving pool's topologies")
     ap.add_argument("--no-serving", action="store_true", help="skip the serving section")
     ap.add_argument("--no-factory", action="store_true",
                     help="skip the stencil-table factory section")
@@ -208,21 +212,37 @@ def bench_patches(args, stream, peak, loop=False):
             "max_abs_err_P_vs_oracle_slice": err_p}
 
 
-def bench_batch(args, stream, peak):
-    """Batching: a population of meshes of uneven size (workloads.batch_population) evaluated
-    per frame as ONE persistent launch replayed from a CUDA graph (GB300StencilBatch, tuned),
-    against one plain EvalStencilsTable call per mesh.  A frame = sinusoidal deformation of
-    every control value (one elementwise pass over all meshes' sources, same in both arms) +
-    evaluation of every mesh."""
+def bench_batch(args, stream, peak, cv_max):
+    """Batching: a population of meshes of uneven size (workloads.batch_population_masks, CV
+    counts log-uniform in [500, cv_max]) evaluated per frame as ONE persistent launch replayed
+    from a CUDA graph (GB300StencilBatch, tuned), against one plain EvalStencilsTable call per
+    mesh.  A frame = sinusoidal deformation of every control value (one elementwise pass over
+    all meshes' sources, same in both arms) + evaluation of every mesh.  The tables are built
+    on the device by the GPU stencil-table factory from host-recorded masks, mesh by mesh as
+    the host threads produce them."""
     import torch
 
     from opensubdiv_gb300 import workloads
     from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
-                                            GB300StencilBatch, GB300StencilTable)
+                                            GB300StencilBatch,
+                                            GB300StencilTableFactory as Factory)
 
     t0 = time.time()
-    pop = workloads.batch_population(n_meshes=args.batch_meshes, cv_max=args.batch_cv_max)
+    pop, tables = [], []
+    factory_s = 0.0
+    for m in workloads.batch_population_masks(n_meshes=args.batch_meshes, cv_max=cv_max):
+        nc, levels = m.pop("masks")
+        t1 = time.time()
+        tables.append(Factory.Create(nc, levels, generateIntermediateLevels=False))
+        factory_s += time.time() - t1
+        m["n_stencils"] = tables[-1].GetNumStencils()
+        m["nnz"] = int(tables[-1].GetNumIndices())
+        pop.append(m)
+    torch.cuda.synchronize()
     gen_s = time.time() - t0
+    order = np.argsort([m["index"] for m in pop], kind="stable")  # population order
+    pop = [pop[i] for i in order]
+    tables = [tables[i] for i in order]
     # one concatenated source / base / phase buffer and one destination buffer, every mesh's
     # slice starting on a 32-byte boundary
     al = lambda x: (x + 7) // 8 * 8  # noqa: E731
@@ -231,7 +251,7 @@ def bench_batch(args, stream, peak):
         s_off.append(so)
         d_off.append(do)
         so += al(m["n_cv"] * m["length"])
-        do += al(len(m["table"]["sizes"]) * m["length"])
+        do += al(m["n_stencils"] * m["length"])
     base_h = np.zeros(so, np.float32)
     phase_h = np.zeros(so, np.float32)
     for m, o in zip(pop, s_off):
@@ -241,14 +261,13 @@ def bench_batch(args, stream, peak):
     phase = torch.from_numpy(phase_h).cuda()
     src = base.clone()
     dst = torch.zeros(do, device="cuda")
-    tables = [GB300StencilTable.Create(**m["table"]) for m in pop]
     descs = [BD(0, m["length"], m["length"]) for m in pop]
     sp = [src.data_ptr() + 4 * o for o in s_off]
     dp = [dst.data_ptr() + 4 * o for o in d_off]
-    n_st = sum(len(m["table"]["sizes"]) for m in pop)
-    nnz = sum(len(m["table"]["indices"]) for m in pop)
-    b_alg = sum(workloads.stencil_bytes(len(m["table"]["sizes"]), len(m["table"]["indices"]),
-                                        m["length"], m["n_cv"]) for m in pop)
+    n_st = sum(m["n_stencils"] for m in pop)
+    nnz = sum(m["nnz"] for m in pop)
+    b_alg = sum(workloads.stencil_bytes(m["n_stencils"], m["nnz"], m["length"], m["n_cv"])
+                for m in pop)
     batch = GB300StencilBatch(list(zip(tables, sp, descs, dp, descs)), stream=stream)
     with torch.cuda.stream(stream):
         batch.Tune(iterations=3, stream=stream)
@@ -299,10 +318,12 @@ def bench_batch(args, stream, peak):
     status = batch.GetDeviceStatus()
     ms_b, ms_p = float(eb.mean()), float(ep.mean())
     return {
-        "workload": f"{len(pop)} meshes, CVs log-uniform [500, {args.batch_cv_max}], 70% "
+        "workload": f"{len(pop)} meshes, CVs log-uniform [500, {cv_max}], 70% "
                     "Catmull-Clark / 30% Loop tori and cubes, uniform L1-4, 3-12 primvars",
         "meshes": len(pop), "stencils_per_frame": n_st, "nnz": nnz,
-        "generation_s": gen_s, "tuned": cfg,
+        "generation_s": gen_s, "generation_factory_s": factory_s,
+        "generation": "host topology + masks on all host threads, tables merged on the "
+                      "device by GB300StencilTableFactory", "tuned": cfg,
         "batched": {"frame_ms": float(fb.mean()), "eval_ms": ms_b,
                     "stencils_per_s": n_st / (ms_b / 1e3),
                     "frame_ms_p50": float(np.percentile(fb, 50)),
@@ -336,7 +357,7 @@ def bench_serving(args):
 
     t0 = time.time()
     pool = workloads.serving_pool(serving_bases(), n_topologies=args.serve_topologies,
-                                  cv_max=args.batch_cv_max)
+                                  cv_max=args.serve_cv_max)
     gen_s = time.time() - t0
     rng = np.random.default_rng(31337)
     # host inputs: per-topology control values, shared query windows, an output ring
@@ -425,7 +446,7 @@ def bench_serving(args):
     table_gb = sum(len(t["refine"]["indices"]) * 8 + len(t["limit"]["pp_indices"]) * 8
                    + len(t["limit"]["patch_indices"]) * 4 for t in pool) / 1e9
     return {
-        "workload": f"{len(pool)} topologies (CVs log-uniform [500, {args.batch_cv_max}], "
+        "workload": f"{len(pool)} topologies (CVs log-uniform [500, {args.serve_cv_max}], "
                     "70% Catmull-Clark / 30% Loop, refine level 1-4, 3-12 primvars), "
                     f"Zipf(1.1) popularity, Poisson arrivals, 50% refine / 50% limit "
                     f"(10k-1M points, P+du+dv), {args.serve_budget_gb} GB table budget",
@@ -1134,7 +1155,9 @@ def run_gb300(args, rank, world):
         line["eval_patches"] = bench_patches(args, stream, peak)
         line["eval_patches_loop"] = bench_patches(args, stream, peak, loop=True)
     if not args.no_batch:
-        line["batching"] = bench_batch(args, stream, peak)
+        line["batching"] = bench_batch(args, stream, peak, args.batch_cv_max)
+        if args.batch_cv_max_scaled > 0:
+            line["batching_scaled"] = bench_batch(args, stream, peak, args.batch_cv_max_scaled)
     if not args.no_serving:
         line["serving"] = bench_serving(args)
     if not args.no_factory:

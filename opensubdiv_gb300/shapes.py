@@ -111,51 +111,48 @@ def torus(nu: int = 512, nv: int = 256, R: float = 1.0, r: float = 0.3,
 
 def cube(n: int = 8, noise: float = 0.01, seed: int = 0, scheme: int = CATMARK) -> Cage:
     """Unit cube [-0.5, 0.5]^3 with every face split into n x n quads (6n^2+2 vertices,
-    eight valence-3 corners).  scheme=LOOP splits every quad into two triangles."""
+    eight valence-3 corners).  scheme=LOOP splits every quad into two triangles.  Vertices are
+    numbered in the order the quads first visit them (cube faces by axis, then sign; quads by
+    x, then y; corners (0,0), (1,0), (1,1), (0,1))."""
     rng = np.random.default_rng(seed)
-    index = {}
-    pos = []
-
-    def vid(p):
-        key = tuple(int(round(x * 2 * n)) for x in p)
-        if key not in index:
-            index[key] = len(pos)
-            pos.append(p)
-        return index[key]
-
-    faces = []
     g = np.linspace(-0.5, 0.5, n + 1)
+    corners = np.array([(0, 0), (1, 0), (1, 1), (0, 1)])
+    xs, ys = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    blocks = []
     # each cube face: fixed axis, sign, two in-plane axes ordered for outward orientation
     for axis in range(3):
         for sign in (-1.0, 1.0):
             a1, a2 = [(axis + 1) % 3, (axis + 2) % 3]
             if sign < 0:
                 a1, a2 = a2, a1
-            for x in range(n):
-                for y in range(n):
-                    quad = []
-                    for dx, dy in ((0, 0), (1, 0), (1, 1), (0, 1)):
-                        p = [0.0, 0.0, 0.0]
-                        p[axis] = 0.5 * sign
-                        p[a1] = g[x + dx]
-                        p[a2] = g[y + dy]
-                        quad.append(vid(tuple(p)))
-                    faces.append(quad)
-    pos = np.asarray(pos, np.float64)
+            p = np.zeros((n, n, 4, 3))
+            p[..., axis] = 0.5 * sign
+            p[..., a1] = g[xs[..., None] + corners[:, 0]]
+            p[..., a2] = g[ys[..., None] + corners[:, 1]]
+            blocks.append(p.reshape(-1, 3))
+    visits = np.concatenate(blocks)                       # corner points in visit order
+    k = np.rint(visits * 2 * n).astype(np.int64) + n     # grid coordinates in [0, 2n]
+    keys = (k[:, 0] * (2 * n + 1) + k[:, 1]) * (2 * n + 1) + k[:, 2]
+    _, first, inverse = np.unique(keys, return_index=True, return_inverse=True)
+    order = np.argsort(first, kind="stable")              # unique points by first visit
+    rank = np.empty_like(order)
+    rank[order] = np.arange(len(order))
+    quads = rank[inverse.ravel()].reshape(-1, 4)
+    pos = visits[first[order]]
     if noise > 0:
         pos = pos + rng.normal(0.0, noise, pos.shape)
-    vpf, fv = [], []
-    for q in faces:
-        if scheme == LOOP:
-            a, b, c, d = q
-            if rng.random() < 0.5:
-                vpf.extend((3, 3)); fv.extend((a, b, c, a, c, d))
-            else:
-                vpf.extend((3, 3)); fv.extend((a, b, d, b, c, d))
-        else:
-            vpf.append(4); fv.extend(q)
-    return Cage(pos.astype(np.float32), np.asarray(vpf, np.int32), np.asarray(fv, np.int32),
-                scheme=scheme, name=f"cube{n}")
+    if scheme == LOOP:
+        split = rng.random(len(quads)) < 0.5
+        a, b, c, d = quads.T
+        tri = np.where(split[:, None], np.stack([a, b, c, a, c, d], 1),
+                       np.stack([a, b, d, b, c, d], 1))
+        vpf = np.full(2 * len(quads), 3, np.int32)
+        fv = tri.reshape(-1)
+    else:
+        vpf = np.full(len(quads), 4, np.int32)
+        fv = quads.reshape(-1)
+    return Cage(pos.astype(np.float32), vpf, np.asarray(fv, np.int32), scheme=scheme,
+                name=f"cube{n}")
 
 
 def icosphere(subdivisions: int = 6, noise: float = 0.005, seed: int = 0) -> Cage:

@@ -174,6 +174,39 @@ def refine_cube(n=8, level=4, seed=1):
                 level=level)
 
 
+def _population_specs(n_meshes, cv_min, cv_max, seed):
+    rng = np.random.default_rng(seed)
+    specs = []
+    for i in range(n_meshes):
+        loop = bool(rng.random() < 0.3)
+        kind = "torus" if rng.random() < 0.5 else "cube"
+        cv = float(np.exp(rng.uniform(np.log(cv_min), np.log(cv_max))))
+        specs.append(dict(index=i, loop=loop, kind=kind, cv=cv, level=int(rng.integers(1, 5)),
+                          length=int(rng.integers(3, 13)),
+                          phase=float(rng.uniform(0.0, 2.0 * np.pi))))
+    return specs
+
+
+def _population_mesh(sp, seed):
+    """The cage and source values of one population mesh (without its table)."""
+    scheme = shapes.LOOP if sp["loop"] else shapes.CATMARK
+    s = seed * 1000 + sp["index"]
+    if sp["kind"] == "torus":
+        nv = max(3, int(round(np.sqrt(sp["cv"] / 2.0))))
+        nu = max(3, int(round(sp["cv"] / nv)))
+        cage = shapes.torus(nu, nv, noise=0.005, seed=s, scheme=scheme)
+    else:
+        n = max(1, int(round(np.sqrt(max(sp["cv"] - 2.0, 6.0) / 6.0))))
+        cage = shapes.cube(n, noise=0.01, seed=s, scheme=scheme)
+    r = np.random.default_rng(s + 1)
+    ncv = cage.num_vertices
+    src = np.concatenate([cage.positions,
+                          r.uniform(-1, 1, (ncv, sp["length"] - 3)).astype(np.float32)], 1)
+    return cage, dict(name=f"{cage.name}_{'loop' if sp['loop'] else 'catmark'}_L{sp['level']}",
+                      scheme=scheme, level=sp["level"], length=sp["length"],
+                      phase=sp["phase"], n_cv=ncv, src=np.ascontiguousarray(src.ravel()))
+
+
 def batch_population(n_meshes=256, cv_min=500, cv_max=200_000, seed=4096, threads=None):
     """Meshes of uneven size for batched evaluation: procedural noisy tori or cubes (50/50)
     with control-vertex counts log-uniform in [cv_min, cv_max], 70% Catmull-Clark and 30%
@@ -189,39 +222,54 @@ def batch_population(n_meshes=256, cv_min=500, cv_max=200_000, seed=4096, thread
 
     from .topology import load as _topo_load
 
-    rng = np.random.default_rng(seed)
-    specs = []
-    for i in range(n_meshes):
-        loop = bool(rng.random() < 0.3)
-        kind = "torus" if rng.random() < 0.5 else "cube"
-        cv = float(np.exp(rng.uniform(np.log(cv_min), np.log(cv_max))))
-        specs.append(dict(index=i, loop=loop, kind=kind, cv=cv, level=int(rng.integers(1, 5)),
-                          length=int(rng.integers(3, 13)),
-                          phase=float(rng.uniform(0.0, 2.0 * np.pi))))
-
     def build(sp):
         _topo_load().GB300TopologySetNumThreads(1)
-        scheme = shapes.LOOP if sp["loop"] else shapes.CATMARK
-        s = seed * 1000 + sp["index"]
-        if sp["kind"] == "torus":
-            nv = max(3, int(round(np.sqrt(sp["cv"] / 2.0))))
-            nu = max(3, int(round(sp["cv"] / nv)))
-            cage = shapes.torus(nu, nv, noise=0.005, seed=s, scheme=scheme)
-        else:
-            n = max(1, int(round(np.sqrt(max(sp["cv"] - 2.0, 6.0) / 6.0))))
-            cage = shapes.cube(n, noise=0.01, seed=s, scheme=scheme)
-        table = UniformRefiner(cage, sp["level"]).stencil_table()
-        r = np.random.default_rng(s + 1)
-        ncv = cage.num_vertices
-        src = np.concatenate([cage.positions,
-                              r.uniform(-1, 1, (ncv, sp["length"] - 3)).astype(np.float32)], 1)
-        return dict(name=f"{cage.name}_{'loop' if sp['loop'] else 'catmark'}_L{sp['level']}",
-                    scheme=scheme, level=sp["level"], length=sp["length"], phase=sp["phase"],
-                    n_cv=ncv, src=np.ascontiguousarray(src.ravel()), table=table)
+        cage, m = _population_mesh(sp, seed)
+        m["table"] = UniformRefiner(cage, sp["level"]).stencil_table()
+        return m
 
     _topo_load()  # load once before the workers start
     with ThreadPoolExecutor(threads or os.cpu_count()) as ex:
-        return list(ex.map(build, specs))
+        return list(ex.map(build, _population_specs(n_meshes, cv_min, cv_max, seed)))
+
+
+def batch_population_masks(n_meshes=256, cv_min=500, cv_max=200_000, seed=4096, threads=None):
+    """The same population as batch_population, each mesh with the Far-form subdivision masks
+    of its levels instead of a table: masks = (number of control vertices, per-level masks),
+    the input of the GPU stencil-table factory.  Host topology and masks are produced on
+    `threads` host threads, largest meshes first, at most 2 x threads meshes ahead of the
+    consumer (bounded host memory); meshes are yielded as they complete, each with its
+    population `index`."""
+    import os
+    from concurrent.futures import FIRST_COMPLETED, ThreadPoolExecutor, wait
+
+    from .topology import load as _topo_load
+
+    def build(sp):
+        _topo_load().GB300TopologySetNumThreads(1)
+        cage, m = _population_mesh(sp, seed)
+        m["index"] = sp["index"]
+        m["masks"] = UniformRefiner(cage, sp["level"], stencils=False).factory_masks()
+        return m
+
+    _topo_load()
+    threads = threads or os.cpu_count() or 1
+    specs = sorted(_population_specs(n_meshes, cv_min, cv_max, seed),
+                   key=lambda sp: -sp["cv"] * 4.0 ** sp["level"])
+    with ThreadPoolExecutor(threads) as ex:
+        it = iter(specs)
+        pending = set()
+        for sp in it:
+            pending.add(ex.submit(build, sp))
+            if len(pending) >= 2 * threads:
+                break
+        while pending:
+            done, pending = wait(pending, return_when=FIRST_COMPLETED)
+            for f in done:
+                nxt = next(it, None)
+                if nxt is not None:
+                    pending.add(ex.submit(build, nxt))
+                yield f.result()
 
 
 def deform(base, phase, frame, amplitude=0.01):
