@@ -87,6 +87,37 @@ PATCH_TABLES = {
 }
 
 
+def host_link_gbs(nbytes=1 << 30, reps=5):
+    """Pinned host <-> device copy bandwidth right now (GB/s, median of `reps`, CUDA events)."""
+    import torch
+    h = torch.empty(nbytes // 4, pin_memory=True)
+    d = torch.empty(nbytes // 4, device="cuda")
+    out = {}
+    for name, dst, src in (("h2d", d, h), ("d2h", h, d)):
+        ms = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            dst.copy_(src, non_blocking=True)
+            e1.record()
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        out[name] = nbytes / (float(np.median(ms)) / 1e3) / 1e9
+    del h, d
+    return out
+
+
+def release_memory():
+    """Frees what a finished section left behind: Python objects (tables, buffers) and the
+    blocks torch's caching allocator keeps."""
+    import gc
+
+    import torch
+    gc.collect()
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+
+
 def fp32_rate(stream):
     """Measured FP32 FMA rate of this GPU in TFLOP/s (GB300MeasureFp32Rate, once per run)."""
     global _FP32
@@ -426,23 +457,39 @@ def bench_serving(args):
         res = []
         for rate in args.serve_rates:
             reqs, arr, work = trace(args.serve_requests, rate, 1000 + int(rate))
+            r0 = srv.stats()
             t1 = time.perf_counter()
             lat = srv.replay(reqs, arr)
             wall = time.perf_counter() - t1
+            r1 = srv.stats()
+            dl = {k: r1[k] - r0[k] for k in r1}
             res.append({"offered_req_per_s": rate, "requests": len(reqs),
                         "achieved_req_per_s": len(reqs) / wall,
                         "evals_per_s": work / wall,
                         "latency_ms": {"p50": float(np.percentile(lat, 50) * 1e3),
                                        "p99": float(np.percentile(lat, 99) * 1e3),
-                                       "mean": float(lat.mean() * 1e3)}})
+                                       "mean": float(lat.mean() * 1e3)},
+                        "time_split": {"wall_s": wall,
+                                       "scheduler_launch_s": dl["launchNanos"] / 1e9,
+                                       "streams_busy_wait_s": dl["streamsBusyNanos"] / 1e9,
+                                       "memory_wait_s": dl["memoryWaitNanos"] / 1e9,
+                                       "round_device_s": dl["roundDeviceNanos"] / 1e9,
+                                       "rounds": dl["rounds"], "uploads": dl["uploads"],
+                                       "upload_gb": dl["bytesUploaded"] / 1e9,
+                                       "h2d_gb": dl["h2dBytes"] / 1e9,
+                                       "d2h_gb": dl["d2hBytes"] / 1e9}})
         s1 = srv.stats()
         srv.close()
         return res, {k: s1[k] - s0[k] for k in ("rounds", "uploads", "evictions",
                                                  "completed", "failed")} | {
+            "host_pinned_gb": s1["hostPinnedBytes"] / 1e9,
+            "host_pin_failures": s1["hostPinFailures"],
             "peak_resident_gb": s1["peakResidentBytes"] / 1e9}
 
+    link_before = host_link_gbs()
     batched, bstats = serve(False)
     plain, pstats = serve(True)
+    link_after = host_link_gbs()
     table_gb = sum(len(t["refine"]["indices"]) * 8 + len(t["limit"]["pp_indices"]) * 8
                    + len(t["limit"]["patch_indices"]) * 4 for t in pool) / 1e9
     return {
@@ -452,6 +499,9 @@ def bench_serving(args):
                     f"(10k-1M points, P+du+dv), {args.serve_budget_gb} GB table budget",
         "pool_table_gb": table_gb, "generation_s": gen_s,
         "latency_definition": "submit -> results in pinned host memory",
+        "host_link_gbs": {"before": link_before, "after": link_after,
+                          "note": "pinned 1 GiB copies, median of 5: the serving rounds are "
+                                  "bound by this link (results back and table re-uploads)"},
         "batched": {"per_rate": batched, "stats": bstats},
         "plain_one_at_a_time": {"per_rate": plain, "stats": pstats},
     }
@@ -1154,12 +1204,18 @@ def run_gb300(args, rank, world):
     if not args.no_patches:
         line["eval_patches"] = bench_patches(args, stream, peak)
         line["eval_patches_loop"] = bench_patches(args, stream, peak, loop=True)
+    # serving first: its host-link-bound rounds measure lower after the batching section's
+    # 200 GB of tables have churned device and host memory
+    if not args.no_serving:
+        release_memory()
+        line["serving"] = bench_serving(args)
     if not args.no_batch:
+        release_memory()
         line["batching"] = bench_batch(args, stream, peak, args.batch_cv_max)
+        release_memory()
         if args.batch_cv_max_scaled > 0:
             line["batching_scaled"] = bench_batch(args, stream, peak, args.batch_cv_max_scaled)
-    if not args.no_serving:
-        line["serving"] = bench_serving(args)
+            release_memory()
     if not args.no_factory:
         line["factory"] = bench_factory(args, w)
     if args.layouts:

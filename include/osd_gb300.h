@@ -395,6 +395,16 @@ typedef struct {
 typedef struct {
     uint64_t submitted, completed, failed, rounds, uploads, evictions;
     uint64_t bytesUploaded, residentBytes, peakResidentBytes;
+    /* where the time goes (nanoseconds): the scheduler thread queueing rounds (host API
+     * calls), waiting with requests pending while every stream is busy, waiting with
+     * requests pending for arena or table-pool space; and the rounds' device time (first
+     * copy to completion, CUDA events, summed over rounds) */
+    uint64_t launchNanos, streamsBusyNanos, memoryWaitNanos, roundDeviceNanos;
+    /* request bytes copied host -> device (control values, queries) and back (results) */
+    uint64_t h2dBytes, d2hBytes;
+    /* host table bytes page-locked by the server (pinHostTables), and table ranges that could
+     * not be (their uploads are staged through pageable copies) */
+    uint64_t hostPinnedBytes, hostPinFailures;
 } GB300ServerStats;
 
 /* ---- table cache (no counterpart in the reference) --------------------------------------- */

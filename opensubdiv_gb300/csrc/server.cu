@@ -154,6 +154,11 @@ struct Round {
     size_t metaOff = 0, metaBytes = 0;  // job table + tile prefix + counter/status in the arena
     std::atomic<bool> done{false};
     Clock::time_point tDone;
+    cudaEvent_t start = nullptr, end = nullptr;  // device time of the round
+    ~Round() {
+        if (start) cudaEventDestroy(start);
+        if (end) cudaEventDestroy(end);
+    }
 };
 
 }  // namespace serve
@@ -326,6 +331,11 @@ int launch_round(GB300Server *s, Round *r) {
     do {                                                   \
         if (err == GB300_OK) err = check_cuda((call), what); \
     } while (0)
+    if (cudaEventCreate(&r->start) == cudaSuccess && cudaEventCreate(&r->end) == cudaSuccess)
+        cudaEventRecord(r->start, st);
+    else
+        cudaGetLastError();
+    uint64_t h2d = 0, d2h = 0;
     for (Topology *t : r->uploads)
         if (err == GB300_OK) err = upload_tables(s, t, st);
     // tables uploaded by rounds on other streams
@@ -342,8 +352,10 @@ int launch_round(GB300Server *s, Round *r) {
         const GB300TopologyDesc &d = q->topo->d;
         chk(cudaMemcpyAsync(a + q->oCv, q->r.controlValues, (size_t)d.numControl * d.length * 4,
                             cudaMemcpyHostToDevice, st), "GB300Server input copy");
+        h2d += (size_t)d.numControl * d.length * 4;
         if (q->r.kind == GB300_REQUEST_LIMIT) {
             const size_t n = (size_t)q->r.numPoints * 4;
+            h2d += 3 * n;
             chk(cudaMemcpyAsync(a + q->oFaces, q->r.faces, n, cudaMemcpyHostToDevice, st),
                 "GB300Server input copy");
             chk(cudaMemcpyAsync(a + q->oU, q->r.u, n, cudaMemcpyHostToDevice, st),
@@ -441,11 +453,18 @@ int launch_round(GB300Server *s, Round *r) {
     // results back to the host
     for (Request *q : r->reqs) {
         const size_t bytes = out_bytes(*q);
+        d2h += bytes;
         if (bytes)
             chk(cudaMemcpyAsync(q->r.out, s->arena.at(q->arenaOff) + q->oOut, bytes,
                                 cudaMemcpyDeviceToHost, st), "GB300Server output copy");
     }
+    if (r->end) cudaEventRecord(r->end, st);
     chk(cudaLaunchHostFunc(st, on_round_done, r), "GB300Server completion callback");
+    {
+        std::lock_guard<std::mutex> lock(s->m);
+        s->stats.h2dBytes += h2d;
+        s->stats.d2hBytes += d2h;
+    }
 #undef chk
     return err;
 }
@@ -473,6 +492,11 @@ void reap(GB300Server *s) {
             finish_request(s, q, GB300_OK, r->tDone);
         }
         if (r->metaBytes) s->arena.release(r->metaOff, r->metaBytes);
+        float ms = 0.0f;
+        if (r->start && r->end && cudaEventElapsedTime(&ms, r->start, r->end) == cudaSuccess)
+            s->stats.roundDeviceNanos += (uint64_t)(ms * 1e6);
+        else
+            cudaGetLastError();
         s->streamBusy[r->stream] = 0;
         s->inflight.erase(s->inflight.begin() + i);
         s->doneCv.notify_all();
@@ -493,7 +517,10 @@ void scheduler(GB300Server *s) {
                 break;
             }
         if (free < 0 || s->pending.empty()) {
+            const auto w0 = Clock::now();
             s->cv.wait_for(lock, std::chrono::microseconds(200));
+            if (!s->pending.empty())
+                s->stats.streamsBusyNanos += (uint64_t)(seconds_since(w0) * 1e9);
             continue;
         }
         auto round = std::make_unique<Round>();
@@ -505,7 +532,9 @@ void scheduler(GB300Server *s) {
                            align256((size_t)(maxPer + 1) * sizeof(int)) + 256;
         if (!s->arena.alloc(round->metaBytes, round->metaOff)) {
             round->metaBytes = 0;
+            const auto w0 = Clock::now();
             s->cv.wait_for(lock, std::chrono::microseconds(200));
+            s->stats.memoryWaitNanos += (uint64_t)(seconds_since(w0) * 1e9);
             continue;
         }
         while (!s->pending.empty() && (int)round->reqs.size() < maxPer) {
@@ -526,7 +555,9 @@ void scheduler(GB300Server *s) {
         }
         if (round->reqs.empty()) {
             s->arena.release(round->metaOff, round->metaBytes);
+            const auto w0 = Clock::now();
             s->cv.wait_for(lock, std::chrono::microseconds(200));
+            s->stats.memoryWaitNanos += (uint64_t)(seconds_since(w0) * 1e9);
             continue;
         }
         s->streamBusy[free] = 1;
@@ -535,8 +566,11 @@ void scheduler(GB300Server *s) {
         s->inflight.push_back(std::move(round));
         // launch outside the lock (the completion callback takes it)
         lock.unlock();
+        const auto l0 = Clock::now();
         const int err = launch_round(s, r);
+        const uint64_t launchNs = (uint64_t)(seconds_since(l0) * 1e9);
         lock.lock();
+        s->stats.launchNanos += launchNs;
         if (err != GB300_OK) {
             // the callback may still run if it was queued; wait for the stream to drain
             lock.unlock();
@@ -668,6 +702,7 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
     int st = check_cuda(cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming), who);
     if (st != GB300_OK) return st;
     std::vector<void *> pinned;  // CUDA calls stay outside the server lock
+    uint64_t pinnedBytes = 0, pinFailures = 0;
     if (s->cfg.pinHostTables) {
         // page-lock the arrays uploads read from; ranges another topology already registered
         // (shared tables) are left as they are, and a range that cannot be registered stays
@@ -676,10 +711,13 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
             if (!p || !bytes) return;
             const cudaError_t e = cudaHostRegister(const_cast<void *>(p), bytes,
                                                    cudaHostRegisterDefault);
-            if (e == cudaSuccess)
+            if (e == cudaSuccess) {
                 pinned.push_back(const_cast<void *>(p));
-            else
+                pinnedBytes += bytes;
+            } else {
+                if (e != cudaErrorHostMemoryAlreadyRegistered) ++pinFailures;
                 cudaGetLastError();
+            }
         };
         pin(d->sizes, (size_t)d->numStencils * 4);
         pin(d->offsets, (size_t)d->numStencils * 4);
@@ -698,6 +736,8 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
     }
     std::lock_guard<std::mutex> lock(s->m);
     s->registered.insert(s->registered.end(), pinned.begin(), pinned.end());
+    s->stats.hostPinnedBytes += pinnedBytes;
+    s->stats.hostPinFailures += pinFailures;
     auto it = s->topos.find(id);
     if (it != s->topos.end()) {
         cudaEventDestroy(t->ready);

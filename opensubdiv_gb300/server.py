@@ -45,7 +45,10 @@ class Request(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(k, C.c_uint64) for k in ("submitted", "completed", "failed", "rounds",
                                           "uploads", "evictions", "bytesUploaded",
-                                          "residentBytes", "peakResidentBytes")]
+                                          "residentBytes", "peakResidentBytes", "launchNanos",
+                                          "streamsBusyNanos", "memoryWaitNanos",
+                                          "roundDeviceNanos", "h2dBytes", "d2hBytes",
+                                          "hostPinnedBytes", "hostPinFailures")]
 
 
 def _addr(a):
