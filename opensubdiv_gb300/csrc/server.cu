@@ -4,9 +4,10 @@
 // Memory: two device pools are allocated once at creation -- the table pool (the budget for
 // resident topologies' stencil / patch tables and PatchMaps) and the request arena (inputs,
 // outputs and scratch of requests in flight) -- and sub-allocated first-fit, so serving never
-// calls cudaMalloc / cudaFree (which would synchronise the device).  A topology is uploaded
-// when a request needs it and is not resident, evicting least-recently-used topologies that no
-// in-flight request pins.
+// calls cudaMalloc / cudaFree (which would synchronise the device).  A topology's tables are
+// resident in two independent units -- its refine table, and its limit tables (patch-point
+// stencils, patch table, PatchMap) -- so a request uploads only the unit it reads when that
+// unit is not resident, evicting least-recently-used units that no in-flight request pins.
 //
 // Scheduling: one scheduler thread takes pending requests in arrival order into a round while
 // a stream is free, the round's requests fit the arena and their topologies fit the pool, up
@@ -118,19 +119,24 @@ struct Topology {
     int quadFamily = 0;
     PatchMapHost map;
     double refineMean = 0, ppMean = 0;
-    // device footprint: piece offsets inside the topology's pool range
-    Layout lay;
+    // device footprint: unit 0 holds the refine table (oSizes .. oWeights, offsets inside
+    // unit 0's pool range), unit 1 the limit tables (oPpSizes .. oHandles, inside unit 1's)
     size_t oSizes, oOffsets, oIndices, oWeights;
     size_t oPpSizes, oPpOffsets, oPpIndices, oPpWeights;
     size_t oArrays, oPIndices, oParams, oNodes, oHandles;
-    // residency
-    bool resident = false;
-    bool needsUpload = false;
-    size_t poolOff = 0;
-    int pins = 0;
-    uint64_t lastUse = 0;
-    cudaEvent_t ready = nullptr;  // recorded after the latest upload
+    struct Unit {
+        Layout lay;
+        bool resident = false;
+        bool needsUpload = false;
+        size_t poolOff = 0;
+        int pins = 0;
+        uint64_t lastUse = 0;
+        cudaEvent_t ready = nullptr;  // recorded after the latest upload
+    } unit[2];
 };
+
+// The unit a request reads: refine requests the refine table, limit requests the limit tables.
+inline int unit_of(int kind) { return kind == GB300_REQUEST_LIMIT ? 1 : 0; }
 
 struct Request {
     GB300Request r{};
@@ -148,7 +154,7 @@ struct Round {
     GB300Server *srv = nullptr;
     std::vector<Request *> reqs;
     int stream = 0;
-    std::vector<Topology *> uploads;  // topologies this round uploads before its work
+    std::vector<std::pair<Topology *, int>> uploads;  // (topology, unit) uploaded first
     std::vector<batch::Job> jobs;
     std::vector<int> tileBase;
     size_t metaOff = 0, metaBytes = 0;  // job table + tile prefix + counter/status in the arena
@@ -229,38 +235,38 @@ size_t out_bytes(const Request &q) {
                                             : (size_t)q.r.numPoints * 36;
 }
 
-// Reserves table-pool space for `t`, evicting least-recently-used topologies that no
+// Reserves table-pool space for unit k of `t`, evicting least-recently-used units that no
 // in-flight request pins; false if it cannot fit now.  Called with the lock held; the upload
 // itself happens outside the lock (upload_tables).
-bool reserve(GB300Server *s, Topology *t) {
-    if (t->resident) return true;
+bool reserve(GB300Server *s, Topology *t, int k) {
+    Topology::Unit &u = t->unit[k];
+    if (u.resident) return true;
     size_t off = 0;
-    while (!s->tables.alloc(t->lay.total, off)) {
-        Topology *victim = nullptr;
-        for (auto &kv : s->topos) {
-            Topology *c = kv.second.get();
-            if (c->resident && c->pins == 0 && (!victim || c->lastUse < victim->lastUse))
-                victim = c;
-        }
+    while (!s->tables.alloc(u.lay.total, off)) {
+        Topology::Unit *victim = nullptr;
+        for (auto &kv : s->topos)
+            for (Topology::Unit &c : kv.second->unit)
+                if (c.resident && c.pins == 0 && (!victim || c.lastUse < victim->lastUse))
+                    victim = &c;
         if (!victim) return false;
         s->tables.release(victim->poolOff, victim->lay.total);
         victim->resident = false;
         s->stats.evictions++;
         s->stats.residentBytes -= victim->lay.total;
     }
-    t->resident = true;
-    t->needsUpload = true;
-    t->poolOff = off;
+    u.resident = true;
+    u.needsUpload = true;
+    u.poolOff = off;
     s->stats.uploads++;
-    s->stats.bytesUploaded += t->lay.total;
-    s->stats.residentBytes += t->lay.total;
+    s->stats.bytesUploaded += u.lay.total;
+    s->stats.residentBytes += u.lay.total;
     s->stats.peakResidentBytes = std::max(s->stats.peakResidentBytes, s->stats.residentBytes);
     return true;
 }
 
-// Host -> device copies of a reserved topology's tables on `st`, then its ready event.
-int upload_tables(GB300Server *s, Topology *t, cudaStream_t st) {
-    char *b = s->tables.at(t->poolOff);
+// Host -> device copies of unit k of a reserved topology on `st`, then the unit's ready event.
+int upload_tables(GB300Server *s, Topology *t, int k, cudaStream_t st) {
+    char *b = s->tables.at(t->unit[k].poolOff);
     const GB300TopologyDesc &d = t->d;
     int err = GB300_OK;
     auto h2d = [&](size_t o, const void *src, size_t bytes) {
@@ -268,11 +274,12 @@ int upload_tables(GB300Server *s, Topology *t, cudaStream_t st) {
             err = check_cuda(cudaMemcpyAsync(b + o, src, bytes, cudaMemcpyHostToDevice, st),
                              "GB300Server table upload");
     };
-    h2d(t->oSizes, d.sizes, (size_t)d.numStencils * 4);
-    h2d(t->oOffsets, d.offsets, (size_t)d.numStencils * 4);
-    h2d(t->oIndices, d.indices, (size_t)d.nnz * 4);
-    h2d(t->oWeights, d.weights, (size_t)d.nnz * 4);
-    if (t->limit) {
+    if (k == 0) {
+        h2d(t->oSizes, d.sizes, (size_t)d.numStencils * 4);
+        h2d(t->oOffsets, d.offsets, (size_t)d.numStencils * 4);
+        h2d(t->oIndices, d.indices, (size_t)d.nnz * 4);
+        h2d(t->oWeights, d.weights, (size_t)d.nnz * 4);
+    } else {
         h2d(t->oPpSizes, d.ppSizes, (size_t)d.numPatchPoints * 4);
         h2d(t->oPpOffsets, d.ppOffsets, (size_t)d.numPatchPoints * 4);
         h2d(t->oPpIndices, d.ppIndices, (size_t)d.patchPointNnz * 4);
@@ -283,12 +290,13 @@ int upload_tables(GB300Server *s, Topology *t, cudaStream_t st) {
         h2d(t->oNodes, t->map.nodes.data(), t->map.nodes.size() * 4);
         h2d(t->oHandles, t->map.handles.data(), t->map.handles.size() * 4);
     }
-    if (err == GB300_OK) err = check_cuda(cudaEventRecord(t->ready, st), "GB300Server upload");
+    if (err == GB300_OK)
+        err = check_cuda(cudaEventRecord(t->unit[k].ready, st), "GB300Server upload");
     return err;
 }
 
 PatchMapDevice device_map(GB300Server *s, Topology *t) {
-    char *b = s->tables.at(t->poolOff);
+    char *b = s->tables.at(t->unit[1].poolOff);
     PatchMapDevice pm;
     pm.nodes = b + t->oNodes;
     pm.handles = b + t->oHandles;
@@ -336,15 +344,18 @@ int launch_round(GB300Server *s, Round *r) {
     else
         cudaGetLastError();
     uint64_t h2d = 0, d2h = 0;
-    for (Topology *t : r->uploads)
-        if (err == GB300_OK) err = upload_tables(s, t, st);
+    for (auto &up : r->uploads)
+        if (err == GB300_OK) err = upload_tables(s, up.first, up.second, st);
     // tables uploaded by rounds on other streams
-    std::vector<Topology *> seen;
-    for (Request *q : r->reqs)
-        if (std::find(seen.begin(), seen.end(), q->topo) == seen.end()) {
-            seen.push_back(q->topo);
-            chk(cudaStreamWaitEvent(st, q->topo->ready, 0), "GB300Server table wait");
+    std::vector<std::pair<Topology *, int>> seen;
+    for (Request *q : r->reqs) {
+        const std::pair<Topology *, int> key(q->topo, unit_of(q->r.kind));
+        if (std::find(seen.begin(), seen.end(), key) == seen.end()) {
+            seen.push_back(key);
+            chk(cudaStreamWaitEvent(st, q->topo->unit[key.second].ready, 0),
+                "GB300Server table wait");
         }
+    }
     std::vector<double> mean;
     // inputs
     for (Request *q : r->reqs) {
@@ -368,7 +379,7 @@ int launch_round(GB300Server *s, Round *r) {
     for (Request *q : r->reqs) {
         Topology *t = q->topo;
         char *a = s->arena.at(q->arenaOff);
-        char *b = s->tables.at(t->poolOff);
+        char *b = s->tables.at(t->unit[unit_of(q->r.kind)].poolOff);
         const GB300TopologyDesc &d = t->d;
         const float *cv = (const float *)(a + q->oCv);
         if (q->r.kind == GB300_REQUEST_REFINE) {
@@ -437,7 +448,7 @@ int launch_round(GB300Server *s, Round *r) {
         if (q->r.kind != GB300_REQUEST_LIMIT || q->r.numPoints == 0 || err != GB300_OK) continue;
         Topology *t = q->topo;
         char *a = s->arena.at(q->arenaOff);
-        char *b = s->tables.at(t->poolOff);
+        char *b = s->tables.at(t->unit[1].poolOff);
         const int n = q->r.numPoints;
         err = find_patches(device_map(s, t), n, (const int *)(a + q->oFaces),
                            (const float *)(a + q->oU), (const float *)(a + q->oV),
@@ -488,7 +499,7 @@ void reap(GB300Server *s) {
         }
         for (Request *q : r->reqs) {
             s->arena.release(q->arenaOff, q->lay.total);
-            q->topo->pins--;
+            q->topo->unit[unit_of(q->r.kind)].pins--;
             finish_request(s, q, GB300_OK, r->tDone);
         }
         if (r->metaBytes) s->arena.release(r->metaOff, r->metaBytes);
@@ -539,17 +550,19 @@ void scheduler(GB300Server *s) {
         }
         while (!s->pending.empty() && (int)round->reqs.size() < maxPer) {
             Request *q = s->pending.front();
+            const int k = unit_of(q->r.kind);
+            Topology::Unit &u = q->topo->unit[k];
             if (!s->arena.alloc(q->lay.total, q->arenaOff)) break;
-            if (!reserve(s, q->topo)) {  // wait for in-flight rounds to unpin tables
+            if (!reserve(s, q->topo, k)) {  // wait for in-flight rounds to unpin tables
                 s->arena.release(q->arenaOff, q->lay.total);
                 break;
             }
-            if (q->topo->needsUpload) {
-                q->topo->needsUpload = false;
-                round->uploads.push_back(q->topo);
+            if (u.needsUpload) {
+                u.needsUpload = false;
+                round->uploads.emplace_back(q->topo, k);
             }
-            q->topo->pins++;
-            q->topo->lastUse = ++s->useClock;
+            u.pins++;
+            u.lastUse = ++s->useClock;
             s->pending.pop_front();
             round->reqs.push_back(q);
         }
@@ -578,15 +591,17 @@ void scheduler(GB300Server *s) {
             lock.lock();
             for (Request *q : r->reqs) {
                 s->arena.release(q->arenaOff, q->lay.total);
-                q->topo->pins--;
+                q->topo->unit[unit_of(q->r.kind)].pins--;
                 finish_request(s, q, err, Clock::now());
             }
-            for (Topology *t : r->uploads)  // their tables may be incomplete: drop them
-                if (t->resident) {
-                    s->tables.release(t->poolOff, t->lay.total);
-                    t->resident = false;
-                    s->stats.residentBytes -= t->lay.total;
+            for (auto &up : r->uploads) {  // their tables may be incomplete: drop them
+                Topology::Unit &u = up.first->unit[up.second];
+                if (u.resident) {
+                    s->tables.release(u.poolOff, u.lay.total);
+                    u.resident = false;
+                    s->stats.residentBytes -= u.lay.total;
                 }
+            }
             s->arena.release(r->metaOff, r->metaBytes);
             s->streamBusy[free] = 0;
             for (size_t i = 0; i < s->inflight.size(); ++i)
@@ -643,7 +658,8 @@ void GB300ServerDestroy(GB300Server *s) {
     if (s->worker.joinable()) s->worker.join();
     for (cudaStream_t st : s->streams) cudaStreamDestroy(st);
     for (auto &kv : s->topos)
-        if (kv.second->ready) cudaEventDestroy(kv.second->ready);
+        for (Topology::Unit &u : kv.second->unit)
+            if (u.ready) cudaEventDestroy(u.ready);
     for (void *p : s->registered) cudaHostUnregister(p);
     for (void *c : s->caches) GB300TableCacheClose(c);
     delete s;
@@ -680,11 +696,12 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
     }
     t->refineMean = d->numStencils ? (double)d->nnz / d->numStencils : 0;
     t->ppMean = d->numPatchPoints ? (double)d->patchPointNnz / d->numPatchPoints : 0;
-    Layout &L = t->lay;
-    t->oSizes = L.add((size_t)d->numStencils * 4);
-    t->oOffsets = L.add((size_t)d->numStencils * 4);
-    t->oIndices = L.add((size_t)d->nnz * 4);
-    t->oWeights = L.add((size_t)d->nnz * 4);
+    Layout &L0 = t->unit[0].lay;
+    t->oSizes = L0.add((size_t)d->numStencils * 4);
+    t->oOffsets = L0.add((size_t)d->numStencils * 4);
+    t->oIndices = L0.add((size_t)d->nnz * 4);
+    t->oWeights = L0.add((size_t)d->nnz * 4);
+    Layout &L = t->unit[1].lay;
     if (t->limit) {
         t->oPpSizes = L.add((size_t)d->numPatchPoints * 4);
         t->oPpOffsets = L.add((size_t)d->numPatchPoints * 4);
@@ -696,11 +713,17 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
         t->oNodes = L.add(t->map.nodes.size() * 4);
         t->oHandles = L.add(t->map.handles.size() * 4);
     }
-    if (L.total > s->tables.capacity())
+    if (std::max(L0.total, L.total) > s->tables.capacity())
         return fail(GB300_ERR_INVALID_ARGUMENT, "%s: topology %d needs %zu bytes, budget %zu",
-                    who, id, L.total, s->tables.capacity());
-    int st = check_cuda(cudaEventCreateWithFlags(&t->ready, cudaEventDisableTiming), who);
-    if (st != GB300_OK) return st;
+                    who, id, std::max(L0.total, L.total), s->tables.capacity());
+    for (Topology::Unit &u : t->unit) {
+        const int st = check_cuda(cudaEventCreateWithFlags(&u.ready, cudaEventDisableTiming), who);
+        if (st != GB300_OK) {
+            for (Topology::Unit &v : t->unit)
+                if (v.ready) cudaEventDestroy(v.ready);
+            return st;
+        }
+    }
     std::vector<void *> pinned;  // CUDA calls stay outside the server lock
     uint64_t pinnedBytes = 0, pinFailures = 0;
     if (s->cfg.pinHostTables) {
@@ -740,7 +763,7 @@ int GB300ServerAddTopology(GB300Server *s, int id, const GB300TopologyDesc *d) {
     s->stats.hostPinFailures += pinFailures;
     auto it = s->topos.find(id);
     if (it != s->topos.end()) {
-        cudaEventDestroy(t->ready);
+        for (Topology::Unit &u : t->unit) cudaEventDestroy(u.ready);
         return fail(GB300_ERR_INVALID_ARGUMENT, "%s: topology %d already registered", who, id);
     }
     s->topos[id] = std::move(t);
