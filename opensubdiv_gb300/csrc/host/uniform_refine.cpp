@@ -814,10 +814,11 @@ int GB300TopologyLimitStencils(void *p, int n, const int *faces, const float *u,
             int c[4];
             double s, tt;
             if (!locate(*t, L, faces[i], u[i], v[i], c, s, tt, emaps)) continue;
-            const Level &l0 = t->levels[0];
-            int f = (int)(std::upper_bound(t->ptexOff.begin(), t->ptexOff.end(), faces[i]) -
-                          t->ptexOff.begin()) - 1;
-            const double ds = (l0.fOff[f + 1] - l0.fOff[f] == 4) ? scale : scale / 2.0;
+            // derivatives with respect to the ptex face's (u, v) scaled by 2^L on every face,
+            // the sub-faces of non-quads included: Far's convention (its patch bases scale by
+            // 2^depth whatever the non-quad root), so the table equals
+            // LimitStencilTableFactory's
+            const double ds = scale;
             const double wp[4] = {(1 - s) * (1 - tt), s * (1 - tt), s * tt, (1 - s) * tt};
             const double wu[4] = {-(1 - tt) * ds, (1 - tt) * ds, tt * ds, -tt * ds};
             const double wv[4] = {-(1 - s) * ds, -s * ds, s * ds, (1 - s) * ds};

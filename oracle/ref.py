@@ -65,12 +65,17 @@ class Refiner:
         L = lib()
         cv = np.ascontiguousarray(cage.crease_verts, np.int32).ravel()
         cs = np.ascontiguousarray(cage.crease_sharpness, np.float32)
-        self._keep = (cage.verts_per_face, cage.face_verts, cv, cs)
+        # optional vertex (corner) sharpness and boundary interpolation of the cage
+        kv = np.ascontiguousarray(getattr(cage, "corner_verts", np.zeros(0)), np.int32)
+        ks = np.ascontiguousarray(getattr(cage, "corner_sharpness", np.zeros(0)), np.float32)
+        boundary = int(getattr(cage, "boundary", boundary))
+        self._keep = (cage.verts_per_face, cage.face_verts, cv, cs, kv, ks)
         if fvar is None:
             self.h = L.ref_refiner_create(
                 C.c_int(cage.scheme), C.c_int(cage.num_vertices), C.c_int(cage.num_faces),
                 _p(cage.verts_per_face), _p(cage.face_verts), C.c_int(len(cs)), _p(cv), _p(cs),
-                C.c_int(0), None, None, C.c_int(boundary))
+                C.c_int(len(ks)), _p(kv) if len(ks) else None, _p(ks) if len(ks) else None,
+                C.c_int(boundary))
         else:
             nvals, fidx, linear = fvar
             fidx = np.ascontiguousarray(fidx, np.int32)

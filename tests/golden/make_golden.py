@@ -289,6 +289,93 @@ def factory_limit_fixture(path):
     np.savez_compressed(path, **out)
 
 
+REFERENCE = os.environ.get("OPENSUBDIV_SOURCE", "/root/reference")
+
+
+def regression_shape(name):
+    """A cage from the reference's regression shape `name` (regression/shapes/<name>.h: OBJ
+    text in a C string -- v / f lines and crease, corner and interpolateboundary tags), read
+    as data where the reference's sources are.  Boundary interpolation follows the
+    regression tools (regression/common/far_utils.h:76-95): edge-only unless tagged."""
+    path = os.path.join(REFERENCE, "regression", "shapes", name + ".h")
+    src = open(path).read()
+    body = src[src.index("std::string " + name):]
+    # one string literal per line: "<obj line>\n"
+    text = "".join(ln.strip()[1:-1] for ln in body.splitlines()[1:]
+                   if ln.strip().startswith('"') and ln.strip().endswith('"'))
+    text = text.replace("\\n", "\n")
+    pos, vpf, fv, cv, cs, kv, ks = [], [], [], [], [], [], []
+    boundary = 1  # Sdc VTX_BOUNDARY_EDGE_ONLY
+    for line in text.split("\n"):
+        t = line.split()
+        if not t:
+            continue
+        if t[0] == "v":
+            pos.append([float(x) for x in t[1:4]])
+        elif t[0] == "f":
+            idx = [int(x.split("/")[0]) - 1 for x in t[1:]]
+            vpf.append(len(idx))
+            fv.extend(idx)
+        elif t[0] == "t":
+            ni, nf = (int(x) for x in t[2].split("/")[:2])
+            ints = [int(x) for x in t[3:3 + ni]]
+            fls = [float(x) for x in t[3 + ni:3 + ni + nf]]
+            if t[1] == "crease":
+                for a, b in zip(ints[:-1], ints[1:]):
+                    cv.append((a, b))
+                    cs.append(fls[0])
+            elif t[1] == "corner":
+                kv.extend(ints)
+                ks.extend([fls[0]] * len(ints))
+            elif t[1] == "interpolateboundary":
+                boundary = {0: 0, 1: 2, 2: 1}[ints[0]]
+    scheme = shapes.LOOP if name.startswith("loop") else shapes.CATMARK
+    cage = shapes.Cage(np.asarray(pos, np.float32), np.asarray(vpf, np.int32),
+                       np.asarray(fv, np.int32), scheme=scheme, name=name)
+    cage.crease_verts = np.asarray(cv, np.int32).reshape(-1, 2)
+    cage.crease_sharpness = np.asarray(cs, np.float32)
+    cage.corner_verts = np.asarray(kv, np.int32)
+    cage.corner_sharpness = np.asarray(ks, np.float32)
+    cage.boundary = boundary
+    return cage
+
+
+# The reference's regression shapes in the parity set: a valence-360 pole (stencils of 360+
+# entries), boundaries with extraordinary vertices and both boundary interpolations, corner
+# and crease tags, non-manifold edges, and Loop boundaries / poles.
+REGRESSION_SHAPES = [
+    ("catmark_pole360", 2, 3), ("catmark_xord_boundary", 3, 3), ("catmark_edgecorner", 3, 3),
+    ("catmark_cube_corner2", 3, 3), ("catmark_cube_creases1", 3, 3),
+    ("catmark_nonman_edges", 2, 3), ("loop_triangle_edgecorner", 3, 3),
+    ("loop_xord_boundary", 3, 3), ("loop_pole64", 2, 3),
+]
+
+
+def regression_fixtures():
+    for k, (name, ulevel, alevel) in enumerate(REGRESSION_SHAPES):
+        cage = regression_shape(name)
+        stencil_fixture(os.path.join(HERE, f"reg_{name}_uniform_L{ulevel}.npz"), cage, ulevel,
+                        seed=100 + k, limit_level=alevel, nlimit=400)
+        patch_fixture(os.path.join(HERE, f"reg_{name}_patches_L{alevel}.npz"), cage, alevel,
+                      seed=200 + k, nq=1000)
+
+
+def limit_pin_fixture(path):
+    """Far::LimitStencilTableFactory on a uniform refiner (far/stencilTableFactory.cpp:411-662;
+    the limit surface of a uniform table is bilinear over the last level's faces) at seeded
+    locations: the table the workload generator's limit_stencil_table must reproduce."""
+    cage = shapes.torus(16, 8, tri_fraction=0.1, crease_fraction=0.05, seed=3)
+    level = 2
+    r = ref.Refiner(cage).refine_uniform(level)
+    face, u, v = shapes.uniform_locations(cage, 500, seed=4)
+    lt = ref.limit_stencil_table(r, face, u, v, d1=True)
+    out = dict(cage_arrays(cage))
+    out.update(level=np.int32(level), face=face, u=u, v=v)
+    for k in ("sizes", "offsets", "indices", "weights", "du_weights", "dv_weights"):
+        out[k] = lt[k]
+    np.savez_compressed(path, **out)
+
+
 LARGE = os.path.join(HERE, "large")
 
 
@@ -337,6 +424,10 @@ def main():
             raise SystemExit("oracle/_ref/libosdref.so missing: run `make -C oracle ref` first")
         large_workloads()
         return
+    if len(sys.argv) > 1 and sys.argv[1] == "regression":
+        regression_fixtures()
+        limit_pin_fixture(os.path.join(HERE, "uniform_limit_pin.npz"))
+        return
     if len(sys.argv) > 1 and sys.argv[1] == "factory":
         factory_fixture(os.path.join(HERE, "factory_masks.npz"))
         factory_limit_fixture(os.path.join(HERE, "factory_limit.npz"))
@@ -381,6 +472,9 @@ def main():
                   nq=1500, adaptive=False)
     factory_fixture(os.path.join(g, "factory_masks.npz"))
     factory_limit_fixture(os.path.join(g, "factory_limit.npz"))
+    # the reference's regression shapes, and the uniform-refiner limit-stencil pin
+    regression_fixtures()
+    limit_pin_fixture(os.path.join(g, "uniform_limit_pin.npz"))
     for f in sorted(os.listdir(g)):
         if f.endswith(".npz"):
             print(f"{f:40s} {os.path.getsize(os.path.join(g, f)) / 1024:8.1f} KiB")

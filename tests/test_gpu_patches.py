@@ -17,9 +17,9 @@ import oracle
 from gpu_util import bbox_diag, bbox_diag_rows, dev, gate, host, smooth_primvars, torch_cuda
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-STENCIL_FIXTURES = set(glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz")))
-FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*.npz"))) - STENCIL_FIXTURES -
-                  set(glob.glob(os.path.join(GOLDEN, "factory_*.npz"))))
+FIXTURES = sorted(set(glob.glob(os.path.join(GOLDEN, "*_patches_*.npz"))) |
+                  set(glob.glob(os.path.join(GOLDEN, "*_uniform_quads_*.npz"))) |
+                  set(glob.glob(os.path.join(GOLDEN, "*_uniform_tris_*.npz"))))
 NAMES = ("P", "du", "dv", "duu", "duv", "dvv")
 
 

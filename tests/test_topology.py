@@ -15,7 +15,10 @@ from scipy.spatial import cKDTree
 from opensubdiv_gb300 import shapes, topology
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
-FIXTURES = sorted(glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz")))
+# the generator takes closed cages with creases only: the reference's regression shapes (open
+# boundaries, corner tags, non-manifold edges; reg_*) are outside its domain
+FIXTURES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "*_uniform_L*.npz"))
+                  if not os.path.basename(p).startswith("reg_"))
 
 
 def _cage(z):
@@ -53,6 +56,26 @@ def test_generator_reproduces_far_stencil_tables(path):
         a, b = _row(mine, i), _row(far, j[i])
         assert set(a) == set(b)
         assert max(abs(a[k] - b[k]) for k in a) <= 2.4e-7
+
+
+def test_generator_limit_stencils_match_far_on_a_uniform_refiner():
+    """The generator's limit stencils (config 2's limit pass) against the table
+    Far::LimitStencilTableFactory builds on the same uniform refiner at the same locations
+    (far/stencilTableFactory.cpp:411-662; tests/golden/uniform_limit_pin.npz): the same
+    supports, with P / du / dv weights within float rounding."""
+    z = np.load(os.path.join(GOLDEN, "uniform_limit_pin.npz"))
+    cage = _cage(z)
+    mine = topology.UniformRefiner(cage, int(z["level"])).limit_stencil_table(z["face"], z["u"],
+                                                                            z["v"])
+    assert np.array_equal(mine["sizes"], z["sizes"])
+    for key in ("weights", "du_weights", "dv_weights"):
+        a = dict(sizes=mine["sizes"], offsets=mine["offsets"], indices=mine["indices"],
+                 weights=mine[key])
+        b = dict(sizes=z["sizes"], offsets=z["offsets"], indices=z["indices"], weights=z[key])
+        for i in range(len(z["sizes"])):
+            ra, rb = _row(a, i), _row(b, i)
+            assert set(ra) == set(rb), (key, i)
+            assert max(abs(ra[k] - rb[k]) for k in ra) <= 2e-6 * max(1.0, max(map(abs, rb.values()))), (key, i)
 
 
 def test_generator_limit_stencils_are_bilinear_partitions():
