@@ -268,6 +268,66 @@ int GB300PatchTableEvalFaceVarying(const GB300PatchTable *table, int channel, co
                                    int dvvStride, int numPatchCoords, const void *patchCoords,
                                    void *stream);
 
+/* ---- Bfr tessellation of a mesh (Bfr::Tessellation, bfr/tessellation.h:142-262) ----------- */
+
+/* Bfr::Tessellation::Options (bfr/tessellation.h:60-100).  facetSize: 4 selects quads-capable
+ * 4-tuples (a triangle's 4th index is -1), anything else triangles (SetFacetSize);
+ * preserveQuads keeps quads of quad-based faces when facetSize is 4; coordStride / facetStride
+ * are floats between (u,v) pairs and ints between facets, 0 for the defaults (2, facetSize). */
+typedef struct GB300TessellationOptions {
+    int facetSize;
+    int preserveQuads;
+    int coordStride;
+    int facetStride;
+} GB300TessellationOptions;
+
+/* One Bfr::Tessellation(Parameterization(scheme, faceSizes[f]), rates, options) per face of a
+ * mesh, all faces at once.  regularFaceSize is the scheme's regular face size (4: Catmark or
+ * Bilinear, 3: Loop) that Bfr::Parameterization derives from the scheme
+ * (bfr/parameterization.cpp:40-66).  Rates, all DEVICE arrays:
+ *   rates == NULL      every face uses the single rate uniformRate (Tessellation(p, rate));
+ *   rateOffsets == NULL  face f uses the single rate rates[f];
+ *   otherwise          face f uses rates[rateOffsets[f] .. rateOffsets[f+1]), interpreted as
+ *                      Tessellation(p, numRates, rates) interprets them (1 inner rate, N edge
+ *                      rates, N+1, or for quads 2 or N+2; bfr/tessellation.h:125-150).
+ * A face whose tessellation is invalid (a rate < 1, a face size the scheme rejects) gets no
+ * coords and no facets, as an invalid Bfr::Tessellation has none; callers skip faces without
+ * a limit surface (holes) the same way, with a rate of 0.
+ *
+ * Count writes, into DEVICE arrays of numFaces + 1 entries, the exclusive scans of each face's
+ * coord count (GetNumCoords), facet count (GetNumFacets) and ptex-face count (Far::PtexIndices,
+ * far/ptexIndices.cpp:37-55: 1 for a regular face, N for an N-gon), and the three totals into
+ * the HOST array totals[3].  It synchronizes `stream` to read the totals.  Totals above
+ * INT_MAX coords are rejected (facet indices are ints). */
+int GB300TessellationCount(int regularFaceSize, int numFaces, const int *faceSizes,
+                           const int *rateOffsets, const int *rates, int uniformRate,
+                           const GB300TessellationOptions *options, int64_t *coordOffsets,
+                           int64_t *facetOffsets, int64_t *ptexOffsets, int64_t *totals,
+                           void *stream);
+
+/* Writes every face's coords (Tessellation::GetCoords: boundary coords first, then interior,
+ * bit-identical to the reference's float coords) at coordOffsets[f] and its facets
+ * (GetFacets) at facetOffsets[f], into DEVICE buffers sized from Count's totals.  With
+ * offsetFacetIndices the facet indices are offset by coordOffsets[f] to number the mesh's
+ * coords (Tessellation::TransformFacetCoordIndices(facets, commonOffset),
+ * tessellation.cpp:2429-2447); otherwise they are face-local, as GetFacets returns them.
+ *
+ * With a patch table (built with the approximation the surfaces should have, e.g. the Far
+ * options the reference's Bfr regression pairs with Bfr::SurfaceFactory's defaults: isolation
+ * 6 for sharp and 2 for smooth features, Gregory-basis end caps, infinitely sharp patches,
+ * regression/bfr_evaluate/farPatchEvaluator.cpp:52-78) and ptexOffsets from Count, each coord
+ * is also located: Parameterization::ConvertCoordToNormalizedSubFace picks an N-gon's ptex
+ * sub-face and the table's PatchMap finds the patch, giving one OsdPatchCoord per coord in
+ * `patchCoords` (DEVICE, 5 x 32 bits each) for GB300PatchTableEval -- the Bfr::Surface::
+ * Evaluate of every tessellation coord of the mesh. */
+int GB300TessellationGenerate(int regularFaceSize, int numFaces, const int *faceSizes,
+                              const int *rateOffsets, const int *rates, int uniformRate,
+                              const GB300TessellationOptions *options,
+                              const int64_t *coordOffsets, const int64_t *facetOffsets,
+                              const int64_t *ptexOffsets, float *coords, int *facets,
+                              int offsetFacetIndices, const GB300PatchTable *table,
+                              void *patchCoords, void *stream);
+
 /* ---- vertex buffer (CudaVertexBuffer, osd/cudaVertexBuffer.h:42-79) ---------------------- */
 
 typedef struct GB300VertexBuffer GB300VertexBuffer;

@@ -143,6 +143,12 @@ struct GB300PatchTable {
     }
 };
 
+namespace gb300 {
+const PatchMapDevice *patch_map_of(const GB300PatchTable *table) {
+    return table ? &table->map : nullptr;
+}
+}  // namespace gb300
+
 struct GB300VertexBuffer {
     int numElements = 0, numVertices = 0;
     float *mem = nullptr;

@@ -10,13 +10,13 @@
 // reference rounds them.
 #include "common.cuh"
 #include "patchmap.h"
+#include "patchmap_walk.cuh"
 
 #include <algorithm>
 #include <cstring>
 
 namespace gb300 {
 
-static constexpr uint32_t kSet = 0x80000000u, kLeaf = 0x40000000u, kIndex = 0x3fffffffu;
 
 struct HostNode {
     uint32_t c[4];
@@ -121,9 +121,7 @@ int build_patch_map(int numArrays, const int *arrays, int numPatches, const int 
 }
 
 struct FindArgs {
-    const uint4 *nodes;
-    const int4 *handles;
-    int minFace, maxFace, maxDepth, triangular, numPatches;
+    PatchMapView map;
     int n;
     const int *faces;
     const float *u;
@@ -131,64 +129,11 @@ struct FindArgs {
     int *out;  // 5 x 32 bit per query (OsdPatchCoord)
 };
 
-__device__ __forceinline__ uint32_t child_of(const uint4 &n, int q) {
-    return q == 0 ? n.x : q == 1 ? n.y : q == 2 ? n.z : n.w;
-}
-
 __global__ void __launch_bounds__(256) k_find_patches(const FindArgs a) {
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += stride) {
-        const int f = a.faces[i];
         const float fu = a.u[i], fv = a.v[i];
-        int4 h = make_int4(-1, -1, -1, 0);
-        const bool in_range = a.numPatches > 0 && f >= a.minFace && f <= a.maxFace &&
-                              fu >= 0.0f && fu <= 1.0f && fv >= 0.0f && fv <= 1.0f;
-        if (in_range) {
-            uint4 node = __ldg(a.nodes + (f - a.minFace));
-            if (node.x & kSet) {
-                if (!a.triangular) {
-                    float u = fu, v = fv, median = 0.5f;
-                    for (int d = 0; d <= a.maxDepth; ++d, median *= 0.5f) {
-                        int q = 0;
-                        if (u >= median) { u -= median; q |= 1; }
-                        if (v >= median) { v -= median; q |= 2; }
-                        const uint32_t c = child_of(node, q);
-                        if (!(c & kSet)) break;
-                        if (c & kLeaf) { h = __ldg(a.handles + (c & kIndex)); break; }
-                        node = __ldg(a.nodes + (c & kIndex));
-                    }
-                } else {
-                    // every subtraction takes the power-of-two median from a value in
-                    // [median, 2 * median] (exact in float, Sterbenz), so u and v hold the
-                    // reference's double values exactly; only the sums u + v, which the
-                    // reference rounds in double, are formed in double
-                    float u = fu, v = fv, median = 0.5f;
-                    bool rot = false;
-                    for (int d = 0; d <= a.maxDepth; ++d, median *= 0.5f) {
-                        int q;
-                        if (!rot) {
-                            if (u >= median) { u -= median; q = 1; }
-                            else if (v >= median) { v -= median; q = 2; }
-                            else if (((double)u + (double)v) >= (double)median) { rot = true; q = 3; }
-                            else q = 0;
-                        } else {
-                            if (u < median) { v -= median; q = 1; }
-                            else if (v < median) { u -= median; q = 2; }
-                            else {
-                                u -= median;
-                                v -= median;
-                                if (((double)u + (double)v) < (double)median) { rot = false; q = 3; }
-                                else q = 0;
-                            }
-                        }
-                        const uint32_t c = child_of(node, q);
-                        if (!(c & kSet)) break;
-                        if (c & kLeaf) { h = __ldg(a.handles + (c & kIndex)); break; }
-                        node = __ldg(a.nodes + (c & kIndex));
-                    }
-                }
-            }
-        }
+        const int4 h = patch_map_find(a.map, a.faces[i], fu, fv);
         int *o = a.out + 5 * (size_t)i;
         o[0] = h.x;
         o[1] = h.y;
@@ -198,19 +143,25 @@ __global__ void __launch_bounds__(256) k_find_patches(const FindArgs a) {
     }
 }
 
+PatchMapView view_of(const PatchMapDevice &m) {
+    PatchMapView v;
+    v.nodes = (const uint4 *)m.nodes;
+    v.handles = (const int4 *)m.handles;
+    v.minFace = m.minFace;
+    v.maxFace = m.maxFace;
+    v.maxDepth = m.maxDepth;
+    v.triangular = m.triangular;
+    v.numPatches = m.numPatches;
+    return v;
+}
+
 int find_patches(const PatchMapDevice &m, int n, const int *faces, const float *u,
                  const float *v, void *coordsOut, cudaStream_t s) {
     if (n <= 0) return ok();
     if (!faces || !u || !v || !coordsOut)
         return fail(GB300_ERR_INVALID_ARGUMENT, "FindPatches: null pointer");
     FindArgs a;
-    a.nodes = (const uint4 *)m.nodes;
-    a.handles = (const int4 *)m.handles;
-    a.minFace = m.minFace;
-    a.maxFace = m.maxFace;
-    a.maxDepth = m.maxDepth;
-    a.triangular = m.triangular;
-    a.numPatches = m.numPatches;
+    a.map = view_of(m);
     a.n = n;
     a.faces = faces;
     a.u = u;

@@ -6,6 +6,9 @@
 #include <cstdint>
 #include <vector>
 
+#include "../../include/osd_gb300.h"
+#include "patchmap_walk.cuh"
+
 namespace gb300 {
 
 struct PatchMapHost {
@@ -24,6 +27,12 @@ struct PatchMapDevice {
 // 3 x 32-bit per patch param).
 int build_patch_map(int numArrays, const int *arrays, int numPatches, const int *params,
                     int triangular, PatchMapHost &out);
+
+// Kernel-argument view of a device map.
+PatchMapView view_of(const PatchMapDevice &m);
+
+// The device map of a patch table (GB300PatchTableCreate), for kernels that locate points.
+const PatchMapDevice *patch_map_of(const GB300PatchTable *table);
 
 int find_patches(const PatchMapDevice &m, int n, const int *faces, const float *u,
                  const float *v, void *coordsOut, cudaStream_t s);

@@ -205,3 +205,77 @@ def compose_rows(base, offsets, sources, weights, append_base=False):
                              C.c_int(len(off) - 1), _p(off), _p(src), C.c_int(len(ws)),
                              _ptrs(ws), C.c_int(int(append_base)))
     return _take_table(ptr)
+
+
+# ---- Bfr::Parameterization / Bfr::Tessellation restatement (bfr_oracle.c) -----------------
+
+def param_to_subface(reg_face_size, face_size, uv):
+    """Parameterization::ConvertCoordToNormalizedSubFace over [n, 2] float32 coords:
+    (sub-face [n], normalized coords [n, 2])."""
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    sub = np.zeros(len(uv), np.int32)
+    st = np.zeros_like(uv)
+    if not lib().orc_param_to_subface(C.c_int(reg_face_size), C.c_int(face_size),
+                                      C.c_int(len(uv)), _p(uv), _p(sub), _p(st)):
+        raise ValueError("invalid parameterization")
+    return sub, st
+
+
+def tess_inventory(reg_face_size, face_size, rates, facet_size=3, preserve_quads=False):
+    """(valid, coords, facets, boundary coords, uniform) of one Bfr::Tessellation."""
+    rates = np.ascontiguousarray(np.atleast_1d(rates), np.int32)
+    c = np.zeros(4, np.int32)
+    ok = lib().orc_tess_inventory(C.c_int(reg_face_size), C.c_int(face_size), C.c_int(len(rates)),
+                                  _p(rates), C.c_int(facet_size), C.c_int(int(preserve_quads)),
+                                  _p(c))
+    return bool(ok), int(c[0]), int(c[1]), int(c[2]), bool(c[3])
+
+
+def tess_generate(reg_face_size, face_size, rates, facet_size=3, preserve_quads=False):
+    """(coords [n, 2] float32, facets [m, facet_size] int32) of one face, or None if invalid."""
+    ok, nc, nf, _, _ = tess_inventory(reg_face_size, face_size, rates, facet_size,
+                                      preserve_quads)
+    if not ok:
+        return None
+    rates = np.ascontiguousarray(np.atleast_1d(rates), np.int32)
+    coords = np.zeros((nc, 2), np.float32)
+    fs = 4 if facet_size == 4 else 3
+    facets = np.zeros((nf, fs), np.int32)
+    r = lib().orc_tess_generate(C.c_int(reg_face_size), C.c_int(face_size), C.c_int(len(rates)),
+                                _p(rates), C.c_int(fs), C.c_int(int(preserve_quads)), _p(coords),
+                                C.c_int(2), _p(facets), C.c_int(fs))
+    if r != 1:
+        raise RuntimeError("tessellation restatement produced inconsistent counts")
+    return coords, facets
+
+
+def tess_mesh(reg_face_size, face_sizes, rate_offsets, rates, facet_size=3,
+              preserve_quads=False, threads=1):
+    """Every face of a mesh (Tessellation per face, facets offset to mesh-wide coords):
+    dict(coord_offsets, facet_offsets, coords [n, 2], facets [m, facet_size])."""
+    face_sizes = np.ascontiguousarray(face_sizes, np.int32)
+    rate_offsets = np.ascontiguousarray(rate_offsets, np.int32)
+    rates = np.ascontiguousarray(rates, np.int32)
+    nfaces = len(face_sizes)
+    counts = np.zeros((nfaces, 2), np.int64)
+    c = np.zeros(4, np.int32)
+    L = lib()
+    for f in range(nfaces):
+        r = rates[rate_offsets[f]:rate_offsets[f + 1]]
+        L.orc_tess_inventory(C.c_int(reg_face_size), C.c_int(int(face_sizes[f])),
+                             C.c_int(len(r)), _p(np.ascontiguousarray(r)), C.c_int(facet_size),
+                             C.c_int(int(preserve_quads)), _p(c))
+        counts[f] = c[:2]
+    co = np.zeros(nfaces + 1, np.int64)
+    fo = np.zeros(nfaces + 1, np.int64)
+    co[1:] = np.cumsum(counts[:, 0])
+    fo[1:] = np.cumsum(counts[:, 1])
+    fs = 4 if facet_size == 4 else 3
+    coords = np.zeros((int(co[-1]), 2), np.float32)
+    facets = np.zeros((int(fo[-1]), fs), np.int32)
+    ok = L.orc_tess_mesh(C.c_int(reg_face_size), C.c_int(nfaces), _p(face_sizes),
+                         _p(rate_offsets), _p(rates), C.c_int(fs), C.c_int(int(preserve_quads)),
+                         _p(co), _p(fo), _p(coords), _p(facets), C.c_int(threads))
+    if not ok:
+        raise RuntimeError("tessellation restatement produced inconsistent counts")
+    return dict(coord_offsets=co, facet_offsets=fo, coords=coords, facets=facets)

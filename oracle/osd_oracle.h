@@ -101,6 +101,31 @@ orc_table *orc_compose_rows(int baseNumStencils, const int *baseSizes, const int
                             const long long *offsets, const int *sources, int numChannels,
                             const float *const *weights, int appendBase);
 
+/* ---- Bfr (bfr_oracle.c) ---- */
+
+/* Bfr::Parameterization::ConvertCoordToNormalizedSubFace (bfr/parameterization.cpp:135-162)
+ * for n (u,v) pairs of a face of size N; sub-face 0 and the coords unchanged where the face
+ * has no sub-faces.  Returns 0 for an invalid parameterization. */
+int orc_param_to_subface(int regFaceSize, int N, int n, const float *uv, int *sub, float *st);
+
+/* Bfr::Tessellation inventory (bfr/tessellation.cpp:2023-2272): counts = {coords, facets,
+ * boundary coords, uniform}.  Returns 0 (and zero counts) for invalid arguments. */
+int orc_tess_inventory(int regFaceSize, int N, int numRates, const int *rates, int facetSize,
+                       int preserveQuads, int *counts);
+
+/* Tessellation::GetCoords<float> + GetFacets (bfr/tessellation.cpp:2300-2426) for one face.
+ * Strides 0 select the defaults (2 and the facet size).  Returns 1, 0 when invalid, -1 when
+ * the produced counts disagree with the inventory. */
+int orc_tess_generate(int regFaceSize, int N, int numRates, const int *rates, int facetSize,
+                      int preserveQuads, float *coords, int coordStride, int *facets,
+                      int facetStride);
+
+/* Every face of a mesh at the offsets of the inventory's exclusive scans, facet indices
+ * offset to the mesh-wide coord numbering. */
+int orc_tess_mesh(int regFaceSize, int numFaces, const int *faceSizes, const int *rateOffsets,
+                  const int *rates, int facetSize, int preserveQuads, const long *coordOffsets,
+                  const long *facetOffsets, float *coords, int *facets, int threads);
+
 #ifdef __cplusplus
 }
 #endif

@@ -102,6 +102,13 @@ class Refiner:
                                   C.c_int(int(inf_sharp)))
         return self
 
+    def refine_adaptive_levels(self, primary, secondary, inf_sharp=True):
+        """Adaptive refinement with a secondary level for smooth features, as the reference's
+        Bfr regression refines the tables it compares Bfr::Surface against."""
+        lib().ref_refine_adaptive_levels(self.h, C.c_int(primary), C.c_int(secondary),
+                                         C.c_int(int(inf_sharp)))
+        return self
+
     def num_vertices_total(self):
         return lib().ref_num_vertices_total(self.h)
 
@@ -230,11 +237,13 @@ class Patches:
     ENDCAP_BILINEAR, ENDCAP_BSPLINE, ENDCAP_GREGORY = 1, 2, 3
 
     def __init__(self, refiner, endcap=3, max_isolation=10, single_crease=False,
-                 inf_sharp=False, share_endcap_points=True):
+                 inf_sharp=False, share_endcap_points=True, legacy_sharp_corners=True):
         L = lib()
-        self.h = C.c_void_p(L.ref_patches_create(refiner.h, C.c_int(endcap), C.c_int(max_isolation),
-                                                 C.c_int(int(single_crease)), C.c_int(int(inf_sharp)),
-                                                 C.c_int(int(share_endcap_points))))
+        L.ref_patches_create_ex.restype = C.c_void_p
+        self.h = C.c_void_p(L.ref_patches_create_ex(
+            refiner.h, C.c_int(endcap), C.c_int(max_isolation), C.c_int(int(single_crease)),
+            C.c_int(int(inf_sharp)), C.c_int(int(share_endcap_points)),
+            C.c_int(int(legacy_sharp_corners))))
         counts = np.zeros(6, np.int64)
         L.ref_patches_counts(self.h, _p(counts))
         na, ni, npar, nloc, nst, nnz = (int(x) for x in counts)
@@ -341,3 +350,68 @@ def cpu_eval_patches(src, src_desc, dsts, dst_descs, coords, arrays, indices, pa
 
 def omp_set_threads(n):
     lib().ref_omp_set_threads(C.c_int(n))
+
+
+# ---- Bfr ----------------------------------------------------------------------------------
+
+def bfr_tess(reg_face_size, face_size, rates, facet_size=3, preserve_quads=False):
+    """The reference's Bfr::Tessellation of one face: (counts {coords, facets, boundary,
+    uniform}, coords [n, 2] float32, facets [m, facet_size]) or None when invalid."""
+    rates = np.ascontiguousarray(np.atleast_1d(rates), np.int32)
+    c = np.zeros(4, np.int32)
+    L = lib()
+    ok = L.ref_bfr_tess_counts(C.c_int(reg_face_size), C.c_int(face_size), C.c_int(len(rates)),
+                               _p(rates), C.c_int(facet_size), C.c_int(int(preserve_quads)),
+                               _p(c))
+    if not ok:
+        return None
+    fs = 4 if facet_size == 4 else 3
+    coords = np.zeros((int(c[0]), 2), np.float32)
+    facets = np.zeros((int(c[1]), fs), np.int32)
+    L.ref_bfr_tess(C.c_int(reg_face_size), C.c_int(face_size), C.c_int(len(rates)), _p(rates),
+                   C.c_int(fs), C.c_int(int(preserve_quads)), _p(coords), _p(facets))
+    return c.copy(), coords, facets
+
+
+def bfr_subface(reg_face_size, face_size, uv):
+    uv = np.ascontiguousarray(uv, np.float32).reshape(-1, 2)
+    sub = np.zeros(len(uv), np.int32)
+    st = np.zeros_like(uv)
+    if not lib().ref_bfr_subface(C.c_int(reg_face_size), C.c_int(face_size), C.c_int(len(uv)),
+                                 _p(uv), _p(sub), _p(st)):
+        return None
+    return sub, st
+
+
+def bfr_mesh_record(refiner, positions, rate_offsets, rates, facet_size=3, preserve_quads=False,
+                    approx_sharp=6, approx_smooth=2):
+    """Bfr tessellate-and-evaluate of every base face (the reference's tutorial loop):
+    dict(coord_offsets, facet_offsets, valid, regular, coords, facets, f32 [6, n, 3],
+    f64 [6, n, 3])."""
+    L = lib()
+    L.ref_bfr_mesh_record.restype = C.c_void_p
+    pos = np.ascontiguousarray(positions, np.float32)
+    ro = np.ascontiguousarray(rate_offsets, np.int32)
+    rt = np.ascontiguousarray(rates, np.int32)
+    h = C.c_void_p(L.ref_bfr_mesh_record(refiner.h, C.c_int(approx_sharp),
+                                         C.c_int(approx_smooth), _p(pos), _p(ro), _p(rt),
+                                         C.c_int(facet_size), C.c_int(int(preserve_quads))))
+    try:
+        sizes = np.zeros(3, np.int64)
+        L.ref_bfr_record_sizes(h, _p(sizes))
+        nf, nc, nfi = (int(x) for x in sizes)
+        fs = 4 if facet_size == 4 else 3
+        out = dict(coord_offsets=np.zeros(nf + 1, np.int64),
+                   facet_offsets=np.zeros(nf + 1, np.int64),
+                   valid=np.zeros(nf, np.int32), regular=np.zeros(nf, np.int32),
+                   coords=np.zeros((nc, 2), np.float32),
+                   facets=np.zeros((nfi // fs, fs), np.int32),
+                   f32=np.zeros((6, nc, 3), np.float32), f64=np.zeros((6, nc, 3), np.float64))
+        pf = (C.c_void_p * 6)(*[out["f32"][k].ctypes.data for k in range(6)])
+        pd = (C.c_void_p * 6)(*[out["f64"][k].ctypes.data for k in range(6)])
+        L.ref_bfr_record_copy(h, _p(out["coord_offsets"]), _p(out["facet_offsets"]),
+                              _p(out["valid"]), _p(out["regular"]), _p(out["coords"]),
+                              _p(out["facets"]), pf, pd)
+        return out
+    finally:
+        L.ref_bfr_record_destroy(h)

@@ -17,6 +17,10 @@
 #include <opensubdiv/osd/ompEvaluator.h>
 #include <opensubdiv/osd/cpuPatchTable.h>
 #include <opensubdiv/osd/bufferDescriptor.h>
+#include <opensubdiv/bfr/parameterization.h>
+#include <opensubdiv/bfr/tessellation.h>
+#include <opensubdiv/bfr/refinerSurfaceFactory.h>
+#include <opensubdiv/bfr/surface.h>
 
 #include <opensubdiv_gb300/far/gb300StencilTableFactory.h>
 
@@ -150,6 +154,18 @@ void ref_refine_adaptive(void *p, int isolation, int useSingleCrease, int useInf
         po.generateFVarLegacyLinearPatches = false;
     }
     ((Refiner *)p)->r->RefineAdaptive(po.GetRefineAdaptiveOptions());
+}
+
+// Adaptive refinement with a secondary (smooth feature) level, as the reference's Bfr
+// regression builds the Far tables it compares Bfr::Surface against
+// (regression/bfr_evaluate/farPatchEvaluator.cpp:52-78).
+void ref_refine_adaptive_levels(void *p, int primary, int secondary, int useInfSharp) {
+    Far::PatchTableFactory::Options po(primary);
+    po.useInfSharpPatch = useInfSharp;
+    Far::TopologyRefiner::AdaptiveOptions ro = po.GetRefineAdaptiveOptions();
+    ro.SetIsolationLevel(primary);
+    ro.SetSecondaryLevel(secondary);
+    ((Refiner *)p)->r->RefineAdaptive(ro);
 }
 
 int ref_num_vertices_total(void *p) { return ((Refiner *)p)->r->GetNumVerticesTotal(); }
@@ -515,14 +531,15 @@ void ref_omp_set_threads(int n) { Osd::OmpEvaluator::SetNumThreads(n); }
 // Far::PatchMap (far/patchMap.cpp) for lookups.  A stencil table covering refined and
 // local points is built the way examples/glEvalLimit does (StencilTableFactory with
 // intermediate levels + AppendLocalPointStencilTable).
-void *ref_patches_create(void *p, int endcap, int maxIsolation, int useSingleCrease,
-                         int useInfSharp, int shareEndCapPoints) {
+void *ref_patches_create_ex(void *p, int endcap, int maxIsolation, int useSingleCrease,
+                            int useInfSharp, int shareEndCapPoints, int legacySharpCorners) {
     Far::TopologyRefiner *r = ((Refiner *)p)->r;
     Far::PatchTableFactory::Options po(maxIsolation);
     po.SetEndCapType((Far::PatchTableFactory::Options::EndCapType)endcap);
     po.useSingleCreasePatch = useSingleCrease;
     po.useInfSharpPatch = useInfSharp;
     po.shareEndCapPatchPoints = shareEndCapPoints;
+    po.generateLegacySharpCornerPatches = legacySharpCorners;
     if (r->GetNumFVarChannels() > 0) {
         po.generateFVarTables = true;
         po.generateFVarLegacyLinearPatches = !r->IsUniform() ? false : true;
@@ -548,6 +565,12 @@ void *ref_patches_create(void *p, int endcap, int maxIsolation, int useSingleCre
     }
     h->all = st;
     return h;
+}
+
+void *ref_patches_create(void *p, int endcap, int maxIsolation, int useSingleCrease,
+                         int useInfSharp, int shareEndCapPoints) {
+    return ref_patches_create_ex(p, endcap, maxIsolation, useSingleCrease, useInfSharp,
+                                 shareEndCapPoints, 1);
 }
 
 void ref_patches_destroy(void *p) {
@@ -717,5 +740,174 @@ void ref_eval_patches_fp64(void *p, const float *src, int length, int srcStride,
         }
     }
 }
+
+// ---- Bfr ------------------------------------------------------------------------------
+
+static Sdc::SchemeType schemeOfRegularFaceSize(int regFaceSize) {
+    return regFaceSize == 3 ? Sdc::SCHEME_LOOP : Sdc::SCHEME_CATMARK;
+}
+
+static Bfr::Tessellation::Options tessOptions(int facetSize, int preserveQuads) {
+    Bfr::Tessellation::Options o;
+    o.SetFacetSize(facetSize);
+    o.PreserveQuads(preserveQuads != 0);
+    return o;
+}
+
+// Bfr::Tessellation (bfr/tessellation.h:142-200): counts = {coords, facets, boundary coords,
+// uniform}; returns IsValid().
+int ref_bfr_tess_counts(int regFaceSize, int N, int numRates, const int *rates, int facetSize,
+                        int preserveQuads, int *counts) {
+    Bfr::Parameterization param(schemeOfRegularFaceSize(regFaceSize), N);
+    Bfr::Tessellation t(param, numRates, rates, tessOptions(facetSize, preserveQuads));
+    counts[0] = t.IsValid() ? t.GetNumCoords() : 0;
+    counts[1] = t.IsValid() ? t.GetNumFacets() : 0;
+    counts[2] = t.IsValid() ? t.GetNumBoundaryCoords() : 0;
+    counts[3] = t.IsValid() ? (int)t.IsUniform() : 0;
+    return t.IsValid() ? 1 : 0;
+}
+
+// Tessellation::GetCoords<float> and GetFacets (bfr/tessellation.h:221-262)
+int ref_bfr_tess(int regFaceSize, int N, int numRates, const int *rates, int facetSize,
+                 int preserveQuads, float *coords, int *facets) {
+    Bfr::Parameterization param(schemeOfRegularFaceSize(regFaceSize), N);
+    Bfr::Tessellation t(param, numRates, rates, tessOptions(facetSize, preserveQuads));
+    if (!t.IsValid()) return 0;
+    t.GetCoords(coords);
+    t.GetFacets(facets);
+    return 1;
+}
+
+// Parameterization::ConvertCoordToNormalizedSubFace (bfr/parameterization.h:166-170)
+int ref_bfr_subface(int regFaceSize, int N, int n, const float *uv, int *sub, float *st) {
+    Bfr::Parameterization param(schemeOfRegularFaceSize(regFaceSize), N);
+    if (!param.IsValid()) return 0;
+    for (int i = 0; i < n; ++i) {
+        float in[2] = {uv[2 * i], uv[2 * i + 1]};
+        if (param.HasSubFaces()) {
+            sub[i] = param.ConvertCoordToNormalizedSubFace(in, st + 2 * i);
+        } else {
+            sub[i] = 0;
+            st[2 * i] = in[0], st[2 * i + 1] = in[1];
+        }
+    }
+    return 1;
+}
+
+}  // extern "C"
+
+namespace {
+struct BfrRecord {
+    std::vector<long> coordOffsets, facetOffsets;
+    std::vector<int> valid, regular, facets;
+    std::vector<float> coords;
+    std::vector<float> outF[6];
+    std::vector<double> outD[6];
+};
+
+template <class REAL>
+void bfrEvalFace(Bfr::Surface<REAL> const &s, std::vector<REAL> &patch, const float *pos,
+                 int nverts, std::vector<float> const &coords, size_t c0, size_t n,
+                 std::vector<REAL> *out) {
+    // mesh points in REAL: PreparePatchPoints reads the mesh array in the surface's precision
+    static thread_local std::vector<REAL> mesh;
+    if (mesh.size() != (size_t)nverts * 3) mesh.resize((size_t)nverts * 3);
+    for (size_t i = 0; i < (size_t)nverts * 3; ++i) mesh[i] = (REAL)pos[i];
+    patch.resize((size_t)s.GetNumPatchPoints() * 3);
+    s.PreparePatchPoints(mesh.data(), 3, patch.data(), 3);
+    for (size_t i = 0; i < n; ++i) {
+        REAL uv[2] = {(REAL)coords[2 * (c0 + i)], (REAL)coords[2 * (c0 + i) + 1]};
+        REAL r[6][3];
+        s.Evaluate(uv, patch.data(), 3, r[0], r[1], r[2], r[3], r[4], r[5]);
+        for (int k = 0; k < 6; ++k)
+            for (int e = 0; e < 3; ++e) out[k][3 * (c0 + i) + e] = r[k][e];
+    }
+}
+}  // namespace
+
+extern "C" {
+
+// The tessellate-and-evaluate loop of the reference's Bfr tutorials
+// (tutorials/bfr/tutorial_1_2/bfr_tutorial_1_2.cpp:170-238) over every base face of a
+// refiner: Bfr::RefinerSurfaceFactory with the given approximation levels, one
+// Bfr::Tessellation per face from rates[rateOffsets[f] .. rateOffsets[f+1]), and
+// Surface::Evaluate (P, Du, Dv, Duu, Duv, Dvv) at each coord in float and in double.
+// Faces without a limit surface get no coords.  Facet indices are offset to the mesh-wide
+// coord numbering (Tessellation::TransformFacetCoordIndices).
+void *ref_bfr_mesh_record(void *refiner, int approxSharp, int approxSmooth, const float *pos,
+                          const int *rateOffsets, const int *rates, int facetSize,
+                          int preserveQuads) {
+    Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
+    Bfr::SurfaceFactory::Options so;
+    so.SetApproxLevelSharp(approxSharp);
+    so.SetApproxLevelSmooth(approxSmooth);
+    Bfr::RefinerSurfaceFactory<> factory(mesh, so);
+    int nf = factory.GetNumFaces();
+    int nverts = mesh.GetLevel(0).GetNumVertices();
+    BfrRecord *rec = new BfrRecord;
+    rec->coordOffsets.assign(nf + 1, 0);
+    rec->facetOffsets.assign(nf + 1, 0);
+    rec->valid.assign(nf, 0);
+    rec->regular.assign(nf, 0);
+    int fs = facetSize == 4 ? 4 : 3;
+    Bfr::Tessellation::Options to = tessOptions(fs, preserveQuads);
+    Bfr::Surface<float> sf;
+    Bfr::Surface<double> sd;
+    std::vector<float> pf;
+    std::vector<double> pd;
+    for (int f = 0; f < nf; ++f) {
+        rec->coordOffsets[f + 1] = rec->coordOffsets[f];
+        rec->facetOffsets[f + 1] = rec->facetOffsets[f];
+        if (!factory.InitVertexSurface(f, &sf)) continue;
+        factory.InitVertexSurface(f, &sd);
+        Bfr::Tessellation t(sf.GetParameterization(), rateOffsets[f + 1] - rateOffsets[f],
+                            rates + rateOffsets[f], to);
+        if (!t.IsValid()) continue;
+        rec->valid[f] = 1;
+        rec->regular[f] = sf.IsRegular() ? 1 : (sf.IsLinear() ? 2 : 0);
+        size_t c0 = rec->coords.size() / 2, n = (size_t)t.GetNumCoords();
+        rec->coords.resize(2 * (c0 + n));
+        t.GetCoords(rec->coords.data() + 2 * c0);
+        size_t f0 = rec->facets.size() / fs;
+        rec->facets.resize(fs * (f0 + (size_t)t.GetNumFacets()));
+        t.GetFacets(rec->facets.data() + fs * f0);
+        t.TransformFacetCoordIndices(rec->facets.data() + fs * f0, (int)c0);
+        for (int k = 0; k < 6; ++k) {
+            rec->outF[k].resize(3 * (c0 + n));
+            rec->outD[k].resize(3 * (c0 + n));
+        }
+        bfrEvalFace(sf, pf, pos, nverts, rec->coords, c0, n, rec->outF);
+        bfrEvalFace(sd, pd, pos, nverts, rec->coords, c0, n, rec->outD);
+        rec->coordOffsets[f + 1] = (long)(c0 + n);
+        rec->facetOffsets[f + 1] = (long)(f0 + t.GetNumFacets());
+    }
+    return rec;
+}
+
+// sizes: {faces, coords, facets}
+void ref_bfr_record_sizes(void *p, long *sizes) {
+    BfrRecord *r = (BfrRecord *)p;
+    sizes[0] = (long)r->valid.size();
+    sizes[1] = (long)r->coords.size() / 2;
+    sizes[2] = (long)r->facets.size();
+}
+
+// out6f / out6d: 6 arrays of 3 values per coord (P, Du, Dv, Duu, Duv, Dvv)
+void ref_bfr_record_copy(void *p, long *coordOffsets, long *facetOffsets, int *valid,
+                         int *regular, float *coords, int *facets, float **out6f, double **out6d) {
+    BfrRecord *r = (BfrRecord *)p;
+    copyVec(r->coordOffsets, coordOffsets);
+    copyVec(r->facetOffsets, facetOffsets);
+    copyVec(r->valid, valid);
+    copyVec(r->regular, regular);
+    copyVec(r->coords, coords);
+    copyVec(r->facets, facets);
+    for (int k = 0; k < 6; ++k) {
+        if (out6f) copyVec(r->outF[k], out6f[k]);
+        if (out6d) copyVec(r->outD[k], out6d[k]);
+    }
+}
+
+void ref_bfr_record_destroy(void *p) { delete (BfrRecord *)p; }
 
 }  // extern "C"

@@ -376,6 +376,153 @@ def limit_pin_fixture(path):
     np.savez_compressed(path, **out)
 
 
+# ---- Bfr ----------------------------------------------------------------------------------
+
+def bfr_tess_cases(seed=0):
+    """(regular face size, face size, rates, facet size, preserve quads) for the pattern sweep:
+    uniform rates, edge rates with and without inner rates, quads' two-inner-rate forms, the
+    three facet options, N-gons to 13 sides, and invalid requests (a zero rate, a 2-gon, a
+    quad of a triangle scheme)."""
+    rng = np.random.default_rng(seed)
+    opts = ((3, 0), (4, 0), (4, 1))
+    cases = []
+    for reg, sizes in ((4, (4, 3, 5, 6, 7, 8, 9, 10, 11, 13)), (3, (3,))):
+        for N in sizes:
+            for fs, pq in opts:
+                for r in list(range(1, 11)) + [16, 31]:
+                    cases.append((reg, N, [r], fs, pq))
+                for _ in range(12):
+                    kind = rng.integers(0, 4)
+                    if kind == 0:
+                        rates = rng.integers(1, 10, N)
+                    elif kind == 1:
+                        rates = rng.integers(1, 10, N + 1)
+                    elif kind == 2 and N == 4:
+                        rates = rng.integers(1, 10, rng.choice([2, 6]))
+                    else:
+                        base = int(rng.integers(2, 9))
+                        rates = np.clip(base + rng.integers(-1, 2, N), 1, None)
+                    cases.append((reg, N, [int(x) for x in rates], fs, pq))
+    cases += [(4, 4, [0], 3, 0), (4, 2, [3], 3, 0), (3, 4, [3], 3, 0), (4, 5, [2, 0, 3, 1, 2], 4, 1)]
+    return cases
+
+
+def bfr_tess_fixture(path):
+    """The reference's Bfr::Tessellation over the sweep of bfr_tess_cases: per case its
+    validity, counts, coords (float32 bits) and facets."""
+    cases = bfr_tess_cases()
+    ro, rates, meta, co, coords, fo, facets = [0], [], [], [0], [], [0], []
+    for reg, N, r, fs, pq in cases:
+        rates += r
+        ro.append(len(rates))
+        t = ref.bfr_tess(reg, N, r, fs, pq)
+        if t is None:
+            meta.append((reg, N, fs, pq, 0, 0, 0, 0))
+            co.append(co[-1])
+            fo.append(fo[-1])
+            continue
+        cnt, c, f = t
+        meta.append((reg, N, fs, pq, 1, int(cnt[2]), int(cnt[3]), 0))
+        coords.append(c)
+        facets.append(f.reshape(-1))
+        co.append(co[-1] + len(c))
+        fo.append(fo[-1] + f.size)
+    np.savez_compressed(path, meta=np.asarray(meta, np.int32), rate_offsets=np.asarray(ro, np.int32),
+                        rates=np.asarray(rates, np.int32), coord_offsets=np.asarray(co, np.int64),
+                        coords=np.concatenate(coords).astype(np.float32),
+                        facet_offsets=np.asarray(fo, np.int64),
+                        facets=np.concatenate(facets).astype(np.int32))
+
+
+def edge_rates(cage, rng, lo=1, hi=7):
+    """Per-face edge rates from one seeded rate per mesh edge (shared edges get one rate, as
+    rates derived from edge lengths do in the reference's tutorial 2.1)."""
+    vpf = cage.verts_per_face
+    fv = cage.face_verts
+    start = np.concatenate([[0], np.cumsum(vpf)])
+    rate_of = {}
+    out = []
+    for f in range(len(vpf)):
+        vs = fv[start[f]:start[f + 1]]
+        for i in range(len(vs)):
+            e = (min(vs[i], vs[(i + 1) % len(vs)]), max(vs[i], vs[(i + 1) % len(vs)]))
+            if e not in rate_of:
+                rate_of[e] = int(rng.integers(lo, hi + 1))
+            out.append(rate_of[e])
+    return start.astype(np.int32), np.asarray(out, np.int32)
+
+
+def bfr_mesh_fixture(path, cage, mode, facet_size=3, preserve_quads=False, seed=0):
+    """Bfr tessellate-and-evaluate of every face (the reference's tutorial loop through
+    Bfr::RefinerSurfaceFactory with its default approximation levels, Surface::Evaluate in
+    float and double), plus the Far patch table the reference's Bfr regression pairs with those
+    levels (isolation 6 / secondary 2, Gregory-basis end caps, infinitely sharp patches, no
+    shared end-cap points, no legacy corner patches) and its PatchMap handles at every coord."""
+    rng = np.random.default_rng(seed)
+    reg = 3 if cage.scheme == shapes.LOOP else 4
+    nf = len(cage.verts_per_face)
+    if mode[0] == "u":
+        ro = np.arange(nf + 1, dtype=np.int32)
+        rates = np.full(nf, int(mode[1:]), np.int32)
+    else:
+        ro, rates = edge_rates(cage, rng)
+    rec = ref.bfr_mesh_record(ref.Refiner(cage), cage.positions, ro, rates, facet_size,
+                              preserve_quads)
+    r = ref.Refiner(cage).refine_adaptive_levels(6, 2, True)
+    p = ref.Patches(r, endcap=3, max_isolation=6, inf_sharp=True, share_endcap_points=False,
+                    legacy_sharp_corners=False)
+    nc = cage.num_vertices
+    ns = len(p.st["sizes"])
+    buf = np.zeros((nc + ns) * 3, np.float32)
+    buf[: nc * 3] = cage.positions.reshape(-1)
+    assert ref.cpu_eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], p.st["sizes"],
+                                 p.st["offsets"], p.st["indices"], [p.st["weights"]], 0, ns)
+    sizes = cage.verts_per_face
+    ptex = np.concatenate([[0], np.cumsum(np.where(sizes == reg, 1, sizes))]).astype(np.int64)
+    co = rec["coord_offsets"]
+    qf, qs, qt = [], [], []
+    for f in range(nf):
+        if co[f + 1] == co[f]:
+            continue
+        sub, st = ref.bfr_subface(reg, int(sizes[f]), rec["coords"][co[f]:co[f + 1]])
+        qf.append(ptex[f] + sub)
+        qs.append(st[:, 0])
+        qt.append(st[:, 1])
+    qf = np.concatenate(qf).astype(np.int32)
+    qs = np.concatenate(qs).astype(np.float32)
+    qt = np.concatenate(qt).astype(np.float32)
+    handles, found = p.find_patches(qf, qs.astype(np.float64), qt.astype(np.float64))
+    out = dict(cage_arrays(cage))
+    out.update(regular_face_size=np.int32(reg), rate_offsets=ro, rates=rates,
+               facet_size=np.int32(facet_size), preserve_quads=np.int32(preserve_quads),
+               arrays=p.arrays, patch_indices=p.indices, params=p.params, src=buf,
+               triangular=np.int32(reg == 3), ptex_offsets=ptex,
+               coord_offsets=co, facet_offsets=rec["facet_offsets"], valid=rec["valid"],
+               regular=rec["regular"], coords=rec["coords"], facets=rec["facets"],
+               out6=rec["f32"], out6_fp64=rec["f64"], q_face=qf, q_s=qs, q_t=qt,
+               q_handles=handles, q_found=found)
+    np.savez_compressed(path, **out)
+
+
+BFR_MESHES = [
+    ("catmark_nonquads", "u5", 3, 0), ("catmark_nonquads", "e", 4, 1),
+    ("catmark_xord_boundary", "u4", 4, 1), ("catmark_edgecorner", "e", 3, 0),
+    ("catmark_smoothtris0", "u3", 3, 0), ("catmark_gregory_test1", "e", 4, 0),
+    ("loop_xord_boundary", "u5", 3, 0), ("loop_xord_boundary", "e", 4, 0),
+]
+
+
+def bfr_fixtures():
+    bfr_tess_fixture(os.path.join(HERE, "bfr_tess_patterns.npz"))
+    for k, (name, mode, fs, pq) in enumerate(BFR_MESHES):
+        bfr_mesh_fixture(os.path.join(HERE, f"bfr_{name}_{mode}_f{fs}{'q' if pq else ''}.npz"),
+                         regression_shape(name), mode, fs, pq, seed=300 + k)
+    tor = shapes.torus(16, 8, tri_fraction=0.1, crease_fraction=0.05, seed=3)
+    bfr_mesh_fixture(os.path.join(HERE, "bfr_torus16x8_e_f3.npz"), tor, "e", 3, 0, seed=320)
+    ico = shapes.icosphere(1, noise=0.005, seed=3)
+    bfr_mesh_fixture(os.path.join(HERE, "bfr_icosphere1_u6_f3.npz"), ico, "u6", 3, 0, seed=321)
+
+
 LARGE = os.path.join(HERE, "large")
 
 
@@ -427,6 +574,9 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "regression":
         regression_fixtures()
         limit_pin_fixture(os.path.join(HERE, "uniform_limit_pin.npz"))
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "bfr":
+        bfr_fixtures()
         return
     if len(sys.argv) > 1 and sys.argv[1] == "factory":
         factory_fixture(os.path.join(HERE, "factory_masks.npz"))

@@ -1,0 +1,124 @@
+"""Pin the Bfr restatement (oracle/bfr_oracle.c) to the reference's Bfr.
+
+tests/golden/bfr_tess_patterns.npz holds the reference's Bfr::Tessellation over a sweep of
+faces, rates and options; tests/golden/bfr_<mesh>_*.npz the reference's Bfr tessellate-and-
+evaluate loop over whole meshes (Bfr::RefinerSurfaceFactory + Tessellation + Surface::Evaluate)
+with the Far patch table its Bfr regression pairs with the same approximation, and Far::PatchMap
+handles at every coord (tests/golden/make_golden.py bfr).
+
+The oracle must reproduce every coord bit for bit, every facet, the sub-face conversion bit for
+bit and the PatchMap handles exactly; evaluating the Far table at the located coords must agree
+with Bfr::Surface::Evaluate within the tolerances of the reference's own Bfr-versus-Far
+regression (regression/bfr_evaluate/main.cpp:610-830).
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MESHES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "bfr_*.npz"))
+                if not p.endswith("bfr_tess_patterns.npz"))
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.int32)
+
+
+def cases(z):
+    meta, ro, rates = z["meta"], z["rate_offsets"], z["rates"]
+    for i in range(len(meta)):
+        reg, N, fs, pq, valid, nb, uni, _ = (int(x) for x in meta[i])
+        yield i, reg, N, rates[ro[i]:ro[i + 1]], fs, pq, bool(valid), nb, bool(uni)
+
+
+def test_tessellation_patterns_match_the_reference_bitwise():
+    z = np.load(os.path.join(GOLDEN, "bfr_tess_patterns.npz"))
+    co, fo = z["coord_offsets"], z["facet_offsets"]
+    n = 0
+    for i, reg, N, rates, fs, pq, valid, nb, uni in cases(z):
+        ok, nc, nf, nbo, unio = oracle.tess_inventory(reg, N, rates, fs, pq)
+        assert ok == valid, i
+        if not valid:
+            assert nc == nf == 0
+            continue
+        c, f = oracle.tess_generate(reg, N, rates, fs, pq)
+        assert np.array_equal(bits(c.ravel()), bits(z["coords"][co[i]:co[i + 1]].ravel())), i
+        assert np.array_equal(f.ravel(), z["facets"][fo[i]:fo[i + 1]]), i
+        assert (nbo, unio) == (nb, uni), i
+        n += 1
+    assert n > 700
+
+
+@pytest.mark.parametrize("path", MESHES, ids=os.path.basename)
+def test_mesh_tessellation_and_location_match_bfr(path):
+    z = np.load(path)
+    reg = int(z["regular_face_size"])
+    sizes = z["verts_per_face"]
+    t = oracle.tess_mesh(reg, sizes, z["rate_offsets"], z["rates"], int(z["facet_size"]),
+                         bool(z["preserve_quads"]), threads=4)
+    assert np.array_equal(t["coord_offsets"], z["coord_offsets"])
+    assert np.array_equal(t["facet_offsets"] * t["facets"].shape[1], z["facet_offsets"] *
+                          z["facets"].shape[1])
+    assert np.array_equal(bits(t["coords"]), bits(z["coords"]))
+    assert np.array_equal(t["facets"], z["facets"])
+    # sub-face conversion and ptex numbering of every coord
+    co = z["coord_offsets"]
+    faces, st = [], []
+    for f in range(len(sizes)):
+        if co[f + 1] == co[f]:
+            continue
+        sub, s = oracle.param_to_subface(reg, int(sizes[f]), z["coords"][co[f]:co[f + 1]])
+        faces.append(z["ptex_offsets"][f] + sub)
+        st.append(s)
+    faces = np.concatenate(faces).astype(np.int32)
+    st = np.concatenate(st)
+    assert np.array_equal(faces, z["q_face"])
+    assert np.array_equal(bits(st[:, 0]), bits(z["q_s"]))
+    assert np.array_equal(bits(st[:, 1]), bits(z["q_t"]))
+    pm = oracle.PatchMap(z["arrays"], z["params"], bool(z["triangular"]))
+    h = pm.find(faces, st[:, 0].astype(np.float64), st[:, 1].astype(np.float64))
+    assert np.array_equal(h, z["q_handles"])
+    assert z["q_found"].all()
+
+
+def bfr_tolerances(positions):
+    """The reference's Bfr-versus-Far regression tolerances (regression/bfr_evaluate/
+    main.cpp:536-563, 676-690): positions within 5e-5 of the largest bounding-box extent,
+    first derivatives within 5 times that, second derivatives within 25 times."""
+    p = np.asarray(positions, np.float64).reshape(-1, 3)
+    ptol = 5e-5 * float((p.max(0) - p.min(0)).max())
+    return (ptol, 5 * ptol, 5 * ptol, 25 * ptol, 25 * ptol, 25 * ptol)
+
+
+@pytest.mark.parametrize("path", MESHES, ids=os.path.basename)
+def test_far_table_evaluation_agrees_with_bfr_surfaces(path):
+    """The Far table at the located coords (the oracle's EvalPatches, float) against
+    Bfr::Surface::Evaluate (float) within the reference's own Bfr-versus-Far tolerances."""
+    z = np.load(path)
+    coords = oracle.make_coords(z["q_handles"], z["q_s"], z["q_t"])
+    n = len(coords)
+    outs = [np.zeros(n * 3, np.float32) for _ in range(6)]
+    assert oracle.eval_patches(z["src"], (0, 3, 3), outs, [(0, 3, 3)] * 6, coords, z["arrays"],
+                               z["patch_indices"], z["params"], threads=4)
+    tol = bfr_tolerances(z["positions"])
+    for k in range(6):
+        far = outs[k].reshape(-1, 3).astype(np.float64)
+        assert np.abs(far - z["out6"][k]).max() <= tol[k], k
+
+
+def test_param_conversion_against_the_reference_library():
+    """Direct comparison with the reference's Bfr::Parameterization where it is built here."""
+    import ref
+    if not ref.available():
+        pytest.skip("reference library not built")
+    rng = np.random.default_rng(5)
+    for N in (3, 5, 6, 7, 9, 10, 12, 17, 40):
+        uv = np.concatenate([oracle.tess_generate(4, N, [7])[0],
+                             (rng.random((300, 2)) * 4).astype(np.float32)])
+        a = ref.bfr_subface(4, N, uv)
+        b = oracle.param_to_subface(4, N, uv)
+        assert np.array_equal(a[0], b[0]) and np.array_equal(bits(a[1]), bits(b[1])), N

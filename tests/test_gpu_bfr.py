@@ -1,0 +1,174 @@
+"""Bfr tessellation and evaluation of whole meshes on the device (GB300TessellationCount /
+GB300TessellationGenerate + GB300PatchTableEval) against the reference's Bfr.
+
+* Patterns: the device tessellation of every case of the reference's Bfr::Tessellation sweep
+  (tests/golden/bfr_tess_patterns.npz) -- counts, coords bit for bit, facets exactly -- through
+  per-face rate runs, and the shared uniform-rate patterns for faces of 3..13 sides against the
+  oracle (pinned to the same sweep by tests/test_bfr_oracle.py).
+* Meshes: the reference's tessellate-and-evaluate loop (tests/golden/bfr_<mesh>_*.npz): coords,
+  facets with mesh-wide indices, located PatchCoords (handles exact, (s,t) bit for bit) and the
+  six evaluated outputs.  P, Du, Dv and the second derivatives are held to the reference's own
+  Bfr-versus-Far tolerances against Bfr::Surface::Evaluate, and to the accuracy gate
+  (tests/gpu_util.py) against the oracle's evaluation of the same Far table.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+from gpu_util import bbox_diag, dev, gate, host, torch_cuda
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MESHES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "bfr_*.npz"))
+                if not p.endswith("bfr_tess_patterns.npz"))
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.int32)
+
+
+def bfr_tolerances(positions):
+    """regression/bfr_evaluate/main.cpp:536-563, 676-690: 5e-5 of the largest bounding-box
+    extent for positions, 5x for first and 25x for second derivatives."""
+    p = np.asarray(positions, np.float64).reshape(-1, 3)
+    ptol = 5e-5 * float((p.max(0) - p.min(0)).max())
+    return (ptol, 5 * ptol, 5 * ptol, 25 * ptol, 25 * ptol, 25 * ptol)
+
+
+@pytest.mark.gpu
+def test_pattern_sweep_matches_the_reference():
+    torch_cuda()
+    from opensubdiv_gb300 import bfr
+    z = np.load(os.path.join(GOLDEN, "bfr_tess_patterns.npz"))
+    meta, ro, rates = z["meta"], z["rate_offsets"], z["rates"]
+    groups = {}
+    for i in range(len(meta)):
+        reg, N, fs, pq = (int(x) for x in meta[i][:4])
+        groups.setdefault((reg, fs, pq), []).append(i)
+    checked = 0
+    for (reg, fs, pq), idx in groups.items():
+        sizes = np.array([meta[i][1] for i in idx], np.int32)
+        runs = [rates[ro[i]:ro[i + 1]] for i in idx]
+        r_off = np.concatenate([[0], np.cumsum([len(r) for r in runs])]).astype(np.int32)
+        m = bfr.MeshTessellation(reg, sizes, rates=np.concatenate(runs), rate_offsets=r_off,
+                                 options=bfr.TessellationOptions(fs, pq))
+        c, f, _ = m.Generate(offset_facet_indices=False)
+        c, f = host(c), host(f)
+        co, fo = host(m.coord_offsets), host(m.facet_offsets)
+        for j, i in enumerate(idx):
+            want_c = z["coords"][z["coord_offsets"][i]:z["coord_offsets"][i + 1]]
+            want_f = z["facets"][z["facet_offsets"][i]:z["facet_offsets"][i + 1]]
+            assert co[j + 1] - co[j] == len(want_c), i
+            assert (fo[j + 1] - fo[j]) * f.shape[1] == len(want_f), i
+            assert np.array_equal(bits(c[co[j]:co[j + 1]]), bits(want_c)), i
+            assert np.array_equal(f[fo[j]:fo[j + 1]].ravel(), want_f), i
+            checked += 1
+    assert checked == len(meta)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("reg,fs,pq", [(4, 3, 0), (4, 4, 0), (4, 4, 1), (3, 3, 0), (3, 4, 1)])
+def test_uniform_rate_patterns_and_mesh_offsets(reg, fs, pq):
+    """A single uniform rate (faces of 3..10 sides share one device pattern each, larger
+    polygons are generated per face), mesh-wide facet indices and ptex offsets."""
+    torch_cuda()
+    from opensubdiv_gb300 import bfr
+    rng = np.random.default_rng(reg * 10 + fs + pq)
+    pool = [3, 4, 5, 6, 7, 8, 9, 10, 11, 13] if reg == 4 else [3, 3, 3, 4]
+    sizes = rng.choice(pool, 400).astype(np.int32)
+    for rate in (1, 2, 3, 4, 5, 8, 13):
+        m = bfr.MeshTessellation(reg, sizes, uniform_rate=rate,
+                                 options=bfr.TessellationOptions(fs, pq))
+        c, f, _ = m.Generate()
+        c, f = host(c), host(f)
+        co, fo, po = host(m.coord_offsets), host(m.facet_offsets), host(m.ptex_offsets)
+        assert np.array_equal(np.diff(po), np.where(sizes == reg, 1, sizes))
+        for j, N in enumerate(sizes):
+            want = oracle.tess_generate(reg, int(N), [rate], fs, pq)
+            if want is None:
+                assert co[j + 1] == co[j] and fo[j + 1] == fo[j]
+                continue
+            wc, wf = want
+            assert np.array_equal(bits(c[co[j]:co[j + 1]]), bits(wc)), (rate, j, N)
+            got = f[fo[j]:fo[j + 1]]
+            assert np.array_equal(np.where(got >= 0, got - co[j], -1), wf), (rate, j, N)
+
+
+@pytest.mark.gpu
+def test_strides_and_face_local_indices():
+    """Coord and facet strides of Tessellation::Options: only the (u,v) pair and facet size
+    entries of each record are written."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import bfr
+    sizes = np.array([4, 5, 3, 4], np.int32)
+    rates = np.array([3, 1, 2, 4, 5, 2, 2, 3, 2, 6, 3, 3, 1, 2, 4], np.int32)
+    r_off = np.array([0, 4, 9, 12, 15], np.int32)
+    opt = bfr.TessellationOptions(4, 1, coord_stride=3, facet_stride=6)
+    m = bfr.MeshTessellation(4, sizes, rates=rates, rate_offsets=r_off, options=opt)
+    c = torch.full((m.num_coords, 3), 7.0, device="cuda")
+    f = torch.full((m.num_facets, 6), -9, dtype=torch.int32, device="cuda")
+    m.Generate(coords=c, facets=f, offset_facet_indices=False)
+    c, f = host(c), host(f)
+    assert (c[:, 2] == 7.0).all() and (f[:, 4:] == -9).all()
+    co, fo = host(m.coord_offsets), host(m.facet_offsets)
+    for j in range(len(sizes)):
+        wc, wf = oracle.tess_generate(4, int(sizes[j]), rates[r_off[j]:r_off[j + 1]], 4, True)
+        assert np.array_equal(bits(c[co[j]:co[j + 1], :2]), bits(wc))
+        assert np.array_equal(f[fo[j]:fo[j + 1], :4], wf)
+
+
+@pytest.mark.gpu
+def test_invalid_requests_are_rejected():
+    torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300._lib import GB300Error
+    with pytest.raises(GB300Error):
+        bfr.MeshTessellation(5, np.array([4], np.int32), uniform_rate=3)
+    with pytest.raises(GB300Error):
+        bfr.MeshTessellation(4, np.array([4], np.int32), uniform_rate=3,
+                             options=bfr.TessellationOptions(3, 0, coord_stride=1))
+    # invalid faces (rate 0, a 2-gon) tessellate to nothing, like an invalid Bfr::Tessellation
+    m = bfr.MeshTessellation(4, np.array([4, 2, 5], np.int32), rates=np.array([0, 3, 2], np.int32))
+    want = oracle.tess_inventory(4, 5, [2])[1]
+    assert list(np.diff(host(m.coord_offsets))) == [0, 0, want]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", MESHES, ids=os.path.basename)
+def test_mesh_tessellate_and_evaluate_matches_bfr(path):
+    torch = torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300PatchTable
+    z = np.load(path)
+    name = os.path.basename(path)[:-4]
+    reg = int(z["regular_face_size"])
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"],
+                                   bool(z["triangular"]))
+    opt = bfr.TessellationOptions(int(z["facet_size"]), bool(z["preserve_quads"]))
+    m = bfr.MeshTessellation(reg, z["verts_per_face"], rates=z["rates"],
+                             rate_offsets=z["rate_offsets"], options=opt)
+    assert np.array_equal(host(m.coord_offsets), z["coord_offsets"])
+    assert np.array_equal(host(m.ptex_offsets), z["ptex_offsets"])
+    c, f, pc = m.Generate(table=table)
+    assert np.array_equal(bits(host(c)), bits(z["coords"]))
+    assert np.array_equal(host(f), z["facets"])
+    pc = host(pc)
+    assert np.array_equal(pc[:, :3], z["q_handles"])
+    assert np.array_equal(pc[:, 3], bits(z["q_s"]))
+    assert np.array_equal(pc[:, 4], bits(z["q_t"]))
+    outs = [host(o) for o in m.Evaluate(dev(z["src"]), BD(0, 3, 3), table, dev(pc), 2)]
+    tol = bfr_tolerances(z["positions"])
+    n = m.num_coords
+    cpu = [np.zeros(n * 3, np.float32) for _ in range(6)]
+    f64 = [np.zeros(n * 3) for _ in range(6)]
+    tab = (pc, z["arrays"], z["patch_indices"], z["params"])
+    assert oracle.eval_patches(z["src"], (0, 3, 3), cpu, [(0, 3, 3)] * 6, *tab, threads=4)
+    assert oracle.eval_patches(z["src"], (0, 3, 3), f64, [(0, 3, 3)] * 6, *tab, threads=4,
+                               fp64=True)
+    diag = bbox_diag(z["positions"])
+    for k in range(6):
+        err = np.abs(outs[k].astype(np.float64) - z["out6"][k]).max()
+        assert err <= tol[k], (name, k, err, tol[k])
+        gate(f"bfr {name}", k, outs[k].ravel(), cpu[k], f64[k], diag)
