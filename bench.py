@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-config1", action="store_true",
                     help="skip the CPU-runnable cube section (warm and cold L2)")
     ap.add_argument("--patch-points", type=int, default=4_000_000)
+    ap.add_argument("--no-bfr", action="store_true",
+                    help="skip the Bfr tessellate-and-evaluate section")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching section")
     ap.add_argument("--batch-meshes", type=int, default=256)
     ap.add_argument("--batch-cv-max", type=int, default=200_000,
@@ -241,6 +243,196 @@ def bench_patches(args, stream, peak, loop=False):
                          "point_types": {str(t): int((types == t).sum())
                                          for t in np.unique(types)}},
             "max_abs_err_P_vs_oracle_slice": err_p}
+
+
+BFR_TABLE = "torus512x256_bfr.npz"
+BFR_INTERVAL = 0.0022  # edge-length interval of the non-uniform rates (mean rate ~5.1)
+
+
+def bench_bfr(args, stream, peak):
+    """Bfr tessellate-and-evaluate of every face of the 512 x 256 torus in one pass (the loop
+    the reference's Bfr tutorials run face by face, tutorials/bfr/tutorial_1_2 and 2_1):
+    GB300TessellationCount + GB300TessellationGenerate (coords, triangle facets with mesh-wide
+    indices, PatchCoords located on the Far table of Bfr::SurfaceFactory's default
+    approximation) + GB300PatchTableEval of P, Du and Dv.  Two rate schemes: the tutorials'
+    uniform rate 5, and per-edge rates from control-hull edge lengths (tutorial 2.1)."""
+    import torch
+
+    from opensubdiv_gb300 import bfr, workloads
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300PatchTable)
+
+    path = os.path.join(GOLDEN, "large", BFR_TABLE)
+    if not os.path.exists(path):
+        return {"skipped": f"{BFR_TABLE} is written where the reference is available "
+                           "(tests/golden/make_golden.py large)"}
+    z = np.load(path)
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"], False)
+    src = torch.from_numpy(z["src"]).cuda()
+    sizes_host = np.ascontiguousarray(z["verts_per_face"], np.int32)
+    nfaces = len(sizes_host)
+    d = BD(0, 3, 3)
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle
+
+    out = {"workload": "torus512x256 (5% triangles, 2% creases), Bfr::SurfaceFactory default "
+                       "approximation (sharp 6 / smooth 2) as a Far table",
+           "faces": nfaces, "patches": int(len(z["params"])), "facet_size": 3,
+           "outputs": "P, Du, Dv"}
+    for mode in ("uniform5", "edge_lengths"):
+        if mode == "uniform5":
+            kw = dict(uniform_rate=5)
+            rate_desc = "uniform rate 5"
+        else:
+            ro, rates = workloads.bfr_edge_length_rates(z["positions"], z["verts_per_face"],
+                                                        z["face_verts"], BFR_INTERVAL)
+            kw = dict(rates=rates, rate_offsets=ro)
+            rate_desc = (f"edge rates ceil(length / {BFR_INTERVAL}) (mean {rates.mean():.2f}, "
+                         f"{rates.min()}..{rates.max()})")
+        m = bfr.MeshTessellation(4, sizes_host, options=bfr.TessellationOptions(3), stream=stream,
+                                 **kw)
+        n, nf = m.num_coords, m.num_facets
+        coords = torch.empty((n, 2), device="cuda")
+        facets = torch.empty((nf, 3), dtype=torch.int32, device="cuda")
+        pc = torch.empty((n, 5), dtype=torch.int32, device="cuda")
+        outs = [torch.empty(n * 3, device="cuda") for _ in range(3)]
+
+        def gen():
+            m.Generate(coords, facets, True, table, pc)
+
+        def ev():
+            assert Ev.EvalPatchesTable(src, d, outs[0], d, n, pc, table, du=outs[1], duDesc=d,
+                                       dv=outs[2], dvDesc=d, stream=stream)
+
+        for _ in range(args.warmup):
+            gen()
+            ev()
+        torch.cuda.synchronize()
+        evs = [tuple(torch.cuda.Event(enable_timing=True) for _ in range(3))
+               for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for k in range(args.steps):
+                evs[k][0].record(stream)
+                gen()
+                evs[k][1].record(stream)
+                ev()
+                evs[k][2].record(stream)
+        torch.cuda.synchronize()
+        gen_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
+        eval_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+        # Count waits for its totals: timed on the host
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            m.Count()
+        count_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+
+        # end to end from host buffers: face sizes and rates in, P / Du / Dv, coords and facets
+        # out (the control points' patch points stay resident, as the tutorial's mesh does)
+        h_sizes = torch.from_numpy(sizes_host).pin_memory()
+        h_rates = (torch.from_numpy(np.concatenate([kw["rate_offsets"], kw["rates"]]))
+                   .pin_memory() if "rates" in kw else None)
+        h_out = [torch.empty(n * 3, pin_memory=True) for _ in range(3)]
+        h_coords = torch.empty((n, 2), pin_memory=True)
+        h_facets = torch.empty((nf, 3), dtype=torch.int32, pin_memory=True)
+
+        def e2e():
+            with torch.cuda.stream(stream):
+                dsz = h_sizes.to("cuda", non_blocking=True)
+                mk = dict(uniform_rate=5)
+                if h_rates is not None:
+                    dr = h_rates.to("cuda", non_blocking=True)
+                    mk = dict(rate_offsets=dr[:nfaces + 1], rates=dr[nfaces + 1:])
+                mm = bfr.MeshTessellation(4, dsz, options=bfr.TessellationOptions(3),
+                                          stream=stream, **mk)
+                mm.Generate(coords, facets, True, table, pc)
+                assert Ev.EvalPatchesTable(src, d, outs[0], d, n, pc, table, du=outs[1],
+                                           duDesc=d, dv=outs[2], dvDesc=d, stream=stream)
+                for a, b in zip(h_out, outs):
+                    a.copy_(b, non_blocking=True)
+                h_coords.copy_(coords, non_blocking=True)
+                h_facets.copy_(facets, non_blocking=True)
+            stream.synchronize()
+
+        for _ in range(2):
+            e2e()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        h2d = 4 * nfaces + (4 * (nfaces + 1 + len(kw["rates"])) if "rates" in kw else 0)
+        d2h = 36 * n + 8 * n + 12 * nf
+
+        # correctness (outside timing): every coord and facet of the mesh bit for bit against
+        # the oracle, and P / Du / Dv on a slice against the oracle's evaluation
+        tm = oracle.tess_mesh(4, sizes_host, kw.get("rate_offsets", np.arange(nfaces + 1)),
+                              kw.get("rates", np.full(nfaces, 5, np.int32)), 3, False, threads=16)
+        exact = bool(np.array_equal(h_coords.numpy().view(np.int32),
+                                    tm["coords"].view(np.int32)) and
+                     np.array_equal(h_facets.numpy(), tm["facets"]))
+        k = min(n, 200_000)
+        pch = pc[:k].cpu().numpy()
+        ref = [np.zeros(k * 3, np.float32) for _ in range(3)]
+        oracle.eval_patches(z["src"], (0, 3, 3), ref, [(0, 3, 3)] * 3, pch, z["arrays"],
+                            z["patch_indices"], z["params"], threads=16)
+        err = max(float(np.abs(h_out[j].numpy()[: k * 3] - ref[j]).max()) for j in range(3))
+
+        # CPU baseline: the oracle's tessellate + locate + evaluate over a bounded face sample
+        sample = max(1, nfaces // 8)
+        so = np.concatenate([[0], np.cumsum(np.ones(sample, np.int64))]) if "rates" not in kw \
+            else None
+        cpu_threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        if "rates" in kw:
+            r_off = kw["rate_offsets"][: sample + 1]
+            r_sel = kw["rates"][: r_off[-1]]
+        else:
+            r_off = so.astype(np.int32)
+            r_sel = np.full(sample, 5, np.int32)
+        ct = oracle.tess_mesh(4, sizes_host[:sample], r_off, r_sel, 3, False, threads=cpu_threads)
+        ptex = np.concatenate([[0], np.cumsum(np.where(sizes_host[:sample] == 4, 1,
+                                                       sizes_host[:sample]))])
+        qf, st = oracle.tess_locate_mesh(4, sizes_host[:sample], ct["coord_offsets"], ptex,
+                                         ct["coords"], threads=cpu_threads)
+        pm = oracle.PatchMap(z["arrays"], z["params"], False)
+        hh = pm.find(qf, st[:, 0].astype(np.float64), st[:, 1].astype(np.float64))
+        cc = oracle.make_coords(hh, st[:, 0], st[:, 1])
+        co3 = [np.zeros(len(cc) * 3, np.float32) for _ in range(3)]
+        oracle.eval_patches(z["src"], (0, 3, 3), co3, [(0, 3, 3)] * 3, cc, z["arrays"],
+                            z["patch_indices"], z["params"], threads=cpu_threads)
+        cpu_s = time.perf_counter() - t0
+
+        facet_b = workloads.bfr_tess_bytes(nfaces, n, nf, 3, True, "rates" not in kw)
+        cvs = float(np.average(z["arrays"][:, 4], weights=z["arrays"][:, 2]))
+        touched = int(len(np.unique(pc[:, 1].cpu().numpy())))
+        eval_b = workloads.patch_bytes(n, 3, 3, len(z["src"]) // 3, touched, cvs)
+        out[mode] = {
+            "rates": rate_desc, "coords": n, "facets": nf,
+            "points_per_s": n / ((gen_ms + eval_ms) / 1e3),
+            "tessellate_ms": gen_ms, "eval_ms": eval_ms, "count_ms_host": count_ms,
+            "e2e": {"points_per_s": n / (e2e_ms / 1e3), "ms": e2e_ms, "h2d_bytes": h2d,
+                    "d2h_bytes": d2h,
+                    "what": "host face sizes (and rates) in; Count, Generate, Eval; P/Du/Dv, "
+                            "coords and facets back to pinned host memory"},
+            "roofline_tessellate": {"bound": "hbm", "kernel": "k_tess_generate + k_tess_finish",
+                                    "algorithmic_bytes": facet_b,
+                                    "achieved": facet_b / (gen_ms / 1e3) / 1e9, "peak": peak,
+                                    "unit": "GB/s",
+                                    "frac": facet_b / (gen_ms / 1e3) / 1e9 / peak,
+                                    "traffic": ncu_traffic("bfr_" + mode)},
+            "roofline_eval": {"bound": "hbm", "kernel": "k_eval_patches_lanes (P, Du, Dv)",
+                              "algorithmic_bytes": eval_b,
+                              "achieved": eval_b / (eval_ms / 1e3) / 1e9, "peak": peak,
+                              "unit": "GB/s", "frac": eval_b / (eval_ms / 1e3) / 1e9 / peak},
+            "exact_coords_and_facets_vs_oracle": exact,
+            "max_abs_err_vs_oracle_slice": err,
+            "cpu_baseline": {"value": len(cc) / cpu_s, "unit": "points/s", "cores": cpu_threads,
+                             "kind": "port",
+                             "sample": f"first {sample} faces ({len(cc)} points): oracle "
+                                       "tessellate + locate + PatchMap + EvalPatches"},
+        }
+        del m, coords, facets, pc, outs
+        release_memory()
+    return out
 
 
 def bench_batch(args, stream, peak, cv_max):
@@ -1204,6 +1396,8 @@ def run_gb300(args, rank, world):
     if not args.no_patches:
         line["eval_patches"] = bench_patches(args, stream, peak)
         line["eval_patches_loop"] = bench_patches(args, stream, peak, loop=True)
+    if not args.no_bfr:
+        line["bfr_tessellation"] = bench_bfr(args, stream, peak)
     # serving first: its host-link-bound rounds measure lower after the batching section's
     # 200 GB of tables have churned device and host memory
     if not args.no_serving:

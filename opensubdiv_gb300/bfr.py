@@ -131,13 +131,19 @@ class MeshTessellation:
         self.coord_offsets = torch.zeros(n1, dtype=torch.int64, device=dev)
         self.facet_offsets = torch.zeros(n1, dtype=torch.int64, device=dev)
         self.ptex_offsets = torch.zeros(n1, dtype=torch.int64, device=dev)
+        self.Count()
+
+    def Count(self):
+        """(Re)computes the per-face offsets and the totals (GB300TessellationCount; reads the
+        totals back, so it waits for the stream)."""
         totals = (C.c_int64 * 3)()
         check(_lib.load().GB300TessellationCount(
             self.regular_face_size, self.num_faces, _ptr(self.face_sizes),
             _ptr(self.rate_offsets), _ptr(self.rates), self.uniform_rate, C.byref(self.options),
             _ptr(self.coord_offsets), _ptr(self.facet_offsets), _ptr(self.ptex_offsets), totals,
-            _stream(stream)))
+            _stream(self.stream)))
         self.num_coords, self.num_facets, self.num_ptex_faces = (int(x) for x in totals)
+        return self.num_coords, self.num_facets
 
     @property
     def coord_stride(self):

@@ -406,3 +406,32 @@ def serving_queries(topo, n, seed):
         f = u + v > 1.0
         u[f], v[f] = 1.0 - u[f], 1.0 - v[f]
     return face, u, v
+
+
+# ---- Bfr tessellation ----------------------------------------------------------------------
+
+def bfr_edge_length_rates(positions, verts_per_face, face_verts, interval, max_rate=64):
+    """Per-face edge rates from control-hull edge lengths, the non-uniform scheme of the
+    reference's Bfr tutorial 2.1 (tutorials/bfr/tutorial_2_1/bfr_tutorial_2_1.cpp): an edge's
+    rate is ceil(length / interval) clamped to [1, max_rate]; both faces of an edge see the
+    same length, so shared edges get one rate.  Returns (rate_offsets, rates) with N rates per
+    N-sided face (rates[i] for the edge from vertex i to i + 1)."""
+    vpf = np.asarray(verts_per_face, np.int64)
+    fv = np.asarray(face_verts, np.int64)
+    start = np.concatenate([[0], np.cumsum(vpf)])
+    nxt = np.arange(len(fv)) + 1
+    last = start[1:] - 1
+    nxt[last] = start[:-1]
+    p = np.asarray(positions, np.float64)
+    length = np.linalg.norm(p[fv[nxt]] - p[fv], axis=1)
+    rates = np.clip(np.ceil(length / interval), 1, max_rate).astype(np.int32)
+    return start.astype(np.int32), rates
+
+
+def bfr_tess_bytes(n_faces, n_coords, n_facets, facet_size, locate=True, uniform=True):
+    """Algorithmic bytes of the tessellation kernels for a mesh: per face its size and (with
+    per-face rates) its rate run, three offsets read twice; per coord the (u,v) pair written
+    and, when located, a 20-byte PatchCoord; per facet its indices."""
+    per_face = 4 + 3 * 8 * 2 + (0 if uniform else 4 * 5)
+    return (per_face * n_faces + 8 * n_coords + (20 * n_coords if locate else 0)
+            + 4 * facet_size * n_facets)

@@ -919,3 +919,26 @@ int orc_tess_mesh(int regFaceSize, int numFaces, const int *faceSizes, const int
     }
     return bad == 0;
 }
+
+/* Every coord of a mesh tessellation located for a patch table: the ptex face
+ * (ptexOffsets[f] + the sub-face of Parameterization::ConvertCoordToNormalizedSubFace) and
+ * its normalized (s, t), as the reference's Bfr regression locates tessellation coords
+ * (regression/bfr_evaluate/farPatchEvaluator.cpp:190-207). */
+int orc_tess_locate_mesh(int regFaceSize, int numFaces, const int *faceSizes,
+                         const long *coordOffsets, const long *ptexOffsets, const float *coords,
+                         int *ptexFaces, float *st, int threads) {
+    int bad = 0;
+#pragma omp parallel for schedule(dynamic, 256) num_threads(threads) reduction(+ : bad)
+    for (int f = 0; f < numFaces; ++f) {
+        long c0 = coordOffsets[f];
+        int n = (int)(coordOffsets[f + 1] - c0);
+        if (n == 0) continue;
+        if (!orc_param_to_subface(regFaceSize, faceSizes[f], n, coords + 2 * c0,
+                                  ptexFaces + c0, st + 2 * c0)) {
+            bad++;
+            continue;
+        }
+        for (int i = 0; i < n; ++i) ptexFaces[c0 + i] += (int)ptexOffsets[f];
+    }
+    return bad == 0;
+}

@@ -279,3 +279,18 @@ def tess_mesh(reg_face_size, face_sizes, rate_offsets, rates, facet_size=3,
     if not ok:
         raise RuntimeError("tessellation restatement produced inconsistent counts")
     return dict(coord_offsets=co, facet_offsets=fo, coords=coords, facets=facets)
+
+
+def tess_locate_mesh(reg_face_size, face_sizes, coord_offsets, ptex_offsets, coords, threads=1):
+    """(ptex faces [n], (s, t) [n, 2]) of every coord of a mesh tessellation."""
+    face_sizes = np.ascontiguousarray(face_sizes, np.int32)
+    co = np.ascontiguousarray(coord_offsets, np.int64)
+    po = np.ascontiguousarray(ptex_offsets, np.int64)
+    coords = np.ascontiguousarray(coords, np.float32).reshape(-1, 2)
+    faces = np.zeros(len(coords), np.int32)
+    st = np.zeros_like(coords)
+    if not lib().orc_tess_locate_mesh(C.c_int(reg_face_size), C.c_int(len(face_sizes)),
+                                      _p(face_sizes), _p(co), _p(po), _p(coords), _p(faces),
+                                      _p(st), C.c_int(threads)):
+        raise ValueError("invalid parameterization in the mesh")
+    return faces, st

@@ -126,6 +126,11 @@ int orc_tess_mesh(int regFaceSize, int numFaces, const int *faceSizes, const int
                   const int *rates, int facetSize, int preserveQuads, const long *coordOffsets,
                   const long *facetOffsets, float *coords, int *facets, int threads);
 
+/* Ptex face and normalized (s, t) of every coord of a mesh tessellation. */
+int orc_tess_locate_mesh(int regFaceSize, int numFaces, const int *faceSizes,
+                         const long *coordOffsets, const long *ptexOffsets, const float *coords,
+                         int *ptexFaces, float *st, int threads);
+
 #ifdef __cplusplus
 }
 #endif

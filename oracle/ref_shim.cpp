@@ -21,10 +21,13 @@
 #include <opensubdiv/bfr/tessellation.h>
 #include <opensubdiv/bfr/refinerSurfaceFactory.h>
 #include <opensubdiv/bfr/surface.h>
+#include <opensubdiv/bfr/surfaceFactoryCache.h>
 
 #include <opensubdiv_gb300/far/gb300StencilTableFactory.h>
 
 #include <cstring>
+#include <mutex>
+#include <shared_mutex>
 #include <vector>
 
 using namespace OpenSubdiv;
@@ -882,6 +885,54 @@ void *ref_bfr_mesh_record(void *refiner, int approxSharp, int approxSmooth, cons
         rec->facetOffsets[f + 1] = (long)(f0 + t.GetNumFacets());
     }
     return rec;
+}
+
+// The same loop in float with P, Du and Dv only (the tutorial's outputs), keeping nothing:
+// the reference's CPU Bfr path for timing.  Faces are split over `threads` OpenMP threads,
+// each with its own Surface and buffers, sharing one factory with a thread-safe cache
+// (Bfr::RefinerSurfaceFactory<Bfr::SurfaceFactoryCacheThreaded<...>>, as the reference's
+// tutorial 2.2 recommends for threaded use).  Returns the number of points evaluated.
+long ref_bfr_mesh_run(void *refiner, int approxSharp, int approxSmooth, const float *pos,
+                      const int *rateOffsets, const int *rates, int facetSize, int threads) {
+    Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
+    Bfr::SurfaceFactory::Options so;
+    so.SetApproxLevelSharp(approxSharp);
+    so.SetApproxLevelSmooth(approxSmooth);
+    typedef Bfr::RefinerSurfaceFactory<
+        Bfr::SurfaceFactoryCacheThreaded<std::shared_mutex, std::shared_lock<std::shared_mutex>,
+                                         std::unique_lock<std::shared_mutex>>>
+        Factory;
+    Factory factory(mesh, so);
+    int nf = factory.GetNumFaces();
+    Bfr::Tessellation::Options to = tessOptions(facetSize == 4 ? 4 : 3, 0);
+    long total = 0;
+#pragma omp parallel num_threads(threads) reduction(+ : total)
+    {
+        Bfr::Surface<float> sf;
+        std::vector<float> patch, coords, P, Du, Dv;
+        std::vector<int> facets;
+#pragma omp for schedule(dynamic, 64)
+        for (int f = 0; f < nf; ++f) {
+            if (!factory.InitVertexSurface(f, &sf)) continue;
+            Bfr::Tessellation t(sf.GetParameterization(), rateOffsets[f + 1] - rateOffsets[f],
+                                rates + rateOffsets[f], to);
+            if (!t.IsValid()) continue;
+            int n = t.GetNumCoords();
+            coords.resize(2 * (size_t)n);
+            t.GetCoords(coords.data());
+            patch.resize((size_t)sf.GetNumPatchPoints() * 3);
+            sf.PreparePatchPoints(pos, 3, patch.data(), 3);
+            P.resize(3 * (size_t)n);
+            Du.resize(3 * (size_t)n);
+            Dv.resize(3 * (size_t)n);
+            for (int i = 0; i < n; ++i)
+                sf.Evaluate(&coords[2 * i], patch.data(), 3, &P[3 * i], &Du[3 * i], &Dv[3 * i]);
+            facets.resize((size_t)t.GetNumFacets() * t.GetFacetSize());
+            t.GetFacets(facets.data());
+            total += n;
+        }
+    }
+    return total;
 }
 
 // sizes: {faces, coords, facets}

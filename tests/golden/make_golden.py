@@ -553,6 +553,39 @@ def large_patch_workload(path, cage, level):
     os.replace(tmp, path)
 
 
+def large_bfr_workload(path, cage, rate=5, sample=0.02, seed=7):
+    """The Bfr benchmark's Far table for the full-size torus: the approximation of
+    Bfr::SurfaceFactory's defaults as the reference's Bfr regression builds it (adaptive
+    isolation 6 for sharp and 2 for smooth features, Gregory-basis end caps, infinitely sharp
+    patches, no shared end-cap points, no legacy corner patches) with its source points, plus
+    the reference's Bfr tessellate-and-evaluate of a seeded `sample` of the faces at `rate`
+    (the others rate 0, skipped) for the full-size parity test."""
+    r = ref.Refiner(cage).refine_adaptive_levels(6, 2, True)
+    p = ref.Patches(r, endcap=3, max_isolation=6, inf_sharp=True, share_endcap_points=False,
+                    legacy_sharp_corners=False)
+    nc = cage.num_vertices
+    ns = len(p.st["sizes"])
+    buf = np.zeros((nc + ns) * 3, np.float32)
+    buf[: nc * 3] = cage.positions.reshape(-1)
+    ref.omp_set_threads(os.cpu_count() or 1)
+    assert ref.cpu_eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], p.st["sizes"],
+                                 p.st["offsets"], p.st["indices"], [p.st["weights"]], 0, ns,
+                                 omp=True)
+    nf = len(cage.verts_per_face)
+    rng = np.random.default_rng(seed)
+    rates = np.where(rng.random(nf) < sample, rate, 0).astype(np.int32)
+    rec = ref.bfr_mesh_record(ref.Refiner(cage), cage.positions,
+                              np.arange(nf + 1, dtype=np.int32), rates)
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp.npz"
+    np.savez_compressed(tmp, positions=cage.positions, verts_per_face=cage.verts_per_face,
+                        face_verts=cage.face_verts, arrays=p.arrays, patch_indices=p.indices, params=p.params, src=buf,
+                        triangular=np.int32(0), rate=np.int32(rate), sample_rates=rates,
+                        sample_coord_offsets=rec["coord_offsets"], sample_coords=rec["coords"],
+                        sample_facets=rec["facets"], sample_out3=rec["f32"][:3])
+    os.replace(tmp, path)
+
+
 def large_workloads():
     """The EvalPatches benchmark tables: the plain-method torus (512 x 256, R = 1, r = 0.3,
     seeded 5% triangles and 2% creases U[0, 4]; the cage of the stencil benchmark) and the
@@ -563,6 +596,7 @@ def large_workloads():
     large_patch_workload(os.path.join(LARGE, "torus512x256_adaptiveL4.npz"), torus, 4)
     ico = shapes.icosphere(6, noise=0.005, seed=3)
     large_patch_workload(os.path.join(LARGE, "icosphere6_loop_adaptiveL4.npz"), ico, 4)
+    large_bfr_workload(os.path.join(LARGE, "torus512x256_bfr.npz"), torus)
 
 
 def main():
@@ -577,6 +611,11 @@ def main():
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr":
         bfr_fixtures()
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "bfr-large":
+        torus = shapes.torus(512, 256, R=1.0, r=0.3, tri_fraction=0.05, crease_fraction=0.02,
+                             max_sharpness=4.0, seed=2024)
+        large_bfr_workload(os.path.join(LARGE, "torus512x256_bfr.npz"), torus)
         return
     if len(sys.argv) > 1 and sys.argv[1] == "factory":
         factory_fixture(os.path.join(HERE, "factory_masks.npz"))
