@@ -1,0 +1,169 @@
+//
+// Bfr-shaped C++ layer over the batched device tessellation of libosd_gb300.so
+// (GB300TessellationCount / GB300TessellationGenerate, include/osd_gb300.h).
+//
+// The reference's Bfr tutorials tessellate a mesh face by face (tutorials/bfr/tutorial_1_2/
+// bfr_tutorial_1_2.cpp:170-238): a Bfr::Tessellation per face, its coords evaluated by
+// Bfr::Surface::Evaluate, its facets offset by the points written so far
+// (Tessellation::TransformFacetCoordIndices).  GB300MeshTessellation does every face of the mesh
+// in one pass on the device: the same coords (bit for bit) and facets, each coord located as a
+// PatchCoord on a device patch table, which the GB300Evaluator's EvalPatches turns into P, Du,
+// Dv (and second derivatives).  Options mirror Bfr::Tessellation::Options
+// (bfr/tessellation.h:60-100); with the reference's headers on the include path they convert
+// from it.
+//
+#ifndef OPENSUBDIV_GB300_BFR_GB300_TESSELLATION_H
+#define OPENSUBDIV_GB300_BFR_GB300_TESSELLATION_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "../osd/gb300Evaluator.h"
+
+#if defined(OSD_GB300_HAVE_OPENSUBDIV) && defined(__has_include)
+#if __has_include(<opensubdiv/bfr/tessellation.h>)
+#define OSD_GB300_HAVE_BFR 1
+#include <opensubdiv/bfr/tessellation.h>
+#endif
+#endif
+
+#ifdef OSD_GB300_HAVE_OPENSUBDIV
+#define OSD_GB300_BFR_NAMESPACE_BEGIN \
+    namespace OpenSubdiv {            \
+    namespace OPENSUBDIV_VERSION {    \
+    namespace Bfr {
+#define OSD_GB300_BFR_NAMESPACE_END \
+    }                               \
+    }                               \
+    }
+#else
+#define OSD_GB300_BFR_NAMESPACE_BEGIN \
+    namespace OpenSubdiv {            \
+    namespace Bfr {
+#define OSD_GB300_BFR_NAMESPACE_END \
+    }                               \
+    }
+#endif
+
+OSD_GB300_BFR_NAMESPACE_BEGIN
+
+/// Bfr::Tessellation of every face of a mesh, on the device.
+class GB300MeshTessellation {
+public:
+    /// Bfr::Tessellation::Options (facet size 3 or 4, quad preservation, strides).
+    class Options {
+    public:
+        Options() { _o.facetSize = 3, _o.preserveQuads = 0, _o.coordStride = 0, _o.facetStride = 0; }
+#ifdef OSD_GB300_HAVE_BFR
+        Options(Tessellation::Options const &b) {
+            _o.facetSize = b.GetFacetSize();
+            _o.preserveQuads = b.PreserveQuads() ? 1 : 0;
+            _o.coordStride = b.GetCoordStride();
+            _o.facetStride = b.GetFacetStride();
+        }
+#endif
+        Options &PreserveQuads(bool on) { _o.preserveQuads = on ? 1 : 0; return *this; }
+        bool PreserveQuads() const { return _o.preserveQuads != 0; }
+        Options &SetFacetSize(int n) { _o.facetSize = (n == 4) ? 4 : 3; return *this; }
+        int GetFacetSize() const { return _o.facetSize == 4 ? 4 : 3; }
+        Options &SetFacetStride(int s) { _o.facetStride = s; return *this; }
+        int GetFacetStride() const { return _o.facetStride; }
+        Options &SetCoordStride(int s) { _o.coordStride = s; return *this; }
+        int GetCoordStride() const { return _o.coordStride; }
+        GB300TessellationOptions const *get() const { return &_o; }
+
+    private:
+        GB300TessellationOptions _o;
+    };
+
+    /// Every face at one uniform rate (Tessellation(param, uniformRate, options)).
+    /// faceSizes: DEVICE array of numFaces face sizes; regularFaceSize: the scheme's regular
+    /// face size (Sdc::SchemeTypeTraits::GetRegularFaceSize).  NULL on failure
+    /// (GB300GetLastErrorString says why).
+    static GB300MeshTessellation *Create(int regularFaceSize, int numFaces, int const *faceSizes,
+                                         int uniformRate, Options const &options = Options(),
+                                         void *stream = NULL) {
+        return create(regularFaceSize, numFaces, faceSizes, NULL, NULL, uniformRate, options,
+                      stream);
+    }
+
+    /// Per-face rates (Tessellation(param, numRates, rates, options)): face f takes
+    /// rates[rateOffsets[f] .. rateOffsets[f+1]) -- DEVICE arrays.  A face with an invalid
+    /// tessellation (rate < 1, a size the scheme rejects) gets no coords, as an invalid
+    /// Bfr::Tessellation has none: give faces without a limit surface a rate of 0.
+    static GB300MeshTessellation *Create(int regularFaceSize, int numFaces, int const *faceSizes,
+                                         int const *rateOffsets, int const *rates,
+                                         Options const &options = Options(),
+                                         void *stream = NULL) {
+        return create(regularFaceSize, numFaces, faceSizes, rateOffsets, rates, 0, options,
+                      stream);
+    }
+
+    ~GB300MeshTessellation() { cudaFree(_offsets); }
+
+    int GetNumFaces() const { return _numFaces; }
+    int GetNumCoords() const { return (int)_totals[0]; }
+    int GetNumFacets() const { return (int)_totals[1]; }
+    int GetNumPtexFaces() const { return (int)_totals[2]; }
+    int GetFacetSize() const { return _options.GetFacetSize(); }
+    int GetCoordStride() const { return _options.GetCoordStride() ? _options.GetCoordStride() : 2; }
+    int GetFacetStride() const {
+        return _options.GetFacetStride() ? _options.GetFacetStride() : GetFacetSize();
+    }
+    /// DEVICE exclusive scans (numFaces + 1 entries) of coords, facets and ptex faces.
+    int64_t const *GetCoordOffsets() const { return _offsets; }
+    int64_t const *GetFacetOffsets() const { return _offsets + (_numFaces + 1); }
+    int64_t const *GetPtexOffsets() const { return _offsets + 2 * (size_t)(_numFaces + 1); }
+
+    /// Writes the coords (Tessellation::GetCoords of each face) and facets (GetFacets, offset
+    /// to the mesh-wide coord numbering unless meshIndices is false) into DEVICE buffers of
+    /// GetNumCoords() x coord stride floats and GetNumFacets() x facet stride ints; with a
+    /// patch table, also one PatchCoord per coord for GB300Evaluator::EvalPatches.
+    bool Generate(float *coords, int *facets, bool meshIndices = true,
+                  Osd::GB300PatchTable const *table = NULL, Osd::PatchCoord *patchCoords = NULL,
+                  void *stream = NULL) const {
+        return GB300TessellationGenerate(
+                   _reg, _numFaces, _faceSizes, _rateOffsets, _rates, _uniformRate,
+                   _options.get(), GetCoordOffsets(), GetFacetOffsets(), GetPtexOffsets(), coords,
+                   facets, meshIndices ? 1 : 0, table ? table->GetHandle() : NULL, patchCoords,
+                   stream) == GB300_OK;
+    }
+
+private:
+    GB300MeshTessellation() {}
+
+    static GB300MeshTessellation *create(int reg, int numFaces, int const *faceSizes,
+                                         int const *rateOffsets, int const *rates,
+                                         int uniformRate, Options const &options, void *stream) {
+        GB300MeshTessellation *t = new GB300MeshTessellation;
+        t->_reg = reg;
+        t->_numFaces = numFaces;
+        t->_faceSizes = faceSizes;
+        t->_rateOffsets = rateOffsets;
+        t->_rates = rates;
+        t->_uniformRate = uniformRate;
+        t->_options = options;
+        if (numFaces < 0 ||
+            cudaMalloc(&t->_offsets, sizeof(int64_t) * 3 * ((size_t)numFaces + 1)) !=
+                cudaSuccess ||
+            GB300TessellationCount(reg, numFaces, faceSizes, rateOffsets, rates, uniformRate,
+                                   options.get(), t->_offsets, t->_offsets + (numFaces + 1),
+                                   t->_offsets + 2 * ((size_t)numFaces + 1), t->_totals,
+                                   stream) != GB300_OK) {
+            delete t;
+            return NULL;
+        }
+        return t;
+    }
+
+    int _reg = 4, _numFaces = 0, _uniformRate = 0;
+    int const *_faceSizes = NULL, *_rateOffsets = NULL, *_rates = NULL;
+    Options _options;
+    int64_t *_offsets = NULL;
+    int64_t _totals[3] = {0, 0, 0};
+};
+
+OSD_GB300_BFR_NAMESPACE_END
+
+#endif  // OPENSUBDIV_GB300_BFR_GB300_TESSELLATION_H

@@ -60,13 +60,23 @@ GB_HD int imin(int a, int b) { return a < b ? a : b; }
 GB_HD int imax(int a, int b) { return a > b ? a : b; }
 
 // Where a face's coords and facets go: coords as (u,v) pairs `cs` floats apart, facets as
-// `fsz` indices `fst` ints apart.
+// `fsz` indices `fst` ints apart, each index offset by `base` (the face's first coord in a
+// mesh-wide numbering, Tessellation::TransformFacetCoordIndices(facets, commonOffset),
+// tessellation.cpp:2429-2447; -1 pads stay -1).
 struct Sink {
     float *c;
     int cs;
     int *f;
     int fsz, fst;
+    int base = 0;
+    bool pairs = false;  // cs == 2 and c 8-byte aligned: a coord is one 8-byte store
     GB_HD void uv(int i, float u, float v) const {
+#ifdef __CUDA_ARCH__
+        if (pairs) {
+            *reinterpret_cast<float2 *>(c + 2 * (int64_t)i) = make_float2(u, v);
+            return;
+        }
+#endif
         c[(int64_t)i * cs] = u;
         c[(int64_t)i * cs + 1] = v;
     }
@@ -74,8 +84,8 @@ struct Sink {
     // Facet::Set of three indices (tessellation.cpp:114-118): a 4-tuple's last slot is -1
     GB_HD int tri(int i, int a, int b, int c2) const {
         int *t = facet(i);
-        t[fsz - 1] = -1;
-        t[0] = a, t[1] = b, t[2] = c2;
+        if (fsz == 4) t[3] = -1;
+        t[0] = a + base, t[1] = b + base, t[2] = c2 + base;
         return 1;
     }
     // appendQuad (tessellation.cpp:200-219): sign 0 keeps the quad, > 0 splits it along
@@ -83,7 +93,7 @@ struct Sink {
     GB_HD int quad(int i, int a, int b, int c2, int d, int sign) const {
         if (sign == 0) {
             int *t = facet(i);
-            t[0] = a, t[1] = b, t[2] = c2, t[3] = d;
+            t[0] = a + base, t[1] = b + base, t[2] = c2 + base, t[3] = d + base;
             return 1;
         }
         if (sign > 0) {
@@ -266,18 +276,23 @@ GB_HD int qsub_uniform_facets(int N, int res, int tri) {
 struct Face {
     int kind = 0, N = 0, udim = 0;
     int nr = 0;
-    const int *rates = nullptr;
+    const int *rates = nullptr;  // the given rates, or null for the one rate `single`
+    int single = 0;
+    int o0 = 0, o1 = 0, o2 = 0, o3 = 0;
     int in0 = 0, in1 = 0;
     int uniform = 0, triangulate = 1, fs = 3;
     int nBoundary = 0, nInterior = 0, nFacets = 0;
     int mode = kGeneral;
     int valid = 0;
 
-    // rate of edge e (the edge from vertex e to e + 1)
+    // rate of edge e (the edge from vertex e to e + 1); the edge rates of triangles and quads
+    // are held in registers (o0..o3), larger faces read theirs from the given rates
     GB_HD int outer(int e) const {
         if (nr < N) return (nr == 2 && N == 4) ? ((e & 1) ? in1 : in0) : in0;
+        if (N <= 4) return e == 0 ? o0 : e == 1 ? o1 : e == 2 ? o2 : o3;
         return imin(rates[e], kMaxRate);
     }
+    GB_HD int given(int i) const { return rates ? rates[i] : single; }
 
     GB_HD void vertex(int v, float uv[2]) const {
         if (kind == kQuad) {
@@ -292,8 +307,10 @@ struct Face {
         }
     }
 
+    // One rate: givenRates may be null and the rate is singleRate (no pointer into the
+    // caller's registers, which would put them in local memory on the device).
     GB_HD bool init(int regFaceSize, int faceSize, int numRates, const int *givenRates,
-                    int facetSize, int preserveQuads) {
+                    int facetSize, int preserveQuads, int singleRate = 0) {
         N = faceSize;
         valid = 0;
         nBoundary = nInterior = nFacets = 0;
@@ -304,11 +321,12 @@ struct Face {
             kind = kQsub;
             udim = (N < 10) ? 2 + (N > 4) : 1 + (int)sqrtf((float)(N - 1));
         }
-        if (numRates < 1) return false;
-        for (int i = 0; i < numRates; ++i)
-            if (givenRates[i] < 1) return false;
+        if (numRates < 1 || (!givenRates && numRates != 1)) return false;
         nr = numRates;
         rates = givenRates;
+        single = singleRate;
+        for (int i = 0; i < numRates; ++i)
+            if (given(i) < 1) return false;
         fs = (facetSize == 4) ? 4 : 3;
         triangulate = (fs == 3) || !preserveQuads;
 
@@ -316,27 +334,33 @@ struct Face {
         int total = 0;
         if (nr < N) {
             if (nr == 2 && quadFace) {
-                in0 = imin(rates[0], kMaxRate);
-                in1 = imin(rates[1], kMaxRate);
+                in0 = imin(given(0), kMaxRate);
+                in1 = imin(given(1), kMaxRate);
                 uniform = in0 == in1;
                 total = 2 * (in0 + in1);
             } else {
-                in0 = in1 = imin(rates[0], kMaxRate);
+                in0 = in1 = imin(given(0), kMaxRate);
                 uniform = 1;
                 total = in0 * N;
             }
         } else {
+            if (N <= 4) {
+                o0 = imin(given(0), kMaxRate);
+                o1 = imin(given(1), kMaxRate);
+                o2 = imin(given(2), kMaxRate);
+                o3 = N == 4 ? imin(given(3), kMaxRate) : 0;
+            }
             uniform = 1;
-            const int o0 = imin(rates[0], kMaxRate);
+            const int r0 = imin(given(0), kMaxRate);
             for (int i = 0; i < N; ++i) {
-                const int oi = imin(rates[i], kMaxRate);
-                uniform = uniform && oi == o0;
+                const int oi = imin(given(i), kMaxRate);
+                uniform = uniform && oi == r0;
                 total += oi;
             }
             if (nr > N) {
-                in0 = imin(rates[N], kMaxRate);
-                in1 = (nr == 6 && quadFace) ? imin(rates[5], kMaxRate) : in0;
-                uniform = uniform && in0 == o0 && in1 == o0;
+                in0 = imin(given(N), kMaxRate);
+                in1 = (nr == 6 && quadFace) ? imin(given(5), kMaxRate) : in0;
+                uniform = uniform && in0 == r0 && in1 == r0;
             } else if (quadFace) {
                 in0 = (outer(0) + outer(2)) / 2;
                 in1 = (outer(1) + outer(3)) / 2;
@@ -419,16 +443,19 @@ struct Face {
         return true;
     }
 
+    // an edge whose rate equals the inner rate along it keeps the uniform strip
+    // (tessellation.cpp:1124-1135)
+    GB_HD bool quad_uniform_edge(int e) const { return outer(e) == ((e & 1) ? in1 : in0); }
+
     // quad::CountNonUniformFacets (tessellation.cpp:829-885)
     GB_HD int quad_nonuniform_facets() const {
         const int uIn = in0 - 2, vIn = in1 - 2;
         int n = uIn * vIn;
         if (triangulate) return 2 * n + 2 * (uIn + vIn) + outer(0) + outer(1) + outer(2) + outer(3);
-        int uni[4] = {outer(0) == in0, outer(1) == in1, outer(2) == in0, outer(3) == in1};
         for (int e = 0; e < 4; ++e) {
             const int in = (e & 1) ? vIn : uIn;
-            if (uni[e]) {
-                n += in + 1 + !(uni[(e + 1) & 3] && uni[e]);
+            if (quad_uniform_edge(e)) {
+                n += in + 1 + !(quad_uniform_edge((e + 1) & 3) && quad_uniform_edge(e));
             } else {
                 int f = imax(outer(e), in);
                 if ((f & 1) == 0) f += (outer(e) & 1) || (in & 1);
@@ -610,9 +637,6 @@ struct Face {
     // quad::getBoundaryRingFacets (tessellation.cpp:1121-1225)
     GB_HD int quad_boundary_ring(const Sink &o) const {
         const int ur = in0, vr = in1, nB = nBoundary, tri = triangulate;
-        const int uni[4] = {outer(0) == ur, outer(1) == vr, outer(2) == ur, outer(3) == vr};
-        const int corner[4] = {uni[0] && uni[3], uni[1] && uni[0], uni[2] && uni[1],
-                               uni[3] && uni[2]};
         const int uIn = ur - 2, vIn = vr - 2;
         int n = 0;
         Strip s;
@@ -631,9 +655,10 @@ struct Face {
                 s.iFirst = s.iLast;
                 s.iLast = (e == 3) ? nB : s.iLast + inner * (s.reversed ? -1 : 1);
             }
-            if (uni[e]) {
-                s.splitFirst = !corner[e];
-                s.splitLast = !corner[(e + 1) & 3];
+            if (quad_uniform_edge(e)) {
+                // a corner keeps its quad when both edges at it are uniform
+                s.splitFirst = !quad_uniform_edge((e + 3) & 3);
+                s.splitLast = !quad_uniform_edge((e + 1) & 3);
                 n += s.quads_uniform(o, n);
             } else {
                 s.splitFirst = s.splitLast = 1;
@@ -673,8 +698,6 @@ struct Face {
     // tri::getBoundaryRingFacets (tessellation.cpp:1484-1561)
     GB_HD int tri_boundary_ring(const Sink &o) const {
         const int res = in0, nB = nBoundary;
-        const int uni[3] = {outer(0) == res, outer(1) == res, outer(2) == res};
-        const int corner[3] = {uni[0] && uni[2], uni[1] && uni[0], uni[2] && uni[1]};
         const int inner = res - 3;
         int n = 0;
         Strip s;
@@ -691,9 +714,9 @@ struct Face {
                 s.iFirst = s.iLast;
                 s.iLast = (e == 2) ? nB : s.iLast + inner;
             }
-            if (uni[e]) {
-                s.splitFirst = !corner[e];
-                s.splitLast = !corner[(e + 1) % 3];
+            if (outer(e) == res) {
+                s.splitFirst = outer((e + 2) % 3) != res;
+                s.splitLast = outer((e + 1) % 3) != res;
                 n += s.tris_uniform(o, n);
             } else {
                 s.splitFirst = s.splitLast = 1;

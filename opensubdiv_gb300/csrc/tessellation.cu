@@ -1,22 +1,25 @@
 // Bfr::Tessellation over every face of a mesh at once (bfr/tessellation.h:142-262), with the
 // points located on a device patch table for evaluation.
 //
-// Three launches on one stream:
+// Launches on one stream:
 //   count    one thread per face: the face's coord, facet and ptex-face counts, then device
 //            exclusive scans into the caller's offset arrays (the only host sync is the read
 //            of the three totals, which the caller needs to size its buffers);
-//   generate one thread per face pattern: with a single uniform rate every face of the same
-//            size has the same pattern, so one thread builds it per face size (3..10) into
-//            library scratch; other faces (per-face rates, larger polygons) are generated by
-//            one thread each straight into their slice of the output;
+//   patterns with a single uniform rate every face of the same size has the same pattern: one
+//            thread builds it per face size (3..10), once per device and request (cached);
+//   generate one thread per face without a shared pattern (per-face rates, polygons above 10
+//            sides) writes its coords and facets straight into its slice of the output, facet
+//            indices offset to the mesh-wide coord numbering
+//            (Tessellation::TransformFacetCoordIndices, tessellation.cpp:2429-2447);
 //   finish   one warp per face, lanes over the face's coords and facets (coalesced): copies
-//            the shared pattern out, offsets facet indices to the mesh-wide coord numbering
-//            (Tessellation::TransformFacetCoordIndices, tessellation.cpp:2429-2447), and turns
-//            each coord into a PatchCoord: Parameterization::ConvertCoordToNormalizedSubFace
-//            (bfr/parameterization.cpp:135-162) picks the ptex sub-face of an N-gon, and the
+//            the shared pattern out with offset indices, and turns each coord into a
+//            PatchCoord: Parameterization::ConvertCoordToNormalizedSubFace
+//            (bfr/parameterization.cpp:135-162) picks the ptex sub-face of an N-gon and the
 //            PatchMap walk finds the patch -- the lookup the reference's Bfr regression does
 //            for every tessellation coord (regression/bfr_evaluate/farPatchEvaluator.cpp:
 //            190-207).
+// A staged variant (faces generated into a shared-memory arena, copied out coalesced) was
+// slower: about 900 bytes of arena per face left too few warps resident to hide latency.
 #include "common.cuh"
 #include "patchmap.h"
 #include "patchmap_walk.cuh"
@@ -24,7 +27,10 @@
 
 #include <cub/device/device_scan.cuh>
 
+#include <atomic>
 #include <climits>
+#include <mutex>
+#include <vector>
 
 namespace gb300 {
 namespace {
@@ -35,17 +41,17 @@ using tess::Sink;
 constexpr int kFirstShared = 3;  // face sizes with a shared uniform pattern: 3 .. 10
 constexpr int kNumShared = 8;
 
+// The rates of face f: p == null means the single rate `one` (the uniform rate).
 struct FaceRates {
-    int one;  // storage for a single rate (uniform or one per face)
     const int *p;
-    int n;
+    int n, one;
 };
 
 __device__ __forceinline__ void rates_of(const int *rateOffsets, const int *rates,
                                          int uniformRate, int f, FaceRates &r) {
+    r.one = uniformRate;
     if (!rates) {
-        r.one = uniformRate;
-        r.p = &r.one;
+        r.p = nullptr;
         r.n = 1;
     } else if (!rateOffsets) {
         r.p = rates + f;
@@ -74,7 +80,7 @@ __global__ void __launch_bounds__(256) k_tess_count(const CountArgs a) {
         FaceRates r;
         rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
         Face face;
-        const bool ok = face.init(a.reg, N, r.n, r.p, a.fs, a.pq);
+        const bool ok = face.init(a.reg, N, r.n, r.p, a.fs, a.pq, r.one);
         a.cc[f] = ok ? face.num_coords() : 0;
         a.fc[f] = ok ? face.nFacets : 0;
         a.pc[f] = N > 0 ? tess::ptex_count(a.reg, N) : 0;
@@ -88,11 +94,13 @@ struct GenArgs {
     float *coords;
     int *facets;
     int offsetIndices;
-    // shared uniform patterns for face sizes kFirstShared + k (packed: stride 2 / fs)
+    int coordPairs;  // coordStride 2 and 8-byte aligned coords: (u,v) stored as one float2
+    // shared uniform patterns for face sizes kFirstShared + k (packed: stride 2 / fs, local
+    // facet indices)
     int shared;
     int patC[kNumShared + 1], patF[kNumShared + 1];
-    float *patCoords;
-    int *patFacets;
+    const float *patCoords;
+    const int *patFacets;
     // location on a patch table (optional)
     int locate;
     PatchMapView map;
@@ -103,34 +111,66 @@ __device__ __forceinline__ bool uses_shared(const GenArgs &a, int N) {
     return a.shared && N >= kFirstShared && N < kFirstShared + kNumShared;
 }
 
-__global__ void __launch_bounds__(128) k_tess_generate(const GenArgs a) {
-    const int nShared = a.shared ? kNumShared : 0;
-    const int total = nShared + a.numFaces;
+// One thread per shared pattern (a face size 3..10 at the uniform rate).
+__global__ void __launch_bounds__(32) k_tess_patterns(int reg, int rate, int fs, int pq,
+                                                      const int *patC, const int *patF,
+                                                      float *patCoords, int *patFacets) {
+    const int t = threadIdx.x;
+    if (t >= kNumShared) return;
+    Face face;
+    if (!face.init(reg, kFirstShared + t, 1, nullptr, fs, pq, rate)) return;
+    Sink o{patCoords + 2 * (int64_t)patC[t], 2, patFacets + (int64_t)fs * patF[t], fs, fs};
+    face.coords(o);
+    face.facets(o);
+}
+
+// PatchCoord of a coord of face (size N, first ptex face ptex0): the ptex sub-face and
+// normalized (s, t) of Parameterization::ConvertCoordToNormalizedSubFace
+// (bfr/parameterization.cpp:135-162), then the PatchMap walk.
+__device__ __forceinline__ void locate_coord(const GenArgs &a, int N, int ptex0, float u, float v,
+                                             int *o) {
+    int sub = 0;
+    float s = u, t = v;
+    if (N != a.reg) {
+        const int udim = (N < 10) ? 2 + (N > 4) : 1 + (int)sqrtf((float)(N - 1));
+        int ut = (int)u, vt = (int)v;
+        float uf = __fsub_rn(u, (float)ut), vf = __fsub_rn(v, (float)vt);
+        if (uf > 0.75f) { ut++; uf = __fsub_rn(uf, 1.0f); }
+        if (vf > 0.75f) { vt++; vf = __fsub_rn(vf, 1.0f); }
+        s = __fmul_rn(uf, 2.0f);
+        t = __fmul_rn(vf, 2.0f);
+        sub = udim * vt + ut;
+    }
+    const int4 h = patch_map_find(a.map, ptex0 + sub, s, t);
+    o[0] = h.x;
+    o[1] = h.y;
+    o[2] = h.z;
+    o[3] = __float_as_int(s);
+    o[4] = __float_as_int(t);
+}
+
+// One thread per face without a shared pattern: the face's coords and facets (indices already
+// offset to the mesh numbering) straight into its slice of the output.
+__global__ void __launch_bounds__(128, 8) k_tess_generate(const GenArgs a) {
     const int stride = gridDim.x * blockDim.x;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += stride) {
-        Face face;
-        if (t < nShared) {
-            const int rate = a.uniformRate;
-            if (!face.init(a.reg, kFirstShared + t, 1, &rate, a.fs, a.pq)) continue;
-            Sink o{a.patCoords + 2 * (int64_t)a.patC[t], 2, a.patFacets + (int64_t)a.fs * a.patF[t],
-                   a.fs, a.fs};
-            face.coords(o);
-            face.facets(o);
-            continue;
-        }
-        const int f = t - nShared;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
         const int N = a.faceSizes[f];
         if (uses_shared(a, N)) continue;
         FaceRates r;
         rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
-        if (!face.init(a.reg, N, r.n, r.p, a.fs, a.pq)) continue;
-        Sink o{a.coords + a.co[f] * a.coordStride, a.coordStride,
-               a.facets + a.fo[f] * a.facetStride, a.fs, a.facetStride};
+        Face face;
+        if (!face.init(a.reg, N, r.n, r.p, a.fs, a.pq, r.one)) continue;
+        const int64_t c0 = a.co[f];
+        Sink o{a.coords + c0 * a.coordStride, a.coordStride, a.facets + a.fo[f] * a.facetStride,
+               a.fs, a.facetStride, a.offsetIndices ? (int)c0 : 0, a.coordPairs != 0};
         face.coords(o);
         face.facets(o);
     }
 }
 
+// One warp per face: copies a shared pattern out (coords as float2 pairs, one lane per facet
+// with its indices offset), and locates every coord of the face on the patch table.
+template <int FS>
 __global__ void __launch_bounds__(256) k_tess_finish(const GenArgs a) {
     const int lane = threadIdx.x & 31;
     const int warps = (gridDim.x * blockDim.x) >> 5;
@@ -138,58 +178,103 @@ __global__ void __launch_bounds__(256) k_tess_finish(const GenArgs a) {
         const int64_t c0 = a.co[f];
         const int nc = (int)(a.co[f + 1] - c0);
         if (nc == 0) continue;
-        const int64_t f0 = a.fo[f];
-        const int nf = (int)(a.fo[f + 1] - f0);
         const int N = a.faceSizes[f];
         const bool sh = uses_shared(a, N);
+        if (!sh && !a.locate) continue;
         const int k = N - kFirstShared;
-        const float *src = sh ? a.patCoords + 2 * (int64_t)a.patC[k] : a.coords + c0 * a.coordStride;
-        const int srcStride = sh ? 2 : a.coordStride;
-
-        if (sh || a.locate) {
-            // Parameterization of the face (bfr/parameterization.cpp:40-66)
-            const bool subfaces = N != a.reg;
-            const int udim = !subfaces ? 0 : (N < 10) ? 2 + (N > 4) : 1 + (int)sqrtf((float)(N - 1));
-            const int ptex0 = a.locate ? (int)a.po[f] : 0;
+        const int ptex0 = a.locate ? (int)a.po[f] : 0;
+        if (sh) {
+            const float2 *pc = reinterpret_cast<const float2 *>(a.patCoords) + a.patC[k];
             for (int i = lane; i < nc; i += 32) {
-                const float u = src[(int64_t)i * srcStride], v = src[(int64_t)i * srcStride + 1];
-                if (sh) {
-                    float *d = a.coords + (c0 + i) * a.coordStride;
-                    d[0] = u;
-                    d[1] = v;
+                const float2 uv = pc[i];
+                float *d = a.coords + (c0 + i) * a.coordStride;
+                if (a.coordPairs) {
+                    *reinterpret_cast<float2 *>(d) = uv;
+                } else {
+                    d[0] = uv.x;
+                    d[1] = uv.y;
                 }
-                if (!a.locate) continue;
-                int sub = 0;
-                float s = u, t = v;
-                if (subfaces) {
-                    int ut = (int)u, vt = (int)v;
-                    float uf = __fsub_rn(u, (float)ut), vf = __fsub_rn(v, (float)vt);
-                    if (uf > 0.75f) { ut++; uf = __fsub_rn(uf, 1.0f); }
-                    if (vf > 0.75f) { vt++; vf = __fsub_rn(vf, 1.0f); }
-                    s = __fmul_rn(uf, 2.0f);
-                    t = __fmul_rn(vf, 2.0f);
-                    sub = udim * vt + ut;
-                }
-                const int4 h = patch_map_find(a.map, ptex0 + sub, s, t);
-                int *o = a.patchCoords + 5 * (c0 + i);
-                o[0] = h.x;
-                o[1] = h.y;
-                o[2] = h.z;
-                o[3] = __float_as_int(s);
-                o[4] = __float_as_int(t);
+                if (a.locate) locate_coord(a, N, ptex0, uv.x, uv.y, a.patchCoords + 5 * (c0 + i));
             }
-        }
-        if (sh || a.offsetIndices) {
+            const int64_t f0 = a.fo[f];
+            const int nf = (int)(a.fo[f + 1] - f0);
             const int off = a.offsetIndices ? (int)c0 : 0;
-            const int *pf = sh ? a.patFacets + (int64_t)a.fs * a.patF[k] : nullptr;
-            for (int j = lane; j < nf * a.fs; j += 32) {
-                const int q = j / a.fs, c = j - q * a.fs;
-                int *d = a.facets + (f0 + q) * a.facetStride + c;
-                const int v = sh ? pf[j] : *d;
-                *d = v >= 0 ? v + off : v;
+            const int *pf = a.patFacets + FS * a.patF[k];
+            for (int q = lane; q < nf; q += 32) {
+                int *d = a.facets + (f0 + q) * a.facetStride;
+#pragma unroll
+                for (int c = 0; c < FS; ++c) {
+                    const int v = pf[FS * q + c];
+                    d[c] = v >= 0 ? v + off : v;
+                }
+            }
+        } else {
+            for (int i = lane; i < nc; i += 32) {
+                const float *c = a.coords + (c0 + i) * a.coordStride;
+                float u, v;
+                if (a.coordPairs) {
+                    const float2 uv = *reinterpret_cast<const float2 *>(c);
+                    u = uv.x;
+                    v = uv.y;
+                } else {
+                    u = c[0];
+                    v = c[1];
+                }
+                locate_coord(a, N, ptex0, u, v, a.patchCoords + 5 * (c0 + i));
             }
         }
     }
+}
+
+// Shared uniform patterns, cached per device and request (they depend only on the scheme's
+// face size, the rate and the facet options) up to kPatternCacheBytes; beyond that a call
+// builds them in per-call scratch.
+struct PatternKey {
+    int dev, reg, rate, fs, pq;
+    bool operator==(const PatternKey &o) const {
+        return dev == o.dev && reg == o.reg && rate == o.rate && fs == o.fs && pq == o.pq;
+    }
+};
+struct Patterns {
+    int patC[kNumShared + 1], patF[kNumShared + 1];
+    void *mem = nullptr;
+    size_t bytes = 0;
+};
+constexpr size_t kPatternCacheBytes = size_t(64) << 20;
+std::mutex g_patMutex;
+std::vector<std::pair<PatternKey, Patterns>> g_patterns;
+size_t g_patBytes = 0;
+
+void pattern_sizes(int reg, int rate, int fs, int pq, Patterns &p) {
+    p.patC[0] = p.patF[0] = 0;
+    for (int k = 0; k < kNumShared; ++k) {
+        Face face;
+        const bool v = face.init(reg, kFirstShared + k, 1, nullptr, fs, pq, rate);
+        p.patC[k + 1] = p.patC[k] + (v ? face.num_coords() : 0);
+        p.patF[k + 1] = p.patF[k] + (v ? face.nFacets : 0);
+    }
+    const size_t cb = sizeof(float) * 2 * (size_t)p.patC[kNumShared];
+    p.bytes = ((cb + 15) & ~size_t(15)) + sizeof(int) * (size_t)fs * p.patF[kNumShared] +
+              sizeof(int) * 2 * (kNumShared + 1);
+}
+
+// Builds the patterns of `p` into p.mem: the offset tables go after the coords and facets.
+int build_patterns(int reg, int rate, int fs, int pq, Patterns &p, cudaStream_t s,
+                   const char *who) {
+    const size_t cb = sizeof(float) * 2 * (size_t)p.patC[kNumShared];
+    float *pc = (float *)p.mem;
+    int *pf = (int *)((char *)p.mem + ((cb + 15) & ~size_t(15)));
+    int *tables = pf + (size_t)fs * p.patF[kNumShared];
+    int host[2 * (kNumShared + 1)];
+    for (int k = 0; k <= kNumShared; ++k) host[k] = p.patC[k], host[kNumShared + 1 + k] = p.patF[k];
+    int st = check_cuda(cudaMemcpyAsync(tables, host, sizeof(host), cudaMemcpyHostToDevice, s), who);
+    if (st != GB300_OK) return st;
+    k_tess_patterns<<<1, 32, 0, s>>>(reg, rate, fs, pq, tables, tables + kNumShared + 1, pc, pf);
+    count_launch();
+    st = check_launch(who);
+    // the host array is read by the copy above
+    if (st == GB300_OK) st = check_cuda(cudaStreamSynchronize(s), who);
+    return st;
 }
 
 int grid_for(long long items, int threads, int perSm) {
@@ -326,39 +411,78 @@ extern "C" int GB300TessellationGenerate(
     a.coords = coords;
     a.facets = facets;
     a.offsetIndices = offsetFacetIndices != 0;
-    a.shared = rates == nullptr;
+    a.coordPairs = o.coordStride == 2 && ((uintptr_t)coords & 7) == 0;
+    a.shared = rates == nullptr && uniformRate >= 1;
     a.patCoords = nullptr;
     a.patFacets = nullptr;
     a.locate = table != nullptr;
     a.patchCoords = (int *)patchCoords;
     if (table) a.map = view_of(*patch_map_of(table));
 
-    void *pat = nullptr;
+    Patterns scratchPat;
     if (a.shared) {
-        // sizes of the shared patterns, from the same inventory the device uses
-        a.patC[0] = a.patF[0] = 0;
-        for (int k = 0; k < kNumShared; ++k) {
-            tess::Face face;
-            const int rate = uniformRate;
-            const bool v = face.init(regularFaceSize, kFirstShared + k, 1, &rate, o.fs, o.pq);
-            a.patC[k + 1] = a.patC[k] + (v ? face.num_coords() : 0);
-            a.patF[k + 1] = a.patF[k] + (v ? face.nFacets : 0);
+        int dev = 0;
+        if ((st = check_cuda(cudaGetDevice(&dev), who)) != GB300_OK) return st;
+        const PatternKey key{dev, regularFaceSize, uniformRate, o.fs, o.pq};
+        const Patterns *use = nullptr;
+        {
+            std::lock_guard<std::mutex> lock(g_patMutex);
+            for (auto &e : g_patterns)
+                if (e.first == key) use = &e.second;
+            if (!use) {
+                Patterns p;
+                pattern_sizes(regularFaceSize, uniformRate, o.fs, o.pq, p);
+                if (g_patBytes + p.bytes <= kPatternCacheBytes) {
+                    if ((st = check_cuda(cudaMalloc(&p.mem, p.bytes), who)) != GB300_OK) return st;
+                    if ((st = build_patterns(regularFaceSize, uniformRate, o.fs, o.pq, p, s,
+                                             who)) != GB300_OK) {
+                        cudaFree(p.mem);
+                        return st;
+                    }
+                    g_patterns.emplace_back(key, p);
+                    g_patBytes += p.bytes;
+                    use = &g_patterns.back().second;
+                }
+            }
+            if (use) {
+                for (int k = 0; k <= kNumShared; ++k) a.patC[k] = use->patC[k], a.patF[k] = use->patF[k];
+                const size_t cb = sizeof(float) * 2 * (size_t)use->patC[kNumShared];
+                a.patCoords = (const float *)use->mem;
+                a.patFacets = (const int *)((const char *)use->mem + ((cb + 15) & ~size_t(15)));
+            }
         }
-        const size_t cb = sizeof(float) * 2 * (size_t)a.patC[kNumShared];
-        const size_t fb = sizeof(int) * (size_t)o.fs * a.patF[kNumShared];
-        if ((st = scratch_alloc(&pat, cb + fb + 16, s, who)) != GB300_OK) return st;
-        a.patCoords = (float *)pat;
-        a.patFacets = (int *)((char *)pat + ((cb + 15) & ~size_t(15)));
+        if (!use) {
+            pattern_sizes(regularFaceSize, uniformRate, o.fs, o.pq, scratchPat);
+            if ((st = scratch_alloc(&scratchPat.mem, scratchPat.bytes, s, who)) != GB300_OK)
+                return st;
+            if ((st = build_patterns(regularFaceSize, uniformRate, o.fs, o.pq, scratchPat, s,
+                                     who)) != GB300_OK) {
+                scratch_free(scratchPat.mem, s);
+                return st;
+            }
+            for (int k = 0; k <= kNumShared; ++k)
+                a.patC[k] = scratchPat.patC[k], a.patF[k] = scratchPat.patF[k];
+            const size_t cb = sizeof(float) * 2 * (size_t)scratchPat.patC[kNumShared];
+            a.patCoords = (const float *)scratchPat.mem;
+            a.patFacets = (const int *)((const char *)scratchPat.mem + ((cb + 15) & ~size_t(15)));
+        }
     }
-    k_tess_generate<<<grid_for((a.shared ? kNumShared : 0) + (long long)numFaces, 128, 16), 128,
-                      0, s>>>(a);
-    count_launch();
-    st = check_launch(who);
-    if (st == GB300_OK && (a.shared || a.locate || a.offsetIndices)) {
-        k_tess_finish<<<grid_for((long long)numFaces * 32, 256, 8), 256, 0, s>>>(a);
+
+    // faces without a shared pattern (per-face rates, polygons above 10 sides)
+    {
+        k_tess_generate<<<grid_for(numFaces, 128, 16), 128, 0, s>>>(a);
         count_launch();
         st = check_launch(who);
     }
-    if (pat) scratch_free(pat, s);
+    if (st == GB300_OK && (a.shared || a.locate)) {
+        const int blocks = grid_for((long long)numFaces * 32, 256, 8);
+        if (o.fs == 4)
+            k_tess_finish<4><<<blocks, 256, 0, s>>>(a);
+        else
+            k_tess_finish<3><<<blocks, 256, 0, s>>>(a);
+        count_launch();
+        st = check_launch(who);
+    }
+    if (scratchPat.mem) scratch_free(scratchPat.mem, s);
     return st;
 }

@@ -9,7 +9,10 @@
 #include <opensubdiv/far/patchTable.h>
 #include <opensubdiv/far/stencilTable.h>
 #include <opensubdiv/osd/mesh.h>
+#include <opensubdiv/bfr/refinerSurfaceFactory.h>
+#include <opensubdiv/bfr/tessellation.h>
 #include <opensubdiv_gb300/osd/gb300Evaluator.h>
+#include <opensubdiv_gb300/bfr/gb300Tessellation.h>
 
 using namespace OpenSubdiv;
 
@@ -64,6 +67,28 @@ bool LimitSurface(Far::PatchTable const *farPatches, Osd::GB300VertexBuffer *src
               Osd::GB300Evaluator::EvalPatchesFaceVarying(
                   fvarSrc, uv, fvarOut[0], uv, fvarOut[1], uv, fvarOut[2], uv, fvarOut[3], uv,
                   fvarOut[4], uv, fvarOut[5], uv, numCoords, coords, table, 0);
+    delete table;
+    return ok;
+}
+
+// The Bfr tutorials' loop (tutorials/bfr/tutorial_1_2/bfr_tutorial_1_2.cpp:155-238) with the
+// per-face Bfr::Tessellation replaced by one device tessellation of the mesh: the client's own
+// Bfr::Tessellation::Options carry over, the face sizes come from its refiner, and the Far table
+// pairs with Bfr::SurfaceFactory's approximation (as the reference's Bfr regression builds it).
+bool tessellateLikeTheTutorial(Far::TopologyRefiner const &mesh, Far::PatchTable const *farTable,
+                               int const *deviceFaceSizes, int tessUniformRate,
+                               bool tessQuadsFlag, float *coords, int *facets,
+                               PatchCoordBuffer *coordsOut) {
+    Bfr::Tessellation::Options tessOptions;
+    tessOptions.SetFacetSize(3 + tessQuadsFlag);
+    tessOptions.PreserveQuads(tessQuadsFlag);
+    const int regularFaceSize = Sdc::SchemeTypeTraits::GetRegularFaceSize(mesh.GetSchemeType());
+    Osd::GB300PatchTable *table = Osd::GB300PatchTable::Create(farTable);
+    Bfr::GB300MeshTessellation *tess = Bfr::GB300MeshTessellation::Create(
+        regularFaceSize, mesh.GetLevel(0).GetNumFaces(), deviceFaceSizes, tessUniformRate,
+        Bfr::GB300MeshTessellation::Options(tessOptions));
+    const bool ok = table && tess && tess->Generate(coords, facets, true, table, coordsOut->d);
+    delete tess;
     delete table;
     return ok;
 }

@@ -181,3 +181,45 @@ def test_client_compiles_against_the_reference_far_headers(tmp_path):
                             f"-L{cuda}/lib64", "-lcudart", "-fopenmp"],
                            capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_bfr_client_header_compiles_standalone():
+    src = os.path.join(ROOT, "tests", "cpp", "bfr_client.cpp")
+    cuda = _cuda_home()
+    r = subprocess.run(["g++", "-std=c++14", "-fsyntax-only", f"-I{ROOT}/include",
+                        f"-I{cuda}/include", src], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["bfr_catmark_nonquads_e_f4q.npz", "bfr_torus16x8_e_f3.npz",
+                                  "bfr_loop_xord_boundary_u5_f3.npz"])
+def test_cpp_bfr_client_tessellates_like_bfr(tmp_path, name):
+    """The Bfr tutorials' tessellate-and-evaluate loop from C++ through
+    include/opensubdiv_gb300/bfr/gb300Tessellation.h and the evaluator header: coords and facets
+    equal the reference's Bfr::Tessellation, PatchCoords its Far::PatchMap, and P..Dvv are within
+    the reference's Bfr-versus-Far tolerances of Bfr::Surface::Evaluate."""
+    import torch
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    z = np.load(os.path.join(GOLDEN, name))
+    for k in ("verts_per_face", "rate_offsets", "rates", "arrays", "patch_indices", "params",
+              "src"):
+        np.ascontiguousarray(z[k]).tofile(tmp_path / f"{k}.bin")
+    np.array([int(z["regular_face_size"]), int(z["facet_size"]), int(z["preserve_quads"]),
+              int(z["triangular"])], np.int32).tofile(tmp_path / "options.bin")
+    exe = _build(tmp_path, "bfr_client")
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    n = len(z["coords"])
+    coords = np.fromfile(tmp_path / "coords.bin", np.float32).reshape(n, 2)
+    assert np.array_equal(coords.view(np.int32), z["coords"].view(np.int32))
+    facets = np.fromfile(tmp_path / "facets.bin", np.int32).reshape(z["facets"].shape)
+    assert np.array_equal(facets, z["facets"])
+    pc = np.fromfile(tmp_path / "patch_coords.bin", np.int32).reshape(n, 5)
+    assert np.array_equal(pc[:, :3], z["q_handles"])
+    p = z["positions"].astype(np.float64)
+    ptol = 5e-5 * float((p.max(0) - p.min(0)).max())
+    for k, tol in enumerate((ptol, 5 * ptol, 5 * ptol, 25 * ptol, 25 * ptol, 25 * ptol)):
+        out = np.fromfile(tmp_path / f"p{k}.bin", np.float32).reshape(n, 3)
+        assert np.abs(out.astype(np.float64) - z["out6"][k]).max() <= tol, k
