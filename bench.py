@@ -254,7 +254,8 @@ def bench_bfr(args, stream, peak):
     the reference's Bfr tutorials run face by face, tutorials/bfr/tutorial_1_2 and 2_1):
     GB300TessellationCount + GB300TessellationGenerate (coords, triangle facets with mesh-wide
     indices, PatchCoords located on the Far table of Bfr::SurfaceFactory's default
-    approximation) + GB300PatchTableEval of P, Du and Dv.  Two rate schemes: the tutorials'
+    approximation) + GB300TessellationEvaluate of P, Du and Dv (and, for comparison, the same
+    points through the general GB300PatchTableEval).  Two rate schemes: the tutorials'
     uniform rate 5, and per-edge rates from control-hull edge lengths (tutorial 2.1)."""
     import torch
 
@@ -301,6 +302,9 @@ def bench_bfr(args, stream, peak):
             m.Generate(coords, facets, True, table, pc)
 
         def ev():
+            m.Evaluate(src, d, table, pc, 1, outs)
+
+        def ev_table():
             assert Ev.EvalPatchesTable(src, d, outs[0], d, n, pc, table, du=outs[1], duDesc=d,
                                        dv=outs[2], dvDesc=d, stream=stream)
 
@@ -320,6 +324,16 @@ def bench_bfr(args, stream, peak):
         torch.cuda.synchronize()
         gen_ms = float(np.mean([e[0].elapsed_time(e[1]) for e in evs]))
         eval_ms = float(np.mean([e[1].elapsed_time(e[2]) for e in evs]))
+        # the same points through the general EvalPatches entry (element-lane kernel)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(stream):
+            ev_table()
+            e0.record(stream)
+            for _ in range(args.steps):
+                ev_table()
+            e1.record(stream)
+        torch.cuda.synchronize()
+        eval_table_ms = e0.elapsed_time(e1) / args.steps
         # Count waits for its totals: timed on the host
         t0 = time.perf_counter()
         for _ in range(args.steps):
@@ -345,8 +359,7 @@ def bench_bfr(args, stream, peak):
                 mm = bfr.MeshTessellation(4, dsz, options=bfr.TessellationOptions(3),
                                           stream=stream, **mk)
                 mm.Generate(coords, facets, True, table, pc)
-                assert Ev.EvalPatchesTable(src, d, outs[0], d, n, pc, table, du=outs[1],
-                                           duDesc=d, dv=outs[2], dvDesc=d, stream=stream)
+                mm.Evaluate(src, d, table, pc, 1, outs)
                 for a, b in zip(h_out, outs):
                     a.copy_(b, non_blocking=True)
                 h_coords.copy_(coords, non_blocking=True)
@@ -409,6 +422,7 @@ def bench_bfr(args, stream, peak):
             "rates": rate_desc, "coords": n, "facets": nf,
             "points_per_s": n / ((gen_ms + eval_ms) / 1e3),
             "tessellate_ms": gen_ms, "eval_ms": eval_ms, "count_ms_host": count_ms,
+            "eval_ms_general_entry": eval_table_ms,
             "e2e": {"points_per_s": n / (e2e_ms / 1e3), "ms": e2e_ms, "h2d_bytes": h2d,
                     "d2h_bytes": d2h,
                     "what": "host face sizes (and rates) in; Count, Generate, Eval; P/Du/Dv, "
@@ -419,7 +433,7 @@ def bench_bfr(args, stream, peak):
                                     "unit": "GB/s",
                                     "frac": facet_b / (gen_ms / 1e3) / 1e9 / peak,
                                     "traffic": ncu_traffic("bfr_" + mode)},
-            "roofline_eval": {"bound": "hbm", "kernel": "k_eval_patches_lanes (P, Du, Dv)",
+            "roofline_eval": {"bound": "hbm", "kernel": "k_eval_patches<3, 1> (P, Du, Dv; GB300TessellationEvaluate)",
                               "algorithmic_bytes": eval_b,
                               "achieved": eval_b / (eval_ms / 1e3) / 1e9, "peak": peak,
                               "unit": "GB/s", "frac": eval_b / (eval_ms / 1e3) / 1e9 / peak},

@@ -130,6 +130,20 @@ public:
                    stream) == GB300_OK;
     }
 
+    /// Bfr::Surface::Evaluate at every coord (GB300TessellationEvaluate): P and any of Du, Dv,
+    /// Duu, Duv, Dvv (NULL to skip) of `length`-wide points from the patch points `src`, at the
+    /// PatchCoords Generate located on `table`; DEVICE buffers, outputs `length` floats apart.
+    bool Evaluate(Osd::GB300PatchTable const *table, Osd::PatchCoord const *patchCoords,
+                  float const *src, int length, int srcStride, float *P, float *Du = NULL,
+                  float *Dv = NULL, float *Duu = NULL, float *Duv = NULL, float *Dvv = NULL,
+                  void *stream = NULL) const {
+        return table && GB300TessellationEvaluate(table->GetHandle(), src, P, Du, Dv, Duu, Duv,
+                                                  Dvv, length, srcStride, length, length,
+                                                  length, length, length, length,
+                                                  GetNumCoords(), patchCoords,
+                                                  stream) == GB300_OK;
+    }
+
 private:
     GB300MeshTessellation() {}
 

@@ -328,6 +328,18 @@ int GB300TessellationGenerate(int regularFaceSize, int numFaces, const int *face
                               int offsetFacetIndices, const GB300PatchTable *table,
                               void *patchCoords, void *stream);
 
+/* Bfr::Surface::Evaluate (bfr/surface.h:227-242) at every coord of a mesh tessellation: P and
+ * any of Du, Dv, Duu, Duv, Dvv (NULL to skip) of `length`-wide points at the PatchCoords that
+ * GB300TessellationGenerate located on `table`.  The same arithmetic as GB300PatchTableEval,
+ * with the kernel chosen for coords grouped by patch, as a tessellation's are (one point per
+ * thread: the warp shares each patch's row loads and every point's basis is computed once).
+ * DEVICE pointers; strides in floats. */
+int GB300TessellationEvaluate(const GB300PatchTable *table, const float *src, float *P,
+                              float *Du, float *Dv, float *Duu, float *Duv, float *Dvv,
+                              int length, int srcStride, int pStride, int duStride, int dvStride,
+                              int duuStride, int duvStride, int dvvStride, int numCoords,
+                              const void *patchCoords, void *stream);
+
 /* ---- vertex buffer (CudaVertexBuffer, osd/cudaVertexBuffer.h:42-79) ---------------------- */
 
 typedef struct GB300VertexBuffer GB300VertexBuffer;

@@ -24,7 +24,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import GB300Error, check, last_error  # noqa: F401
-from .evaluator import BufferDescriptor, GB300Evaluator, _ptr, _stream
+from .evaluator import _ptr, _stream
 
 # Bfr::Limits::MaxFaceSize (bfr/limits.h:43) and the short range of rates (tessellation.cpp:2091)
 MAX_FACE_SIZE = 65535
@@ -178,24 +178,21 @@ class MeshTessellation:
             _ptr(patch_coords) if table is not None else None, _stream(self.stream)))
         return coords, facets, patch_coords
 
-    def Evaluate(self, src, src_desc, table, patch_coords, derivatives=1):
-        """Limit points at every coord (Bfr::Surface::Evaluate): P, and with derivatives >= 1
-        Du, Dv, with 2 also Duu, Duv, Dvv; each [num_coords, length] float32."""
+    def Evaluate(self, src, src_desc, table, patch_coords, derivatives=1, outputs=None):
+        """Limit points at every coord (Bfr::Surface::Evaluate, GB300TessellationEvaluate): P,
+        and with derivatives >= 1 Du, Dv, with 2 also Duu, Duv, Dvv; each [num_coords, length]
+        float32 (allocated unless `outputs` gives them)."""
         torch = _torch()
         n = self.num_coords
         L = src_desc.length
         k = 1 if derivatives == 0 else 3 if derivatives == 1 else 6
-        outs = [torch.zeros((n, L), dtype=torch.float32, device="cuda") for _ in range(k)]
-        d = BufferDescriptor(0, L, L)
-        kw = {}
-        names = ["du", "dv", "duu", "duv", "dvv"]
-        for i in range(1, k):
-            kw[names[i - 1]] = outs[i]
-            kw[names[i - 1] + "Desc"] = d
-        if not GB300Evaluator.EvalPatchesTable(src, src_desc, outs[0], d, n, patch_coords, table,
-                                               stream=self.stream, **kw):
-            raise GB300Error(1, last_error())
-        return outs
+        outs = outputs if outputs is not None else [
+            torch.zeros((n, L), dtype=torch.float32, device="cuda") for _ in range(k)]
+        ptrs = [_ptr(outs[i]) if i < k else None for i in range(6)]
+        check(_lib.load().GB300TessellationEvaluate(
+            table.handle, _ptr(src, src_desc.offset), *ptrs, L, src_desc.stride, *([L] * 6), n,
+            _ptr(patch_coords), _stream(self.stream)))
+        return outs[:k]
 
 
 class Tessellation:

@@ -513,6 +513,19 @@ int GB300PatchTableEval(const GB300PatchTable *t, const float *src, float *dst, 
                         "GB300PatchTableEval", t->quadFamily);
 }
 
+int GB300TessellationEvaluate(const GB300PatchTable *t, const float *src, float *P, float *du,
+                              float *dv, float *duu, float *duv, float *dvv, int length,
+                              int srcStride, int pStride, int duStride, int dvStride,
+                              int duuStride, int duvStride, int dvvStride, int numCoords,
+                              const void *patchCoords, void *stream) {
+    if (!t) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300TessellationEvaluate: null table");
+    float *d[6] = {P, du, dv, duu, duv, dvv};
+    const int st[6] = {pStride, duStride, dvStride, duuStride, duvStride, dvvStride};
+    return eval_patches(src, d, st, length, srcStride, numCoords, patchCoords, t->arrays,
+                        (const int *)t->indices, t->params, as_stream(stream),
+                        "GB300TessellationEvaluate", t->quadFamily, 1);
+}
+
 int GB300PatchTableSetVarying(GB300PatchTable *t, int numArrays, const void *patchArrays,
                               int64_t numIndices, const int *patchIndices, void *stream) {
     PatchSet set;

@@ -52,9 +52,13 @@ struct PatchArgs {
     const ParamRec *params;
 };
 
+// Highest output index a derivative order needs: 0 P only, 1 P + du + dv, 2 all six.  The
+// kernels are instantiated per order so the unused accumulations compile away.
+__host__ __device__ constexpr int last_output(int order) { return order == 0 ? 0 : order == 1 ? 2 : 5; }
+
 // 5 resident blocks per SM where the registers allow it without spills (0.2847 vs 0.2908 ms
 // for 4 M Loop points at LC = 3; LC = 4 would spill)
-template <int LC>
+template <int LC, int ORDER>
 __global__ void __launch_bounds__(128, LC == 4 ? 4 : 5) k_eval_patches(const PatchArgs a) {
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.numCoords; i += stride) {
@@ -76,7 +80,7 @@ __global__ void __launch_bounds__(128, LC == 4 ? 4 : 5) k_eval_patches(const Pat
             }
             const float scale[6] = {1.0f, d1, d1, d2, d2, d2};
 #pragma unroll
-            for (int k = 0; k < 6; ++k) {
+            for (int k = 0; k <= last_output(ORDER); ++k) {
                 if (!(a.active & (1 << k))) continue;
                 float *out = a.dst[k] + (size_t)i * a.dstStride[k] + e0;
 #pragma unroll
@@ -91,7 +95,7 @@ __global__ void __launch_bounds__(128, LC == 4 ? 4 : 5) k_eval_patches(const Pat
 // single coalesced access for the whole group, the accumulators are per element (6 per
 // lane) and no cross-lane reduction is needed.  The basis is evaluated by every lane of the
 // group (cheap for the separable quad-family bases this kernel is used for).
-template <int G>
+template <int G, int ORDER>
 __global__ void __launch_bounds__(256, 4) k_eval_patches_lanes(const PatchArgs a) {
     // G need not be a power of two: a warp holds floor(32 / G) groups (3 lanes per point
     // for xyz: 10 points per warp) and its remaining lanes stay idle
@@ -125,7 +129,7 @@ __global__ void __launch_bounds__(256, 4) k_eval_patches_lanes(const PatchArgs a
             if (e < a.length) {
                 const float scale[6] = {1.0f, d1, d1, d2, d2, d2};
 #pragma unroll
-                for (int k = 0; k < 6; ++k)
+                for (int k = 0; k <= last_output(ORDER); ++k)
                     if (a.active & (1 << k))
                         st_stream(a.dst[k] + (size_t)i * a.dstStride[k] + e, acc.v[k][0] * scale[k]);
             }
@@ -133,10 +137,33 @@ __global__ void __launch_bounds__(256, 4) k_eval_patches_lanes(const PatchArgs a
     }
 }
 
+template <int ORDER>
+void launch_lanes(int G, int grid, int threads, cudaStream_t s, const PatchArgs &a) {
+    switch (G) {
+        case 1: k_eval_patches_lanes<1, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 2: k_eval_patches_lanes<2, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 3: k_eval_patches_lanes<3, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 4: k_eval_patches_lanes<4, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 6: k_eval_patches_lanes<6, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 8: k_eval_patches_lanes<8, ORDER><<<grid, threads, 0, s>>>(a); break;
+        default: k_eval_patches_lanes<32, ORDER><<<grid, threads, 0, s>>>(a); break;
+    }
+}
+
+template <int ORDER>
+void launch_points(int length, int grid, int threads, cudaStream_t s, const PatchArgs &a) {
+    switch (length) {
+        case 1: k_eval_patches<1, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 2: k_eval_patches<2, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 3: k_eval_patches<3, ORDER><<<grid, threads, 0, s>>>(a); break;
+        default: k_eval_patches<4, ORDER><<<grid, threads, 0, s>>>(a); break;
+    }
+}
+
 int eval_patches(const float *src, float *const *dst, const int *strides, int length,
                  int srcStride, int numCoords, const void *coords, const void *arrays,
                  const int *indices, const void *params, cudaStream_t s, const char *who,
-                 int quadFamily) {
+                 int quadFamily, int grouped) {
     if (numCoords <= 0) return ok();
     if (!src || !coords || !arrays || !indices || !params)
         return fail(GB300_ERR_INVALID_ARGUMENT, "%s: null source, coord or table pointer", who);
@@ -162,7 +189,8 @@ int eval_patches(const float *src, float *const *dst, const int *strides, int le
         a.active |= 1 << k;
     }
     if (!a.active) return ok();
-    if (quadFamily) {
+    const int order = (a.active & 0x38) ? 2 : (a.active & 0x6) ? 1 : 0;
+    if (quadFamily && !grouped) {
         // element-lane kernel: G = length lanes per point for the common widths, else 32
         // lanes looping over element chunks
         const int G = (length <= 4 || length == 6 || length == 8) ? length : 32;
@@ -172,28 +200,22 @@ int eval_patches(const float *src, float *const *dst, const int *strides, int le
         long long blocks = (warps * 32 + threads - 1) / threads;
         long long cap = (long long)num_sms() * 16;
         const int grid = (int)(blocks < cap ? blocks : cap);
-        switch (G) {
-            case 1: k_eval_patches_lanes<1><<<grid, threads, 0, s>>>(a); break;
-            case 2: k_eval_patches_lanes<2><<<grid, threads, 0, s>>>(a); break;
-            case 3: k_eval_patches_lanes<3><<<grid, threads, 0, s>>>(a); break;
-            case 4: k_eval_patches_lanes<4><<<grid, threads, 0, s>>>(a); break;
-            case 6: k_eval_patches_lanes<6><<<grid, threads, 0, s>>>(a); break;
-            case 8: k_eval_patches_lanes<8><<<grid, threads, 0, s>>>(a); break;
-            default: k_eval_patches_lanes<32><<<grid, threads, 0, s>>>(a); break;
-        }
+        if (order == 0) launch_lanes<0>(G, grid, threads, s, a);
+        else if (order == 1) launch_lanes<1>(G, grid, threads, s, a);
+        else launch_lanes<2>(G, grid, threads, s, a);
         count_launch();
         return check_launch(who);
     }
+    // one thread per point: tables with triangle patches, and points grouped by patch (a
+    // tessellation's coords), whose row loads are shared by the warp and whose basis each
+    // thread then computes once rather than once per element lane
     const int threads = 128;
     long long blocks = ((long long)numCoords + threads - 1) / threads;
     long long cap = (long long)num_sms() * 32;
     const int grid = (int)(blocks < cap ? blocks : cap);
-    switch (length) {
-        case 1: k_eval_patches<1><<<grid, threads, 0, s>>>(a); break;
-        case 2: k_eval_patches<2><<<grid, threads, 0, s>>>(a); break;
-        case 3: k_eval_patches<3><<<grid, threads, 0, s>>>(a); break;
-        default: k_eval_patches<4><<<grid, threads, 0, s>>>(a); break;
-    }
+    if (order == 0) launch_points<0>(length, grid, threads, s, a);
+    else if (order == 1) launch_points<1>(length, grid, threads, s, a);
+    else launch_points<2>(length, grid, threads, s, a);
     count_launch();
     return check_launch(who);
 }
@@ -211,7 +233,7 @@ int GB300EvalPatches(const float *src, float *dst, int length, int srcStride, in
     float *d[6] = {dst, 0, 0, 0, 0, 0};
     int st[6] = {dstStride, 0, 0, 0, 0, 0};
     return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, patchArrays,
-                        patchIndices, patchParams, as_stream(stream), "GB300EvalPatches", 0);
+                        patchIndices, patchParams, as_stream(stream), "GB300EvalPatches", 0, 0);
 }
 
 int GB300EvalPatchesWithDerivatives(
@@ -223,7 +245,7 @@ int GB300EvalPatchesWithDerivatives(
     int st[6] = {dstStride, duStride, dvStride, duuStride, duvStride, dvvStride};
     return eval_patches(src, d, st, length, srcStride, numPatchCoords, patchCoords, patchArrays,
                         patchIndices, patchParams, as_stream(stream),
-                        "GB300EvalPatchesWithDerivatives", 0);
+                        "GB300EvalPatchesWithDerivatives", 0, 0);
 }
 
 }  // extern "C"

@@ -44,9 +44,11 @@ int eval_stencils(const float *src, float *const *dst, const int *strides,
 
 // quadFamily: every patch array holds only REGULAR / GREGORY_BASIS / QUADS patches, which
 // selects the element-lane kernel (known for device tables; raw-pointer calls pass 0).
+// grouped: consecutive coords mostly share a patch (a tessellation's coords), which selects
+// the one-thread-per-point kernel for every table.
 int eval_patches(const float *src, float *const *dst, const int *strides, int length,
                  int srcStride, int numCoords, const void *coords, const void *arrays,
                  const int *indices, const void *params, cudaStream_t s, const char *who,
-                 int quadFamily);
+                 int quadFamily, int grouped = 0);
 
 }  // namespace gb300

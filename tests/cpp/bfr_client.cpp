@@ -1,10 +1,11 @@
 // A C++ client of the Bfr-shaped header: the tessellate-and-evaluate loop of the reference's
 // Bfr tutorials (tutorials/bfr/tutorial_1_2/bfr_tutorial_1_2.cpp:170-238) for every face of a
 // mesh at once -- GB300MeshTessellation (per-face rates, mesh-wide facet indices, PatchCoords on
-// a device patch table) and GB300Evaluator::EvalPatches (P and all five derivatives).
+// a device patch table), its Evaluate (Surface::Evaluate: P and all five derivatives), and the
+// same coords through GB300Evaluator::EvalPatches (P, Du, Dv).
 //
 // usage: bfr_client <dir>  (reads *.bin written by the test; writes coords.bin, facets.bin,
-//                           patch_coords.bin, p{k}.bin for k = 0..5)
+//                           patch_coords.bin, p{k}.bin for k = 0..5, g{k}.bin for k = 0..2)
 #include <opensubdiv_gb300/bfr/gb300Tessellation.h>
 
 #include <cuda_runtime.h>
@@ -87,9 +88,19 @@ int main(int argc, char **argv) {
     vsrc->UpdateData(src.data(), 0, nsrc);
     Osd::GB300VertexBuffer *p[6];
     for (int k = 0; k < 6; ++k) p[k] = Osd::GB300VertexBuffer::Create(3, n);
+    // Surface::Evaluate at every coord (P and all five derivatives), and P, Du, Dv of the same
+    // coords through the evaluator header's EvalPatches into a second set of buffers
+    if (!tess->Evaluate(table, pc.d, vsrc->BindCudaBuffer(), 3, 3, p[0]->BindCudaBuffer(),
+                        p[1]->BindCudaBuffer(), p[2]->BindCudaBuffer(), p[3]->BindCudaBuffer(),
+                        p[4]->BindCudaBuffer(), p[5]->BindCudaBuffer())) {
+        std::fprintf(stderr, "Evaluate failed: %s\n", GB300GetLastErrorString());
+        return 1;
+    }
+    Osd::GB300VertexBuffer *g[3];
+    for (int k = 0; k < 3; ++k) g[k] = Osd::GB300VertexBuffer::Create(3, n);
     Osd::BufferDescriptor d3(0, 3, 3);
-    if (!Osd::GB300Evaluator::EvalPatches(vsrc, d3, p[0], d3, p[1], d3, p[2], d3, p[3], d3,
-                                          p[4], d3, p[5], d3, n, &pc, table)) {
+    if (!Osd::GB300Evaluator::EvalPatches(vsrc, d3, g[0], d3, g[1], d3, g[2], d3, n, &pc,
+                                          table)) {
         std::fprintf(stderr, "EvalPatches failed: %s\n", GB300GetLastErrorString());
         return 1;
     }
@@ -99,6 +110,10 @@ int main(int argc, char **argv) {
     write(dir + "/patch_coords.bin", reinterpret_cast<int *>(pc.d), 5 * (size_t)n);
     for (int k = 0; k < 6; ++k)
         write(dir + "/p" + std::to_string(k) + ".bin", p[k]->BindCudaBuffer(), 3 * (size_t)n);
+    for (int k = 0; k < 3; ++k) {
+        write(dir + "/g" + std::to_string(k) + ".bin", g[k]->BindCudaBuffer(), 3 * (size_t)n);
+        delete g[k];
+    }
     delete tess;
     delete table;
     for (auto *b : p) delete b;

@@ -223,3 +223,6 @@ def test_cpp_bfr_client_tessellates_like_bfr(tmp_path, name):
     for k, tol in enumerate((ptol, 5 * ptol, 5 * ptol, 25 * ptol, 25 * ptol, 25 * ptol)):
         out = np.fromfile(tmp_path / f"p{k}.bin", np.float32).reshape(n, 3)
         assert np.abs(out.astype(np.float64) - z["out6"][k]).max() <= tol, k
+        if k < 3:  # the general EvalPatches entry on the same coords
+            g = np.fromfile(tmp_path / f"g{k}.bin", np.float32).reshape(n, 3)
+            assert np.abs(g.astype(np.float64) - z["out6"][k]).max() <= tol, k
