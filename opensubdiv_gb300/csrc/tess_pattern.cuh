@@ -490,15 +490,16 @@ struct Face {
         return n;
     }
 
-    GB_HD int boundary_coords(const Sink &o) const {
+    template <int K>
+    GB_HD int boundary_coords_k(const Sink &o) const {
         int n = 0;
-        if (kind == kQuad) {
+        if constexpr (K == kQuad) {
             const int r0 = outer(0), r1 = outer(1), r2 = outer(2), r3 = outer(3);
             n += o.run_u(n, r0, 0.0f, 0.0f, frcp(r0));
             n += o.run_v(n, r1, 1.0f, 0.0f, frcp(r1));
             n += o.run_u(n, r2, 1.0f, 1.0f, -frcp(r2));
             n += o.run_v(n, r3, 0.0f, 1.0f, -frcp(r3));
-        } else if (kind == kTri) {
+        } else if constexpr (K == kTri) {
             const int r0 = outer(0), r1 = outer(1), r2 = outer(2);
             n += o.run_u(n, r0, 0.0f, 0.0f, frcp(r0));
             n += o.run_uv(n, r1, 1.0f, 0.0f, -frcp(r1), frcp(r1));
@@ -512,15 +513,16 @@ struct Face {
         return n;
     }
 
-    GB_HD int interior_coords(const Sink &o, int at) const {
+    template <int K>
+    GB_HD int interior_coords_k(const Sink &o, int at) const {
         if (nInterior == 0) return 0;
         if (nInterior == 1) {
-            const float c = (kind == kTri) ? 1.0f / 3.0f : 0.5f;
+            const float c = (K == kTri) ? 1.0f / 3.0f : 0.5f;
             o.uv(at, c, c);
             return 1;
         }
         int n = 0;
-        if (kind == kQuad) {
+        if constexpr (K == kQuad) {
             const int rings = imin(in0 / 2, in1 / 2);
             const float du = frcp(in0), dv = frcp(in1);
             float u = du, v = dv;
@@ -540,7 +542,7 @@ struct Face {
                     o.uv(at + n++, 0.5f, 0.5f);
                 }
             }
-        } else if (kind == kTri) {
+        } else if constexpr (K == kTri) {
             const int rings = in0 / 3;
             const float dt = frcp(in0);
             float u = dt, v = dt;
@@ -578,9 +580,16 @@ struct Face {
         return n;
     }
 
+    // Generation for a face of parameterization kind K (compiled per kind, so a kernel that
+    // handles one kind carries only that kind's code); coords() / facets() dispatch on `kind`.
+    template <int K>
+    GB_HD int coords_k(const Sink &o) const {
+        const int n = boundary_coords_k<K>(o);
+        return n + interior_coords_k<K>(o, n);
+    }
     GB_HD int coords(const Sink &o) const {
-        const int n = boundary_coords(o);
-        return n + interior_coords(o, n);
+        return kind == kQuad ? coords_k<kQuad>(o) : kind == kTri ? coords_k<kTri>(o)
+                                                                 : coords_k<kQsub>(o);
     }
 
     // ---- facets (Tessellation::GetFacets, tessellation.cpp:2370-2426) ----------------------
@@ -786,13 +795,14 @@ struct Face {
         return n;
     }
 
-    GB_HD int facets(const Sink &o) const {
+    template <int K>
+    GB_HD int facets_k(const Sink &o) const {
         const int tri = triangulate;
         if (mode == kSingle) return (N == 3) ? o.tri(0, 0, 1, 2) : o.quad(0, 0, 1, 2, 3, 0);
         if (mode == kFan) return o.fan(0, nFacets, 0);
         if (mode == kSplitQuad) return o.quad(0, 0, 1, 2, 3, tri);
         int n = 0;
-        if (kind == kQuad) {
+        if constexpr (K == kQuad) {
             if (uniform) {
                 int c0 = 0, res = in0;
                 for (int ring = 0; ring < (in0 + 1) / 2; ++ring, res -= 2) {
@@ -812,7 +822,7 @@ struct Face {
                     c0 += 2 * (ur + vr);
                 }
             }
-        } else if (kind == kTri) {
+        } else if constexpr (K == kTri) {
             int res = in0;
             if (uniform) {
                 int c0 = 0;
@@ -853,6 +863,10 @@ struct Face {
             }
         }
         return n;
+    }
+    GB_HD int facets(const Sink &o) const {
+        return kind == kQuad ? facets_k<kQuad>(o) : kind == kTri ? facets_k<kTri>(o)
+                                                                 : facets_k<kQsub>(o);
     }
 };
 

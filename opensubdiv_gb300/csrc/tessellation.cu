@@ -150,12 +150,15 @@ __device__ __forceinline__ void locate_coord(const GenArgs &a, int N, int ptex0,
 }
 
 // One thread per face without a shared pattern: the face's coords and facets (indices already
-// offset to the mesh numbering) straight into its slice of the output.
+// offset to the mesh numbering) straight into its slice of the output.  One launch per
+// parameterization kind K present in the scheme, each generating only that kind's faces.
+template <int K>
 __global__ void __launch_bounds__(128, 8) k_tess_generate(const GenArgs a) {
     const int stride = gridDim.x * blockDim.x;
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
         const int N = a.faceSizes[f];
-        if (uses_shared(a, N)) continue;
+        const int kind = N == a.reg ? (a.reg == 4 ? tess::kQuad : tess::kTri) : tess::kQsub;
+        if (kind != K || uses_shared(a, N)) continue;
         FaceRates r;
         rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
         Face face;
@@ -163,8 +166,8 @@ __global__ void __launch_bounds__(128, 8) k_tess_generate(const GenArgs a) {
         const int64_t c0 = a.co[f];
         Sink o{a.coords + c0 * a.coordStride, a.coordStride, a.facets + a.fo[f] * a.facetStride,
                a.fs, a.facetStride, a.offsetIndices ? (int)c0 : 0, a.coordPairs != 0};
-        face.coords(o);
-        face.facets(o);
+        face.coords_k<K>(o);
+        face.facets_k<K>(o);
     }
 }
 
@@ -470,8 +473,22 @@ extern "C" int GB300TessellationGenerate(
 
     // faces without a shared pattern (per-face rates, polygons above 10 sides)
     {
-        k_tess_generate<<<grid_for(numFaces, 128, 16), 128, 0, s>>>(a);
-        count_launch();
+        // with shared patterns only polygons above 10 sides are generated per face: none for
+        // a triangle scheme, only quad sub-face polygons for a quad scheme
+        const int grid = grid_for(numFaces, 128, 16);
+        if (regularFaceSize == 3) {
+            if (!a.shared) {
+                k_tess_generate<tess::kTri><<<grid, 128, 0, s>>>(a);
+                count_launch();
+            }
+        } else {
+            if (!a.shared) {
+                k_tess_generate<tess::kQuad><<<grid, 128, 0, s>>>(a);
+                count_launch();
+            }
+            k_tess_generate<tess::kQsub><<<grid, 128, 0, s>>>(a);
+            count_launch();
+        }
         st = check_launch(who);
     }
     if (st == GB300_OK && (a.shared || a.locate)) {
