@@ -105,6 +105,14 @@ struct GenArgs {
     int locate;
     PatchMapView map;
     int *patchCoords;  // 5 x 32 bit per coord
+    // per-face rates: faces with the same size and rates share one pattern, generated by the
+    // lowest-numbered of them (the owner) and copied from its output slice by the others;
+    // faceSlot[f] is the face's hash slot (-1: generated on its own), owners[slot] the owner
+    int dedupe;
+    unsigned long long *keys;
+    int *owners;
+    int *faceSlot;
+    unsigned int slotMask;
 };
 
 __device__ __forceinline__ bool uses_shared(const GenArgs &a, int N) {
@@ -149,6 +157,64 @@ __device__ __forceinline__ void locate_coord(const GenArgs &a, int N, int ptex0,
     o[4] = __float_as_int(t);
 }
 
+constexpr unsigned long long kEmptyKey = ~0ull;
+
+// The face's (size, rates) as one 64-bit key: triangles and quads with at most 6 rates below
+// 1024 (1 bit size, 3 bits rate count, 10 bits per rate; a count of 7 never occurs, so the
+// all-ones empty key cannot either).  Other faces are not shared.
+__device__ __forceinline__ bool pattern_key(int N, const FaceRates &r, unsigned long long &key) {
+    if (N < 3 || N > 4 || r.n < 1 || r.n > 6) return false;
+    unsigned long long k = (unsigned long long)(N - 3) | ((unsigned long long)r.n << 1);
+    for (int i = 0; i < r.n; ++i) {
+        const int v = r.p ? r.p[i] : r.one;
+        if (v < 0 || v > 1023) return false;
+        k |= (unsigned long long)v << (4 + 10 * i);
+    }
+    key = k;
+    return true;
+}
+
+__device__ __forceinline__ unsigned int key_hash(unsigned long long k) {
+    k ^= k >> 33;
+    k *= 0xff51afd7ed558ccdull;
+    k ^= k >> 33;
+    k *= 0xc4ceb9fe1a85ec53ull;
+    k ^= k >> 33;
+    return (unsigned int)k;
+}
+
+// One thread per face: the face's slot in an open-addressing table of keys (capacity at least
+// twice the faces, so a free slot is always found), and the lowest face index per key.
+__global__ void __launch_bounds__(256) k_tess_dedupe(const GenArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
+        FaceRates r;
+        rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
+        unsigned long long key;
+        int slot = -1;
+        if (pattern_key(a.faceSizes[f], r, key)) {
+            unsigned int h = key_hash(key) & a.slotMask;
+            for (unsigned int probe = 0; probe <= a.slotMask; ++probe) {
+                const unsigned long long prev = atomicCAS(a.keys + h, kEmptyKey, key);
+                if (prev == kEmptyKey || prev == key) {
+                    atomicMin(a.owners + h, f);
+                    slot = (int)h;
+                    break;
+                }
+                h = (h + 1) & a.slotMask;
+            }
+        }
+        a.faceSlot[f] = slot;
+    }
+}
+
+// The face whose output slice holds face f's pattern (f itself unless a lower face shares it).
+__device__ __forceinline__ int owner_of(const GenArgs &a, int f) {
+    if (!a.dedupe) return f;
+    const int slot = a.faceSlot[f];
+    return slot < 0 ? f : a.owners[slot];
+}
+
 // One thread per face without a shared pattern: the face's coords and facets (indices already
 // offset to the mesh numbering) straight into its slice of the output.  One launch per
 // parameterization kind K present in the scheme, each generating only that kind's faces.
@@ -158,7 +224,7 @@ __global__ void __launch_bounds__(128, 8) k_tess_generate(const GenArgs a) {
     for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
         const int N = a.faceSizes[f];
         const int kind = N == a.reg ? (a.reg == 4 ? tess::kQuad : tess::kTri) : tess::kQsub;
-        if (kind != K || uses_shared(a, N)) continue;
+        if (kind != K || uses_shared(a, N) || owner_of(a, f) != f) continue;
         FaceRates r;
         rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
         Face face;
@@ -183,10 +249,44 @@ __global__ void __launch_bounds__(256) k_tess_finish(const GenArgs a) {
         if (nc == 0) continue;
         const int N = a.faceSizes[f];
         const bool sh = uses_shared(a, N);
-        if (!sh && !a.locate) continue;
+        const int own = sh ? f : owner_of(a, f);
+        if (!sh && own == f && !a.locate) continue;
         const int k = N - kFirstShared;
         const int ptex0 = a.locate ? (int)a.po[f] : 0;
-        if (sh) {
+        if (!sh && own != f) {
+            // a copy of the owner's slice: same coords, facet indices moved by the difference
+            // of the two faces' first coords
+            const int64_t s0 = a.co[own];
+            for (int i = lane; i < nc; i += 32) {
+                const float *c = a.coords + (s0 + i) * a.coordStride;
+                float *d = a.coords + (c0 + i) * a.coordStride;
+                float u, v;
+                if (a.coordPairs) {
+                    const float2 uv = *reinterpret_cast<const float2 *>(c);
+                    *reinterpret_cast<float2 *>(d) = uv;
+                    u = uv.x;
+                    v = uv.y;
+                } else {
+                    u = c[0];
+                    v = c[1];
+                    d[0] = u;
+                    d[1] = v;
+                }
+                if (a.locate) locate_coord(a, N, ptex0, u, v, a.patchCoords + 5 * (c0 + i));
+            }
+            const int64_t f0 = a.fo[f], g0 = a.fo[own];
+            const int nf = (int)(a.fo[f + 1] - f0);
+            const int delta = a.offsetIndices ? (int)(c0 - s0) : 0;
+            for (int q = lane; q < nf; q += 32) {
+                const int *src = a.facets + (g0 + q) * a.facetStride;
+                int *d = a.facets + (f0 + q) * a.facetStride;
+#pragma unroll
+                for (int c = 0; c < FS; ++c) {
+                    const int v = src[c];
+                    d[c] = v >= 0 ? v + delta : v;
+                }
+            }
+        } else if (sh) {
             const float2 *pc = reinterpret_cast<const float2 *>(a.patCoords) + a.patC[k];
             for (int i = lane; i < nc; i += 32) {
                 const float2 uv = pc[i];
@@ -472,7 +572,30 @@ extern "C" int GB300TessellationGenerate(
     }
 
     // faces without a shared pattern (per-face rates, polygons above 10 sides)
-    {
+    void *dd = nullptr;
+    a.dedupe = 0;
+    if (!a.shared && st == GB300_OK) {
+        unsigned int cap = 1024;
+        while (cap < 2u * (unsigned int)numFaces && cap < (1u << 30)) cap <<= 1;
+        const size_t kb = sizeof(unsigned long long) * cap, ob = sizeof(int) * cap;
+        const size_t fb = sizeof(int) * (size_t)numFaces;
+        st = scratch_alloc(&dd, kb + ob + fb, s, who);
+        if (st == GB300_OK) {
+            a.keys = (unsigned long long *)dd;
+            a.owners = (int *)((char *)dd + kb);
+            a.faceSlot = (int *)((char *)dd + kb + ob);
+            a.slotMask = cap - 1;
+            st = check_cuda(cudaMemsetAsync(a.keys, 0xff, kb, s), who);
+            if (st == GB300_OK) st = check_cuda(cudaMemsetAsync(a.owners, 0x7f, ob, s), who);
+        }
+        if (st == GB300_OK) {
+            k_tess_dedupe<<<grid_for(numFaces, 256, 8), 256, 0, s>>>(a);
+            count_launch();
+            st = check_launch(who);
+            a.dedupe = 1;
+        }
+    }
+    if (st == GB300_OK) {
         // with shared patterns only polygons above 10 sides are generated per face: none for
         // a triangle scheme, only quad sub-face polygons for a quad scheme
         const int grid = grid_for(numFaces, 128, 16);
@@ -491,7 +614,7 @@ extern "C" int GB300TessellationGenerate(
         }
         st = check_launch(who);
     }
-    if (st == GB300_OK && (a.shared || a.locate)) {
+    if (st == GB300_OK && (a.shared || a.locate || a.dedupe)) {
         const int blocks = grid_for((long long)numFaces * 32, 256, 8);
         if (o.fs == 4)
             k_tess_finish<4><<<blocks, 256, 0, s>>>(a);
@@ -500,6 +623,7 @@ extern "C" int GB300TessellationGenerate(
         count_launch();
         st = check_launch(who);
     }
+    if (dd) scratch_free(dd, s);
     if (scratchPat.mem) scratch_free(scratchPat.mem, s);
     return st;
 }

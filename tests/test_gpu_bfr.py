@@ -172,3 +172,47 @@ def test_mesh_tessellate_and_evaluate_matches_bfr(path):
         err = np.abs(outs[k].astype(np.float64) - z["out6"][k]).max()
         assert err <= tol[k], (name, k, err, tol[k])
         gate(f"bfr {name}", k, outs[k].ravel(), cpu[k], f64[k], diag)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("reg,fs,pq,offset,strides", [(4, 3, 0, True, (0, 0)),
+                                                      (4, 4, 1, False, (3, 6)),
+                                                      (3, 4, 0, True, (0, 5))])
+def test_per_face_rates_with_repeated_tuples(reg, fs, pq, offset, strides):
+    """Per-face rate runs drawn from a small set, so most faces share their (size, rates) with
+    others: one face per tuple generates the pattern, the rest copy it from that face's output
+    slice (indices moved to their own coords).  Every face against the oracle."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import bfr
+    rng = np.random.default_rng(77 + reg + fs)
+    nfaces = 3000
+    pool = [3, 4, 4, 4, 5, 6, 11] if reg == 4 else [3, 3, 3, 4]
+    sizes = rng.choice(pool, nfaces).astype(np.int32)
+    runs = []
+    for N in sizes:
+        kind = rng.integers(0, 3)
+        if kind == 0:
+            runs.append(rng.integers(1, 4, 1))
+        elif kind == 1:
+            runs.append(rng.integers(2, 5, N))
+        else:
+            runs.append(rng.integers(2, 4, N + 1))
+    r_off = np.concatenate([[0], np.cumsum([len(r) for r in runs])]).astype(np.int32)
+    rates = np.concatenate(runs).astype(np.int32)
+    cs, fst = strides
+    opt = bfr.TessellationOptions(fs, pq, coord_stride=cs, facet_stride=fst)
+    m = bfr.MeshTessellation(reg, sizes, rates=rates, rate_offsets=r_off, options=opt)
+    c, f, _ = m.Generate(offset_facet_indices=offset)
+    c, f = host(c), host(f)
+    co, fo = host(m.coord_offsets), host(m.facet_offsets)
+    for j in range(nfaces):
+        want = oracle.tess_generate(reg, int(sizes[j]), rates[r_off[j]:r_off[j + 1]], fs, pq)
+        if want is None:
+            assert co[j + 1] == co[j]
+            continue
+        wc, wf = want
+        assert np.array_equal(bits(c[co[j]:co[j + 1], :2]), bits(wc)), j
+        got = f[fo[j]:fo[j + 1], :wf.shape[1]]
+        if offset:
+            got = np.where(got >= 0, got - co[j], -1)
+        assert np.array_equal(got, wf), j
