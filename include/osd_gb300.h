@@ -340,6 +340,43 @@ int GB300TessellationEvaluate(const GB300PatchTable *table, const float *src, fl
                               int duuStride, int duvStride, int dvvStride, int numCoords,
                               const void *patchCoords, void *stream);
 
+/* ---- draw-time tessellation factors (osd/glslPatchCommonTess.glsl:92-760) ------------------ */
+
+/* The tess-control settings of OpenSubdiv's patch shaders.  tessLevel: OsdTessLevel();
+ * maxTessLevel: the device maximum the shaders read as gl_MaxTessGenLevel (64 on current
+ * hardware); screenSpace: OSD_ENABLE_SCREENSPACE_TESSELLATION; spacing: 0 equal,
+ * 1 fractional even, 2 fractional odd (OSD_FRACTIONAL_EVEN/ODD_SPACING); modelView,
+ * projection: OsdModelViewMatrix() / OsdProjectionMatrix(), column-major like a GLSL mat4. */
+typedef struct GB300PatchTessOptions {
+    float tessLevel;
+    float maxTessLevel;
+    int screenSpace;
+    int spacing;
+    float modelView[16];
+    float projection[16];
+} GB300PatchTessOptions;
+
+/* Per-patch tessellation factors for every patch of a device table, as the tess-control stage
+ * of the patch shaders computes them: uniform (OsdGetTessLevelsUniform[Triangle], from the
+ * refinement level and transition mask) or screen-space (OsdComputeTessLevel of each boundary
+ * edge, and of each half of a transition edge, between limit positions at the patch's corners
+ * and edge midpoints), then outer and inner levels for the spacing (OsdComputeTessLevels
+ * [Triangle]).  src: the patch points (xyz at srcStride floats; only read for screen-space
+ * factors).  DEVICE outputs per patch, in patch-param order: outer[4] (16-byte aligned),
+ * inner[2], and optionally the Lo / Hi halves of the outer levels (tessOuterLo / tessOuterHi,
+ * 16-byte aligned) that GB300PatchTessParameterization needs. */
+int GB300PatchTableTessFactors(const GB300PatchTable *table, const float *src, int srcStride,
+                               const GB300PatchTessOptions *options, float *outer, float *inner,
+                               float *outerLo, float *outerHi, void *stream);
+
+/* OsdGetTessParameterization[Triangle] (glslPatchCommonTess.glsl:692-730): maps n tessellator
+ * domain points (u, v, w; w unused for quads) of patches patchIndex[i] to patch coordinates,
+ * placing the points of split transition edges on their two halves.  DEVICE arrays; uv gets 2
+ * floats per point. */
+int GB300PatchTessParameterization(int n, const float *domain, const int *patchIndex,
+                                   const float *outerLo, const float *outerHi, int spacing,
+                                   int triangular, float *uv, void *stream);
+
 /* ---- vertex buffer (CudaVertexBuffer, osd/cudaVertexBuffer.h:42-79) ---------------------- */
 
 typedef struct GB300VertexBuffer GB300VertexBuffer;

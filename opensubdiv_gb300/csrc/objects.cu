@@ -526,6 +526,15 @@ int GB300TessellationEvaluate(const GB300PatchTable *t, const float *src, float 
                         "GB300TessellationEvaluate", t->quadFamily, 1);
 }
 
+int GB300PatchTableTessFactors(const GB300PatchTable *t, const float *src, int srcStride,
+                               const GB300PatchTessOptions *options, float *outer, float *inner,
+                               float *outerLo, float *outerHi, void *stream) {
+    if (!t) return fail(GB300_ERR_INVALID_ARGUMENT, "GB300PatchTableTessFactors: null table");
+    return tess_factors(t->arrays, t->numArrays, (const int *)t->indices, t->params,
+                        t->numPatches, src, srcStride, options, outer, inner, outerLo, outerHi,
+                        as_stream(stream));
+}
+
 int GB300PatchTableSetVarying(GB300PatchTable *t, int numArrays, const void *patchArrays,
                               int64_t numIndices, const int *patchIndices, void *stream) {
     PatchSet set;

@@ -51,4 +51,10 @@ int eval_patches(const float *src, float *const *dst, const int *strides, int le
                  const int *indices, const void *params, cudaStream_t s, const char *who,
                  int quadFamily, int grouped = 0);
 
+// Draw-time tessellation factors of every patch of a table (tess_factors.cu).
+int tess_factors(const void *arrays, int numArrays, const int *indices, const void *params,
+                 int numPatches, const float *src, int srcStride,
+                 const GB300PatchTessOptions *o, float *outer, float *inner, float *outerLo,
+                 float *outerHi, cudaStream_t s);
+
 }  // namespace gb300

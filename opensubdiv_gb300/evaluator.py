@@ -462,10 +462,52 @@ class GB300PatchTable:
     def GetFVarPatchParamBuffer(self, channel=0):
         return _lib.load().GB300PatchTableGetFVarBuffer(self.handle, channel, 2)
 
+    def TessFactors(self, options, outer, inner, outer_lo=None, outer_hi=None, src=None,
+                    src_stride=3, stream=None):
+        """Draw-time tessellation factors of every patch (GB300PatchTableTessFactors):
+        outer [numPatches, 4], inner [numPatches, 2] and optionally the Lo / Hi outer halves
+        [numPatches, 4]; `options` is a PatchTessOptions."""
+        import ctypes as C
+        check(_lib.load().GB300PatchTableTessFactors(
+            self.handle, _ptr(src), int(src_stride), C.byref(options), _ptr(outer), _ptr(inner),
+            _ptr(outer_lo), _ptr(outer_hi), _stream(stream)))
+
     def FindPatches(self, n, faces, u, v, coords_out, stream=None):
         """Device PatchMap lookup: writes n OsdPatchCoord records to coords_out."""
         check(_lib.load().GB300PatchTableFindPatches(self.handle, n, _ptr(faces), _ptr(u),
                                                      _ptr(v), _ptr(coords_out), _stream(stream)))
+
+
+class PatchTessOptions(C.Structure):
+    """The patch shaders' tess-control settings (OsdTessLevel, the device maximum level,
+    screen-space tessellation, spacing 0 equal / 1 fractional even / 2 fractional odd, and the
+    model-view and projection matrices as 4x4 arrays in the usual row-major math layout; they
+    are stored column-major like a GLSL mat4)."""
+
+    _fields_ = [("tessLevel", C.c_float), ("maxTessLevel", C.c_float),
+                ("screenSpace", C.c_int), ("spacing", C.c_int),
+                ("modelView", C.c_float * 16), ("projection", C.c_float * 16)]
+
+    def __init__(self, tess_level=1.0, max_tess_level=64.0, screen_space=False, spacing=0,
+                 model_view=None, projection=None):
+        super().__init__()
+        self.tessLevel = float(tess_level)
+        self.maxTessLevel = float(max_tess_level)
+        self.screenSpace = int(bool(screen_space))
+        self.spacing = int(spacing)
+        mv = np.asarray(model_view if model_view is not None else np.eye(4), np.float32)
+        pr = np.asarray(projection if projection is not None else np.eye(4), np.float32)
+        self.modelView[:] = mv.T.ravel().tolist()
+        self.projection[:] = pr.T.ravel().tolist()
+
+
+def PatchTessParameterization(n, domain, patch_index, outer_lo, outer_hi, uv, spacing=0,
+                              triangular=False, stream=None):
+    """OsdGetTessParameterization[Triangle] on the device (GB300PatchTessParameterization):
+    n domain points (u, v, w) of patches patch_index -> patch (u, v) in uv."""
+    check(_lib.load().GB300PatchTessParameterization(
+        int(n), _ptr(domain), _ptr(patch_index), _ptr(outer_lo), _ptr(outer_hi), int(spacing),
+        int(bool(triangular)), _ptr(uv), _stream(stream)))
 
 
 class GB300VertexBuffer:

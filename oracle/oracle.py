@@ -294,3 +294,38 @@ def tess_locate_mesh(reg_face_size, face_sizes, coord_offsets, ptex_offsets, coo
                                       _p(st), C.c_int(threads)):
         raise ValueError("invalid parameterization in the mesh")
     return faces, st
+
+
+# ---- draw-time tessellation factors (tess_factors_oracle.c) --------------------------------
+
+def tess_factors(arrays, indices, params, src, src_stride, tess_level, max_tess_level=64.0,
+                 screen_space=False, spacing=0, model_view=None, projection=None):
+    """Per-patch (outer [n, 4], inner [n, 2], lo [n, 4], hi [n, 4]) of the patch shaders'
+    tess-control math (osd/glslPatchCommonTess.glsl:92-550)."""
+    arrays = np.ascontiguousarray(arrays, np.int32)
+    indices = np.ascontiguousarray(indices, np.int32)
+    params = np.ascontiguousarray(params, np.int32)
+    n = len(params)
+    mv = np.ascontiguousarray(model_view if model_view is not None else np.eye(4), np.float32)
+    pr = np.ascontiguousarray(projection if projection is not None else np.eye(4), np.float32)
+    outs = [np.zeros((n, 4), np.float32), np.zeros((n, 2), np.float32),
+            np.zeros((n, 4), np.float32), np.zeros((n, 4), np.float32)]
+    srcp = np.ascontiguousarray(src, np.float32) if src is not None else None
+    lib().orc_tess_factors(_p(arrays), C.c_int(len(arrays)), _p(indices), _p(params), C.c_int(n),
+                           _p(srcp), C.c_int(src_stride), C.c_float(tess_level),
+                           C.c_float(max_tess_level), C.c_int(int(screen_space)),
+                           C.c_int(spacing), _p(mv.T.copy()), _p(pr.T.copy()),
+                           *[_p(o) for o in outs])
+    return tuple(outs)
+
+
+def tess_parameterization(domain, patch_index, lo, hi, spacing=0, triangular=False):
+    """OsdGetTessParameterization[Triangle]: patch (u, v) [n, 2] of domain points [n, 3]."""
+    domain = np.ascontiguousarray(domain, np.float32).reshape(-1, 3)
+    patch_index = np.ascontiguousarray(patch_index, np.int32)
+    uv = np.zeros((len(domain), 2), np.float32)
+    lib().orc_tess_parameterization(C.c_int(len(domain)), _p(domain), _p(patch_index),
+                                    _p(np.ascontiguousarray(lo, np.float32)),
+                                    _p(np.ascontiguousarray(hi, np.float32)), C.c_int(spacing),
+                                    C.c_int(int(triangular)), _p(uv))
+    return uv

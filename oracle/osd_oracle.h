@@ -131,6 +131,21 @@ int orc_tess_locate_mesh(int regFaceSize, int numFaces, const int *faceSizes,
                          const long *coordOffsets, const long *ptexOffsets, const float *coords,
                          int *ptexFaces, float *st, int threads);
 
+/* ---- draw-time tessellation factors (tess_factors_oracle.c) ---- */
+
+/* Per-patch tess levels of the patch shaders (osd/glslPatchCommonTess.glsl:92-550): outer[4],
+ * inner[2], and the Lo / Hi outer halves (4 each) per patch in param order; arrays are the
+ * flattened PatchArray (6 ints), params 3 ints per patch, matrices column-major. */
+int orc_tess_factors(const int *arrays, int numArrays, const int *indices, const int *params,
+                     int numPatches, const float *src, int srcStride, float tessLevel,
+                     float maxTessLevel, int screenSpace, int spacing, const float *mv,
+                     const float *proj, float *outer, float *inner, float *outLo, float *outHi);
+
+/* OsdGetTessParameterization[Triangle] (osd/glslPatchCommonTess.glsl:692-730) */
+int orc_tess_parameterization(int n, const float *domain, const int *patchIndex,
+                              const float *outerLo, const float *outerHi, int spacing,
+                              int triangular, float *uv);
+
 #ifdef __cplusplus
 }
 #endif
