@@ -446,6 +446,40 @@ def bench_bfr(args, stream, peak):
         }
         del m, coords, facets, pc, outs
         release_memory()
+
+    # draw-time tessellation factors of every patch of the table (screen-space, camera framing
+    # the torus, fractional-odd spacing): the patch shaders' tess-control math
+    from opensubdiv_gb300.evaluator import PatchTessOptions
+    npatch = int(len(z["params"]))
+    p = np.asarray(z["positions"], np.float64)
+    c, r = 0.5 * (p.min(0) + p.max(0)), float(np.linalg.norm(p.max(0) - p.min(0)))
+    eye = c + np.array([0.3, 0.4, 1.0]) * r
+    f = (c - eye) / np.linalg.norm(c - eye)
+    sx = np.cross(f, [0.0, 1.0, 0.0])
+    sx /= np.linalg.norm(sx)
+    ux = np.cross(sx, f)
+    mv = np.eye(4)
+    mv[0, :3], mv[1, :3], mv[2, :3] = sx, ux, -f
+    mv[:3, 3] = -mv[:3, :3] @ eye
+    near, far = 0.01 * r, 10.0 * r
+    pr = np.zeros((4, 4))
+    pr[0, 0] = pr[1, 1] = 1.0 / np.tan(np.radians(22.5))
+    pr[2, 2], pr[2, 3], pr[3, 2] = (far + near) / (near - far), 2 * far * near / (near - far), -1
+    to = PatchTessOptions(24.0, 64.0, True, 2, mv, pr)
+    tf = [torch.empty((npatch, 4), device="cuda"), torch.empty((npatch, 2), device="cuda"),
+          torch.empty((npatch, 4), device="cuda"), torch.empty((npatch, 4), device="cuda")]
+    for _ in range(args.warmup):
+        table.TessFactors(to, *tf, src=src, stream=stream)
+    t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(stream):
+        t0.record(stream)
+        for _ in range(args.steps):
+            table.TessFactors(to, *tf, src=src, stream=stream)
+        t1.record(stream)
+    torch.cuda.synchronize()
+    tf_ms = t0.elapsed_time(t1) / args.steps
+    out["tess_factors"] = {"patches": npatch, "ms": tf_ms, "patches_per_s": npatch / (tf_ms / 1e3),
+                           "mode": "screen-space, fractional-odd spacing, tess level 24"}
     return out
 
 

@@ -245,6 +245,17 @@ public:
         return gb300_detail::ok(GB300PatchTableFindPatches(
             _h, n, faces, u, v, coordsOut, gb300_detail::stream_of(deviceContext)));
     }
+    /// Draw-time tessellation factors of every patch (GB300PatchTableTessFactors): the
+    /// tess-control math of the patch shaders (osd/glslPatchCommonTess.glsl), per patch in
+    /// param order, into DEVICE arrays of 4 (outer, 16-byte aligned) and 2 (inner) floats.
+    bool TessFactors(GB300PatchTessOptions const &options, float const *src, int srcStride,
+                     float *outer, float *inner, float *outerLo = NULL, float *outerHi = NULL,
+                     void *deviceContext = NULL) const {
+        return gb300_detail::ok(GB300PatchTableTessFactors(
+            _h, src, srcStride, &options, outer, inner, outerLo, outerHi,
+            gb300_detail::stream_of(deviceContext)));
+    }
+
     ::GB300PatchTable *GetHandle() const { return _h; }
 
 private:

@@ -59,7 +59,8 @@ __host__ __device__ constexpr int last_output(int order) { return order == 0 ? 0
 // 5 resident blocks per SM where the registers allow it without spills (0.2847 vs 0.2908 ms
 // for 4 M Loop points at LC = 3; LC = 4 would spill)
 template <int LC, int ORDER>
-__global__ void __launch_bounds__(128, LC == 4 ? 4 : 5) k_eval_patches(const PatchArgs a) {
+__global__ void __launch_bounds__(128, LC == 4 ? 4 : (ORDER < 2 ? 6 : 5))
+    k_eval_patches(const PatchArgs a) {
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.numCoords; i += stride) {
         const Coord c = load_coord(a.coords + i);

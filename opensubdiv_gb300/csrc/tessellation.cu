@@ -185,14 +185,27 @@ __device__ __forceinline__ unsigned int key_hash(unsigned long long k) {
 
 // One thread per face: the face's slot in an open-addressing table of keys (capacity at least
 // twice the faces, so a free slot is always found), and the lowest face index per key.
+// Neighbouring faces often share a key, so the lanes of a warp with the same key insert once,
+// through their lowest lane (the lowest face of the group).
 __global__ void __launch_bounds__(256) k_tess_dedupe(const GenArgs a) {
     const int stride = gridDim.x * blockDim.x;
-    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
-        FaceRates r;
-        rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
-        unsigned long long key;
+    const int lane = threadIdx.x & 31;
+    // every lane runs the same number of iterations, so the warp stays converged
+    const int rounds = (a.numFaces + stride - 1) / stride;
+    for (int it = 0; it < rounds; ++it) {
+        const int f = it * stride + blockIdx.x * blockDim.x + threadIdx.x;
+        unsigned long long key = kEmptyKey;
+        bool keyed = false;
+        if (f < a.numFaces) {
+            FaceRates r;
+            rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
+            keyed = pattern_key(a.faceSizes[f], r, key);
+        }
+        const unsigned keyedMask = __ballot_sync(0xffffffffu, keyed);
+        const unsigned same = __match_any_sync(0xffffffffu, key) & keyedMask;
+        const int leader = same ? __ffs(same) - 1 : lane;
         int slot = -1;
-        if (pattern_key(a.faceSizes[f], r, key)) {
+        if (keyed && leader == lane) {
             unsigned int h = key_hash(key) & a.slotMask;
             for (unsigned int probe = 0; probe <= a.slotMask; ++probe) {
                 const unsigned long long prev = atomicCAS(a.keys + h, kEmptyKey, key);
@@ -204,7 +217,8 @@ __global__ void __launch_bounds__(256) k_tess_dedupe(const GenArgs a) {
                 h = (h + 1) & a.slotMask;
             }
         }
-        a.faceSlot[f] = slot;
+        slot = __shfl_sync(0xffffffffu, slot, leader);
+        if (f < a.numFaces) a.faceSlot[f] = keyed ? slot : -1;
     }
 }
 

@@ -91,7 +91,8 @@ def test_screen_space_factors(name, spacing):
     got = run_gpu(z, opts, z["src"])
     want = oracle.tess_factors(z["arrays"], z["patch_indices"], z["params"], z["src"], 3, 24.0,
                                64.0, True, spacing, mv, pr)
-    assert (want[0] > 0).all()
+    edges = 3 if int(z["triangular"]) else 4
+    assert (want[0][:, :edges] >= 1).all()
     # fractional spacings keep the unrounded halves: compare them directly
     if spacing != 0:
         for g, w in zip(got[2:], want[2:]):
