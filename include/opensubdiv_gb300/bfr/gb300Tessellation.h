@@ -25,6 +25,8 @@
 #if __has_include(<opensubdiv/bfr/tessellation.h>)
 #define OSD_GB300_HAVE_BFR 1
 #include <opensubdiv/bfr/tessellation.h>
+#include <opensubdiv/far/patchTableFactory.h>
+#include <opensubdiv/far/topologyRefiner.h>
 #endif
 #endif
 
@@ -177,6 +179,29 @@ private:
     int64_t *_offsets = NULL;
     int64_t _totals[3] = {0, 0, 0};
 };
+
+#ifdef OSD_GB300_HAVE_BFR
+/// The Far patch table whose patches are the surfaces Bfr::SurfaceFactory builds with the given
+/// approximation levels (its defaults: 6 for sharp and 2 for smooth features), with the options
+/// the reference's Bfr regression pairs with them (regression/bfr_evaluate/
+/// farPatchEvaluator.cpp:52-78): adaptive refinement of `refiner` to those levels, Gregory-basis
+/// end caps, infinitely sharp patches, no shared end-cap points, no legacy corner patches.
+/// The refiner is refined adaptively in place; the caller owns the returned table.
+inline Far::PatchTable const *GB300CreateSurfacePatchTable(Far::TopologyRefiner &refiner,
+                                                            int approxLevelSharp = 6,
+                                                            int approxLevelSmooth = 2) {
+    Far::PatchTableFactory::Options po(approxLevelSharp);
+    po.useInfSharpPatch = true;
+    po.generateLegacySharpCornerPatches = false;
+    po.shareEndCapPatchPoints = false;
+    po.endCapType = Far::PatchTableFactory::Options::ENDCAP_GREGORY_BASIS;
+    Far::TopologyRefiner::AdaptiveOptions ro = po.GetRefineAdaptiveOptions();
+    ro.SetIsolationLevel(approxLevelSharp);
+    ro.SetSecondaryLevel(approxLevelSmooth);
+    refiner.RefineAdaptive(ro);
+    return Far::PatchTableFactory::Create(refiner, po);
+}
+#endif
 
 OSD_GB300_BFR_NAMESPACE_END
 

@@ -75,10 +75,10 @@ bool LimitSurface(Far::PatchTable const *farPatches, Osd::GB300VertexBuffer *src
 // per-face Bfr::Tessellation replaced by one device tessellation of the mesh: the client's own
 // Bfr::Tessellation::Options carry over, the face sizes come from its refiner, and the Far table
 // pairs with Bfr::SurfaceFactory's approximation (as the reference's Bfr regression builds it).
-bool tessellateLikeTheTutorial(Far::TopologyRefiner const &mesh, Far::PatchTable const *farTable,
-                               int const *deviceFaceSizes, int tessUniformRate,
-                               bool tessQuadsFlag, float *coords, int *facets,
-                               PatchCoordBuffer *coordsOut) {
+bool tessellateLikeTheTutorial(Far::TopologyRefiner &mesh, int const *deviceFaceSizes,
+                               int tessUniformRate, bool tessQuadsFlag, float *coords,
+                               int *facets, PatchCoordBuffer *coordsOut) {
+    Far::PatchTable const *farTable = Bfr::GB300CreateSurfacePatchTable(mesh);
     Bfr::Tessellation::Options tessOptions;
     tessOptions.SetFacetSize(3 + tessQuadsFlag);
     tessOptions.PreserveQuads(tessQuadsFlag);
@@ -90,6 +90,7 @@ bool tessellateLikeTheTutorial(Far::TopologyRefiner const &mesh, Far::PatchTable
     const bool ok = table && tess && tess->Generate(coords, facets, true, table, coordsOut->d);
     delete tess;
     delete table;
+    delete farTable;
     return ok;
 }
 
