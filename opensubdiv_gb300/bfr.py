@@ -195,6 +195,25 @@ class MeshTessellation:
         return outs[:k]
 
 
+    def EvaluateFaceVarying(self, src, src_desc, table, patch_coords, channel=0, derivatives=0,
+                            outputs=None):
+        """Face-varying values at every coord (the face-varying surfaces of
+        Bfr::SurfaceFactory::InitFaceVaryingSurface): channel `channel` of `table` evaluated at
+        the coords' PatchCoords (GB300PatchTableEvalFaceVarying); value, and with
+        derivatives >= 1 d/du and d/dv, each [num_coords, length] float32."""
+        torch = _torch()
+        n = self.num_coords
+        L = src_desc.length
+        k = 1 if derivatives == 0 else 3
+        outs = outputs if outputs is not None else [
+            torch.zeros((n, L), dtype=torch.float32, device="cuda") for _ in range(k)]
+        ptrs = [_ptr(outs[i]) if i < k else None for i in range(6)]
+        check(_lib.load().GB300PatchTableEvalFaceVarying(
+            table.handle, int(channel), _ptr(src, src_desc.offset), *ptrs, L, src_desc.stride,
+            *([L] * 6), n, _ptr(patch_coords), _stream(self.stream)))
+        return outs[:k]
+
+
 class Tessellation:
     """Bfr::Tessellation of one face (its pattern is computed on the device)."""
 

@@ -384,18 +384,21 @@ def bfr_subface(reg_face_size, face_size, uv):
 
 
 def bfr_mesh_record(refiner, positions, rate_offsets, rates, facet_size=3, preserve_quads=False,
-                    approx_sharp=6, approx_smooth=2):
+                    approx_sharp=6, approx_smooth=2, uvs=None):
     """Bfr tessellate-and-evaluate of every base face (the reference's tutorial loop):
     dict(coord_offsets, facet_offsets, valid, regular, coords, facets, f32 [6, n, 3],
-    f64 [6, n, 3])."""
+    f64 [6, n, 3]); with `uvs` (values of face-varying channel 0, [m, 2]) also uv [3, n, 2]:
+    UV, dUV/du, dUV/dv of the face-varying surfaces."""
     L = lib()
     L.ref_bfr_mesh_record.restype = C.c_void_p
     pos = np.ascontiguousarray(positions, np.float32)
     ro = np.ascontiguousarray(rate_offsets, np.int32)
     rt = np.ascontiguousarray(rates, np.int32)
+    uv = np.ascontiguousarray(uvs, np.float32) if uvs is not None else None
     h = C.c_void_p(L.ref_bfr_mesh_record(refiner.h, C.c_int(approx_sharp),
                                          C.c_int(approx_smooth), _p(pos), _p(ro), _p(rt),
-                                         C.c_int(facet_size), C.c_int(int(preserve_quads))))
+                                         C.c_int(facet_size), C.c_int(int(preserve_quads)),
+                                         _p(uv)))
     try:
         sizes = np.zeros(3, np.int64)
         L.ref_bfr_record_sizes(h, _p(sizes))
@@ -412,6 +415,10 @@ def bfr_mesh_record(refiner, positions, rate_offsets, rates, facet_size=3, prese
         L.ref_bfr_record_copy(h, _p(out["coord_offsets"]), _p(out["facet_offsets"]),
                               _p(out["valid"]), _p(out["regular"]), _p(out["coords"]),
                               _p(out["facets"]), pf, pd)
+        if uv is not None:
+            out["uv"] = np.zeros((3, nc, 2), np.float32)
+            pu = (C.c_void_p * 3)(*[out["uv"][k].ctypes.data for k in range(3)])
+            L.ref_bfr_record_uv(h, pu)
         return out
     finally:
         L.ref_bfr_record_destroy(h)

@@ -165,6 +165,11 @@ void ref_refine_adaptive(void *p, int isolation, int useSingleCrease, int useInf
 void ref_refine_adaptive_levels(void *p, int primary, int secondary, int useInfSharp) {
     Far::PatchTableFactory::Options po(primary);
     po.useInfSharpPatch = useInfSharp;
+    if (((Refiner *)p)->r->GetNumFVarChannels() > 0) {
+        // non-linear face-varying patches: isolate the face-varying topology too
+        po.generateFVarTables = true;
+        po.generateFVarLegacyLinearPatches = false;
+    }
     Far::TopologyRefiner::AdaptiveOptions ro = po.GetRefineAdaptiveOptions();
     ro.SetIsolationLevel(primary);
     ro.SetSecondaryLevel(secondary);
@@ -806,6 +811,7 @@ struct BfrRecord {
     std::vector<float> coords;
     std::vector<float> outF[6];
     std::vector<double> outD[6];
+    std::vector<float> uv[3];  // face-varying channel 0 (2 values): UV, dUV/du, dUV/dv
 };
 
 template <class REAL>
@@ -837,13 +843,17 @@ extern "C" {
 // Surface::Evaluate (P, Du, Dv, Duu, Duv, Dvv) at each coord in float and in double.
 // Faces without a limit surface get no coords.  Facet indices are offset to the mesh-wide
 // coord numbering (Tessellation::TransformFacetCoordIndices).
+// uvs: optional values (2 floats each) of face-varying channel 0, evaluated per coord through
+// SurfaceFactory::InitFaceVaryingSurface as the reference's tutorial 1.3 does
+// (tutorials/bfr/tutorial_1_3/bfr_tutorial_1_3.cpp).
 void *ref_bfr_mesh_record(void *refiner, int approxSharp, int approxSmooth, const float *pos,
                           const int *rateOffsets, const int *rates, int facetSize,
-                          int preserveQuads) {
+                          int preserveQuads, const float *uvs) {
     Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
     Bfr::SurfaceFactory::Options so;
     so.SetApproxLevelSharp(approxSharp);
     so.SetApproxLevelSmooth(approxSmooth);
+    if (uvs) so.SetDefaultFVarID(0);
     Bfr::RefinerSurfaceFactory<> factory(mesh, so);
     int nf = factory.GetNumFaces();
     int nverts = mesh.GetLevel(0).GetNumVertices();
@@ -881,6 +891,20 @@ void *ref_bfr_mesh_record(void *refiner, int approxSharp, int approxSmooth, cons
         }
         bfrEvalFace(sf, pf, pos, nverts, rec->coords, c0, n, rec->outF);
         bfrEvalFace(sd, pd, pos, nverts, rec->coords, c0, n, rec->outD);
+        if (uvs) {
+            Bfr::Surface<float> su;
+            for (int k = 0; k < 3; ++k) rec->uv[k].resize(2 * (c0 + n));
+            if (factory.InitFaceVaryingSurface(f, &su)) {
+                std::vector<float> patch((size_t)su.GetNumPatchPoints() * 2);
+                su.PreparePatchPoints(uvs, 2, patch.data(), 2);
+                for (size_t i = 0; i < n; ++i) {
+                    float r[3][2];
+                    su.Evaluate(&rec->coords[2 * (c0 + i)], patch.data(), 2, r[0], r[1], r[2]);
+                    for (int k = 0; k < 3; ++k)
+                        for (int e = 0; e < 2; ++e) rec->uv[k][2 * (c0 + i) + e] = r[k][e];
+                }
+            }
+        }
         rec->coordOffsets[f + 1] = (long)(c0 + n);
         rec->facetOffsets[f + 1] = (long)(f0 + t.GetNumFacets());
     }
@@ -944,6 +968,11 @@ void ref_bfr_record_sizes(void *p, long *sizes) {
 }
 
 // out6f / out6d: 6 arrays of 3 values per coord (P, Du, Dv, Duu, Duv, Dvv)
+void ref_bfr_record_uv(void *p, float **uv3) {
+    BfrRecord *r = (BfrRecord *)p;
+    for (int k = 0; k < 3; ++k) copyVec(r->uv[k], uv3[k]);
+}
+
 void ref_bfr_record_copy(void *p, long *coordOffsets, long *facetOffsets, int *valid,
                          int *regular, float *coords, int *facets, float **out6f, double **out6d) {
     BfrRecord *r = (BfrRecord *)p;

@@ -452,7 +452,7 @@ def edge_rates(cage, rng, lo=1, hi=7):
     return start.astype(np.int32), np.asarray(out, np.int32)
 
 
-def bfr_mesh_fixture(path, cage, mode, facet_size=3, preserve_quads=False, seed=0):
+def bfr_mesh_fixture(path, cage, mode, facet_size=3, preserve_quads=False, seed=0, fvar=None):
     """Bfr tessellate-and-evaluate of every face (the reference's tutorial loop through
     Bfr::RefinerSurfaceFactory with its default approximation levels, Surface::Evaluate in
     float and double), plus the Far patch table the reference's Bfr regression pairs with those
@@ -466,9 +466,10 @@ def bfr_mesh_fixture(path, cage, mode, facet_size=3, preserve_quads=False, seed=
         rates = np.full(nf, int(mode[1:]), np.int32)
     else:
         ro, rates = edge_rates(cage, rng)
-    rec = ref.bfr_mesh_record(ref.Refiner(cage), cage.positions, ro, rates, facet_size,
-                              preserve_quads)
-    r = ref.Refiner(cage).refine_adaptive_levels(6, 2, True)
+    rf = None if fvar is None else (fvar[0], fvar[1], False)
+    rec = ref.bfr_mesh_record(ref.Refiner(cage, fvar=rf), cage.positions, ro, rates, facet_size,
+                              preserve_quads, uvs=None if fvar is None else fvar[2])
+    r = ref.Refiner(cage, fvar=rf).refine_adaptive_levels(6, 2, True)
     p = ref.Patches(r, endcap=3, max_isolation=6, inf_sharp=True, share_endcap_points=False,
                     legacy_sharp_corners=False)
     nc = cage.num_vertices
@@ -501,6 +502,19 @@ def bfr_mesh_fixture(path, cage, mode, facet_size=3, preserve_quads=False, seed=
                regular=rec["regular"], coords=rec["coords"], facets=rec["facets"],
                out6=rec["f32"], out6_fp64=rec["f64"], q_face=qf, q_s=qs, q_t=qt,
                q_handles=handles, q_found=found)
+    if fvar is not None:
+        # face-varying channel 0: the Far table's fvar patches and their points (the channel's
+        # values, refined, then its local points), and Bfr's face-varying surfaces at the coords
+        fa, fi, fp = p.fvar(0)
+        fst = p.fvar_stencils(r, 0)
+        nv = fvar[0]
+        fbuf = np.zeros((nv + len(fst["sizes"])) * 2, np.float32)
+        fbuf[: nv * 2] = np.asarray(fvar[2], np.float32).ravel()
+        assert ref.cpu_eval_stencils(fbuf, (0, 2, 2), [fbuf], [(nv * 2, 2, 2)], fst["sizes"],
+                                     fst["offsets"], fst["indices"], [fst["weights"]], 0,
+                                     len(fst["sizes"]))
+        out.update(fvar_arrays=fa, fvar_indices=fi, fvar_params=fp, fvar_src=fbuf,
+                   uv_values=np.asarray(fvar[2], np.float32), uv3=rec["uv"])
     np.savez_compressed(path, **out)
 
 
@@ -521,6 +535,13 @@ def bfr_fixtures():
     bfr_mesh_fixture(os.path.join(HERE, "bfr_torus16x8_e_f3.npz"), tor, "e", 3, 0, seed=320)
     ico = shapes.icosphere(1, noise=0.005, seed=3)
     bfr_mesh_fixture(os.path.join(HERE, "bfr_icosphere1_u6_f3.npz"), ico, "u6", 3, 0, seed=321)
+    # face-varying UVs with seams (the reference's tutorial 1.3): Catmark with triangles, Loop
+    ftor = shapes.torus(12, 8, tri_fraction=0.1, crease_fraction=0.05, seed=31, noise=0.01)
+    bfr_mesh_fixture(os.path.join(HERE, "bfr_torus12x8_uv_e_f3.npz"), ftor, "e", 3, 0, seed=322,
+                     fvar=uv_seams(ftor, 12, 8) + (uv_grid(12, 8),))
+    fltor = shapes.torus(12, 8, seed=33, noise=0.01, scheme=shapes.LOOP)
+    bfr_mesh_fixture(os.path.join(HERE, "bfr_looptorus12x8_uv_u4_f3.npz"), fltor, "u4", 3, 0,
+                     seed=323, fvar=uv_seams(fltor, 12, 8) + (uv_grid(12, 8),))
 
 
 LARGE = os.path.join(HERE, "large")

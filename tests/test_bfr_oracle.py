@@ -94,6 +94,30 @@ def bfr_tolerances(positions):
     return (ptol, 5 * ptol, 5 * ptol, 25 * ptol, 25 * ptol, 25 * ptol)
 
 
+def rotated_triangles(z):
+    """Coords located on rotated triangle sub-patches.  Far::PatchTable::EvaluateBasis scales the
+    second derivatives there by -4^depth (far/patchBasis.cpp:1339-1366: d2Scale = derivSign *
+    d1Scale^2, derivSign = -1), where the parameter map s' = c - 2^depth s of a rotated triangle
+    gives +4^depth.  Bfr applies the same rule inside its own patch trees, but a face Bfr
+    evaluates as one regular surface has no sub-patches, so where Far's table splits such a face
+    (e.g. isolating face-varying seams) the two reference paths disagree in the sign of the
+    second derivatives.  The device reproduces Far (EvalPatches' contract)."""
+    prm = z["params"][z["q_handles"][:, 1]]
+    arr = z["arrays"][z["q_handles"][:, 0]]
+    regular = (prm[:, 1] >> 5) & 1
+    ptype = np.where(regular == 1, arr[:, 0], arr[:, 1])
+    depth = prm[:, 1] & 0xF
+    u, v = (prm[:, 1] >> 22) & 0x3FF, (prm[:, 1] >> 12) & 0x3FF
+    return np.isin(ptype, (4, 5, 10)) & ((u + v) >= (1 << depth))
+
+
+def second_derivative_error(far, bfr, flip):
+    """|far - bfr|, with the sign of Far's value taken back on the points in `flip`."""
+    far = np.array(far, np.float64)
+    far[flip] = -far[flip]
+    return np.abs(far - bfr)
+
+
 @pytest.mark.parametrize("path", MESHES, ids=os.path.basename)
 def test_far_table_evaluation_agrees_with_bfr_surfaces(path):
     """The Far table at the located coords (the oracle's EvalPatches, float) against
@@ -105,9 +129,16 @@ def test_far_table_evaluation_agrees_with_bfr_surfaces(path):
     assert oracle.eval_patches(z["src"], (0, 3, 3), outs, [(0, 3, 3)] * 6, coords, z["arrays"],
                                z["patch_indices"], z["params"], threads=4)
     tol = bfr_tolerances(z["positions"])
+    rot = rotated_triangles(z)
     for k in range(6):
         far = outs[k].reshape(-1, 3).astype(np.float64)
-        assert np.abs(far - z["out6"][k]).max() <= tol[k], k
+        if k < 3:
+            assert np.abs(far - z["out6"][k]).max() <= tol[k], k
+        else:
+            # where Bfr's surface is not split the sign differs on rotated sub-triangles (above)
+            err = np.minimum(np.abs(far - z["out6"][k]),
+                             second_derivative_error(far, z["out6"][k], rot))
+            assert err.max() <= tol[k], k
 
 
 def test_param_conversion_against_the_reference_library():
@@ -122,3 +153,22 @@ def test_param_conversion_against_the_reference_library():
         a = ref.bfr_subface(4, N, uv)
         b = oracle.param_to_subface(4, N, uv)
         assert np.array_equal(a[0], b[0]) and np.array_equal(bits(a[1]), bits(b[1])), N
+
+
+UV_MESHES = [p for p in MESHES if "_uv_" in os.path.basename(p)]
+
+
+@pytest.mark.parametrize("path", UV_MESHES, ids=os.path.basename)
+def test_far_face_varying_patches_agree_with_bfr_uv_surfaces(path):
+    """Face-varying channel 0 (UVs with seams): the Far table's face-varying patches at the
+    located coords against Bfr's face-varying surfaces (SurfaceFactory::InitFaceVaryingSurface,
+    the reference's tutorial 1.3), within the UV tolerance of the reference's Bfr regression
+    (regression/bfr_evaluate/main.cpp:123-125: 1e-4), derivatives within 5 times that."""
+    z = np.load(path)
+    coords = oracle.make_coords(z["q_handles"], z["q_s"], z["q_t"])
+    n = len(coords)
+    outs = [np.zeros(n * 2, np.float32) for _ in range(3)]
+    assert oracle.eval_patches(z["fvar_src"], (0, 2, 2), outs, [(0, 2, 2)] * 3, coords,
+                               z["fvar_arrays"], z["fvar_indices"], z["fvar_params"], threads=4)
+    for k, tol in enumerate((1e-4, 5e-4, 5e-4)):
+        assert np.abs(outs[k].reshape(-1, 2) - z["uv3"][k]).max() <= tol, k
