@@ -185,8 +185,9 @@ private:
 /// approximation levels (its defaults: 6 for sharp and 2 for smooth features), with the options
 /// the reference's Bfr regression pairs with them (regression/bfr_evaluate/
 /// farPatchEvaluator.cpp:52-78): adaptive refinement of `refiner` to those levels, Gregory-basis
-/// end caps, infinitely sharp patches, no shared end-cap points, no legacy corner patches.
-/// The refiner is refined adaptively in place; the caller owns the returned table.
+/// end caps, infinitely sharp patches, no shared end-cap points, no legacy corner patches, and
+/// non-linear face-varying patches when the refiner has face-varying channels.  The refiner is
+/// refined adaptively in place; the caller owns the returned table.
 inline Far::PatchTable const *GB300CreateSurfacePatchTable(Far::TopologyRefiner &refiner,
                                                             int approxLevelSharp = 6,
                                                             int approxLevelSmooth = 2) {
@@ -195,6 +196,12 @@ inline Far::PatchTable const *GB300CreateSurfacePatchTable(Far::TopologyRefiner 
     po.generateLegacySharpCornerPatches = false;
     po.shareEndCapPatchPoints = false;
     po.endCapType = Far::PatchTableFactory::Options::ENDCAP_GREGORY_BASIS;
+    if (refiner.GetNumFVarChannels() > 0) {
+        // face-varying surfaces (SurfaceFactory::InitFaceVaryingSurface): non-linear
+        // face-varying patches for every channel, isolated like the reference's Bfr regression
+        po.generateFVarTables = true;
+        po.generateFVarLegacyLinearPatches = false;
+    }
     Far::TopologyRefiner::AdaptiveOptions ro = po.GetRefineAdaptiveOptions();
     ro.SetIsolationLevel(approxLevelSharp);
     ro.SetSecondaryLevel(approxLevelSmooth);
