@@ -273,6 +273,11 @@ def bench_bfr(args, stream, peak):
     sizes_host = np.ascontiguousarray(z["verts_per_face"], np.int32)
     nfaces = len(sizes_host)
     d = BD(0, 3, 3)
+    cvs = float(np.average(z["arrays"][:, 4], weights=z["arrays"][:, 2]))
+
+    def touched_patches(patch_coords):
+        return int(len(np.unique(patch_coords[:, 1].cpu().numpy())))
+
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle
 
@@ -389,6 +394,106 @@ def bench_bfr(args, stream, peak):
                             z["patch_indices"], z["params"], threads=16)
         err = max(float(np.abs(h_out[j].numpy()[: k * 3] - ref[j]).max()) for j in range(3))
 
+        # shared (watertight) points, the reference's tutorial 2.2: Share on a fresh copy of the
+        # facets each step (the call reads the point total back), then each point evaluated
+        # once; end to end from host buffers with the face vertices and edges uploaded too
+        fe_host, n_edges = workloads.face_edges(z["verts_per_face"], z["face_verts"])
+        fv_host = np.ascontiguousarray(z["face_verts"], np.int32)
+        n_verts = len(z["positions"])
+        fv_dev = torch.from_numpy(fv_host).cuda()
+        fe_dev = torch.from_numpy(fe_host).cuda()
+        gen()
+        facets_coord = facets.clone()
+        sh_facets = torch.empty_like(facets)
+        pts = None
+        for _ in range(args.warmup):
+            sh_facets.copy_(facets_coord)
+            pts = m.Share(fv_dev, fe_dev, n_verts, n_edges, sh_facets, patch_coords=pc)
+        np_ = pts.num_points
+        pouts = [torch.empty(np_ * 3, device="cuda") for _ in range(3)]
+        share_ms, peval_ms = [], []
+        for _ in range(args.steps):
+            e0, e1, e2 = (torch.cuda.Event(enable_timing=True) for _ in range(3))
+            with torch.cuda.stream(stream):
+                sh_facets.copy_(facets_coord)
+                e0.record(stream)
+                pts = m.Share(fv_dev, fe_dev, n_verts, n_edges, sh_facets, patch_coords=pc,
+                              out=pts)
+                e1.record(stream)
+                m.Evaluate(src, d, table, pts.patch_coords, 1, pouts, num_points=np_)
+                e2.record(stream)
+            torch.cuda.synchronize()
+            share_ms.append(e0.elapsed_time(e1))
+            peval_ms.append(e1.elapsed_time(e2))
+        share_ms, peval_ms = float(np.median(share_ms)), float(np.median(peval_ms))
+        h_fv = torch.from_numpy(fv_host).pin_memory()
+        h_fe = torch.from_numpy(fe_host).pin_memory()
+        h_pout = [torch.empty(np_ * 3, pin_memory=True) for _ in range(3)]
+
+        def e2e_shared():
+            with torch.cuda.stream(stream):
+                dsz = h_sizes.to("cuda", non_blocking=True)
+                dfv = h_fv.to("cuda", non_blocking=True)
+                dfe = h_fe.to("cuda", non_blocking=True)
+                mk = dict(uniform_rate=5)
+                if h_rates is not None:
+                    dr = h_rates.to("cuda", non_blocking=True)
+                    mk = dict(rate_offsets=dr[:nfaces + 1], rates=dr[nfaces + 1:])
+                mm = bfr.MeshTessellation(4, dsz, options=bfr.TessellationOptions(3),
+                                          stream=stream, **mk)
+                mm.Generate(coords, facets, True, table, pc)
+                sp = mm.Share(dfv, dfe, n_verts, n_edges, facets, patch_coords=pc)
+                mm.Evaluate(src, d, table, sp.patch_coords, 1, pouts, num_points=sp.num_points)
+                for a, b in zip(h_pout, pouts):
+                    a.copy_(b, non_blocking=True)
+                h_facets.copy_(facets, non_blocking=True)
+            stream.synchronize()
+
+        for _ in range(2):
+            e2e_shared()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_shared()
+        e2e_sh_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        h2d_sh = h2d + 8 * len(fv_host)
+        d2h_sh = 36 * np_ + 12 * nf
+        # outside timing: the watertight facets and point numbering against the oracle's
+        # bookkeeping (exact), the points' P against the per-coord evaluation
+        w_f, w_po, w_src = oracle.tess_share(4, sizes_host, fv_host, fe_host, n_verts, n_edges,
+                                             kw.get("rate_offsets", np.arange(nfaces + 1)),
+                                             kw.get("rates", np.full(nfaces, 5, np.int32)),
+                                             tm["coord_offsets"], tm["facet_offsets"],
+                                             tm["facets"])
+        shared_exact = bool(np_ == len(w_src) and np.array_equal(h_facets.numpy(), w_f))
+        pp = h_pout[0].numpy().reshape(-1, 3)
+        shared_p_bitwise = bool(np.array_equal(pp.view(np.int32),
+                                               h_out[0].numpy().reshape(-1, 3)[w_src]
+                                               .view(np.int32)))
+        share_b = workloads.bfr_share_bytes(nfaces, len(fv_host), n_verts, n_edges, nf, np_, 3)
+        peval_b = workloads.patch_bytes(np_, 3, 3, len(z["src"]) // 3, touched_patches(pc), cvs)
+        shared = {
+            "points": np_, "points_per_coord": np_ / n,
+            "share_ms": share_ms, "eval_points_ms": peval_ms,
+            "points_per_s": np_ / ((gen_ms + share_ms + peval_ms) / 1e3),
+            "e2e": {"points_per_s": np_ / (e2e_sh_ms / 1e3), "ms": e2e_sh_ms,
+                    "h2d_bytes": h2d_sh, "d2h_bytes": d2h_sh,
+                    "what": "host face sizes (and rates), face vertices and edges in; Count, "
+                            "Generate, Share, Eval of each point once; P/Du/Dv of the points "
+                            "and the facets back to pinned host memory"},
+            "roofline_share": {"bound": "hbm", "kernel": "k_share_* (7 launches + 2 scans)",
+                               "algorithmic_bytes": share_b,
+                               "achieved": share_b / (share_ms / 1e3) / 1e9, "peak": peak,
+                               "unit": "GB/s", "frac": share_b / (share_ms / 1e3) / 1e9 / peak,
+                               "note": "share_ms is the whole call, including its host read of "
+                                       "the point total"},
+            "roofline_eval": {"bound": "hbm", "algorithmic_bytes": peval_b,
+                              "achieved": peval_b / (peval_ms / 1e3) / 1e9, "peak": peak,
+                              "unit": "GB/s", "frac": peval_b / (peval_ms / 1e3) / 1e9 / peak},
+            "exact_facets_and_points_vs_oracle": shared_exact,
+            "points_p_bitwise_vs_per_coord_eval": shared_p_bitwise,
+        }
+        del fv_dev, fe_dev, facets_coord, sh_facets, pouts, h_pout, pts
+
         # CPU baseline: the oracle's tessellate + locate + evaluate over a bounded face sample
         sample = max(1, nfaces // 8)
         so = np.concatenate([[0], np.cumsum(np.ones(sample, np.int64))]) if "rates" not in kw \
@@ -415,9 +520,7 @@ def bench_bfr(args, stream, peak):
         cpu_s = time.perf_counter() - t0
 
         facet_b = workloads.bfr_tess_bytes(nfaces, n, nf, 3, True, "rates" not in kw)
-        cvs = float(np.average(z["arrays"][:, 4], weights=z["arrays"][:, 2]))
-        touched = int(len(np.unique(pc[:, 1].cpu().numpy())))
-        eval_b = workloads.patch_bytes(n, 3, 3, len(z["src"]) // 3, touched, cvs)
+        eval_b = workloads.patch_bytes(n, 3, 3, len(z["src"]) // 3, touched_patches(pc), cvs)
         out[mode] = {
             "rates": rate_desc, "coords": n, "facets": nf,
             "points_per_s": n / ((gen_ms + eval_ms) / 1e3),
@@ -439,6 +542,7 @@ def bench_bfr(args, stream, peak):
                               "unit": "GB/s", "frac": eval_b / (eval_ms / 1e3) / 1e9 / peak},
             "exact_coords_and_facets_vs_oracle": exact,
             "max_abs_err_vs_oracle_slice": err,
+            "shared_points": shared,
             "cpu_baseline": {"value": len(cc) / cpu_s, "unit": "points/s", "cores": cpu_threads,
                              "kind": "port",
                              "sample": f"first {sample} faces ({len(cc)} points): oracle "

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "../osd/gb300Evaluator.h"
 
@@ -146,6 +147,45 @@ public:
                                                   stream) == GB300_OK;
     }
 
+    /// Shared (watertight) points, as the reference's Bfr tutorial 2.2 shares the points of
+    /// mesh vertices and edges (tutorials/bfr/tutorial_2_2/bfr_tutorial_2_2.cpp:244-430;
+    /// GB300TessellationShare): after Generate, `facets` (mesh-wide coord indices, or
+    /// face-local ones when meshIndices is false) become point indices in place; each point is
+    /// made once, by the first face (in face order) that reaches it, and numbered as the
+    /// tutorial numbers it.  faceVerts / faceEdges: DEVICE face vertices and edges per corner of
+    /// the base level, numCorners each (GB300GetFaceVerticesAndEdges).  pointOffsets (DEVICE, GetNumFaces() + 1)
+    /// receives each face's first point; pointPatchCoords (DEVICE, capacity GetNumCoords()) one
+    /// PatchCoord per point, copied from Generate's patchCoords, for EvaluatePoints.  Every
+    /// edge needs one rate in all its faces.  Returns the number of points, or -1
+    /// (GB300GetLastErrorString says why).
+    int64_t Share(int const *faceVerts, int const *faceEdges, int64_t numCorners,
+                  int numVertices, int numEdges, int *facets,
+                  Osd::PatchCoord const *patchCoords, int64_t *pointOffsets,
+                  Osd::PatchCoord *pointPatchCoords, bool meshIndices = true,
+                  void *stream = NULL) const {
+        int64_t n = 0;
+        if (GB300TessellationShare(_reg, _numFaces, _faceSizes, _rateOffsets, _rates,
+                                   _uniformRate, _options.get(), GetCoordOffsets(),
+                                   GetFacetOffsets(), faceVerts, faceEdges, numCorners,
+                                   numVertices, numEdges, facets, meshIndices ? 1 : 0,
+                                   patchCoords, NULL,
+                                   pointOffsets, pointPatchCoords, NULL, NULL, NULL, NULL, &n,
+                                   stream) != GB300_OK)
+            return -1;
+        return n;
+    }
+
+    /// Evaluate at `numPoints` PatchCoords -- the shared points of Share, each evaluated once.
+    bool EvaluatePoints(Osd::GB300PatchTable const *table, Osd::PatchCoord const *pointCoords,
+                        int numPoints, float const *src, int length, int srcStride, float *P,
+                        float *Du = NULL, float *Dv = NULL, float *Duu = NULL,
+                        float *Duv = NULL, float *Dvv = NULL, void *stream = NULL) const {
+        return table && GB300TessellationEvaluate(table->GetHandle(), src, P, Du, Dv, Duu, Duv,
+                                                  Dvv, length, srcStride, length, length,
+                                                  length, length, length, length, numPoints,
+                                                  pointCoords, stream) == GB300_OK;
+    }
+
 private:
     GB300MeshTessellation() {}
 
@@ -181,6 +221,24 @@ private:
 };
 
 #ifdef OSD_GB300_HAVE_BFR
+/// The base level's face vertices and face edges, one entry per face corner, faces in order
+/// (Far::TopologyLevel::GetFaceVertices / GetFaceEdges): the topology
+/// GB300MeshTessellation::Share shares points along.  Host vectors, to upload.
+inline void GB300GetFaceVerticesAndEdges(Far::TopologyRefiner const &refiner,
+                                         std::vector<int> &faceVerts,
+                                         std::vector<int> &faceEdges) {
+    Far::TopologyLevel const &base = refiner.GetLevel(0);
+    faceVerts.clear();
+    faceEdges.clear();
+    faceVerts.reserve((size_t)base.GetNumFaceVertices());
+    faceEdges.reserve((size_t)base.GetNumFaceVertices());
+    for (int f = 0; f < base.GetNumFaces(); ++f) {
+        Far::ConstIndexArray v = base.GetFaceVertices(f), e = base.GetFaceEdges(f);
+        faceVerts.insert(faceVerts.end(), v.begin(), v.end());
+        faceEdges.insert(faceEdges.end(), e.begin(), e.end());
+    }
+}
+
 /// The Far patch table whose patches are the surfaces Bfr::SurfaceFactory builds with the given
 /// approximation levels (its defaults: 6 for sharp and 2 for smooth features), with the options
 /// the reference's Bfr regression pairs with them (regression/bfr_evaluate/

@@ -340,6 +340,43 @@ int GB300TessellationEvaluate(const GB300PatchTable *table, const float *src, fl
                               int duuStride, int duvStride, int dvvStride, int numCoords,
                               const void *patchCoords, void *stream);
 
+/* Shared (watertight) points of a mesh tessellation: the bookkeeping of the reference's Bfr
+ * tutorial with shared vertex and edge points (tutorials/bfr/tutorial_2_2/
+ * bfr_tutorial_2_2.cpp:244-430), for every face at once, after Count and Generate with the
+ * same faces, rates and options.  faceVerts / faceEdges (DEVICE, numCorners entries each, one
+ * per face corner, faces in order: Far::TopologyLevel::GetFaceVertices / GetFaceEdges of the
+ * base level, edge i running from corner i to corner i + 1; the face sizes must add up to
+ * numCorners) name numVertices vertices and numEdges edges.
+ *
+ * The point of a mesh vertex, and the rate - 1 points inside a mesh edge, are made by the
+ * first face (in face order) that reaches them, from its own coords; later faces reuse them,
+ * edge points reversed where a face runs the edge from the other end.  A face's interior coords
+ * are all new points.  Points are numbered face by face, in each face its new boundary points
+ * in boundary order and then its interior coords, as the tutorial numbers them.  Faces without
+ * coords take no part.  An edge needs one rate in all its faces (rates from edge lengths have
+ * that); an edge with two rates is rejected.
+ *
+ * facets (DEVICE, in place): Generate's facets, mesh-wide (meshFacetIndices != 0) or face-local
+ * coord indices in, point indices out (Tessellation::TransformFacetCoordIndices(facets,
+ * boundaryIndices, interiorOffset), tessellation.cpp:2449-2464); -1 entries stay -1.
+ * pointOffsets (DEVICE, numFaces + 1): the first point each face makes; *numPoints (HOST) the
+ * total.  Optional DEVICE outputs, one entry per point (capacity: Count's coord total):
+ * pointPatchCoords (5 x 32 bits, copied from the coord's PatchCoord in coordPatchCoords, so
+ * GB300TessellationEvaluate evaluates each point once), pointCoords (the coord's (u, v)) and
+ * pointFaces (the face that made it); vertexPoints (numVertices) and edgePoints (numEdges: the
+ * first point inside the edge in its maker's direction), -1 where none.  Synchronizes
+ * `stream`.  Overlapping calls with the same outputs race. */
+int GB300TessellationShare(int regularFaceSize, int numFaces, const int *faceSizes,
+                           const int *rateOffsets, const int *rates, int uniformRate,
+                           const GB300TessellationOptions *options,
+                           const int64_t *coordOffsets, const int64_t *facetOffsets,
+                           const int *faceVerts, const int *faceEdges, int64_t numCorners,
+                           int numVertices, int numEdges, int *facets, int meshFacetIndices,
+                           const void *coordPatchCoords, const float *coords,
+                           int64_t *pointOffsets, void *pointPatchCoords, float *pointCoords,
+                           int *pointFaces, int *vertexPoints, int *edgePoints,
+                           int64_t *numPoints, void *stream);
+
 /* ---- draw-time tessellation factors (osd/glslPatchCommonTess.glsl:92-760) ------------------ */
 
 /* The tess-control settings of OpenSubdiv's patch shaders.  tessLevel: OsdTessLevel();

@@ -96,6 +96,14 @@ def _torch():
     return torch
 
 
+class SharedPoints:
+    """The shared points of MeshTessellation.Share (attributes set there; the full-capacity
+    buffers behind patch_coords, coords and faces are kept for reuse through `out`)."""
+    num_points = 0
+    point_offsets = patch_coords = coords = faces = vertex_points = edge_points = None
+    _pc = _coords = _faces = None
+
+
 class MeshTessellation:
     """Bfr::Tessellation of every face of a mesh, on the device.
 
@@ -178,12 +186,71 @@ class MeshTessellation:
             _ptr(patch_coords) if table is not None else None, _stream(self.stream)))
         return coords, facets, patch_coords
 
-    def Evaluate(self, src, src_desc, table, patch_coords, derivatives=1, outputs=None):
-        """Limit points at every coord (Bfr::Surface::Evaluate, GB300TessellationEvaluate): P,
-        and with derivatives >= 1 Du, Dv, with 2 also Duu, Duv, Dvv; each [num_coords, length]
-        float32 (allocated unless `outputs` gives them)."""
+    def Share(self, face_verts, face_edges, num_vertices, num_edges, facets,
+              patch_coords=None, coords=None, mesh_facet_indices=True, point_coords=False,
+              point_faces=False, vertex_points=False, edge_points=False, out=None):
+        """Shared (watertight) points, as the reference's Bfr tutorial 2.2 shares vertex and
+        edge points (GB300TessellationShare): face_verts / face_edges are the base level's
+        face vertices and edges per corner (host arrays or CUDA tensors); `facets` from
+        Generate (mesh-wide indices unless mesh_facet_indices is False) are rewritten in place
+        to point indices.  Returns a SharedPoints: num_points, point_offsets [faces + 1] and,
+        as asked, patch_coords [num_points, 5] (copied from the coords' `patch_coords`: give
+        them to Evaluate with num_points), coords [num_points, 2], faces, vertex_points,
+        edge_points.  `out`: a SharedPoints from an earlier call on the same mesh, whose
+        buffers are reused (nothing is allocated)."""
         torch = _torch()
-        n = self.num_coords
+        dev = torch.device("cuda")
+
+        def on_device(x):
+            t = x if hasattr(x, "data_ptr") else torch.from_numpy(np.ascontiguousarray(x, np.int32))
+            return t.to(dev, torch.int32).contiguous()
+
+        fv, fe = on_device(face_verts), on_device(face_edges)
+        if point_coords and coords is None:
+            raise ValueError("point_coords needs the tessellation's coords")
+        if out is None:
+            cap = max(self.num_coords, 1)
+            out = SharedPoints()
+            out.point_offsets = torch.empty(self.num_faces + 1, dtype=torch.int64, device=dev)
+            out._pc = (torch.empty((cap, 5), dtype=torch.int32, device=dev)
+                       if patch_coords is not None else None)
+            out._coords = (torch.empty((cap, 2), dtype=torch.float32, device=dev)
+                           if point_coords else None)
+            out._faces = (torch.empty(cap, dtype=torch.int32, device=dev)
+                          if point_faces else None)
+            out.vertex_points = (torch.empty(max(int(num_vertices), 1), dtype=torch.int32,
+                                             device=dev) if vertex_points else None)
+            out.edge_points = (torch.empty(max(int(num_edges), 1), dtype=torch.int32,
+                                           device=dev) if edge_points else None)
+        elif ((patch_coords is not None and out._pc is None) or
+              (point_coords and out._coords is None) or (point_faces and out._faces is None)):
+            raise ValueError("`out` lacks a buffer this call writes")
+        n = C.c_int64(0)
+        check(_lib.load().GB300TessellationShare(
+            self.regular_face_size, self.num_faces, _ptr(self.face_sizes),
+            _ptr(self.rate_offsets), _ptr(self.rates), self.uniform_rate, C.byref(self.options),
+            _ptr(self.coord_offsets), _ptr(self.facet_offsets), _ptr(fv), _ptr(fe),
+            int(fv.numel()), int(num_vertices), int(num_edges), _ptr(facets),
+            int(bool(mesh_facet_indices)),
+            _ptr(patch_coords), _ptr(coords), _ptr(out.point_offsets),
+            _ptr(out._pc if patch_coords is not None else None),
+            _ptr(out._coords if point_coords else None),
+            _ptr(out._faces if point_faces else None), _ptr(out.vertex_points),
+            _ptr(out.edge_points), C.byref(n), _stream(self.stream)))
+        out.num_points = np_ = int(n.value)
+        out.patch_coords = out._pc[:np_] if patch_coords is not None else None
+        out.coords = out._coords[:np_] if point_coords else None
+        out.faces = out._faces[:np_] if point_faces else None
+        return out
+
+    def Evaluate(self, src, src_desc, table, patch_coords, derivatives=1, outputs=None,
+                 num_points=None):
+        """Limit points at every coord (Bfr::Surface::Evaluate, GB300TessellationEvaluate): P,
+        and with derivatives >= 1 Du, Dv, with 2 also Duu, Duv, Dvv; each [n, length] float32
+        (allocated unless `outputs` gives them), n = num_coords, or num_points for the shared
+        points of Share."""
+        torch = _torch()
+        n = self.num_coords if num_points is None else int(num_points)
         L = src_desc.length
         k = 1 if derivatives == 0 else 3 if derivatives == 1 else 6
         outs = outputs if outputs is not None else [

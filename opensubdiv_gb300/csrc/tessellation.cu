@@ -18,6 +18,10 @@
 //            PatchMap walk finds the patch -- the lookup the reference's Bfr regression does
 //            for every tessellation coord (regression/bfr_evaluate/farPatchEvaluator.cpp:
 //            190-207).
+//   share    (GB300TessellationShare, optional) shared vertex and edge points as the
+//            reference's tutorial 2.2 makes them: claims by 64-bit atomicMin, counts, a scan
+//            that numbers the points, per-corner records, then one warp per face moves the
+//            PatchCoords of the points it makes and rewrites its facets to point indices.
 // A staged variant (faces generated into a shared-memory arena, copied out coalesced) was
 // slower: about 900 bytes of arena per face left too few warps resident to hide latency.
 #include "common.cuh"
@@ -29,6 +33,7 @@
 
 #include <atomic>
 #include <climits>
+#include <cstring>
 #include <mutex>
 #include <vector>
 
@@ -343,6 +348,366 @@ __global__ void __launch_bounds__(256) k_tess_finish(const GenArgs a) {
     }
 }
 
+// ---- shared (watertight) points --------------------------------------------------------------
+// The bookkeeping of the reference's tessellation with shared vertex and edge points
+// (tutorials/bfr/tutorial_2_2/bfr_tutorial_2_2.cpp:244-430) for every face at once.  The point
+// of a mesh vertex, and the points inside a mesh edge, are made by the lowest face that reaches
+// them (its lowest corner that does): the face the tutorial's in-order loop reaches them with
+// first.  Each face makes its points in boundary order (vertex, then the points inside the
+// edge that follows it), then its interior coords; a prefix sum over the faces numbers them as
+// the tutorial does.  Faces without coords take no part.
+struct ShareArgs {
+    int reg, numFaces, uniformRate, fs, pq, coordStride, facetStride, meshIndices;
+    int numVertices, numEdges;
+    int64_t numCorners;  // entries of faceVerts and faceEdges
+    const int *faceSizes, *faceVerts, *faceEdges, *rateOffsets, *rates;
+    const int64_t *co, *fo;
+    int64_t *cornerOff;                     // first corner of each face (scan of faceSizes)
+    int4 *cornerInfo;                       // per corner: share_corner's record
+    unsigned long long *vertKey, *edgeKey;  // min over faces of (face << 32 | corner)
+    int *edgeN;                             // points inside each edge, set by its maker
+    int64_t *counts;                        // points each face makes; [numFaces] = 0
+    const int64_t *po;                      // their exclusive scan: first point of each face
+    int *vertPoint, *edgePoint;             // point of each vertex, first point of each edge
+    int *facets;
+    const int *coordPC;  // 5 x 32 bit per coord (PatchCoord), optional
+    const float *coords;
+    int *pointPC;
+    float *pointCoords;
+    int *pointFaces;
+    int *err;  // {index errors, first such face, rate mismatches, first such face}, then the
+               // point and corner totals (two 64-bit words), read back in one copy
+};
+
+constexpr int kCornerEdgeMask = 0x7fff;  // points inside the edge (rate - 1 <= 32766)
+constexpr int kCornerVertNew = 1 << 15;
+constexpr int kCornerEdgeNew = 1 << 16;
+constexpr int kCornerReversed = 1 << 17;
+constexpr int kCornerBad = 1 << 18;
+
+__device__ __forceinline__ void share_error(int *err, int kind, int f) {
+    atomicAdd(err + 2 * kind, 1);
+    atomicMin(err + 2 * kind + 1, f);
+}
+
+__device__ __forceinline__ unsigned long long corner_key(int f, int i) {
+    return ((unsigned long long)(unsigned)f << 32) | (unsigned)i;
+}
+
+__device__ __forceinline__ bool share_face(const ShareArgs &a, int f, Face &face) {
+    FaceRates r;
+    rates_of(a.rateOffsets, a.rates, a.uniformRate, f, r);
+    return face.init(a.reg, a.faceSizes[f], r.n, r.p, a.fs, a.pq, r.one);
+}
+
+// Face sizes (scanned into corner offsets after), unclaimed vertices and edges without
+// points, and the error words.
+__global__ void __launch_bounds__(256) k_share_init(const ShareArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t == 0) a.err[0] = 0, a.err[1] = INT_MAX, a.err[2] = 0, a.err[3] = INT_MAX;
+    for (int f = t; f <= a.numFaces; f += stride)
+        a.counts[f] = f < a.numFaces ? a.faceSizes[f] : 0;
+    for (int v = t; v < a.numVertices; v += stride) {
+        a.vertKey[v] = ~0ull;
+        a.vertPoint[v] = -1;
+    }
+    for (int e = t; e < a.numEdges; e += stride) {
+        a.edgeKey[e] = ~0ull;
+        a.edgePoint[e] = -1;
+    }
+}
+
+// One thread per face: claim the face's vertices and edges (lowest face and corner wins).
+__global__ void __launch_bounds__(256) k_share_own(const ShareArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
+        Face face;
+        if (a.co[f + 1] == a.co[f] || !share_face(a, f, face)) continue;
+        const int N = face.N;
+        const int64_t c0 = a.cornerOff[f];
+        if (c0 + N > a.numCorners) {
+            share_error(a.err, 0, f);
+            continue;
+        }
+        for (int i = 0; i < N; ++i) {
+            const int v = a.faceVerts[c0 + i], e = a.faceEdges[c0 + i];
+            if ((unsigned)v >= (unsigned)a.numVertices || (unsigned)e >= (unsigned)a.numEdges) {
+                share_error(a.err, 0, f);
+                continue;
+            }
+            atomicMin(a.vertKey + v, corner_key(f, i));
+            atomicMin(a.edgeKey + e, corner_key(f, i));
+        }
+    }
+}
+
+// One thread per face: the points the face makes (its claimed vertices, the points inside its
+// claimed edges, its interior coords); a claimed edge records its number of inside points.
+__global__ void __launch_bounds__(256) k_share_count(const ShareArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f <= a.numFaces; f += stride) {
+        int64_t n = 0;
+        const int64_t nc = f < a.numFaces ? a.co[f + 1] - a.co[f] : 0;
+        Face face;
+        const bool valid = nc > 0 && share_face(a, f, face);
+        if (nc > 0 && !valid) share_error(a.err, 0, f);  // coords the tessellation cannot have
+        const int64_t c0 = valid ? a.cornerOff[f] : 0;
+        if (valid && c0 + face.N <= a.numCorners) {
+            n = nc - face.nBoundary;
+            for (int i = 0; i < face.N; ++i) {
+                const int v = a.faceVerts[c0 + i], e = a.faceEdges[c0 + i];
+                if ((unsigned)v >= (unsigned)a.numVertices ||
+                    (unsigned)e >= (unsigned)a.numEdges)
+                    continue;
+                const unsigned long long key = corner_key(f, i);
+                if (a.vertKey[v] == key) ++n;
+                if (a.edgeKey[e] == key) {
+                    const int k = face.outer(i) - 1;
+                    a.edgeN[e] = k;
+                    n += k;
+                }
+            }
+        }
+        a.counts[f] = n;
+    }
+}
+
+// One thread per face: number the points of the vertices and edges the face claimed.
+__global__ void __launch_bounds__(256) k_share_assign(const ShareArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
+        if (a.co[f + 1] == a.co[f]) continue;
+        Face face;
+        if (!share_face(a, f, face)) continue;
+        const int64_t c0 = a.cornerOff[f];
+        if (c0 + face.N > a.numCorners) continue;
+        int p = (int)a.po[f];
+        for (int i = 0; i < face.N; ++i) {
+            const int v = a.faceVerts[c0 + i], e = a.faceEdges[c0 + i];
+            if ((unsigned)v >= (unsigned)a.numVertices || (unsigned)e >= (unsigned)a.numEdges)
+                continue;
+            const unsigned long long key = corner_key(f, i);
+            if (a.vertKey[v] == key) a.vertPoint[v] = p++;
+            if (a.edgeKey[e] == key) {
+                a.edgePoint[e] = p;
+                p += face.outer(i) - 1;
+            }
+        }
+    }
+}
+
+// Corner i of face f, whose vertex coord is boundary coord P: {P, the vertex's point, the
+// first point inside the edge that follows, flags | points inside the edge}.  An edge run
+// from the other end than its maker ran it takes its points in reverse.
+__device__ __forceinline__ int4 share_corner(const ShareArgs &a, const Face &face, int f,
+                                             int64_t c0, int i, int P) {
+    const int v = a.faceVerts[c0 + i], e = a.faceEdges[c0 + i];
+    const int n = face.outer(i) - 1;
+    if ((unsigned)v >= (unsigned)a.numVertices || (unsigned)e >= (unsigned)a.numEdges)
+        return make_int4(P, -1, -1, n | kCornerBad);
+    const unsigned long long key = corner_key(f, i);
+    int meta = n;
+    if (a.vertKey[v] == key) meta |= kCornerVertNew;
+    const unsigned long long ek = a.edgeKey[e];
+    if (ek == key) {
+        meta |= kCornerEdgeNew;
+    } else if (a.edgeN[e] != n) {
+        meta |= kCornerBad;
+    } else {
+        const int g = (int)(ek >> 32), j = (int)(ek & 0xffffffffu);
+        if (a.faceVerts[a.cornerOff[g] + j] != v) meta |= kCornerReversed;
+    }
+    return make_int4(P, a.vertPoint[v], a.edgePoint[e], meta);
+}
+
+// The point of boundary coord idx in corner c (its vertex coord or inside its edge); `made`
+// when this face made the point.
+__device__ __forceinline__ int share_boundary_point(int4 c, int idx, bool &made) {
+    const int j = idx - c.x;
+    if (j == 0) {
+        made = (c.w & kCornerVertNew) != 0;
+        return c.y;
+    }
+    made = (c.w & kCornerEdgeNew) != 0;
+    if (c.w & kCornerBad) return -1;
+    const int n = c.w & kCornerEdgeMask;
+    return (c.w & kCornerReversed) ? c.z + n - j : c.z + j - 1;
+}
+
+// The point of coord idx of a face with N corner records `cs` (shared or global memory),
+// nb boundary coords and interior coord idx at point idx + interior; `made` when the face
+// made the point.
+__device__ __forceinline__ int share_point(const int4 *cs, int N, int nb, int interior,
+                                           int idx, bool &made) {
+    if (idx >= nb) {
+        made = true;
+        return idx + interior;
+    }
+    int lo = 0, hi = N - 1;  // the last corner whose vertex coord is at or before idx
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (cs[mid].x <= idx) lo = mid; else hi = mid - 1;
+    }
+    return share_boundary_point(cs[lo], idx, made);
+}
+
+// The point and corner totals beside the error words, so one copy reads all of them.
+__global__ void k_share_totals(const ShareArgs a) {
+    if (threadIdx.x == 0) {
+        long long *t = reinterpret_cast<long long *>(a.err + 4);
+        t[0] = a.po[a.numFaces];
+        t[1] = a.cornerOff[a.numFaces];
+    }
+}
+
+// One thread per face: the record of each of its corners, for the emit pass.
+__global__ void __launch_bounds__(256) k_share_corners(const ShareArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f < a.numFaces; f += stride) {
+        if (a.co[f + 1] == a.co[f]) continue;
+        Face face;
+        if (!share_face(a, f, face)) continue;
+        const int64_t c0 = a.cornerOff[f];
+        if (c0 + face.N > a.numCorners) continue;
+        int P = 0;
+        for (int i = 0; i < face.N; ++i) {
+            const int4 c = share_corner(a, face, f, c0, i, P);
+            if (c.w & kCornerBad) share_error(a.err, c.y < 0 ? 0 : 1, f);
+            a.cornerInfo[c0 + i] = c;
+            P += face.outer(i);
+        }
+    }
+}
+
+// One warp per face.  Every load of a face is issued before its first store -- its corner
+// records, PatchCoord words and facet index words, kShareWords of each per lane per round --
+// so a face costs about one memory latency, and the next face's offsets (eight words, one per
+// lane) are fetched while this one is processed.  The point of each boundary coord goes into
+// a per-warp table in shared memory (faces up to kShareTable boundary coords and 32 sides;
+// larger faces search their corner records per index), interior coords map to points by an
+// offset.  Then each PatchCoord word of a coord that makes a point goes to the point's slot,
+// and each facet index becomes its point (Tessellation::TransformFacetCoordIndices with
+// boundary indices and an interior offset, tessellation.cpp:2449-2464).
+constexpr int kShareWords = 6;
+constexpr int kShareTable = 128;
+constexpr int kShareMade = int(0x80000000u);
+
+template <int FS>
+__global__ void __launch_bounds__(256, 4) k_share_emit(const ShareArgs a) {
+    __shared__ int4 corners[8][32];
+    __shared__ int table[8][kShareTable];  // point | kShareMade of each boundary coord
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int warps = (gridDim.x * blockDim.x) >> 5;
+    // lane j < 8 holds offset j of face f: co[f], co[f+1], cornerOff[f], cornerOff[f+1],
+    // fo[f], fo[f+1], po[f], po[f+1]
+    auto offsets_of = [&](int f) -> long long {
+        if (f >= a.numFaces || lane >= 8) return 0;
+        const int64_t *src = lane < 2 ? a.co : lane < 4 ? a.cornerOff : lane < 6 ? a.fo : a.po;
+        return __ldg((const long long *)src + f + (lane & 1));
+    };
+    int f = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    long long next = offsets_of(f);
+    for (; f < a.numFaces; f += warps) {
+        const long long mine = next;
+        next = offsets_of(f + warps);
+        const int64_t c0 = __shfl_sync(0xffffffffu, mine, 0);
+        const int64_t c1 = __shfl_sync(0xffffffffu, mine, 1);
+        const int64_t k0 = __shfl_sync(0xffffffffu, mine, 2);
+        const int64_t k1 = __shfl_sync(0xffffffffu, mine, 3);
+        const int64_t f0 = __shfl_sync(0xffffffffu, mine, 4);
+        const int64_t f1 = __shfl_sync(0xffffffffu, mine, 5);
+        const int base = (int)__shfl_sync(0xffffffffu, mine, 6);
+        const int end = (int)__shfl_sync(0xffffffffu, mine, 7);
+        const int nc = (int)(c1 - c0), N = (int)(k1 - k0);
+        if (nc == 0 || k1 > a.numCorners || N < 3) continue;
+        const int4 *cg = a.cornerInfo + k0;
+        const bool small = N <= 32;
+        const int pcWords = a.pointPC ? 5 * nc : 0;
+        const int nf = (int)(f1 - f0), fWords = nf * FS;
+        const int *pcSrc = a.coordPC + 5 * c0;
+        int *d0 = a.facets + f0 * a.facetStride;
+        const int off = a.meshIndices ? (int)c0 : 0;
+        int nb = 0, interior = 0;
+        bool tabled = false;
+        // the point of coord idx, with kShareMade when this face made it
+        auto point_of = [&](int idx) -> int {
+            if (idx >= nb) return (idx + interior) | kShareMade;
+            if (tabled) return table[w][idx];
+            bool made;
+            const int p = small ? share_point(corners[w], N, nb, interior, idx, made)
+                                : share_point(cg, N, nb, interior, idx, made);
+            return made ? (p | kShareMade) : p;
+        };
+        const int rounds = max(pcWords, fWords);
+        for (int r0 = 0; r0 < rounds; r0 += 32 * kShareWords) {
+            int pw[kShareWords], fw[kShareWords];
+            int4 mine4 = make_int4(0, 0, 0, 0);
+            if (r0 == 0 && small && lane < N) mine4 = __ldg(cg + lane);
+#pragma unroll
+            for (int u = 0; u < kShareWords; ++u) {
+                const int k = r0 + lane + 32 * u;
+                pw[u] = k < pcWords ? __ldg(pcSrc + k) : 0;
+                fw[u] = k < fWords ? d0[(int64_t)(k / FS) * a.facetStride + (k % FS)] : -1;
+            }
+            if (r0 == 0) {
+                if (small) {
+                    if (lane < N) corners[w][lane] = mine4;
+                    __syncwarp();
+                }
+                const int4 last = small ? corners[w][N - 1] : cg[N - 1];
+                nb = last.x + (last.w & kCornerEdgeMask) + 1;
+                interior = end - nc;
+                if (small && nb <= kShareTable) {
+                    for (int i = lane; i < nb; i += 32) {
+                        bool made;
+                        const int p = share_point(corners[w], N, nb, interior, i, made);
+                        table[w][i] = made ? (p | kShareMade) : p;
+                    }
+                    __syncwarp();
+                    tabled = true;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kShareWords; ++u) {
+                const int k = r0 + lane + 32 * u;
+                if (k < pcWords) {
+                    const int i = k / 5;
+                    const int t = point_of(i);
+                    const int p = t & ~kShareMade;
+                    if ((t & kShareMade) && p >= base && p < end)
+                        a.pointPC[5 * (int64_t)p + (k - 5 * i)] = pw[u];
+                }
+                if (k < fWords && fw[u] >= 0) {
+                    const int local = fw[u] - off;
+                    int p = -1;
+                    if (local < nc && local >= 0) {
+                        const int t = point_of(local);
+                        p = (t == -1) ? -1 : (t & ~kShareMade);
+                    } else {
+                        share_error(a.err, 0, f);
+                    }
+                    d0[(int64_t)(k / FS) * a.facetStride + (k % FS)] = p;
+                }
+            }
+        }
+        if (a.pointCoords || a.pointFaces) {
+            for (int i = lane; i < nc; i += 32) {
+                const int t = point_of(i);
+                const int p = t & ~kShareMade;
+                if (!(t & kShareMade) || p < base || p >= end) continue;
+                if (a.pointCoords) {
+                    const float *s = a.coords + (c0 + i) * a.coordStride;
+                    a.pointCoords[2 * (int64_t)p] = s[0];
+                    a.pointCoords[2 * (int64_t)p + 1] = s[1];
+                }
+                if (a.pointFaces) a.pointFaces[p] = f;
+            }
+        }
+        __syncwarp();
+    }
+}
+
 // Shared uniform patterns, cached per device and request (they depend only on the scheme's
 // face size, the rate and the facet options) up to kPatternCacheBytes; beyond that a call
 // builds them in per-call scratch.
@@ -640,4 +1005,148 @@ extern "C" int GB300TessellationGenerate(
     if (dd) scratch_free(dd, s);
     if (scratchPat.mem) scratch_free(scratchPat.mem, s);
     return st;
+}
+
+extern "C" int GB300TessellationShare(
+    int regularFaceSize, int numFaces, const int *faceSizes, const int *rateOffsets,
+    const int *rates, int uniformRate, const GB300TessellationOptions *options,
+    const int64_t *coordOffsets, const int64_t *facetOffsets, const int *faceVerts,
+    const int *faceEdges, int64_t numCorners, int numVertices, int numEdges, int *facets,
+    int meshFacetIndices,
+    const void *coordPatchCoords, const float *coords, int64_t *pointOffsets,
+    void *pointPatchCoords, float *pointCoords, int *pointFaces, int *vertexPoints,
+    int *edgePoints, int64_t *numPoints, void *stream) {
+    const char *who = "GB300TessellationShare";
+    int st = check_faces(regularFaceSize, numFaces, faceSizes, who);
+    if (st != GB300_OK) return st;
+    Opts o;
+    if ((st = read_options(options, o, who)) != GB300_OK) return st;
+    if (!coordOffsets || !facetOffsets || !facets || !pointOffsets || !numPoints)
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: null offsets, facets or outputs", who);
+    if (numVertices < 0 || numEdges < 0 || numCorners < 0 ||
+        (numCorners > 0 && (!faceVerts || !faceEdges)))
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad face vertices or edges", who);
+    if ((pointPatchCoords && !coordPatchCoords) || (pointCoords && !coords))
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "%s: per-point outputs need the per-coord inputs they copy", who);
+    cudaStream_t s = as_stream(stream);
+    ShareArgs a;
+    a.reg = regularFaceSize;
+    a.numFaces = numFaces;
+    a.uniformRate = uniformRate;
+    a.fs = o.fs;
+    a.pq = o.pq;
+    a.coordStride = o.coordStride;
+    a.facetStride = o.facetStride;
+    a.meshIndices = meshFacetIndices != 0;
+    a.numVertices = numVertices;
+    a.numEdges = numEdges;
+    a.numCorners = numCorners;
+    a.faceSizes = faceSizes;
+    a.faceVerts = faceVerts;
+    a.faceEdges = faceEdges;
+    a.rateOffsets = rateOffsets;
+    a.rates = rates;
+    a.co = coordOffsets;
+    a.fo = facetOffsets;
+    a.po = pointOffsets;
+    a.facets = facets;
+    a.coordPC = (const int *)coordPatchCoords;
+    a.coords = coords;
+    a.pointPC = (int *)pointPatchCoords;
+    a.pointCoords = pointCoords;
+    a.pointFaces = pointFaces;
+
+    // scratch: corner offsets and counts (numFaces + 1 each), corner records, vertex and edge
+    // keys, inside counts of edges, the point arrays the caller did not ask for, error words
+    const size_t n1 = (size_t)numFaces + 1, nv = (size_t)numVertices, ne = (size_t)numEdges;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    const size_t bOff = up(sizeof(int64_t) * n1), bKeyV = up(sizeof(unsigned long long) * nv),
+                 bKeyE = up(sizeof(unsigned long long) * ne), bEdgeN = up(sizeof(int) * ne),
+                 bVP = vertexPoints ? 0 : up(sizeof(int) * nv),
+                 bEP = edgePoints ? 0 : up(sizeof(int) * ne), bErr = up(sizeof(int) * 8),
+                 bCorner = up(sizeof(int4) * (size_t)numCorners);
+    size_t scanBytes = 0;
+    if ((st = check_cuda(cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (int64_t *)nullptr,
+                                                       (int64_t *)nullptr, (int)n1, s),
+                         who)) != GB300_OK)
+        return st;
+    char *mem = nullptr;
+    const size_t total =
+        2 * bOff + bCorner + bKeyV + bKeyE + bEdgeN + bVP + bEP + bErr + up(scanBytes);
+    if ((st = scratch_alloc((void **)&mem, total, s, who)) != GB300_OK) return st;
+    char *q = mem;
+    a.cornerOff = (int64_t *)q, q += bOff;
+    a.counts = (int64_t *)q, q += bOff;
+    a.cornerInfo = (int4 *)q, q += bCorner;
+    a.vertKey = (unsigned long long *)q, q += bKeyV;
+    a.edgeKey = (unsigned long long *)q, q += bKeyE;
+    a.edgeN = (int *)q, q += bEdgeN;
+    a.vertPoint = vertexPoints ? vertexPoints : (int *)q, q += bVP;
+    a.edgePoint = edgePoints ? edgePoints : (int *)q, q += bEP;
+    a.err = (int *)q, q += bErr;
+    void *scan = q;
+
+    const int grid = grid_for((long long)n1, 256, 16);
+    const size_t most = n1 > nv ? (n1 > ne ? n1 : ne) : (nv > ne ? nv : ne);
+    k_share_init<<<grid_for((long long)most, 256, 16), 256, 0, s>>>(a);
+    count_launch();
+    st = check_launch(who);
+    if (st == GB300_OK)
+        st = check_cuda(cub::DeviceScan::ExclusiveSum(scan, scanBytes, a.counts, a.cornerOff,
+                                                      (int)n1, s),
+                        who);
+    if (st == GB300_OK) {
+        k_share_own<<<grid, 256, 0, s>>>(a);
+        count_launch();
+        k_share_count<<<grid, 256, 0, s>>>(a);
+        count_launch();
+        st = check_launch(who);
+    }
+    if (st == GB300_OK)
+        st = check_cuda(cub::DeviceScan::ExclusiveSum(scan, scanBytes, a.counts, pointOffsets,
+                                                      (int)n1, s),
+                        who);
+    if (st == GB300_OK && numFaces > 0) {
+        k_share_assign<<<grid, 256, 0, s>>>(a);
+        count_launch();
+        k_share_corners<<<grid, 256, 0, s>>>(a);
+        count_launch();
+        const int blocks = grid_for((long long)numFaces * 32, 256, 8);
+        if (o.fs == 4)
+            k_share_emit<4><<<blocks, 256, 0, s>>>(a);
+        else
+            k_share_emit<3><<<blocks, 256, 0, s>>>(a);
+        count_launch();
+        st = check_launch(who);
+    }
+    int host[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    if (st == GB300_OK) {
+        k_share_totals<<<1, 32, 0, s>>>(a);
+        count_launch();
+        st = check_launch(who);
+    }
+    if (st == GB300_OK)
+        st = check_cuda(cudaMemcpyAsync(host, a.err, sizeof(host), cudaMemcpyDeviceToHost, s), who);
+    scratch_free(mem, s);
+    if (st == GB300_OK) st = check_cuda(cudaStreamSynchronize(s), who);
+    if (st != GB300_OK) return st;
+    int64_t points = 0, corners = 0;
+    std::memcpy(&points, host + 4, sizeof(points));
+    std::memcpy(&corners, host + 6, sizeof(corners));
+    if (corners != numCorners)
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "%s: the face sizes add up to %lld corners, the face vertices and edges "
+                    "have %lld", who, (long long)corners, (long long)numCorners);
+    if (host[0])
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "%s: %d vertex, edge or facet indices out of range, or faces whose coords "
+                    "disagree with Count (first in face %d)", who, host[0], host[1]);
+    if (host[2])
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "%s: %d face edges run at another rate than the face that made the edge's "
+                    "points (first in face %d): shared points need one rate per edge",
+                    who, host[2], host[3]);
+    *numPoints = points;
+    return ok();
 }

@@ -435,3 +435,31 @@ def bfr_tess_bytes(n_faces, n_coords, n_facets, facet_size, locate=True, uniform
     per_face = 4 + 3 * 8 * 2 + (0 if uniform else 4 * 5)
     return (per_face * n_faces + 8 * n_coords + (20 * n_coords if locate else 0)
             + 4 * facet_size * n_facets)
+
+
+def face_edges(verts_per_face, face_verts):
+    """Edge index of every face corner (the edge from corner i to corner i + 1), undirected
+    edges numbered in order of first appearance, and the number of edges: the base level's
+    face edges (Far::TopologyLevel::GetFaceEdges) for a mesh given as face vertices.  Shared
+    tessellation points depend only on which corners name the same edge, not on its number."""
+    vpf = np.asarray(verts_per_face, np.int64)
+    fv = np.asarray(face_verts, np.int64)
+    start = np.concatenate([[0], np.cumsum(vpf)])
+    nxt = np.arange(len(fv)) + 1
+    has = vpf > 0
+    nxt[start[1:][has] - 1] = start[:-1][has]
+    b = fv[nxt] if len(fv) else fv
+    key = np.minimum(fv, b) * (int(fv.max(initial=0)) + 1) + np.maximum(fv, b)
+    _, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    rank = np.empty(len(first), np.int64)
+    rank[np.argsort(first)] = np.arange(len(first))
+    return rank[inv].astype(np.int32), len(first)
+
+
+def bfr_share_bytes(n_faces, n_corners, n_vertices, n_edges, n_facets, n_points, facet_size):
+    """Algorithmic bytes of the shared-point pass: per face its size and three offsets; per
+    corner its vertex and edge, read once; per vertex a 64-bit claim and its point, per edge a
+    64-bit claim, its inside count and first point; per facet its indices read and rewritten;
+    per point the source PatchCoord read and the point's PatchCoord written."""
+    return (4 * n_faces + 3 * 8 * (n_faces + 1) + 8 * n_corners + 12 * n_vertices
+            + 16 * n_edges + 2 * 4 * facet_size * n_facets + 40 * n_points)

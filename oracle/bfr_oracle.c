@@ -942,3 +942,102 @@ int orc_tess_locate_mesh(int regFaceSize, int numFaces, const int *faceSizes,
     }
     return bad == 0;
 }
+
+/* Shared (watertight) points of a mesh tessellation: the bookkeeping of the reference's
+ * tessellation with shared vertex and edge points (tutorials/bfr/tutorial_2_2/
+ * bfr_tutorial_2_2.cpp:244-430), with per-face rates.  Faces in order, faces without coords
+ * skipped.  Walking the corners of a face, the first face to reach a mesh vertex makes its
+ * vertex coord a new point; the first face to reach a mesh edge makes the rate - 1 coords
+ * inside the edge new points, numbered in its own direction along the edge; later faces reuse
+ * those points, reversed where they run the edge from its other end (the tutorial reverses
+ * for every later face, which is the same on the manifold, consistently oriented meshes it
+ * accepts).  All interior coords of a face are new.  Points are numbered in the order made.
+ * Each facet index (a coord of its face: mesh-wide when meshIndices, else face-local) becomes
+ * the index of its point, as Tessellation::TransformFacetCoordIndices(facets,
+ * boundaryIndices, interiorOffset) maps it (tessellation.cpp:2449-2464); -1 stays -1.
+ * pointOffsets[f] = the first point face f made (numFaces + 1 entries); pointSources[p] = the
+ * mesh coord the point was made from.  Returns the number of points, -1 - f when face f runs
+ * an edge at another rate than the face that made the edge's points, or -1 - numFaces for a
+ * vertex or edge index out of range. */
+long orc_tess_share(int regFaceSize, int numFaces, const int *faceSizes, const int *faceVerts,
+                    const int *faceEdges, int numVertices, int numEdges, const int *rateOffsets,
+                    const int *rates, int facetSize, int preserveQuads, const long *coordOffsets,
+                    const long *facetOffsets, int facetStride, int meshIndices, int *facets,
+                    long *pointOffsets, long *pointSources) {
+    int fs = (facetSize == 4) ? 4 : 3;
+    int fst = facetStride ? facetStride : fs;
+    long *vpt = (long *)malloc(sizeof(long) * (size_t)(numVertices > 0 ? numVertices : 1));
+    long *efirst = (long *)malloc(sizeof(long) * (size_t)(numEdges > 0 ? numEdges : 1));
+    int *ecount = (int *)malloc(sizeof(int) * (size_t)(numEdges > 0 ? numEdges : 1));
+    int *estart = (int *)malloc(sizeof(int) * (size_t)(numEdges > 0 ? numEdges : 1));
+    for (int v = 0; v < numVertices; ++v) vpt[v] = -1;
+    for (int e = 0; e < numEdges; ++e) efirst[e] = -1;
+    long next = 0, corner = 0, result = 0;
+    long *bidx = NULL;
+    size_t bcap = 0;
+    for (int f = 0; f < numFaces && result == 0; ++f) {
+        int N = faceSizes[f];
+        long c0 = coordOffsets[f], nc = coordOffsets[f + 1] - c0;
+        pointOffsets[f] = next;
+        const int *fv = faceVerts + corner, *fe = faceEdges + corner;
+        corner += N;
+        if (nc == 0) continue;
+        Tess t;
+        tess_init(&t, regFaceSize, N, rateOffsets[f + 1] - rateOffsets[f], rates + rateOffsets[f],
+                  fs, preserveQuads);
+        int nb = t.nBoundary;
+        if ((size_t)nb > bcap) {
+            bcap = (size_t)nb;
+            bidx = (long *)realloc(bidx, sizeof(long) * bcap);
+        }
+        int k = 0;
+        for (int i = 0; i < N && result == 0; ++i) {
+            int v = fv[i], e = fe[i], n = t.outer[i] - 1;
+            if (v < 0 || v >= numVertices || e < 0 || e >= numEdges) {
+                result = -1 - (long)numFaces;
+                break;
+            }
+            if (vpt[v] < 0) {
+                vpt[v] = next;
+                pointSources[next++] = c0 + k;
+            }
+            bidx[k++] = vpt[v];
+            if (efirst[e] < 0) {
+                efirst[e] = next, ecount[e] = n, estart[e] = v;
+                for (int j = 0; j < n; ++j) {
+                    pointSources[next] = c0 + k;
+                    bidx[k++] = next++;
+                }
+            } else if (ecount[e] != n) {
+                result = -1 - (long)f;
+            } else {
+                int rev = estart[e] != v;
+                for (int j = 0; j < n; ++j) bidx[k++] = efirst[e] + (rev ? n - 1 - j : j);
+            }
+        }
+        if (result == 0) {
+            long interiorOffset = next - nb;
+            for (long j = nb; j < nc; ++j) pointSources[next++] = c0 + j;
+            long nfac = facetOffsets[f + 1] - facetOffsets[f];
+            int *F = facets + (long)fst * facetOffsets[f];
+            for (long q = 0; q < nfac; ++q)
+                for (int j = 0; j < fs; ++j) {
+                    int *x = F + q * fst + j;
+                    if (*x < 0) continue;
+                    long local = *x - (meshIndices ? c0 : 0);
+                    *x = (int)(local < nb ? bidx[local] : local + interiorOffset);
+                }
+        }
+        free(t.outer);
+    }
+    if (result == 0) {
+        pointOffsets[numFaces] = next;
+        result = next;
+    }
+    free(bidx);
+    free(vpt);
+    free(efirst);
+    free(ecount);
+    free(estart);
+    return result;
+}

@@ -296,6 +296,54 @@ def tess_locate_mesh(reg_face_size, face_sizes, coord_offsets, ptex_offsets, coo
     return faces, st
 
 
+def tess_share(reg_face_size, face_sizes, face_verts, face_edges, num_vertices, num_edges,
+               rate_offsets, rates, coord_offsets, facet_offsets, facets, facet_size=3,
+               preserve_quads=False, mesh_indices=True):
+    """Shared (watertight) points of a mesh tessellation (the reference's tutorial 2.2
+    bookkeeping): (facets rewritten to point indices, point_offsets [faces + 1],
+    point_sources [points] = the mesh coord each point was made from)."""
+    face_sizes = np.ascontiguousarray(face_sizes, np.int32)
+    fv = np.ascontiguousarray(face_verts, np.int32)
+    fe = np.ascontiguousarray(face_edges, np.int32)
+    ro = np.ascontiguousarray(rate_offsets, np.int32)
+    rates = np.ascontiguousarray(rates, np.int32)
+    co = np.ascontiguousarray(coord_offsets, np.int64)
+    fo = np.ascontiguousarray(facet_offsets, np.int64)
+    fs = 4 if facet_size == 4 else 3
+    out = np.array(facets, np.int32, copy=True).reshape(-1, fs)
+    nf = len(face_sizes)
+    po = np.zeros(nf + 1, np.int64)
+    src = np.zeros(max(int(co[-1]), 1), np.int64)
+    L = lib()
+    L.orc_tess_share.restype = C.c_long
+    n = L.orc_tess_share(C.c_int(reg_face_size), C.c_int(nf), _p(face_sizes), _p(fv), _p(fe),
+                         C.c_int(num_vertices), C.c_int(num_edges), _p(ro), _p(rates),
+                         C.c_int(fs), C.c_int(int(preserve_quads)), _p(co), _p(fo), C.c_int(fs),
+                         C.c_int(int(mesh_indices)), _p(out), _p(po), _p(src))
+    if n < -nf:
+        raise ValueError("vertex or edge index out of range")
+    if n < 0:
+        raise ValueError(f"face {-1 - n} runs a shared edge at another rate")
+    return out, po, src[:n]
+
+
+def edge_numbering(face_sizes, face_verts):
+    """One index per undirected edge (numbered in order of first appearance) for every face
+    corner -- the edge from corner i to corner i + 1 -- and the number of edges.  Any
+    consistent numbering gives the same shared points."""
+    face_sizes = np.asarray(face_sizes, np.int64)
+    fv = np.asarray(face_verts, np.int64)
+    start = np.concatenate([[0], np.cumsum(face_sizes)])
+    nxt = np.arange(len(fv)) + 1
+    last = start[1:] - 1
+    nxt[last[face_sizes > 0]] = start[:-1][face_sizes > 0]
+    a, b = fv, fv[nxt] if len(fv) else fv
+    key = np.minimum(a, b) * (int(fv.max(initial=0)) + 1) + np.maximum(a, b)
+    _, first, inv = np.unique(key, return_index=True, return_inverse=True)
+    order = np.argsort(np.argsort(first))
+    return order[inv].astype(np.int32), len(first)
+
+
 # ---- draw-time tessellation factors (tess_factors_oracle.c) --------------------------------
 
 def tess_factors(arrays, indices, params, src, src_stride, tess_level, max_tess_level=64.0,

@@ -131,6 +131,17 @@ int orc_tess_locate_mesh(int regFaceSize, int numFaces, const int *faceSizes,
                          const long *coordOffsets, const long *ptexOffsets, const float *coords,
                          int *ptexFaces, float *st, int threads);
 
+/* Shared (watertight) points of a mesh tessellation (tutorials/bfr/tutorial_2_2/
+ * bfr_tutorial_2_2.cpp:244-430): facets (written by orc_tess_mesh when meshIndices, else
+ * face-local) rewritten in place to point indices; pointOffsets (numFaces + 1) and
+ * pointSources (one mesh coord per point, capacity = the number of coords).  Returns the
+ * number of points, or a negative code (bfr_oracle.c). */
+long orc_tess_share(int regFaceSize, int numFaces, const int *faceSizes, const int *faceVerts,
+                    const int *faceEdges, int numVertices, int numEdges, const int *rateOffsets,
+                    const int *rates, int facetSize, int preserveQuads, const long *coordOffsets,
+                    const long *facetOffsets, int facetStride, int meshIndices, int *facets,
+                    long *pointOffsets, long *pointSources);
+
 /* ---- draw-time tessellation factors (tess_factors_oracle.c) ---- */
 
 /* Per-patch tess levels of the patch shaders (osd/glslPatchCommonTess.glsl:92-550): outer[4],

@@ -422,3 +422,24 @@ def bfr_mesh_record(refiner, positions, rate_offsets, rates, facet_size=3, prese
         return out
     finally:
         L.ref_bfr_record_destroy(h)
+
+
+def bfr_share(refiner, rate_offsets, rates, num_coords, num_facets, facet_size=3,
+              preserve_quads=False, approx_sharp=6, approx_smooth=2):
+    """The reference's tessellation with shared vertex and edge points (tutorial 2.2 loop):
+    (facets [m, facet_size] of point indices, point_offsets [faces + 1], point_sources
+    [points] = the coord of bfr_mesh_record's numbering each point is evaluated at)."""
+    L = lib()
+    L.ref_bfr_share.restype = C.c_long
+    ro = np.ascontiguousarray(rate_offsets, np.int32)
+    rt = np.ascontiguousarray(rates, np.int32)
+    fs = 4 if facet_size == 4 else 3
+    facets = np.zeros((num_facets, fs), np.int32)
+    po = np.zeros(len(ro), np.int64)
+    src = np.zeros(max(num_coords, 1), np.int64)
+    n = L.ref_bfr_share(refiner.h, C.c_int(approx_sharp), C.c_int(approx_smooth), _p(ro),
+                        _p(rt), C.c_int(fs), C.c_int(int(preserve_quads)), _p(facets), _p(po),
+                        _p(src))
+    if n < 0:
+        raise ValueError("non-manifold or mismatched shared edge")
+    return facets, po, src[:n]

@@ -990,4 +990,76 @@ void ref_bfr_record_copy(void *p, long *coordOffsets, long *facetOffsets, int *v
 
 void ref_bfr_record_destroy(void *p) { delete (BfrRecord *)p; }
 
+// The tessellation with shared vertex and edge points of the reference's tutorial 2.2
+// (tutorials/bfr/tutorial_2_2/bfr_tutorial_2_2.cpp:160-430), with per-face rates: faces in
+// order through Bfr::RefinerSurfaceFactory (faces without a limit surface skipped), the
+// boundary coords of each Bfr::Tessellation walked vertex by vertex and edge by edge against
+// the base level's face vertices and edges; the point of a vertex, and the points inside an
+// edge, are made by the first face to reach them and reused, edge points in reverse, by the
+// later face; the facets are mapped through Tessellation::TransformFacetCoordIndices(facets,
+// boundaryIndices, interiorOffset).  Writes the facets (point indices) in the order of
+// ref_bfr_mesh_record, pointOffsets (faces + 1: the first point each face made) and, per
+// point, the mesh coord (ref_bfr_mesh_record's numbering) it is evaluated at.  Returns the
+// number of points; -1 for a shared edge that is non-manifold or has another rate.
+long ref_bfr_share(void *refiner, int approxSharp, int approxSmooth, const int *rateOffsets,
+                   const int *rates, int facetSize, int preserveQuads, int *facets,
+                   long *pointOffsets, long *pointSources) {
+    Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
+    Far::TopologyLevel const &base = mesh.GetLevel(0);
+    Bfr::SurfaceFactory::Options so;
+    so.SetApproxLevelSharp(approxSharp);
+    so.SetApproxLevelSmooth(approxSmooth);
+    Bfr::RefinerSurfaceFactory<> factory(mesh, so);
+    const int nf = factory.GetNumFaces();
+    const int fs = facetSize == 4 ? 4 : 3;
+    Bfr::Tessellation::Options to = tessOptions(fs, preserveQuads);
+    std::vector<long> vertPoint(base.GetNumVertices(), -1), edgePoint(base.GetNumEdges(), -1);
+    std::vector<int> edgeCount(base.GetNumEdges(), 0);
+    std::vector<int> boundary, local;
+    Bfr::Surface<float> sf;
+    long points = 0, coords = 0, facetsDone = 0;
+    for (int f = 0; f < nf; ++f) {
+        pointOffsets[f] = points;
+        if (!factory.InitVertexSurface(f, &sf)) continue;
+        Bfr::Tessellation t(sf.GetParameterization(), rateOffsets[f + 1] - rateOffsets[f],
+                            rates + rateOffsets[f], to);
+        if (!t.IsValid()) continue;
+        Far::ConstIndexArray fv = base.GetFaceVertices(f), fe = base.GetFaceEdges(f);
+        boundary.resize(t.GetNumBoundaryCoords());
+        int b = 0;
+        for (int i = 0; i < fv.size(); ++i) {
+            long &vp = vertPoint[fv[i]];
+            if (vp < 0) {
+                vp = points;
+                pointSources[points++] = coords + b;
+            }
+            boundary[b++] = (int)vp;
+            const int n = t.GetNumEdgeCoords(i);
+            if (n < 1) continue;
+            long &ep = edgePoint[fe[i]];
+            if (ep < 0) {
+                ep = points;
+                edgeCount[fe[i]] = n;
+                for (int j = 0; j < n; ++j) {
+                    pointSources[points] = coords + b;
+                    boundary[b++] = (int)points++;
+                }
+            } else {
+                if (base.IsEdgeNonManifold(fe[i]) || edgeCount[fe[i]] != n) return -1;
+                for (int j = 0; j < n; ++j) boundary[b++] = (int)(ep + n - 1 - j);
+            }
+        }
+        const int nc = t.GetNumCoords(), ni = t.GetNumInteriorCoords();
+        for (int j = 0; j < ni; ++j) pointSources[points++] = coords + b + j;
+        local.resize((size_t)t.GetNumFacets() * fs);
+        t.GetFacets(local.data());
+        t.TransformFacetCoordIndices(local.data(), boundary.data(), (int)(points - nc));
+        std::copy(local.begin(), local.end(), facets + facetsDone * fs);
+        facetsDone += t.GetNumFacets();
+        coords += nc;
+    }
+    pointOffsets[nf] = points;
+    return points;
+}
+
 }  // extern "C"

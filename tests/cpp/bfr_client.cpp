@@ -2,10 +2,12 @@
 // Bfr tutorials (tutorials/bfr/tutorial_1_2/bfr_tutorial_1_2.cpp:170-238) for every face of a
 // mesh at once -- GB300MeshTessellation (per-face rates, mesh-wide facet indices, PatchCoords on
 // a device patch table), its Evaluate (Surface::Evaluate: P and all five derivatives), and the
-// same coords through GB300Evaluator::EvalPatches (P, Du, Dv).
+// same coords through GB300Evaluator::EvalPatches (P, Du, Dv); then the shared (watertight)
+// points of the reference's tutorial 2.2 (GB300MeshTessellation::Share + EvaluatePoints).
 //
 // usage: bfr_client <dir>  (reads *.bin written by the test; writes coords.bin, facets.bin,
-//                           patch_coords.bin, p{k}.bin for k = 0..5, g{k}.bin for k = 0..2)
+//                           patch_coords.bin, p{k}.bin for k = 0..5, g{k}.bin for k = 0..2,
+//                           shared_facets.bin, point_offsets.bin, point_p.bin)
 #include <opensubdiv_gb300/bfr/gb300Tessellation.h>
 
 #include <cuda_runtime.h>
@@ -104,7 +106,39 @@ int main(int argc, char **argv) {
         std::fprintf(stderr, "EvalPatches failed: %s\n", GB300GetLastErrorString());
         return 1;
     }
+    // shared (watertight) points: the reference's tutorial 2.2 bookkeeping on a copy of the
+    // facets, each point evaluated once
+    auto faceVerts = read<int>(dir + "/face_verts.bin");
+    auto faceEdges = read<int>(dir + "/face_edges.bin");
+    auto topo = read<int>(dir + "/topology.bin");  // vertices, edges
+    int *dVerts = upload(faceVerts), *dEdges = upload(faceEdges), *shared = nullptr;
+    int64_t *pointOffsets = nullptr;
+    Osd::PatchCoord *pointCoords = nullptr;
+    const size_t facetInts = (size_t)tess->GetFacetStride() * nf;
+    cudaMalloc(&shared, sizeof(int) * facetInts);
+    cudaMemcpy(shared, facets, sizeof(int) * facetInts, cudaMemcpyDeviceToDevice);
+    cudaMalloc(&pointOffsets, sizeof(int64_t) * (size_t)(numFaces + 1));
+    cudaMalloc(&pointCoords, sizeof(Osd::PatchCoord) * (size_t)n);
+    const int64_t numPoints = tess->Share(dVerts, dEdges, (int64_t)faceVerts.size(), topo[0],
+                                          topo[1], shared, pc.d, pointOffsets, pointCoords);
+    if (numPoints < 0) {
+        std::fprintf(stderr, "Share failed: %s\n", GB300GetLastErrorString());
+        return 1;
+    }
+    Osd::GB300VertexBuffer *sp = Osd::GB300VertexBuffer::Create(3, (int)numPoints);
+    if (!tess->EvaluatePoints(table, pointCoords, (int)numPoints, vsrc->BindCudaBuffer(), 3, 3,
+                              sp->BindCudaBuffer())) {
+        std::fprintf(stderr, "EvaluatePoints failed: %s\n", GB300GetLastErrorString());
+        return 1;
+    }
     cudaDeviceSynchronize();
+    write(dir + "/shared_facets.bin", shared, facetInts);
+    write(dir + "/point_offsets.bin", pointOffsets, (size_t)numFaces + 1);
+    write(dir + "/point_p.bin", sp->BindCudaBuffer(), 3 * (size_t)numPoints);
+    delete sp;
+    cudaFree(shared);
+    cudaFree(pointOffsets);
+    cudaFree(pointCoords);
     write(dir + "/coords.bin", coords, 2 * (size_t)n);
     write(dir + "/facets.bin", facets, (size_t)tess->GetFacetStride() * nf);
     write(dir + "/patch_coords.bin", reinterpret_cast<int *>(pc.d), 5 * (size_t)n);

@@ -94,4 +94,37 @@ bool tessellateLikeTheTutorial(Far::TopologyRefiner &mesh, int const *deviceFace
     return ok;
 }
 
+// The reference's tutorial 2.2 (tutorials/bfr/tutorial_2_2/bfr_tutorial_2_2.cpp:160-430):
+// the same tessellation with the points of mesh vertices and edges shared between faces --
+// the base level's face vertices and edges go to the device, Share rewrites the facets to
+// shared point indices and each point is evaluated once.
+long long tessellateWatertight(Far::TopologyRefiner &mesh, int const *deviceFaceSizes,
+                               int tessUniformRate, float *coords, int *facets,
+                               PatchCoordBuffer *coordsOut, Osd::PatchCoord *points,
+                               int64_t *pointOffsets) {
+    Far::PatchTable const *farTable = Bfr::GB300CreateSurfacePatchTable(mesh);
+    const int regularFaceSize = Sdc::SchemeTypeTraits::GetRegularFaceSize(mesh.GetSchemeType());
+    Osd::GB300PatchTable *table = Osd::GB300PatchTable::Create(farTable);
+    Bfr::GB300MeshTessellation *tess = Bfr::GB300MeshTessellation::Create(
+        regularFaceSize, mesh.GetLevel(0).GetNumFaces(), deviceFaceSizes, tessUniformRate);
+    std::vector<int> faceVerts, faceEdges;
+    Bfr::GB300GetFaceVerticesAndEdges(mesh, faceVerts, faceEdges);
+    int *dv = nullptr, *de = nullptr;
+    cudaMalloc(&dv, sizeof(int) * faceVerts.size());
+    cudaMalloc(&de, sizeof(int) * faceEdges.size());
+    cudaMemcpy(dv, faceVerts.data(), sizeof(int) * faceVerts.size(), cudaMemcpyHostToDevice);
+    cudaMemcpy(de, faceEdges.data(), sizeof(int) * faceEdges.size(), cudaMemcpyHostToDevice);
+    long long n = -1;
+    if (table && tess && tess->Generate(coords, facets, true, table, coordsOut->d))
+        n = tess->Share(dv, de, (int64_t)faceVerts.size(), mesh.GetLevel(0).GetNumVertices(),
+                        mesh.GetLevel(0).GetNumEdges(), facets, coordsOut->d, pointOffsets,
+                        points);
+    cudaFree(dv);
+    cudaFree(de);
+    delete tess;
+    delete table;
+    delete farTable;
+    return n;
+}
+
 int main() { return 0; }

@@ -544,6 +544,31 @@ def bfr_fixtures():
                      seed=323, fvar=uv_seams(fltor, 12, 8) + (uv_grid(12, 8),))
 
 
+def bfr_share_fixture(path):
+    """The reference's tessellation with shared vertex and edge points (its tutorial 2.2
+    bookkeeping over Bfr::Tessellation, through ref_bfr_share) on the cage and rates of every
+    Bfr mesh fixture: per fixture the facets as point indices, the first point of each face
+    and the coord each point is evaluated at."""
+    out = {}
+    for name in sorted(os.listdir(HERE)):
+        if not (name.startswith("bfr_") and name.endswith(".npz")) or name == "bfr_share.npz" \
+                or name == "bfr_tess_patterns.npz":
+            continue
+        d = np.load(os.path.join(HERE, name))
+        cage = shapes.Cage(positions=d["positions"], verts_per_face=d["verts_per_face"],
+                           face_verts=d["face_verts"], scheme=int(d["scheme"]),
+                           crease_verts=d["crease_verts"], crease_sharpness=d["crease_sharpness"])
+        co, fo = d["coord_offsets"], d["facet_offsets"]
+        facets, po, src = ref.bfr_share(ref.Refiner(cage), d["rate_offsets"], d["rates"],
+                                        int(co[-1]), int(fo[-1]), int(d["facet_size"]),
+                                        bool(d["preserve_quads"]))
+        key = name[:-4]
+        out[key + "__facets"] = facets
+        out[key + "__point_offsets"] = po
+        out[key + "__point_sources"] = src
+    np.savez_compressed(path, **out)
+
+
 LARGE = os.path.join(HERE, "large")
 
 
@@ -632,6 +657,10 @@ def main():
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr":
         bfr_fixtures()
+        bfr_share_fixture(os.path.join(HERE, "bfr_share.npz"))
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "bfr-share":
+        bfr_share_fixture(os.path.join(HERE, "bfr_share.npz"))
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr-large":
         torus = shapes.torus(512, 256, R=1.0, r=0.3, tri_fraction=0.05, crease_fraction=0.02,

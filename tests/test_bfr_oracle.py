@@ -21,7 +21,7 @@ import oracle
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 MESHES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "bfr_*.npz"))
-                if not p.endswith("bfr_tess_patterns.npz"))
+                if not p.endswith(("bfr_tess_patterns.npz", "bfr_share.npz")))
 
 
 def bits(a):
@@ -172,3 +172,57 @@ def test_far_face_varying_patches_agree_with_bfr_uv_surfaces(path):
                                z["fvar_arrays"], z["fvar_indices"], z["fvar_params"], threads=4)
     for k, tol in enumerate((1e-4, 5e-4, 5e-4)):
         assert np.abs(outs[k].reshape(-1, 2) - z["uv3"][k]).max() <= tol, k
+
+
+SHARE = os.path.join(GOLDEN, "bfr_share.npz")
+
+
+def share_inputs(z):
+    """(face edges per corner, number of edges) for a mesh fixture: the oracle's own edge
+    numbering (shared points do not depend on how edges are numbered)."""
+    return oracle.edge_numbering(z["verts_per_face"], z["face_verts"])
+
+
+@pytest.mark.parametrize("path", MESHES, ids=os.path.basename)
+def test_shared_points_match_the_reference_tutorial(path):
+    """The shared-point bookkeeping (tutorial 2.2's, restated in oracle/bfr_oracle.c) against
+    the reference's own Tessellation + TransformFacetCoordIndices run through that loop
+    (tests/golden/bfr_share.npz): facets as point indices, each face's first point, and the
+    coord every point is evaluated at -- exactly; and every facet corner of a point lies where
+    that point's source coord lies (the two faces' coords name the same surface point)."""
+    z = np.load(path)
+    g = np.load(SHARE)
+    key = os.path.basename(path)[:-4]
+    fe, ne = share_inputs(z)
+    facets, po, src = oracle.tess_share(
+        int(z["regular_face_size"]), z["verts_per_face"], z["face_verts"], fe,
+        len(z["positions"]), ne, z["rate_offsets"], z["rates"], z["coord_offsets"],
+        z["facet_offsets"], z["facets"], int(z["facet_size"]), bool(z["preserve_quads"]))
+    assert np.array_equal(facets, g[key + "__facets"])
+    assert np.array_equal(po, g[key + "__point_offsets"])
+    assert np.array_equal(src, g[key + "__point_sources"])
+    # every point is used, and every coord maps to a point evaluated within the Bfr tolerance
+    fs = int(z["facet_size"])
+    used = np.zeros(len(src), bool)
+    used[facets[facets >= 0]] = True
+    assert used.all()
+    coord_of = z["facets"].reshape(-1, fs)
+    m = coord_of >= 0
+    p_coord = z["out6"][0][coord_of[m]]
+    p_point = z["out6"][0][src[facets[m]]]
+    ptol = bfr_tolerances(z["positions"])[0]
+    assert np.abs(p_coord - p_point).max() <= ptol
+
+
+def test_shared_points_reject_edges_with_two_rates():
+    """An edge run at two rates by its two faces cannot share its points: rejected (a face's
+    edge rates from edge lengths are always consistent)."""
+    sizes = np.array([4, 4], np.int32)
+    fv = np.array([0, 1, 4, 3, 1, 2, 5, 4], np.int32)
+    fe, ne = oracle.edge_numbering(sizes, fv)
+    ro = np.array([0, 4, 8], np.int32)
+    rates = np.array([2, 3, 2, 3, 2, 3, 2, 4], np.int32)  # shared edge 1-4: 3 vs 4
+    mesh = oracle.tess_mesh(4, sizes, ro, rates)
+    with pytest.raises(ValueError):
+        oracle.tess_share(4, sizes, fv, fe, 6, ne, ro, rates, mesh["coord_offsets"],
+                          mesh["facet_offsets"], mesh["facets"])

@@ -22,7 +22,7 @@ from gpu_util import bbox_diag, dev, gate, host, torch_cuda
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 MESHES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "bfr_*.npz"))
-                if not p.endswith("bfr_tess_patterns.npz"))
+                if not p.endswith(("bfr_tess_patterns.npz", "bfr_share.npz")))
 
 
 def bits(a):
@@ -254,3 +254,104 @@ def test_mesh_face_varying_uvs_match_bfr(path):
     for k, tol in enumerate((1e-4, 5e-4, 5e-4)):
         assert np.abs(outs[k] - z["uv3"][k]).max() <= tol, k
         assert np.abs(outs[k].ravel() - cpu[k]).max() <= 1e-5, k
+
+
+SHARE = os.path.join(GOLDEN, "bfr_share.npz")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", MESHES, ids=os.path.basename)
+@pytest.mark.parametrize("local", [False, True], ids=["mesh", "local"])
+def test_mesh_shared_points_match_the_reference_tutorial(path, local):
+    """Shared (watertight) points on the device (GB300TessellationShare) against the
+    reference's tutorial 2.2 loop (tests/golden/bfr_share.npz): facets as point indices and
+    each face's first point exactly; each point's PatchCoord, (u, v) and face copied from the
+    coord that made it; vertex and edge points as the oracle's bookkeeping numbers them; and
+    the points evaluated once each equal the per-coord evaluation bit for bit."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300PatchTable
+    z = np.load(path)
+    g = np.load(SHARE)
+    key = os.path.basename(path)[:-4]
+    reg = int(z["regular_face_size"])
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"],
+                                   bool(z["triangular"]))
+    opt = bfr.TessellationOptions(int(z["facet_size"]), bool(z["preserve_quads"]))
+    m = bfr.MeshTessellation(reg, z["verts_per_face"], rates=z["rates"],
+                             rate_offsets=z["rate_offsets"], options=opt)
+    c, f, pc = m.Generate(table=table, offset_facet_indices=not local)
+    fe, ne = oracle.edge_numbering(z["verts_per_face"], z["face_verts"])
+    nv = len(z["positions"])
+    coord_facets = host(f).copy()
+    sp = m.Share(z["face_verts"], fe, nv, ne, f, patch_coords=pc, coords=c,
+                 mesh_facet_indices=not local, point_coords=True, point_faces=True,
+                 vertex_points=True, edge_points=True)
+    src = g[key + "__point_sources"]
+    assert sp.num_points == len(src)
+    assert np.array_equal(host(f), g[key + "__facets"])
+    assert np.array_equal(host(sp.point_offsets), g[key + "__point_offsets"])
+    assert np.array_equal(host(sp.patch_coords), host(pc)[src])
+    assert np.array_equal(bits(host(sp.coords)), bits(host(c)[src]))
+    co = z["coord_offsets"]
+    assert np.array_equal(host(sp.faces), np.searchsorted(co, src, side="right") - 1)
+    # vertex points: the point every face corner's vertex coord maps to
+    fs = int(z["facet_size"])
+    cf = coord_facets.reshape(-1, fs)
+    pf = host(f).reshape(-1, fs)
+    if local:
+        fo = z["facet_offsets"]
+        owner = np.repeat(np.arange(len(co) - 1), np.diff(fo))
+        cf = np.where(cf >= 0, cf + co[owner][:, None], -1)
+    point_of_coord = np.full(int(co[-1]), -1, np.int64)
+    point_of_coord[cf[cf >= 0]] = pf[cf >= 0]
+    vp = host(sp.vertex_points)
+    starts = np.concatenate([[0], np.cumsum(z["verts_per_face"])])
+    for fi in range(len(co) - 1):
+        if co[fi + 1] == co[fi]:
+            continue
+        r = z["rates"][z["rate_offsets"][fi]:z["rate_offsets"][fi + 1]]
+        N = int(z["verts_per_face"][fi])
+        outer = np.broadcast_to(r[:N] if len(r) >= N else r[:1], (N,))
+        pos = co[fi] + np.concatenate([[0], np.cumsum(outer)[:-1]])
+        verts = z["face_verts"][starts[fi]:starts[fi + 1]]
+        assert np.array_equal(vp[verts], point_of_coord[pos]), fi
+    # evaluate each point once: equal to the evaluation at the coord that made it
+    per_coord = [host(o) for o in m.Evaluate(dev(z["src"]), BD(0, 3, 3), table, pc, 1)]
+    per_point = [host(o) for o in m.Evaluate(dev(z["src"]), BD(0, 3, 3), table,
+                                             sp.patch_coords, 1, num_points=sp.num_points)]
+    for k in range(3):
+        assert np.array_equal(bits(per_point[k]), bits(per_coord[k][src])), k
+
+
+@pytest.mark.gpu
+def test_shared_points_reject_bad_edges():
+    """Two rates on one shared edge, and vertex or edge indices out of range, are rejected
+    (the device checks every index before it uses it)."""
+    torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300._lib import GB300Error
+    sizes = np.array([4, 4], np.int32)
+    fv = np.array([0, 1, 4, 3, 1, 2, 5, 4], np.int32)
+    fe, ne = oracle.edge_numbering(sizes, fv)
+    ro = np.array([0, 4, 8], np.int32)
+    for rates, verts, edges, nedges in (
+            ([2, 3, 2, 3, 2, 3, 2, 4], fv, fe, ne),  # two rates on the shared edge
+            ([2, 3, 2, 3, 2, 3, 2, 3], fv, fe, ne - 1),  # an edge index out of range
+            ([2, 3, 2, 3, 2, 3, 2, 3], np.where(fv == 5, 6, fv), fe, ne),  # a vertex index
+            ([2, 3, 2, 3, 2, 3, 2, 3], fv[:-1], fe[:-1], ne)):  # fewer corners than sizes
+        m = bfr.MeshTessellation(4, sizes, rates=np.array(rates, np.int32), rate_offsets=ro)
+        _, f, _ = m.Generate()
+        with pytest.raises(GB300Error):
+            m.Share(verts, edges, 6, nedges, f)
+    # the consistent mesh shares the edge: 6 vertices + 4 * 2 + 3 * 1 edge points + interior
+    m = bfr.MeshTessellation(4, sizes, rates=np.array([2, 3, 2, 3] * 2, np.int32),
+                             rate_offsets=ro)
+    _, f, _ = m.Generate()
+    sp = m.Share(fv, fe, 6, ne, f)
+    mesh = oracle.tess_mesh(4, sizes, ro, np.array([2, 3, 2, 3] * 2, np.int32))
+    want, po, src = oracle.tess_share(4, sizes, fv, fe, 6, ne, ro, np.array([2, 3, 2, 3] * 2),
+                                      mesh["coord_offsets"], mesh["facet_offsets"],
+                                      mesh["facets"])
+    assert sp.num_points == len(src)
+    assert np.array_equal(host(f), want)

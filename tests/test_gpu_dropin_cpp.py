@@ -208,6 +208,11 @@ def test_cpp_bfr_client_tessellates_like_bfr(tmp_path, name):
         np.ascontiguousarray(z[k]).tofile(tmp_path / f"{k}.bin")
     np.array([int(z["regular_face_size"]), int(z["facet_size"]), int(z["preserve_quads"]),
               int(z["triangular"])], np.int32).tofile(tmp_path / "options.bin")
+    import oracle
+    fe, ne = oracle.edge_numbering(z["verts_per_face"], z["face_verts"])
+    np.ascontiguousarray(z["face_verts"], np.int32).tofile(tmp_path / "face_verts.bin")
+    np.ascontiguousarray(fe, np.int32).tofile(tmp_path / "face_edges.bin")
+    np.array([len(z["positions"]), ne], np.int32).tofile(tmp_path / "topology.bin")
     exe = _build(tmp_path, "bfr_client")
     r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
@@ -226,3 +231,14 @@ def test_cpp_bfr_client_tessellates_like_bfr(tmp_path, name):
         if k < 3:  # the general EvalPatches entry on the same coords
             g = np.fromfile(tmp_path / f"g{k}.bin", np.float32).reshape(n, 3)
             assert np.abs(g.astype(np.float64) - z["out6"][k]).max() <= tol, k
+    # shared points: the reference's tutorial 2.2 facets and numbering, P once per point
+    share = np.load(os.path.join(GOLDEN, "bfr_share.npz"))
+    key = name[:-4]
+    sf = np.fromfile(tmp_path / "shared_facets.bin", np.int32).reshape(z["facets"].shape)
+    assert np.array_equal(sf, share[key + "__facets"])
+    po = np.fromfile(tmp_path / "point_offsets.bin", np.int64)
+    assert np.array_equal(po, share[key + "__point_offsets"])
+    src = share[key + "__point_sources"]
+    pp = np.fromfile(tmp_path / "point_p.bin", np.float32).reshape(len(src), 3)
+    p0 = np.fromfile(tmp_path / "p0.bin", np.float32).reshape(n, 3)
+    assert np.array_equal(pp.view(np.int32), p0[src].view(np.int32))

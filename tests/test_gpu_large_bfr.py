@@ -58,3 +58,35 @@ def test_full_mesh_rate5_against_oracle_and_bfr_sample():
     for k, tol in enumerate((ptol, 5 * ptol, 5 * ptol)):
         err = np.abs(outs[k][idx].astype(np.float64) - z["sample_out3"][k]).max()
         assert err <= tol, (k, err, tol)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", ["uniform5", "edge_lengths"])
+def test_full_mesh_shared_points_against_oracle(mode):
+    """Shared (watertight) points of every face of the torus, at the uniform rate and at
+    edge-length rates: facets, first points and point sources equal the oracle's bookkeeping
+    (pinned to the reference's tutorial 2.2 loop by tests/test_bfr_oracle.py) exactly."""
+    if not os.path.exists(PATH):
+        pytest.skip("torus512x256_bfr.npz is written where the reference is available")
+    torch_cuda()
+    from opensubdiv_gb300 import bfr, workloads
+    from opensubdiv_gb300.evaluator import GB300PatchTable
+    z = np.load(PATH)
+    sizes, fv = z["verts_per_face"], z["face_verts"]
+    nf = len(sizes)
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"], False)
+    if mode == "uniform5":
+        ro, rates = np.arange(nf + 1, dtype=np.int32), np.full(nf, int(z["rate"]), np.int32)
+    else:
+        ro, rates = workloads.bfr_edge_length_rates(z["positions"], sizes, fv, 0.0022)
+    m = bfr.MeshTessellation(4, sizes, rates=rates, rate_offsets=ro)
+    c, f, pc = m.Generate(table=table)
+    t = oracle.tess_mesh(4, sizes, ro, rates, 3, False, threads=16)
+    fe, ne = oracle.edge_numbering(sizes, fv)
+    sp = m.Share(fv, fe, len(z["positions"]), ne, f, patch_coords=pc)
+    want, po, src = oracle.tess_share(4, sizes, fv, fe, len(z["positions"]), ne, ro, rates,
+                                      t["coord_offsets"], t["facet_offsets"], t["facets"])
+    assert sp.num_points == len(src)
+    assert np.array_equal(host(f), want)
+    assert np.array_equal(host(sp.point_offsets), po)
+    assert np.array_equal(host(sp.patch_coords), host(pc)[src])
