@@ -485,7 +485,8 @@ def bench_bfr(args, stream, peak):
                                "achieved": share_b / (share_ms / 1e3) / 1e9, "peak": peak,
                                "unit": "GB/s", "frac": share_b / (share_ms / 1e3) / 1e9 / peak,
                                "note": "share_ms is the whole call, including its host read of "
-                                       "the point total"},
+                                       "the point total",
+                               "traffic_emit": ncu_traffic("bfr_share_emit")},
             "roofline_eval": {"bound": "hbm", "algorithmic_bytes": peval_b,
                               "achieved": peval_b / (peval_ms / 1e3) / 1e9, "peak": peak,
                               "unit": "GB/s", "frac": peval_b / (peval_ms / 1e3) / 1e9 / peak},
