@@ -186,6 +186,30 @@ public:
                                                   pointCoords, stream) == GB300_OK;
     }
 
+    /// Bfr::Surface::EvaluateStencil at `numPoints` PatchCoords (those of Generate, or the
+    /// shared points of Share; GB300TessellationStencils): a limit stencil table over the
+    /// mesh's control vertices -- P and, with numChannels 3, Du and Dv (6: also the second
+    /// derivatives) -- for Osd::GB300Evaluator::EvalStencils each frame, with no refinement.
+    /// `pointStencils`: one stencil per point the patch indices name (control vertices first,
+    /// then refined and local points: Far::StencilTableFactory with generateControlVerts plus
+    /// Far::PatchTable::GetLocalPointStencilTable appended, as LimitStencilTableFactory
+    /// builds it).  The caller owns the result; NULL on failure.
+    static Osd::GB300StencilTable *EvaluateStencils(Osd::GB300PatchTable const *table,
+                                                    Osd::PatchCoord const *patchCoords,
+                                                    int numPoints,
+                                                    Osd::GB300StencilTable const *pointStencils,
+                                                    int numChannels = 3, void *stream = NULL) {
+        if (!table || !pointStencils) return NULL;
+        ::GB300StencilTable *h = GB300TessellationStencils(
+            table->GetHandle(), numPoints, patchCoords, pointStencils->GetNumStencils(),
+            GB300StencilTableGetNumIndices(pointStencils->GetHandle()),
+            (int const *)pointStencils->GetSizesBuffer(),
+            (int const *)pointStencils->GetOffsetsBuffer(),
+            (int const *)pointStencils->GetIndicesBuffer(),
+            (float const *)pointStencils->GetWeightsBuffer(), numChannels, 1, stream);
+        return Osd::GB300StencilTable::Adopt(h);
+    }
+
 private:
     GB300MeshTessellation() {}
 

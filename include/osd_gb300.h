@@ -377,6 +377,26 @@ int GB300TessellationShare(int regularFaceSize, int numFaces, const int *faceSiz
                            int *pointFaces, int *vertexPoints, int *edgePoints,
                            int64_t *numPoints, void *stream);
 
+/* Bfr::Surface::EvaluateStencil (bfr/surface.h:244-265) at every point: one limit stencil per
+ * PatchCoord (DEVICE, 5 x 32 bits each, e.g. located by GB300TessellationGenerate or shared by
+ * GB300TessellationShare) over the mesh's control vertices, so that GB300EvalStencils /
+ * GB300StencilTableEval evaluate the points straight from the control vertices, frame after
+ * frame, without refining.  The base table (DEVICE arrays in Far's layout: sizes / offsets per
+ * stencil, indices, weights) holds one stencil per point the patch indices name, in their
+ * numbering: the control vertices first (identity rows), then the refined and local points --
+ * Far::StencilTableFactory with generateControlVerts plus AppendLocalPointStencilTable, as
+ * Far::LimitStencilTableFactory builds it (far/stencilTableFactory.cpp:411-662).  Each point's
+ * stencil merges the basis weights of its patch's control points (P; with numChannels 3 also
+ * Du, Dv; with 6 the second derivatives) times their base stencils, in first-touch order, as
+ * LimitStencilTableFactory merges its per-location masks.  sortEntries as in
+ * GB300StencilTableComposeRows.  Returns NULL on failure (status recorded). */
+GB300StencilTable *GB300TessellationStencils(const GB300PatchTable *table, int numPoints,
+                                             const void *patchCoords, int baseNumStencils,
+                                             int64_t baseNumIndices, const int *baseSizes,
+                                             const int *baseOffsets, const int *baseIndices,
+                                             const float *baseWeights, int numChannels,
+                                             int sortEntries, void *stream);
+
 /* ---- draw-time tessellation factors (osd/glslPatchCommonTess.glsl:92-760) ------------------ */
 
 /* The tess-control settings of OpenSubdiv's patch shaders.  tessLevel: OsdTessLevel();

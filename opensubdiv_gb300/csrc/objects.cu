@@ -526,6 +526,25 @@ int GB300TessellationEvaluate(const GB300PatchTable *t, const float *src, float 
                         "GB300TessellationEvaluate", t->quadFamily, 1);
 }
 
+GB300StencilTable *GB300TessellationStencils(const GB300PatchTable *t, int numPoints,
+                                             const void *patchCoords, int baseNumStencils,
+                                             int64_t baseNumIndices, const int *baseSizes,
+                                             const int *baseOffsets, const int *baseIndices,
+                                             const float *baseWeights, int numChannels,
+                                             int sortEntries, void *stream) {
+    const char *who = "GB300TessellationStencils";
+    if (!t || numPoints < 0 || (numPoints > 0 && !patchCoords) || baseNumStencils < 0 ||
+        baseNumIndices < 0 || (baseNumStencils > 0 && (!baseSizes || !baseOffsets)) ||
+        (baseNumIndices > 0 && (!baseIndices || !baseWeights)) ||
+        !(numChannels == 1 || numChannels == 3 || numChannels == 6)) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
+        return nullptr;
+    }
+    return tess_stencils(t->arrays, (const int *)t->indices, t->params, numPoints, patchCoords,
+                         baseNumStencils, baseNumIndices, baseSizes, baseOffsets, baseIndices,
+                         baseWeights, numChannels, sortEntries, as_stream(stream), who);
+}
+
 int GB300PatchTableTessFactors(const GB300PatchTable *t, const float *src, int srcStride,
                                const GB300PatchTessOptions *options, float *outer, float *inner,
                                float *outerLo, float *outerHi, void *stream) {

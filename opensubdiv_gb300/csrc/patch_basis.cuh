@@ -384,10 +384,9 @@ __device__ __forceinline__ void box_fold(int mask, float *w) {
     if (vb & 4) { a = w[11]; w[8] += a; w[9] += a; w[5] -= a; b = w[10]; w[8] += b; w[7] += b; w[4] -= b; w[11] = w[10] = 0.0f; }
 }
 
-template <int LC>
-__device__ void eval_box_tri(float s, float t, int boundary, const int *__restrict__ cvs,
-                             const float *__restrict__ src, int stride, int e0, int length,
-                             Acc6<LC> &acc) {
+// Box-spline weights of the 12 control points for derivative order k (0 value, 1 d/ds, 2 d/dt,
+// 3 d2/ds2, 4 d2/dsdt, 5 d2/dt2) from the monomials m, before boundary folds.
+__device__ __forceinline__ void box_weights(int k, const float *m, float (&w)[12]) {
     constexpr signed char kP[12][15] = {
         {1, -2, -4, 0, 6, 6, 2, 0, -6, -4, -1, -2, 0, 2, 1},
         {1, 2, -2, 0, -6, 0, -4, 0, 6, 2, 2, 4, 0, -2, -1},
@@ -427,6 +426,22 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
         {1, 0, -2, -1, 0, 1}, {-1, 0, 2, 2, 0, -1}, {0, 0, 0, -1, 0, 0}, {1, -2, 0, 1, 0, -1},
         {-2, 4, 4, -1, 0, -1}, {1, -2, -4, -1, 0, 2}, {0, 0, 0, 1, 0, 0}, {-1, 2, 0, -1, 0, 2},
         {1, -4, -2, 2, 0, -1}, {0, 2, 2, -1, 0, -1}, {0, 0, 0, 0, 0, -1}, {0, 0, 0, 0, 0, 1}};
+    const float k12 = 1.0f / 12.0f, k6 = 1.0f / 6.0f;
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+        w[j] = (k == 0) ? k12 * box_row(kP[j], 15, m)
+             : (k == 1) ? k6 * box_row(kDs[j], 10, m)
+             : (k == 2) ? k6 * box_row(kDt[j], 10, m)
+             : (k == 3) ? box_row(kDss[j], 6, m)
+             : (k == 4) ? 0.5f * box_row(kDst[j], 6, m)
+             : box_row(kDtt[j], 6, m);
+    }
+}
+
+template <int LC>
+__device__ void eval_box_tri(float s, float t, int boundary, const int *__restrict__ cvs,
+                             const float *__restrict__ src, int stride, int e0, int length,
+                             Acc6<LC> &acc) {
     float m[15];
     m[0] = 1.0f; m[1] = s; m[2] = t;
     m[3] = s * s; m[4] = s * t; m[5] = t * t;
@@ -443,19 +458,10 @@ __device__ void eval_box_tri(float s, float t, int boundary, const int *__restri
 #pragma unroll
         for (int j = 0; j < 12; ++j) load_row<LC>(src, stride, idx[j], e0, length, x[j], xc);
     }
-    const float k12 = 1.0f / 12.0f, k6 = 1.0f / 6.0f;
 #pragma unroll
     for (int k = 0; k < 6; ++k) {
         float w[12];
-#pragma unroll
-        for (int j = 0; j < 12; ++j) {
-            w[j] = (k == 0) ? k12 * box_row(kP[j], 15, m)
-                 : (k == 1) ? k6 * box_row(kDs[j], 10, m)
-                 : (k == 2) ? k6 * box_row(kDt[j], 10, m)
-                 : (k == 3) ? box_row(kDss[j], 6, m)
-                 : (k == 4) ? 0.5f * box_row(kDst[j], 6, m)
-                 : box_row(kDtt[j], 6, m);
-        }
+        box_weights(k, m, w);
         box_fold(boundary, w);
 #pragma unroll
         for (int j = 0; j < 12; ++j) {
@@ -553,6 +559,166 @@ __device__ bool eval_patch_point(int type, Param p, float s, float t,
     d1 = sign * (float)(1 << depth);
     d2 = sign * d1 * d1;
     return true;
+}
+
+// ---- per-control-point weights ---------------------------------------------------------------
+// The bases above written out per control point instead of applied to points: w[k][j] is the
+// weight of control point j for output k (P, Ds, Dt, Dss, Dst, Dtt), k < NK, derivatives scaled
+// by +-2^depth / +-4^depth as eval_patch_point scales its sums.  These are the per-location
+// masks Far::LimitStencilTableFactory merges over its point stencils
+// (far/stencilTableFactory.cpp:560-640) and the coefficients Bfr::Surface::EvaluateStencil
+// returns (bfr/surface.h:244-265).  Returns the number of control points, 0 for an unknown type.
+template <int NK>
+__device__ __forceinline__ void put_tensor(float (&w)[NK][20], int j, float cell[6]) {
+#pragma unroll
+    for (int k = 0; k < NK; ++k) w[k][j] += cell[k];
+}
+
+template <int NK>
+__device__ int patch_point_weights(int type, Param p, float s, float t, float (&w)[NK][20]) {
+#pragma unroll
+    for (int k = 0; k < NK; ++k)
+#pragma unroll
+        for (int j = 0; j < 20; ++j) w[k][j] = 0.0f;
+    const int depth = p.depth();
+    const float frac = 1.0f / (float)(1 << (depth - p.nonquad()));
+    const float fracInv = 1.0f / frac;
+    float sign = 1.0f;
+    const bool tri = (type == 5 || type == 10 || type == 4);
+    if (tri && (p.u() + p.v()) >= (1 << depth)) {
+        const int df = 1 << depth;
+        s = (float)(df - p.u()) - s * fracInv;
+        t = (float)(df - p.v()) - t * fracInv;
+        sign = -1.0f;
+    } else {
+        s = s * fracInv - (float)p.u();
+        t = t * fracInv - (float)p.v();
+    }
+    int n = 0;
+    if (type == 6 || type == 9) {
+        // tensor products: cell (r, c) weights for the six outputs
+        float sp[4], sd[4], sdd[4], tp[4], td[4], tdd[4];
+        if (type == 6) {
+            bspline_curve(s, sp, sd, sdd);
+            bspline_curve(t, tp, td, tdd);
+            const int b = p.boundary();
+            if (b & 1) { fold_first(tp); fold_first(td); fold_first(tdd); }
+            if (b & 2) { fold_last(sp); fold_last(sd); fold_last(sdd); }
+            if (b & 4) { fold_last(tp); fold_last(td); fold_last(tdd); }
+            if (b & 8) { fold_first(sp); fold_first(sd); fold_first(sdd); }
+            n = 16;
+        } else {
+            bezier_curve(s, sp, sd, sdd);
+            bezier_curve(t, tp, td, tdd);
+            n = 20;
+        }
+        const float sc = 1.0f - s, tc = 1.0f - t;
+        float d0 = s + t;   d0 = (d0 <= 0.0f) ? 1.0f : (1.0f / d0);
+        float d1 = sc + t;  d1 = (d1 <= 0.0f) ? 1.0f : (1.0f / d1);
+        float d2 = sc + tc; d2 = (d2 <= 0.0f) ? 1.0f : (1.0f / d2);
+        float d3 = s + tc;  d3 = (d3 <= 0.0f) ? 1.0f : (1.0f / d3);
+        const float g0 = s * d0, g2 = t * d1, g4 = sc * d2, g6 = tc * d3;
+        constexpr int kGrid[4][4] = {{0, 1, 7, 5}, {2, -1, -2, 6}, {16, -4, -3, 12},
+                                     {15, 17, 11, 10}};
+#pragma unroll
+        for (int r = 0; r < 4; ++r)
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+                float cell[6] = {sp[c] * tp[r], sd[c] * tp[r], sp[c] * td[r],
+                                 sdd[c] * tp[r], sd[c] * td[r], sp[c] * tdd[r]};
+                if (type == 6) {
+                    put_tensor<NK>(w, 4 * r + c, cell);
+                    continue;
+                }
+                const int g = kGrid[r][c];
+                if (g >= 0) {
+                    put_tensor<NK>(w, g, cell);
+                } else {
+                    // blended interior pair (a, a + 1) by ga (patchBasis.h:346-378)
+                    const int a = (g == -1) ? 3 : (g == -2) ? 8 : (g == -3) ? 13 : 18;
+                    const float ga = (g == -1) ? g0 : (g == -2) ? g2 : (g == -3) ? g4 : g6;
+                    float ca[6], cb[6];
+#pragma unroll
+                    for (int k = 0; k < 6; ++k) ca[k] = ga * cell[k], cb[k] = (1.0f - ga) * cell[k];
+                    put_tensor<NK>(w, a, ca);
+                    put_tensor<NK>(w, a + 1, cb);
+                }
+            }
+    } else if (type == 10) {
+        float g[6] = {1.0f, 0.0f, 1.0f, 0.0f, 1.0f, 0.0f};
+        const float u = s, v = t, ww = 1.0f - u - v;
+        if ((u + v) > 0) { g[0] = u / (u + v); g[1] = v / (u + v); }
+        if ((v + ww) > 0) { g[2] = v / (v + ww); g[3] = ww / (v + ww); }
+        if ((ww + u) > 0) { g[4] = ww / (ww + u); g[5] = u / (ww + u); }
+        constexpr int kBez[15] = {0, 1, 15, 7, 5, 2, -1, -2, 6, 17, -3, 16, 11, 12, 10};
+        constexpr int kOrd[6][2] = {{0, 0}, {1, 0}, {0, 1}, {2, 0}, {1, 1}, {0, 2}};
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+            float b[15];
+            bezier_tri_weights(s, t, kOrd[k][0], kOrd[k][1], b);
+#pragma unroll
+            for (int m = 0; m < 15; ++m) {
+                const int gi = kBez[m];
+                if (gi >= 0) {
+                    w[k][gi] += b[m];
+                } else {
+                    const int a = (gi == -1) ? 3 : (gi == -2) ? 8 : 13;
+                    const float ga = (gi == -1) ? g[0] : (gi == -2) ? g[2] : g[4];
+                    const float gb = (gi == -1) ? g[1] : (gi == -2) ? g[3] : g[5];
+                    w[k][a] += ga * b[m];
+                    w[k][a + 1] += gb * b[m];
+                }
+            }
+        }
+        n = 18;
+    } else if (type == 5) {
+        // the box-spline rows of eval_box_tri, per derivative order, with the boundary folds
+        float m[15];
+        m[0] = 1.0f; m[1] = s; m[2] = t;
+        m[3] = s * s; m[4] = s * t; m[5] = t * t;
+        m[6] = m[3] * s; m[7] = m[4] * s; m[8] = m[4] * t; m[9] = m[5] * t;
+        m[10] = m[6] * s; m[11] = m[7] * s; m[12] = m[3] * m[5]; m[13] = m[8] * t;
+        m[14] = m[9] * t;
+#pragma unroll
+        for (int k = 0; k < NK; ++k) {
+            float wk[12];
+            box_weights(k, m, wk);
+            box_fold(p.boundary(), wk);
+#pragma unroll
+            for (int j = 0; j < 12; ++j) w[k][j] = wk[j];
+        }
+        n = 12;
+    } else if (type == 3) {
+        const float sc = 1.0f - s, tc = 1.0f - t;
+        const float wp[4] = {sc * tc, s * tc, s * t, sc * t};
+        const float ws[4] = {-tc, tc, t, -t};
+        const float wt[4] = {-sc, -s, s, sc};
+        const float wst[4] = {1.0f, -1.0f, 1.0f, -1.0f};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            w[0][j] = wp[j];
+            if constexpr (NK > 2) w[1][j] = ws[j], w[2][j] = wt[j];
+            if constexpr (NK > 4) w[4][j] = wst[j];
+        }
+        n = 4;
+    } else if (type == 4) {
+        w[0][0] = 1.0f - s - t, w[0][1] = s, w[0][2] = t;
+        if constexpr (NK > 2) {
+            w[1][0] = -1.0f, w[1][1] = 1.0f;
+            w[2][0] = -1.0f, w[2][2] = 1.0f;
+        }
+        n = 3;
+    } else {
+        return 0;
+    }
+    const float d1 = sign * (float)(1 << depth), d2 = sign * d1 * d1;
+#pragma unroll
+    for (int k = 1; k < NK; ++k) {
+        const float sc = k < 3 ? d1 : d2;
+#pragma unroll
+        for (int j = 0; j < 20; ++j) w[k][j] *= sc;
+    }
+    return n;
 }
 
 }  // namespace gb300

@@ -57,4 +57,13 @@ int tess_factors(const void *arrays, int numArrays, const int *indices, const vo
                  const GB300PatchTessOptions *o, float *outer, float *inner, float *outerLo,
                  float *outerHi, cudaStream_t s);
 
+// Limit stencils at device PatchCoords of a table, composed over the stencils of its points
+// (stencil_factory.cu).
+GB300StencilTable *tess_stencils(const void *arrays, const int *indices, const void *params,
+                                 int numPoints, const void *patchCoords, int baseNumStencils,
+                                 int64_t baseNumIndices, const int *baseSizes,
+                                 const int *baseOffsets, const int *baseIndices,
+                                 const float *baseWeights, int numChannels, int sortEntries,
+                                 cudaStream_t s, const char *who);
+
 }  // namespace gb300

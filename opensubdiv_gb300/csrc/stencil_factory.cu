@@ -22,6 +22,8 @@
 // rows are copied into the output table (optionally with each stencil's entries sorted by
 // control index).
 #include "common.cuh"
+#include "patch_basis.cuh"
+#include "patchmap.h"
 #include "tables.h"
 
 #include <cub/device/device_scan.cuh>
@@ -869,25 +871,20 @@ GB300StencilTable *GB300StencilTableFactoryCreate(int numControl, int numLevels,
     return t;
 }
 
-GB300StencilTable *GB300StencilTableComposeRows(
-    int baseNumStencils, int64_t baseNumIndices, const int *baseSizes, const int *baseOffsets,
-    const int *baseIndices, const float *baseWeights, int numRows, int64_t nnz,
-    const int64_t *offsets, const int *sources, int numChannels, const float *const *weights,
-    int appendBase, int sortEntries, void *stream) {
-    const char *who = "GB300StencilTableComposeRows";
-    GB300StencilMasks m{numRows, nnz, offsets, sources, weights ? weights[0] : nullptr};
-    bool good = baseNumStencils >= 0 && baseNumIndices >= 0 &&
-                (baseNumStencils == 0 || (baseSizes && baseOffsets)) &&
-                (baseNumIndices == 0 || (baseIndices && baseWeights)) &&
-                (numChannels == 1 || numChannels == 3 || numChannels == 6) && weights &&
-                masks_ok(m) && !(appendBase && numChannels != 1);
-    for (int c = 0; good && c < numChannels; ++c) good = nnz == 0 || weights[c];
-    if (!good) {
-        fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
-        return nullptr;
-    }
-    cudaStream_t s = as_stream(stream);
-    Scratch sc(s);
+}  // extern "C"
+
+namespace gb300 {
+
+// The composition of GB300StencilTableComposeRows with its masks already in device memory
+// (moff: numRows + 1 offsets, msrc / mw[c]: nnz sources and weights); scratch from `sc`.
+GB300StencilTable *compose_rows_device(int baseNumStencils, int64_t baseNumIndices,
+                                       const int *baseSizes, const int *baseOffsets,
+                                       const int *baseIndices, const float *baseWeights,
+                                       int numRows, int64_t nnz, const long long *moff,
+                                       const int *msrc, float *const *mw, int numChannels,
+                                       int appendBase, int sortEntries, Scratch &sc,
+                                       const char *who) {
+    cudaStream_t s = sc.s;
     long long *baseOff = sc.alloc<long long>((size_t)baseNumStencils, who);
     int *metaSize = sc.alloc<int>((size_t)numRows, who);
     long long *metaOff = sc.alloc<long long>((size_t)numRows, who);
@@ -895,19 +892,8 @@ GB300StencilTable *GB300StencilTableComposeRows(
     long long *scanTmp = sc.alloc<long long>((size_t)numRows + 1, who);
     int *dStatus = sc.alloc<int>(4, who);
     unsigned long long *dUsed = sc.alloc<unsigned long long>(1, who);
-    long long *moff = sc.alloc<long long>((size_t)numRows + 1, who);
-    int *msrc = sc.alloc<int>((size_t)nnz, who);
-    if (!baseOff || !metaSize || !metaOff || !sizesTmp || !scanTmp || !dStatus || !dUsed ||
-        !moff || !msrc)
+    if (!baseOff || !metaSize || !metaOff || !sizesTmp || !scanTmp || !dStatus || !dUsed)
         return nullptr;
-    float *mw[6] = {};
-    for (int c = 0; c < numChannels; ++c)
-        if (!(mw[c] = sc.alloc<float>((size_t)nnz, who))) return nullptr;
-    if (!h2d(moff, (const long long *)offsets, (size_t)numRows + 1, s, who) ||
-        !h2d(msrc, sources, (size_t)nnz, s, who))
-        return nullptr;
-    for (int c = 0; c < numChannels; ++c)
-        if (!h2d(mw[c], weights[c], (size_t)nnz, s, who)) return nullptr;
     if (check_cuda(cudaMemsetAsync(dStatus, 0, 16, s), who) != GB300_OK) return nullptr;
     if (baseNumStencils > 0) {
         k_base_rows<<<grid_for(baseNumStencils, 256), 256, 0, s>>>(
@@ -978,6 +964,131 @@ GB300StencilTable *GB300StencilTableComposeRows(
     }
     if (t) ok();
     return t;
+}
+
+
+// Masks of a limit stencil per point at its PatchCoord (5 words: array, patch, vertex, s,
+// t), at a fixed stride of 20 entries: the patch's control points and the per-control-point
+// basis weights of P (and Ds, Dt; and Dss, Dst, Dtt), padded with the first control point at
+// weight 0 (which adds no entries and changes no sums).  A point the PatchMap missed gets an
+// all-zero mask over base stencil 0.
+template <int NK>
+__global__ void __launch_bounds__(128) k_point_masks(int numPoints, const int *coords,
+                                                      const int *arrays, const int *indices,
+                                                      const int *params, long long *moff,
+                                                      int *msrc, float *mw0, float *mw1,
+                                                      float *mw2, float *mw3, float *mw4,
+                                                      float *mw5, int *status) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i <= numPoints; i += stride) {
+        moff[i] = 20LL * i;
+        if (i == numPoints) continue;
+        const int *c = coords + 5 * (size_t)i;
+        const int ai = c[0], pi = c[1];
+        float w[NK][20];
+        int n = 0, cv[20];
+        if (ai >= 0) {
+            const int *arr = arrays + 6 * ai;
+            const Param p{params[3 * pi], params[3 * pi + 1]};
+            const int type = p.regular() ? arr[0] : arr[1];
+            n = patch_point_weights<NK>(type, p, __int_as_float(c[3]), __int_as_float(c[4]), w);
+            if (n == 0) atomicOr(status, 1);
+            const int *row = indices + arr[3] + (size_t)arr[4] * (pi - arr[5]);
+#pragma unroll
+            for (int j = 0; j < 20; ++j) cv[j] = j < n ? row[j] : 0;
+        }
+        float *mw[6] = {mw0, mw1, mw2, mw3, mw4, mw5};
+        const size_t o = 20 * (size_t)i;
+#pragma unroll
+        for (int j = 0; j < 20; ++j) {
+            msrc[o + j] = j < n ? cv[j] : (n ? cv[0] : 0);
+#pragma unroll
+            for (int k = 0; k < NK; ++k) mw[k][o + j] = j < n ? w[k][j] : 0.0f;
+        }
+    }
+}
+
+// Limit stencils at numPoints device PatchCoords of a device patch table, composed over the
+// stencils of the table's points (base table, Far's layout, one row per point the patch
+// indices name: control vertices first, then refined and local points).
+GB300StencilTable *tess_stencils(const void *arrays, const int *indices, const void *params,
+                                 int numPoints, const void *patchCoords, int baseNumStencils,
+                                 int64_t baseNumIndices, const int *baseSizes,
+                                 const int *baseOffsets, const int *baseIndices,
+                                 const float *baseWeights, int numChannels, int sortEntries,
+                                 cudaStream_t s, const char *who) {
+    Scratch sc(s);
+    const int64_t nnz = 20LL * numPoints;
+    long long *moff = sc.alloc<long long>((size_t)numPoints + 1, who);
+    int *msrc = sc.alloc<int>((size_t)nnz, who);
+    int *status = sc.alloc<int>(1, who);
+    if (!moff || !msrc || !status) return nullptr;
+    float *mw[6] = {};
+    for (int c = 0; c < numChannels; ++c)
+        if (!(mw[c] = sc.alloc<float>((size_t)nnz, who))) return nullptr;
+    if (check_cuda(cudaMemsetAsync(status, 0, sizeof(int), s), who) != GB300_OK) return nullptr;
+    const int grid = grid_for((long long)numPoints + 1, 128);
+    const int *co = (const int *)patchCoords, *ar = (const int *)arrays,
+              *pa = (const int *)params;
+    if (numChannels == 1)
+        k_point_masks<1><<<grid, 128, 0, s>>>(numPoints, co, ar, indices, pa, moff, msrc,
+                                              mw[0], mw[0], mw[0], mw[0], mw[0], mw[0], status);
+    else if (numChannels == 3)
+        k_point_masks<3><<<grid, 128, 0, s>>>(numPoints, co, ar, indices, pa, moff, msrc,
+                                              mw[0], mw[1], mw[2], mw[0], mw[0], mw[0], status);
+    else
+        k_point_masks<6><<<grid, 128, 0, s>>>(numPoints, co, ar, indices, pa, moff, msrc,
+                                              mw[0], mw[1], mw[2], mw[3], mw[4], mw[5], status);
+    count_launch();
+    if (check_launch(who) != GB300_OK) return nullptr;
+    int st = 0;
+    if (!d2h(&st, status, 1, s, who)) return nullptr;
+    if (st) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "%s: a patch of a type without a basis", who);
+        return nullptr;
+    }
+    return compose_rows_device(baseNumStencils, baseNumIndices, baseSizes, baseOffsets,
+                               baseIndices, baseWeights, numPoints, nnz, moff, msrc, mw,
+                               numChannels, 0, sortEntries, sc, who);
+}
+
+}  // namespace gb300
+
+extern "C" {
+
+GB300StencilTable *GB300StencilTableComposeRows(
+    int baseNumStencils, int64_t baseNumIndices, const int *baseSizes, const int *baseOffsets,
+    const int *baseIndices, const float *baseWeights, int numRows, int64_t nnz,
+    const int64_t *offsets, const int *sources, int numChannels, const float *const *weights,
+    int appendBase, int sortEntries, void *stream) {
+    const char *who = "GB300StencilTableComposeRows";
+    GB300StencilMasks m{numRows, nnz, offsets, sources, weights ? weights[0] : nullptr};
+    bool good = baseNumStencils >= 0 && baseNumIndices >= 0 &&
+                (baseNumStencils == 0 || (baseSizes && baseOffsets)) &&
+                (baseNumIndices == 0 || (baseIndices && baseWeights)) &&
+                (numChannels == 1 || numChannels == 3 || numChannels == 6) && weights &&
+                masks_ok(m) && !(appendBase && numChannels != 1);
+    for (int c = 0; good && c < numChannels; ++c) good = nnz == 0 || weights[c];
+    if (!good) {
+        fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
+        return nullptr;
+    }
+    cudaStream_t s = as_stream(stream);
+    Scratch sc(s);
+    long long *moff = sc.alloc<long long>((size_t)numRows + 1, who);
+    int *msrc = sc.alloc<int>((size_t)nnz, who);
+    if (!moff || !msrc) return nullptr;
+    float *mw[6] = {};
+    for (int c = 0; c < numChannels; ++c)
+        if (!(mw[c] = sc.alloc<float>((size_t)nnz, who))) return nullptr;
+    if (!h2d(moff, (const long long *)offsets, (size_t)numRows + 1, s, who) ||
+        !h2d(msrc, sources, (size_t)nnz, s, who))
+        return nullptr;
+    for (int c = 0; c < numChannels; ++c)
+        if (!h2d(mw[c], weights[c], (size_t)nnz, s, who)) return nullptr;
+    return compose_rows_device(baseNumStencils, baseNumIndices, baseSizes, baseOffsets,
+                               baseIndices, baseWeights, numRows, nnz, moff, msrc, mw,
+                               numChannels, appendBase, sortEntries, sc, who);
 }
 
 }  // extern "C"

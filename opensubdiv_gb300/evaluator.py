@@ -290,6 +290,24 @@ class GB300StencilTable:
             raise GB300Error(1, last_error())
         return cls(h)
 
+    @classmethod
+    def FromPatchCoords(cls, table, patch_coords, base, num_points=None, channels=3,
+                        sortEntries=True, stream=None):
+        """Bfr::Surface::EvaluateStencil at every point (GB300TessellationStencils): one limit
+        stencil per PatchCoord of the GB300PatchTable `table` (a CUDA tensor of [n, 5] int32,
+        e.g. from MeshTessellation.Generate or Share), over the control vertices, composed
+        over `base` -- a GB300StencilTable holding one stencil per point the patch indices
+        name (identity rows for the control vertices, then the refined and local points).
+        channels: 1 (P), 3 (P, Du, Dv) or 6 (with the second derivatives)."""
+        n = int(patch_coords.shape[0]) if num_points is None else int(num_points)
+        h = _lib.load().GB300TessellationStencils(
+            table.handle, n, _ptr(patch_coords), base.GetNumStencils(), base.GetNumIndices(),
+            base.GetSizesBuffer(), base.GetOffsetsBuffer(), base.GetIndicesBuffer(),
+            base.GetWeightsBuffer(), int(channels), int(bool(sortEntries)), _stream(stream))
+        if not h:
+            raise GB300Error(1, last_error())
+        return cls(h)
+
     def GetSizesBuffer(self): return self._buf(0)
     def GetOffsetsBuffer(self): return self._buf(1)
     def GetIndicesBuffer(self): return self._buf(2)

@@ -107,6 +107,35 @@ def patch_basis(ptype, field0, field1, s, t, fp64=False):
     return w.reshape(6, 20)[:, :n]
 
 
+def patch_masks(coords, arrays, indices, params, channels=3):
+    """Per-point masks of limit stencils at PatchCoords (int32 [n, 5]): the patch's control
+    points and their basis weights (patch_basis), as Far::LimitStencilTableFactory merges them
+    over its point stencils (far/stencilTableFactory.cpp:560-640).  Returns (offsets [n + 1],
+    sources, [weights per channel]) for compose_rows; a point without a patch gets no entries."""
+    c = np.asarray(coords, np.int32).reshape(-1, 5)
+    arrays = np.asarray(arrays, np.int32).reshape(-1, 6)
+    indices = np.asarray(indices, np.int32)
+    params = np.asarray(params, np.int32).reshape(-1, 3)
+    st = c[:, 3:5].copy().view(np.float32)
+    offs, src, ws = [0], [], [[] for _ in range(channels)]
+    for i in range(len(c)):
+        a, pi = int(c[i, 0]), int(c[i, 1])
+        if a < 0:
+            offs.append(offs[-1])
+            continue
+        reg, desc, _, ib, stride, pb = (int(x) for x in arrays[a])
+        f0, f1 = int(params[pi, 0]), int(params[pi, 1])
+        ptype = reg if (f1 >> 5) & 1 else desc
+        w = patch_basis(ptype, f0, f1, float(st[i, 0]), float(st[i, 1]))
+        n = w.shape[1]
+        src.extend(indices[ib + stride * (pi - pb): ib + stride * (pi - pb) + n])
+        for k in range(channels):
+            ws[k].extend(w[k])
+        offs.append(offs[-1] + n)
+    return (np.asarray(offs, np.int64), np.asarray(src, np.int32),
+            [np.asarray(w, np.float32) for w in ws])
+
+
 class PatchMap:
     """Restated Far::PatchMap (far/patchMap.cpp)."""
 

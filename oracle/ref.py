@@ -443,3 +443,28 @@ def bfr_share(refiner, rate_offsets, rates, num_coords, num_facets, facet_size=3
     if n < 0:
         raise ValueError("non-manifold or mismatched shared edge")
     return facets, po, src[:n]
+
+
+def bfr_stencils(refiner, rate_offsets, rates, num_coords, facet_size=3, preserve_quads=False,
+                 approx_sharp=6, approx_smooth=2):
+    """Bfr::Surface::EvaluateStencil (P, Du, Dv) at every coord of the reference's tessellate
+    loop, over mesh vertices: dict(sizes [coords], offsets [coords + 1], indices, wP, wDu, wDv)."""
+    L = lib()
+    L.ref_bfr_stencils.restype = C.c_long
+    ro = np.ascontiguousarray(rate_offsets, np.int32)
+    rt = np.ascontiguousarray(rates, np.int32)
+    sizes = np.zeros(max(num_coords, 1), np.int32)
+    args = (refiner.h, C.c_int(approx_sharp), C.c_int(approx_smooth), _p(ro), _p(rt),
+            C.c_int(facet_size), C.c_int(int(preserve_quads)), C.c_long(num_coords))
+    n = L.ref_bfr_stencils(*args, _p(sizes), C.c_long(0), None, None, None, None)
+    if n < 0:
+        raise ValueError("coord capacity")
+    idx = np.zeros(max(n, 1), np.int32)
+    w = [np.zeros(max(n, 1), np.float32) for _ in range(3)]
+    m = L.ref_bfr_stencils(*args, _p(sizes), C.c_long(n), _p(idx), _p(w[0]), _p(w[1]), _p(w[2]))
+    if m != n:
+        raise ValueError("entry count changed between passes")
+    sizes = sizes[:num_coords]
+    off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    return dict(sizes=sizes, offsets=off, indices=idx[:n], wP=w[0][:n], wDu=w[1][:n],
+                wDv=w[2][:n])

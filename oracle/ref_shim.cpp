@@ -990,6 +990,70 @@ void ref_bfr_record_copy(void *p, long *coordOffsets, long *facetOffsets, int *v
 
 void ref_bfr_record_destroy(void *p) { delete (BfrRecord *)p; }
 
+// Bfr::Surface::EvaluateStencil (bfr/surface.h:244-265) at every coord of the reference's
+// tessellate loop (faces and coords in ref_bfr_mesh_record's order): each coord's limit
+// stencils for P, Du and Dv over the surface's control points, mapped to mesh vertices through
+// Surface::GetControlPointIndices (a vertex named twice sums its weights, at its first place).
+// Writes stencil sizes (one per coord, capacity `maxCoords`) and returns the total number of
+// entries, copying indices and the three weight arrays when `indices` is not null (capacity
+// `maxEntries`); -1 when a capacity is too small.
+long ref_bfr_stencils(void *refiner, int approxSharp, int approxSmooth, const int *rateOffsets,
+                      const int *rates, int facetSize, int preserveQuads, long maxCoords,
+                      int *sizes, long maxEntries, int *indices, float *wP, float *wDu,
+                      float *wDv) {
+    Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
+    Bfr::SurfaceFactory::Options so;
+    so.SetApproxLevelSharp(approxSharp);
+    so.SetApproxLevelSmooth(approxSmooth);
+    Bfr::RefinerSurfaceFactory<> factory(mesh, so);
+    const int nf = factory.GetNumFaces();
+    Bfr::Tessellation::Options to = tessOptions(facetSize == 4 ? 4 : 3, preserveQuads);
+    Bfr::Surface<float> sf;
+    std::vector<float> coords, sp, sdu, sdv;
+    std::vector<Far::Index> cps;
+    long nc = 0, ne = 0;
+    for (int f = 0; f < nf; ++f) {
+        if (!factory.InitVertexSurface(f, &sf)) continue;
+        Bfr::Tessellation t(sf.GetParameterization(), rateOffsets[f + 1] - rateOffsets[f],
+                            rates + rateOffsets[f], to);
+        if (!t.IsValid()) continue;
+        const int n = t.GetNumCoords(), ncp = sf.GetNumControlPoints();
+        coords.resize(2 * (size_t)n);
+        t.GetCoords(coords.data());
+        cps.resize(ncp);
+        sf.GetControlPointIndices(cps.data());
+        sp.resize(ncp), sdu.resize(ncp), sdv.resize(ncp);
+        for (int i = 0; i < n; ++i) {
+            sf.EvaluateStencil(&coords[2 * i], sp.data(), sdu.data(), sdv.data());
+            if (nc >= maxCoords) return -1;
+            const long e0 = ne;
+            for (int j = 0; j < ncp; ++j) {
+                long at = -1;
+                for (long k = e0; indices && k < ne; ++k)
+                    if (indices[k] == cps[j]) at = k;
+                if (!indices) {
+                    // count distinct vertices only
+                    bool seen = false;
+                    for (int q = 0; q < j; ++q) seen = seen || cps[q] == cps[j];
+                    if (!seen) ++ne;
+                    continue;
+                }
+                if (at < 0) {
+                    if (ne >= maxEntries) return -1;
+                    at = ne++;
+                    indices[at] = cps[j];
+                    wP[at] = wDu[at] = wDv[at] = 0.0f;
+                }
+                wP[at] += sp[j];
+                wDu[at] += sdu[j];
+                wDv[at] += sdv[j];
+            }
+            sizes[nc++] = (int)(ne - e0);
+        }
+    }
+    return ne;
+}
+
 // The tessellation with shared vertex and edge points of the reference's tutorial 2.2
 // (tutorials/bfr/tutorial_2_2/bfr_tutorial_2_2.cpp:160-430), with per-face rates: faces in
 // order through Bfr::RefinerSurfaceFactory (faces without a limit surface skipped), the

@@ -544,6 +544,24 @@ def bfr_fixtures():
                      seed=323, fvar=uv_seams(fltor, 12, 8) + (uv_grid(12, 8),))
 
 
+def bfr_fixture_cage(key):
+    """The cage a Bfr mesh fixture (bfr_<name>_<mode>_f<n>[q]) was written from, with the
+    boundary and corner settings the fixture arrays do not carry."""
+    for name, mode, fs, pq in BFR_MESHES:
+        if key == f"bfr_{name}_{mode}_f{fs}{'q' if pq else ''}":
+            return regression_shape(name)
+    others = {
+        "bfr_torus16x8_e_f3": lambda: shapes.torus(16, 8, tri_fraction=0.1,
+                                                   crease_fraction=0.05, seed=3),
+        "bfr_icosphere1_u6_f3": lambda: shapes.icosphere(1, noise=0.005, seed=3),
+        "bfr_torus12x8_uv_e_f3": lambda: shapes.torus(12, 8, tri_fraction=0.1,
+                                                      crease_fraction=0.05, seed=31, noise=0.01),
+        "bfr_looptorus12x8_uv_u4_f3": lambda: shapes.torus(12, 8, seed=33, noise=0.01,
+                                                           scheme=shapes.LOOP),
+    }
+    return others[key]()
+
+
 def bfr_share_fixture(path):
     """The reference's tessellation with shared vertex and edge points (its tutorial 2.2
     bookkeeping over Bfr::Tessellation, through ref_bfr_share) on the cage and rates of every
@@ -551,13 +569,12 @@ def bfr_share_fixture(path):
     and the coord each point is evaluated at."""
     out = {}
     for name in sorted(os.listdir(HERE)):
-        if not (name.startswith("bfr_") and name.endswith(".npz")) or name == "bfr_share.npz" \
-                or name == "bfr_tess_patterns.npz":
+        if not (name.startswith("bfr_") and name.endswith(".npz")) or name in (
+                "bfr_share.npz", "bfr_tess_patterns.npz", "bfr_stencils.npz"):
             continue
         d = np.load(os.path.join(HERE, name))
-        cage = shapes.Cage(positions=d["positions"], verts_per_face=d["verts_per_face"],
-                           face_verts=d["face_verts"], scheme=int(d["scheme"]),
-                           crease_verts=d["crease_verts"], crease_sharpness=d["crease_sharpness"])
+        cage = bfr_fixture_cage(name[:-4])
+        assert np.array_equal(cage.face_verts, d["face_verts"])
         co, fo = d["coord_offsets"], d["facet_offsets"]
         facets, po, src = ref.bfr_share(ref.Refiner(cage), d["rate_offsets"], d["rates"],
                                         int(co[-1]), int(fo[-1]), int(d["facet_size"]),
@@ -566,6 +583,35 @@ def bfr_share_fixture(path):
         out[key + "__facets"] = facets
         out[key + "__point_offsets"] = po
         out[key + "__point_sources"] = src
+    np.savez_compressed(path, **out)
+
+
+BFR_STENCIL_MESHES = ["bfr_catmark_nonquads_u5_f3", "bfr_catmark_xord_boundary_u4_f4q",
+                      "bfr_catmark_gregory_test1_e_f4", "bfr_loop_xord_boundary_u5_f3",
+                      "bfr_torus16x8_e_f3"]
+
+
+def bfr_stencil_fixture(path):
+    """Bfr::Surface::EvaluateStencil (P, Du, Dv over mesh vertices) at every coord of the
+    reference's tessellate loop, for some of the Bfr mesh fixtures, with the Far stencils of
+    the paired patch table's points beyond the cage (refined and local points: the rows of the
+    fixture's source buffer after the cage points)."""
+    out = {}
+    for key in BFR_STENCIL_MESHES:
+        d = np.load(os.path.join(HERE, key + ".npz"))
+        cage = bfr_fixture_cage(key)
+        r = ref.Refiner(cage).refine_adaptive_levels(6, 2, True)
+        p = ref.Patches(r, endcap=3, max_isolation=6, inf_sharp=True, share_endcap_points=False,
+                        legacy_sharp_corners=False)
+        assert np.array_equal(p.indices, d["patch_indices"])
+        st = p.st
+        bfr = ref.bfr_stencils(ref.Refiner(cage), d["rate_offsets"], d["rates"],
+                               int(d["coord_offsets"][-1]), int(d["facet_size"]),
+                               bool(d["preserve_quads"]))
+        for k in ("sizes", "offsets", "indices", "weights"):
+            out[f"{key}__st_{k}"] = np.asarray(st[k])
+        for k in ("sizes", "indices", "wP", "wDu", "wDv"):
+            out[f"{key}__bfr_{k}"] = bfr[k]
     np.savez_compressed(path, **out)
 
 
@@ -658,9 +704,13 @@ def main():
     if len(sys.argv) > 1 and sys.argv[1] == "bfr":
         bfr_fixtures()
         bfr_share_fixture(os.path.join(HERE, "bfr_share.npz"))
+        bfr_stencil_fixture(os.path.join(HERE, "bfr_stencils.npz"))
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr-share":
         bfr_share_fixture(os.path.join(HERE, "bfr_share.npz"))
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "bfr-stencils":
+        bfr_stencil_fixture(os.path.join(HERE, "bfr_stencils.npz"))
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr-large":
         torus = shapes.torus(512, 256, R=1.0, r=0.3, tri_fraction=0.05, crease_fraction=0.02,

@@ -21,7 +21,7 @@ import oracle
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 MESHES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "bfr_*.npz"))
-                if not p.endswith(("bfr_tess_patterns.npz", "bfr_share.npz")))
+                if not p.endswith(("bfr_tess_patterns.npz", "bfr_share.npz", "bfr_stencils.npz")))
 
 
 def bits(a):
@@ -226,3 +226,74 @@ def test_shared_points_reject_edges_with_two_rates():
     with pytest.raises(ValueError):
         oracle.tess_share(4, sizes, fv, fe, 6, ne, ro, rates, mesh["coord_offsets"],
                           mesh["facet_offsets"], mesh["facets"])
+
+
+STENCILS = os.path.join(GOLDEN, "bfr_stencils.npz")
+STENCIL_MESHES = sorted({k.split("__")[0] for k in np.load(STENCILS).files})
+
+
+def point_base(z, g, key):
+    """Stencils of every point the fixture's patch indices name: identity rows for the cage
+    vertices, then Far's stencils of the refined and local points (the fixture's source rows)."""
+    nc = len(z["positions"])
+    st = {k: g[f"{key}__st_{k}"] for k in ("sizes", "offsets", "indices", "weights")}
+    return dict(sizes=np.concatenate([np.ones(nc, np.int32), st["sizes"]]).astype(np.int32),
+                offsets=np.concatenate([np.arange(nc), nc + st["offsets"]]).astype(np.int32),
+                indices=np.concatenate([np.arange(nc), st["indices"]]).astype(np.int32),
+                weights=np.concatenate([np.ones(nc, np.float32), st["weights"]]))
+
+
+def apply_stencils(sizes, indices, weights, points):
+    """sum_j w_j x_j per stencil, in double."""
+    rows = np.repeat(np.arange(len(sizes)), sizes)
+    out = np.zeros((len(sizes), points.shape[1]))
+    np.add.at(out, rows, weights.astype(np.float64)[:, None] * points[indices])
+    return out
+
+
+def oracle_point_stencils(z, base, channels=3):
+    coords = oracle.make_coords(z["q_handles"], z["q_s"], z["q_t"])
+    off, src, ws = oracle.patch_masks(coords, z["arrays"], z["patch_indices"], z["params"],
+                                      channels)
+    return oracle.compose_rows(base, off, src, ws)
+
+
+@pytest.mark.parametrize("key", STENCIL_MESHES)
+def test_point_stencils_match_bfr_evaluate_stencil(key):
+    """Limit stencils at every tessellation coord over the cage vertices -- the patch basis of
+    the coord's Far patch merged over the stencils of the patch's points, as
+    Far::LimitStencilTableFactory merges them -- against the reference's
+    Bfr::Surface::EvaluateStencil at the same coords (tests/golden/bfr_stencils.npz): applied
+    to the cage, within the reference's Bfr-versus-Far tolerances; and on faces Bfr evaluates
+    as regular patches, weight for weight (both are the B-spline weights of the same 16
+    points)."""
+    z = np.load(os.path.join(GOLDEN, key + ".npz"))
+    g = np.load(STENCILS)
+    ours = oracle_point_stencils(z, point_base(z, g, key))
+    pos = z["positions"].astype(np.float64)
+    bs = g[f"{key}__bfr_sizes"]
+    bi = g[f"{key}__bfr_indices"]
+    tol = bfr_tolerances(z["positions"])
+    rot = rotated_triangles(z)
+    for k, (ow, bw) in enumerate((("weights", "wP"), ("du_weights", "wDu"),
+                                  ("dv_weights", "wDv"))):
+        a = apply_stencils(ours["sizes"], ours["indices"], ours[ow], pos)
+        b = apply_stencils(bs, bi, g[f"{key}__bfr_{bw}"], pos)
+        assert np.abs(a - b).max() <= tol[k], (key, k, np.abs(a - b).max(), tol[k])
+        assert np.abs(a - z["out6"][k]).max() <= tol[k], k
+    # regular faces: dense weights
+    nc = len(pos)
+    co = z["coord_offsets"]
+    regular = np.repeat(z["regular"] == 1, np.diff(co))
+    ob = np.concatenate([[0], np.cumsum(ours["sizes"])])
+    bb = np.concatenate([[0], np.cumsum(bs)])
+    checked = 0
+    for i in np.nonzero(regular)[0][::7]:
+        for ow, bw in (("weights", "wP"), ("du_weights", "wDu"), ("dv_weights", "wDv")):
+            da = np.zeros(nc)
+            np.add.at(da, ours["indices"][ob[i]:ob[i + 1]], ours[ow][ob[i]:ob[i + 1]])
+            db = np.zeros(nc)
+            np.add.at(db, bi[bb[i]:bb[i + 1]], g[f"{key}__bfr_{bw}"][bb[i]:bb[i + 1]])
+            assert np.abs(da - db).max() <= 2e-6 * max(1.0, np.abs(db).max()), (key, i, ow)
+        checked += 1
+    assert checked > 0 or not regular.any()

@@ -19,10 +19,11 @@ import pytest
 
 import oracle
 from gpu_util import bbox_diag, dev, gate, host, torch_cuda
+from test_bfr_oracle import STENCIL_MESHES, STENCILS, oracle_point_stencils, point_base
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 MESHES = sorted(p for p in glob.glob(os.path.join(GOLDEN, "bfr_*.npz"))
-                if not p.endswith(("bfr_tess_patterns.npz", "bfr_share.npz")))
+                if not p.endswith(("bfr_tess_patterns.npz", "bfr_share.npz", "bfr_stencils.npz")))
 
 
 def bits(a):
@@ -355,3 +356,52 @@ def test_shared_points_reject_bad_edges():
                                       mesh["facets"])
     assert sp.num_points == len(src)
     assert np.array_equal(host(f), want)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", STENCIL_MESHES)
+def test_point_stencils_on_the_device(key):
+    """GB300TessellationStencils (Bfr::Surface::EvaluateStencil at every coord): the device
+    masks merged over the patch points' stencils hold the same entries as the oracle's merge
+    (rows compared with sorted entries) with weights within float rounding; evaluated from the
+    cage by EvalStencils they give GB300TessellationEvaluate's points (flat 1e-5 x bbox
+    diagonal) and Bfr::Surface::Evaluate's within the reference's Bfr-versus-Far tolerances."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300PatchTable, GB300StencilTable)
+    z = np.load(os.path.join(GOLDEN, key + ".npz"))
+    g = np.load(STENCILS)
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"],
+                                   bool(z["triangular"]))
+    opt = bfr.TessellationOptions(int(z["facet_size"]), bool(z["preserve_quads"]))
+    m = bfr.MeshTessellation(int(z["regular_face_size"]), z["verts_per_face"], rates=z["rates"],
+                             rate_offsets=z["rate_offsets"], options=opt)
+    _, _, pc = m.Generate(table=table)
+    bh = point_base(z, g, key)
+    base = GB300StencilTable.Create(bh["sizes"], bh["offsets"], bh["indices"], bh["weights"])
+    st = GB300StencilTable.FromPatchCoords(table, pc, base, channels=3)
+    h = st.CopyToHost()
+    want = oracle_point_stencils(z, bh)
+    assert np.array_equal(h["sizes"], want["sizes"])
+    o = np.concatenate([[0], np.cumsum(want["sizes"])])
+    for name in ("weights", "du_weights", "dv_weights"):
+        scale = max(1.0, float(np.abs(want[name]).max()))
+        for i in range(len(want["sizes"])):
+            a, b = slice(h["offsets"][i], h["offsets"][i] + h["sizes"][i]), slice(o[i], o[i + 1])
+            pa, pb = np.argsort(h["indices"][a]), np.argsort(want["indices"][b])
+            assert np.array_equal(h["indices"][a][pa], want["indices"][b][pb]), (key, i)
+            err = np.abs(h[name][a][pa] - want[name][b][pb]).max()
+            assert err <= 4e-6 * scale, (key, name, i, err, scale)
+    n = m.num_coords
+    d = BD(0, 3, 3)
+    outs = [torch.zeros(n * 3, device="cuda") for _ in range(3)]
+    assert Ev.EvalStencilsTable(dev(z["positions"].ravel()), d, outs[0], d, st, du=outs[1],
+                                duDesc=d, dv=outs[2], dvDesc=d)
+    per = m.Evaluate(dev(z["src"]), d, table, pc, 1)
+    diag = bbox_diag(z["positions"])
+    tol = bfr_tolerances(z["positions"])
+    for k in range(3):
+        got = host(outs[k]).reshape(-1, 3).astype(np.float64)
+        assert np.abs(got - host(per[k]).reshape(-1, 3)).max() <= 1e-5 * diag * (1 if k == 0 else 4), k
+        assert np.abs(got - z["out6"][k]).max() <= tol[k], k
