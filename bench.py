@@ -585,7 +585,103 @@ def bench_bfr(args, stream, peak):
     tf_ms = t0.elapsed_time(t1) / args.steps
     out["tess_factors"] = {"patches": npatch, "ms": tf_ms, "patches_per_s": npatch / (tf_ms / 1e3),
                            "mode": "screen-space, fractional-odd spacing, tess level 24"}
+    del table, src
+    release_memory()
+    out["limit_stencils"] = bench_bfr_stencils(args, stream, peak)
     return out
+
+
+BFR_STENCIL_TABLE = "torus256x128_bfr_stencils.npz"
+
+
+def bench_bfr_stencils(args, stream, peak):
+    """Bfr::Surface::EvaluateStencil at every tessellation point (GB300TessellationStencils) on
+    the 256 x 128 torus at rate 5, and the two per-frame paths it enables: (a) EvalStencils of
+    the points straight from the cage with those stencils, against (b) refining the patch
+    points from the cage with Far's point stencils, then GB300TessellationEvaluate.  Each frame
+    evaluates P, Du and Dv of every point."""
+    import torch
+
+    from opensubdiv_gb300 import bfr, workloads
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300PatchTable, GB300StencilTable)
+
+    path = os.path.join(GOLDEN, "large", BFR_STENCIL_TABLE)
+    if not os.path.exists(path):
+        return {"skipped": f"{BFR_STENCIL_TABLE} is written where the reference is available "
+                           "(tests/golden/make_golden.py large)"}
+    z = np.load(path)
+    pos = np.ascontiguousarray(z["positions"], np.float32)
+    nc = len(pos)
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"], False)
+    m = bfr.MeshTessellation(4, z["verts_per_face"], uniform_rate=5,
+                             options=bfr.TessellationOptions(3), stream=stream)
+    _, _, pc = m.Generate(table=table)
+    n = m.num_coords
+    st_sizes, st_offsets = z["st_sizes"], z["st_offsets"]
+    st_indices, st_weights = z["st_indices"], z["st_weights"]
+    base = GB300StencilTable.Create(
+        np.concatenate([np.ones(nc, np.int32), st_sizes]),
+        np.concatenate([np.arange(nc), nc + st_offsets]),
+        np.concatenate([np.arange(nc), st_indices]),
+        np.concatenate([np.ones(nc, np.float32), st_weights]))
+    refine = GB300StencilTable.Create(st_sizes, st_offsets, st_indices, st_weights)
+    setup = []
+    lim = None
+    for _ in range(max(args.warmup, 3)):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lim = GB300StencilTable.FromPatchCoords(table, pc, base, channels=3, stream=stream)
+        torch.cuda.synchronize()
+        setup.append((time.perf_counter() - t0) * 1e3)
+    nnz = lim.GetNumIndices()
+    d = BD(0, 3, 3)
+    cage = torch.from_numpy(pos.ravel()).cuda()
+    srcbuf = torch.zeros(len(z["src"]), device="cuda")
+    srcbuf[: nc * 3] = cage
+    a_out = [torch.empty(n * 3, device="cuda") for _ in range(3)]
+    b_out = [torch.empty(n * 3, device="cuda") for _ in range(3)]
+
+    def path_a():
+        Ev.EvalStencilsTable(cage, d, a_out[0], d, lim, du=a_out[1], duDesc=d, dv=a_out[2],
+                             dvDesc=d, stream=stream)
+
+    def path_b():
+        Ev.EvalStencilsTable(srcbuf, d, srcbuf, BD(nc * 3, 3, 3), refine, stream=stream)
+        m.Evaluate(srcbuf, d, table, pc, 1, b_out)
+
+    res = {}
+    for name, fn in (("stencils_from_cage", path_a), ("refine_then_patches", path_b)):
+        with torch.cuda.stream(stream):
+            for _ in range(args.warmup):
+                fn()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+              for _ in range(args.steps)]
+        with torch.cuda.stream(stream):
+            for e0, e1 in ev:
+                e0.record(stream)
+                fn()
+                e1.record(stream)
+        torch.cuda.synchronize()
+        res[name] = float(np.median([e0.elapsed_time(e1) for e0, e1 in ev]))
+    diag = float(np.linalg.norm(pos.max(0).astype(np.float64) - pos.min(0)))
+    err = max(float((a - b).abs().max()) for a, b in zip(a_out, b_out))
+    sb = workloads.stencil_bytes(n, nnz, 3, nc, n_weight_arrays=3, n_outputs=3)
+    return {
+        "workload": "torus256x128 (5% triangles, 2% creases), uniform rate 5, P/Du/Dv, "
+                    "Bfr::SurfaceFactory default approximation as a Far table",
+        "faces": int(len(z["verts_per_face"])), "points": n, "stencil_entries": int(nnz),
+        "setup_ms_host": float(np.median(setup)),
+        "frame_ms": res,
+        "frame_points_per_s": {k: n / (v / 1e3) for k, v in res.items()},
+        "roofline_stencils_from_cage": {
+            "bound": "hbm", "kernel": "EvalStencils over the point stencils",
+            "algorithmic_bytes": sb, "achieved": sb / (res["stencils_from_cage"] / 1e3) / 1e9,
+            "peak": peak, "unit": "GB/s",
+            "frac": sb / (res["stencils_from_cage"] / 1e3) / 1e9 / peak},
+        "max_abs_diff_between_paths_rel_bbox_diag": err / diag,
+    }
 
 
 def bench_batch(args, stream, peak, cv_max):

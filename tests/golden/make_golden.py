@@ -678,6 +678,32 @@ def large_bfr_workload(path, cage, rate=5, sample=0.02, seed=7):
     os.replace(tmp, path)
 
 
+def large_bfr_stencil_workload(path, cage):
+    """The Bfr limit-stencil benchmark's inputs: the Far table of Bfr::SurfaceFactory's default
+    approximation for `cage` (as large_bfr_workload builds it), its source points, and Far's
+    stencils of the refined and local points (the rows after the cage points) over the cage:
+    the base GB300TessellationStencils composes over.  Written under large/ (kept out of git)."""
+    r = ref.Refiner(cage).refine_adaptive_levels(6, 2, True)
+    p = ref.Patches(r, endcap=3, max_isolation=6, inf_sharp=True, share_endcap_points=False,
+                    legacy_sharp_corners=False)
+    nc = cage.num_vertices
+    ns = len(p.st["sizes"])
+    buf = np.zeros((nc + ns) * 3, np.float32)
+    buf[: nc * 3] = cage.positions.reshape(-1)
+    ref.omp_set_threads(os.cpu_count() or 1)
+    assert ref.cpu_eval_stencils(buf, (0, 3, 3), [buf], [(nc * 3, 3, 3)], p.st["sizes"],
+                                 p.st["offsets"], p.st["indices"], [p.st["weights"]], 0, ns,
+                                 omp=True)
+    os.makedirs(os.path.dirname(path), exist_ok=True)
+    tmp = path + ".tmp.npz"
+    np.savez_compressed(tmp, positions=cage.positions, verts_per_face=cage.verts_per_face,
+                        face_verts=cage.face_verts, arrays=p.arrays, patch_indices=p.indices,
+                        params=p.params, src=buf, st_sizes=p.st["sizes"],
+                        st_offsets=p.st["offsets"], st_indices=p.st["indices"],
+                        st_weights=p.st["weights"])
+    os.replace(tmp, path)
+
+
 def large_workloads():
     """The EvalPatches benchmark tables: the plain-method torus (512 x 256, R = 1, r = 0.3,
     seeded 5% triangles and 2% creases U[0, 4]; the cage of the stencil benchmark) and the
@@ -689,6 +715,9 @@ def large_workloads():
     ico = shapes.icosphere(6, noise=0.005, seed=3)
     large_patch_workload(os.path.join(LARGE, "icosphere6_loop_adaptiveL4.npz"), ico, 4)
     large_bfr_workload(os.path.join(LARGE, "torus512x256_bfr.npz"), torus)
+    large_bfr_stencil_workload(os.path.join(LARGE, "torus256x128_bfr_stencils.npz"),
+                               shapes.torus(256, 128, R=1.0, r=0.3, tri_fraction=0.05,
+                                            crease_fraction=0.02, max_sharpness=4.0, seed=2024))
 
 
 def main():
@@ -711,6 +740,12 @@ def main():
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr-stencils":
         bfr_stencil_fixture(os.path.join(HERE, "bfr_stencils.npz"))
+        return
+    if len(sys.argv) > 1 and sys.argv[1] == "bfr-stencils-large":
+        large_bfr_stencil_workload(
+            os.path.join(LARGE, "torus256x128_bfr_stencils.npz"),
+            shapes.torus(256, 128, R=1.0, r=0.3, tri_fraction=0.05, crease_fraction=0.02,
+                         max_sharpness=4.0, seed=2024))
         return
     if len(sys.argv) > 1 and sys.argv[1] == "bfr-large":
         torus = shapes.torus(512, 256, R=1.0, r=0.3, tri_fraction=0.05, crease_fraction=0.02,
