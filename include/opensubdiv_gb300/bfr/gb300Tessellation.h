@@ -186,6 +186,20 @@ public:
                                                   pointCoords, stream) == GB300_OK;
     }
 
+    /// Varying values at `numPoints` PatchCoords: the linear surfaces of
+    /// Bfr::SurfaceFactory::InitVaryingSurface (bfr/surfaceFactory.h:252), as the table's
+    /// varying patches (GB300PatchTableEvalVarying) over `src` holding the varying values of
+    /// the control and refined vertices (Far::StencilTableFactory, INTERPOLATE_VARYING).
+    bool EvaluateVarying(Osd::GB300PatchTable const *table, Osd::PatchCoord const *patchCoords,
+                         int numPoints, float const *src, int length, int srcStride,
+                         float *value, float *du = NULL, float *dv = NULL,
+                         void *stream = NULL) const {
+        return table && GB300PatchTableEvalVarying(table->GetHandle(), src, value, du, dv, NULL,
+                                                   NULL, NULL, length, srcStride, length,
+                                                   length, length, length, length, length,
+                                                   numPoints, patchCoords, stream) == GB300_OK;
+    }
+
     /// Bfr::Surface::EvaluateStencil at `numPoints` PatchCoords (those of Generate, or the
     /// shared points of Share; GB300TessellationStencils): a limit stencil table over the
     /// mesh's control vertices -- P and, with numChannels 3, Du and Dv (6: also the second

@@ -262,6 +262,27 @@ class MeshTessellation:
         return outs[:k]
 
 
+    def EvaluateVarying(self, src, src_desc, table, patch_coords, derivatives=0, outputs=None,
+                        num_points=None):
+        """Varying values at every coord (the linear surfaces of
+        Bfr::SurfaceFactory::InitVaryingSurface, bfr/surfaceFactory.h:252): `table`'s varying
+        patches (GB300PatchTable.SetVarying, or Create from a Far table) at the coords'
+        PatchCoords, over `src` holding the varying values of the control vertices and of the
+        refined vertices (Far::StencilTableFactory in INTERPOLATE_VARYING mode) --
+        GB300PatchTableEvalVarying; value, and with derivatives >= 1 d/du and d/dv, each
+        [n, length] float32."""
+        torch = _torch()
+        n = self.num_coords if num_points is None else int(num_points)
+        L = src_desc.length
+        k = 1 if derivatives == 0 else 3
+        outs = outputs if outputs is not None else [
+            torch.zeros((n, L), dtype=torch.float32, device="cuda") for _ in range(k)]
+        ptrs = [_ptr(outs[i]) if i < k else None for i in range(6)]
+        check(_lib.load().GB300PatchTableEvalVarying(
+            table.handle, _ptr(src, src_desc.offset), *ptrs, L, src_desc.stride, *([L] * 6), n,
+            _ptr(patch_coords), _stream(self.stream)))
+        return outs[:k]
+
     def EvaluateFaceVarying(self, src, src_desc, table, patch_coords, channel=0, derivatives=0,
                             outputs=None):
         """Face-varying values at every coord (the face-varying surfaces of

@@ -468,3 +468,20 @@ def bfr_stencils(refiner, rate_offsets, rates, num_coords, facet_size=3, preserv
     off = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
     return dict(sizes=sizes, offsets=off, indices=idx[:n], wP=w[0][:n], wDu=w[1][:n],
                 wDv=w[2][:n])
+
+
+def bfr_varying(refiner, rate_offsets, rates, num_coords, values, facet_size=3,
+                preserve_quads=False, approx_sharp=6, approx_smooth=2):
+    """Varying surfaces (SurfaceFactory::InitVaryingSurface) evaluated at every coord of the
+    reference's tessellate loop: [coords, length] from `values` [vertices, length]."""
+    L = lib()
+    L.ref_bfr_varying.restype = C.c_long
+    v = np.ascontiguousarray(values, np.float32)
+    out = np.zeros((max(num_coords, 1), v.shape[1]), np.float32)
+    n = L.ref_bfr_varying(refiner.h, C.c_int(approx_sharp), C.c_int(approx_smooth),
+                          _p(np.ascontiguousarray(rate_offsets, np.int32)),
+                          _p(np.ascontiguousarray(rates, np.int32)), C.c_int(facet_size),
+                          C.c_int(int(preserve_quads)), _p(v), C.c_int(v.shape[1]), _p(out))
+    if n != num_coords:
+        raise ValueError(f"varying loop visited {n} coords, expected {num_coords}")
+    return out[:num_coords]

@@ -1054,6 +1054,41 @@ long ref_bfr_stencils(void *refiner, int approxSharp, int approxSmooth, const in
     return ne;
 }
 
+// Varying surfaces (Bfr::SurfaceFactory::InitVaryingSurface, bfr/surfaceFactory.h:252) at
+// every coord of the reference's tessellate loop (faces and coords in ref_bfr_mesh_record's
+// order): `values` holds `length` floats per mesh vertex; writes the evaluated value per coord.
+// Returns the number of coords.
+long ref_bfr_varying(void *refiner, int approxSharp, int approxSmooth, const int *rateOffsets,
+                     const int *rates, int facetSize, int preserveQuads, const float *values,
+                     int length, float *out) {
+    Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
+    Bfr::SurfaceFactory::Options so;
+    so.SetApproxLevelSharp(approxSharp);
+    so.SetApproxLevelSmooth(approxSmooth);
+    Bfr::RefinerSurfaceFactory<> factory(mesh, so);
+    const int nf = factory.GetNumFaces();
+    Bfr::Tessellation::Options to = tessOptions(facetSize == 4 ? 4 : 3, preserveQuads);
+    Bfr::Surface<float> sf, sv;
+    std::vector<float> coords, patch;
+    long nc = 0;
+    for (int f = 0; f < nf; ++f) {
+        if (!factory.InitVertexSurface(f, &sf)) continue;
+        Bfr::Tessellation t(sf.GetParameterization(), rateOffsets[f + 1] - rateOffsets[f],
+                            rates + rateOffsets[f], to);
+        if (!t.IsValid()) continue;
+        const int n = t.GetNumCoords();
+        coords.resize(2 * (size_t)n);
+        t.GetCoords(coords.data());
+        if (!factory.InitVaryingSurface(f, &sv)) return -1;
+        patch.resize((size_t)sv.GetNumPatchPoints() * length);
+        sv.PreparePatchPoints(values, length, patch.data(), length);
+        for (int i = 0; i < n; ++i)
+            sv.Evaluate(&coords[2 * i], patch.data(), length, out + (size_t)(nc + i) * length);
+        nc += n;
+    }
+    return nc;
+}
+
 // The tessellation with shared vertex and edge points of the reference's tutorial 2.2
 // (tutorials/bfr/tutorial_2_2/bfr_tutorial_2_2.cpp:160-430), with per-face rates: faces in
 // order through Bfr::RefinerSurfaceFactory (faces without a limit surface skipped), the

@@ -612,6 +612,20 @@ def bfr_stencil_fixture(path):
             out[f"{key}__st_{k}"] = np.asarray(st[k])
         for k in ("sizes", "indices", "wP", "wDu", "wDv"):
             out[f"{key}__bfr_{k}"] = bfr[k]
+        # varying surfaces (InitVaryingSurface): seeded values per vertex, Far's varying
+        # patches and varying stencils of the same refinement, and Bfr's values at every coord
+        rng = np.random.default_rng(400 + len(out))
+        vals = rng.uniform(-1, 1, (cage.num_vertices, 3)).astype(np.float32)
+        va, vi = p.varying()
+        vst = ref.stencil_table_mode(r, mode=ref.INTERPOLATE_VARYING)
+        out[f"{key}__var_values"] = vals
+        out[f"{key}__var_arrays"] = va
+        out[f"{key}__var_indices"] = vi
+        for k in ("sizes", "offsets", "indices", "weights"):
+            out[f"{key}__var_st_{k}"] = np.asarray(vst[k])
+        out[f"{key}__var_bfr"] = ref.bfr_varying(
+            ref.Refiner(cage), d["rate_offsets"], d["rates"], int(d["coord_offsets"][-1]), vals,
+            int(d["facet_size"]), bool(d["preserve_quads"]))
     np.savez_compressed(path, **out)
 
 

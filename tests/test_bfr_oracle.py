@@ -297,3 +297,32 @@ def test_point_stencils_match_bfr_evaluate_stencil(key):
             assert np.abs(da - db).max() <= 2e-6 * max(1.0, np.abs(db).max()), (key, i, ow)
         checked += 1
     assert checked > 0 or not regular.any()
+
+
+def varying_source(g, key):
+    """Varying values of the control vertices, then of every refined vertex (Far's varying
+    stencils): the points the varying patches index."""
+    vals = g[f"{key}__var_values"]
+    nc = len(vals)
+    sizes = g[f"{key}__var_st_sizes"]
+    src = np.zeros((nc + len(sizes)) * 3, np.float32)
+    src[: nc * 3] = vals.ravel()
+    oracle.eval_stencils(src, (0, 3, 3), [src], [(nc * 3, 3, 3)], sizes,
+                         g[f"{key}__var_st_offsets"], g[f"{key}__var_st_indices"],
+                         [g[f"{key}__var_st_weights"]])
+    return src
+
+
+@pytest.mark.parametrize("key", STENCIL_MESHES)
+def test_far_varying_patches_agree_with_bfr_varying_surfaces(key):
+    """Bfr::SurfaceFactory::InitVaryingSurface evaluated by the reference at every coord
+    against the paired Far table's varying patches at the located coords, over Far's varying
+    refinement of the same values: equal within float rounding (1e-6)."""
+    z = np.load(os.path.join(GOLDEN, key + ".npz"))
+    g = np.load(STENCILS)
+    src = varying_source(g, key)
+    coords = oracle.make_coords(z["q_handles"], z["q_s"], z["q_t"])
+    out = [np.zeros(len(coords) * 3, np.float32)]
+    assert oracle.eval_patches(src, (0, 3, 3), out, [(0, 3, 3)], coords, g[f"{key}__var_arrays"],
+                               g[f"{key}__var_indices"], z["params"], threads=4)
+    assert np.abs(out[0].reshape(-1, 3) - g[f"{key}__var_bfr"]).max() <= 1e-6

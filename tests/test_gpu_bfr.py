@@ -405,3 +405,33 @@ def test_point_stencils_on_the_device(key):
         got = host(outs[k]).reshape(-1, 3).astype(np.float64)
         assert np.abs(got - host(per[k]).reshape(-1, 3)).max() <= 1e-5 * diag * (1 if k == 0 else 4), k
         assert np.abs(got - z["out6"][k]).max() <= tol[k], k
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("key", STENCIL_MESHES)
+def test_mesh_varying_values_match_bfr(key):
+    """Varying surfaces (InitVaryingSurface) at every coord on the device: the values refined
+    by EvalStencils with Far's varying stencils, then MeshTessellation.EvaluateVarying at the
+    located coords -- within 1e-6 of the reference's Bfr varying evaluation."""
+    torch = torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300.evaluator import (BufferDescriptor as BD, GB300Evaluator as Ev,
+                                            GB300PatchTable, GB300StencilTable)
+    z = np.load(os.path.join(GOLDEN, key + ".npz"))
+    g = np.load(STENCILS)
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"],
+                                   bool(z["triangular"]))
+    table.SetVarying(g[f"{key}__var_arrays"], g[f"{key}__var_indices"])
+    opt = bfr.TessellationOptions(int(z["facet_size"]), bool(z["preserve_quads"]))
+    m = bfr.MeshTessellation(int(z["regular_face_size"]), z["verts_per_face"], rates=z["rates"],
+                             rate_offsets=z["rate_offsets"], options=opt)
+    _, _, pc = m.Generate(table=table)
+    vals = g[f"{key}__var_values"]
+    nc = len(vals)
+    vst = GB300StencilTable.Create(g[f"{key}__var_st_sizes"], g[f"{key}__var_st_offsets"],
+                                   g[f"{key}__var_st_indices"], g[f"{key}__var_st_weights"])
+    src = torch.zeros((nc + vst.GetNumStencils()) * 3, device="cuda")
+    src[: nc * 3] = dev(vals.ravel())
+    assert Ev.EvalStencilsTable(src, BD(0, 3, 3), src, BD(nc * 3, 3, 3), vst)
+    (val,) = m.EvaluateVarying(src, BD(0, 3, 3), table, pc)
+    assert np.abs(host(val) - g[f"{key}__var_bfr"]).max() <= 1e-6
