@@ -58,8 +58,10 @@ __host__ __device__ constexpr int last_output(int order) { return order == 0 ? 0
 
 // 5 resident blocks per SM where the registers allow it without spills (0.2847 vs 0.2908 ms
 // for 4 M Loop points at LC = 3; LC = 4 would spill)
-template <int LC, int ORDER>
-__global__ void __launch_bounds__(128, LC == 4 ? 4 : (ORDER < 2 ? 6 : 5))
+// QUAD: Catmull-Clark tables (REGULAR / GREGORY_BASIS / QUADS only): without the Loop and
+// triangle bases the kernel fits 7 blocks per SM for orders 0 and 1 without spills.
+template <int LC, int ORDER, bool QUAD = false>
+__global__ void __launch_bounds__(128, LC == 4 ? 4 : (ORDER < 2 ? (QUAD ? 7 : 6) : 5))
     k_eval_patches(const PatchArgs a) {
     const int stride = gridDim.x * blockDim.x;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.numCoords; i += stride) {
@@ -75,8 +77,8 @@ __global__ void __launch_bounds__(128, LC == 4 ? 4 : (ORDER < 2 ? 6 : 5))
                 const int type = p.regular() ? arr.regDesc : arr.desc;
                 const int *cvs =
                     a.indices + arr.indexBase + arr.stride * (c.patchIndex - arr.primitiveIdBase);
-                if (!eval_patch_point<LC>(type, p, c.s, c.t, cvs, a.src, a.srcStride, e0,
-                                          a.length, acc, d1, d2))
+                if (!eval_patch_point<LC, QUAD>(type, p, c.s, c.t, cvs, a.src, a.srcStride, e0,
+                                                a.length, acc, d1, d2))
                     acc.zero();
             }
             const float scale[6] = {1.0f, d1, d1, d2, d2, d2};
@@ -151,13 +153,13 @@ void launch_lanes(int G, int grid, int threads, cudaStream_t s, const PatchArgs 
     }
 }
 
-template <int ORDER>
+template <int ORDER, bool QUAD>
 void launch_points(int length, int grid, int threads, cudaStream_t s, const PatchArgs &a) {
     switch (length) {
-        case 1: k_eval_patches<1, ORDER><<<grid, threads, 0, s>>>(a); break;
-        case 2: k_eval_patches<2, ORDER><<<grid, threads, 0, s>>>(a); break;
-        case 3: k_eval_patches<3, ORDER><<<grid, threads, 0, s>>>(a); break;
-        default: k_eval_patches<4, ORDER><<<grid, threads, 0, s>>>(a); break;
+        case 1: k_eval_patches<1, ORDER, QUAD><<<grid, threads, 0, s>>>(a); break;
+        case 2: k_eval_patches<2, ORDER, QUAD><<<grid, threads, 0, s>>>(a); break;
+        case 3: k_eval_patches<3, ORDER, QUAD><<<grid, threads, 0, s>>>(a); break;
+        default: k_eval_patches<4, ORDER, QUAD><<<grid, threads, 0, s>>>(a); break;
     }
 }
 
@@ -214,9 +216,15 @@ int eval_patches(const float *src, float *const *dst, const int *strides, int le
     long long blocks = ((long long)numCoords + threads - 1) / threads;
     long long cap = (long long)num_sms() * 32;
     const int grid = (int)(blocks < cap ? blocks : cap);
-    if (order == 0) launch_points<0>(length, grid, threads, s, a);
-    else if (order == 1) launch_points<1>(length, grid, threads, s, a);
-    else launch_points<2>(length, grid, threads, s, a);
+    if (quadFamily) {
+        if (order == 0) launch_points<0, true>(length, grid, threads, s, a);
+        else if (order == 1) launch_points<1, true>(length, grid, threads, s, a);
+        else launch_points<2, true>(length, grid, threads, s, a);
+    } else {
+        if (order == 0) launch_points<0, false>(length, grid, threads, s, a);
+        else if (order == 1) launch_points<1, false>(length, grid, threads, s, a);
+        else launch_points<2, false>(length, grid, threads, s, a);
+    }
     count_launch();
     return check_launch(who);
 }
