@@ -293,7 +293,7 @@ def bench_bfr(args, stream, peak):
             ro, rates = workloads.bfr_edge_length_rates(z["positions"], z["verts_per_face"],
                                                         z["face_verts"], BFR_INTERVAL)
             kw = dict(rates=rates, rate_offsets=ro)
-            rate_desc = (f"edge rates ceil(length / {BFR_INTERVAL}) (mean {rates.mean():.2f}, "
+            rate_desc = (f"edge rates 1 + int(hull length / {BFR_INTERVAL}) (mean {rates.mean():.2f}, "
                          f"{rates.min()}..{rates.max()})")
         m = bfr.MeshTessellation(4, sizes_host, options=bfr.TessellationOptions(3), stream=stream,
                                  **kw)

@@ -412,20 +412,23 @@ def serving_queries(topo, n, seed):
 
 def bfr_edge_length_rates(positions, verts_per_face, face_verts, interval, max_rate=64):
     """Per-face edge rates from control-hull edge lengths, the non-uniform scheme of the
-    reference's Bfr tutorial 2.1 (tutorials/bfr/tutorial_2_1/bfr_tutorial_2_1.cpp): an edge's
-    rate is ceil(length / interval) clamped to [1, max_rate]; both faces of an edge see the
-    same length, so shared edges get one rate.  Returns (rate_offsets, rates) with N rates per
-    N-sided face (rates[i] for the edge from vertex i to i + 1)."""
+    reference's Bfr tutorial 2.1 with its hull option (tutorials/bfr/tutorial_2_1/
+    bfr_tutorial_2_1.cpp:121-166): an edge's length in float from the absolute coordinate
+    differences of its two control points, its rate 1 + (int)(length / interval) capped at
+    max_rate; both faces of an edge see the same length, so shared edges get one rate.
+    Returns (rate_offsets, rates) with N rates per N-sided face (rates[i] for the edge from
+    vertex i to i + 1)."""
     vpf = np.asarray(verts_per_face, np.int64)
     fv = np.asarray(face_verts, np.int64)
     start = np.concatenate([[0], np.cumsum(vpf)])
     nxt = np.arange(len(fv)) + 1
     last = start[1:] - 1
     nxt[last] = start[:-1]
-    p = np.asarray(positions, np.float64)
-    length = np.linalg.norm(p[fv[nxt]] - p[fv], axis=1)
-    rates = np.clip(np.ceil(length / interval), 1, max_rate).astype(np.int32)
-    return start.astype(np.int32), rates
+    p = np.asarray(positions, np.float32)
+    dv = np.abs(p[fv] - p[fv[nxt]])
+    length = np.sqrt(dv[:, 0] * dv[:, 0] + dv[:, 1] * dv[:, 1] + dv[:, 2] * dv[:, 2])
+    rates = np.minimum(1 + (length / np.float32(interval)).astype(np.int32), max_rate)
+    return start.astype(np.int32), rates.astype(np.int32)
 
 
 def bfr_tess_bytes(n_faces, n_coords, n_facets, facet_size, locate=True, uniform=True):
