@@ -80,6 +80,23 @@ public:
         GB300TessellationOptions _o;
     };
 
+    /// Per-edge rates from edge lengths, as the reference's Bfr tutorial 2.1 computes them
+    /// (GB300TessellationEdgeRates): for each face corner, 1 + (int)(length / interval) capped
+    /// at maxRate, the length between the points of the corner and the next corner -- mesh
+    /// vertex points named by faceVerts (the hull option), or one point per corner
+    /// (pointsPerCorner: the limit option).  Writes DEVICE rateOffsets (numFaces + 1) and rates
+    /// (numCorners) for Create's per-face form.
+    static bool ComputeEdgeRates(int numFaces, int const *faceSizes, int const *faceVerts,
+                                 int64_t numCorners, float const *points, int numPoints,
+                                 int pointStride, bool pointsPerCorner, float interval,
+                                 int maxRate, int *rateOffsets, int *rates,
+                                 void *stream = NULL) {
+        return GB300TessellationEdgeRates(numFaces, faceSizes, faceVerts, numCorners, points,
+                                          numPoints, pointStride, pointsPerCorner ? 1 : 0,
+                                          interval, maxRate, rateOffsets, rates,
+                                          stream) == GB300_OK;
+    }
+
     /// Every face at one uniform rate (Tessellation(param, uniformRate, options)).
     /// faceSizes: DEVICE array of numFaces face sizes; regularFaceSize: the scheme's regular
     /// face size (Sdc::SchemeTypeTraits::GetRegularFaceSize).  NULL on failure

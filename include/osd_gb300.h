@@ -340,6 +340,22 @@ int GB300TessellationEvaluate(const GB300PatchTable *table, const float *src, fl
                               int duuStride, int duvStride, int dvvStride, int numCoords,
                               const void *patchCoords, void *stream);
 
+/* Per-edge tessellation rates from edge lengths, the non-uniform rates of the reference's Bfr
+ * tutorial 2.1 (tutorials/bfr/tutorial_2_1/bfr_tutorial_2_1.cpp:121-166, 240-308): for every
+ * face corner, the length of the edge to the next corner of its face (float, from the absolute
+ * coordinate differences of the two points) and the rate 1 + (int)(length / interval), capped
+ * at maxRate.  Points (DEVICE, xyz at `pointStride` floats): with pointsPerCorner 0, one per
+ * mesh vertex, named by faceVerts (the tutorial's control-hull option); with pointsPerCorner 1,
+ * one per face corner in corner order (the tutorial's limit option: the limit positions at the
+ * face's corners, e.g. GB300TessellationEvaluate at the rate-1 tessellation's vertex coords).
+ * Writes rates (DEVICE, numCorners ints) and, if not NULL, rateOffsets (DEVICE, numFaces + 1:
+ * the exclusive scan of the face sizes), the per-face runs GB300TessellationCount takes.  With
+ * hull points a shared edge gets one rate from both faces.  Synchronizes `stream`. */
+int GB300TessellationEdgeRates(int numFaces, const int *faceSizes, const int *faceVerts,
+                               int64_t numCorners, const float *points, int numPoints,
+                               int pointStride, int pointsPerCorner, float interval,
+                               int maxRate, int *rateOffsets, int *rates, void *stream);
+
 /* Shared (watertight) points of a mesh tessellation: the bookkeeping of the reference's Bfr
  * tutorial with shared vertex and edge points (tutorials/bfr/tutorial_2_2/
  * bfr_tutorial_2_2.cpp:244-430), for every face at once, after Count and Generate with the

@@ -58,6 +58,8 @@ _PROTOS = {
     "GB300TessellationGenerate": (i32, [i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, vp, vp, i32,
                                         vp, vp, vp]),
     "GB300TessellationEvaluate": (i32, [vp, vp] + [vp] * 6 + [i32] * 8 + [i32, vp, vp]),
+    "GB300TessellationEdgeRates": (i32, [i32, vp, vp, i64, vp, i32, i32, i32, C.c_float, i32,
+                                         vp, vp, vp]),
     "GB300TessellationStencils": (vp, [vp, i32, vp, i32, i64, vp, vp, vp, vp, i32, i32, vp]),
     "GB300TessellationShare": (i32, [i32, i32, vp, vp, vp, i32, vp, vp, vp, vp, vp, i64, i32,
                                      i32, vp, i32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp]),

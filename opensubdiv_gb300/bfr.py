@@ -96,6 +96,34 @@ def _torch():
     return torch
 
 
+def EdgeRates(face_sizes, face_verts, points, interval, max_rate=10, points_per_corner=False,
+              stride=3, stream=None):
+    """Per-edge rates from edge lengths, as the reference's Bfr tutorial 2.1 computes them
+    (GB300TessellationEdgeRates): rate 1 + int(length / interval) capped at max_rate, lengths
+    between the points of consecutive face corners -- mesh-vertex points named by face_verts
+    (the tutorial's hull option), or one point per face corner (its limit option).  Returns
+    (rate_offsets [faces + 1], rates [corners]) as int32 CUDA tensors, ready for
+    MeshTessellation(rates=..., rate_offsets=...)."""
+    torch = _torch()
+    dev = torch.device("cuda")
+
+    def on_device(x, dtype):
+        t = x if hasattr(x, "data_ptr") else torch.from_numpy(np.ascontiguousarray(x))
+        return t.to(dev, dtype).contiguous()
+
+    sizes = on_device(face_sizes, torch.int32)
+    fv = on_device(face_verts, torch.int32)
+    pts = on_device(points, torch.float32).reshape(-1)
+    nf, nc = int(sizes.numel()), int(fv.numel())
+    offsets = torch.empty(nf + 1, dtype=torch.int32, device=dev)
+    rates = torch.empty(max(nc, 1), dtype=torch.int32, device=dev)
+    check(_lib.load().GB300TessellationEdgeRates(
+        nf, _ptr(sizes), _ptr(fv), nc, _ptr(pts), int(pts.numel()) // stride, int(stride),
+        int(bool(points_per_corner)), float(interval), int(max_rate), _ptr(offsets),
+        _ptr(rates), _stream(stream)))
+    return offsets, rates[:nc]
+
+
 class SharedPoints:
     """The shared points of MeshTessellation.Share (attributes set there; the full-capacity
     buffers behind patch_coords, coords and faces are kept for reuse through `out`)."""

@@ -708,6 +708,60 @@ __global__ void __launch_bounds__(256, 4) k_share_emit(const ShareArgs a) {
     }
 }
 
+// ---- edge rates from edge lengths (tutorial 2.1) ---------------------------------------------
+// Thread per face corner: the length of the edge from the corner to the next corner of its
+// face, from the corners' points (mesh vertices, or one point per corner), and the rate
+// 1 + (int)(length / interval) capped at maxRate (tutorials/bfr/tutorial_2_1/
+// bfr_tutorial_2_1.cpp:121-166).  Every float step is explicitly rounded, so a shared edge
+// gets the same rate from both of its faces.
+struct RateArgs {
+    int numFaces, perCorner, stride, maxRate, numPoints;
+    int64_t numCorners;
+    float interval;
+    const int *faceSizes, *faceVerts;
+    const int64_t *cornerOff;
+    const float *points;
+    int *rates, *rateOffsets;
+    int *err;
+};
+
+__global__ void __launch_bounds__(256) k_edge_rates(const RateArgs a) {
+    const int stride = gridDim.x * blockDim.x;
+    for (int f = blockIdx.x * blockDim.x + threadIdx.x; f <= a.numFaces; f += stride) {
+        const int64_t c0 = a.cornerOff[f];
+        if (a.rateOffsets) a.rateOffsets[f] = (int)c0;
+        if (f == a.numFaces) continue;
+        const int N = a.faceSizes[f];
+        if (c0 + N > a.numCorners) {
+            atomicAdd(a.err, 1);
+            continue;
+        }
+        for (int i = 0; i < N; ++i) {
+            const int64_t ci = c0 + i, cj = c0 + (i + 1 == N ? 0 : i + 1);
+            int64_t pi = ci, pj = cj;
+            if (!a.perCorner) {
+                pi = a.faceVerts[ci];
+                pj = a.faceVerts[cj];
+                if ((uint64_t)pi >= (uint64_t)a.numPoints || (uint64_t)pj >= (uint64_t)a.numPoints) {
+                    atomicAdd(a.err, 1);
+                    a.rates[ci] = 1;
+                    continue;
+                }
+            }
+            const float *x0 = a.points + pi * a.stride, *x1 = a.points + pj * a.stride;
+            const float d0 = fabsf(__fsub_rn(x0[0], x1[0]));
+            const float d1 = fabsf(__fsub_rn(x0[1], x1[1]));
+            const float d2 = fabsf(__fsub_rn(x0[2], x1[2]));
+            const float len = __fsqrt_rn(
+                __fadd_rn(__fadd_rn(__fmul_rn(d0, d0), __fmul_rn(d1, d1)), __fmul_rn(d2, d2)));
+            const float q = __fdiv_rn(len, a.interval);
+            // (int) of the quotient, saturated before the cap
+            const int r = q < (float)a.maxRate ? 1 + (int)q : a.maxRate;
+            a.rates[ci] = r < a.maxRate ? r : a.maxRate;
+        }
+    }
+}
+
 // Shared uniform patterns, cached per device and request (they depend only on the scheme's
 // face size, the rate and the facet options) up to kPatternCacheBytes; beyond that a call
 // builds them in per-call scratch.
@@ -1148,5 +1202,83 @@ extern "C" int GB300TessellationShare(
                     "points (first in face %d): shared points need one rate per edge",
                     who, host[2], host[3]);
     *numPoints = points;
+    return ok();
+}
+
+extern "C" int GB300TessellationEdgeRates(int numFaces, const int *faceSizes,
+                                          const int *faceVerts, int64_t numCorners,
+                                          const float *points, int numPoints, int pointStride,
+                                          int pointsPerCorner, float interval, int maxRate,
+                                          int *rateOffsets, int *rates, void *stream) {
+    const char *who = "GB300TessellationEdgeRates";
+    if (numFaces < 0 || numCorners < 0 || (numFaces > 0 && !faceSizes) || !rates ||
+        !points || pointStride < 3 || !(interval > 0.0f) || maxRate < 1 ||
+        (!pointsPerCorner && (!faceVerts || numPoints < 0)))
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: bad arguments", who);
+    cudaStream_t s = as_stream(stream);
+    const size_t n1 = (size_t)numFaces + 1;
+    auto up = [](size_t b) { return (b + 255) & ~size_t(255); };
+    size_t scanBytes = 0;
+    int st = check_cuda(cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (int64_t *)nullptr,
+                                                      (int64_t *)nullptr, (int)n1, s),
+                        who);
+    if (st != GB300_OK) return st;
+    char *mem = nullptr;
+    if ((st = scratch_alloc((void **)&mem, 2 * up(8 * n1) + up(8 * 4) + up(scanBytes), s,
+                            who)) != GB300_OK)
+        return st;
+    ShareArgs sa{};
+    sa.numFaces = numFaces;
+    sa.faceSizes = faceSizes;
+    sa.counts = (int64_t *)mem;
+    sa.err = (int *)(mem + 2 * up(8 * n1));
+    sa.numVertices = sa.numEdges = 0;
+    RateArgs a{};
+    a.numFaces = numFaces;
+    a.perCorner = pointsPerCorner != 0;
+    a.stride = pointStride;
+    a.maxRate = maxRate;
+    a.numPoints = pointsPerCorner ? 0 : numPoints;
+    a.numCorners = numCorners;
+    a.interval = interval;
+    a.faceSizes = faceSizes;
+    a.faceVerts = faceVerts;
+    a.cornerOff = (const int64_t *)(mem + up(8 * n1));
+    a.points = points;
+    a.rates = rates;
+    a.rateOffsets = rateOffsets;
+    a.err = sa.err;
+    const int grid = grid_for((long long)n1, 256, 16);
+    k_share_init<<<grid, 256, 0, s>>>(sa);  // face sizes into counts, error words cleared
+    count_launch();
+    st = check_launch(who);
+    if (st == GB300_OK)
+        st = check_cuda(cub::DeviceScan::ExclusiveSum(mem + 2 * up(8 * n1) + up(32), scanBytes,
+                                                      sa.counts, (int64_t *)a.cornerOff,
+                                                      (int)n1, s),
+                        who);
+    if (st == GB300_OK) {
+        k_edge_rates<<<grid, 256, 0, s>>>(a);
+        count_launch();
+        st = check_launch(who);
+    }
+    int host[2] = {0, 0};
+    int64_t corners = 0;
+    if (st == GB300_OK)
+        st = check_cuda(cudaMemcpyAsync(host, a.err, sizeof(host), cudaMemcpyDeviceToHost, s), who);
+    if (st == GB300_OK)
+        st = check_cuda(cudaMemcpyAsync(&corners, a.cornerOff + numFaces, sizeof(corners),
+                                        cudaMemcpyDeviceToHost, s),
+                        who);
+    scratch_free(mem, s);
+    if (st == GB300_OK) st = check_cuda(cudaStreamSynchronize(s), who);
+    if (st != GB300_OK) return st;
+    if (corners != numCorners)
+        return fail(GB300_ERR_INVALID_ARGUMENT,
+                    "%s: the face sizes add up to %lld corners, not %lld", who,
+                    (long long)corners, (long long)numCorners);
+    if (host[0])
+        return fail(GB300_ERR_INVALID_ARGUMENT, "%s: %d vertex indices out of range", who,
+                    host[0]);
     return ok();
 }

@@ -435,3 +435,74 @@ def test_mesh_varying_values_match_bfr(key):
     assert Ev.EvalStencilsTable(src, BD(0, 3, 3), src, BD(nc * 3, 3, 3), vst)
     (val,) = m.EvaluateVarying(src, BD(0, 3, 3), table, pc)
     assert np.abs(host(val) - g[f"{key}__var_bfr"]).max() <= 1e-6
+
+
+def tutorial_rates(points_per_corner, sizes, interval, max_rate):
+    """Tutorial 2.1's rule on host points, one per face corner (float arithmetic)."""
+    sizes = np.asarray(sizes, np.int64)
+    start = np.concatenate([[0], np.cumsum(sizes)])
+    nxt = np.arange(start[-1]) + 1
+    nxt[start[1:] - 1] = start[:-1]
+    p = np.asarray(points_per_corner, np.float32).reshape(-1, 3)
+    dv = np.abs(p - p[nxt])
+    length = np.sqrt(dv[:, 0] * dv[:, 0] + dv[:, 1] * dv[:, 1] + dv[:, 2] * dv[:, 2])
+    return np.minimum(1 + (length / np.float32(interval)).astype(np.int32), max_rate)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("path", MESHES[:4] + [os.path.join(GOLDEN, "large", "torus512x256_bfr.npz")],
+                         ids=os.path.basename)
+def test_edge_rates_follow_tutorial_2_1(path):
+    """GB300TessellationEdgeRates: with the control hull (mesh-vertex points) the rates equal
+    tutorial 2.1's rule computed on the host bit for bit, shared edges get one rate from both
+    faces, and the offsets are the face sizes' scan; with limit points (one per face corner:
+    the limit surface evaluated at the rate-1 tessellation's vertex coords, the tutorial's
+    other option) they equal the rule on the same points."""
+    if not os.path.exists(path):
+        pytest.skip("large fixture is written where the reference is available")
+    torch_cuda()
+    from opensubdiv_gb300 import bfr, workloads
+    from opensubdiv_gb300.evaluator import BufferDescriptor as BD, GB300PatchTable
+    z = np.load(path)
+    sizes, fv, pos = z["verts_per_face"], z["face_verts"], z["positions"]
+    ext = float((pos.max(0) - pos.min(0)).max())
+    interval, max_rate = ext / 40.0, 10
+    off, rates = bfr.EdgeRates(sizes, fv, pos, interval, max_rate)
+    want_off, want = workloads.bfr_edge_length_rates(pos, sizes, fv, interval, max_rate)
+    assert np.array_equal(host(off), want_off)
+    assert np.array_equal(host(rates), want)
+    assert np.array_equal(want, tutorial_rates(pos[fv], sizes, interval, max_rate))
+    fe, ne = workloads.face_edges(sizes, fv)
+    per_edge = np.full(ne, -1)
+    per_edge[fe] = want
+    assert np.array_equal(per_edge[fe], want)
+    # limit option: points at the faces' corners on the limit surface
+    reg = int(z["regular_face_size"]) if "regular_face_size" in z.files else 4
+    tri = bool(z["triangular"])
+    table = GB300PatchTable.Create(z["arrays"], z["patch_indices"], z["params"], tri)
+    m = bfr.MeshTessellation(reg, sizes, uniform_rate=1)
+    _, _, pc = m.Generate(table=table)
+    co = host(m.coord_offsets)
+    (P,) = m.Evaluate(dev(z["src"]), BD(0, 3, 3), table, pc, 0)
+    P = host(P)
+    valid = np.diff(co) > 0
+    corners = np.concatenate([np.arange(co[f], co[f] + sizes[f]) for f in np.nonzero(valid)[0]])
+    vs = sizes[valid]
+    cp = np.ascontiguousarray(P[corners], np.float32)
+    _, lrates = bfr.EdgeRates(vs, np.zeros(int(vs.sum()), np.int32), cp, interval, max_rate,
+                              points_per_corner=True)
+    assert np.array_equal(host(lrates), tutorial_rates(cp, vs, interval, max_rate))
+
+
+@pytest.mark.gpu
+def test_edge_rates_reject_bad_topology():
+    torch_cuda()
+    from opensubdiv_gb300 import bfr
+    from opensubdiv_gb300._lib import GB300Error
+    pos = np.zeros((6, 3), np.float32)
+    with pytest.raises(GB300Error):
+        bfr.EdgeRates(np.array([4, 4], np.int32), np.array([0, 1, 4, 3, 1, 2, 5], np.int32),
+                      pos, 0.1)
+    with pytest.raises(GB300Error):
+        bfr.EdgeRates(np.array([4, 4], np.int32), np.array([0, 1, 4, 3, 1, 2, 9, 4], np.int32),
+                      pos, 0.1)
