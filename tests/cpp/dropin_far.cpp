@@ -127,4 +127,38 @@ long long tessellateWatertight(Far::TopologyRefiner &mesh, int const *deviceFace
     return n;
 }
 
+// The reference's tutorial 2.1 (tutorials/bfr/tutorial_2_1/bfr_tutorial_2_1.cpp:160-360):
+// per-edge rates from the control hull's edge lengths, then the non-uniform tessellation --
+// the rates computed on the device from the mesh's face vertices and positions.
+bool tessellateByEdgeLength(Far::TopologyRefiner &mesh, int const *deviceFaceSizes,
+                            float const *devicePositions, float tessInterval, int tessRateMax,
+                            float *coords, int *facets, PatchCoordBuffer *coordsOut) {
+    Far::TopologyLevel const &base = mesh.GetLevel(0);
+    std::vector<int> faceVerts, faceEdges;
+    Bfr::GB300GetFaceVerticesAndEdges(mesh, faceVerts, faceEdges);
+    int *dv = nullptr, *rateOffsets = nullptr, *rates = nullptr;
+    cudaMalloc(&dv, sizeof(int) * faceVerts.size());
+    cudaMalloc(&rateOffsets, sizeof(int) * (base.GetNumFaces() + 1));
+    cudaMalloc(&rates, sizeof(int) * faceVerts.size());
+    cudaMemcpy(dv, faceVerts.data(), sizeof(int) * faceVerts.size(), cudaMemcpyHostToDevice);
+    bool ok = Bfr::GB300MeshTessellation::ComputeEdgeRates(
+        base.GetNumFaces(), deviceFaceSizes, dv, (int64_t)faceVerts.size(), devicePositions,
+        base.GetNumVertices(), 3, false, tessInterval, tessRateMax, rateOffsets, rates);
+    Far::PatchTable const *farTable = Bfr::GB300CreateSurfacePatchTable(mesh);
+    Osd::GB300PatchTable *table = Osd::GB300PatchTable::Create(farTable);
+    Bfr::GB300MeshTessellation *tess =
+        ok ? Bfr::GB300MeshTessellation::Create(
+                 Sdc::SchemeTypeTraits::GetRegularFaceSize(mesh.GetSchemeType()),
+                 base.GetNumFaces(), deviceFaceSizes, rateOffsets, rates)
+           : nullptr;
+    ok = table && tess && tess->Generate(coords, facets, true, table, coordsOut->d);
+    delete tess;
+    delete table;
+    delete farTable;
+    cudaFree(dv);
+    cudaFree(rateOffsets);
+    cudaFree(rates);
+    return ok;
+}
+
 int main() { return 0; }
