@@ -485,3 +485,15 @@ def bfr_varying(refiner, rate_offsets, rates, num_coords, values, facet_size=3,
     if n != num_coords:
         raise ValueError(f"varying loop visited {n} coords, expected {num_coords}")
     return out[:num_coords]
+
+
+def bfr_limit_rates(refiner, positions, num_corners, interval, max_rate, approx_sharp=6,
+                    approx_smooth=2):
+    """Tutorial 2.1's limit-option rates (one per face corner, 0 for faces without a surface)
+    and the limit positions at the corners it measured ([corners, 3])."""
+    rates = np.zeros(max(num_corners, 1), np.int32)
+    pts = np.zeros((max(num_corners, 1), 3), np.float32)
+    lib().ref_bfr_limit_rates(refiner.h, C.c_int(approx_sharp), C.c_int(approx_smooth),
+                              _p(np.ascontiguousarray(positions, np.float32)),
+                              C.c_float(interval), C.c_int(max_rate), _p(rates), _p(pts))
+    return rates[:num_corners], pts[:num_corners]

@@ -1054,6 +1054,50 @@ long ref_bfr_stencils(void *refiner, int approxSharp, int approxSmooth, const in
     return ne;
 }
 
+// The per-edge rates of the reference's tutorial 2.1 with its limit option
+// (tutorials/bfr/tutorial_2_1/bfr_tutorial_2_1.cpp:240-299): for each face with a limit
+// surface, its limit positions at the face's corners (Parameterization::GetVertexCoord +
+// Surface::Evaluate) and rate 1 + (int)(length / interval) capped at maxRate for the edge to
+// the next corner.  One rate per face corner, faces in order; faces without a surface get 0.
+void ref_bfr_limit_rates(void *refiner, int approxSharp, int approxSmooth, const float *pos,
+                         float interval, int maxRate, int *rates, float *cornerPoints) {
+    Far::TopologyRefiner const &mesh = *((Refiner *)refiner)->r;
+    Bfr::SurfaceFactory::Options so;
+    so.SetApproxLevelSharp(approxSharp);
+    so.SetApproxLevelSmooth(approxSmooth);
+    Bfr::RefinerSurfaceFactory<> factory(mesh, so);
+    Bfr::Surface<float> sf;
+    std::vector<float> patch, corner;
+    long c = 0;
+    for (int f = 0; f < factory.GetNumFaces(); ++f) {
+        const int N = mesh.GetLevel(0).GetFaceVertices(f).size();
+        if (!factory.InitVertexSurface(f, &sf)) {
+            for (int i = 0; i < N; ++i) rates[c + i] = 0;
+            c += N;
+            continue;
+        }
+        patch.resize((size_t)sf.GetNumPatchPoints() * 3);
+        sf.PreparePatchPoints(pos, 3, patch.data(), 3);
+        corner.resize(3 * (size_t)N);
+        Bfr::Parameterization param = sf.GetParameterization();
+        for (int i = 0; i < N; ++i) {
+            float uv[2];
+            param.GetVertexCoord(i, uv);
+            sf.Evaluate(uv, patch.data(), 3, &corner[3 * i]);
+        }
+        for (int i = 0; i < N; ++i) {
+            const float *a = &corner[3 * i], *b = &corner[3 * ((i + 1) % N)];
+            float d[3];
+            for (int k = 0; k < 3; ++k) d[k] = std::abs(a[k] - b[k]);
+            const float len = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            rates[c + i] = std::min(1 + (int)(len / interval), maxRate);
+            if (cornerPoints)
+                for (int k = 0; k < 3; ++k) cornerPoints[3 * (c + i) + k] = a[k];
+        }
+        c += N;
+    }
+}
+
 // Varying surfaces (Bfr::SurfaceFactory::InitVaryingSurface, bfr/surfaceFactory.h:252) at
 // every coord of the reference's tessellate loop (faces and coords in ref_bfr_mesh_record's
 // order): `values` holds `length` floats per mesh vertex; writes the evaluated value per coord.

@@ -623,6 +623,12 @@ def bfr_stencil_fixture(path):
         out[f"{key}__var_indices"] = vi
         for k in ("sizes", "offsets", "indices", "weights"):
             out[f"{key}__var_st_{k}"] = np.asarray(vst[k])
+        # tutorial 2.1's limit option: rates from the limit positions at the face corners
+        ext = float((cage.positions.max(0) - cage.positions.min(0)).max())
+        lr, lp = ref.bfr_limit_rates(ref.Refiner(cage), cage.positions, len(cage.face_verts),
+                                     ext / 40.0, 10)
+        out[f"{key}__limit_rates"] = lr
+        out[f"{key}__limit_points"] = lp
         out[f"{key}__var_bfr"] = ref.bfr_varying(
             ref.Refiner(cage), d["rate_offsets"], d["rates"], int(d["coord_offsets"][-1]), vals,
             int(d["facet_size"]), bool(d["preserve_quads"]))

@@ -326,3 +326,61 @@ def test_far_varying_patches_agree_with_bfr_varying_surfaces(key):
     assert oracle.eval_patches(src, (0, 3, 3), out, [(0, 3, 3)], coords, g[f"{key}__var_arrays"],
                                g[f"{key}__var_indices"], z["params"], threads=4)
     assert np.abs(out[0].reshape(-1, 3) - g[f"{key}__var_bfr"]).max() <= 1e-6
+
+
+@pytest.mark.parametrize("key", STENCIL_MESHES)
+def test_limit_option_rates_agree_with_tutorial_2_1(key):
+    """Tutorial 2.1's limit option (rates from the limit positions at each face's corners,
+    computed by the reference's Bfr in tests/golden/bfr_stencils.npz) against the same rule on
+    the paired Far table's limit positions at the located corner coords: the corner points
+    within the Bfr-vs-Far position tolerance, and the rates equal wherever the length quotient
+    is not within that tolerance of an integer (where either side may round across it)."""
+    from opensubdiv_gb300.bfr import Parameterization
+    z = np.load(os.path.join(GOLDEN, key + ".npz"))
+    g = np.load(STENCILS)
+    reg = int(z["regular_face_size"])
+    sizes = z["verts_per_face"]
+    want, want_pts = g[f"{key}__limit_rates"], g[f"{key}__limit_points"]
+    pos = z["positions"]
+    ext = float((pos.max(0) - pos.min(0)).max())
+    interval, max_rate = ext / 40.0, 10
+    ptex = z["ptex_offsets"]
+    faces, sts, corners = [], [], []
+    start = np.concatenate([[0], np.cumsum(sizes)])
+    for f in range(len(sizes)):
+        if want[start[f]] == 0:
+            continue
+        N = int(sizes[f])
+        uv = np.array([Parameterization(reg, N).GetVertexCoord(i) for i in range(N)], np.float32)
+        sub, st = oracle.param_to_subface(reg, N, uv)
+        faces.append(ptex[f] + sub)
+        sts.append(st)
+        corners.append(np.arange(start[f], start[f] + N))
+    faces, sts, corners = np.concatenate(faces), np.concatenate(sts), np.concatenate(corners)
+    pm = oracle.PatchMap(z["arrays"], z["params"], bool(z["triangular"]))
+    h = pm.find(faces, sts[:, 0].astype(np.float64), sts[:, 1].astype(np.float64))
+    coords = oracle.make_coords(h, sts[:, 0], sts[:, 1])
+    P = [np.zeros(len(coords) * 3, np.float32)]
+    assert oracle.eval_patches(z["src"], (0, 3, 3), P, [(0, 3, 3)], coords, z["arrays"],
+                               z["patch_indices"], z["params"], threads=4)
+    P = P[0].reshape(-1, 3)
+    ptol = 5e-5 * ext
+    assert np.abs(P - want_pts[corners]).max() <= ptol
+    # the rule on the Far points, per face (corner i to corner i + 1 of the same face)
+    got = np.zeros_like(want)
+    quotient = np.zeros(len(want))
+    k = 0
+    for f in range(len(sizes)):
+        if want[start[f]] == 0:
+            continue
+        N = int(sizes[f])
+        pts = P[k:k + N]
+        k += N
+        d = np.abs(pts - np.roll(pts, -1, axis=0))
+        length = np.sqrt(d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1] + d[:, 2] * d[:, 2])
+        q = length / np.float32(interval)
+        got[start[f]:start[f] + N] = np.minimum(1 + q.astype(np.int32), max_rate)
+        quotient[start[f]:start[f] + N] = q
+    near = np.abs(quotient - np.round(quotient)) <= 2 * ptol / interval
+    assert np.array_equal(got[~near], want[~near])
+    assert np.all(np.abs(got[near] - want[near]) <= 1)
