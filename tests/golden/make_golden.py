@@ -614,7 +614,7 @@ def bfr_stencil_fixture(path):
             out[f"{key}__bfr_{k}"] = bfr[k]
         # varying surfaces (InitVaryingSurface): seeded values per vertex, Far's varying
         # patches and varying stencils of the same refinement, and Bfr's values at every coord
-        rng = np.random.default_rng(400 + len(out))
+        rng = np.random.default_rng(409 + 17 * BFR_STENCIL_MESHES.index(key))
         vals = rng.uniform(-1, 1, (cage.num_vertices, 3)).astype(np.float32)
         va, vi = p.varying()
         vst = ref.stencil_table_mode(r, mode=ref.INTERPOLATE_VARYING)
