@@ -4,12 +4,17 @@ Run in a container that has the reference sources (it builds oracle/_ref/libosdr
 reference's own Far + Osd CPU code compiled from source, and drives it through
 oracle/ref_shim.cpp):
 
-    make -C oracle ref && python tests/golden/make_golden.py [factory]
+    make -C oracle ref && python tests/golden/make_golden.py [mode]
+
+Modes: none (the stencil and patch fixtures), `regression`, `factory`, `bfr` (the Bfr pattern
+sweep, the mesh fixtures, shared points and limit stencils), `bfr-share`, `bfr-stencils`, and
+`large`, `bfr-large`, `bfr-stencils-large` (full-size workloads under large/, kept out of git).
 
 Every array written here comes out of the reference: Far factories build the tables,
-Osd::CpuEvaluator produces the float outputs, Far::PatchMap the handles and
-Far::PatchTable::EvaluateBasis<double> the FP64 outputs.  The cages are the seeded
-synthetic shapes of opensubdiv_gb300/shapes.py at reduced sizes.
+Osd::CpuEvaluator produces the float outputs, Far::PatchMap the handles,
+Far::PatchTable::EvaluateBasis<double> the FP64 outputs, and Bfr (SurfaceFactory, Surface,
+Tessellation) the Bfr outputs, through the reference tutorials' loops.  The cages are the
+seeded synthetic shapes of opensubdiv_gb300/shapes.py at reduced sizes.
 """
 from __future__ import annotations
 
